@@ -1,0 +1,128 @@
+/*
+ * Oracle C API — TEST INFRASTRUCTURE ONLY.
+ *
+ * Two libraries export this same set of functions:
+ *   - liboracle_port.so : a CPU restatement (C++/OpenMP) of the Jet pressure
+ *     projection written in this repository (oracle/port/jet_port.cpp);
+ *   - _ref/libjet_ref_harness.so : a thin harness that drives the real Jet
+ *     reference classes compiled from their own sources (oracle/ref_harness.cpp).
+ * Tests use them to check the CUDA product against the reference algorithm;
+ * the product never links or calls either.
+ *
+ * Conventions follow Jet: arrays are i-fastest (index = i + nx*(j + ny*k),
+ * include/jet/detail/array_accessor3-inl.h:197-200); face-centred velocity
+ * has u:(nx+1,ny,nz), v:(nx,ny+1,nz), w:(nx,ny,nz+1)
+ * (src/jet/face_centered_grid3.cpp:428-445).
+ */
+#ifndef ORACLE_ORACLE_API_H_
+#define ORACLE_ORACLE_API_H_
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* A scalar field argument of GridPressureSolver3::solve
+ * (include/jet/grid_pressure_solver3.h:58-64): either a constant
+ * (ConstantScalarField3) or a CellCenteredScalarGrid3 whose data point (0,0,0)
+ * sits at `origin` (the grid's dataOrigin()). */
+typedef struct orc_field {
+    int kind;            /* 0 = constant, 1 = grid */
+    double value;        /* constant value when kind == 0 */
+    const double* data;  /* res[0]*res[1]*res[2] doubles when kind == 1 */
+    int res[3];
+    double origin[3];
+    double spacing[3];
+} orc_field;
+
+/* FdmMgpcgSolver3 constructor arguments (include/jet/fdm_mgpcg_solver3.h:35-41). */
+typedef struct orc_mg_params {
+    unsigned int max_cg_iter;
+    unsigned int max_levels;
+    unsigned int restrict_iter;
+    unsigned int correct_iter;
+    unsigned int coarsest_iter;
+    unsigned int final_iter;
+    double tolerance;
+    double sor;
+    int red_black;
+} orc_mg_params;
+
+/* Face-centred grid geometry: resolution, spacing, origin. */
+typedef struct orc_grid {
+    int res[3];
+    double spacing[3];
+    double origin[3];
+} orc_grid;
+
+/* GridFractionalSinglePhasePressureSolver3::solve with an FdmMgpcgSolver3
+ * installed. solid_{u,v,w} are the collider velocity's normal component at
+ * each face position (NULL = static collider). out_p receives the level-0
+ * pressure (may be NULL). Returns the MGPCG solver's bool result. */
+int orc_pressure_solve(const orc_grid* g, const double* u, const double* v,
+                       const double* w, const orc_field* boundary_sdf,
+                       const orc_field* fluid_sdf, const double* solid_u,
+                       const double* solid_v, const double* solid_w,
+                       const orc_mg_params* p, double* out_u, double* out_v,
+                       double* out_w, double* out_p, unsigned int* iters,
+                       double* resid);
+
+/* Number of multigrid levels built by the last orc_pressure_solve. */
+int orc_level_count(void);
+
+/* Copies a level of the last solve's internal state into dst.
+ * what: 0 fluid SDF (float), 1/2/3 u/v/w weights (float),
+ *       4 matrix rows (4 doubles per cell: center,right,up,front), 5 rhs b.
+ * Returns the number of elements copied (cells or faces), or -1. */
+long orc_get_level(int level, int what, void* dst);
+
+/* FdmMgpcgSolver3::solve on a caller-built multigrid system. Levels are
+ * concatenated finest first; level l has resolution res0 >> l.
+ * A: 4 doubles per cell; b: 1 double per cell; x0: finest solution out. */
+int orc_mgpcg_system(const int res0[3], int levels, const double* A,
+                     const double* b, const orc_mg_params* p, double* x0,
+                     unsigned int* iters, double* resid);
+
+/* FdmGaussSeidelSolver3::relaxRedBlack (red_black=1) or ::relax (0),
+ * `sweeps` times, in place on x. */
+void orc_relax(const int res[3], const double* A, const double* b,
+               double sor, int red_black, int sweeps, double* x);
+
+/* FdmMgUtils3::restrict and ::correct; fine resolution = 2 * coarse. */
+void orc_mg_restrict(const int coarse_res[3], const double* finer,
+                     double* coarser);
+void orc_mg_correct(const int coarse_res[3], const double* coarser,
+                    double* finer);
+
+/* FdmBlas3::residual and ::dot. */
+void orc_residual(const int res[3], const double* A, const double* x,
+                  const double* b, double* r);
+double orc_dot(long n, const double* a, const double* b);
+
+/* PicSolver3::transferFromParticlesToGrids (pic_solver3.cpp:118-193) followed
+ * by the FlipSolver3 float snapshot (flip_solver3.cpp:27-48).
+ * pos/vel: AoS xyz doubles. markers: char per face (may be NULL).
+ * snap: float per face (may be NULL). */
+void orc_p2g(const orc_grid* g, long np, const double* pos, const double* vel,
+             double* u, double* v, double* w, char* mu, char* mv, char* mw,
+             float* snap_u, float* snap_v, float* snap_w);
+
+/* FlipSolver3::transferFromGridsToParticles (flip_solver3.cpp:50-99).
+ * snap_* hold the P2G snapshot on entry and the float delta on exit.
+ * vel is updated in place. */
+void orc_g2p_flip(const orc_grid* g, long np, const double* pos, double* vel,
+                  const double* u, const double* v, const double* w,
+                  float* snap_u, float* snap_v, float* snap_w,
+                  double pic_blend);
+
+/* PicSolver3::transferFromGridsToParticles (pic_solver3.cpp:195-204). */
+void orc_g2p_pic(const orc_grid* g, long np, const double* pos, double* vel,
+                 const double* u, const double* v, const double* w);
+
+/* Sets the number of host threads the library may use (0 = all). */
+void orc_set_threads(int n);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* ORACLE_ORACLE_API_H_ */
