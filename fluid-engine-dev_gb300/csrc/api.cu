@@ -1,0 +1,764 @@
+// C ABI of libjetgpu (include/jetgpu.h): context lifetime, buffer
+// management, input validation and the pressure-projection pipeline.
+
+#include "ctx.h"
+
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <new>
+
+struct jetgpu_ctx : public jg::Ctx {};
+
+namespace jg {
+
+jetgpu_status fail(Ctx* c, jetgpu_status s, const std::string& msg) {
+    if (c) c->err = msg;
+    return s;
+}
+
+namespace {
+
+template <typename T>
+cudaError_t alloc(T** p, size_t count) {
+    *p = nullptr;
+    if (count == 0) return cudaSuccess;
+    return cudaMalloc((void**)p, count * sizeof(T));
+}
+
+template <typename T>
+void release(T** p) {
+    if (*p) cudaFree((void*)*p);
+    *p = nullptr;
+}
+
+void free_buffers(Ctx* c) {
+    for (Level& L : c->levels) {
+        release(&L.phi);
+        release(&L.uw);
+        release(&L.vw);
+        release(&L.ww);
+        release(&L.A);
+        release(&L.x);
+        release(&L.x2);
+        release(&L.b);
+        release(&L.r);
+        release(&L.xh);
+        release(&L.bh);
+        release(&L.Ah);
+    }
+    c->levels.clear();
+    release(&c->A64);
+    release(&c->b64);
+    release(&c->x64);
+    release(&c->r64);
+    release(&c->kx);
+    release(&c->kr);
+    release(&c->kd);
+    release(&c->kq);
+    release(&c->kz);
+    release(&c->dx);
+    release(&c->dr);
+    release(&c->dd);
+    release(&c->dq);
+    release(&c->dz);
+    c->n0 = Dims{0, 0, 0};
+    c->built_levels = 0;
+}
+
+double ms_since(std::chrono::steady_clock::time_point t0) {
+    return std::chrono::duration<double, std::milli>(
+               std::chrono::steady_clock::now() - t0)
+        .count();
+}
+
+jetgpu_status check_config(Ctx* c, const jetgpu_config* cfg) {
+    if (!cfg) return fail(c, JETGPU_BAD_INPUT, "null config");
+    if (cfg->max_levels < 1) return fail(c, JETGPU_BAD_INPUT, "max_levels < 1");
+    if (!(cfg->tolerance >= 0.0))
+        return fail(c, JETGPU_BAD_INPUT, "tolerance must be >= 0");
+    if (!(cfg->sor > 0.0 && cfg->sor < 2.0))
+        return fail(c, JETGPU_BAD_INPUT, "sor must be in (0, 2)");
+    if (!cfg->red_black)
+        return fail(c, JETGPU_BAD_INPUT,
+                    "only red-black smoothing is provided on the GPU");
+    if (cfg->precision < 0 || cfg->precision > 2)
+        return fail(c, JETGPU_BAD_INPUT, "unknown precision");
+    if (cfg->preconditioner < 0 || cfg->preconditioner > 1)
+        return fail(c, JETGPU_BAD_INPUT, "unknown preconditioner");
+    return JETGPU_OK;
+}
+
+jetgpu_status check_grid(Ctx* c, const jetgpu_grid* g) {
+    if (!g) return fail(c, JETGPU_BAD_INPUT, "null grid");
+    for (int a = 0; a < 3; ++a) {
+        if (g->res[a] < 1) return fail(c, JETGPU_BAD_INPUT, "resolution < 1");
+        if (!(g->spacing[a] > 0.0) || !std::isfinite(g->spacing[a]))
+            return fail(c, JETGPU_BAD_INPUT, "grid spacing must be > 0");
+        if (!std::isfinite(g->origin[a]))
+            return fail(c, JETGPU_BAD_INPUT, "non-finite origin");
+    }
+    const double cells = (double)g->res[0] * g->res[1] * g->res[2];
+    if (cells > 2147483647.0)
+        return fail(c, JETGPU_BAD_INPUT, "grid too large");
+    return JETGPU_OK;
+}
+
+jetgpu_status check_field(Ctx* c, const jetgpu_scalar_field* f,
+                          const char* name) {
+    if (!f) return fail(c, JETGPU_BAD_INPUT, std::string("null ") + name);
+    if (f->kind == 0) return JETGPU_OK;
+    if (f->kind != 1)
+        return fail(c, JETGPU_BAD_INPUT, std::string(name) + ": unknown kind");
+    if (!f->data) return fail(c, JETGPU_BAD_INPUT, std::string(name) + ": null data");
+    for (int a = 0; a < 3; ++a) {
+        if (f->res[a] < 1)
+            return fail(c, JETGPU_BAD_INPUT, std::string(name) + ": resolution < 1");
+        if (!(f->spacing[a] > 0.0))
+            return fail(c, JETGPU_BAD_INPUT, std::string(name) + ": spacing <= 0");
+    }
+    return JETGPU_OK;
+}
+
+FieldDesc to_desc(const jetgpu_scalar_field* f, const double* data) {
+    FieldDesc d;
+    d.kind = f->kind;
+    d.value = f->value;
+    d.data = data;
+    for (int a = 0; a < 3; ++a) {
+        d.res[a] = f->res[a];
+        d.origin[a] = f->origin[a];
+        d.spacing[a] = f->spacing[a];
+    }
+    return d;
+}
+
+GridDesc to_desc(const jetgpu_grid* g) {
+    GridDesc d;
+    for (int a = 0; a < 3; ++a) {
+        d.res[a] = g->res[a];
+        d.spacing[a] = g->spacing[a];
+        d.origin[a] = g->origin[a];
+    }
+    return d;
+}
+
+long field_count(const jetgpu_scalar_field* f) {
+    return f->kind == 1 ? (long)f->res[0] * f->res[1] * f->res[2] : 0;
+}
+
+__global__ void k_rows_to_f32(const double* __restrict__ A, float4* __restrict__ out,
+                              long N) {
+    for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < N;
+         c += (long)gridDim.x * blockDim.x)
+        out[c] = make_float4((float)A[4 * c], (float)A[4 * c + 1],
+                             (float)A[4 * c + 2], (float)A[4 * c + 3]);
+}
+
+__global__ void k_rows_f32_to_f64(const float4* __restrict__ A,
+                                  double* __restrict__ out, long N) {
+    for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < N;
+         c += (long)gridDim.x * blockDim.x) {
+        const float4 r = A[c];
+        out[4 * c] = r.x;
+        out[4 * c + 1] = r.y;
+        out[4 * c + 2] = r.z;
+        out[4 * c + 3] = r.w;
+    }
+}
+
+jetgpu_status grow_stage(Ctx* c, size_t bytes) {
+    if (bytes <= c->stage_bytes) return JETGPU_OK;
+    release(&c->stage);
+    c->stage_bytes = 0;
+    JG_CUDA(c, cudaMalloc((void**)&c->stage, bytes));
+    c->stage_bytes = bytes;
+    return JETGPU_OK;
+}
+
+}  // namespace
+
+jetgpu_status ensure_buffers(Ctx* c, Dims n, unsigned max_levels) {
+    const unsigned nl = level_count(n, max_levels);
+    if (c->n0.x == n.x && c->n0.y == n.y && c->n0.z == n.z &&
+        c->built_levels == nl)
+        return JETGPU_OK;
+    JG_CUDA(c, cudaStreamSynchronize(c->stream));
+    free_buffers(c);
+    c->levels.resize(nl);
+    Dims s = n;
+    for (unsigned l = 0; l < nl; ++l) {
+        Level& L = c->levels[l];
+        L.n = s;
+        const long N = s.count();
+        JG_CUDA(c, alloc(&L.phi, N));
+        JG_CUDA(c, alloc(&L.uw, (size_t)(s.x + 1) * s.y * s.z));
+        JG_CUDA(c, alloc(&L.vw, (size_t)s.x * (s.y + 1) * s.z));
+        JG_CUDA(c, alloc(&L.ww, (size_t)s.x * s.y * (s.z + 1)));
+        JG_CUDA(c, alloc(&L.A, N));
+        JG_CUDA(c, alloc(&L.x, N));
+        JG_CUDA(c, alloc(&L.x2, N));
+        JG_CUDA(c, alloc(&L.b, N));
+        JG_CUDA(c, alloc(&L.r, N));
+        s = Dims{s.x / 2, s.y / 2, s.z / 2};
+    }
+    const long N = n.count();
+    JG_CUDA(c, alloc(&c->A64, 4 * (size_t)N));
+    JG_CUDA(c, alloc(&c->b64, N));
+    JG_CUDA(c, alloc(&c->x64, N));
+    JG_CUDA(c, alloc(&c->r64, N));
+    JG_CUDA(c, alloc(&c->kx, N));
+    JG_CUDA(c, alloc(&c->kr, N));
+    JG_CUDA(c, alloc(&c->kd, N));
+    JG_CUDA(c, alloc(&c->kq, N));
+    JG_CUDA(c, alloc(&c->kz, N));
+    JG_CUDA(c, alloc(&c->dd, N));
+    JG_CUDA(c, alloc(&c->dq, N));
+    c->n0 = n;
+    c->built_levels = nl;
+    return JETGPU_OK;
+}
+
+// The device-resident pipeline shared by the host and device entry points.
+static jetgpu_status solve_pressure_dev(
+    Ctx* c, const jetgpu_grid* grid, const double* u, const double* v,
+    const double* w, const jetgpu_scalar_field* bsdf, const double* bdata,
+    const jetgpu_scalar_field* fsdf, const double* fdata, const double* su,
+    const double* sv, const double* sw, double* ou, double* ov, double* ow,
+    double* op, jetgpu_solve_stats* st) {
+    auto t0 = std::chrono::steady_clock::now();
+    const Dims n{grid->res[0], grid->res[1], grid->res[2]};
+    jetgpu_status s = ensure_buffers(c, n, c->cfg.max_levels);
+    if (s != JETGPU_OK) return s;
+    const GridDesc g = to_desc(grid);
+    s = build_weights(c, g, to_desc(bsdf, bdata), to_desc(fsdf, fdata));
+    if (s != JETGPU_OK) return s;
+    s = build_system(c, g, u, v, w, su, sv, sw);
+    if (s != JETGPU_OK) return s;
+    s = prepare_levels(c);
+    if (s != JETGPU_OK) return s;
+    JG_CUDA(c, cudaStreamSynchronize(c->stream));
+    const double setup = ms_since(t0);
+    auto t1 = std::chrono::steady_clock::now();
+    jetgpu_status solve_status = mgpcg_solve(c, st);
+    if (solve_status != JETGPU_OK && solve_status != JETGPU_NOT_CONVERGED)
+        return solve_status;
+    const double solve = ms_since(t1);
+    // The reference applies the gradient whatever the solver returned
+    // (grid_fractional_single_phase_pressure_solver3.cpp:466-483).
+    s = apply_gradient(c, g, u, v, w, ou, ov, ow);
+    if (s != JETGPU_OK) return s;
+    if (op)
+        JG_CUDA(c, cudaMemcpyAsync(op, c->x64, n.count() * sizeof(double),
+                                   cudaMemcpyDeviceToDevice, c->stream));
+    JG_CUDA(c, cudaStreamSynchronize(c->stream));
+    st->levels = c->built_levels;
+    st->setup_ms = setup;
+    st->solve_ms = solve;
+    st->total_ms = ms_since(t0);
+    return solve_status;
+}
+
+}  // namespace jg
+
+using namespace jg;
+
+extern "C" {
+
+const char* jetgpu_version(void) { return "jetgpu 0.1 (sm_103a)"; }
+
+void jetgpu_config_default(jetgpu_config* cfg) {
+    if (!cfg) return;
+    std::memset(cfg, 0, sizeof(*cfg));
+    cfg->device = 0;
+    cfg->max_cg_iter = 100;
+    cfg->max_levels = 5;
+    cfg->restrict_iter = 2;
+    cfg->correct_iter = 2;
+    cfg->coarsest_iter = 10;
+    cfg->final_iter = 2;
+    cfg->tolerance = 1e-6;
+    cfg->sor = 1.0;
+    cfg->red_black = 1;
+    cfg->precision = JETGPU_PRECISION_FP32;
+    cfg->preconditioner = JETGPU_PRECOND_MULTIGRID;
+    cfg->max_refinements = 6;
+}
+
+jetgpu_status jetgpu_create(const jetgpu_config* cfg, jetgpu_ctx** out) {
+    if (!out) return JETGPU_BAD_INPUT;
+    *out = nullptr;
+    jetgpu_ctx* c = new (std::nothrow) jetgpu_ctx();
+    if (!c) return JETGPU_OUT_OF_MEMORY;
+    jetgpu_config def;
+    jetgpu_config_default(&def);
+    const jetgpu_config* use = cfg ? cfg : &def;
+    jetgpu_status s = check_config(c, use);
+    if (s != JETGPU_OK) {
+        delete c;
+        return s;
+    }
+    c->cfg = *use;
+    c->device = use->device;
+    auto init = [&]() -> jetgpu_status {
+        JG_CUDA(c, cudaSetDevice(c->device));
+        JG_CUDA(c, cudaDeviceGetAttribute(&c->num_sms,
+                                          cudaDevAttrMultiProcessorCount,
+                                          c->device));
+        JG_CUDA(c, cudaStreamCreateWithFlags(&c->stream,
+                                             cudaStreamNonBlocking));
+        JG_CUDA(c, cudaMalloc((void**)&c->scal, S_COUNT * sizeof(double)));
+        JG_CUDA(c, cudaMemset(c->scal, 0, S_COUNT * sizeof(double)));
+        JG_CUDA(c, cudaMalloc((void**)&c->partials,
+                              (size_t)kRedSlots * kMaxRedBlocks * sizeof(double)));
+        JG_CUDA(c, cudaMalloc((void**)&c->counters, kRedSlots * sizeof(unsigned)));
+        JG_CUDA(c, cudaMemset(c->counters, 0, kRedSlots * sizeof(unsigned)));
+        JG_CUDA(c, cudaMallocHost((void**)&c->h_scal, S_COUNT * sizeof(double)));
+        for (auto& e : c->ev) JG_CUDA(c, cudaEventCreate(&e));
+        return JETGPU_OK;
+    };
+    s = init();
+    if (s != JETGPU_OK) {
+        jetgpu_destroy(c);
+        return s;
+    }
+    *out = c;
+    return JETGPU_OK;
+}
+
+void jetgpu_destroy(jetgpu_ctx* c) {
+    if (!c) return;
+    cudaSetDevice(c->device);
+    if (c->stream) cudaStreamSynchronize(c->stream);
+    free_buffers(c);
+    release(&c->scal);
+    release(&c->partials);
+    release(&c->counters);
+    release(&c->stage);
+    release(&c->pscratch);
+    if (c->h_scal) cudaFreeHost(c->h_scal);
+    if (c->host_stage) cudaFreeHost(c->host_stage);
+    for (auto& e : c->ev)
+        if (e) cudaEventDestroy(e);
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+const char* jetgpu_last_error(const jetgpu_ctx* c) {
+    return c ? c->err.c_str() : "null context";
+}
+
+jetgpu_status jetgpu_set_config(jetgpu_ctx* c, const jetgpu_config* cfg) {
+    if (!c) return JETGPU_BAD_INPUT;
+    jetgpu_status s = check_config(c, cfg);
+    if (s != JETGPU_OK) return s;
+    if (cfg->device != c->device)
+        return fail(c, JETGPU_BAD_INPUT, "device cannot change on a context");
+    c->cfg = *cfg;
+    return JETGPU_OK;
+}
+
+jetgpu_status jetgpu_solve_pressure_device(
+    jetgpu_ctx* c, const jetgpu_grid* grid, const double* u, const double* v,
+    const double* w, const jetgpu_scalar_field* boundary_sdf,
+    const jetgpu_scalar_field* fluid_sdf, const double* solid_u,
+    const double* solid_v, const double* solid_w, double* out_u,
+    double* out_v, double* out_w, double* out_pressure,
+    jetgpu_solve_stats* stats) {
+    if (!c) return JETGPU_BAD_INPUT;
+    jetgpu_status s = check_grid(c, grid);
+    if (s != JETGPU_OK) return s;
+    if (!u || !v || !w || !out_u || !out_v || !out_w)
+        return fail(c, JETGPU_BAD_INPUT, "null velocity pointer");
+    if ((s = check_field(c, boundary_sdf, "boundary_sdf")) != JETGPU_OK) return s;
+    if ((s = check_field(c, fluid_sdf, "fluid_sdf")) != JETGPU_OK) return s;
+    JG_CUDA(c, cudaSetDevice(c->device));
+    jetgpu_solve_stats local;
+    std::memset(&local, 0, sizeof(local));
+    s = solve_pressure_dev(c, grid, u, v, w, boundary_sdf, boundary_sdf->data,
+                           fluid_sdf, fluid_sdf->data, solid_u, solid_v,
+                           solid_w, out_u, out_v, out_w, out_pressure, &local);
+    if (stats) *stats = local;
+    return s;
+}
+
+jetgpu_status jetgpu_solve_pressure(
+    jetgpu_ctx* c, const jetgpu_grid* grid, const double* u, const double* v,
+    const double* w, const jetgpu_scalar_field* boundary_sdf,
+    const jetgpu_scalar_field* fluid_sdf, const double* solid_u,
+    const double* solid_v, const double* solid_w, double* out_u,
+    double* out_v, double* out_w, double* out_pressure,
+    jetgpu_solve_stats* stats) {
+    if (!c) return JETGPU_BAD_INPUT;
+    auto t0 = std::chrono::steady_clock::now();
+    jetgpu_status s = check_grid(c, grid);
+    if (s != JETGPU_OK) return s;
+    if (!u || !v || !w || !out_u || !out_v || !out_w)
+        return fail(c, JETGPU_BAD_INPUT, "null velocity pointer");
+    if ((s = check_field(c, boundary_sdf, "boundary_sdf")) != JETGPU_OK) return s;
+    if ((s = check_field(c, fluid_sdf, "fluid_sdf")) != JETGPU_OK) return s;
+    JG_CUDA(c, cudaSetDevice(c->device));
+    const long nx = grid->res[0], ny = grid->res[1], nz = grid->res[2];
+    const size_t nu = (size_t)(nx + 1) * ny * nz, nv = (size_t)nx * (ny + 1) * nz,
+                 nw = (size_t)nx * ny * (nz + 1), nc = (size_t)nx * ny * nz;
+    const size_t nb = field_count(boundary_sdf), nf = field_count(fluid_sdf);
+    const size_t ns = (solid_u ? nu : 0) + (solid_v ? nv : 0) + (solid_w ? nw : 0);
+    // Device staging: inputs u,v,w | solid | sdf data | outputs u,v,w | p.
+    const size_t total = 2 * (nu + nv + nw) + ns + nb + nf + nc;
+    s = grow_stage(c, total * sizeof(double));
+    if (s != JETGPU_OK) return s;
+    double* base = reinterpret_cast<double*>(c->stage);
+    double* du = base;
+    double* dv = du + nu;
+    double* dw = dv + nv;
+    double* p = dw + nw;
+    double* dsu = solid_u ? p : nullptr;
+    p += solid_u ? nu : 0;
+    double* dsv = solid_v ? p : nullptr;
+    p += solid_v ? nv : 0;
+    double* dsw = solid_w ? p : nullptr;
+    p += solid_w ? nw : 0;
+    double* db = nb ? p : nullptr;
+    p += nb;
+    double* df = nf ? p : nullptr;
+    p += nf;
+    double* ou = p;
+    double* ov = ou + nu;
+    double* ow = ov + nv;
+    double* dp = ow + nw;
+    cudaStream_t st = c->stream;
+    JG_CUDA(c, cudaMemcpyAsync(du, u, nu * 8, cudaMemcpyHostToDevice, st));
+    JG_CUDA(c, cudaMemcpyAsync(dv, v, nv * 8, cudaMemcpyHostToDevice, st));
+    JG_CUDA(c, cudaMemcpyAsync(dw, w, nw * 8, cudaMemcpyHostToDevice, st));
+    if (dsu) JG_CUDA(c, cudaMemcpyAsync(dsu, solid_u, nu * 8, cudaMemcpyHostToDevice, st));
+    if (dsv) JG_CUDA(c, cudaMemcpyAsync(dsv, solid_v, nv * 8, cudaMemcpyHostToDevice, st));
+    if (dsw) JG_CUDA(c, cudaMemcpyAsync(dsw, solid_w, nw * 8, cudaMemcpyHostToDevice, st));
+    if (db) JG_CUDA(c, cudaMemcpyAsync(db, boundary_sdf->data, nb * 8, cudaMemcpyHostToDevice, st));
+    if (df) JG_CUDA(c, cudaMemcpyAsync(df, fluid_sdf->data, nf * 8, cudaMemcpyHostToDevice, st));
+    jetgpu_solve_stats local;
+    std::memset(&local, 0, sizeof(local));
+    jetgpu_status solve_status = solve_pressure_dev(
+        c, grid, du, dv, dw, boundary_sdf, db, fluid_sdf, df, dsu, dsv, dsw,
+        ou, ov, ow, out_pressure ? dp : nullptr, &local);
+    if (solve_status != JETGPU_OK && solve_status != JETGPU_NOT_CONVERGED) {
+        if (stats) *stats = local;
+        return solve_status;
+    }
+    JG_CUDA(c, cudaMemcpyAsync(out_u, ou, nu * 8, cudaMemcpyDeviceToHost, st));
+    JG_CUDA(c, cudaMemcpyAsync(out_v, ov, nv * 8, cudaMemcpyDeviceToHost, st));
+    JG_CUDA(c, cudaMemcpyAsync(out_w, ow, nw * 8, cudaMemcpyDeviceToHost, st));
+    if (out_pressure)
+        JG_CUDA(c, cudaMemcpyAsync(out_pressure, dp, nc * 8, cudaMemcpyDeviceToHost, st));
+    JG_CUDA(c, cudaStreamSynchronize(st));
+    local.total_ms = ms_since(t0);
+    if (stats) *stats = local;
+    return solve_status;
+}
+
+jetgpu_status jetgpu_mgpcg_solve_system(jetgpu_ctx* c, const int res0[3],
+                                        int levels, const double* A,
+                                        const double* b, double* x,
+                                        jetgpu_solve_stats* stats) {
+    if (!c) return JETGPU_BAD_INPUT;
+    if (!res0 || !A || !b || !x || levels < 1)
+        return fail(c, JETGPU_BAD_INPUT, "null argument or levels < 1");
+    for (int a = 0; a < 3; ++a)
+        if (res0[a] < 1 || (res0[a] >> (levels - 1)) < 1 ||
+            ((res0[a] >> (levels - 1)) << (levels - 1)) != res0[a])
+            return fail(c, JETGPU_BAD_INPUT,
+                        "level resolutions must halve exactly");
+    JG_CUDA(c, cudaSetDevice(c->device));
+    auto t0 = std::chrono::steady_clock::now();
+    const Dims n{res0[0], res0[1], res0[2]};
+    jetgpu_status s = ensure_buffers(c, n, (unsigned)levels);
+    if (s != JETGPU_OK) return s;
+    if ((int)c->built_levels != levels)
+        return fail(c, JETGPU_BAD_INPUT, "level count does not match sizes");
+    long total = 0;
+    for (int l = 0; l < levels; ++l) total += c->levels[l].n.count();
+    s = grow_stage(c, (size_t)total * 4 * sizeof(double));
+    if (s != JETGPU_OK) return s;
+    double* dA = reinterpret_cast<double*>(c->stage);
+    cudaStream_t st = c->stream;
+    JG_CUDA(c, cudaMemcpyAsync(dA, A, (size_t)total * 32, cudaMemcpyHostToDevice, st));
+    const long N0 = n.count();
+    JG_CUDA(c, cudaMemcpyAsync(c->A64, dA, (size_t)N0 * 32, cudaMemcpyDeviceToDevice, st));
+    JG_CUDA(c, cudaMemcpyAsync(c->b64, b, (size_t)N0 * 8, cudaMemcpyHostToDevice, st));
+    long off = 0;
+    for (int l = 0; l < levels; ++l) {
+        const long N = c->levels[l].n.count();
+        k_rows_to_f32<<<blocks_for(N), kThreads, 0, st>>>(dA + 4 * off,
+                                                         c->levels[l].A, N);
+        off += N;
+    }
+    JG_CUDA(c, cudaGetLastError());
+    s = prepare_levels(c);
+    if (s != JETGPU_OK) return s;
+    jetgpu_solve_stats local;
+    std::memset(&local, 0, sizeof(local));
+    JG_CUDA(c, cudaStreamSynchronize(st));
+    local.setup_ms = ms_since(t0);
+    auto t1 = std::chrono::steady_clock::now();
+    jetgpu_status solve_status = mgpcg_solve(c, &local);
+    local.solve_ms = ms_since(t1);
+    if (solve_status == JETGPU_OK || solve_status == JETGPU_NOT_CONVERGED) {
+        JG_CUDA(c, cudaMemcpyAsync(x, c->x64, (size_t)N0 * 8, cudaMemcpyDeviceToHost, st));
+        JG_CUDA(c, cudaStreamSynchronize(st));
+    }
+    local.levels = c->built_levels;
+    local.total_ms = ms_since(t0);
+    if (stats) *stats = local;
+    return solve_status;
+}
+
+jetgpu_status jetgpu_get_level(jetgpu_ctx* c, int level, int what, void* dst,
+                               size_t capacity, size_t* count) {
+    if (!c || !dst) return JETGPU_BAD_INPUT;
+    if (level < 0 || level >= (int)c->built_levels)
+        return fail(c, JETGPU_BAD_INPUT, "level out of range");
+    JG_CUDA(c, cudaSetDevice(c->device));
+    const Level& L = c->levels[level];
+    const Dims s = L.n;
+    const void* src = nullptr;
+    size_t elems = 0, esize = 0;
+    double* tmp = nullptr;
+    switch (what) {
+        case 0: src = L.phi; elems = s.count(); esize = 4; break;
+        case 1: src = L.uw; elems = (size_t)(s.x + 1) * s.y * s.z; esize = 4; break;
+        case 2: src = L.vw; elems = (size_t)s.x * (s.y + 1) * s.z; esize = 4; break;
+        case 3: src = L.ww; elems = (size_t)s.x * s.y * (s.z + 1); esize = 4; break;
+        case 4:
+            elems = s.count();
+            esize = 32;
+            if (level == 0) {
+                src = c->A64;
+            } else {
+                jetgpu_status g = grow_stage(c, elems * 32);
+                if (g != JETGPU_OK) return g;
+                tmp = reinterpret_cast<double*>(c->stage);
+                k_rows_f32_to_f64<<<blocks_for(elems), kThreads, 0, c->stream>>>(
+                    L.A, tmp, (long)elems);
+                src = tmp;
+            }
+            break;
+        case 5:
+            if (level != 0)
+                return fail(c, JETGPU_BAD_INPUT, "b is kept on level 0 only");
+            src = c->b64; elems = s.count(); esize = 8; break;
+        default:
+            return fail(c, JETGPU_BAD_INPUT, "unknown field selector");
+    }
+    if (count) *count = elems;
+    if (capacity < elems * esize)
+        return fail(c, JETGPU_BAD_INPUT, "destination too small");
+    JG_CUDA(c, cudaMemcpyAsync(dst, src, elems * esize, cudaMemcpyDeviceToHost,
+                               c->stream));
+    JG_CUDA(c, cudaStreamSynchronize(c->stream));
+    return JETGPU_OK;
+}
+
+}  // extern "C"
+
+// ---- particle transfers ----------------------------------------------------
+
+namespace {
+
+jetgpu_status check_transfer(jetgpu_ctx* c, const jetgpu_grid* grid,
+                             long np, const void* pos, const void* vel) {
+    if (!c) return JETGPU_BAD_INPUT;
+    jetgpu_status s = check_grid(c, grid);
+    if (s != JETGPU_OK) return s;
+    if (np < 0) return fail(c, JETGPU_BAD_INPUT, "negative particle count");
+    if (np > 0 && (!pos || !vel))
+        return fail(c, JETGPU_BAD_INPUT, "null particle arrays");
+    return JETGPU_OK;
+}
+
+void face_counts(const jetgpu_grid* g, size_t n[3]) {
+    const size_t nx = g->res[0], ny = g->res[1], nz = g->res[2];
+    n[0] = (nx + 1) * ny * nz;
+    n[1] = nx * (ny + 1) * nz;
+    n[2] = nx * ny * (nz + 1);
+}
+
+}  // namespace
+
+extern "C" {
+
+jetgpu_status jetgpu_p2g_device(jetgpu_ctx* c, const jetgpu_grid* grid,
+                                long np, const double* pos, const double* vel,
+                                double* u, double* v, double* w,
+                                unsigned char* mu, unsigned char* mv,
+                                unsigned char* mw, float* su, float* sv,
+                                float* sw) {
+    jetgpu_status s = check_transfer(c, grid, np, pos, vel);
+    if (s != JETGPU_OK) return s;
+    if (!u || !v || !w) return fail(c, JETGPU_BAD_INPUT, "null grid arrays");
+    JG_CUDA(c, cudaSetDevice(c->device));
+    s = p2g(c, to_desc(grid), np, pos, vel, u, v, w, mu, mv, mw, su, sv, sw);
+    if (s != JETGPU_OK) return s;
+    JG_CUDA(c, cudaStreamSynchronize(c->stream));
+    return JETGPU_OK;
+}
+
+jetgpu_status jetgpu_g2p_flip_device(jetgpu_ctx* c, const jetgpu_grid* grid,
+                                     long np, const double* pos, double* vel,
+                                     const double* u, const double* v,
+                                     const double* w, float* su, float* sv,
+                                     float* sw, double blend) {
+    jetgpu_status s = check_transfer(c, grid, np, pos, vel);
+    if (s != JETGPU_OK) return s;
+    if (!u || !v || !w || !su || !sv || !sw)
+        return fail(c, JETGPU_BAD_INPUT, "null grid arrays");
+    if (!(blend >= 0.0 && blend <= 1.0))
+        return fail(c, JETGPU_BAD_INPUT, "pic blending factor outside [0,1]");
+    JG_CUDA(c, cudaSetDevice(c->device));
+    s = g2p_flip(c, to_desc(grid), np, pos, vel, u, v, w, su, sv, sw, blend);
+    if (s != JETGPU_OK) return s;
+    JG_CUDA(c, cudaStreamSynchronize(c->stream));
+    return JETGPU_OK;
+}
+
+jetgpu_status jetgpu_g2p_pic_device(jetgpu_ctx* c, const jetgpu_grid* grid,
+                                    long np, const double* pos, double* vel,
+                                    const double* u, const double* v,
+                                    const double* w) {
+    jetgpu_status s = check_transfer(c, grid, np, pos, vel);
+    if (s != JETGPU_OK) return s;
+    if (!u || !v || !w) return fail(c, JETGPU_BAD_INPUT, "null grid arrays");
+    JG_CUDA(c, cudaSetDevice(c->device));
+    s = g2p_pic(c, to_desc(grid), np, pos, vel, u, v, w);
+    if (s != JETGPU_OK) return s;
+    JG_CUDA(c, cudaStreamSynchronize(c->stream));
+    return JETGPU_OK;
+}
+
+jetgpu_status jetgpu_p2g(jetgpu_ctx* c, const jetgpu_grid* grid, long np,
+                         const double* pos, const double* vel, double* u,
+                         double* v, double* w, unsigned char* mu,
+                         unsigned char* mv, unsigned char* mw, float* su,
+                         float* sv, float* sw) {
+    jetgpu_status s = check_transfer(c, grid, np, pos, vel);
+    if (s != JETGPU_OK) return s;
+    if (!u || !v || !w) return fail(c, JETGPU_BAD_INPUT, "null grid arrays");
+    JG_CUDA(c, cudaSetDevice(c->device));
+    size_t n[3];
+    face_counts(grid, n);
+    const size_t nf = n[0] + n[1] + n[2];
+    const size_t bytes = (size_t)np * 48 + nf * (8 + 1 + 4);
+    s = grow_stage(c, bytes + 64);
+    if (s != JETGPU_OK) return s;
+    unsigned char* p = c->stage;
+    double* dpos = reinterpret_cast<double*>(p); p += (size_t)np * 24;
+    double* dvel = reinterpret_cast<double*>(p); p += (size_t)np * 24;
+    double* dg = reinterpret_cast<double*>(p); p += nf * 8;
+    float* ds = reinterpret_cast<float*>(p); p += nf * 4;
+    unsigned char* dm = p;
+    cudaStream_t st = c->stream;
+    if (np) {
+        JG_CUDA(c, cudaMemcpyAsync(dpos, pos, np * 24, cudaMemcpyHostToDevice, st));
+        JG_CUDA(c, cudaMemcpyAsync(dvel, vel, np * 24, cudaMemcpyHostToDevice, st));
+    }
+    const bool want_m = mu || mv || mw, want_s = su || sv || sw;
+    s = p2g(c, to_desc(grid), np, dpos, dvel, dg, dg + n[0], dg + n[0] + n[1],
+            want_m ? dm : nullptr, want_m ? dm + n[0] : nullptr,
+            want_m ? dm + n[0] + n[1] : nullptr, want_s ? ds : nullptr,
+            want_s ? ds + n[0] : nullptr, want_s ? ds + n[0] + n[1] : nullptr);
+    if (s != JETGPU_OK) return s;
+    double* outs[3] = {u, v, w};
+    unsigned char* marks[3] = {mu, mv, mw};
+    float* snaps[3] = {su, sv, sw};
+    size_t off = 0;
+    for (int a = 0; a < 3; ++a) {
+        JG_CUDA(c, cudaMemcpyAsync(outs[a], dg + off, n[a] * 8, cudaMemcpyDeviceToHost, st));
+        if (marks[a]) JG_CUDA(c, cudaMemcpyAsync(marks[a], dm + off, n[a], cudaMemcpyDeviceToHost, st));
+        if (snaps[a]) JG_CUDA(c, cudaMemcpyAsync(snaps[a], ds + off, n[a] * 4, cudaMemcpyDeviceToHost, st));
+        off += n[a];
+    }
+    JG_CUDA(c, cudaStreamSynchronize(st));
+    return JETGPU_OK;
+}
+
+jetgpu_status jetgpu_g2p_flip(jetgpu_ctx* c, const jetgpu_grid* grid, long np,
+                              const double* pos, double* vel, const double* u,
+                              const double* v, const double* w, float* su,
+                              float* sv, float* sw, double blend) {
+    jetgpu_status s = check_transfer(c, grid, np, pos, vel);
+    if (s != JETGPU_OK) return s;
+    if (!u || !v || !w || !su || !sv || !sw)
+        return fail(c, JETGPU_BAD_INPUT, "null grid arrays");
+    if (!(blend >= 0.0 && blend <= 1.0))
+        return fail(c, JETGPU_BAD_INPUT, "pic blending factor outside [0,1]");
+    JG_CUDA(c, cudaSetDevice(c->device));
+    size_t n[3];
+    face_counts(grid, n);
+    const size_t nf = n[0] + n[1] + n[2];
+    s = grow_stage(c, (size_t)np * 48 + nf * 12 + 64);
+    if (s != JETGPU_OK) return s;
+    unsigned char* p = c->stage;
+    double* dpos = reinterpret_cast<double*>(p); p += (size_t)np * 24;
+    double* dvel = reinterpret_cast<double*>(p); p += (size_t)np * 24;
+    double* dg = reinterpret_cast<double*>(p); p += nf * 8;
+    float* ds = reinterpret_cast<float*>(p);
+    cudaStream_t st = c->stream;
+    const double* ins[3] = {u, v, w};
+    float* snaps[3] = {su, sv, sw};
+    if (np) {
+        JG_CUDA(c, cudaMemcpyAsync(dpos, pos, np * 24, cudaMemcpyHostToDevice, st));
+        JG_CUDA(c, cudaMemcpyAsync(dvel, vel, np * 24, cudaMemcpyHostToDevice, st));
+    }
+    size_t off = 0;
+    for (int a = 0; a < 3; ++a) {
+        JG_CUDA(c, cudaMemcpyAsync(dg + off, ins[a], n[a] * 8, cudaMemcpyHostToDevice, st));
+        JG_CUDA(c, cudaMemcpyAsync(ds + off, snaps[a], n[a] * 4, cudaMemcpyHostToDevice, st));
+        off += n[a];
+    }
+    s = g2p_flip(c, to_desc(grid), np, dpos, dvel, dg, dg + n[0],
+                 dg + n[0] + n[1], ds, ds + n[0], ds + n[0] + n[1], blend);
+    if (s != JETGPU_OK) return s;
+    if (np) JG_CUDA(c, cudaMemcpyAsync(vel, dvel, np * 24, cudaMemcpyDeviceToHost, st));
+    off = 0;
+    for (int a = 0; a < 3; ++a) {
+        JG_CUDA(c, cudaMemcpyAsync(snaps[a], ds + off, n[a] * 4, cudaMemcpyDeviceToHost, st));
+        off += n[a];
+    }
+    JG_CUDA(c, cudaStreamSynchronize(st));
+    return JETGPU_OK;
+}
+
+jetgpu_status jetgpu_g2p_pic(jetgpu_ctx* c, const jetgpu_grid* grid, long np,
+                             const double* pos, double* vel, const double* u,
+                             const double* v, const double* w) {
+    jetgpu_status s = check_transfer(c, grid, np, pos, vel);
+    if (s != JETGPU_OK) return s;
+    if (!u || !v || !w) return fail(c, JETGPU_BAD_INPUT, "null grid arrays");
+    JG_CUDA(c, cudaSetDevice(c->device));
+    size_t n[3];
+    face_counts(grid, n);
+    const size_t nf = n[0] + n[1] + n[2];
+    s = grow_stage(c, (size_t)np * 48 + nf * 8 + 64);
+    if (s != JETGPU_OK) return s;
+    unsigned char* p = c->stage;
+    double* dpos = reinterpret_cast<double*>(p); p += (size_t)np * 24;
+    double* dvel = reinterpret_cast<double*>(p); p += (size_t)np * 24;
+    double* dg = reinterpret_cast<double*>(p);
+    cudaStream_t st = c->stream;
+    const double* ins[3] = {u, v, w};
+    if (np) {
+        JG_CUDA(c, cudaMemcpyAsync(dpos, pos, np * 24, cudaMemcpyHostToDevice, st));
+        JG_CUDA(c, cudaMemcpyAsync(dvel, vel, np * 24, cudaMemcpyHostToDevice, st));
+    }
+    size_t off = 0;
+    for (int a = 0; a < 3; ++a) {
+        JG_CUDA(c, cudaMemcpyAsync(dg + off, ins[a], n[a] * 8, cudaMemcpyHostToDevice, st));
+        off += n[a];
+    }
+    s = g2p_pic(c, to_desc(grid), np, dpos, dvel, dg, dg + n[0], dg + n[0] + n[1]);
+    if (s != JETGPU_OK) return s;
+    if (np) JG_CUDA(c, cudaMemcpyAsync(vel, dvel, np * 24, cudaMemcpyDeviceToHost, st));
+    JG_CUDA(c, cudaStreamSynchronize(st));
+    return JETGPU_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,525 @@
+// Weights, system build and pressure-gradient kernels (K1-K4, K12).
+//
+// These kernels replay the reference's double-precision arithmetic exactly so
+// that cell classification, face weights, the FP64 matrix and the projected
+// velocity are bit-identical to GridFractionalSinglePhasePressureSolver3
+// (src/jet/grid_fractional_single_phase_pressure_solver3.cpp). This
+// translation unit is compiled with -fmad=false: no multiply-add contraction,
+// every product and sum rounds on its own, in the reference's order.
+//
+// All kernels are HBM-bound elementwise/stencil passes: one thread per output
+// element, consecutive threads on consecutive i (coalesced), neighbour loads
+// served by L1/L2.
+
+#include "ctx.h"
+
+#include <cfloat>
+
+namespace jg {
+namespace {
+
+// ---------------------------------------------------------------------------
+// Exact sampling: LinearArraySampler3<double,double>::operator()
+// (include/jet/detail/array_samplers3-inl.h:115-149), getBarycentric
+// (include/jet/detail/math_utils-inl.h:147-172), lerp/bilerp/trilerp (:177-211).
+
+__device__ __forceinline__ void barycentric(double x, int iHigh, int* i,
+                                            double* f) {
+    double s = floor(x);
+    // Clamp before the integer conversion; the reference converts first, but
+    // both select the same branch for every in-range and out-of-range x.
+    if (iHigh == 0) {
+        *i = 0;
+        *f = 0.0;
+    } else if (s < 0.0) {
+        *i = 0;
+        *f = 0.0;
+    } else if (s > (double)(iHigh - 1)) {
+        *i = iHigh - 1;
+        *f = 1.0;
+    } else {
+        *i = (int)s;
+        *f = x - s;
+    }
+}
+
+__device__ __forceinline__ double lerpd(double a, double b, double f) {
+    return (1.0 - f) * a + f * b;
+}
+
+__device__ double sample_field(const FieldDesc& F, double x, double y,
+                               double z) {
+    if (F.kind == 0) return F.value;
+    const double nx = (x - F.origin[0]) / F.spacing[0];
+    const double ny = (y - F.origin[1]) / F.spacing[1];
+    const double nz = (z - F.origin[2]) / F.spacing[2];
+    int i, j, k;
+    double fx, fy, fz;
+    barycentric(nx, F.res[0] - 1, &i, &fx);
+    barycentric(ny, F.res[1] - 1, &j, &fy);
+    barycentric(nz, F.res[2] - 1, &k, &fz);
+    const int ip1 = min(i + 1, F.res[0] - 1);
+    const int jp1 = min(j + 1, F.res[1] - 1);
+    const int kp1 = min(k + 1, F.res[2] - 1);
+    const int rx = F.res[0], ry = F.res[1];
+    const double* d = F.data;
+    const double f000 = d[lin(i, j, k, rx, ry)], f100 = d[lin(ip1, j, k, rx, ry)];
+    const double f010 = d[lin(i, jp1, k, rx, ry)], f110 = d[lin(ip1, jp1, k, rx, ry)];
+    const double f001 = d[lin(i, j, kp1, rx, ry)], f101 = d[lin(ip1, j, kp1, rx, ry)];
+    const double f011 = d[lin(i, jp1, kp1, rx, ry)], f111 = d[lin(ip1, jp1, kp1, rx, ry)];
+    const double b0 = lerpd(lerpd(f000, f100, fx), lerpd(f010, f110, fx), fy);
+    const double b1 = lerpd(lerpd(f001, f101, fx), lerpd(f011, f111, fx), fy);
+    return lerpd(b0, b1, fz);
+}
+
+// ---------------------------------------------------------------------------
+// Level-set helpers (include/jet/detail/level_set_utils-inl.h:23-147).
+
+__device__ __forceinline__ bool inside(double p) { return p < 0.0; }
+
+__device__ __forceinline__ double frac_sdf(double p0, double p1) {
+    if (inside(p0) && inside(p1)) return 1.0;
+    if (inside(p0) && !inside(p1)) return p0 / (p0 - p1);
+    if (!inside(p0) && inside(p1)) return p1 / (p1 - p0);
+    return 0.0;
+}
+
+__device__ __forceinline__ void cycle4(double* a) {
+    double t = a[0];
+    a[0] = a[1];
+    a[1] = a[2];
+    a[2] = a[3];
+    a[3] = t;
+}
+
+// Marching-squares area of the inside region of a face (fractionInside).
+__device__ double frac_inside(double bl, double br, double tl, double tr) {
+    const int n = (bl < 0) + (tl < 0) + (br < 0) + (tr < 0);
+    double l[4] = {bl, br, tr, tl};
+    const double half = 0.5;  // 0.5f widened, exact
+    const double quarter = 0.25;
+    if (n == 4) return 1.0;
+    if (n == 3) {
+        for (int r = 0; r < 4 && l[0] < 0; ++r) cycle4(l);
+        const double s0 = 1.0 - frac_sdf(l[0], l[3]);
+        const double s1 = 1.0 - frac_sdf(l[0], l[1]);
+        return 1.0 - half * s0 * s1;
+    }
+    if (n == 2) {
+        for (int r = 0; r < 4 && (l[0] >= 0 || !(l[1] < 0 || l[2] < 0)); ++r)
+            cycle4(l);
+        if (l[1] < 0) {
+            const double sl = frac_sdf(l[0], l[3]);
+            const double sr = frac_sdf(l[1], l[2]);
+            return half * (sl + sr);
+        }
+        const double mid = quarter * (l[0] + l[1] + l[2] + l[3]);
+        if (mid < 0) {
+            double area = 0.0;
+            const double s1 = 1.0 - frac_sdf(l[0], l[3]);
+            const double s3 = 1.0 - frac_sdf(l[2], l[3]);
+            area += half * s1 * s3;
+            const double s2 = 1.0 - frac_sdf(l[2], l[1]);
+            const double s0 = 1.0 - frac_sdf(l[0], l[1]);
+            area += half * s0 * s2;
+            return 1.0 - area;
+        }
+        double area = 0.0;
+        const double s0 = frac_sdf(l[0], l[1]);
+        const double s1 = frac_sdf(l[0], l[3]);
+        area += half * s0 * s1;
+        const double s2 = frac_sdf(l[2], l[1]);
+        const double s3 = frac_sdf(l[2], l[3]);
+        area += half * s2 * s3;
+        return area;
+    }
+    if (n == 1) {
+        for (int r = 0; r < 4 && l[0] >= 0; ++r) cycle4(l);
+        const double s0 = frac_sdf(l[0], l[3]);
+        const double s1 = frac_sdf(l[0], l[1]);
+        return half * s0 * s1;
+    }
+    return 0.0;
+}
+
+__device__ __forceinline__ float face_weight(double p0, double p1, double p2,
+                                             double p3) {
+    const double frac = frac_inside(p0, p1, p2, p3);
+    double w = 1.0 - frac;
+    w = (w < 0.0) ? 0.0 : ((w > 1.0) ? 1.0 : w);
+    if (w < 0.01 && w > 0.0) w = 0.01;  // kMinWeight (:25, :566-570)
+    return (float)w;
+}
+
+// K1: _fluidSdf[0](i,j,k) = float(fluidSdf.sample(cellCenter)) (:548-551).
+__global__ void k_sample_fluid(float* __restrict__ phi, Dims n, GridDesc g,
+                               FieldDesc F) {
+    const long N = n.count();
+    for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < N;
+         c += (long)gridDim.x * blockDim.x) {
+        const int i = (int)(c % n.x);
+        const int j = (int)((c / n.x) % n.y);
+        const int k = (int)(c / ((long)n.x * n.y));
+        // Grid3::cellCenterPosition (src/jet/grid3.cpp:32-38).
+        const double px = g.origin[0] + g.spacing[0] * ((double)i + 0.5);
+        const double py = g.origin[1] + g.spacing[1] * ((double)j + 0.5);
+        const double pz = g.origin[2] + g.spacing[2] * ((double)k + 0.5);
+        phi[c] = (float)sample_field(F, px, py, pz);
+    }
+}
+
+// K2: face weights from four boundary-SDF corner samples (:553-617).
+// axis 0/1/2 = u/v/w faces.
+__global__ void k_face_weights(float* __restrict__ wgt, int axis, Dims fn,
+                               GridDesc g, FieldDesc B) {
+    const long N = fn.count();
+    const double hx = g.spacing[0], hy = g.spacing[1], hz = g.spacing[2];
+    // Face data origins (src/jet/face_centered_grid3.cpp:440-442).
+    const double ox = g.origin[0] + 0.5 * (axis == 0 ? 0.0 : hx);
+    const double oy = g.origin[1] + 0.5 * (axis == 1 ? 0.0 : hy);
+    const double oz = g.origin[2] + 0.5 * (axis == 2 ? 0.0 : hz);
+    for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < N;
+         c += (long)gridDim.x * blockDim.x) {
+        const int i = (int)(c % fn.x);
+        const int j = (int)((c / fn.x) % fn.y);
+        const int k = (int)(c / ((long)fn.x * fn.y));
+        const double px = ox + hx * (double)i;
+        const double py = oy + hy * (double)j;
+        const double pz = oz + hz * (double)k;
+        double p0, p1, p2, p3;
+        if (axis == 0) {
+            p0 = sample_field(B, px + 0.0, py + -0.5 * hy, pz + -0.5 * hz);
+            p1 = sample_field(B, px + 0.0, py + 0.5 * hy, pz + -0.5 * hz);
+            p2 = sample_field(B, px + 0.0, py + -0.5 * hy, pz + 0.5 * hz);
+            p3 = sample_field(B, px + 0.0, py + 0.5 * hy, pz + 0.5 * hz);
+        } else if (axis == 1) {
+            p0 = sample_field(B, px + -0.5 * hx, py + 0.0, pz + -0.5 * hz);
+            p1 = sample_field(B, px + -0.5 * hx, py + 0.0, pz + 0.5 * hz);
+            p2 = sample_field(B, px + 0.5 * hx, py + 0.0, pz + -0.5 * hz);
+            p3 = sample_field(B, px + 0.5 * hx, py + 0.0, pz + 0.5 * hz);
+        } else {
+            p0 = sample_field(B, px + -0.5 * hx, py + -0.5 * hy, pz + 0.0);
+            p1 = sample_field(B, px + -0.5 * hx, py + 0.5 * hy, pz + 0.0);
+            p2 = sample_field(B, px + 0.5 * hx, py + -0.5 * hy, pz + 0.0);
+            p3 = sample_field(B, px + 0.5 * hx, py + 0.5 * hy, pz + 0.0);
+        }
+        wgt[c] = face_weight(p0, p1, p2, p3);
+    }
+}
+
+// K3: the anonymous float `restrict` (:29-115): 1-3-3-1/8 on axes where the
+// fine size is twice the coarse size, injection {0,1,0} otherwise (the
+// face-normal axis of a face array), boundary taps clamped with the coarse
+// size. Float sums in the reference's z, y, x order.
+__global__ void k_restrict_f32(const float* __restrict__ fine, Dims fs,
+                               float* __restrict__ coarse, Dims cs) {
+    const long N = cs.count();
+    const int ksx = (fs.x != 2 * cs.x) ? 3 : 4;
+    const int ksy = (fs.y != 2 * cs.y) ? 3 : 4;
+    const int ksz = (fs.z != 2 * cs.z) ? 3 : 4;
+    const float cen[4] = {0.125f, 0.375f, 0.375f, 0.125f};
+    const float stg[4] = {0.f, 1.f, 0.f, 0.f};
+    for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < N;
+         c += (long)gridDim.x * blockDim.x) {
+        const int i = (int)(c % cs.x);
+        const int j = (int)((c / cs.x) % cs.y);
+        const int k = (int)(c / ((long)cs.x * cs.y));
+        int iI[4], jI[4], kI[4];
+        auto taps = [](int ks, int q, int nq, int* o) {
+            o[0] = (q > 0) ? 2 * q - 1 : 2 * q;
+            o[1] = 2 * q;
+            if (ks == 3) {
+                o[2] = (q + 1 < nq) ? 2 * q + 1 : 2 * q;
+                o[3] = 0;
+            } else {
+                o[2] = 2 * q + 1;
+                o[3] = (q + 1 < nq) ? 2 * q + 2 : 2 * q + 1;
+            }
+        };
+        taps(ksx, i, cs.x, iI);
+        taps(ksy, j, cs.y, jI);
+        taps(ksz, k, cs.z, kI);
+        const float* kx = (ksx == 3) ? stg : cen;
+        const float* ky = (ksy == 3) ? stg : cen;
+        const float* kz = (ksz == 3) ? stg : cen;
+        float sum = 0.0f;
+        for (int z = 0; z < ksz; ++z)
+            for (int y = 0; y < ksy; ++y)
+                for (int x = 0; x < ksx; ++x) {
+                    const float w = kx[x] * ky[y] * kz[z];
+                    sum += w * fine[lin(iI[x], jI[y], kI[z], fs.x, fs.y)];
+                }
+        coarse[c] = sum;
+    }
+}
+
+// K4: buildSingleSystem (:117-267). Writes the FP32 rows of every level;
+// on the finest level also the exact FP64 rows and rhs. u/v/w are the input
+// velocity (finest level only; coarse right-hand sides are dead, overwritten
+// by restriction in the V-cycle, include/jet/detail/mg-inl.h:28-30).
+__global__ void k_build_system(Dims n, double hx, double hy, double hz,
+                               const float* __restrict__ phi,
+                               const float* __restrict__ uw,
+                               const float* __restrict__ vw,
+                               const float* __restrict__ ww,
+                               const double* __restrict__ u,
+                               const double* __restrict__ v,
+                               const double* __restrict__ w,
+                               const double* __restrict__ su,
+                               const double* __restrict__ sv,
+                               const double* __restrict__ sw,
+                               double* __restrict__ A64,
+                               double* __restrict__ b64,
+                               float4* __restrict__ A32) {
+    const long N = n.count();
+    const double ihx = 1.0 / hx, ihy = 1.0 / hy, ihz = 1.0 / hz;
+    const double ihx2 = ihx * ihx, ihy2 = ihy * ihy, ihz2 = ihz * ihz;
+    const int ux = n.x + 1;  // u-face row length
+    for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < N;
+         c += (long)gridDim.x * blockDim.x) {
+        const int i = (int)(c % n.x);
+        const int j = (int)((c / n.x) % n.y);
+        const int k = (int)(c / ((long)n.x * n.y));
+        double center = 0.0, right = 0.0, up = 0.0, front = 0.0, bb = 0.0;
+        const double cphi = phi[c];
+        if (inside(cphi)) {
+            const long uR = lin(i + 1, j, k, ux, n.y), uL = lin(i, j, k, ux, n.y);
+            const long vU = lin(i, j + 1, k, n.x, n.y + 1),
+                       vD = lin(i, j, k, n.x, n.y + 1);
+            const long wF = lin(i, j, k + 1, n.x, n.y), wB = lin(i, j, k, n.x, n.y);
+            const long sy = n.x, sz = (long)n.x * n.y;
+            double term;
+            if (i + 1 < n.x) {
+                term = (double)uw[uR] * ihx2;
+                const double np = phi[c + 1];
+                if (inside(np)) {
+                    center += term;
+                    right -= term;
+                } else {
+                    center += term / fmax(frac_sdf(cphi, np), 0.01);
+                }
+                if (u) bb += (double)uw[uR] * u[uR] * ihx;
+            } else if (u) {
+                bb += u[uR] * ihx;
+            }
+            if (i > 0) {
+                term = (double)uw[uL] * ihx2;
+                const double np = phi[c - 1];
+                if (inside(np)) center += term;
+                else center += term / fmax(frac_sdf(cphi, np), 0.01);
+                if (u) bb -= (double)uw[uL] * u[uL] * ihx;
+            } else if (u) {
+                bb -= u[uL] * ihx;
+            }
+            if (j + 1 < n.y) {
+                term = (double)vw[vU] * ihy2;
+                const double np = phi[c + sy];
+                if (inside(np)) {
+                    center += term;
+                    up -= term;
+                } else {
+                    center += term / fmax(frac_sdf(cphi, np), 0.01);
+                }
+                if (u) bb += (double)vw[vU] * v[vU] * ihy;
+            } else if (u) {
+                bb += v[vU] * ihy;
+            }
+            if (j > 0) {
+                term = (double)vw[vD] * ihy2;
+                const double np = phi[c - sy];
+                if (inside(np)) center += term;
+                else center += term / fmax(frac_sdf(cphi, np), 0.01);
+                if (u) bb -= (double)vw[vD] * v[vD] * ihy;
+            } else if (u) {
+                bb -= v[vD] * ihy;
+            }
+            if (k + 1 < n.z) {
+                term = (double)ww[wF] * ihz2;
+                const double np = phi[c + sz];
+                if (inside(np)) {
+                    center += term;
+                    front -= term;
+                } else {
+                    center += term / fmax(frac_sdf(cphi, np), 0.01);
+                }
+                if (u) bb += (double)ww[wF] * w[wF] * ihz;
+            } else if (u) {
+                bb += w[wF] * ihz;
+            }
+            if (k > 0) {
+                term = (double)ww[wB] * ihz2;
+                const double np = phi[c - sz];
+                if (inside(np)) center += term;
+                else center += term / fmax(frac_sdf(cphi, np), 0.01);
+                if (u) bb -= (double)ww[wB] * w[wB] * ihz;
+            } else if (u) {
+                bb -= w[wB] * ihz;
+            }
+            if (u) {
+                // Moving-boundary contribution (:241-255), evaluated as the
+                // reference's single left-to-right expression.
+                const double sR = su ? su[uR] : 0.0, sL = su ? su[uL] : 0.0;
+                const double sU = sv ? sv[vU] : 0.0, sD = sv ? sv[vD] : 0.0;
+                const double sF = sw ? sw[wF] : 0.0, sB = sw ? sw[wB] : 0.0;
+                const double contrib = (1.0 - (double)uw[uR]) * sR * ihx -
+                                       (1.0 - (double)uw[uL]) * sL * ihx +
+                                       (1.0 - (double)vw[vU]) * sU * ihy -
+                                       (1.0 - (double)vw[vD]) * sD * ihy +
+                                       (1.0 - (double)ww[wF]) * sF * ihz -
+                                       (1.0 - (double)ww[wB]) * sB * ihz;
+                bb += contrib;
+            }
+            if (center < DBL_EPSILON) {  // kEpsilonD (:259-262)
+                center = 1.0;
+                bb = 0.0;
+            }
+        } else {
+            center = 1.0;
+        }
+        if (A64) {
+            A64[4 * c + 0] = center;
+            A64[4 * c + 1] = right;
+            A64[4 * c + 2] = up;
+            A64[4 * c + 3] = front;
+        }
+        if (b64) b64[c] = bb;
+        A32[c] = make_float4((float)center, (float)right, (float)up,
+                             (float)front);
+    }
+}
+
+// K12: applyPressureGradient (:715-765). Each face i+1/j+1/k+1 of cell c is
+// written only by the thread of cell c, which also reads it, so the output
+// may alias the input.
+__global__ void k_apply_gradient(Dims n, double ihx, double ihy, double ihz,
+                                 const float* __restrict__ phi,
+                                 const float* __restrict__ uw,
+                                 const float* __restrict__ vw,
+                                 const float* __restrict__ ww,
+                                 const double* __restrict__ x,
+                                 const double* u, const double* v,
+                                 const double* w, double* ou, double* ov,
+                                 double* ow) {
+    const long N = n.count();
+    const int ux = n.x + 1;
+    for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < N;
+         c += (long)gridDim.x * blockDim.x) {
+        const int i = (int)(c % n.x);
+        const int j = (int)((c / n.x) % n.y);
+        const int k = (int)(c / ((long)n.x * n.y));
+        const double cphi = phi[c];
+        if (i + 1 < n.x) {
+            const long f = lin(i + 1, j, k, ux, n.y);
+            const double np = phi[c + 1];
+            if ((double)uw[f] > 0.0 && (inside(cphi) || inside(np))) {
+                const double th = fmax(frac_sdf(cphi, np), 0.01);
+                ou[f] = u[f] + ihx / th * (x[c + 1] - x[c]);
+            }
+        }
+        if (j + 1 < n.y) {
+            const long f = lin(i, j + 1, k, n.x, n.y + 1);
+            const double np = phi[c + n.x];
+            if ((double)vw[f] > 0.0 && (inside(cphi) || inside(np))) {
+                const double th = fmax(frac_sdf(cphi, np), 0.01);
+                ov[f] = v[f] + ihy / th * (x[c + n.x] - x[c]);
+            }
+        }
+        if (k + 1 < n.z) {
+            const long sz = (long)n.x * n.y;
+            const long f = lin(i, j, k + 1, n.x, n.y);
+            const double np = phi[c + sz];
+            if ((double)ww[f] > 0.0 && (inside(cphi) || inside(np))) {
+                const double th = fmax(frac_sdf(cphi, np), 0.01);
+                ow[f] = w[f] + ihz / th * (x[c + sz] - x[c]);
+            }
+        }
+    }
+}
+
+}  // namespace
+
+jetgpu_status build_weights(Ctx* c, const GridDesc& g, const FieldDesc& bsdf,
+                            const FieldDesc& fsdf) {
+    const unsigned nl = c->built_levels;
+    Level& L0 = c->levels[0];
+    const Dims n = L0.n;
+    k_sample_fluid<<<blocks_for(n.count()), kThreads, 0, c->stream>>>(
+        L0.phi, n, g, fsdf);
+    const Dims fu{n.x + 1, n.y, n.z}, fv{n.x, n.y + 1, n.z},
+        fw{n.x, n.y, n.z + 1};
+    k_face_weights<<<blocks_for(fu.count()), kThreads, 0, c->stream>>>(
+        L0.uw, 0, fu, g, bsdf);
+    k_face_weights<<<blocks_for(fv.count()), kThreads, 0, c->stream>>>(
+        L0.vw, 1, fv, g, bsdf);
+    k_face_weights<<<blocks_for(fw.count()), kThreads, 0, c->stream>>>(
+        L0.ww, 2, fw, g, bsdf);
+    for (unsigned l = 1; l < nl; ++l) {
+        const Level& F = c->levels[l - 1];
+        Level& C = c->levels[l];
+        const Dims f = F.n, s = C.n;
+        k_restrict_f32<<<blocks_for(s.count()), kThreads, 0, c->stream>>>(
+            F.phi, f, C.phi, s);
+        k_restrict_f32<<<blocks_for((long)(s.x + 1) * s.y * s.z), kThreads, 0,
+                         c->stream>>>(F.uw, Dims{f.x + 1, f.y, f.z}, C.uw,
+                                      Dims{s.x + 1, s.y, s.z});
+        k_restrict_f32<<<blocks_for((long)s.x * (s.y + 1) * s.z), kThreads, 0,
+                         c->stream>>>(F.vw, Dims{f.x, f.y + 1, f.z}, C.vw,
+                                      Dims{s.x, s.y + 1, s.z});
+        k_restrict_f32<<<blocks_for((long)s.x * s.y * (s.z + 1)), kThreads, 0,
+                         c->stream>>>(F.ww, Dims{f.x, f.y, f.z + 1}, C.ww,
+                                      Dims{s.x, s.y, s.z + 1});
+    }
+    JG_CUDA(c, cudaGetLastError());
+    return JETGPU_OK;
+}
+
+jetgpu_status build_system(Ctx* c, const GridDesc& g, const double* u,
+                           const double* v, const double* w,
+                           const double* su, const double* sv,
+                           const double* sw) {
+    double hx = g.spacing[0], hy = g.spacing[1], hz = g.spacing[2];
+    for (unsigned l = 0; l < c->built_levels; ++l) {
+        Level& L = c->levels[l];
+        if (l > 0) {
+            hx *= 2.0;
+            hy *= 2.0;
+            hz *= 2.0;
+        }
+        L.h[0] = hx;
+        L.h[1] = hy;
+        L.h[2] = hz;
+        const bool top = (l == 0);
+        k_build_system<<<blocks_for(L.n.count()), kThreads, 0, c->stream>>>(
+            L.n, hx, hy, hz, L.phi, L.uw, L.vw, L.ww, top ? u : nullptr,
+            top ? v : nullptr, top ? w : nullptr, top ? su : nullptr,
+            top ? sv : nullptr, top ? sw : nullptr, top ? c->A64 : nullptr,
+            top ? c->b64 : nullptr, L.A);
+    }
+    JG_CUDA(c, cudaGetLastError());
+    return JETGPU_OK;
+}
+
+jetgpu_status apply_gradient(Ctx* c, const GridDesc& g, const double* u,
+                             const double* v, const double* w, double* ou,
+                             double* ov, double* ow) {
+    const Level& L = c->levels[0];
+    const Dims n = L.n;
+    const long nu = (long)(n.x + 1) * n.y * n.z, nv = (long)n.x * (n.y + 1) * n.z,
+               nw = (long)n.x * n.y * (n.z + 1);
+    if (ou != u)
+        JG_CUDA(c, cudaMemcpyAsync(ou, u, nu * 8, cudaMemcpyDeviceToDevice,
+                                   c->stream));
+    if (ov != v)
+        JG_CUDA(c, cudaMemcpyAsync(ov, v, nv * 8, cudaMemcpyDeviceToDevice,
+                                   c->stream));
+    if (ow != w)
+        JG_CUDA(c, cudaMemcpyAsync(ow, w, nw * 8, cudaMemcpyDeviceToDevice,
+                                   c->stream));
+    k_apply_gradient<<<blocks_for(n.count()), kThreads, 0, c->stream>>>(
+        n, 1.0 / g.spacing[0], 1.0 / g.spacing[1], 1.0 / g.spacing[2], L.phi,
+        L.uw, L.vw, L.ww, c->x64, u, v, w, ou, ov, ow);
+    JG_CUDA(c, cudaGetLastError());
+    return JETGPU_OK;
+}
+
+}  // namespace jg

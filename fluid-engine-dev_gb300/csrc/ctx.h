@@ -1,0 +1,153 @@
+// Host-side context of libjetgpu: device buffers, stream, launch helpers.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/jetgpu.h"
+#include "common.cuh"
+
+namespace jg {
+
+// One multigrid level.
+struct Level {
+    Dims n{0, 0, 0};
+    double h[3] = {0, 0, 0};
+    float* phi = nullptr;        // fluid SDF at cell centres
+    float* uw = nullptr;         // face weights
+    float* vw = nullptr;
+    float* ww = nullptr;
+    float4* A = nullptr;         // FP32 matrix rows
+    float* x = nullptr;          // V-cycle solution
+    float* x2 = nullptr;         // ping-pong partner of x (fused smoother)
+    float* b = nullptr;          // V-cycle rhs
+    float* r = nullptr;          // residual scratch
+    __nv_bfloat16* xh = nullptr; // BF16 storage (mixed mode)
+    __nv_bfloat16* bh = nullptr;
+    uint2* Ah = nullptr;         // BF16 matrix rows (4 x bf16)
+};
+
+struct Ctx {
+    jetgpu_config cfg;
+    int device = 0;
+    int num_sms = 0;
+    cudaStream_t stream = nullptr;
+    std::string err;
+
+    // Allocated geometry.
+    Dims n0{0, 0, 0};
+    unsigned built_levels = 0;
+    std::vector<Level> levels;
+
+    // Finest-level FP64 system and solution.
+    double* A64 = nullptr;  // 4 doubles per cell
+    double* b64 = nullptr;
+    double* x64 = nullptr;
+    double* r64 = nullptr;
+
+    // Krylov vectors (FP32 modes).
+    float* kx = nullptr;
+    float* kr = nullptr;
+    float* kd = nullptr;
+    float* kq = nullptr;
+    float* kz = nullptr;
+    // Krylov vectors (FP64 mode).
+    double* dx = nullptr;
+    double* dr = nullptr;
+    double* dd = nullptr;
+    double* dq = nullptr;
+    double* dz = nullptr;
+
+    // Reductions.
+    double* scal = nullptr;
+    double* partials = nullptr;
+    unsigned* counters = nullptr;
+    double* h_scal = nullptr;  // pinned mirror
+
+    // Staging for the host-pointer API (device copies of inputs/outputs).
+    size_t stage_bytes = 0;
+    unsigned char* stage = nullptr;
+    size_t host_stage_bytes = 0;
+    unsigned char* host_stage = nullptr;  // pinned
+
+    // Particle-transfer scratch.
+    size_t pscratch_bytes = 0;
+    unsigned char* pscratch = nullptr;
+
+    cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
+
+    // Learned preconditioner (opaque; see unet.cu).
+    void* unet = nullptr;
+};
+
+// Sets ctx->err and returns the status.
+jetgpu_status fail(Ctx* c, jetgpu_status s, const std::string& msg);
+
+#define JG_CUDA(c, call)                                                    \
+    do {                                                                    \
+        cudaError_t e_ = (call);                                            \
+        if (e_ != cudaSuccess) {                                            \
+            return ::jg::fail((c), e_ == cudaErrorMemoryAllocation          \
+                                       ? JETGPU_OUT_OF_MEMORY               \
+                                       : JETGPU_CUDA_ERROR,                 \
+                              std::string(#call) + ": " +                   \
+                                  cudaGetErrorString(e_));                  \
+        }                                                                   \
+    } while (0)
+
+// Number of blocks for a grid-stride kernel over n elements.
+inline int blocks_for(long n, int threads = kThreads, int cap = 1 << 30) {
+    long b = (n + threads - 1) / threads;
+    if (b < 1) b = 1;
+    if (b > cap) b = cap;
+    return (int)b;
+}
+
+// Reduction grid size: fixed per resolution, at most kMaxRedBlocks.
+inline int red_blocks(const Ctx* c, long n) {
+    int cap = c->num_sms * 6;
+    if (cap > kMaxRedBlocks) cap = kMaxRedBlocks;
+    return blocks_for(n, kThreads, cap);
+}
+
+// ---- build.cu -------------------------------------------------------------
+jetgpu_status build_weights(Ctx* c, const GridDesc& g, const FieldDesc& bsdf,
+                            const FieldDesc& fsdf);
+jetgpu_status build_system(Ctx* c, const GridDesc& g, const double* u,
+                           const double* v, const double* w,
+                           const double* su, const double* sv,
+                           const double* sw);
+jetgpu_status apply_gradient(Ctx* c, const GridDesc& g, const double* u,
+                             const double* v, const double* w, double* ou,
+                             double* ov, double* ow);
+
+// ---- mgpcg.cu -------------------------------------------------------------
+// Allocates the multigrid hierarchy and solver buffers for resolution n.
+jetgpu_status ensure_buffers(Ctx* c, Dims n, unsigned max_levels);
+// Derives FP32 (and BF16) matrices of every level from the built system.
+jetgpu_status prepare_levels(Ctx* c);
+// Solves A64 x64 = b64 on the finest level; fills stats.
+jetgpu_status mgpcg_solve(Ctx* c, jetgpu_solve_stats* st);
+// Computes level count for resolution n (FdmMgUtils3::resizeArrayWithFinest).
+unsigned level_count(Dims n, unsigned max_levels);
+
+// Applies one V-cycle z = M r on FP32 vectors (exposed for tests).
+jetgpu_status vcycle(Ctx* c, const float* r, float* z);
+
+// ---- transfer.cu ----------------------------------------------------------
+jetgpu_status p2g(Ctx* c, const GridDesc& g, long np, const double* pos,
+                  const double* vel, double* u, double* v, double* w,
+                  unsigned char* mu, unsigned char* mv, unsigned char* mw,
+                  float* su, float* sv, float* sw);
+jetgpu_status g2p_flip(Ctx* c, const GridDesc& g, long np, const double* pos,
+                       double* vel, const double* u, const double* v,
+                       const double* w, float* su, float* sv, float* sw,
+                       double blend);
+jetgpu_status g2p_pic(Ctx* c, const GridDesc& g, long np, const double* pos,
+                      double* vel, const double* u, const double* v,
+                      const double* w);
+
+}  // namespace jg

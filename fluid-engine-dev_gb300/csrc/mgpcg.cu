@@ -1,0 +1,673 @@
+// Multigrid-preconditioned CG on GB300 (K5-K11).
+//
+// Replaces FdmMgpcgSolver3::solve (src/jet/fdm_mgpcg_solver3.cpp:54-80), the
+// generic pcg (include/jet/detail/cg-inl.h:15-94) and mgVCycle
+// (include/jet/detail/mg-inl.h:16-68) with red-black SOR smoothing
+// (src/jet/fdm_gauss_seidel_solver3.cpp:150-221) and the FdmMgUtils3
+// transfer operators (src/jet/fdm_mg_linear_system3.cpp:43-179).
+//
+// Design (GB300-first):
+//   * Krylov vectors FP32 (or FP64), matrix rows as one aligned float4 per
+//     cell, V-cycle in FP32; every global reduction is FP64, deterministic
+//     (fixed grid, per-block partials summed in block order by the last block
+//     to finish; no block ever waits on another).
+//   * alpha and beta never leave the device: the last block of each reduction
+//     computes them, the next kernel reads them. The host reads one scalar per
+//     iteration (the residual norm) for the stopping test.
+//   * FP32 modes reach the FP64 tolerance by iterative refinement: the FP64
+//     residual b - A x is evaluated with the exact FP64 matrix the reference
+//     builds, the FP32 PCG solves for a correction, and x accumulates in FP64.
+//   * The V-cycle is symmetric (post-smoothing sweeps the colours in reverse
+//     order, restriction is 1/8 of the prolongation's transpose — true of the
+//     reference's operators including their clamped boundaries) and starts
+//     from zero, so it is a fixed SPD preconditioner for CG.
+
+#include "ctx.h"
+
+#include <chrono>
+#include <cmath>
+#include <cstring>
+
+namespace jg {
+namespace {
+
+enum Fin : int { FIN_NONE = 0, FIN_BETA = 1, FIN_ALPHA = 2 };
+enum : int { S_ALPHA = 8, S_BETA = 9, S_FIRST = 10 };
+
+// Finishes a reduction: stores the total and derives alpha/beta.
+__device__ __forceinline__ void finish(double* scal, int target, double v,
+                                       int fin) {
+    scal[target] = v;
+    if (fin == FIN_BETA) {
+        const double old = scal[S_RZ_OLD];
+        scal[S_BETA] = (scal[S_FIRST] != 0.0 || old == 0.0) ? 0.0 : v / old;
+        scal[S_RZ_OLD] = v;
+        scal[S_FIRST] = 0.0;
+    } else if (fin == FIN_ALPHA) {
+        scal[S_ALPHA] = scal[S_RZ] / v;
+    }
+}
+
+template <int NT>
+__device__ __forceinline__ void reduce_finish(double partial, int slot,
+                                              int target, int fin,
+                                              double* partials,
+                                              unsigned* counters,
+                                              double* scal, double* smem) {
+    __shared__ bool is_last;
+    double bs = block_sum<NT>(partial, smem);
+    if (threadIdx.x == 0) {
+        partials[slot * kMaxRedBlocks + blockIdx.x] = bs;
+        __threadfence();
+        const unsigned done = atomicAdd(&counters[slot], 1u);
+        is_last = (done == gridDim.x - 1);
+    }
+    __syncthreads();
+    if (is_last) {
+        __threadfence();
+        double v = 0.0;
+        for (int b = threadIdx.x; b < (int)gridDim.x; b += NT)
+            v += __ldcg(&partials[slot * kMaxRedBlocks + b]);
+        v = block_sum<NT>(v, smem);
+        if (threadIdx.x == 0) {
+            finish(scal, target, v, fin);
+            counters[slot] = 0u;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Matrix access: FP32 rows (float4) or the exact FP64 rows (4 doubles).
+
+struct RowsF {
+    const float4* A;
+    __device__ __forceinline__ float4 row(long c) const { return A[c]; }
+};
+struct RowsD {
+    const double* A;
+    __device__ __forceinline__ double4 row(long c) const {
+        const double2 a = reinterpret_cast<const double2*>(A)[2 * c];
+        const double2 b = reinterpret_cast<const double2*>(A)[2 * c + 1];
+        return make_double4(a.x, a.y, b.x, b.y);
+    }
+};
+
+// 7-point symmetric apply at cell c (FdmBlas3::mvm, fdm_linear_system3.cpp:79-96).
+template <typename T, typename Rows, typename V>
+__device__ __forceinline__ T apply7(const Rows& M, const V* __restrict__ v,
+                                    long c, int i, int j, int k, Dims n) {
+    const long sy = n.x, sz = (long)n.x * n.y;
+    const auto r = M.row(c);
+    T s = (T)r.x * (T)v[c];
+    if (i > 0) s += (T)M.row(c - 1).y * (T)v[c - 1];
+    if (i + 1 < n.x) s += (T)r.y * (T)v[c + 1];
+    if (j > 0) s += (T)M.row(c - sy).z * (T)v[c - sy];
+    if (j + 1 < n.y) s += (T)r.z * (T)v[c + sy];
+    if (k > 0) s += (T)M.row(c - sz).w * (T)v[c - sz];
+    if (k + 1 < n.z) s += (T)r.w * (T)v[c + sz];
+    return s;
+}
+
+// K5: q = A d and d.q (FP64).
+template <typename V, typename Rows>
+__global__ void __launch_bounds__(kThreads)
+    k_spmv_dot(Rows M, const V* __restrict__ d, V* __restrict__ q, Dims n,
+               double* partials, unsigned* counters, double* scal) {
+    __shared__ double smem[32];
+    const long N = n.count();
+    double acc = 0.0;
+    for (long c = blockIdx.x * (long)kThreads + threadIdx.x; c < N;
+         c += (long)gridDim.x * kThreads) {
+        const int i = (int)(c % n.x);
+        const int j = (int)((c / n.x) % n.y);
+        const int k = (int)(c / ((long)n.x * n.y));
+        const V qv = apply7<V>(M, d, c, i, j, k, n);
+        q[c] = qv;
+        acc += (double)d[c] * (double)qv;
+    }
+    reduce_finish<kThreads>(acc, 0, S_DQ, FIN_ALPHA, partials, counters, scal,
+                            smem);
+}
+
+// K7a: x += alpha d; r -= alpha q; r.r (FP64). Optionally writes an FP32
+// copy of r for the V-cycle (FP64 mode).
+template <typename V>
+__global__ void __launch_bounds__(kThreads)
+    k_update_xr(V* __restrict__ x, V* __restrict__ r, const V* __restrict__ d,
+                const V* __restrict__ q, float* __restrict__ r32, long N,
+                double* partials, unsigned* counters, double* scal) {
+    __shared__ double smem[32];
+    const V alpha = (V)scal[S_ALPHA];
+    double acc = 0.0;
+    for (long c = blockIdx.x * (long)kThreads + threadIdx.x; c < N;
+         c += (long)gridDim.x * kThreads) {
+        x[c] += alpha * d[c];
+        const V rv = r[c] - alpha * q[c];
+        r[c] = rv;
+        if (r32) r32[c] = (float)rv;
+        acc += (double)rv * (double)rv;
+    }
+    reduce_finish<kThreads>(acc, 1, S_RR, FIN_NONE, partials, counters, scal,
+                            smem);
+}
+
+// K7b: r.z (FP64), finishing beta.
+template <typename V, typename Z>
+__global__ void __launch_bounds__(kThreads)
+    k_dot_rz(const V* __restrict__ r, const Z* __restrict__ z, long N,
+             double* partials, unsigned* counters, double* scal) {
+    __shared__ double smem[32];
+    double acc = 0.0;
+    for (long c = blockIdx.x * (long)kThreads + threadIdx.x; c < N;
+         c += (long)gridDim.x * kThreads)
+        acc += (double)r[c] * (double)z[c];
+    reduce_finish<kThreads>(acc, 2, S_RZ, FIN_BETA, partials, counters, scal,
+                            smem);
+}
+
+// K7c: d = z + beta d.
+template <typename V, typename Z>
+__global__ void __launch_bounds__(kThreads)
+    k_update_d(V* __restrict__ d, const Z* __restrict__ z, long N,
+               const double* scal) {
+    const V beta = (V)scal[S_BETA];
+    for (long c = blockIdx.x * (long)kThreads + threadIdx.x; c < N;
+         c += (long)gridDim.x * kThreads)
+        d[c] = (beta == (V)0) ? (V)z[c] : (V)z[c] + beta * d[c];
+}
+
+// K6 (FP64): r64 = b64 - A64 x64 with the exact reference rows
+// (FdmBlas3::residual, fdm_linear_system3.cpp:98-116); ||r64||^2; optional
+// FP32 copy of r64 and zeroing of the FP32 correction.
+__global__ void __launch_bounds__(kThreads)
+    k_residual64(const double* __restrict__ A64, const double* __restrict__ x,
+                 const double* __restrict__ b, double* __restrict__ r,
+                 float* __restrict__ r32, float* __restrict__ zero32, Dims n,
+                 double* partials, unsigned* counters, double* scal,
+                 int target) {
+    __shared__ double smem[32];
+    const long N = n.count();
+    RowsD M{A64};
+    double acc = 0.0;
+    for (long c = blockIdx.x * (long)kThreads + threadIdx.x; c < N;
+         c += (long)gridDim.x * kThreads) {
+        const int i = (int)(c % n.x);
+        const int j = (int)((c / n.x) % n.y);
+        const int k = (int)(c / ((long)n.x * n.y));
+        const double rv = b[c] - apply7<double>(M, x, c, i, j, k, n);
+        if (r) r[c] = rv;
+        if (r32) r32[c] = (float)rv;
+        if (zero32) zero32[c] = 0.0f;
+        acc += rv * rv;
+    }
+    reduce_finish<kThreads>(acc, 3, target, FIN_NONE, partials, counters,
+                            scal, smem);
+}
+
+// x64 += e (FP32 correction).
+__global__ void k_accumulate(double* __restrict__ x, const float* __restrict__ e,
+                             long N) {
+    for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < N;
+         c += (long)gridDim.x * blockDim.x)
+        x[c] += (double)e[c];
+}
+
+// ||v||^2 (FP64).
+__global__ void __launch_bounds__(kThreads)
+    k_norm2(const double* __restrict__ v, long N, double* partials,
+            unsigned* counters, double* scal, int target) {
+    __shared__ double smem[32];
+    double acc = 0.0;
+    for (long c = blockIdx.x * (long)kThreads + threadIdx.x; c < N;
+         c += (long)gridDim.x * kThreads)
+        acc += v[c] * v[c];
+    reduce_finish<kThreads>(acc, 4, target, FIN_NONE, partials, counters,
+                            scal, smem);
+}
+
+__global__ void k_init_scalars(double* scal) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        scal[S_RZ] = 0.0;
+        scal[S_RZ_OLD] = 0.0;
+        scal[S_DQ] = 0.0;
+        scal[S_RR] = 0.0;
+        scal[S_ALPHA] = 0.0;
+        scal[S_BETA] = 0.0;
+        scal[S_FIRST] = 1.0;
+    }
+}
+
+template <typename V>
+__global__ void k_zero(V* __restrict__ p, long N) {
+    for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < N;
+         c += (long)gridDim.x * blockDim.x)
+        p[c] = (V)0;
+}
+
+// ---------------------------------------------------------------------------
+// V-cycle kernels (FP32).
+
+// K8: one red-black SOR half-sweep (relaxRedBlack, :150-221). One thread per
+// pair of cells along i; `color` 0 updates (i+j+k) even cells. With ZERO the
+// whole vector is taken as zero on entry: the updated colour gets
+// omega*b/center and the other colour is written 0 (no read of x).
+template <bool ZERO>
+__global__ void __launch_bounds__(kThreads)
+    k_rb_half(const float4* __restrict__ A, const float* __restrict__ b,
+              float* __restrict__ x, Dims n, int color, float omega) {
+    const int hx = (n.x + 1) >> 1;
+    const long N = (long)hx * n.y * n.z;
+    const long sy = n.x, sz = (long)n.x * n.y;
+    for (long t = blockIdx.x * (long)kThreads + threadIdx.x; t < N;
+         t += (long)gridDim.x * kThreads) {
+        const int p = (int)(t % hx);
+        const long row = t / hx;
+        const int j = (int)(row % n.y);
+        const int k = (int)(row / n.y);
+        const int off = (j + k + color) & 1;
+        const int i = 2 * p + off;
+        const long base = lin(2 * p, j, k, n.x, n.y);
+        if (ZERO) {
+            if (i < n.x) {
+                const long c = base + off;
+                const float4 r = A[c];
+                x[c] = omega * b[c] / r.x;
+            }
+            const int io = 2 * p + (off ^ 1);
+            if (io < n.x) x[base + (off ^ 1)] = 0.0f;
+        } else {
+            if (i >= n.x) continue;
+            const long c = base + off;
+            const float4 r = A[c];
+            float s = 0.0f;
+            if (i > 0) s += A[c - 1].y * x[c - 1];
+            if (i + 1 < n.x) s += r.y * x[c + 1];
+            if (j > 0) s += A[c - sy].z * x[c - sy];
+            if (j + 1 < n.y) s += r.z * x[c + sy];
+            if (k > 0) s += A[c - sz].w * x[c - sz];
+            if (k + 1 < n.z) s += r.w * x[c + sz];
+            x[c] = (1.0f - omega) * x[c] + omega * (b[c] - s) / r.x;
+        }
+    }
+}
+
+// K9a: r = b - A x (FP32).
+__global__ void __launch_bounds__(kThreads)
+    k_residual32(const float4* __restrict__ A, const float* __restrict__ x,
+                 const float* __restrict__ b, float* __restrict__ r, Dims n) {
+    const long N = n.count();
+    RowsF M{A};
+    for (long c = blockIdx.x * (long)kThreads + threadIdx.x; c < N;
+         c += (long)gridDim.x * kThreads) {
+        const int i = (int)(c % n.x);
+        const int j = (int)((c / n.x) % n.y);
+        const int k = (int)(c / ((long)n.x * n.y));
+        r[c] = b[c] - apply7<float>(M, x, c, i, j, k, n);
+    }
+}
+
+// K9b: FdmMgUtils3::restrict (fdm_mg_linear_system3.cpp:43-98): 4x4x4
+// (1,3,3,1)/8 tensor filter with taps clamped at the edges.
+__global__ void __launch_bounds__(kThreads)
+    k_restrict(const float* __restrict__ fine, float* __restrict__ coarse,
+               Dims c) {
+    const long N = c.count();
+    const int fx = 2 * c.x, fy = 2 * c.y;
+    const float kern[4] = {0.125f, 0.375f, 0.375f, 0.125f};
+    for (long t = blockIdx.x * (long)kThreads + threadIdx.x; t < N;
+         t += (long)gridDim.x * kThreads) {
+        const int i = (int)(t % c.x);
+        const int j = (int)((t / c.x) % c.y);
+        const int k = (int)(t / ((long)c.x * c.y));
+        int iI[4] = {i > 0 ? 2 * i - 1 : 2 * i, 2 * i, 2 * i + 1,
+                     i + 1 < c.x ? 2 * i + 2 : 2 * i + 1};
+        int jI[4] = {j > 0 ? 2 * j - 1 : 2 * j, 2 * j, 2 * j + 1,
+                     j + 1 < c.y ? 2 * j + 2 : 2 * j + 1};
+        int kI[4] = {k > 0 ? 2 * k - 1 : 2 * k, 2 * k, 2 * k + 1,
+                     k + 1 < c.z ? 2 * k + 2 : 2 * k + 1};
+        float sum = 0.0f;
+#pragma unroll
+        for (int z = 0; z < 4; ++z) {
+            float sy = 0.0f;
+#pragma unroll
+            for (int y = 0; y < 4; ++y) {
+                const float* rowp = fine + lin(0, jI[y], kI[z], fx, fy);
+                const float sx = kern[0] * rowp[iI[0]] + kern[1] * rowp[iI[1]] +
+                                 kern[2] * rowp[iI[2]] + kern[3] * rowp[iI[3]];
+                sy += kern[y] * sx;
+            }
+            sum += kern[z] * sy;
+        }
+        coarse[t] = sum;
+    }
+}
+
+// K10: FdmMgUtils3::correct (fdm_mg_linear_system3.cpp:100-179): fine +=
+// trilinear (1/4, 3/4) prolongation of coarse, clamped at the edges.
+__global__ void __launch_bounds__(kThreads)
+    k_correct(const float* __restrict__ coarse, float* __restrict__ fine,
+              Dims c) {
+    const Dims n{2 * c.x, 2 * c.y, 2 * c.z};
+    const long N = n.count();
+    for (long t = blockIdx.x * (long)kThreads + threadIdx.x; t < N;
+         t += (long)gridDim.x * kThreads) {
+        const int i = (int)(t % n.x);
+        const int j = (int)((t / n.x) % n.y);
+        const int k = (int)(t / ((long)n.x * n.y));
+        const int ci = i >> 1, cj = j >> 1, ck = k >> 1;
+        int i0, i1, j0, j1, k0, k1;
+        float wi0, wi1, wj0, wj1, wk0, wk1;
+        if ((i & 1) == 0) { i0 = i > 1 ? ci - 1 : ci; i1 = ci; wi0 = 0.25f; wi1 = 0.75f; }
+        else { i0 = ci; i1 = i + 1 < n.x ? ci + 1 : ci; wi0 = 0.75f; wi1 = 0.25f; }
+        if ((j & 1) == 0) { j0 = j > 1 ? cj - 1 : cj; j1 = cj; wj0 = 0.25f; wj1 = 0.75f; }
+        else { j0 = cj; j1 = j + 1 < n.y ? cj + 1 : cj; wj0 = 0.75f; wj1 = 0.25f; }
+        if ((k & 1) == 0) { k0 = k > 1 ? ck - 1 : ck; k1 = ck; wk0 = 0.25f; wk1 = 0.75f; }
+        else { k0 = ck; k1 = k + 1 < n.z ? ck + 1 : ck; wk0 = 0.75f; wk1 = 0.25f; }
+        const float c000 = coarse[lin(i0, j0, k0, c.x, c.y)];
+        const float c100 = coarse[lin(i1, j0, k0, c.x, c.y)];
+        const float c010 = coarse[lin(i0, j1, k0, c.x, c.y)];
+        const float c110 = coarse[lin(i1, j1, k0, c.x, c.y)];
+        const float c001 = coarse[lin(i0, j0, k1, c.x, c.y)];
+        const float c101 = coarse[lin(i1, j0, k1, c.x, c.y)];
+        const float c011 = coarse[lin(i0, j1, k1, c.x, c.y)];
+        const float c111 = coarse[lin(i1, j1, k1, c.x, c.y)];
+        const float a0 = wj0 * (wi0 * c000 + wi1 * c100) + wj1 * (wi0 * c010 + wi1 * c110);
+        const float a1 = wj0 * (wi0 * c001 + wi1 * c101) + wj1 * (wi0 * c011 + wi1 * c111);
+        fine[t] += wk0 * a0 + wk1 * a1;
+    }
+}
+
+// K11: coarsest level in one CTA: x and b in shared memory, `sweeps`
+// forward red-black sweeps followed by `sweeps` sweeps in reverse colour
+// order (symmetric), starting from x = 0.
+constexpr int kCoarsestMaxCells = 4096;
+__global__ void __launch_bounds__(1024)
+    k_coarsest(const float4* __restrict__ A, const float* __restrict__ b,
+               float* __restrict__ x, Dims n, int sweeps, float omega) {
+    __shared__ float sx[kCoarsestMaxCells];
+    __shared__ float sb[kCoarsestMaxCells];
+    const int N = (int)n.count();
+    const int sy = n.x, sz = n.x * n.y;
+    for (int c = threadIdx.x; c < N; c += blockDim.x) {
+        sx[c] = 0.0f;
+        sb[c] = b[c];
+    }
+    __syncthreads();
+    for (int pass = 0; pass < 2 * sweeps; ++pass) {
+        for (int h = 0; h < 2; ++h) {
+            const int color = (pass < sweeps) ? h : 1 - h;
+            for (int c = threadIdx.x; c < N; c += blockDim.x) {
+                const int i = c % n.x, j = (c / n.x) % n.y, k = c / sz;
+                if (((i + j + k) & 1) != color) continue;
+                const float4 r = A[c];
+                float s = 0.0f;
+                if (i > 0) s += A[c - 1].y * sx[c - 1];
+                if (i + 1 < n.x) s += r.y * sx[c + 1];
+                if (j > 0) s += A[c - sy].z * sx[c - sy];
+                if (j + 1 < n.y) s += r.z * sx[c + sy];
+                if (k > 0) s += A[c - sz].w * sx[c - sz];
+                if (k + 1 < n.z) s += r.w * sx[c + sz];
+                sx[c] = (1.0f - omega) * sx[c] + omega * (sb[c] - s) / r.x;
+            }
+            __syncthreads();
+        }
+    }
+    for (int c = threadIdx.x; c < N; c += blockDim.x) x[c] = sx[c];
+}
+
+// ---------------------------------------------------------------------------
+
+int grid_for(const Ctx* c, long work) {
+    int cap = c->num_sms * 8;
+    return blocks_for(work, kThreads, cap);
+}
+
+void rb_half(Ctx* c, const Level& L, const float* b, float* x, int color,
+             bool zero) {
+    const long pairs = (long)((L.n.x + 1) / 2) * L.n.y * L.n.z;
+    const float w = (float)c->cfg.sor;
+    if (zero)
+        k_rb_half<true><<<grid_for(c, pairs), kThreads, 0, c->stream>>>(
+            L.A, b, x, L.n, color, w);
+    else
+        k_rb_half<false><<<grid_for(c, pairs), kThreads, 0, c->stream>>>(
+            L.A, b, x, L.n, color, w);
+}
+
+// Forward sweeps (red then black) from x = 0 when `zero`.
+void smooth(Ctx* c, const Level& L, const float* b, float* x, unsigned sweeps,
+            bool reverse, bool zero) {
+    for (unsigned s = 0; s < sweeps; ++s) {
+        const int first = reverse ? 1 : 0;
+        rb_half(c, L, b, x, first, zero && s == 0);
+        rb_half(c, L, b, x, 1 - first, false);
+    }
+    if (sweeps == 0 && zero) k_zero<float><<<grid_for(c, L.n.count()), kThreads, 0, c->stream>>>(x, L.n.count());
+}
+
+void vcycle_level(Ctx* c, unsigned l, const float* b, float* x) {
+    const Level& L = c->levels[l];
+    const unsigned nl = c->built_levels;
+    const jetgpu_config& cfg = c->cfg;
+    if (l + 1 == nl) {
+        if (L.n.count() <= kCoarsestMaxCells) {
+            int nt = (int)std::min<long>(1024, ((L.n.count() + 31) / 32) * 32);
+            k_coarsest<<<1, nt, 0, c->stream>>>(L.A, b, x, L.n,
+                                                (int)cfg.coarsest_iter,
+                                                (float)cfg.sor);
+        } else {
+            smooth(c, L, b, x, cfg.coarsest_iter, false, true);
+            smooth(c, L, b, x, cfg.coarsest_iter, true, false);
+        }
+        return;
+    }
+    const Level& C = c->levels[l + 1];
+    smooth(c, L, b, x, cfg.restrict_iter, false, true);
+    k_residual32<<<grid_for(c, L.n.count()), kThreads, 0, c->stream>>>(
+        L.A, x, b, L.r, L.n);
+    k_restrict<<<grid_for(c, C.n.count()), kThreads, 0, c->stream>>>(
+        L.r, C.b, C.n);
+    vcycle_level(c, l + 1, C.b, C.x);
+    k_correct<<<grid_for(c, L.n.count()), kThreads, 0, c->stream>>>(C.x, x,
+                                                                    C.n);
+    smooth(c, L, b, x, l == 0 ? cfg.final_iter : cfg.correct_iter, true,
+           false);
+}
+
+double now_ms() {
+    using namespace std::chrono;
+    return duration<double, std::milli>(
+               steady_clock::now().time_since_epoch())
+        .count();
+}
+
+jetgpu_status read_scalars(Ctx* c) {
+    JG_CUDA(c, cudaMemcpyAsync(c->h_scal, c->scal, S_COUNT * sizeof(double),
+                               cudaMemcpyDeviceToHost, c->stream));
+    JG_CUDA(c, cudaStreamSynchronize(c->stream));
+    return JETGPU_OK;
+}
+
+}  // namespace
+
+unsigned level_count(Dims n, unsigned max_levels) {
+    unsigned i = 1;
+    Dims r = n;
+    for (; i < max_levels; ++i) {
+        if (r.x % 2 == 0 && r.y % 2 == 0 && r.z % 2 == 0) {
+            r.x >>= 1;
+            r.y >>= 1;
+            r.z >>= 1;
+        } else {
+            break;
+        }
+    }
+    return i < 1 ? 1 : i;
+}
+
+jetgpu_status vcycle(Ctx* c, const float* r, float* z) {
+    vcycle_level(c, 0, r, z);
+    JG_CUDA(c, cudaGetLastError());
+    return JETGPU_OK;
+}
+
+jetgpu_status prepare_levels(Ctx* c) {
+    (void)c;
+    return JETGPU_OK;
+}
+
+// PCG on the FP32 rows for a correction e with A e = r (r = kr on entry).
+// Stops when ||r_k|| <= target or after max_it iterations.
+static jetgpu_status pcg_f32(Ctx* c, double target, unsigned max_it,
+                             unsigned* it_out, double* rr_out) {
+    const Level& L0 = c->levels[0];
+    const Dims n = L0.n;
+    const long N = n.count();
+    const int G = red_blocks(c, N);
+    RowsF M{L0.A};
+    k_init_scalars<<<1, 32, 0, c->stream>>>(c->scal);
+    unsigned it = 0;
+    double rr = 0;
+    while (it < max_it) {
+        if (jetgpu_status vs = vcycle(c, c->kr, c->kz)) return vs;
+        k_dot_rz<float, float><<<G, kThreads, 0, c->stream>>>(
+            c->kr, c->kz, N, c->partials, c->counters, c->scal);
+        k_update_d<float, float><<<G, kThreads, 0, c->stream>>>(c->kd, c->kz,
+                                                                N, c->scal);
+        k_spmv_dot<float, RowsF><<<G, kThreads, 0, c->stream>>>(
+            M, c->kd, c->kq, n, c->partials, c->counters, c->scal);
+        k_update_xr<float><<<G, kThreads, 0, c->stream>>>(
+            c->kx, c->kr, c->kd, c->kq, nullptr, N, c->partials, c->counters,
+            c->scal);
+        ++it;
+        jetgpu_status s = read_scalars(c);
+        if (s != JETGPU_OK) return s;
+        rr = c->h_scal[S_RR];
+        if (!std::isfinite(rr))
+            return fail(c, JETGPU_NUMERICAL_ERROR,
+                        "non-finite residual in FP32 PCG");
+        if (std::sqrt(rr) <= target) break;
+    }
+    *it_out = it;
+    *rr_out = rr;
+    return JETGPU_OK;
+}
+
+// PCG in FP64 on the exact rows; x64 is the iterate, r64 the residual.
+static jetgpu_status pcg_f64(Ctx* c, double target, unsigned max_it,
+                             unsigned* it_out, double* rr_out) {
+    const Level& L0 = c->levels[0];
+    const Dims n = L0.n;
+    const long N = n.count();
+    const int G = red_blocks(c, N);
+    RowsD M{c->A64};
+    k_init_scalars<<<1, 32, 0, c->stream>>>(c->scal);
+    unsigned it = 0;
+    double rr = 0;
+    float* r32 = L0.b;  // FP32 copy of r feeds the V-cycle
+    // r32 already holds float(r64) (written by the residual kernel).
+    while (it < max_it) {
+        if (jetgpu_status vs = vcycle(c, r32, L0.x)) return vs;
+        k_dot_rz<double, float><<<G, kThreads, 0, c->stream>>>(
+            c->r64, L0.x, N, c->partials, c->counters, c->scal);
+        k_update_d<double, float><<<G, kThreads, 0, c->stream>>>(c->dd, L0.x,
+                                                                 N, c->scal);
+        k_spmv_dot<double, RowsD><<<G, kThreads, 0, c->stream>>>(
+            M, c->dd, c->dq, n, c->partials, c->counters, c->scal);
+        k_update_xr<double><<<G, kThreads, 0, c->stream>>>(
+            c->x64, c->r64, c->dd, c->dq, r32, N, c->partials, c->counters,
+            c->scal);
+        ++it;
+        jetgpu_status s = read_scalars(c);
+        if (s != JETGPU_OK) return s;
+        rr = c->h_scal[S_RR];
+        if (!std::isfinite(rr))
+            return fail(c, JETGPU_NUMERICAL_ERROR,
+                        "non-finite residual in FP64 PCG");
+        if (std::sqrt(rr) <= target) break;
+    }
+    *it_out = it;
+    *rr_out = rr;
+    return JETGPU_OK;
+}
+
+jetgpu_status mgpcg_solve(Ctx* c, jetgpu_solve_stats* st) {
+    const Level& L0 = c->levels[0];
+    const Dims n = L0.n;
+    const long N = n.count();
+    const int G = red_blocks(c, N);
+    const jetgpu_config& cfg = c->cfg;
+    const bool fp64 = (cfg.precision == JETGPU_PRECISION_FP64);
+
+    // ||b||, x64 = 0.
+    k_norm2<<<G, kThreads, 0, c->stream>>>(c->b64, N, c->partials,
+                                           c->counters, c->scal, S_B64);
+    k_zero<double><<<grid_for(c, N), kThreads, 0, c->stream>>>(c->x64, N);
+    jetgpu_status s = read_scalars(c);
+    if (s != JETGPU_OK) return s;
+    const double bnorm = std::sqrt(c->h_scal[S_B64]);
+    if (!std::isfinite(bnorm))
+        return fail(c, JETGPU_NUMERICAL_ERROR, "non-finite right-hand side");
+    st->b_norm = bnorm;
+    st->iterations = 0;
+    st->refinements = 0;
+    st->residual = 0.0;
+    st->relative_residual = 0.0;
+    if (bnorm == 0.0) return JETGPU_OK;
+
+    const double goal = cfg.tolerance * bnorm;
+    double rnorm = bnorm;
+    unsigned total = 0;
+    const unsigned max_pass = cfg.max_refinements > 0 ? cfg.max_refinements : 1;
+    for (unsigned pass = 0; pass < max_pass && total < cfg.max_cg_iter;
+         ++pass) {
+        // True FP64 residual r64 = b - A x64 (and its FP32 image).
+        float* r32 = fp64 ? L0.b : c->kr;
+        k_residual64<<<G, kThreads, 0, c->stream>>>(
+            c->A64, c->x64, c->b64, c->r64, r32, fp64 ? nullptr : c->kx, n,
+            c->partials, c->counters, c->scal, S_R64);
+        s = read_scalars(c);
+        if (s != JETGPU_OK) return s;
+        rnorm = std::sqrt(c->h_scal[S_R64]);
+        st->residual = rnorm;
+        st->relative_residual = rnorm / bnorm;
+        if (!std::isfinite(rnorm))
+            return fail(c, JETGPU_NUMERICAL_ERROR, "non-finite residual");
+        if (rnorm <= goal) break;
+        st->refinements = pass + 1;
+        unsigned it = 0;
+        double rr = 0;
+        if (fp64) {
+            s = pcg_f64(c, goal * 0.5, cfg.max_cg_iter - total, &it, &rr);
+        } else {
+            // Inner FP32 solve to a relative reduction the FP32 operator can
+            // deliver; the FP64 pass loop does the rest.
+            double eta = 0.5 * goal / rnorm;
+            if (eta < 1e-4) eta = 1e-4;
+            s = pcg_f32(c, eta * rnorm, cfg.max_cg_iter - total, &it, &rr);
+            if (s == JETGPU_OK)
+                k_accumulate<<<grid_for(c, N), kThreads, 0, c->stream>>>(
+                    c->x64, c->kx, N);
+        }
+        if (s != JETGPU_OK) return s;
+        total += it;
+        st->iterations = total;
+    }
+    if (st->relative_residual > cfg.tolerance) {
+        // Final check after the last pass.
+        k_residual64<<<G, kThreads, 0, c->stream>>>(
+            c->A64, c->x64, c->b64, c->r64, nullptr, nullptr, n, c->partials,
+            c->counters, c->scal, S_R64);
+        s = read_scalars(c);
+        if (s != JETGPU_OK) return s;
+        rnorm = std::sqrt(c->h_scal[S_R64]);
+        st->residual = rnorm;
+        st->relative_residual = rnorm / bnorm;
+        if (rnorm > goal)
+            return fail(c, JETGPU_NOT_CONVERGED,
+                        "tolerance not reached within the iteration cap");
+    }
+    return JETGPU_OK;
+}
+
+}  // namespace jg

@@ -1,0 +1,278 @@
+// FLIP/PIC particle<->grid transfers (K13, K14).
+//
+// P2G replaces PicSolver3::transferFromParticlesToGrids
+// (src/jet/pic_solver3.cpp:118-193), a serial scatter in the reference, and
+// FlipSolver3's float snapshot (src/jet/flip_solver3.cpp:27-48). G2P replaces
+// FlipSolver3::transferFromGridsToParticles (flip_solver3.cpp:50-99) and
+// PicSolver3::transferFromGridsToParticles (pic_solver3.cpp:195-204).
+//
+// Stencil coordinates and trilinear weights replay
+// LinearArraySampler3::getCoordinatesAndWeights
+// (include/jet/detail/array_samplers3-inl.h:151-193) in double precision
+// without multiply-add contraction (this unit is built with -fmad=false), so
+// every particle's eight indices and weights are the reference's. The
+// scatter accumulates with FP64 atomics, so sums match the reference's
+// serial order to rounding, not bit for bit.
+
+#include "ctx.h"
+
+namespace jg {
+namespace {
+
+template <typename T>
+__device__ __forceinline__ void bary(T x, int iHigh, int* i, T* f) {
+    T s = floor(x);
+    if (iHigh == 0) {
+        *i = 0;
+        *f = (T)0;
+    } else if (s < (T)0) {
+        *i = 0;
+        *f = (T)0;
+    } else if (s > (T)(iHigh - 1)) {
+        *i = iHigh - 1;
+        *f = (T)1;
+    } else {
+        *i = (int)s;
+        *f = x - s;
+    }
+}
+
+template <typename T>
+__device__ __forceinline__ T lerp_t(T a, T b, T f) {
+    return ((T)1 - f) * a + f * b;
+}
+
+// Trilinear sample of a face array with the reference's operator() rule
+// (normalised coordinate = (x - origin) / spacing).
+template <typename V, typename T>
+__device__ T sample_face(const V* __restrict__ d, Dims s, T nx, T ny, T nz) {
+    int i, j, k;
+    T fx, fy, fz;
+    bary<T>(nx, s.x - 1, &i, &fx);
+    bary<T>(ny, s.y - 1, &j, &fy);
+    bary<T>(nz, s.z - 1, &k, &fz);
+    const int ip1 = min(i + 1, s.x - 1), jp1 = min(j + 1, s.y - 1),
+              kp1 = min(k + 1, s.z - 1);
+    const T f000 = d[lin(i, j, k, s.x, s.y)], f100 = d[lin(ip1, j, k, s.x, s.y)];
+    const T f010 = d[lin(i, jp1, k, s.x, s.y)], f110 = d[lin(ip1, jp1, k, s.x, s.y)];
+    const T f001 = d[lin(i, j, kp1, s.x, s.y)], f101 = d[lin(ip1, j, kp1, s.x, s.y)];
+    const T f011 = d[lin(i, jp1, kp1, s.x, s.y)], f111 = d[lin(ip1, jp1, kp1, s.x, s.y)];
+    const T b0 = lerp_t(lerp_t(f000, f100, fx), lerp_t(f010, f110, fx), fy);
+    const T b1 = lerp_t(lerp_t(f001, f101, fx), lerp_t(f011, f111, fx), fy);
+    return lerp_t(b0, b1, fz);
+}
+
+struct FaceSet {
+    Dims s[3];
+    double o[3][3];
+};
+
+FaceSet face_set(const GridDesc& g) {
+    FaceSet f;
+    const int nx = g.res[0], ny = g.res[1], nz = g.res[2];
+    f.s[0] = Dims{nx + 1, ny, nz};
+    f.s[1] = Dims{nx, ny + 1, nz};
+    f.s[2] = Dims{nx, ny, nz + 1};
+    for (int a = 0; a < 3; ++a)
+        for (int d = 0; d < 3; ++d)
+            f.o[a][d] = g.origin[d] + 0.5 * (a == d ? 0.0 : g.spacing[d]);
+    return f;
+}
+
+// K13a: scatter vel*w and w with FP64 atomics; markers set to 1.
+__global__ void k_p2g_scatter(long np, const double* __restrict__ pos,
+                              const double* __restrict__ vel, FaceSet fs,
+                              double ihx, double ihy, double ihz, double* u,
+                              double* v, double* w, double* wu, double* wv,
+                              double* ww, unsigned char* mu, unsigned char* mv,
+                              unsigned char* mw) {
+    double* grid[3] = {u, v, w};
+    double* wsum[3] = {wu, wv, ww};
+    unsigned char* mark[3] = {mu, mv, mw};
+    for (long p = blockIdx.x * (long)blockDim.x + threadIdx.x; p < np;
+         p += (long)gridDim.x * blockDim.x) {
+        const double px = pos[3 * p], py = pos[3 * p + 1], pz = pos[3 * p + 2];
+        for (int a = 0; a < 3; ++a) {
+            const Dims s = fs.s[a];
+            const double nx = (px - fs.o[a][0]) * ihx;
+            const double ny = (py - fs.o[a][1]) * ihy;
+            const double nz = (pz - fs.o[a][2]) * ihz;
+            int i, j, k;
+            double fx, fy, fz;
+            bary<double>(nx, s.x - 1, &i, &fx);
+            bary<double>(ny, s.y - 1, &j, &fy);
+            bary<double>(nz, s.z - 1, &k, &fz);
+            const int ip1 = min(i + 1, s.x - 1), jp1 = min(j + 1, s.y - 1),
+                      kp1 = min(k + 1, s.z - 1);
+            const long idx[8] = {lin(i, j, k, s.x, s.y),     lin(ip1, j, k, s.x, s.y),
+                                 lin(i, jp1, k, s.x, s.y),   lin(ip1, jp1, k, s.x, s.y),
+                                 lin(i, j, kp1, s.x, s.y),   lin(ip1, j, kp1, s.x, s.y),
+                                 lin(i, jp1, kp1, s.x, s.y), lin(ip1, jp1, kp1, s.x, s.y)};
+            const double wt[8] = {(1 - fx) * (1 - fy) * (1 - fz), fx * (1 - fy) * (1 - fz),
+                                  (1 - fx) * fy * (1 - fz),       fx * fy * (1 - fz),
+                                  (1 - fx) * (1 - fy) * fz,       fx * (1 - fy) * fz,
+                                  (1 - fx) * fy * fz,             fx * fy * fz};
+            const double va = vel[3 * p + a];
+            for (int q = 0; q < 8; ++q) {
+                atomicAdd(&grid[a][idx[q]], va * wt[q]);
+                atomicAdd(&wsum[a][idx[q]], wt[q]);
+                if (mark[a]) mark[a][idx[q]] = 1;
+            }
+        }
+    }
+}
+
+// K13b: divide by the weight sum where positive; float snapshot.
+__global__ void k_p2g_normalize(double* __restrict__ g,
+                                const double* __restrict__ wsum,
+                                float* __restrict__ snap, long n) {
+    for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < n;
+         c += (long)gridDim.x * blockDim.x) {
+        double v = g[c];
+        const double ws = wsum[c];
+        if (ws > 0.0) v /= ws;
+        g[c] = v;
+        if (snap) snap[c] = (float)v;
+    }
+}
+
+// K14a: snap = float(new) - snap (flip_solver3.cpp:57-70).
+__global__ void k_flip_delta(const double* __restrict__ g,
+                             float* __restrict__ snap, long n) {
+    for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < n;
+         c += (long)gridDim.x * blockDim.x)
+        snap[c] = (float)g[c] - snap[c];
+}
+
+// K14b: v_p += float trilinear(delta) at the float position; optional PIC
+// blend toward the double sample of the new grid.
+__global__ void k_g2p_flip(long np, const double* __restrict__ pos,
+                           double* __restrict__ vel, FaceSet fs, float hfx,
+                           float hfy, float hfz, const float* __restrict__ du,
+                           const float* __restrict__ dv,
+                           const float* __restrict__ dw,
+                           const double* __restrict__ u,
+                           const double* __restrict__ v,
+                           const double* __restrict__ w, double hx, double hy,
+                           double hz, double blend) {
+    const float* dl[3] = {du, dv, dw};
+    const double* g[3] = {u, v, w};
+    for (long p = blockIdx.x * (long)blockDim.x + threadIdx.x; p < np;
+         p += (long)gridDim.x * blockDim.x) {
+        const double px = pos[3 * p], py = pos[3 * p + 1], pz = pos[3 * p + 2];
+        const float xf = (float)px, yf = (float)py, zf = (float)pz;
+        double out[3];
+        for (int a = 0; a < 3; ++a) {
+            const float nx = (xf - (float)fs.o[a][0]) / hfx;
+            const float ny = (yf - (float)fs.o[a][1]) / hfy;
+            const float nz = (zf - (float)fs.o[a][2]) / hfz;
+            const double d = (double)sample_face<float, float>(dl[a], fs.s[a],
+                                                               nx, ny, nz);
+            out[a] = vel[3 * p + a] + d;
+        }
+        if (blend > 0.0) {
+            double pic[3];
+            for (int a = 0; a < 3; ++a)
+                pic[a] = sample_face<double, double>(
+                    g[a], fs.s[a], (px - fs.o[a][0]) / hx,
+                    (py - fs.o[a][1]) / hy, (pz - fs.o[a][2]) / hz);
+            for (int a = 0; a < 3; ++a)
+                out[a] = (1 - blend) * out[a] + blend * pic[a];
+        }
+        vel[3 * p] = out[0];
+        vel[3 * p + 1] = out[1];
+        vel[3 * p + 2] = out[2];
+    }
+}
+
+// K14c: v_p = sample(new grid) (PIC).
+__global__ void k_g2p_pic(long np, const double* __restrict__ pos,
+                          double* __restrict__ vel, FaceSet fs,
+                          const double* __restrict__ u,
+                          const double* __restrict__ v,
+                          const double* __restrict__ w, double hx, double hy,
+                          double hz) {
+    const double* g[3] = {u, v, w};
+    for (long p = blockIdx.x * (long)blockDim.x + threadIdx.x; p < np;
+         p += (long)gridDim.x * blockDim.x) {
+        const double px = pos[3 * p], py = pos[3 * p + 1], pz = pos[3 * p + 2];
+        for (int a = 0; a < 3; ++a)
+            vel[3 * p + a] = sample_face<double, double>(
+                g[a], fs.s[a], (px - fs.o[a][0]) / hx, (py - fs.o[a][1]) / hy,
+                (pz - fs.o[a][2]) / hz);
+    }
+}
+
+}  // namespace
+
+jetgpu_status p2g(Ctx* c, const GridDesc& g, long np, const double* pos,
+                  const double* vel, double* u, double* v, double* w,
+                  unsigned char* mu, unsigned char* mv, unsigned char* mw,
+                  float* su, float* sv, float* sw) {
+    const FaceSet fs = face_set(g);
+    const long n[3] = {fs.s[0].count(), fs.s[1].count(), fs.s[2].count()};
+    const size_t need = (size_t)(n[0] + n[1] + n[2]) * sizeof(double);
+    if (need > c->pscratch_bytes) {
+        if (c->pscratch) cudaFree(c->pscratch);
+        c->pscratch = nullptr;
+        c->pscratch_bytes = 0;
+        JG_CUDA(c, cudaMalloc((void**)&c->pscratch, need));
+        c->pscratch_bytes = need;
+    }
+    double* wsum = reinterpret_cast<double*>(c->pscratch);
+    double* grid[3] = {u, v, w};
+    unsigned char* mark[3] = {mu, mv, mw};
+    float* snap[3] = {su, sv, sw};
+    JG_CUDA(c, cudaMemsetAsync(wsum, 0, need, c->stream));
+    for (int a = 0; a < 3; ++a) {
+        JG_CUDA(c, cudaMemsetAsync(grid[a], 0, n[a] * sizeof(double), c->stream));
+        if (mark[a]) JG_CUDA(c, cudaMemsetAsync(mark[a], 0, n[a], c->stream));
+    }
+    if (np > 0)
+        k_p2g_scatter<<<blocks_for(np, kThreads, c->num_sms * 16), kThreads, 0,
+                        c->stream>>>(np, pos, vel, fs, 1.0 / g.spacing[0],
+                                     1.0 / g.spacing[1], 1.0 / g.spacing[2],
+                                     u, v, w, wsum, wsum + n[0],
+                                     wsum + n[0] + n[1], mu, mv, mw);
+    long off = 0;
+    for (int a = 0; a < 3; ++a) {
+        k_p2g_normalize<<<blocks_for(n[a]), kThreads, 0, c->stream>>>(
+            grid[a], wsum + off, snap[a], n[a]);
+        off += n[a];
+    }
+    JG_CUDA(c, cudaGetLastError());
+    return JETGPU_OK;
+}
+
+jetgpu_status g2p_flip(Ctx* c, const GridDesc& g, long np, const double* pos,
+                       double* vel, const double* u, const double* v,
+                       const double* w, float* su, float* sv, float* sw,
+                       double blend) {
+    const FaceSet fs = face_set(g);
+    const double* grid[3] = {u, v, w};
+    float* snap[3] = {su, sv, sw};
+    for (int a = 0; a < 3; ++a)
+        k_flip_delta<<<blocks_for(fs.s[a].count()), kThreads, 0, c->stream>>>(
+            grid[a], snap[a], fs.s[a].count());
+    if (np > 0)
+        k_g2p_flip<<<blocks_for(np), kThreads, 0, c->stream>>>(
+            np, pos, vel, fs, (float)g.spacing[0], (float)g.spacing[1],
+            (float)g.spacing[2], su, sv, sw, u, v, w, g.spacing[0],
+            g.spacing[1], g.spacing[2], blend);
+    JG_CUDA(c, cudaGetLastError());
+    return JETGPU_OK;
+}
+
+jetgpu_status g2p_pic(Ctx* c, const GridDesc& g, long np, const double* pos,
+                      double* vel, const double* u, const double* v,
+                      const double* w) {
+    const FaceSet fs = face_set(g);
+    if (np > 0)
+        k_g2p_pic<<<blocks_for(np), kThreads, 0, c->stream>>>(
+            np, pos, vel, fs, u, v, w, g.spacing[0], g.spacing[1],
+            g.spacing[2]);
+    JG_CUDA(c, cudaGetLastError());
+    return JETGPU_OK;
+}
+
+}  // namespace jg

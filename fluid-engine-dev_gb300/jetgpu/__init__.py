@@ -1,0 +1,530 @@
+"""jetgpu — GB300-native pressure projection for the Jet fluid engine.
+
+Host-side mirror of the reference's plug-in interface for this path, over the
+C ABI of ``libjetgpu.so`` (``include/jetgpu.h``):
+
+* :class:`GridFractionalSinglePhasePressureSolver3` — the drop-in
+  ``GridPressureSolver3`` (include/jet/grid_pressure_solver3.h:29-75,
+  include/jet/grid_fractional_single_phase_pressure_solver3.h:46-129):
+  ``solve(input, dt, output, boundarySdf, boundaryVelocity, fluidSdf,
+  useCompressed)``, ``pressure()``, ``linearSystemSolver``,
+  ``suggestedBoundaryConditionSolver()``.
+* :class:`FdmMgpcgSolver3` — the multigrid-preconditioned CG linear solver
+  (include/jet/fdm_mgpcg_solver3.h:35-56) with ``solve(system)``,
+  ``lastNumberOfIterations()``, ``lastResidual()``.
+* :func:`transfer_from_particles_to_grids`,
+  :func:`flip_transfer_from_grids_to_particles`,
+  :func:`pic_transfer_from_grids_to_particles` — the FLIP/PIC transfers.
+
+Every compute call runs the CUDA kernels of libjetgpu. There is no CPU
+fallback: importing this package without the built library raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+from dataclasses import dataclass, field as dc_field
+
+import numpy as np
+
+from . import _build
+
+LIB_PATH = _build.LIB
+
+# ---------------------------------------------------------------------------
+# C structures (include/jetgpu.h)
+
+
+class Config(C.Structure):
+    _fields_ = [
+        ("device", C.c_int),
+        ("max_cg_iter", C.c_uint),
+        ("max_levels", C.c_uint),
+        ("restrict_iter", C.c_uint),
+        ("correct_iter", C.c_uint),
+        ("coarsest_iter", C.c_uint),
+        ("final_iter", C.c_uint),
+        ("tolerance", C.c_double),
+        ("sor", C.c_double),
+        ("red_black", C.c_int),
+        ("precision", C.c_int),
+        ("preconditioner", C.c_int),
+        ("max_refinements", C.c_uint),
+    ]
+
+
+class ScalarField(C.Structure):
+    _fields_ = [
+        ("kind", C.c_int),
+        ("value", C.c_double),
+        ("data", C.c_void_p),
+        ("res", C.c_int * 3),
+        ("origin", C.c_double * 3),
+        ("spacing", C.c_double * 3),
+    ]
+
+
+class Grid(C.Structure):
+    _fields_ = [
+        ("res", C.c_int * 3),
+        ("spacing", C.c_double * 3),
+        ("origin", C.c_double * 3),
+    ]
+
+
+class SolveStats(C.Structure):
+    _fields_ = [
+        ("iterations", C.c_uint),
+        ("refinements", C.c_uint),
+        ("levels", C.c_uint),
+        ("residual", C.c_double),
+        ("relative_residual", C.c_double),
+        ("b_norm", C.c_double),
+        ("setup_ms", C.c_double),
+        ("solve_ms", C.c_double),
+        ("total_ms", C.c_double),
+        ("fallback_used", C.c_int),
+    ]
+
+    def as_dict(self) -> dict:
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+STATUS = {0: "OK", 1: "NOT_CONVERGED", 2: "STALLED_FALLBACK_USED",
+          3: "BAD_INPUT", 4: "CUDA_ERROR", 5: "OUT_OF_MEMORY",
+          6: "NUMERICAL_ERROR"}
+PRECISION = {"fp32": 0, "fp64": 1, "mixed": 2, "bf16": 2}
+
+# Symbols include/jetgpu.h declares (checked by the CPU test suite).
+EXPORTS = (
+    "jetgpu_config_default", "jetgpu_create", "jetgpu_destroy",
+    "jetgpu_last_error", "jetgpu_set_config", "jetgpu_solve_pressure",
+    "jetgpu_solve_pressure_device", "jetgpu_mgpcg_solve_system",
+    "jetgpu_p2g_device", "jetgpu_g2p_flip_device", "jetgpu_g2p_pic_device",
+    "jetgpu_p2g", "jetgpu_g2p_flip", "jetgpu_g2p_pic", "jetgpu_get_level",
+    "jetgpu_version",
+)
+
+
+class JetGpuError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{STATUS.get(status, status)}: {message}")
+        self.status = status
+
+
+_lib = None
+
+
+def library() -> C.CDLL:
+    """Loads libjetgpu.so (built by ``__graft_entry__.build()``)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(
+            f"{LIB_PATH} is not built; run __graft_entry__.build() "
+            "(the CUDA library is required, there is no CPU path)")
+    L = C.CDLL(LIB_PATH)
+    vp, dp, fp, up = C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p
+    L.jetgpu_config_default.argtypes = [C.POINTER(Config)]
+    L.jetgpu_config_default.restype = None
+    L.jetgpu_create.argtypes = [C.POINTER(Config), C.POINTER(C.c_void_p)]
+    L.jetgpu_create.restype = C.c_int
+    L.jetgpu_destroy.argtypes = [vp]
+    L.jetgpu_destroy.restype = None
+    L.jetgpu_last_error.argtypes = [vp]
+    L.jetgpu_last_error.restype = C.c_char_p
+    L.jetgpu_set_config.argtypes = [vp, C.POINTER(Config)]
+    L.jetgpu_set_config.restype = C.c_int
+    solve_args = [vp, C.POINTER(Grid), dp, dp, dp, C.POINTER(ScalarField),
+                  C.POINTER(ScalarField), dp, dp, dp, dp, dp, dp, dp,
+                  C.POINTER(SolveStats)]
+    L.jetgpu_solve_pressure.argtypes = solve_args
+    L.jetgpu_solve_pressure.restype = C.c_int
+    L.jetgpu_solve_pressure_device.argtypes = solve_args
+    L.jetgpu_solve_pressure_device.restype = C.c_int
+    L.jetgpu_mgpcg_solve_system.argtypes = [vp, C.POINTER(C.c_int), C.c_int,
+                                            dp, dp, dp, C.POINTER(SolveStats)]
+    L.jetgpu_mgpcg_solve_system.restype = C.c_int
+    p2g_args = [vp, C.POINTER(Grid), C.c_long, dp, dp, dp, dp, dp, up, up, up,
+                fp, fp, fp]
+    L.jetgpu_p2g.argtypes = p2g_args
+    L.jetgpu_p2g.restype = C.c_int
+    L.jetgpu_p2g_device.argtypes = p2g_args
+    L.jetgpu_p2g_device.restype = C.c_int
+    flip_args = [vp, C.POINTER(Grid), C.c_long, dp, dp, dp, dp, dp, fp, fp, fp,
+                 C.c_double]
+    L.jetgpu_g2p_flip.argtypes = flip_args
+    L.jetgpu_g2p_flip.restype = C.c_int
+    L.jetgpu_g2p_flip_device.argtypes = flip_args
+    L.jetgpu_g2p_flip_device.restype = C.c_int
+    pic_args = [vp, C.POINTER(Grid), C.c_long, dp, dp, dp, dp, dp]
+    L.jetgpu_g2p_pic.argtypes = pic_args
+    L.jetgpu_g2p_pic.restype = C.c_int
+    L.jetgpu_g2p_pic_device.argtypes = pic_args
+    L.jetgpu_g2p_pic_device.restype = C.c_int
+    L.jetgpu_get_level.argtypes = [vp, C.c_int, C.c_int, vp, C.c_size_t,
+                                   C.POINTER(C.c_size_t)]
+    L.jetgpu_get_level.restype = C.c_int
+    L.jetgpu_version.argtypes = []
+    L.jetgpu_version.restype = C.c_char_p
+    _lib = L
+    return L
+
+
+def _p(a) -> int | None:
+    """Address of a numpy array or torch tensor (None passes NULL)."""
+    if a is None:
+        return None
+    if isinstance(a, np.ndarray):
+        return a.ctypes.data
+    return a.data_ptr()
+
+
+# ---------------------------------------------------------------------------
+# Host-side field types (mirroring the reference's argument types)
+
+
+@dataclass
+class FaceCenteredGrid3:
+    """MAC velocity grid (src/jet/face_centered_grid3.cpp): numpy arrays
+    u (nz,ny,nx+1), v (nz,ny+1,nx), w (nz+1,ny,nx), float64, i-fastest."""
+    resolution: tuple
+    gridSpacing: tuple = (1.0, 1.0, 1.0)
+    origin: tuple = (0.0, 0.0, 0.0)
+    u: np.ndarray = None
+    v: np.ndarray = None
+    w: np.ndarray = None
+
+    def __post_init__(self):
+        nx, ny, nz = self.resolution
+        if np.isscalar(self.gridSpacing):
+            self.gridSpacing = (float(self.gridSpacing),) * 3
+        if self.u is None:
+            self.u = np.zeros((nz, ny, nx + 1))
+        if self.v is None:
+            self.v = np.zeros((nz, ny + 1, nx))
+        if self.w is None:
+            self.w = np.zeros((nz + 1, ny, nx))
+
+    def clone(self) -> "FaceCenteredGrid3":
+        return FaceCenteredGrid3(self.resolution, self.gridSpacing,
+                                 self.origin, self.u.copy(), self.v.copy(),
+                                 self.w.copy())
+
+    def c_grid(self) -> Grid:
+        g = Grid()
+        g.res[:] = tuple(int(r) for r in self.resolution)
+        g.spacing[:] = tuple(float(h) for h in self.gridSpacing)
+        g.origin[:] = tuple(float(o) for o in self.origin)
+        return g
+
+
+@dataclass
+class ConstantScalarField3:
+    value: float
+
+
+@dataclass
+class CellCenteredScalarGrid3:
+    """Cell-centred scalar grid: data (nz,ny,nx) sampled trilinearly with the
+    data origin at origin + h/2."""
+    resolution: tuple
+    gridSpacing: tuple
+    origin: tuple
+    data: np.ndarray
+
+    def dataOrigin(self):
+        return tuple(o + 0.5 * h for o, h in zip(self.origin, self.gridSpacing))
+
+
+kMaxD = float(np.finfo(np.float64).max)
+
+
+def _field(f, keep: list) -> ScalarField:
+    s = ScalarField()
+    if f is None:
+        raise ValueError("field required")
+    if np.isscalar(f):
+        f = ConstantScalarField3(float(f))
+    if isinstance(f, ConstantScalarField3):
+        s.kind = 0
+        s.value = float(f.value)
+        return s
+    if isinstance(f, CellCenteredScalarGrid3):
+        data = f.data
+        if isinstance(data, np.ndarray):
+            data = np.ascontiguousarray(data, np.float64)
+        keep.append(data)
+        s.kind = 1
+        s.data = _p(data)
+        nz, ny, nx = data.shape
+        s.res[:] = (nx, ny, nz)
+        s.origin[:] = f.dataOrigin()
+        s.spacing[:] = tuple(float(h) for h in f.gridSpacing)
+        return s
+    raise TypeError(f"unsupported field type {type(f).__name__}")
+
+
+# ---------------------------------------------------------------------------
+# Solvers
+
+
+class FdmMgpcgSolver3:
+    """GPU multigrid-preconditioned CG with the reference constructor's
+    arguments (fdm_mgpcg_solver3.h:35-41). ``maxTolerance`` is the relative
+    true residual ||b - Ax|| / ||b|| the solve reaches."""
+
+    def __init__(self, numberOfCgIter=100, maxNumberOfLevels=5,
+                 numberOfRestrictionIter=2, numberOfCorrectionIter=2,
+                 numberOfCoarsestIter=10, numberOfFinalIter=2,
+                 maxTolerance=1e-6, sorFactor=1.0, useRedBlackOrdering=True,
+                 precision="fp32", device=0, maxRefinements=6):
+        if not useRedBlackOrdering:
+            raise ValueError("the GPU smoother is red-black; the lexicographic "
+                             "Gauss-Seidel sweep is serial by construction")
+        self.config = Config()
+        library().jetgpu_config_default(C.byref(self.config))
+        cfg = self.config
+        cfg.device = device
+        cfg.max_cg_iter = numberOfCgIter
+        cfg.max_levels = maxNumberOfLevels
+        cfg.restrict_iter = numberOfRestrictionIter
+        cfg.correct_iter = numberOfCorrectionIter
+        cfg.coarsest_iter = numberOfCoarsestIter
+        cfg.final_iter = numberOfFinalIter
+        cfg.tolerance = maxTolerance
+        cfg.sor = sorFactor
+        cfg.red_black = 1
+        cfg.precision = PRECISION[precision]
+        cfg.max_refinements = maxRefinements
+        self._ctx = None
+        self.last_stats = SolveStats()
+
+    # -- context ------------------------------------------------------------
+    def context(self) -> C.c_void_p:
+        if self._ctx is None:
+            h = C.c_void_p()
+            st = library().jetgpu_create(C.byref(self.config), C.byref(h))
+            if st != 0:
+                raise JetGpuError(st, "jetgpu_create failed")
+            self._ctx = h
+        return self._ctx
+
+    def close(self):
+        if self._ctx is not None:
+            library().jetgpu_destroy(self._ctx)
+            self._ctx = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def check(self, status: int, allow=(0,)) -> int:
+        if status not in allow:
+            msg = library().jetgpu_last_error(self._ctx)
+            raise JetGpuError(status, msg.decode() if msg else "")
+        return status
+
+    # -- reference accessors ------------------------------------------------
+    def maxNumberOfIterations(self) -> int:
+        return self.config.max_cg_iter
+
+    def lastNumberOfIterations(self) -> int:
+        return self.last_stats.iterations
+
+    def tolerance(self) -> float:
+        return self.config.tolerance
+
+    def lastResidual(self) -> float:
+        return self.last_stats.relative_residual
+
+    def solve(self, system) -> bool:
+        """FdmMgpcgSolver3::solve(FdmMgLinearSystem3*): ``system`` has
+        ``A`` (list of (nz,ny,nx,4) float64 rows per level, finest first),
+        ``b`` (list; level 0 is read) and ``x`` (list; level 0 written)."""
+        A0 = system.A[0]
+        res0 = (C.c_int * 3)(A0.shape[2], A0.shape[1], A0.shape[0])
+        A = np.ascontiguousarray(np.concatenate([a.reshape(-1) for a in system.A]))
+        b = np.ascontiguousarray(system.b[0], np.float64)
+        x = np.zeros(A0.shape[:3])
+        st = library().jetgpu_mgpcg_solve_system(
+            self.context(), res0, len(system.A), _p(A), _p(b), _p(x),
+            C.byref(self.last_stats))
+        self.check(st, allow=(0, 1))
+        system.x[0][...] = x
+        return st == 0
+
+
+@dataclass
+class FdmMgLinearSystem3:
+    A: list = dc_field(default_factory=list)
+    x: list = dc_field(default_factory=list)
+    b: list = dc_field(default_factory=list)
+
+
+class GridFractionalSinglePhasePressureSolver3:
+    """Drop-in GPU GridPressureSolver3 (grid_pressure_solver3.h:58-64)."""
+
+    def __init__(self, linearSystemSolver: FdmMgpcgSolver3 | None = None):
+        self._solver = linearSystemSolver or FdmMgpcgSolver3()
+        self._pressure = None
+        self.last_stats = SolveStats()
+
+    @property
+    def linearSystemSolver(self) -> FdmMgpcgSolver3:
+        return self._solver
+
+    @linearSystemSolver.setter
+    def linearSystemSolver(self, s: FdmMgpcgSolver3):
+        if not isinstance(s, FdmMgpcgSolver3):
+            raise TypeError("the GPU pressure solver takes an FdmMgpcgSolver3")
+        self._solver = s
+
+    def setLinearSystemSolver(self, s: FdmMgpcgSolver3):
+        self.linearSystemSolver = s
+
+    @staticmethod
+    def suggestedBoundaryConditionSolver() -> str:
+        # grid_fractional_single_phase_pressure_solver3.cpp:486-490
+        return "GridFractionalBoundaryConditionSolver3"
+
+    def pressure(self) -> np.ndarray:
+        return self._pressure
+
+    def solve(self, input: FaceCenteredGrid3, timeIntervalInSeconds: float,
+              output: FaceCenteredGrid3,
+              boundarySdf=ConstantScalarField3(kMaxD),
+              boundaryVelocity=None,
+              fluidSdf=ConstantScalarField3(-kMaxD),
+              useCompressed: bool = False) -> int:
+        """Projects ``input`` into ``output`` (host arrays). boundaryVelocity
+        is None (static collider) or a tuple of per-face normal components
+        (solid_u, solid_v, solid_w). ``useCompressed`` selects the
+        reference's CSR storage; the GPU system is matrix-row based either
+        way, so it has no effect. Returns the C status (0 or NOT_CONVERGED)."""
+        del timeIntervalInSeconds, useCompressed  # unused, as in the reference
+        keep = []
+        bs = _field(boundarySdf, keep)
+        fs = _field(fluidSdf, keep)
+        g = input.c_grid()
+        u = np.ascontiguousarray(input.u, np.float64)
+        v = np.ascontiguousarray(input.v, np.float64)
+        w = np.ascontiguousarray(input.w, np.float64)
+        su = sv = sw = None
+        if boundaryVelocity is not None:
+            su, sv, sw = (None if a is None else np.ascontiguousarray(a, np.float64)
+                          for a in boundaryVelocity)
+        for a, ref in ((output.u, u), (output.v, v), (output.w, w)):
+            if a.shape != ref.shape or a.dtype != np.float64 or not a.flags.c_contiguous:
+                raise ValueError("output arrays must match the input layout")
+        nx, ny, nz = input.resolution
+        p = np.zeros((nz, ny, nx))
+        solver = self._solver
+        st = library().jetgpu_solve_pressure(
+            solver.context(), C.byref(g), _p(u), _p(v), _p(w), C.byref(bs),
+            C.byref(fs), _p(su), _p(sv), _p(sw), _p(output.u), _p(output.v),
+            _p(output.w), _p(p), C.byref(self.last_stats))
+        solver.last_stats = self.last_stats
+        solver.check(st, allow=(0, 1))
+        self._pressure = p
+        return st
+
+    def level(self, level: int, what: str) -> np.ndarray:
+        """Internal weights/system of the last solve (for parity checks)."""
+        solver = self._solver
+        code = {"fluid": 0, "uw": 1, "vw": 2, "ww": 3, "A": 4, "b": 5}[what]
+        cnt = C.c_size_t(0)
+        L = library()
+        # Query size first with a zero-capacity call.
+        dummy = np.zeros(1, np.float64)
+        L.jetgpu_get_level(solver.context(), level, code, _p(dummy), 0,
+                           C.byref(cnt))
+        n = cnt.value
+        if what in ("fluid", "uw", "vw", "ww"):
+            out = np.zeros(n, np.float32)
+        elif what == "A":
+            out = np.zeros(n * 4, np.float64)
+        else:
+            out = np.zeros(n, np.float64)
+        st = L.jetgpu_get_level(solver.context(), level, code, _p(out),
+                                out.nbytes, C.byref(cnt))
+        solver.check(st)
+        return out
+
+
+def solve_pressure_device(solver: FdmMgpcgSolver3, grid: Grid, u, v, w,
+                          boundary: ScalarField, fluid: ScalarField,
+                          out_u, out_v, out_w, out_p=None, solid=(None, None, None),
+                          stats: SolveStats | None = None) -> int:
+    """Device-pointer form (torch CUDA float64 tensors)."""
+    stats = stats if stats is not None else SolveStats()
+    st = library().jetgpu_solve_pressure_device(
+        solver.context(), C.byref(grid), _p(u), _p(v), _p(w), C.byref(boundary),
+        C.byref(fluid), _p(solid[0]), _p(solid[1]), _p(solid[2]), _p(out_u),
+        _p(out_v), _p(out_w), _p(out_p), C.byref(stats))
+    solver.last_stats = stats
+    return solver.check(st, allow=(0, 1))
+
+
+# ---------------------------------------------------------------------------
+# Particle transfers (host arrays)
+
+
+def transfer_from_particles_to_grids(solver: FdmMgpcgSolver3,
+                                     grid: FaceCenteredGrid3, positions,
+                                     velocities, markers=True, snapshot=True):
+    """PicSolver3::transferFromParticlesToGrids (+ FLIP snapshot).
+    Fills grid.u/v/w; returns (markers, snapshots) lists."""
+    pos = np.ascontiguousarray(positions, np.float64)
+    vel = np.ascontiguousarray(velocities, np.float64)
+    shapes = [grid.u.shape, grid.v.shape, grid.w.shape]
+    marks = [np.zeros(s, np.uint8) for s in shapes] if markers else [None] * 3
+    snaps = [np.zeros(s, np.float32) for s in shapes] if snapshot else [None] * 3
+    g = grid.c_grid()
+    st = library().jetgpu_p2g(solver.context(), C.byref(g), pos.shape[0],
+                              _p(pos), _p(vel), _p(grid.u), _p(grid.v),
+                              _p(grid.w), *[_p(m) for m in marks],
+                              *[_p(s) for s in snaps])
+    solver.check(st)
+    return marks, snaps
+
+
+def flip_transfer_from_grids_to_particles(solver: FdmMgpcgSolver3,
+                                          grid: FaceCenteredGrid3, positions,
+                                          velocities, snapshots,
+                                          picBlendingFactor=0.0):
+    """FlipSolver3::transferFromGridsToParticles. Updates ``velocities`` and
+    turns ``snapshots`` into the float deltas, in place."""
+    pos = np.ascontiguousarray(positions, np.float64)
+    if not (velocities.dtype == np.float64 and velocities.flags.c_contiguous):
+        raise ValueError("velocities must be C-contiguous float64")
+    g = grid.c_grid()
+    st = library().jetgpu_g2p_flip(solver.context(), C.byref(g), pos.shape[0],
+                                   _p(pos), _p(velocities), _p(grid.u),
+                                   _p(grid.v), _p(grid.w),
+                                   *[_p(s) for s in snapshots],
+                                   float(picBlendingFactor))
+    solver.check(st)
+    return velocities
+
+
+def pic_transfer_from_grids_to_particles(solver: FdmMgpcgSolver3,
+                                         grid: FaceCenteredGrid3, positions,
+                                         velocities):
+    """PicSolver3::transferFromGridsToParticles (in place)."""
+    pos = np.ascontiguousarray(positions, np.float64)
+    if not (velocities.dtype == np.float64 and velocities.flags.c_contiguous):
+        raise ValueError("velocities must be C-contiguous float64")
+    g = grid.c_grid()
+    st = library().jetgpu_g2p_pic(solver.context(), C.byref(g), pos.shape[0],
+                                  _p(pos), _p(velocities), _p(grid.u),
+                                  _p(grid.v), _p(grid.w))
+    solver.check(st)
+    return velocities
+
+
+def version() -> str:
+    return library().jetgpu_version().decode()

@@ -1,0 +1,249 @@
+/*
+ * jetgpu — GB300-native pressure projection for the Jet fluid engine.
+ *
+ * C ABI of libjetgpu.so. Plain C types only: no C++ types, no exceptions, no
+ * torch types cross this boundary. Every function returns a jetgpu_status;
+ * jetgpu_last_error() gives the message of the last failure on a context.
+ *
+ * Array conventions follow Jet: 3-D arrays are i-fastest,
+ * index = i + nx*(j + ny*k) (include/jet/detail/array_accessor3-inl.h:197-200).
+ * A face-centred velocity grid of resolution (nx,ny,nz) stores
+ * u:(nx+1,ny,nz), v:(nx,ny+1,nz), w:(nx,ny,nz+1) doubles whose data origins
+ * are origin + h/2 on the two tangential axes
+ * (src/jet/face_centered_grid3.cpp:428-445).
+ *
+ * Threading: one context per solver instance, used by one host thread at a
+ * time. Each context owns one CUDA stream and its device buffers; buffers are
+ * reallocated only when the resolution changes. Every call is synchronous on
+ * return, as the reference's solvers are.
+ */
+#ifndef JETGPU_H_
+#define JETGPU_H_
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum jetgpu_status {
+    JETGPU_OK = 0,
+    /* The iteration cap was reached before the tolerance. The outputs hold
+     * the last iterate, as the reference's FdmMgpcgSolver3 does
+     * (src/jet/fdm_mgpcg_solver3.cpp:54-80). */
+    JETGPU_NOT_CONVERGED = 1,
+    /* The flexible-PCG iteration with the learned preconditioner stalled and
+     * the solve finished with the plain multigrid preconditioner. */
+    JETGPU_STALLED_FALLBACK_USED = 2,
+    JETGPU_BAD_INPUT = 3,
+    JETGPU_CUDA_ERROR = 4,
+    JETGPU_OUT_OF_MEMORY = 5,
+    /* A NaN or Inf appeared in a reduction (input or breakdown). */
+    JETGPU_NUMERICAL_ERROR = 6
+} jetgpu_status;
+
+/* Arithmetic of the Krylov iteration. In every mode the global r.z and p.Ap
+ * reductions and the final true-residual check are FP64, and the true
+ * residual is taken against the FP64 operator the reference builds. */
+typedef enum jetgpu_precision {
+    /* FP32 Krylov vectors and FP32 V-cycle; FP64 iterative refinement
+     * accumulates the solution and checks the true residual. */
+    JETGPU_PRECISION_FP32 = 0,
+    /* FP64 Krylov vectors and operator; FP32 V-cycle. */
+    JETGPU_PRECISION_FP64 = 1,
+    /* As FP32, with BF16 storage of the V-cycle's vectors and coefficients. */
+    JETGPU_PRECISION_MIXED_BF16 = 2
+} jetgpu_precision;
+
+typedef enum jetgpu_preconditioner {
+    JETGPU_PRECOND_MULTIGRID = 0,
+    /* Learned U-Net preconditioner in flexible PCG, with the multigrid
+     * preconditioner as fallback when iterations stall. Requires weights
+     * loaded with jetgpu_load_unet(). */
+    JETGPU_PRECOND_LEARNED = 1
+} jetgpu_preconditioner;
+
+/* Solver configuration. The first nine fields mirror the FdmMgpcgSolver3
+ * constructor (include/jet/fdm_mgpcg_solver3.h:35-41):
+ * FdmMgpcgSolver3(numberOfCgIter, maxNumberOfLevels, numberOfRestrictionIter,
+ *                 numberOfCorrectionIter, numberOfCoarsestIter,
+ *                 numberOfFinalIter, maxTolerance, sorFactor,
+ *                 useRedBlackOrdering).
+ * Differences, by design: `tolerance` is the relative true residual
+ * ||b - A x||_2 / ||b||_2 (the reference stops on the absolute
+ * sqrt(r.M^-1 r), include/jet/detail/cg-inl.h:48); smoothing is always
+ * red-black (the lexicographic sweep is serial by construction); and the
+ * V-cycle is made symmetric (post-smoothing runs the colours in reverse order)
+ * with a zero initial guess, so that it is a fixed SPD preconditioner. */
+typedef struct jetgpu_config {
+    int device;                 /* CUDA device ordinal */
+    unsigned int max_cg_iter;   /* numberOfCgIter */
+    unsigned int max_levels;    /* maxNumberOfLevels */
+    unsigned int restrict_iter; /* pre-smoothing sweeps */
+    unsigned int correct_iter;  /* post-smoothing sweeps, coarse levels */
+    unsigned int coarsest_iter; /* sweeps on the coarsest level */
+    unsigned int final_iter;    /* post-smoothing sweeps, finest level */
+    double tolerance;           /* relative true residual target */
+    double sor;                 /* SOR factor of the red-black smoother */
+    int red_black;              /* must be nonzero */
+    int precision;              /* jetgpu_precision */
+    int preconditioner;         /* jetgpu_preconditioner */
+    unsigned int max_refinements; /* FP32 modes: FP64 refinement passes */
+} jetgpu_config;
+
+/* Fills `cfg` with defaults: FdmMgpcgSolver3(100, 5, 2, 2, 10, 2, 1e-6, 1.0,
+ * true), FP32, multigrid, 6 refinements, device 0. */
+void jetgpu_config_default(jetgpu_config* cfg);
+
+/* A scalar-field argument of GridPressureSolver3::solve
+ * (include/jet/grid_pressure_solver3.h:58-64): a ConstantScalarField3
+ * (kind 0) or a grid sampled with Jet's trilinear rule (kind 1), e.g. a
+ * CellCenteredScalarGrid3 whose data point (0,0,0) sits at `origin`
+ * (its dataOrigin()). */
+typedef struct jetgpu_scalar_field {
+    int kind;            /* 0 = constant, 1 = grid */
+    double value;        /* kind 0 */
+    const double* data;  /* kind 1: res[0]*res[1]*res[2] doubles */
+    int res[3];
+    double origin[3];
+    double spacing[3];
+} jetgpu_scalar_field;
+
+/* Geometry of a FaceCenteredGrid3: resolution, grid spacing, origin. */
+typedef struct jetgpu_grid {
+    int res[3];
+    double spacing[3];
+    double origin[3];
+} jetgpu_grid;
+
+typedef struct jetgpu_solve_stats {
+    unsigned int iterations;     /* Krylov iterations, all passes */
+    unsigned int refinements;    /* FP64 refinement passes (FP32 modes) */
+    unsigned int levels;         /* multigrid levels used */
+    double residual;             /* ||b - A x||_2, FP64, reference operator */
+    double relative_residual;    /* residual / ||b||_2 */
+    double b_norm;               /* ||b||_2 */
+    double setup_ms;             /* weights + system build */
+    double solve_ms;             /* Krylov solve */
+    double total_ms;             /* whole call, including copies */
+    int fallback_used;           /* learned preconditioner fell back */
+} jetgpu_solve_stats;
+
+/* Context lifetime. */
+jetgpu_status jetgpu_create(const jetgpu_config* cfg, struct jetgpu_ctx** out);
+void jetgpu_destroy(struct jetgpu_ctx* ctx);
+const char* jetgpu_last_error(const struct jetgpu_ctx* ctx);
+jetgpu_status jetgpu_set_config(struct jetgpu_ctx* ctx,
+                                const jetgpu_config* cfg);
+
+/* GridFractionalSinglePhasePressureSolver3::solve
+ * (src/jet/grid_fractional_single_phase_pressure_solver3.cpp:456-484) with
+ * an MGPCG linear solver installed: buildWeights (:520-636), buildSystem
+ * (:651-713), the multigrid-preconditioned CG solve
+ * (src/jet/fdm_mgpcg_solver3.cpp:54-80) and applyPressureGradient (:715-765).
+ *
+ * HOST pointers. u/v/w: the input velocity. boundary_sdf: collider SDF
+ * (negative inside solids). fluid_sdf: liquid SDF (negative inside liquid).
+ * solid_u/v/w: the collider velocity's normal component sampled at every
+ * u/v/w face position, or NULL for a static collider (boundaryVelocity).
+ * out_u/v/w: the projected velocity; faces the reference leaves untouched
+ * keep the input values (out may alias the input). out_pressure: the level-0
+ * pressure (GridFractionalSinglePhasePressureSolver3::pressure(), :512-518),
+ * or NULL. stats may be NULL. */
+jetgpu_status jetgpu_solve_pressure(
+    struct jetgpu_ctx* ctx, const jetgpu_grid* grid, const double* u,
+    const double* v, const double* w, const jetgpu_scalar_field* boundary_sdf,
+    const jetgpu_scalar_field* fluid_sdf, const double* solid_u,
+    const double* solid_v, const double* solid_w, double* out_u,
+    double* out_v, double* out_w, double* out_pressure,
+    jetgpu_solve_stats* stats);
+
+/* Same as jetgpu_solve_pressure with every array (including the SDF grids'
+ * data) in DEVICE memory of the context's device. For solvers that keep the
+ * simulation resident on the GPU. */
+jetgpu_status jetgpu_solve_pressure_device(
+    struct jetgpu_ctx* ctx, const jetgpu_grid* grid, const double* u,
+    const double* v, const double* w, const jetgpu_scalar_field* boundary_sdf,
+    const jetgpu_scalar_field* fluid_sdf, const double* solid_u,
+    const double* solid_v, const double* solid_w, double* out_u,
+    double* out_v, double* out_w, double* out_pressure,
+    jetgpu_solve_stats* stats);
+
+/* FdmMgpcgSolver3::solve(FdmMgLinearSystem3*)
+ * (src/jet/fdm_mgpcg_solver3.cpp:54-80) on a caller-built multigrid system.
+ * HOST pointers. Levels are concatenated finest first; level l has
+ * resolution res0 >> l. A: FdmMatrixRow3 {center,right,up,front} doubles per
+ * cell (include/jet/fdm_linear_system3.h:18-30); b: doubles per cell, only
+ * level 0 is read; x: level-0 solution out. */
+jetgpu_status jetgpu_mgpcg_solve_system(struct jetgpu_ctx* ctx,
+                                        const int res0[3], int levels,
+                                        const double* A, const double* b,
+                                        double* x, jetgpu_solve_stats* stats);
+
+/* PicSolver3::transferFromParticlesToGrids (src/jet/pic_solver3.cpp:118-193)
+ * and, when snap_* are non-NULL, FlipSolver3's float snapshot of the result
+ * (src/jet/flip_solver3.cpp:27-48). DEVICE pointers. pos/vel: AoS xyz
+ * doubles (particle_system_data3.h:114-123). u/v/w: velocity out. mu/mv/mw:
+ * face markers out (1 where a particle contributed). */
+jetgpu_status jetgpu_p2g_device(struct jetgpu_ctx* ctx,
+                                const jetgpu_grid* grid, long num_particles,
+                                const double* pos, const double* vel,
+                                double* u, double* v, double* w,
+                                unsigned char* mu, unsigned char* mv,
+                                unsigned char* mw, float* snap_u,
+                                float* snap_v, float* snap_w);
+
+/* FlipSolver3::transferFromGridsToParticles (src/jet/flip_solver3.cpp:50-99).
+ * DEVICE pointers. snap_* hold the P2G snapshot on entry and the float delta
+ * on exit; vel is updated in place. */
+jetgpu_status jetgpu_g2p_flip_device(struct jetgpu_ctx* ctx,
+                                     const jetgpu_grid* grid,
+                                     long num_particles, const double* pos,
+                                     double* vel, const double* u,
+                                     const double* v, const double* w,
+                                     float* snap_u, float* snap_v,
+                                     float* snap_w, double pic_blending);
+
+/* PicSolver3::transferFromGridsToParticles (src/jet/pic_solver3.cpp:195-204).
+ * DEVICE pointers. */
+jetgpu_status jetgpu_g2p_pic_device(struct jetgpu_ctx* ctx,
+                                    const jetgpu_grid* grid,
+                                    long num_particles, const double* pos,
+                                    double* vel, const double* u,
+                                    const double* v, const double* w);
+
+/* Host-pointer forms of the three transfers (copies inside the call). */
+jetgpu_status jetgpu_p2g(struct jetgpu_ctx* ctx, const jetgpu_grid* grid,
+                         long num_particles, const double* pos,
+                         const double* vel, double* u, double* v, double* w,
+                         unsigned char* mu, unsigned char* mv,
+                         unsigned char* mw, float* snap_u, float* snap_v,
+                         float* snap_w);
+jetgpu_status jetgpu_g2p_flip(struct jetgpu_ctx* ctx, const jetgpu_grid* grid,
+                              long num_particles, const double* pos,
+                              double* vel, const double* u, const double* v,
+                              const double* w, float* snap_u, float* snap_v,
+                              float* snap_w, double pic_blending);
+jetgpu_status jetgpu_g2p_pic(struct jetgpu_ctx* ctx, const jetgpu_grid* grid,
+                             long num_particles, const double* pos,
+                             double* vel, const double* u, const double* v,
+                             const double* w);
+
+/* Copies internal state of the last pressure solve to HOST memory, for
+ * checking against the reference's private members
+ * (grid_fractional_single_phase_pressure_solver3.h:103-115).
+ * what: 0 fluid SDF (float, cells), 1/2/3 u/v/w weights (float, faces),
+ *       4 matrix rows (4 doubles per cell; level 0 exact FP64, coarse levels
+ *       as stored in FP32 and widened), 5 rhs b (doubles, level 0 only).
+ * Returns the element count via *count. */
+jetgpu_status jetgpu_get_level(struct jetgpu_ctx* ctx, int level, int what,
+                               void* dst, size_t capacity, size_t* count);
+
+/* Library version string. */
+const char* jetgpu_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* JETGPU_H_ */

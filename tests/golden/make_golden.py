@@ -1,0 +1,202 @@
+"""Generates the golden fixtures in tests/golden/ from the Jet reference.
+
+Run in a checkout where the reference sources exist (the harness is compiled
+from them by oracle/Makefile.ref):
+
+    python tests/golden/make_golden.py
+
+Every fixture holds inputs and the reference's outputs for one small case:
+
+* kat_free_surface_3.npz — the reference's own known-answer case
+  (src/tests/unit_tests/grid_fractional_single_phase_pressure_solver3_tests.cpp:17-74),
+  solved with FdmMgpcgSolver3 installed.
+* sphere_union_16.npz — 16^3 sphere-union liquid, solid sphere, random face
+  velocities (seed 1): weights, fluid SDF and matrix of every level, rhs,
+  pressure and projected velocity.
+* noncubic_12x8x16.npz — a non-cubic anisotropic grid with a moving solid.
+* mgpcg_poisson_32.npz — the 4-level Poisson system of
+  src/tests/unit_tests/fdm_mgpcg_solver3_tests.cpp:13-60 and its solution.
+* transfer_16.npz — P2G (grids, markers, FLIP snapshot) and G2P (FLIP, FLIP
+  with PIC blending, PIC) for 3,000 particles on a 16^3 grid.
+* rng_streams.npz — the first doubles of std::mt19937(seed) +
+  std::uniform_real_distribution<double>(0,1) for seeds 0, 1, 2, produced by
+  a C++ program compiled here.
+"""
+from __future__ import annotations
+
+import os
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, REPO)
+sys.path.insert(0, os.path.join(REPO, "fluid-engine-dev_gb300"))
+sys.path.insert(0, os.path.join(REPO, "tests"))
+
+import oracle  # noqa: E402
+from jetgpu import scenes  # noqa: E402
+from make_systems import poisson_system  # noqa: E402
+
+KMAX = float(np.finfo(np.float64).max)
+
+
+def save(name, **arrays):
+    np.savez_compressed(os.path.join(HERE, name), **arrays)
+    print("wrote", name)
+
+
+def pressure_case(ref, res, h, fields, params):
+    out = ref.pressure_solve(res, h, (0, 0, 0), fields["u"], fields["v"],
+                             fields["w"], fields["boundary_sdf"],
+                             fields["fluid_sdf"], params,
+                             solid=fields.get("solid", (None, None, None)))
+    arrays = dict(out_u=out["u"], out_v=out["v"], out_w=out["w"], p=out["p"],
+                  iters=np.array(out["iters"]), resid=np.array(out["resid"]))
+    for l in range(ref.level_count()):
+        for what in ("fluid", "uw", "vw", "ww", "A"):
+            arrays[f"L{l}_{what}"] = ref.level(l, what, res)
+    arrays["L0_b"] = ref.level(0, "b", res)
+    arrays["levels"] = np.array(ref.level_count())
+    return arrays
+
+
+def params_array(p: oracle.MgParams):
+    return np.array([p.max_cg_iter, p.max_levels, p.restrict_iter,
+                     p.correct_iter, p.coarsest_iter, p.final_iter,
+                     p.tolerance, p.sor, float(p.red_black)])
+
+
+def kat_free_surface(ref):
+    n = 3
+    u = np.zeros((n, n, n + 1))
+    v = np.zeros((n, n + 1, n))
+    w = np.zeros((n + 1, n, n))
+    v[:, 1:3, :] = 1.0
+    ys = np.arange(n) + 0.5
+    fluid = np.broadcast_to((ys - 2.0)[None, :, None], (n, n, n)).copy()
+    p = oracle.MgParams(100, 5, 5, 5, 20, 20, 1e-12, 1.5, True)
+    f = dict(u=u, v=v, w=w, boundary_sdf=KMAX, fluid_sdf=fluid)
+    a = pressure_case(ref, (n, n, n), (1.0, 1.0, 1.0), f, p)
+    save("kat_free_surface_3.npz", u=u, v=v, w=w, fluid_sdf=fluid,
+         params=params_array(p), **a)
+
+
+def sphere_union(ref):
+    n = 16
+    h = 1.0 / n
+    sc = scenes.sphere_union_scene(n, seed=1)
+    p = oracle.MgParams(200, 4, 5, 5, 20, 20, 1e-10, 1.5, True)
+    a = pressure_case(ref, (n, n, n), (h, h, h), sc, p)
+    save("sphere_union_16.npz", u=sc["u"], v=sc["v"], w=sc["w"],
+         fluid_sdf=sc["fluid_sdf"], boundary_sdf=sc["boundary_sdf"],
+         params=params_array(p), **a)
+
+
+def noncubic(ref):
+    res = (12, 8, 16)
+    h = (1.0 / 12, 0.8 / 8, 1.5 / 16)
+    nx, ny, nz = res
+    rng = np.random.default_rng(7)
+    cz, cy, cx = [(np.arange(m) + 0.5) * hh for m, hh in zip((nz, ny, nx),
+                                                              (h[2], h[1], h[0]))]
+    Z, Y, X = np.meshgrid(cz, cy, cx, indexing="ij")
+    fluid = np.minimum(Y - 0.55, np.sqrt((X - .6) ** 2 + (Y - .6) ** 2 +
+                                         (Z - .7) ** 2) - 0.25)
+    solid = np.sqrt((X - 0.4) ** 2 + (Y - 0.3) ** 2 + (Z - 0.8) ** 2) - 0.2
+    u = rng.uniform(-1, 1, (nz, ny, nx + 1))
+    v = rng.uniform(-1, 1, (nz, ny + 1, nx))
+    w = rng.uniform(-1, 1, (nz + 1, ny, nx))
+    su = rng.uniform(-0.5, 0.5, u.shape)
+    sv = rng.uniform(-0.5, 0.5, v.shape)
+    sw = rng.uniform(-0.5, 0.5, w.shape)
+    p = oracle.MgParams(200, 3, 5, 5, 20, 20, 1e-10, 1.5, True)
+    f = dict(u=u, v=v, w=w, boundary_sdf=solid, fluid_sdf=fluid,
+             solid=(su, sv, sw))
+    a = pressure_case(ref, res, h, f, p)
+    save("noncubic_12x8x16.npz", u=u, v=v, w=w, fluid_sdf=fluid,
+         boundary_sdf=solid, solid_u=su, solid_v=sv, solid_w=sw,
+         spacing=np.array(h), params=params_array(p), **a)
+
+
+def mgpcg_poisson(ref):
+    A, b = poisson_system()
+    p = oracle.MgParams(50, 4, 5, 5, 10, 10, 1e-4, 1.5, False)
+    r = ref.mgpcg_system(A, b, p)
+    pt = oracle.MgParams(500, 4, 5, 5, 10, 10, 1e-11, 1.5, True)
+    rt = ref.mgpcg_system(A, b, pt)
+    out = {f"A{l}": a for l, a in enumerate(A)}
+    out.update({f"b{l}": x for l, x in enumerate(b)})
+    save("mgpcg_poisson_32.npz", x=r["x"], ok=np.array(r["ok"]),
+         iters=np.array(r["iters"]), resid=np.array(r["resid"]),
+         x_tight=rt["x"], params=params_array(p), params_tight=params_array(pt),
+         **out)
+
+
+def transfers(ref):
+    n = 16
+    h = 1.0 / n
+    rng = np.random.default_rng(3)
+    pos = rng.uniform(0.0, 1.0, (3000, 3))
+    pos[:8] = [[0, 0, 0], [1, 1, 1], [0.5, 0.5, 0.5], [1e-12, 0.3, 0.99999],
+               [1.02, -0.01, 0.5], [0.03125, 0.5, 0.5], [0.0625, 0.5, 1.0],
+               [0.999, 0.001, 0.25]]
+    vel = rng.uniform(-1.0, 1.0, (3000, 3))
+    grids, marks, snaps = ref.p2g((n, n, n), (h, h, h), (0, 0, 0), pos, vel)
+    new = [g + rng.uniform(-0.2, 0.2, g.shape) for g in grids]
+    vflip, dflip = ref.g2p_flip((n, n, n), (h, h, h), (0, 0, 0), pos, vel, new,
+                                snaps, 0.0)
+    vblend, _ = ref.g2p_flip((n, n, n), (h, h, h), (0, 0, 0), pos, vel, new,
+                             snaps, 0.25)
+    vpic = ref.g2p_pic((n, n, n), (h, h, h), (0, 0, 0), pos, vel, new)
+    save("transfer_16.npz", pos=pos, vel=vel, u=grids[0], v=grids[1],
+         w=grids[2], mu=marks[0], mv=marks[1], mw=marks[2], su=snaps[0],
+         sv=snaps[1], sw=snaps[2], new_u=new[0], new_v=new[1], new_w=new[2],
+         vel_flip=vflip, du=dflip[0], dv=dflip[1], dw=dflip[2],
+         vel_blend=vblend, vel_pic=vpic)
+
+
+RNG_CPP = r"""
+#include <cstdio>
+#include <random>
+int main() {
+  for (unsigned seed = 0; seed < 3; ++seed) {
+    std::mt19937 g(seed);
+    std::uniform_real_distribution<double> d(0.0, 1.0);
+    for (int i = 0; i < 64; ++i) std::printf("%.17g\n", d(g));
+  }
+}
+"""
+
+
+def rng_streams():
+    with tempfile.TemporaryDirectory() as td:
+        src = os.path.join(td, "rng.cpp")
+        exe = os.path.join(td, "rng")
+        with open(src, "w") as f:
+            f.write(RNG_CPP)
+        subprocess.run(["g++", "-O2", src, "-o", exe], check=True)
+        out = subprocess.run([exe], check=True, capture_output=True, text=True)
+    vals = np.array([float(x) for x in out.stdout.split()]).reshape(3, 64)
+    save("rng_streams.npz", seed0=vals[0], seed1=vals[1], seed2=vals[2])
+
+
+def main():
+    ref = oracle.reference()
+    if ref is None:
+        raise SystemExit("the reference harness is required (reference sources "
+                         "not found)")
+    ref.set_threads(0)
+    kat_free_surface(ref)
+    sphere_union(ref)
+    noncubic(ref)
+    mgpcg_poisson(ref)
+    transfers(ref)
+    rng_streams()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,167 @@
+"""GPU pressure projection against the reference (golden fixtures) and the
+oracle port, through the C ABI.
+
+Bars: cell classification, face weights (every level) and the FP64 matrix and
+rhs are bit-exact; FP32 coarse rows equal the FP32 rounding of the reference's
+rows; pressure within 1e-5 relative L2 of the tightly-solved reference and
+true relative residual <= the 1e-6 tolerance.
+"""
+import numpy as np
+import pytest
+
+import jetgpu
+import oracle
+from conftest import golden
+from jetgpu import scenes
+
+pytestmark = pytest.mark.gpu
+
+KMAX = jetgpu.kMaxD
+TOL = 1e-6          # relative true residual the solver must reach
+P_REL_L2 = 1e-5     # pressure vs FP64 reference
+
+
+def grid_field(data, res, h):
+    return jetgpu.CellCenteredScalarGrid3(res, h, (0, 0, 0), data)
+
+
+def solve(res, h, u, v, w, bsdf, fsdf, precision="fp32", levels=5, solid=None,
+          **kw):
+    solver = jetgpu.FdmMgpcgSolver3(200, levels, 2, 2, 10, 2, TOL, 1.0, True,
+                                    precision=precision, **kw)
+    ps = jetgpu.GridFractionalSinglePhasePressureSolver3(solver)
+    vel = jetgpu.FaceCenteredGrid3(res, h, (0, 0, 0), u.copy(), v.copy(),
+                                   w.copy())
+    out = vel.clone()
+    b = bsdf if np.isscalar(bsdf) else grid_field(bsdf, res, h)
+    f = fsdf if np.isscalar(fsdf) else grid_field(fsdf, res, h)
+    st = ps.solve(vel, 1.0 / 60.0, out, b, solid, f)
+    return ps, out, st
+
+
+def rel_l2(a, b):
+    return np.linalg.norm(a - b) / max(np.linalg.norm(b), 1e-300)
+
+
+def check_levels(ps, g, res):
+    for l in range(int(g["levels"])):
+        for what in ("fluid", "uw", "vw", "ww"):
+            got = ps.level(l, what)
+            assert np.array_equal(got, g[f"L{l}_{what}"].reshape(-1)), (l, what)
+        A = ps.level(l, "A")
+        ref = g[f"L{l}_A"].reshape(-1)
+        if l == 0:
+            assert np.array_equal(A, ref), "level-0 FP64 matrix"
+        else:
+            assert np.array_equal(A, ref.astype(np.float32).astype(np.float64)), l
+    assert np.array_equal(ps.level(0, "b"), g["L0_b"].reshape(-1))
+
+
+@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+def test_sphere_union_16(precision):
+    g = golden("sphere_union_16.npz")
+    n, h = 16, (1 / 16,) * 3
+    ps, out, st = solve((n,) * 3, h, g["u"], g["v"], g["w"], g["boundary_sdf"],
+                        g["fluid_sdf"], precision, levels=int(g["params"][1]))
+    assert st == 0
+    check_levels(ps, g, (n,) * 3)
+    assert ps.last_stats.relative_residual <= TOL
+    assert rel_l2(ps.pressure(), g["p"]) < P_REL_L2
+    for k in "uvw":
+        assert np.abs(getattr(out, k) - g["out_" + k]).max() < 1e-4
+
+
+def test_noncubic_moving_solid():
+    g = golden("noncubic_12x8x16.npz")
+    res, h = (12, 8, 16), tuple(g["spacing"])
+    ps, out, st = solve(res, h, g["u"], g["v"], g["w"], g["boundary_sdf"],
+                        g["fluid_sdf"], levels=int(g["params"][1]),
+                        solid=(g["solid_u"], g["solid_v"], g["solid_w"]))
+    assert st == 0
+    check_levels(ps, g, res)
+    assert rel_l2(ps.pressure(), g["p"]) < P_REL_L2
+
+
+def test_known_answer_free_surface():
+    """grid_fractional_single_phase_pressure_solver3_tests.cpp:17-74."""
+    g = golden("kat_free_surface_3.npz")
+    ps, out, st = solve((3, 3, 3), (1.0, 1.0, 1.0), g["u"], g["v"], g["w"],
+                        KMAX, g["fluid_sdf"])
+    assert st == 0
+    check_levels(ps, g, (3, 3, 3))
+    p = ps.pressure()
+    for j in range(2):
+        assert np.allclose(p[:, j, :], 1.5 - j, atol=1e-6)
+    for k in "uvw":
+        assert np.abs(getattr(out, k)).max() < 1e-6
+
+
+@pytest.mark.parametrize("n", [32, 64])
+def test_sphere_union_vs_port(port, n):
+    h = (1.0 / n,) * 3
+    sc = scenes.sphere_union_scene(n, seed=1)
+    ref = port.pressure_solve((n,) * 3, h, (0, 0, 0), sc["u"], sc["v"], sc["w"],
+                              sc["boundary_sdf"], sc["fluid_sdf"],
+                              oracle.MgParams(400, 5, 3, 3, 20, 20, 1e-13, 1.5,
+                                              True))
+    ps, out, st = solve((n,) * 3, h, sc["u"], sc["v"], sc["w"],
+                        sc["boundary_sdf"], sc["fluid_sdf"])
+    assert st == 0
+    for what in ("fluid", "uw", "vw", "ww"):
+        assert np.array_equal(ps.level(0, what),
+                              port.level(0, what, (n,) * 3).reshape(-1))
+    assert np.array_equal(ps.level(0, "A"), port.level(0, "A", (n,) * 3).reshape(-1))
+    assert ps.last_stats.relative_residual <= TOL
+    assert rel_l2(ps.pressure(), ref["p"]) < P_REL_L2
+
+
+def test_flip_substep_64_vs_port(port):
+    n = 64
+    h = (1.0 / n,) * 3
+    sc = scenes.flip_first_substep(n, box_hi=(0.25, 0.75, 1.0))
+    ref = port.pressure_solve((n,) * 3, h, (0, 0, 0), sc["u"], sc["v"], sc["w"],
+                              sc["boundary_sdf"], sc["fluid_sdf"],
+                              oracle.MgParams(400, 5, 3, 3, 20, 20, 1e-13, 1.5,
+                                              True))
+    ps, out, st = solve((n,) * 3, h, sc["u"], sc["v"], sc["w"],
+                        sc["boundary_sdf"], sc["fluid_sdf"])
+    assert st == 0
+    assert ps.last_stats.relative_residual <= TOL
+    assert rel_l2(ps.pressure(), ref["p"]) < P_REL_L2
+    for k in "uvw":
+        assert np.abs(getattr(out, k) - ref[k]).max() < 1e-4
+
+
+def test_deterministic():
+    n = 32
+    h = (1.0 / n,) * 3
+    sc = scenes.sphere_union_scene(n, seed=1)
+    a = solve((n,) * 3, h, sc["u"], sc["v"], sc["w"], sc["boundary_sdf"],
+              sc["fluid_sdf"])
+    b = solve((n,) * 3, h, sc["u"], sc["v"], sc["w"], sc["boundary_sdf"],
+              sc["fluid_sdf"])
+    assert np.array_equal(a[0].pressure(), b[0].pressure())
+    for k in "uvw":
+        assert np.array_equal(getattr(a[1], k), getattr(b[1], k))
+
+
+def test_no_fluid_leaves_velocity():
+    n = 16
+    h = (1.0 / n,) * 3
+    rng = np.random.default_rng(0)
+    u = rng.uniform(-1, 1, (n, n, n + 1))
+    v = rng.uniform(-1, 1, (n, n + 1, n))
+    w = rng.uniform(-1, 1, (n + 1, n, n))
+    ps, out, st = solve((n,) * 3, h, u, v, w, KMAX, 1.0)
+    assert st == 0
+    assert np.array_equal(ps.pressure(), np.zeros((n, n, n)))
+    assert np.array_equal(out.u, u) and np.array_equal(out.v, v)
+
+
+def test_bad_inputs_rejected():
+    solver = jetgpu.FdmMgpcgSolver3()
+    ps = jetgpu.GridFractionalSinglePhasePressureSolver3(solver)
+    vel = jetgpu.FaceCenteredGrid3((8, 8, 8), (0.0, 0.1, 0.1))
+    with pytest.raises(jetgpu.JetGpuError) as e:
+        ps.solve(vel, 0.1, vel.clone())
+    assert e.value.status == 3

@@ -1,0 +1,161 @@
+"""Pins the oracle port to the reference (CPU only).
+
+The port (oracle/port/jet_port.cpp) must reproduce the reference's outputs bit
+for bit: against the committed golden fixtures everywhere, and against the
+reference compiled from its own sources where those sources exist.
+"""
+import numpy as np
+import pytest
+
+import oracle
+from conftest import golden
+from jetgpu import scenes
+
+KMAX = float(np.finfo(np.float64).max)
+
+
+def params_from(arr):
+    a = list(arr)
+    return oracle.MgParams(int(a[0]), int(a[1]), int(a[2]), int(a[3]),
+                           int(a[4]), int(a[5]), float(a[6]), float(a[7]),
+                           bool(a[8]))
+
+
+def check_pressure_case(o, g, res, h, bsdf, fsdf, solid=(None, None, None)):
+    out = o.pressure_solve(res, h, (0, 0, 0), g["u"], g["v"], g["w"], bsdf,
+                           fsdf, params_from(g["params"]), solid=solid)
+    assert out["iters"] == int(g["iters"])
+    for k in ("u", "v", "w"):
+        assert np.array_equal(out[k], g["out_" + k]), k
+    assert np.array_equal(out["p"], g["p"])
+    assert o.level_count() == int(g["levels"])
+    for l in range(int(g["levels"])):
+        for what in ("fluid", "uw", "vw", "ww", "A"):
+            assert np.array_equal(o.level(l, what, res), g[f"L{l}_{what}"]), \
+                (l, what)
+    assert np.array_equal(o.level(0, "b", res), g["L0_b"])
+
+
+def test_known_answer_free_surface(port):
+    """grid_fractional_single_phase_pressure_solver3_tests.cpp:17-74."""
+    g = golden("kat_free_surface_3.npz")
+    check_pressure_case(port, g, (3, 3, 3), (1.0, 1.0, 1.0), KMAX,
+                        g["fluid_sdf"])
+    p = g["p"]
+    for j in range(2):
+        assert np.allclose(p[:, j, :], 1.5 - j, atol=1e-6)
+    for k in ("out_u", "out_v", "out_w"):
+        assert np.abs(g[k]).max() < 1e-6
+
+
+def test_sphere_union_bit_exact(port):
+    g = golden("sphere_union_16.npz")
+    h = 1.0 / 16
+    check_pressure_case(port, g, (16, 16, 16), (h, h, h), g["boundary_sdf"],
+                        g["fluid_sdf"])
+
+
+def test_noncubic_moving_solid_bit_exact(port):
+    g = golden("noncubic_12x8x16.npz")
+    check_pressure_case(port, g, (12, 8, 16), tuple(g["spacing"]),
+                        g["boundary_sdf"], g["fluid_sdf"],
+                        solid=(g["solid_u"], g["solid_v"], g["solid_w"]))
+
+
+def test_mgpcg_poisson(port):
+    """fdm_mgpcg_solver3_tests.cpp:13-60: converges (returns true)."""
+    g = golden("mgpcg_poisson_32.npz")
+    A = [g[f"A{l}"] for l in range(4)]
+    b = [g[f"b{l}"] for l in range(4)]
+    r = port.mgpcg_system(A, b, params_from(g["params"]))
+    assert r["ok"] and bool(g["ok"])
+    assert r["iters"] == int(g["iters"])
+    assert np.array_equal(r["x"], g["x"])
+    rt = port.mgpcg_system(A, b, params_from(g["params_tight"]))
+    assert np.array_equal(rt["x"], g["x_tight"])
+
+
+def test_transfers_bit_exact(port):
+    g = golden("transfer_16.npz")
+    n, h = 16, 1.0 / 16
+    grids, marks, snaps = port.p2g((n, n, n), (h, h, h), (0, 0, 0), g["pos"],
+                                   g["vel"])
+    for a, k in enumerate("uvw"):
+        assert np.array_equal(grids[a], g[k])
+        assert np.array_equal(marks[a], g["m" + k])
+        assert np.array_equal(snaps[a], g["s" + k])
+    new = [g["new_u"], g["new_v"], g["new_w"]]
+    v, d = port.g2p_flip((n, n, n), (h, h, h), (0, 0, 0), g["pos"], g["vel"],
+                         new, snaps, 0.0)
+    assert np.array_equal(v, g["vel_flip"])
+    for a, k in enumerate("uvw"):
+        assert np.array_equal(d[a], g["d" + k])
+    v, _ = port.g2p_flip((n, n, n), (h, h, h), (0, 0, 0), g["pos"], g["vel"],
+                         new, snaps, 0.25)
+    assert np.array_equal(v, g["vel_blend"])
+    v = port.g2p_pic((n, n, n), (h, h, h), (0, 0, 0), g["pos"], g["vel"], new)
+    assert np.array_equal(v, g["vel_pic"])
+
+
+def test_red_black_relax_decreases_residual(port):
+    """fdm_gauss_seidel_solver3_tests.cpp:66-85 on the test-helper system."""
+    from make_systems import helper_system
+    A, b = helper_system(32)
+    x = np.zeros_like(b)
+    r0 = np.linalg.norm(port.residual(A, x, b))
+    for it in range(40):
+        x = port.relax(A, b, x, 1.0, True, 1)
+        r = np.linalg.norm(port.residual(A, x, b))
+        if it > 0:
+            assert r < r0
+        r0 = r
+
+
+def test_restrict_correct_transpose(port):
+    """Restriction is 1/8 of the prolongation's transpose (boundaries too),
+    which the GPU's symmetric V-cycle relies on."""
+    rng = np.random.default_rng(0)
+    f = rng.standard_normal((8, 8, 8))
+    c = rng.standard_normal((4, 4, 4))
+    Rf = port.mg_restrict(f)
+    Pc = port.mg_correct(c, np.zeros((8, 8, 8)))
+    assert abs(np.sum(Rf * c) - np.sum(f * Pc) / 8.0) < 1e-12
+
+
+def test_rng_streams_match_cpp():
+    g = golden("rng_streams.npz")
+    for s in range(3):
+        ours = scenes.Mt19937Uniform(s).canonical(64)
+        assert np.array_equal(ours, g[f"seed{s}"])
+
+
+def test_dam_break_particle_counts():
+    pos, vel = scenes.dam_break_particles(64, (0.25, 0.75, 1.0), seed=0)
+    assert pos.shape == (393216, 3)
+    assert pos.min() >= 0 and pos[:, 0].max() < 0.25 + 1e-12
+    # 256^3 box [0,.3]x[0,.8]x[0,1]: cells whose centre is inside.
+    c = (np.arange(256) + 0.5) / 256
+    counts = [int(np.count_nonzero(c < b)) for b in (0.3, 0.8, 1.0)]
+    assert counts == [77, 205, 256]
+
+
+def test_port_matches_reference_random(port, reference):
+    """Fresh random scenes through both libraries (needs the reference)."""
+    rng = np.random.default_rng(11)
+    for n, levels in ((20, 3), (24, 4)):
+        h = 1.0 / n
+        X, Y, Z = scenes.cell_centres(n)
+        fl = np.minimum(Y - rng.uniform(0.3, 0.7),
+                        np.sqrt((X - .5) ** 2 + (Y - .5) ** 2 + (Z - .5) ** 2) - .2)
+        bs = np.sqrt((X - .3) ** 2 + (Y - .2) ** 2 + (Z - .6) ** 2) - .18
+        u = rng.uniform(-1, 1, (n, n, n + 1))
+        v = rng.uniform(-1, 1, (n, n + 1, n))
+        w = rng.uniform(-1, 1, (n + 1, n, n))
+        p = oracle.MgParams(100, levels, 3, 3, 10, 10, 1e-9, 1.5, True)
+        a = port.pressure_solve((n, n, n), (h, h, h), (0, 0, 0), u, v, w, bs,
+                                fl, p)
+        b = reference.pressure_solve((n, n, n), (h, h, h), (0, 0, 0), u, v, w,
+                                     bs, fl, p)
+        for k in ("u", "v", "w", "p"):
+            assert np.array_equal(a[k], b[k]), k
+        assert a["iters"] == b["iters"]
