@@ -156,6 +156,12 @@ __global__ void k_rows_to_f32(const double* __restrict__ A, float4* __restrict__
                              (float)A[4 * c + 2], (float)A[4 * c + 3]);
 }
 
+__global__ void k_fill_f32(float* __restrict__ p, float v, long N) {
+    for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < N;
+         c += (long)gridDim.x * blockDim.x)
+        p[c] = v;
+}
+
 __global__ void k_rows_f32_to_f64(const float4* __restrict__ A,
                                   double* __restrict__ out, long N) {
     for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < N;
@@ -316,6 +322,8 @@ jetgpu_status jetgpu_create(const jetgpu_config* cfg, jetgpu_ctx** out) {
         JG_CUDA(c, cudaMemset(c->counters, 0, kRedSlots * sizeof(unsigned)));
         JG_CUDA(c, cudaMallocHost((void**)&c->h_scal, S_COUNT * sizeof(double)));
         for (auto& e : c->ev) JG_CUDA(c, cudaEventCreate(&e));
+        jetgpu_status k = init_kernels(c);
+        if (k != JETGPU_OK) return k;
         return JETGPU_OK;
     };
     s = init();
@@ -341,6 +349,7 @@ void jetgpu_destroy(jetgpu_ctx* c) {
     if (c->host_stage) cudaFreeHost(c->host_stage);
     for (auto& e : c->ev)
         if (e) cudaEventDestroy(e);
+    for (auto& e : c->prof_ev) cudaEventDestroy(e);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
@@ -490,6 +499,9 @@ jetgpu_status jetgpu_mgpcg_solve_system(jetgpu_ctx* c, const int res0[3],
         const long N = c->levels[l].n.count();
         k_rows_to_f32<<<blocks_for(N), kThreads, 0, st>>>(dA + 4 * off,
                                                          c->levels[l].A, N);
+        // A caller-built system has no fluid SDF: every cell is an unknown.
+        k_fill_f32<<<blocks_for(N), kThreads, 0, st>>>(c->levels[l].phi,
+                                                      -1.0f, N);
         off += N;
     }
     JG_CUDA(c, cudaGetLastError());
@@ -758,6 +770,90 @@ jetgpu_status jetgpu_g2p_pic(jetgpu_ctx* c, const jetgpu_grid* grid, long np,
     if (s != JETGPU_OK) return s;
     if (np) JG_CUDA(c, cudaMemcpyAsync(vel, dvel, np * 24, cudaMemcpyDeviceToHost, st));
     JG_CUDA(c, cudaStreamSynchronize(st));
+    return JETGPU_OK;
+}
+
+}  // extern "C"
+
+// ---- live per-kernel profile -------------------------------------------------
+
+namespace jg {
+
+const char* kernel_class_name(int cls) {
+    static const char* names[K_CLASS_COUNT] = {
+        "rb_sweep_fused_l0", "rb_sweep_fused_coarse", "rb_half_l0",
+        "rb_half_coarse", "coarsest", "residual32", "restrict",
+        "correct", "spmv_dot", "update_xr", "dot_rz", "update_d",
+        "residual64", "accumulate", "build", "gradient", "p2g", "g2p",
+        "unet"};
+    return (cls >= 0 && cls < K_CLASS_COUNT) ? names[cls] : "?";
+}
+
+int prof_begin(Ctx* c) {
+    if (!c->prof_on) return -1;
+    if (c->prof_used + 2 > c->prof_ev.size()) {
+        for (int i = 0; i < 256; ++i) {
+            cudaEvent_t e;
+            if (cudaEventCreate(&e) != cudaSuccess) return -1;
+            c->prof_ev.push_back(e);
+        }
+    }
+    const int e0 = (int)c->prof_used++;
+    cudaEventRecord(c->prof_ev[e0], c->stream);
+    return e0;
+}
+
+void prof_end(Ctx* c, int cls, int e0, double bytes) {
+    if (e0 < 0 || !c->prof_on) return;
+    const int e1 = (int)c->prof_used++;
+    cudaEventRecord(c->prof_ev[e1], c->stream);
+    c->prof_recs.push_back(ProfRec{cls, e0, e1, bytes});
+}
+
+}  // namespace jg
+
+extern "C" {
+
+jetgpu_status jetgpu_get_stream(jetgpu_ctx* c, void** stream) {
+    if (!c || !stream) return JETGPU_BAD_INPUT;
+    *stream = (void*)c->stream;
+    return JETGPU_OK;
+}
+
+jetgpu_status jetgpu_profile(jetgpu_ctx* c, int enable) {
+    if (!c) return JETGPU_BAD_INPUT;
+    JG_CUDA(c, cudaStreamSynchronize(c->stream));
+    c->prof_on = enable != 0;
+    c->prof_used = 0;
+    c->prof_recs.clear();
+    return JETGPU_OK;
+}
+
+jetgpu_status jetgpu_profile_read(jetgpu_ctx* c, jetgpu_kernel_stat* out,
+                                  int capacity, int* count) {
+    if (!c || !count) return JETGPU_BAD_INPUT;
+    JG_CUDA(c, cudaStreamSynchronize(c->stream));
+    jetgpu_kernel_stat acc[K_CLASS_COUNT];
+    std::memset(acc, 0, sizeof(acc));
+    for (const ProfRec& r : c->prof_recs) {
+        float ms = 0.f;
+        JG_CUDA(c, cudaEventElapsedTime(&ms, c->prof_ev[r.e0], c->prof_ev[r.e1]));
+        jetgpu_kernel_stat& a = acc[r.cls];
+        a.launches += 1;
+        a.total_ms += ms;
+        a.bytes += r.bytes;
+    }
+    int n = 0;
+    for (int k = 0; k < K_CLASS_COUNT; ++k) {
+        if (acc[k].launches == 0) continue;
+        if (out && n < capacity) {
+            out[n] = acc[k];
+            std::snprintf(out[n].name, sizeof(out[n].name), "%s",
+                          kernel_class_name(k));
+        }
+        ++n;
+    }
+    *count = n;
     return JETGPU_OK;
 }
 

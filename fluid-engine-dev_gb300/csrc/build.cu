@@ -443,6 +443,7 @@ jetgpu_status build_weights(Ctx* c, const GridDesc& g, const FieldDesc& bsdf,
     const unsigned nl = c->built_levels;
     Level& L0 = c->levels[0];
     const Dims n = L0.n;
+    Prof pr(c, K_BUILD, (8.0 + 4.0) * (double)n.count() + 3.0 * 4.0 * n.count());
     k_sample_fluid<<<blocks_for(n.count()), kThreads, 0, c->stream>>>(
         L0.phi, n, g, fsdf);
     const Dims fu{n.x + 1, n.y, n.z}, fv{n.x, n.y + 1, n.z},
@@ -489,6 +490,8 @@ jetgpu_status build_system(Ctx* c, const GridDesc& g, const double* u,
         L.h[1] = hy;
         L.h[2] = hz;
         const bool top = (l == 0);
+        Prof pr(c, K_BUILD, (top ? 16.0 + 32.0 + 8.0 + 24.0 : 16.0 + 16.0) *
+                                (double)L.n.count());
         k_build_system<<<blocks_for(L.n.count()), kThreads, 0, c->stream>>>(
             L.n, hx, hy, hz, L.phi, L.uw, L.vw, L.ww, top ? u : nullptr,
             top ? v : nullptr, top ? w : nullptr, top ? su : nullptr,
@@ -515,6 +518,7 @@ jetgpu_status apply_gradient(Ctx* c, const GridDesc& g, const double* u,
     if (ow != w)
         JG_CUDA(c, cudaMemcpyAsync(ow, w, nw * 8, cudaMemcpyDeviceToDevice,
                                    c->stream));
+    Prof pr(c, K_GRADIENT, (4.0 + 12.0 + 8.0 + 48.0) * (double)n.count());
     k_apply_gradient<<<blocks_for(n.count()), kThreads, 0, c->stream>>>(
         n, 1.0 / g.spacing[0], 1.0 / g.spacing[1], 1.0 / g.spacing[2], L.phi,
         L.uw, L.vw, L.ww, c->x64, u, v, w, ou, ov, ow);

@@ -30,6 +30,37 @@ struct Level {
     uint2* Ah = nullptr;         // BF16 matrix rows (4 x bf16)
 };
 
+// Kernel classes of the live per-kernel profile (jetgpu_profile_read).
+enum KernelClass : int {
+    K_SWEEP_L0 = 0,   // fused red-black sweep, finest level
+    K_SWEEP_COARSE,   // fused red-black sweep, coarse levels
+    K_HALF_L0,        // red or black half-sweep, finest level
+    K_HALF_COARSE,    // red or black half-sweep, coarse levels
+    K_COARSEST,       // one-CTA coarsest-level sweeps
+    K_RESIDUAL,       // FP32 residual (V-cycle)
+    K_RESTRICT,       // residual restriction
+    K_CORRECT,        // prolongation + correction
+    K_SPMV,           // q = A d, d.q
+    K_UPDATE_XR,      // x += a d, r -= a q, r.r
+    K_DOT_RZ,         // r.z
+    K_UPDATE_D,       // d = z + b d
+    K_RESIDUAL64,     // FP64 true residual
+    K_ACCUMULATE,     // x64 += e
+    K_BUILD,          // weights + system build
+    K_GRADIENT,       // pressure gradient
+    K_P2G,
+    K_G2P,
+    K_UNET,
+    K_CLASS_COUNT
+};
+const char* kernel_class_name(int cls);
+
+struct ProfRec {
+    int cls;
+    int e0, e1;
+    double bytes;
+};
+
 struct Ctx {
     jetgpu_config cfg;
     int device = 0;
@@ -81,6 +112,30 @@ struct Ctx {
 
     // Learned preconditioner (opaque; see unet.cu).
     void* unet = nullptr;
+
+    // Live per-kernel profile: CUDA events recorded on `stream` around
+    // launches while enabled.
+    bool prof_on = false;
+    std::vector<cudaEvent_t> prof_ev;
+    size_t prof_used = 0;
+    std::vector<ProfRec> prof_recs;
+};
+
+// Records an event before a launch; returns its index or -1.
+int prof_begin(Ctx* c);
+// Records the closing event and files the launch under `cls`.
+void prof_end(Ctx* c, int cls, int e0, double bytes);
+
+// Brackets one launch for the live per-kernel profile (no-op unless on).
+struct Prof {
+    Ctx* c;
+    int cls;
+    double bytes;
+    int e0;
+    Prof(Ctx* c_, int cls_, double bytes_) : c(c_), cls(cls_), bytes(bytes_) {
+        e0 = prof_begin(c);
+    }
+    ~Prof() { prof_end(c, cls, e0, bytes); }
 };
 
 // Sets ctx->err and returns the status.
@@ -134,8 +189,12 @@ jetgpu_status mgpcg_solve(Ctx* c, jetgpu_solve_stats* st);
 // Computes level count for resolution n (FdmMgUtils3::resizeArrayWithFinest).
 unsigned level_count(Dims n, unsigned max_levels);
 
-// Applies one V-cycle z = M r on FP32 vectors (exposed for tests).
-jetgpu_status vcycle(Ctx* c, const float* r, float* z);
+// Applies one V-cycle z = M r on FP32 vectors; the result lands in z or
+// alt (returned through *result).
+jetgpu_status vcycle(Ctx* c, const float* r, float* z, float* alt,
+                     float** result);
+// One-time kernel attributes (dynamic shared memory limits).
+jetgpu_status init_kernels(Ctx* c);
 
 // ---- transfer.cu ----------------------------------------------------------
 jetgpu_status p2g(Ctx* c, const GridDesc& g, long np, const double* pos,

@@ -291,6 +291,166 @@ __global__ void __launch_bounds__(kThreads)
     }
 }
 
+// K8 (fused): one full red-black SOR sweep in a single pass over memory.
+//
+// A block owns a 64 x 8 (i, j) tile and marches through a slab of k planes
+// (2.5-D blocking). x is read from `xin` and the swept x written to `xout`
+// (ping-pong), so blocks never see each other's updates: each block redoes
+// the first-colour update on a one-cell ring around its tile, from old
+// values, exactly as the sequential sweep would produce them. Per plane the
+// block stages x with a two-cell ring, the matrix rows and b with cp.async
+// 16-byte copies (zero-filled outside the domain), then
+//   (1) updates the first colour of plane t+1 on tile + ring (in shared
+//       memory; the 7-point neighbours of a cell all have the other colour),
+//   (2) updates the second colour of plane t on the tile, reading first-
+//       colour values of planes t-1, t, t+1 that (1) produced, and writes
+//       both colours of plane t to global memory as one float2 per thread.
+// HBM traffic per sweep: x, b and A read once, x written once — 28 B/cell —
+// plus ring re-reads that mostly hit L2. Requires nx % 4 == 0.
+namespace fused {
+constexpr int TX = 64, TY = 8;          // tile (cells)
+constexpr int SX = TX + 8, SY = TY + 4; // staged plane: i0-4 .. i0+67, j0-2 .. j0+9
+constexpr int PLANE = SX * SY;          // 864 cells
+constexpr int XS = 4, AS = 3, BS = 2;   // ring depths (planes)
+constexpr size_t SMEM = (size_t)PLANE * (XS * 4 + AS * 16 + BS * 4);
+
+__device__ __forceinline__ int ring(int p, int m) { return ((p % m) + m) % m; }
+
+__device__ __forceinline__ void cp16(void* smem, const void* gmem, bool valid) {
+    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
+    const int src = valid ? 16 : 0;
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s),
+                 "l"(gmem), "r"(src));
+}
+__device__ __forceinline__ void cp_commit_wait() {
+    asm volatile("cp.async.commit_group;\n" ::);
+    asm volatile("cp.async.wait_group 0;\n" ::);
+}
+}  // namespace fused
+
+__global__ void __launch_bounds__(256)
+    k_rb_sweep_fused(const float4* __restrict__ A, const float* __restrict__ b,
+                     const float* __restrict__ xin, float* __restrict__ xout,
+                     Dims n, int first, float omega, int kz) {
+    using namespace fused;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    float* sx = reinterpret_cast<float*>(smem_raw);               // XS planes
+    float4* sA = reinterpret_cast<float4*>(sx + XS * PLANE);      // AS planes
+    float* sb = reinterpret_cast<float*>(sA + AS * PLANE);        // BS planes
+    const int tid = threadIdx.x;
+    const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
+    const int k0 = blockIdx.z * kz;
+    const int k1 = min(n.z, k0 + kz);
+    const long sy = n.x, sz = (long)n.x * n.y;
+    const int second = first ^ 1;
+
+    // Stage plane p of x / A / b (zero outside the domain).
+    auto load_x = [&](int p) {
+        float* dst = sx + ring(p, XS) * PLANE;
+        if (xin == nullptr || p < 0 || p >= n.z) {
+            for (int q = tid; q < PLANE; q += 256) dst[q] = 0.0f;
+            return;
+        }
+        for (int f = tid; f < PLANE / 4; f += 256) {
+            const int r = f / (SX / 4), c4 = f % (SX / 4);
+            const int gi = i0 - 4 + 4 * c4, gj = j0 - 2 + r;
+            const bool ok = gi >= 0 && gi < n.x && gj >= 0 && gj < n.y;
+            const float* src = ok ? xin + gi + sy * gj + sz * p : xin;
+            cp16(dst + r * SX + 4 * c4, src, ok);
+        }
+    };
+    auto load_A = [&](int p) {
+        float4* dst = sA + ring(p, AS) * PLANE;
+        const bool pin = p >= 0 && p < n.z;
+        for (int f = tid; f < PLANE; f += 256) {
+            const int r = f / SX, c = f % SX;
+            const int gi = i0 - 4 + c, gj = j0 - 2 + r;
+            const bool ok = pin && gi >= 0 && gi < n.x && gj >= 0 && gj < n.y;
+            const float4* src = ok ? A + gi + sy * gj + sz * p : A;
+            cp16(dst + f, src, ok);
+        }
+    };
+    auto load_b = [&](int p) {
+        float* dst = sb + ring(p, BS) * PLANE;
+        const bool pin = p >= 0 && p < n.z;
+        for (int f = tid; f < PLANE / 4; f += 256) {
+            const int r = f / (SX / 4), c4 = f % (SX / 4);
+            const int gi = i0 - 4 + 4 * c4, gj = j0 - 2 + r;
+            const bool ok = pin && gi >= 0 && gi < n.x && gj >= 0 && gj < n.y;
+            const float* src = ok ? b + gi + sy * gj + sz * p : b;
+            cp16(dst + r * SX + 4 * c4, src, ok);
+        }
+    };
+    // SOR update of local cell (ii, jj) in plane p; neighbours outside the
+    // domain contribute nothing (FdmBlas3 guards, fdm_linear_system3.cpp:79-96).
+    auto relax = [&](int ii, int jj, int p) -> float {
+        const int s = (jj + 2) * SX + (ii + 4);
+        const int gi = i0 + ii, gj = j0 + jj;
+        const float* xc = sx + ring(p, XS) * PLANE;
+        const float4* Ac = sA + ring(p, AS) * PLANE;
+        const float4 row = Ac[s];
+        float acc = 0.0f;
+        if (gi > 0) acc += Ac[s - 1].y * xc[s - 1];
+        if (gi + 1 < n.x) acc += row.y * xc[s + 1];
+        if (gj > 0) acc += Ac[s - SX].z * xc[s - SX];
+        if (gj + 1 < n.y) acc += row.z * xc[s + SX];
+        if (p > 0)
+            acc += sA[ring(p - 1, AS) * PLANE + s].w *
+                   sx[ring(p - 1, XS) * PLANE + s];
+        if (p + 1 < n.z) acc += row.w * sx[ring(p + 1, XS) * PLANE + s];
+        const float bb = sb[ring(p, BS) * PLANE + s];
+        return (1.0f - omega) * xc[s] + omega * (bb - acc) / row.x;
+    };
+
+    const int t0 = k0 - 2;
+    load_x(t0);
+    load_x(t0 + 1);
+    load_A(t0);
+    for (int t = t0; t < k1; ++t) {
+        load_x(t + 2);
+        load_A(t + 1);
+        load_b(t + 1);
+        fused::cp_commit_wait();
+        __syncthreads();
+        // (1) first colour of plane t+1 on tile + 1-cell ring.
+        const int p1 = t + 1;
+        if (p1 >= k0 - 1 && p1 <= k1 && p1 >= 0 && p1 < n.z) {
+            float* xp = sx + ring(p1, XS) * PLANE;
+            for (int q = tid; q < 33 * (TY + 2); q += 256) {
+                const int jj = q / 33 - 1;
+                const int ii = -1 + 2 * (q % 33) + ((first - jj - p1 + 1) & 1);
+                const int gi = i0 + ii, gj = j0 + jj;
+                if (gi < 0 || gi >= n.x || gj < 0 || gj >= n.y) continue;
+                const float v = relax(ii, jj, p1);
+                xp[(jj + 2) * SX + (ii + 4)] = v;
+            }
+        }
+        __syncthreads();
+        // (2) second colour of plane t on the tile; write plane t.
+        if (t >= k0) {
+            const int tx = tid & 31, ty = tid >> 5;
+            const int ii = 2 * tx, jj = ty;
+            const int gi = i0 + ii, gj = j0 + jj;
+            if (gi < n.x && gj < n.y) {
+                const int odd = ((ii + jj + t) & 1) != second;  // S cell at ii+odd
+                const float* xp = sx + ring(t, XS) * PLANE;
+                const int s = (jj + 2) * SX + (ii + 4);
+                float2 out;
+                const float vs = relax(ii + odd, jj, t);
+                if (odd) {
+                    out.x = xp[s];
+                    out.y = vs;
+                } else {
+                    out.x = vs;
+                    out.y = xp[s + 1];
+                }
+                *reinterpret_cast<float2*>(xout + gi + sy * gj + sz * t) = out;
+            }
+        }
+        __syncthreads();
+    }
+}
+
 // K9a: r = b - A x (FP32).
 __global__ void __launch_bounds__(kThreads)
     k_residual32(const float4* __restrict__ A, const float* __restrict__ x,
@@ -307,10 +467,15 @@ __global__ void __launch_bounds__(kThreads)
 }
 
 // K9b: FdmMgUtils3::restrict (fdm_mg_linear_system3.cpp:43-98): 4x4x4
-// (1,3,3,1)/8 tensor filter with taps clamped at the edges.
+// (1,3,3,1)/8 tensor filter with taps clamped at the edges. Coarse cells
+// whose fluid SDF is not negative receive 0: their rows are identity rows
+// (no unknown), so the coarse correction there must stay 0, the Dirichlet
+// value of the air. The reference passes the residual into those rows and
+// prolongates the resulting non-zero values back into the fluid next to the
+// free surface, which costs it multigrid's mesh-independent convergence.
 __global__ void __launch_bounds__(kThreads)
     k_restrict(const float* __restrict__ fine, float* __restrict__ coarse,
-               Dims c) {
+               const float* __restrict__ coarse_phi, Dims c) {
     const long N = c.count();
     const int fx = 2 * c.x, fy = 2 * c.y;
     const float kern[4] = {0.125f, 0.375f, 0.375f, 0.125f};
@@ -338,7 +503,7 @@ __global__ void __launch_bounds__(kThreads)
             }
             sum += kern[z] * sy;
         }
-        coarse[t] = sum;
+        coarse[t] = (coarse_phi[t] < 0.0f) ? sum : 0.0f;
     }
 }
 
@@ -423,9 +588,10 @@ int grid_for(const Ctx* c, long work) {
 }
 
 void rb_half(Ctx* c, const Level& L, const float* b, float* x, int color,
-             bool zero) {
+             bool zero, int cls) {
     const long pairs = (long)((L.n.x + 1) / 2) * L.n.y * L.n.z;
     const float w = (float)c->cfg.sor;
+    Prof pr(c, cls, 14.0 * L.n.count());
     if (zero)
         k_rb_half<true><<<grid_for(c, pairs), kThreads, 0, c->stream>>>(
             L.A, b, x, L.n, color, w);
@@ -434,44 +600,99 @@ void rb_half(Ctx* c, const Level& L, const float* b, float* x, int color,
             L.A, b, x, L.n, color, w);
 }
 
-// Forward sweeps (red then black) from x = 0 when `zero`.
-void smooth(Ctx* c, const Level& L, const float* b, float* x, unsigned sweeps,
-            bool reverse, bool zero) {
-    for (unsigned s = 0; s < sweeps; ++s) {
-        const int first = reverse ? 1 : 0;
-        rb_half(c, L, b, x, first, zero && s == 0);
-        rb_half(c, L, b, x, 1 - first, false);
-    }
-    if (sweeps == 0 && zero) k_zero<float><<<grid_for(c, L.n.count()), kThreads, 0, c->stream>>>(x, L.n.count());
+bool fused_ok(const Level& L) {
+    return L.n.x % 4 == 0 && L.n.x >= 64 && L.n.y >= 8 && L.n.z >= 2;
 }
 
-void vcycle_level(Ctx* c, unsigned l, const float* b, float* x) {
+// Slab depth of the fused sweep: about two waves of resident blocks.
+int fused_kz(const Ctx* c, const Level& L) {
+    const long tiles = (long)((L.n.x + fused::TX - 1) / fused::TX) *
+                       ((L.n.y + fused::TY - 1) / fused::TY);
+    const long resident = (long)c->num_sms * 3;
+    long kz = (long)L.n.z * tiles / (2 * resident);
+    if (kz < 8) kz = 8;
+    if (kz > 64) kz = 64;
+    if (kz > L.n.z) kz = L.n.z;
+    return (int)kz;
+}
+
+// `sweeps` red-black sweeps (colour order reversed when `reverse`) starting
+// from x = 0 when `zero`, else from *x. Levels the fused kernel serves
+// ping-pong between x and alt; the return value holds the result.
+float* smooth(Ctx* c, const Level& L, const float* b, float* x, float* alt,
+              unsigned sweeps, bool reverse, bool zero, int l) {
+    const int first = reverse ? 1 : 0;
+    if (sweeps == 0) {
+        if (zero)
+            k_zero<float><<<grid_for(c, L.n.count()), kThreads, 0,
+                            c->stream>>>(x, L.n.count());
+        return x;
+    }
+    if (alt != nullptr && fused_ok(L)) {
+        const int kz = fused_kz(c, L);
+        dim3 grid((L.n.x + fused::TX - 1) / fused::TX,
+                  (L.n.y + fused::TY - 1) / fused::TY, (L.n.z + kz - 1) / kz);
+        float* cur = x;
+        float* oth = alt;
+        for (unsigned s = 0; s < sweeps; ++s) {
+            const bool z0 = zero && s == 0;
+            Prof pr(c, l == 0 ? K_SWEEP_L0 : K_SWEEP_COARSE,
+                    (z0 ? 24.0 : 28.0) * L.n.count());
+            k_rb_sweep_fused<<<grid, 256, fused::SMEM, c->stream>>>(
+                L.A, b, z0 ? nullptr : cur, oth, L.n, first, (float)c->cfg.sor,
+                kz);
+            std::swap(cur, oth);
+        }
+        return cur;
+    }
+    const int cls = l == 0 ? K_HALF_L0 : K_HALF_COARSE;
+    for (unsigned s = 0; s < sweeps; ++s) {
+        rb_half(c, L, b, x, first, zero && s == 0, cls);
+        rb_half(c, L, b, x, 1 - first, false, cls);
+    }
+    return x;
+}
+
+// Symmetric V-cycle on level l from a zero initial guess; returns the
+// buffer (x or alt) that holds the result.
+float* vcycle_level(Ctx* c, unsigned l, const float* b, float* x, float* alt) {
     const Level& L = c->levels[l];
     const unsigned nl = c->built_levels;
     const jetgpu_config& cfg = c->cfg;
     if (l + 1 == nl) {
         if (L.n.count() <= kCoarsestMaxCells) {
             int nt = (int)std::min<long>(1024, ((L.n.count() + 31) / 32) * 32);
+            Prof pr(c, K_COARSEST, 28.0 * L.n.count());
             k_coarsest<<<1, nt, 0, c->stream>>>(L.A, b, x, L.n,
                                                 (int)cfg.coarsest_iter,
                                                 (float)cfg.sor);
-        } else {
-            smooth(c, L, b, x, cfg.coarsest_iter, false, true);
-            smooth(c, L, b, x, cfg.coarsest_iter, true, false);
+            return x;
         }
-        return;
+        float* cur = smooth(c, L, b, x, alt, cfg.coarsest_iter, false, true, l);
+        return smooth(c, L, b, cur, cur == x ? alt : x, cfg.coarsest_iter,
+                      true, false, l);
     }
     const Level& C = c->levels[l + 1];
-    smooth(c, L, b, x, cfg.restrict_iter, false, true);
-    k_residual32<<<grid_for(c, L.n.count()), kThreads, 0, c->stream>>>(
-        L.A, x, b, L.r, L.n);
-    k_restrict<<<grid_for(c, C.n.count()), kThreads, 0, c->stream>>>(
-        L.r, C.b, C.n);
-    vcycle_level(c, l + 1, C.b, C.x);
-    k_correct<<<grid_for(c, L.n.count()), kThreads, 0, c->stream>>>(C.x, x,
-                                                                    C.n);
-    smooth(c, L, b, x, l == 0 ? cfg.final_iter : cfg.correct_iter, true,
-           false);
+    float* cur = smooth(c, L, b, x, alt, cfg.restrict_iter, false, true, l);
+    float* other = (cur == x) ? alt : x;
+    {
+        Prof pr(c, K_RESIDUAL, 28.0 * L.n.count());
+        k_residual32<<<grid_for(c, L.n.count()), kThreads, 0, c->stream>>>(
+            L.A, cur, b, L.r, L.n);
+    }
+    {
+        Prof pr(c, K_RESTRICT, 4.0 * L.n.count() + 8.0 * C.n.count());
+        k_restrict<<<grid_for(c, C.n.count()), kThreads, 0, c->stream>>>(
+            L.r, C.b, C.phi, C.n);
+    }
+    const float* xc = vcycle_level(c, l + 1, C.b, C.x, C.x2);
+    {
+        Prof pr(c, K_CORRECT, 8.0 * L.n.count() + 4.0 * C.n.count());
+        k_correct<<<grid_for(c, L.n.count()), kThreads, 0, c->stream>>>(
+            xc, cur, C.n);
+    }
+    return smooth(c, L, b, cur, other,
+                  l == 0 ? cfg.final_iter : cfg.correct_iter, true, false, l);
 }
 
 double now_ms() {
@@ -505,14 +726,22 @@ unsigned level_count(Dims n, unsigned max_levels) {
     return i < 1 ? 1 : i;
 }
 
-jetgpu_status vcycle(Ctx* c, const float* r, float* z) {
-    vcycle_level(c, 0, r, z);
+jetgpu_status vcycle(Ctx* c, const float* r, float* z, float* alt,
+                     float** result) {
+    *result = vcycle_level(c, 0, r, z, alt);
     JG_CUDA(c, cudaGetLastError());
     return JETGPU_OK;
 }
 
 jetgpu_status prepare_levels(Ctx* c) {
     (void)c;
+    return JETGPU_OK;
+}
+
+jetgpu_status init_kernels(Ctx* c) {
+    JG_CUDA(c, cudaFuncSetAttribute(k_rb_sweep_fused,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)fused::SMEM));
     return JETGPU_OK;
 }
 
@@ -529,16 +758,29 @@ static jetgpu_status pcg_f32(Ctx* c, double target, unsigned max_it,
     unsigned it = 0;
     double rr = 0;
     while (it < max_it) {
-        if (jetgpu_status vs = vcycle(c, c->kr, c->kz)) return vs;
-        k_dot_rz<float, float><<<G, kThreads, 0, c->stream>>>(
-            c->kr, c->kz, N, c->partials, c->counters, c->scal);
-        k_update_d<float, float><<<G, kThreads, 0, c->stream>>>(c->kd, c->kz,
-                                                                N, c->scal);
-        k_spmv_dot<float, RowsF><<<G, kThreads, 0, c->stream>>>(
-            M, c->kd, c->kq, n, c->partials, c->counters, c->scal);
-        k_update_xr<float><<<G, kThreads, 0, c->stream>>>(
-            c->kx, c->kr, c->kd, c->kq, nullptr, N, c->partials, c->counters,
-            c->scal);
+        float* z = nullptr;
+        if (jetgpu_status vs = vcycle(c, c->kr, c->kz, L0.x2, &z)) return vs;
+        {
+            Prof pr(c, K_DOT_RZ, 8.0 * N);
+            k_dot_rz<float, float><<<G, kThreads, 0, c->stream>>>(
+                c->kr, z, N, c->partials, c->counters, c->scal);
+        }
+        {
+            Prof pr(c, K_UPDATE_D, 12.0 * N);
+            k_update_d<float, float><<<G, kThreads, 0, c->stream>>>(c->kd, z,
+                                                                    N, c->scal);
+        }
+        {
+            Prof pr(c, K_SPMV, 24.0 * N);
+            k_spmv_dot<float, RowsF><<<G, kThreads, 0, c->stream>>>(
+                M, c->kd, c->kq, n, c->partials, c->counters, c->scal);
+        }
+        {
+            Prof pr(c, K_UPDATE_XR, 24.0 * N);
+            k_update_xr<float><<<G, kThreads, 0, c->stream>>>(
+                c->kx, c->kr, c->kd, c->kq, nullptr, N, c->partials,
+                c->counters, c->scal);
+        }
         ++it;
         jetgpu_status s = read_scalars(c);
         if (s != JETGPU_OK) return s;
@@ -567,16 +809,29 @@ static jetgpu_status pcg_f64(Ctx* c, double target, unsigned max_it,
     float* r32 = L0.b;  // FP32 copy of r feeds the V-cycle
     // r32 already holds float(r64) (written by the residual kernel).
     while (it < max_it) {
-        if (jetgpu_status vs = vcycle(c, r32, L0.x)) return vs;
-        k_dot_rz<double, float><<<G, kThreads, 0, c->stream>>>(
-            c->r64, L0.x, N, c->partials, c->counters, c->scal);
-        k_update_d<double, float><<<G, kThreads, 0, c->stream>>>(c->dd, L0.x,
-                                                                 N, c->scal);
-        k_spmv_dot<double, RowsD><<<G, kThreads, 0, c->stream>>>(
-            M, c->dd, c->dq, n, c->partials, c->counters, c->scal);
-        k_update_xr<double><<<G, kThreads, 0, c->stream>>>(
-            c->x64, c->r64, c->dd, c->dq, r32, N, c->partials, c->counters,
-            c->scal);
+        float* z = nullptr;
+        if (jetgpu_status vs = vcycle(c, r32, L0.x, L0.x2, &z)) return vs;
+        {
+            Prof pr(c, K_DOT_RZ, 12.0 * N);
+            k_dot_rz<double, float><<<G, kThreads, 0, c->stream>>>(
+                c->r64, z, N, c->partials, c->counters, c->scal);
+        }
+        {
+            Prof pr(c, K_UPDATE_D, 20.0 * N);
+            k_update_d<double, float><<<G, kThreads, 0, c->stream>>>(
+                c->dd, z, N, c->scal);
+        }
+        {
+            Prof pr(c, K_SPMV, 48.0 * N);
+            k_spmv_dot<double, RowsD><<<G, kThreads, 0, c->stream>>>(
+                M, c->dd, c->dq, n, c->partials, c->counters, c->scal);
+        }
+        {
+            Prof pr(c, K_UPDATE_XR, 52.0 * N);
+            k_update_xr<double><<<G, kThreads, 0, c->stream>>>(
+                c->x64, c->r64, c->dd, c->dq, r32, N, c->partials,
+                c->counters, c->scal);
+        }
         ++it;
         jetgpu_status s = read_scalars(c);
         if (s != JETGPU_OK) return s;
@@ -623,9 +878,12 @@ jetgpu_status mgpcg_solve(Ctx* c, jetgpu_solve_stats* st) {
          ++pass) {
         // True FP64 residual r64 = b - A x64 (and its FP32 image).
         float* r32 = fp64 ? L0.b : c->kr;
-        k_residual64<<<G, kThreads, 0, c->stream>>>(
-            c->A64, c->x64, c->b64, c->r64, r32, fp64 ? nullptr : c->kx, n,
-            c->partials, c->counters, c->scal, S_R64);
+        {
+            Prof pr(c, K_RESIDUAL64, 60.0 * N);
+            k_residual64<<<G, kThreads, 0, c->stream>>>(
+                c->A64, c->x64, c->b64, c->r64, r32, fp64 ? nullptr : c->kx,
+                n, c->partials, c->counters, c->scal, S_R64);
+        }
         s = read_scalars(c);
         if (s != JETGPU_OK) return s;
         rnorm = std::sqrt(c->h_scal[S_R64]);
@@ -645,9 +903,11 @@ jetgpu_status mgpcg_solve(Ctx* c, jetgpu_solve_stats* st) {
             double eta = 0.5 * goal / rnorm;
             if (eta < 1e-4) eta = 1e-4;
             s = pcg_f32(c, eta * rnorm, cfg.max_cg_iter - total, &it, &rr);
-            if (s == JETGPU_OK)
+            if (s == JETGPU_OK) {
+                Prof pr(c, K_ACCUMULATE, 20.0 * N);
                 k_accumulate<<<grid_for(c, N), kThreads, 0, c->stream>>>(
                     c->x64, c->kx, N);
+            }
         }
         if (s != JETGPU_OK) return s;
         total += it;

@@ -102,8 +102,18 @@ EXPORTS = (
     "jetgpu_solve_pressure_device", "jetgpu_mgpcg_solve_system",
     "jetgpu_p2g_device", "jetgpu_g2p_flip_device", "jetgpu_g2p_pic_device",
     "jetgpu_p2g", "jetgpu_g2p_flip", "jetgpu_g2p_pic", "jetgpu_get_level",
-    "jetgpu_version",
+    "jetgpu_version", "jetgpu_get_stream", "jetgpu_profile",
+    "jetgpu_profile_read",
 )
+
+
+class KernelStat(C.Structure):
+    _fields_ = [
+        ("name", C.c_char * 32),
+        ("launches", C.c_uint),
+        ("total_ms", C.c_double),
+        ("bytes", C.c_double),
+    ]
 
 
 class JetGpuError(RuntimeError):
@@ -168,6 +178,13 @@ def library() -> C.CDLL:
     L.jetgpu_get_level.restype = C.c_int
     L.jetgpu_version.argtypes = []
     L.jetgpu_version.restype = C.c_char_p
+    L.jetgpu_get_stream.argtypes = [vp, C.POINTER(C.c_void_p)]
+    L.jetgpu_get_stream.restype = C.c_int
+    L.jetgpu_profile.argtypes = [vp, C.c_int]
+    L.jetgpu_profile.restype = C.c_int
+    L.jetgpu_profile_read.argtypes = [vp, C.POINTER(KernelStat), C.c_int,
+                                      C.POINTER(C.c_int)]
+    L.jetgpu_profile_read.restype = C.c_int
     _lib = L
     return L
 
@@ -321,6 +338,24 @@ class FdmMgpcgSolver3:
             self.close()
         except Exception:
             pass
+
+    def stream(self) -> int:
+        """The context's cudaStream_t as an integer handle."""
+        h = C.c_void_p()
+        self.check(library().jetgpu_get_stream(self.context(), C.byref(h)))
+        return h.value or 0
+
+    def profile(self, enable: bool) -> None:
+        self.check(library().jetgpu_profile(self.context(), int(enable)))
+
+    def profile_read(self) -> list:
+        arr = (KernelStat * 64)()
+        cnt = C.c_int(0)
+        self.check(library().jetgpu_profile_read(self.context(), arr, 64,
+                                                 C.byref(cnt)))
+        return [dict(name=arr[i].name.decode(), launches=arr[i].launches,
+                     total_ms=arr[i].total_ms, bytes=arr[i].bytes)
+                for i in range(min(cnt.value, 64))]
 
     def check(self, status: int, allow=(0,)) -> int:
         if status not in allow:

@@ -239,6 +239,30 @@ jetgpu_status jetgpu_g2p_pic(struct jetgpu_ctx* ctx, const jetgpu_grid* grid,
 jetgpu_status jetgpu_get_level(struct jetgpu_ctx* ctx, int level, int what,
                                void* dst, size_t capacity, size_t* count);
 
+/* The context's CUDA stream (a cudaStream_t), so callers can order their
+ * own work and time the library's kernels with events on it. No
+ * counterpart in the reference, which has no device. */
+jetgpu_status jetgpu_get_stream(struct jetgpu_ctx* ctx, void** stream);
+
+/* Live per-kernel profile: while enabled, every kernel launch of the
+ * context is bracketed by CUDA events on its stream and filed under its
+ * kernel class with the launch's algorithmic bytes. Enabling (or disabling)
+ * clears the record. Replaces the reference's Timer logs around each phase
+ * (src/jet/grid_fluid_solver3.cpp:189-207). */
+typedef struct jetgpu_kernel_stat {
+    char name[32];
+    unsigned int launches;
+    double total_ms;   /* sum of event-timed launch durations */
+    double bytes;      /* sum of algorithmic bytes of those launches */
+} jetgpu_kernel_stat;
+
+jetgpu_status jetgpu_profile(struct jetgpu_ctx* ctx, int enable);
+/* Fills up to `capacity` entries (one per kernel class seen) and returns the
+ * number of classes through *count. */
+jetgpu_status jetgpu_profile_read(struct jetgpu_ctx* ctx,
+                                  jetgpu_kernel_stat* out, int capacity,
+                                  int* count);
+
 /* Library version string. */
 const char* jetgpu_version(void);
 
