@@ -1,0 +1,461 @@
+"""Benchmark: 256^3 FLIP pressure solve on one GB300 (replicas for N > 1).
+
+Workload: the pressure system of the first sub-step of the 256^3 FLIP dam
+break with a static solid sphere (water box [0,.3]x[0,.8]x[0,1], sphere
+r=.15 at (.6,.2,.5), gravity for one 1/60 s step, closed walls; h = 1/256),
+solved to a true relative residual of 1e-6 by
+GridFractionalSinglePhasePressureSolver3 + MGPCG: weights, system build,
+MGPCG and the pressure-gradient update — the whole projection per step.
+
+Arms:
+* ours (default): `value` = ms per pressure solve with inputs resident in
+  HBM (device-pointer C ABI); `e2e` = the same through the host-pointer C ABI
+  with pinned host buffers (H2D of the inputs and D2H of the projected
+  velocity and pressure inside the timed region).
+* --impl reference: the reference's CPU algorithm (the oracle port, bit-exact
+  with the reference; or the reference itself where it was compiled on this
+  machine) on all host cores, each step one full reference pressure solve
+  (about 10 s on 8 cores); the reference's MGPCG breaks down at 256^3 before
+  1e-6, and the residual it reaches is reported.
+
+Timing: W warm-up solves, then K solves bracketed by a barrier and
+synchronize, timed with CUDA events on the library's own stream, max over
+ranks. The working set (0.5 GB of FP64 inputs, 3+ GB of solver state) is
+far larger than L2, so no flush is needed. Clocks are sampled with
+nvidia-smi during the timed region.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import tempfile
+import time
+
+REPO = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(REPO, "fluid-engine-dev_gb300"))
+sys.path.insert(0, REPO)
+
+METRIC = ("256³ FLIP pressure-solve ms & steps/s at 1e-6 residual: "
+          "learned vs plain MGPCG")
+TOL = 1e-6
+
+
+def parse_args():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=256)
+    ap.add_argument("--precision", default="fp32",
+                    choices=["fp32", "fp64", "mixed"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_setup(args):
+    """One process per GPU under torchrun; replicas (no collective on the
+    data path, only a barrier and a max for the timing)."""
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        backend = "nccl" if args.impl == "ours" else "gloo"
+        if backend == "nccl":
+            torch.cuda.set_device(local)
+        dist.init_process_group(backend=backend)
+        pg = dist
+    return rank, world, local, pg
+
+
+def barrier(pg, device=None):
+    if pg is not None:
+        if device is not None:
+            pg.barrier(device_ids=[device])
+        else:
+            pg.barrier()
+
+
+def max_over_ranks(pg, value: float, device=None) -> float:
+    if pg is None:
+        return value
+    import torch
+    t = torch.tensor([value], dtype=torch.float64,
+                     device=f"cuda:{device}" if device is not None else "cpu")
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+class Clocks:
+    """nvidia-smi sampling during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,"
+             "clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu: int):
+        self.gpu = gpu
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        try:
+            fd, self.path = tempfile.mkstemp(suffix=".csv")
+            os.close(fd)
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except (OSError, FileNotFoundError):
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        rows = []
+        for line in open(self.path):
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 9:
+                rows.append(parts)
+        os.unlink(self.path)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = sorted(float(r[1]) for r in rows if r[1].replace(".", "").isdigit())
+        mx = [float(r[2]) for r in rows if r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                 "sw_power_cap"]
+        reasons = sorted({names[i] for r in rows for i in range(4)
+                          if r[5 + i].lower() == "active"})
+        return {"sm_mhz": sm[len(sm) // 2] if sm else None,
+                "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(rows)}
+
+
+def workload(n: int):
+    from jetgpu import scenes
+    return scenes.flip_first_substep(n, box_hi=(0.3, 0.8, 1.0),
+                                     sphere=((0.6, 0.2, 0.5), 0.15))
+
+
+def solver_params(precision: str):
+    """GPU MGPCG settings: FdmMgpcgSolver3(200, 6, 2, 2, 10, 2, 1e-6, 1.0,
+    true). Two symmetric red-black sweeps per level and a masked coarse
+    residual give mesh-independent convergence (5-8 iterations)."""
+    return dict(numberOfCgIter=200, maxNumberOfLevels=6,
+                numberOfRestrictionIter=2, numberOfCorrectionIter=2,
+                numberOfCoarsestIter=10, numberOfFinalIter=2,
+                maxTolerance=TOL, sorFactor=1.0, useRedBlackOrdering=True,
+                precision=precision)
+
+
+def peaks() -> dict:
+    path = os.path.join(REPO, "MEASURED_PEAKS.json")
+    if os.path.exists(path):
+        d = json.load(open(path))
+        return {"hbm_gbs": d.get("hbm_gbs"), "source": "measured"}
+    return {"hbm_gbs": 6800.0, "source": "fallback"}
+
+
+def traffic_per_launch(kernel: str, n: int):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary
+    (profiles/traffic.json), scaled by cells to this resolution; None when
+    no capture covers the kernel."""
+    path = os.path.join(REPO, "profiles", "traffic.json")
+    if not os.path.exists(path):
+        return None
+    rec = json.load(open(path)).get(kernel)
+    if not rec:
+        return None
+    return rec["dram_bytes_per_launch"] * (n ** 3) / float(rec["cells"])
+
+
+def run_ours(args, rank, world, local, pg):
+    import ctypes as C
+    import numpy as np
+    import torch
+    import jetgpu
+
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    n = args.n
+    h = 1.0 / n
+    sc = workload(n)
+    solver = jetgpu.FdmMgpcgSolver3(**solver_params(args.precision),
+                                    device=local)
+    grid = jetgpu.Grid()
+    grid.res[:] = (n, n, n)
+    grid.spacing[:] = (h, h, h)
+    grid.origin[:] = (0.0, 0.0, 0.0)
+
+    # Device-resident inputs (the resident FLIP solver's layout: FP64 faces
+    # and cell-centred SDF grids).
+    d = {k: torch.from_numpy(np.ascontiguousarray(sc[k])).to(dev)
+         for k in ("u", "v", "w", "boundary_sdf", "fluid_sdf")}
+    out = {k: torch.empty_like(d[k]) for k in ("u", "v", "w")}
+    p_out = torch.empty((n, n, n), dtype=torch.float64, device=dev)
+
+    def field(t):
+        f = jetgpu.ScalarField()
+        f.kind = 1
+        f.data = t.data_ptr()
+        f.res[:] = (n, n, n)
+        f.origin[:] = (0.5 * h,) * 3
+        f.spacing[:] = (h, h, h)
+        return f
+
+    bsdf, fsdf = field(d["boundary_sdf"]), field(d["fluid_sdf"])
+    stats = jetgpu.SolveStats()
+
+    def solve_device():
+        return jetgpu.solve_pressure_device(solver, grid, d["u"], d["v"],
+                                            d["w"], bsdf, fsdf, out["u"],
+                                            out["v"], out["w"], p_out,
+                                            stats=stats)
+
+    for _ in range(args.warmup):
+        solve_device()
+    stream = torch.cuda.ExternalStream(solver.stream(), device=dev)
+    clocks = Clocks(local)
+    iters, rel = [], []
+    barrier(pg, local)
+    torch.cuda.synchronize()
+    clocks.start()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        solve_device()
+        iters.append(stats.iterations)
+        rel.append(stats.relative_residual)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ck = clocks.stop()
+    barrier(pg, local)
+    ms = e0.elapsed_time(e1) / args.steps
+    ms = max_over_ranks(pg, ms, local)
+    setup_ms, solve_ms = stats.setup_ms, stats.solve_ms
+
+    # Second pass of the same K solves with every launch bracketed by events
+    # on the library stream: per-kernel durations and launch counts.
+    solver.profile(True)
+    for _ in range(args.steps):
+        solve_device()
+    prof = solver.profile_read()
+    solver.profile(False)
+    launches = sum(k["launches"] for k in prof)
+    top = max(prof, key=lambda k: k["total_ms"])
+    total_prof_ms = sum(k["total_ms"] for k in prof)
+    pk = peaks()
+    achieved = (top["bytes"] / top["launches"]) / (
+        top["total_ms"] / top["launches"] * 1e-3) / 1e9
+    traffic = traffic_per_launch(top["name"], n)
+    roofline = {
+        "kernel": top["name"], "bound": "hbm",
+        "achieved": round(achieved, 1), "peak": pk["hbm_gbs"],
+        "unit": "GB/s", "frac": round(achieved / pk["hbm_gbs"], 3),
+        "peak_source": pk["source"],
+        "algorithmic_bytes_per_launch": top["bytes"] / top["launches"],
+        "avg_launch_us": round(top["total_ms"] / top["launches"] * 1e3, 2),
+        "share": round(top["total_ms"] / total_prof_ms, 3),
+        "traffic": traffic,
+    }
+    # Whole-solve roofline: algorithmic bytes of every launch / solve time.
+    solve_bytes = sum(k["bytes"] for k in prof) / args.steps
+    whole = solve_bytes / (ms * 1e-3) / 1e9
+
+    # End-to-end through the host-pointer C ABI with pinned host buffers.
+    pin = {k: torch.from_numpy(np.ascontiguousarray(sc[k])).pin_memory()
+           for k in ("u", "v", "w", "boundary_sdf", "fluid_sdf")}
+    hout = {k: torch.empty_like(pin[k]).pin_memory() for k in ("u", "v", "w")}
+    vel = jetgpu.FaceCenteredGrid3((n, n, n), (h, h, h), (0, 0, 0),
+                                   pin["u"].numpy(), pin["v"].numpy(),
+                                   pin["w"].numpy())
+    outg = jetgpu.FaceCenteredGrid3((n, n, n), (h, h, h), (0, 0, 0),
+                                    hout["u"].numpy(), hout["v"].numpy(),
+                                    hout["w"].numpy())
+    ps = jetgpu.GridFractionalSinglePhasePressureSolver3(solver)
+    cg = lambda t: jetgpu.CellCenteredScalarGrid3((n, n, n), (h, h, h),
+                                                  (0, 0, 0), t.numpy())
+    bg, fg = cg(pin["boundary_sdf"]), cg(pin["fluid_sdf"])
+    for _ in range(max(1, args.warmup)):
+        ps.solve(vel, 1 / 60, outg, bg, None, fg)
+    barrier(pg, local)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(args.steps):
+        ps.solve(vel, 1 / 60, outg, bg, None, fg)
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e2e_ms = max_over_ranks(pg, e0.elapsed_time(e1) / args.steps, local)
+    h2d = sum(pin[k].numel() * 8 for k in pin)
+    d2h = sum(hout[k].numel() * 8 for k in hout) + n ** 3 * 8
+    return dict(ms=ms, e2e_ms=e2e_ms, h2d=h2d, d2h=d2h, clocks=ck,
+                iters=iters, rel=rel, roofline=roofline, launches=launches,
+                whole_gbs=whole, solve_bytes=solve_bytes, profile=prof,
+                setup_ms=setup_ms, solve_ms=solve_ms, peak=pk)
+
+
+def cpu_reference():
+    """The reference's CPU algorithm on this host: the compiled reference
+    when it exists here, else the oracle port (bit-exact with it)."""
+    import oracle
+    kind = "port"
+    o = None
+    try:
+        if os.path.exists(oracle.REF_SO):
+            o = oracle.Oracle(oracle.REF_SO)
+            kind = "reference"
+    except OSError:
+        o = None
+    if o is None:
+        o = oracle.port()
+    threads = os.cpu_count() or 1
+    o.set_threads(threads)
+    return o, kind, threads
+
+
+# The reference's MGPCG as the reference's configs install it
+# (FdmMgpcgSolver3(100, L, 5, 5, 20, 20, tol, 1.5, true)).
+REF_PARAMS = dict(max_cg_iter=100, max_levels=5, restrict_iter=5,
+                  correct_iter=5, coarsest_iter=20, final_iter=20,
+                  tolerance=TOL, sor=1.5, red_black=True)
+
+
+def cpu_solve(o, n, sc):
+    """One full reference pressure solve (weights, system, MGPCG to its own
+    termination, gradient). Returns (seconds, iterations, true relative
+    residual of the returned pressure)."""
+    import numpy as np
+    import oracle
+    h = (1.0 / n,) * 3
+    t = time.perf_counter()
+    r = o.pressure_solve((n,) * 3, h, (0, 0, 0), sc["u"], sc["v"], sc["w"],
+                         sc["boundary_sdf"], sc["fluid_sdf"],
+                         oracle.MgParams(**REF_PARAMS))
+    dt = time.perf_counter() - t
+    A = o.level(0, "A", (n,) * 3)
+    b = o.level(0, "b", (n,) * 3)
+    res = o.residual(A, r["p"], b)
+    return dt, r["iters"], float(np.linalg.norm(res) / np.linalg.norm(b))
+
+
+def cpu_baseline(n: int, steps: int = 1, warmup: int = 0):
+    """ms per reference pressure solve on all host cores. At 256^3 the
+    reference's MGPCG stops after a few iterations when r.z turns
+    non-positive (its V-cycle is not symmetric), so the solve it returns is
+    far from 1e-6; the residual it reaches is reported beside the time."""
+    sc = workload(n)
+    o, kind, threads = cpu_reference()
+    for _ in range(warmup):
+        cpu_solve(o, n, sc)
+    times, its, rel = [], None, None
+    for _ in range(steps):
+        dt, its, rel = cpu_solve(o, n, sc)
+        times.append(dt * 1e3)
+    value = sum(times) / len(times)
+    sample = (f"full {n}^3 pressure solve with the reference's "
+              f"FdmMgpcgSolver3(100,5,5,5,20,20,1e-6,1.5,true): {its} MGPCG "
+              f"iterations until its own stop, true relative residual "
+              f"{rel:.2e}; mean of {steps} solve(s)")
+    return dict(value=value, unit="ms/solve", cores=threads, kind=kind,
+                sample=sample, iterations=its, relative_residual=rel)
+
+
+def run_reference(args, rank, world, pg):
+    if rank != 0:
+        return None
+    cb = cpu_baseline(args.n, steps=args.steps, warmup=args.warmup)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": cb["value"],
+        "unit": "ms/solve", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": cb["value"],
+        "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (seeded scene, no dataset)",
+        "config": {"workload": f"{args.n}^3 FLIP dam break, first sub-step "
+                               "pressure solve (sphere obstacle)",
+                   "grid": args.n, "tolerance": TOL,
+                   "solver": "FdmMgpcgSolver3(100,5,5,5,20,20,1e-6,1.5,true)"},
+        "cpu_baseline": {k: cb[k] for k in ("value", "unit", "cores", "kind",
+                                            "sample")},
+        "reference_relative_residual": cb["relative_residual"],
+        "reference_iterations": cb["iterations"],
+        "e2e": {"value": cb["value"], "unit": "ms/solve",
+                "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    return line
+
+
+def main():
+    args = parse_args()
+    rank, world, local, pg = dist_setup(args)
+    if args.impl == "reference":
+        line = run_reference(args, rank, world, pg)
+        if line is not None:
+            print(json.dumps(line), flush=True)
+        return
+    r = run_ours(args, rank, world, local, pg)
+    cb = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cb = cpu_baseline(args.n, steps=1)
+    if rank != 0:
+        return
+    iters = r["iters"]
+    line = {
+        "metric": METRIC, "value": round(r["ms"], 3), "unit": "ms/solve",
+        "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": round(r["ms"], 3), "higher_is_better": False,
+        "scaling": "weak", "vs_baseline": None,
+        "dtype": {"fp32": "f32 (f64 reductions/refinement)",
+                  "fp64": "f64 (f32 V-cycle)",
+                  "mixed": "f32/bf16 (f64 reductions/refinement)"}[args.precision],
+        "data": "synthetic (seeded scene, no dataset)",
+        "config": {
+            "workload": f"{args.n}^3 FLIP dam break, first sub-step pressure "
+                        "solve (weights + system + MGPCG + gradient), sphere "
+                        "obstacle",
+            "grid": args.n, "tolerance": TOL, "precision": args.precision,
+            "solver": "MGPCG(200,6,2,2,10,2,1e-6,1.0,red-black), masked "
+                      "symmetric V-cycle",
+            "parallelism": f"replicas x{world}",
+            "l2": "inputs and solver state >> L2 (no flush)",
+            "roofline_timing": "per-launch CUDA events on the library stream "
+                               "over a second pass of the K solves",
+        },
+        "iterations_per_solve": iters[-1] if iters else None,
+        "relative_residual": max(r["rel"]) if r["rel"] else None,
+        "steps_per_s": round(1000.0 / r["ms"], 2),
+        "setup_ms": round(r["setup_ms"], 3),
+        "solve_ms": round(r["solve_ms"], 3),
+        "whole_solve_gbs": round(r["whole_gbs"], 1),
+        "whole_solve_frac": round(r["whole_gbs"] / r["peak"]["hbm_gbs"], 3),
+        "roofline": r["roofline"],
+        "e2e": {"value": round(r["e2e_ms"], 3), "unit": "ms/solve",
+                "h2d_bytes_per_step": r["h2d"], "d2h_bytes_per_step": r["d2h"]},
+        "gpu_launches": r["launches"],
+        "clocks": r["clocks"],
+        "kernels": [{"name": k["name"], "launches": k["launches"],
+                     "ms": round(k["total_ms"], 3)} for k in
+                    sorted(r["profile"], key=lambda k: -k["total_ms"])],
+    }
+    if cb is not None:
+        line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores",
+                                                   "kind", "sample")}
+    print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -350,6 +350,15 @@ void jetgpu_destroy(jetgpu_ctx* c) {
     for (auto& e : c->ev)
         if (e) cudaEventDestroy(e);
     for (auto& e : c->prof_ev) cudaEventDestroy(e);
+    {
+        SampleTables& T = c->tabs;
+        release(&T.idx);
+        release(&T.frac);
+        release(&T.slot);
+        release(&T.sidx);
+        release(&T.sfrac);
+        release(&T.node);
+    }
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
@@ -784,7 +793,8 @@ const char* kernel_class_name(int cls) {
         "rb_sweep_fused_l0", "rb_sweep_fused_coarse", "rb_half_l0",
         "rb_half_coarse", "coarsest", "residual32", "restrict",
         "correct", "spmv_dot", "update_xr", "dot_rz", "update_d",
-        "residual64", "accumulate", "build", "gradient", "p2g", "g2p",
+        "residual64", "accumulate", "weights", "pyramid", "system",
+        "gradient", "p2g", "g2p",
         "unet"};
     return (cls >= 0 && cls < K_CLASS_COUNT) ? names[cls] : "?";
 }

@@ -14,6 +14,10 @@
 #include "ctx.h"
 
 #include <cfloat>
+#include <cstring>
+#include <map>
+#include <utility>
+#include <vector>
 
 namespace jg {
 namespace {
@@ -355,7 +359,12 @@ __global__ void k_build_system(Dims n, double hx, double hy, double hz,
             } else if (u) {
                 bb -= w[wB] * ihz;
             }
-            if (u) {
+            if (u && !su && !sv && !sw) {
+                // Static collider: every term of the moving-boundary sum is
+                // (1 - w) * 0 * invH = +0, so the sum is +0 and adding it
+                // only turns -0 into +0 — exactly what this does.
+                bb = bb + 0.0;
+            } else if (u) {
                 // Moving-boundary contribution (:241-255), evaluated as the
                 // reference's single left-to-right expression.
                 const double sR = su ? su[uR] : 0.0, sL = su ? su[uL] : 0.0;
@@ -436,6 +445,286 @@ __global__ void k_apply_gradient(Dims n, double ihx, double ihy, double ihz,
     }
 }
 
+// ---------------------------------------------------------------------------
+// Separable sampling tables.
+//
+// Every sample position of buildWeights is a per-axis expression: the
+// x coordinate of a u-face corner depends on i alone, and so on. The
+// barycentric (index, fraction) pair of each coordinate is therefore computed
+// once per axis and expression, with the reference's arithmetic, instead of
+// twelve times per cell. Corner points shared by several faces resolve to the
+// same (index, fraction) triple; the host dedupes the triples into "slots",
+// every slot triple is sampled once into a node grid, and the face kernels
+// look their four corners up. Because a trilinear sample depends only on its
+// (index, fraction) triple and the data, the result is bit-identical to
+// sampling each corner directly.
+//
+// Table kinds per axis a (n = grid resolution along a):
+//   N: face-normal coordinate   (o_a + 0.5*0.0) + h_a*i + 0.0,     i in [0,n]
+//   M: tangential, lower corner (o_a + 0.5*h_a) + h_a*i + (-0.5*h_a), i < n
+//   P: tangential, upper corner (o_a + 0.5*h_a) + h_a*i + 0.5*h_a,    i < n
+//   C: cell centre              o_a + h_a*(i + 0.5),                  i < n
+
+__device__ __forceinline__ double trilerp_at(const double* __restrict__ d,
+                                             const int* res, int i, double fx,
+                                             int j, double fy, int k,
+                                             double fz) {
+    const int ip1 = min(i + 1, res[0] - 1);
+    const int jp1 = min(j + 1, res[1] - 1);
+    const int kp1 = min(k + 1, res[2] - 1);
+    const int rx = res[0], ry = res[1];
+    const double f000 = d[lin(i, j, k, rx, ry)], f100 = d[lin(ip1, j, k, rx, ry)];
+    const double f010 = d[lin(i, jp1, k, rx, ry)], f110 = d[lin(ip1, jp1, k, rx, ry)];
+    const double f001 = d[lin(i, j, kp1, rx, ry)], f101 = d[lin(ip1, j, kp1, rx, ry)];
+    const double f011 = d[lin(i, jp1, kp1, rx, ry)], f111 = d[lin(ip1, jp1, kp1, rx, ry)];
+    const double b0 = lerpd(lerpd(f000, f100, fx), lerpd(f010, f110, fx), fy);
+    const double b1 = lerpd(lerpd(f001, f101, fx), lerpd(f011, f111, fx), fy);
+    return lerpd(b0, b1, fz);
+}
+
+struct TabLayout {
+    int off[3][4];  // [axis][N,M,P,C] entry offsets
+    int total;
+};
+
+__global__ void k_axis_tables(GridDesc g, FieldDesc B, FieldDesc F,
+                              TabLayout L, int* __restrict__ idx,
+                              double* __restrict__ frac) {
+    for (int e = blockIdx.x * blockDim.x + threadIdx.x; e < L.total;
+         e += gridDim.x * blockDim.x) {
+        int a = 0, kind = 0;
+        for (int aa = 0; aa < 3; ++aa)
+            for (int kk = 0; kk < 4; ++kk)
+                if (e >= L.off[aa][kk]) {
+                    a = aa;
+                    kind = kk;
+                }
+        const int i = e - L.off[a][kind];
+        const double o = g.origin[a], h = g.spacing[a];
+        double coord;
+        if (kind == 0) coord = (o + 0.5 * 0.0) + h * (double)i + 0.0;
+        else if (kind == 1) coord = (o + 0.5 * h) + h * (double)i + -0.5 * h;
+        else if (kind == 2) coord = (o + 0.5 * h) + h * (double)i + 0.5 * h;
+        else coord = o + h * ((double)i + 0.5);
+        const FieldDesc& S = (kind == 3) ? F : B;
+        if (S.kind != 1) {
+            idx[e] = 0;
+            frac[e] = 0.0;
+            continue;
+        }
+        const double nrm = (coord - S.origin[a]) / S.spacing[a];
+        int ii;
+        double ff;
+        barycentric(nrm, S.res[a] - 1, &ii, &ff);
+        idx[e] = ii;
+        frac[e] = ff;
+    }
+}
+
+// One trilinear sample per slot triple (sx fastest).
+__global__ void k_node_grid(FieldDesc B, const int* __restrict__ sidx,
+                            const double* __restrict__ sfrac, int3 soff,
+                            int3 S, double* __restrict__ node) {
+    const long N = (long)S.x * S.y * S.z;
+    for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < N;
+         c += (long)gridDim.x * blockDim.x) {
+        const int a = (int)(c % S.x), b = (int)((c / S.x) % S.y),
+                  z = (int)(c / ((long)S.x * S.y));
+        node[c] = trilerp_at(B.data, B.res, sidx[soff.x + a], sfrac[soff.x + a],
+                             sidx[soff.y + b], sfrac[soff.y + b],
+                             sidx[soff.z + z], sfrac[soff.z + z]);
+    }
+}
+
+// Face weights from the node grid. slot[] maps a table entry to its slot.
+__global__ void k_face_weights_nodes(float* __restrict__ wgt, int axis,
+                                     Dims fn, const int* __restrict__ slot,
+                                     TabLayout L, int3 S,
+                                     const double* __restrict__ node) {
+    const long N = fn.count();
+    for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < N;
+         c += (long)gridDim.x * blockDim.x) {
+        const int i = (int)(c % fn.x);
+        const int j = (int)((c / fn.x) % fn.y);
+        const int k = (int)(c / ((long)fn.x * fn.y));
+        // Lower/upper slot along each axis: N for the normal axis (same for
+        // both), M/P for the tangential axes.
+        const int q[3] = {i, j, k};
+        int lo[3], hi[3];
+        for (int a = 0; a < 3; ++a) {
+            if (a == axis) {
+                lo[a] = hi[a] = slot[L.off[a][0] + q[a]];
+            } else {
+                lo[a] = slot[L.off[a][1] + q[a]];
+                hi[a] = slot[L.off[a][2] + q[a]];
+            }
+        }
+        auto at = [&](int x, int y, int z) {
+            return node[x + (long)S.x * (y + (long)S.y * z)];
+        };
+        double p0, p1, p2, p3;
+        if (axis == 0) {  // (0,-y,-z) (0,+y,-z) (0,-y,+z) (0,+y,+z)
+            p0 = at(lo[0], lo[1], lo[2]);
+            p1 = at(lo[0], hi[1], lo[2]);
+            p2 = at(lo[0], lo[1], hi[2]);
+            p3 = at(lo[0], hi[1], hi[2]);
+        } else if (axis == 1) {  // (-x,0,-z) (-x,0,+z) (+x,0,-z) (+x,0,+z)
+            p0 = at(lo[0], lo[1], lo[2]);
+            p1 = at(lo[0], lo[1], hi[2]);
+            p2 = at(hi[0], lo[1], lo[2]);
+            p3 = at(hi[0], lo[1], hi[2]);
+        } else {  // (-x,-y,0) (-x,+y,0) (+x,-y,0) (+x,+y,0)
+            p0 = at(lo[0], lo[1], lo[2]);
+            p1 = at(lo[0], hi[1], lo[2]);
+            p2 = at(hi[0], lo[1], lo[2]);
+            p3 = at(hi[0], hi[1], lo[2]);
+        }
+        wgt[c] = face_weight(p0, p1, p2, p3);
+    }
+}
+
+// Fluid SDF at cell centres from the C tables.
+__global__ void k_sample_fluid_tab(float* __restrict__ phi, Dims n,
+                                   FieldDesc F, const int* __restrict__ idx,
+                                   const double* __restrict__ frac,
+                                   TabLayout L) {
+    const long N = n.count();
+    const int ox = L.off[0][3], oy = L.off[1][3], oz = L.off[2][3];
+    for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < N;
+         c += (long)gridDim.x * blockDim.x) {
+        const int i = (int)(c % n.x);
+        const int j = (int)((c / n.x) % n.y);
+        const int k = (int)(c / ((long)n.x * n.y));
+        phi[c] = (float)trilerp_at(F.data, F.res, idx[ox + i], frac[ox + i],
+                                   idx[oy + j], frac[oy + j], idx[oz + k],
+                                   frac[oz + k]);
+    }
+}
+
+bool same_geom(const FieldDesc& a, const FieldDesc& b) {
+    if (a.kind != b.kind) return false;
+    for (int d = 0; d < 3; ++d)
+        if (a.res[d] != b.res[d] || a.origin[d] != b.origin[d] ||
+            a.spacing[d] != b.spacing[d])
+            return false;
+    return true;
+}
+
+bool same_grid(const GridDesc& a, const GridDesc& b) {
+    for (int d = 0; d < 3; ++d)
+        if (a.res[d] != b.res[d] || a.origin[d] != b.origin[d] ||
+            a.spacing[d] != b.spacing[d])
+            return false;
+    return true;
+}
+
+// Builds (or reuses) the axis tables, slots and node-grid geometry for the
+// given grid and field geometries.
+jetgpu_status ensure_tables(Ctx* c, const GridDesc& g, const FieldDesc& B,
+                            const FieldDesc& F) {
+    SampleTables& T = c->tabs;
+    if (T.valid && same_grid(T.g, g) && same_geom(T.B, B) && same_geom(T.F, F))
+        return JETGPU_OK;
+    T.valid = false;
+    TabLayout L;
+    int off = 0;
+    for (int a = 0; a < 3; ++a) {
+        const int n = g.res[a];
+        L.off[a][0] = off; off += n + 1;
+        L.off[a][1] = off; off += n;
+        L.off[a][2] = off; off += n;
+        L.off[a][3] = off; off += n;
+    }
+    L.total = off;
+    if ((size_t)off > T.cap) {
+        if (T.idx) cudaFree(T.idx);
+        if (T.frac) cudaFree(T.frac);
+        if (T.slot) cudaFree(T.slot);
+        if (T.sidx) cudaFree(T.sidx);
+        if (T.sfrac) cudaFree(T.sfrac);
+        T.idx = nullptr; T.frac = nullptr; T.slot = nullptr;
+        T.sidx = nullptr; T.sfrac = nullptr; T.cap = 0;
+        JG_CUDA(c, cudaMalloc((void**)&T.idx, off * sizeof(int)));
+        JG_CUDA(c, cudaMalloc((void**)&T.frac, off * sizeof(double)));
+        JG_CUDA(c, cudaMalloc((void**)&T.slot, off * sizeof(int)));
+        JG_CUDA(c, cudaMalloc((void**)&T.sidx, off * sizeof(int)));
+        JG_CUDA(c, cudaMalloc((void**)&T.sfrac, off * sizeof(double)));
+        T.cap = off;
+    }
+    k_axis_tables<<<blocks_for(off), kThreads, 0, c->stream>>>(g, B, F, L,
+                                                               T.idx, T.frac);
+    JG_CUDA(c, cudaGetLastError());
+    std::vector<int> hidx(off);
+    std::vector<double> hfrac(off);
+    JG_CUDA(c, cudaMemcpyAsync(hidx.data(), T.idx, off * sizeof(int),
+                               cudaMemcpyDeviceToHost, c->stream));
+    JG_CUDA(c, cudaMemcpyAsync(hfrac.data(), T.frac, off * sizeof(double),
+                               cudaMemcpyDeviceToHost, c->stream));
+    JG_CUDA(c, cudaStreamSynchronize(c->stream));
+    // Dedupe N/M/P entries of each axis by exact (index, fraction).
+    std::vector<int> hslot(off, 0), sidx(off, 0);
+    std::vector<double> sfrac(off, 0.0);
+    int soff[3], nslot[3], used = 0;
+    for (int a = 0; a < 3; ++a) {
+        std::map<std::pair<int, uint64_t>, int> seen;
+        soff[a] = used;
+        for (int e = L.off[a][0]; e < L.off[a][3]; ++e) {
+            uint64_t bits;
+            std::memcpy(&bits, &hfrac[e], 8);
+            auto key = std::make_pair(hidx[e], bits);
+            auto it = seen.find(key);
+            int s;
+            if (it == seen.end()) {
+                s = (int)seen.size();
+                seen.emplace(key, s);
+                sidx[used + s] = hidx[e];
+                sfrac[used + s] = hfrac[e];
+            } else {
+                s = it->second;
+            }
+            hslot[e] = s;
+        }
+        nslot[a] = (int)seen.size();
+        used += nslot[a];
+    }
+    JG_CUDA(c, cudaMemcpyAsync(T.slot, hslot.data(), off * sizeof(int),
+                               cudaMemcpyHostToDevice, c->stream));
+    JG_CUDA(c, cudaMemcpyAsync(T.sidx, sidx.data(), used * sizeof(int),
+                               cudaMemcpyHostToDevice, c->stream));
+    JG_CUDA(c, cudaMemcpyAsync(T.sfrac, sfrac.data(), used * sizeof(double),
+                               cudaMemcpyHostToDevice, c->stream));
+    const size_t nodes = (size_t)nslot[0] * nslot[1] * nslot[2];
+    const size_t cells = (size_t)(g.res[0] + 1) * (g.res[1] + 1) * (g.res[2] + 1);
+    T.use_nodes = nodes <= 4 * cells;
+    if (T.use_nodes && nodes > T.node_cap) {
+        if (T.node) cudaFree(T.node);
+        T.node = nullptr;
+        T.node_cap = 0;
+        JG_CUDA(c, cudaMalloc((void**)&T.node, nodes * sizeof(double)));
+        T.node_cap = nodes;
+    }
+    JG_CUDA(c, cudaStreamSynchronize(c->stream));
+    for (int a = 0; a < 3; ++a) {
+        for (int k = 0; k < 4; ++k) T.off[a][k] = L.off[a][k];
+        T.soff[a] = soff[a];
+        T.nslot[a] = nslot[a];
+    }
+    T.total = L.total;
+    T.g = g;
+    T.B = B;
+    T.F = F;
+    T.valid = true;
+    return JETGPU_OK;
+}
+
+TabLayout layout_of(const SampleTables& T) {
+    TabLayout L;
+    for (int a = 0; a < 3; ++a)
+        for (int k = 0; k < 4; ++k) L.off[a][k] = T.off[a][k];
+    L.total = T.total;
+    return L;
+}
+
 }  // namespace
 
 jetgpu_status build_weights(Ctx* c, const GridDesc& g, const FieldDesc& bsdf,
@@ -443,17 +732,51 @@ jetgpu_status build_weights(Ctx* c, const GridDesc& g, const FieldDesc& bsdf,
     const unsigned nl = c->built_levels;
     Level& L0 = c->levels[0];
     const Dims n = L0.n;
-    Prof pr(c, K_BUILD, (8.0 + 4.0) * (double)n.count() + 3.0 * 4.0 * n.count());
-    k_sample_fluid<<<blocks_for(n.count()), kThreads, 0, c->stream>>>(
-        L0.phi, n, g, fsdf);
     const Dims fu{n.x + 1, n.y, n.z}, fv{n.x, n.y + 1, n.z},
         fw{n.x, n.y, n.z + 1};
-    k_face_weights<<<blocks_for(fu.count()), kThreads, 0, c->stream>>>(
-        L0.uw, 0, fu, g, bsdf);
-    k_face_weights<<<blocks_for(fv.count()), kThreads, 0, c->stream>>>(
-        L0.vw, 1, fv, g, bsdf);
-    k_face_weights<<<blocks_for(fw.count()), kThreads, 0, c->stream>>>(
-        L0.ww, 2, fw, g, bsdf);
+    if (bsdf.kind == 1 || fsdf.kind == 1) {
+        jetgpu_status s = ensure_tables(c, g, bsdf, fsdf);
+        if (s != JETGPU_OK) return s;
+    }
+    const SampleTables& T = c->tabs;
+    const TabLayout TL = layout_of(T);
+    {
+        Prof pr(c, K_WEIGHTS, (8.0 + 4.0) * (double)n.count());
+        if (fsdf.kind == 1)
+            k_sample_fluid_tab<<<blocks_for(n.count()), kThreads, 0,
+                                 c->stream>>>(L0.phi, n, fsdf, T.idx, T.frac,
+                                              TL);
+        else
+            k_sample_fluid<<<blocks_for(n.count()), kThreads, 0, c->stream>>>(
+                L0.phi, n, g, fsdf);
+    }
+    {
+        Prof pr(c, K_WEIGHTS, (8.0 + 3.0 * 4.0) * (double)n.count());
+        if (bsdf.kind == 1 && T.use_nodes) {
+            const int3 S = make_int3(T.nslot[0], T.nslot[1], T.nslot[2]);
+            const int3 so = make_int3(T.soff[0], T.soff[1], T.soff[2]);
+            const long nodes = (long)S.x * S.y * S.z;
+            k_node_grid<<<blocks_for(nodes), kThreads, 0, c->stream>>>(
+                bsdf, T.sidx, T.sfrac, so, S, T.node);
+            k_face_weights_nodes<<<blocks_for(fu.count()), kThreads, 0,
+                                   c->stream>>>(L0.uw, 0, fu, T.slot, TL, S,
+                                                T.node);
+            k_face_weights_nodes<<<blocks_for(fv.count()), kThreads, 0,
+                                   c->stream>>>(L0.vw, 1, fv, T.slot, TL, S,
+                                                T.node);
+            k_face_weights_nodes<<<blocks_for(fw.count()), kThreads, 0,
+                                   c->stream>>>(L0.ww, 2, fw, T.slot, TL, S,
+                                                T.node);
+        } else {
+            k_face_weights<<<blocks_for(fu.count()), kThreads, 0, c->stream>>>(
+                L0.uw, 0, fu, g, bsdf);
+            k_face_weights<<<blocks_for(fv.count()), kThreads, 0, c->stream>>>(
+                L0.vw, 1, fv, g, bsdf);
+            k_face_weights<<<blocks_for(fw.count()), kThreads, 0, c->stream>>>(
+                L0.ww, 2, fw, g, bsdf);
+        }
+    }
+    Prof pyr(c, K_PYRAMID, 0.0);
     for (unsigned l = 1; l < nl; ++l) {
         const Level& F = c->levels[l - 1];
         Level& C = c->levels[l];
@@ -490,7 +813,7 @@ jetgpu_status build_system(Ctx* c, const GridDesc& g, const double* u,
         L.h[1] = hy;
         L.h[2] = hz;
         const bool top = (l == 0);
-        Prof pr(c, K_BUILD, (top ? 16.0 + 32.0 + 8.0 + 24.0 : 16.0 + 16.0) *
+        Prof pr(c, K_SYSTEM, (top ? 16.0 + 32.0 + 8.0 + 24.0 : 16.0 + 16.0) *
                                 (double)L.n.count());
         k_build_system<<<blocks_for(L.n.count()), kThreads, 0, c->stream>>>(
             L.n, hx, hy, hz, L.phi, L.uw, L.vw, L.ww, top ? u : nullptr,

@@ -47,6 +47,18 @@ __host__ __device__ __forceinline__ long lin(int i, int j, int k, int nx,
     return (long)i + (long)nx * ((long)j + (long)ny * k);
 }
 
+// (i, j, k) of linear index c with 32-bit arithmetic (grids have < 2^31
+// cells; 64-bit division costs several times more instructions).
+__device__ __forceinline__ void cell_ijk(long c, Dims n, int& i, int& j,
+                                         int& k) {
+    const unsigned cc = (unsigned)c, nx = (unsigned)n.x, ny = (unsigned)n.y;
+    const unsigned q = cc / nx;
+    i = (int)(cc - q * nx);
+    const unsigned r = q / ny;
+    j = (int)(q - r * ny);
+    k = (int)r;
+}
+
 // A scalar field: a constant or a grid sampled with Jet's trilinear rule.
 struct FieldDesc {
     int kind;

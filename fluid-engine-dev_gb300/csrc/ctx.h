@@ -46,7 +46,9 @@ enum KernelClass : int {
     K_UPDATE_D,       // d = z + b d
     K_RESIDUAL64,     // FP64 true residual
     K_ACCUMULATE,     // x64 += e
-    K_BUILD,          // weights + system build
+    K_WEIGHTS,        // fluid SDF sampling + face weights
+    K_PYRAMID,        // restriction of the weight/SDF pyramid
+    K_SYSTEM,         // matrix rows + rhs
     K_GRADIENT,       // pressure gradient
     K_P2G,
     K_G2P,
@@ -54,6 +56,26 @@ enum KernelClass : int {
     K_CLASS_COUNT
 };
 const char* kernel_class_name(int cls);
+
+// Per-axis exact sampling tables of buildWeights (see build.cu), cached per
+// grid/field geometry.
+struct SampleTables {
+    bool valid = false;
+    bool use_nodes = false;
+    GridDesc g{};
+    FieldDesc B{}, F{};
+    int off[3][4] = {};   // entry offsets [axis][N,M,P,C]
+    int total = 0;
+    int soff[3] = {}, nslot[3] = {};
+    size_t cap = 0;       // entries allocated
+    int* idx = nullptr;
+    double* frac = nullptr;
+    int* slot = nullptr;
+    int* sidx = nullptr;
+    double* sfrac = nullptr;
+    size_t node_cap = 0;
+    double* node = nullptr;
+};
 
 struct ProfRec {
     int cls;
@@ -112,6 +134,9 @@ struct Ctx {
 
     // Learned preconditioner (opaque; see unet.cu).
     void* unet = nullptr;
+
+    // Exact sampling tables of the weights build.
+    SampleTables tabs;
 
     // Live per-kernel profile: CUDA events recorded on `stream` around
     // launches while enabled.

@@ -118,9 +118,8 @@ __global__ void __launch_bounds__(kThreads)
     double acc = 0.0;
     for (long c = blockIdx.x * (long)kThreads + threadIdx.x; c < N;
          c += (long)gridDim.x * kThreads) {
-        const int i = (int)(c % n.x);
-        const int j = (int)((c / n.x) % n.y);
-        const int k = (int)(c / ((long)n.x * n.y));
+        int i, j, k;
+        cell_ijk(c, n, i, j, k);
         const V qv = apply7<V>(M, d, c, i, j, k, n);
         q[c] = qv;
         acc += (double)d[c] * (double)qv;
@@ -191,9 +190,8 @@ __global__ void __launch_bounds__(kThreads)
     double acc = 0.0;
     for (long c = blockIdx.x * (long)kThreads + threadIdx.x; c < N;
          c += (long)gridDim.x * kThreads) {
-        const int i = (int)(c % n.x);
-        const int j = (int)((c / n.x) % n.y);
-        const int k = (int)(c / ((long)n.x * n.y));
+        int i, j, k;
+        cell_ijk(c, n, i, j, k);
         const double rv = b[c] - apply7<double>(M, x, c, i, j, k, n);
         if (r) r[c] = rv;
         if (r32) r32[c] = (float)rv;
@@ -311,7 +309,11 @@ namespace fused {
 constexpr int TX = 64, TY = 8;          // tile (cells)
 constexpr int SX = TX + 8, SY = TY + 4; // staged plane: i0-4 .. i0+67, j0-2 .. j0+9
 constexpr int PLANE = SX * SY;          // 864 cells
-constexpr int XS = 4, AS = 3, BS = 2;   // ring depths (planes)
+// Ring depths (planes): in use at step t are x t-1..t+2, A t-1..t+1 and
+// b t..t+1; PD more slots each hold the prefetches for steps t+1..t+PD, so
+// every block keeps PD planes of loads in flight while it computes.
+constexpr int PD = 2;
+constexpr int XS = 4 + PD, AS = 3 + PD, BS = 2 + PD;
 constexpr size_t SMEM = (size_t)PLANE * (XS * 4 + AS * 16 + BS * 4);
 
 __device__ __forceinline__ int ring(int p, int m) { return ((p % m) + m) % m; }
@@ -322,9 +324,13 @@ __device__ __forceinline__ void cp16(void* smem, const void* gmem, bool valid) {
     asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s),
                  "l"(gmem), "r"(src));
 }
-__device__ __forceinline__ void cp_commit_wait() {
+__device__ __forceinline__ void cp_commit() {
     asm volatile("cp.async.commit_group;\n" ::);
-    asm volatile("cp.async.wait_group 0;\n" ::);
+}
+// Waits until at most `pending` committed groups are still in flight.
+template <int pending>
+__device__ __forceinline__ void cp_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(pending));
 }
 }  // namespace fused
 
@@ -344,85 +350,123 @@ __global__ void __launch_bounds__(256)
     const long sy = n.x, sz = (long)n.x * n.y;
     const int second = first ^ 1;
 
-    // Stage plane p of x / A / b (zero outside the domain).
+    // Per-thread copy descriptors. The in-plane offsets of a thread's 16-byte
+    // chunks are the same for every plane, so their index arithmetic is done
+    // once here; a plane load only adds the plane base.
+    // x and b: PLANE/4 = 216 chunks of 4 floats, one per thread below 216.
+    int vgo = 0, vso = 0;
+    bool vok = false;
+    if (tid < PLANE / 4) {
+        const int r = tid / (SX / 4), c4 = tid - r * (SX / 4);
+        const int gi = i0 - 4 + 4 * c4, gj = j0 - 2 + r;
+        vok = gi >= 0 && gi < n.x && gj >= 0 && gj < n.y;
+        vgo = vok ? gi + n.x * gj : 0;
+        vso = r * SX + 4 * c4;
+    }
+    // A: PLANE rows of 16 bytes, up to AM per thread.
+    constexpr int AM = (PLANE + 255) / 256;
+    int ago[AM];
+    bool aok[AM];
+#pragma unroll
+    for (int m = 0; m < AM; ++m) {
+        const int f = tid + 256 * m;
+        const int r = f / SX, c = f - r * SX;
+        const int gi = i0 - 4 + c, gj = j0 - 2 + r;
+        aok[m] = f < PLANE && gi >= 0 && gi < n.x && gj >= 0 && gj < n.y;
+        ago[m] = aok[m] ? gi + n.x * gj : 0;
+    }
+
+    // Stage plane p of x / A / b (zero-filled outside the domain, so the
+    // update below needs no bounds tests: an outside neighbour has x = 0 and
+    // a zero matrix row, exactly the reference's guarded terms,
+    // FdmBlas3::mvm, fdm_linear_system3.cpp:79-96).
     auto load_x = [&](int p) {
         float* dst = sx + ring(p, XS) * PLANE;
         if (xin == nullptr || p < 0 || p >= n.z) {
             for (int q = tid; q < PLANE; q += 256) dst[q] = 0.0f;
             return;
         }
-        for (int f = tid; f < PLANE / 4; f += 256) {
-            const int r = f / (SX / 4), c4 = f % (SX / 4);
-            const int gi = i0 - 4 + 4 * c4, gj = j0 - 2 + r;
-            const bool ok = gi >= 0 && gi < n.x && gj >= 0 && gj < n.y;
-            const float* src = ok ? xin + gi + sy * gj + sz * p : xin;
-            cp16(dst + r * SX + 4 * c4, src, ok);
+        if (tid < PLANE / 4) {
+            const float* base = xin + sz * p;
+            cp16(dst + vso, vok ? base + vgo : xin, vok);
         }
     };
     auto load_A = [&](int p) {
         float4* dst = sA + ring(p, AS) * PLANE;
         const bool pin = p >= 0 && p < n.z;
-        for (int f = tid; f < PLANE; f += 256) {
-            const int r = f / SX, c = f % SX;
-            const int gi = i0 - 4 + c, gj = j0 - 2 + r;
-            const bool ok = pin && gi >= 0 && gi < n.x && gj >= 0 && gj < n.y;
-            const float4* src = ok ? A + gi + sy * gj + sz * p : A;
-            cp16(dst + f, src, ok);
+        const float4* base = A + (pin ? sz * p : 0);
+#pragma unroll
+        for (int m = 0; m < AM; ++m) {
+            const int f = tid + 256 * m;
+            if (f < PLANE) cp16(dst + f, base + ago[m], pin && aok[m]);
         }
     };
     auto load_b = [&](int p) {
         float* dst = sb + ring(p, BS) * PLANE;
         const bool pin = p >= 0 && p < n.z;
-        for (int f = tid; f < PLANE / 4; f += 256) {
-            const int r = f / (SX / 4), c4 = f % (SX / 4);
-            const int gi = i0 - 4 + 4 * c4, gj = j0 - 2 + r;
-            const bool ok = pin && gi >= 0 && gi < n.x && gj >= 0 && gj < n.y;
-            const float* src = ok ? b + gi + sy * gj + sz * p : b;
-            cp16(dst + r * SX + 4 * c4, src, ok);
+        if (tid < PLANE / 4) {
+            const float* base = b + (pin ? sz * p : 0);
+            cp16(dst + vso, base + vgo, pin && vok);
         }
     };
-    // SOR update of local cell (ii, jj) in plane p; neighbours outside the
-    // domain contribute nothing (FdmBlas3 guards, fdm_linear_system3.cpp:79-96).
-    auto relax = [&](int ii, int jj, int p) -> float {
-        const int s = (jj + 2) * SX + (ii + 4);
-        const int gi = i0 + ii, gj = j0 + jj;
-        const float* xc = sx + ring(p, XS) * PLANE;
-        const float4* Ac = sA + ring(p, AS) * PLANE;
+    // SOR update at staged index s: xc/Ac/bc this plane, xdn/Adn the plane
+    // below, xup the plane above.
+    auto relax = [&](const float* xc, const float* xdn, const float* xup,
+                     const float4* Ac, const float4* Adn, const float* bc,
+                     int s) -> float {
         const float4 row = Ac[s];
-        float acc = 0.0f;
-        if (gi > 0) acc += Ac[s - 1].y * xc[s - 1];
-        if (gi + 1 < n.x) acc += row.y * xc[s + 1];
-        if (gj > 0) acc += Ac[s - SX].z * xc[s - SX];
-        if (gj + 1 < n.y) acc += row.z * xc[s + SX];
-        if (p > 0)
-            acc += sA[ring(p - 1, AS) * PLANE + s].w *
-                   sx[ring(p - 1, XS) * PLANE + s];
-        if (p + 1 < n.z) acc += row.w * sx[ring(p + 1, XS) * PLANE + s];
-        const float bb = sb[ring(p, BS) * PLANE + s];
-        return (1.0f - omega) * xc[s] + omega * (bb - acc) / row.x;
+        const float acc = Ac[s - 1].y * xc[s - 1] + row.y * xc[s + 1] +
+                          Ac[s - SX].z * xc[s - SX] + row.z * xc[s + SX] +
+                          Adn[s].w * xdn[s] + row.w * xup[s];
+        return (1.0f - omega) * xc[s] + omega * __fdividef(bc[s] - acc, row.x);
     };
 
+    // Step t needs x planes t..t+2, A planes t..t+1 and b plane t+1 staged.
+    // Group g holds the loads of step t0+g; groups for steps t+1..t+PD are
+    // in flight while step t computes (empty groups keep the count uniform).
     const int t0 = k0 - 2;
     load_x(t0);
     load_x(t0 + 1);
     load_A(t0);
+    for (int q = 0; q < PD; ++q) {
+        if (t0 + q < k1) {
+            load_x(t0 + q + 2);
+            load_A(t0 + q + 1);
+            load_b(t0 + q + 1);
+        }
+        fused::cp_commit();
+    }
     for (int t = t0; t < k1; ++t) {
-        load_x(t + 2);
-        load_A(t + 1);
-        load_b(t + 1);
-        fused::cp_commit_wait();
+        if (t + PD < k1) {
+            load_x(t + PD + 2);
+            load_A(t + PD + 1);
+            load_b(t + PD + 1);
+        }
+        fused::cp_commit();
+        fused::cp_wait<PD>();
         __syncthreads();
+        // Slot pointers of the planes this step touches.
+        float* xm1 = sx + ring(t - 1, XS) * PLANE;
+        float* x0 = sx + ring(t, XS) * PLANE;
+        float* x1 = sx + ring(t + 1, XS) * PLANE;
+        const float* x2 = sx + ring(t + 2, XS) * PLANE;
+        const float4* am1 = sA + ring(t - 1, AS) * PLANE;
+        const float4* a0 = sA + ring(t, AS) * PLANE;
+        const float4* a1 = sA + ring(t + 1, AS) * PLANE;
+        const float* b0 = sb + ring(t, BS) * PLANE;
+        const float* b1 = sb + ring(t + 1, BS) * PLANE;
         // (1) first colour of plane t+1 on tile + 1-cell ring.
         const int p1 = t + 1;
         if (p1 >= k0 - 1 && p1 <= k1 && p1 >= 0 && p1 < n.z) {
-            float* xp = sx + ring(p1, XS) * PLANE;
+            const int par = (first - p1 + 1) & 1;
             for (int q = tid; q < 33 * (TY + 2); q += 256) {
-                const int jj = q / 33 - 1;
-                const int ii = -1 + 2 * (q % 33) + ((first - jj - p1 + 1) & 1);
+                const int row = q / 33;
+                const int jj = row - 1;
+                const int ii = -1 + 2 * (q - 33 * row) + ((par - jj) & 1);
                 const int gi = i0 + ii, gj = j0 + jj;
                 if (gi < 0 || gi >= n.x || gj < 0 || gj >= n.y) continue;
-                const float v = relax(ii, jj, p1);
-                xp[(jj + 2) * SX + (ii + 4)] = v;
+                const int s = (jj + 2) * SX + (ii + 4);
+                x1[s] = relax(x1, x0, x2, a1, a0, b1, s);
             }
         }
         __syncthreads();
@@ -433,10 +477,10 @@ __global__ void __launch_bounds__(256)
             const int gi = i0 + ii, gj = j0 + jj;
             if (gi < n.x && gj < n.y) {
                 const int odd = ((ii + jj + t) & 1) != second;  // S cell at ii+odd
-                const float* xp = sx + ring(t, XS) * PLANE;
+                const float* xp = x0;
                 const int s = (jj + 2) * SX + (ii + 4);
                 float2 out;
-                const float vs = relax(ii + odd, jj, t);
+                const float vs = relax(x0, xm1, x1, a0, am1, b0, s + odd);
                 if (odd) {
                     out.x = xp[s];
                     out.y = vs;
@@ -459,9 +503,8 @@ __global__ void __launch_bounds__(kThreads)
     RowsF M{A};
     for (long c = blockIdx.x * (long)kThreads + threadIdx.x; c < N;
          c += (long)gridDim.x * kThreads) {
-        const int i = (int)(c % n.x);
-        const int j = (int)((c / n.x) % n.y);
-        const int k = (int)(c / ((long)n.x * n.y));
+        int i, j, k;
+        cell_ijk(c, n, i, j, k);
         r[c] = b[c] - apply7<float>(M, x, c, i, j, k, n);
     }
 }
@@ -481,9 +524,8 @@ __global__ void __launch_bounds__(kThreads)
     const float kern[4] = {0.125f, 0.375f, 0.375f, 0.125f};
     for (long t = blockIdx.x * (long)kThreads + threadIdx.x; t < N;
          t += (long)gridDim.x * kThreads) {
-        const int i = (int)(t % c.x);
-        const int j = (int)((t / c.x) % c.y);
-        const int k = (int)(t / ((long)c.x * c.y));
+        int i, j, k;
+        cell_ijk(t, c, i, j, k);
         int iI[4] = {i > 0 ? 2 * i - 1 : 2 * i, 2 * i, 2 * i + 1,
                      i + 1 < c.x ? 2 * i + 2 : 2 * i + 1};
         int jI[4] = {j > 0 ? 2 * j - 1 : 2 * j, 2 * j, 2 * j + 1,
@@ -516,9 +558,8 @@ __global__ void __launch_bounds__(kThreads)
     const long N = n.count();
     for (long t = blockIdx.x * (long)kThreads + threadIdx.x; t < N;
          t += (long)gridDim.x * kThreads) {
-        const int i = (int)(t % n.x);
-        const int j = (int)((t / n.x) % n.y);
-        const int k = (int)(t / ((long)n.x * n.y));
+        int i, j, k;
+        cell_ijk(t, n, i, j, k);
         const int ci = i >> 1, cj = j >> 1, ck = k >> 1;
         int i0, i1, j0, j1, k0, k1;
         float wi0, wi1, wj0, wj1, wk0, wk1;
@@ -608,7 +649,7 @@ bool fused_ok(const Level& L) {
 int fused_kz(const Ctx* c, const Level& L) {
     const long tiles = (long)((L.n.x + fused::TX - 1) / fused::TX) *
                        ((L.n.y + fused::TY - 1) / fused::TY);
-    const long resident = (long)c->num_sms * 3;
+    const long resident = (long)c->num_sms * 2;
     long kz = (long)L.n.z * tiles / (2 * resident);
     if (kz < 8) kz = 8;
     if (kz > 64) kz = 64;

@@ -169,6 +169,12 @@ class Oracle:
     def set_threads(self, n: int = 0) -> None:
         self.lib.orc_set_threads(int(n))
 
+    def set_relative_stop(self, rel: float) -> None:
+        """Port only: also stop on ||b-Ax||/||b|| <= rel (0 disables)."""
+        f = self.lib.orc_set_relative_stop
+        f.argtypes = [C.c_double]
+        f(float(rel))
+
     # -- pressure projection ------------------------------------------------
     def pressure_solve(self, res, spacing, origin, u, v, w, boundary_sdf,
                        fluid_sdf, params: MgParams, solid=(None, None, None)):

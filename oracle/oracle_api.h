@@ -118,6 +118,11 @@ void orc_g2p_flip(const orc_grid* g, long np, const double* pos, double* vel,
 void orc_g2p_pic(const orc_grid* g, long np, const double* pos, double* vel,
                  const double* u, const double* v, const double* w);
 
+/* Port only: additionally stop MGPCG once the true relative residual
+ * ||b - A x|| / ||b|| falls to `rel` (0 disables). Used to state the CPU
+ * baseline at the GPU solver's accuracy. */
+void orc_set_relative_stop(double rel);
+
 /* Sets the number of host threads the library may use (0 = all). */
 void orc_set_threads(int n);
 

@@ -341,6 +341,11 @@ void mgCorrect(const double* coarser, double* finer, const Size3& c) {
 // Multigrid-preconditioned CG (include/jet/detail/mg-inl.h:16-68,
 // include/jet/detail/cg-inl.h:15-94, src/jet/fdm_mgpcg_solver3.cpp:15-80).
 
+// Optional extra stop test, used only to state a CPU baseline at the same
+// accuracy as the GPU solver: stop once ||b - A x||_2 <= g_rel_stop * ||b||_2
+// (0 = the reference's own test only).
+double g_rel_stop = 0.0;
+
 struct MgSolver {
     orc_mg_params p;
     std::vector<Level>* levels;
@@ -414,6 +419,9 @@ struct MgSolver {
         unsigned iter = 0;
         bool trigger = false;
         double tol = p.tolerance;
+        const double bnorm = std::sqrt(dot(b.data(), b.data(), n));
+        std::vector<double> tr;
+        if (g_rel_stop > 0.0) tr.assign(n, 0.0);
         while (sigmaNew > tol * tol && iter < p.max_cg_iter) {
             mvm(F.A.data(), d.data(), q.data(), F.size);
             double alpha = sigmaNew / dot(d.data(), q.data(), n);
@@ -431,6 +439,11 @@ struct MgSolver {
             double beta = sigmaNew / sigmaOld;
             axpy(beta, d.data(), s.data(), d.data(), n);
             ++iter;
+            if (g_rel_stop > 0.0) {
+                residual(F.A.data(), x.data(), b.data(), tr.data(), F.size);
+                if (std::sqrt(dot(tr.data(), tr.data(), n)) <= g_rel_stop * bnorm)
+                    break;
+            }
         }
         *iters_out = iter;
         *resid_out = std::sqrt(std::fabs(sigmaNew));
@@ -838,6 +851,8 @@ int g_threads = 0;
 }  // namespace
 
 extern "C" {
+
+void orc_set_relative_stop(double rel) { g_rel_stop = rel > 0.0 ? rel : 0.0; }
 
 void orc_set_threads(int n) {
     g_threads = n;
