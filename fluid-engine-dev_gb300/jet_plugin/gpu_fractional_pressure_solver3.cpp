@@ -1,0 +1,149 @@
+// GPU drop-in for Jet's GridPressureSolver3: argument marshalling onto the
+// C ABI of libjetgpu. See gpu_fractional_pressure_solver3.h.
+#include "gpu_fractional_pressure_solver3.h"
+
+#include <jet/cell_centered_scalar_grid3.h>
+#include <jet/constant_scalar_field3.h>
+#include <jet/constant_vector_field3.h>
+#include <jet/face_centered_grid3.h>
+#include <jet/grid_fractional_boundary_condition_solver3.h>
+#include <jet/logging.h>
+
+#include <cstring>
+#include <memory>
+
+namespace jetgpu_jet {
+
+using namespace jet;
+
+GpuFractionalSinglePhasePressureSolver3::GpuFractionalSinglePhasePressureSolver3(
+    const jetgpu_config* cfg) {
+    jetgpu_config_default(&_config);
+    if (cfg) _config = *cfg;
+}
+
+GpuFractionalSinglePhasePressureSolver3::
+    ~GpuFractionalSinglePhasePressureSolver3() {
+    if (_ctx) jetgpu_destroy(_ctx);
+}
+
+GridBoundaryConditionSolver3Ptr
+GpuFractionalSinglePhasePressureSolver3::suggestedBoundaryConditionSolver()
+    const {
+    return std::make_shared<GridFractionalBoundaryConditionSolver3>();
+}
+
+jetgpu_scalar_field GpuFractionalSinglePhasePressureSolver3::describe(
+    const ScalarField3& field, const FaceCenteredGrid3& grid,
+    std::vector<double>* raster) const {
+    jetgpu_scalar_field f;
+    std::memset(&f, 0, sizeof(f));
+    if (auto c = dynamic_cast<const ConstantScalarField3*>(&field)) {
+        f.kind = 0;
+        f.value = c->sample(Vector3D());
+        return f;
+    }
+    const CellCenteredScalarGrid3* g =
+        dynamic_cast<const CellCenteredScalarGrid3*>(&field);
+    std::shared_ptr<CellCenteredScalarGrid3> owned;
+    if (!g) {
+        // Any other field: rasterise at the velocity grid's cell centres.
+        owned = std::make_shared<CellCenteredScalarGrid3>(
+            grid.resolution(), grid.gridSpacing(), grid.origin());
+        owned->fill([&](const Vector3D& x) { return field.sample(x); });
+        g = owned.get();
+    }
+    const Size3 r = g->resolution();
+    const size_t n = r.x * r.y * r.z;
+    auto acc = g->constDataAccessor();
+    raster->assign(acc.data(), acc.data() + n);
+    f.kind = 1;
+    f.data = raster->data();
+    f.res[0] = (int)r.x;
+    f.res[1] = (int)r.y;
+    f.res[2] = (int)r.z;
+    const Vector3D o = g->dataOrigin(), h = g->gridSpacing();
+    f.origin[0] = o.x;
+    f.origin[1] = o.y;
+    f.origin[2] = o.z;
+    f.spacing[0] = h.x;
+    f.spacing[1] = h.y;
+    f.spacing[2] = h.z;
+    return f;
+}
+
+void GpuFractionalSinglePhasePressureSolver3::solve(
+    const FaceCenteredGrid3& input, double timeIntervalInSeconds,
+    FaceCenteredGrid3* output, const ScalarField3& boundarySdf,
+    const VectorField3& boundaryVelocity, const ScalarField3& fluidSdf,
+    bool useCompressed) {
+    (void)timeIntervalInSeconds;  // unused, as in the reference (:461)
+    (void)useCompressed;          // the GPU system is row based either way
+    if (!_ctx) {
+        _status = jetgpu_create(&_config, &_ctx);
+        if (_status != JETGPU_OK) {
+            JET_ERROR << "jetgpu_create failed with status " << _status;
+            return;
+        }
+    }
+    const Size3 res = input.resolution();
+    const Vector3D h = input.gridSpacing(), o = input.origin();
+    jetgpu_grid g;
+    g.res[0] = (int)res.x;
+    g.res[1] = (int)res.y;
+    g.res[2] = (int)res.z;
+    g.spacing[0] = h.x;
+    g.spacing[1] = h.y;
+    g.spacing[2] = h.z;
+    g.origin[0] = o.x;
+    g.origin[1] = o.y;
+    g.origin[2] = o.z;
+    const jetgpu_scalar_field bsdf = describe(boundarySdf, input, &_boundaryRaster);
+    const jetgpu_scalar_field fsdf = describe(fluidSdf, input, &_fluidRaster);
+
+    // Collider velocity: only the normal component at each face is used
+    // (grid_fractional_single_phase_pressure_solver3.cpp:241-255).
+    const double* su = nullptr;
+    const double* sv = nullptr;
+    const double* sw = nullptr;
+    auto cv = dynamic_cast<const ConstantVectorField3*>(&boundaryVelocity);
+    const bool still = cv && cv->sample(Vector3D()).lengthSquared() == 0.0;
+    if (!still) {
+        auto sample = [&](std::vector<double>* out, const Size3& s,
+                          VectorGrid3::DataPositionFunc pos, int axis) {
+            out->resize(s.x * s.y * s.z);
+            size_t c = 0;
+            for (size_t k = 0; k < s.z; ++k)
+                for (size_t j = 0; j < s.y; ++j)
+                    for (size_t i = 0; i < s.x; ++i)
+                        (*out)[c++] = boundaryVelocity.sample(pos(i, j, k))[axis];
+        };
+        sample(&_solidU, input.uSize(), input.uPosition(), 0);
+        sample(&_solidV, input.vSize(), input.vPosition(), 1);
+        sample(&_solidW, input.wSize(), input.wPosition(), 2);
+        su = _solidU.data();
+        sv = _solidV.data();
+        sw = _solidW.data();
+    }
+
+    _pressure.resize(res);
+    auto u = input.uConstAccessor();
+    auto v = input.vConstAccessor();
+    auto w = input.wConstAccessor();
+    auto ou = output->uAccessor();
+    auto ov = output->vAccessor();
+    auto ow = output->wAccessor();
+    _status = jetgpu_solve_pressure(_ctx, &g, u.data(), v.data(), w.data(),
+                                    &bsdf, &fsdf, su, sv, sw, ou.data(),
+                                    ov.data(), ow.data(), _pressure.data(),
+                                    &_stats);
+    if (_status != JETGPU_OK) {
+        // The reference ignores its linear solver's result
+        // (grid_fractional_single_phase_pressure_solver3.cpp:466-483); the
+        // projected velocity of the last iterate has been applied.
+        JET_WARN << "jetgpu_solve_pressure: status " << _status << ": "
+                 << jetgpu_last_error(_ctx);
+    }
+}
+
+}  // namespace jetgpu_jet

@@ -1,0 +1,73 @@
+"""The C++ drop-in compiles against the reference and installs (CPU only).
+
+Builds fluid-engine-dev_gb300/jet_plugin/gpu_fractional_pressure_solver3.cpp
+against the reference's own headers, links it with the reference library
+(oracle/_ref/libjet_ref.a) and libjetgpu.so, and runs a program that
+installs the GPU solver with setPressureSolver() on FlipSolver3, PicSolver3,
+GridSmokeSolver3 and LevelSetLiquidSolver3 — the reference's install point
+(src/jet/grid_fluid_solver3.cpp:110-121). No solve runs (no GPU here); the
+CUDA context is created lazily on the first solve. Skipped where the
+reference sources are absent.
+"""
+import os
+import subprocess
+
+import pytest
+
+from conftest import PKG, REPO
+
+REF = "/root/reference"
+
+MAIN = r"""
+#include <jet/jet.h>
+#include "gpu_fractional_pressure_solver3.h"
+#include <cstdio>
+#include <memory>
+
+template <typename S>
+bool install(S solver) {
+    auto gpu = std::make_shared<jetgpu_jet::GpuFractionalSinglePhasePressureSolver3>();
+    solver->setPressureSolver(gpu);
+    return solver->pressureSolver() == gpu;
+}
+
+int main() {
+    jet::Logging::mute();
+    bool ok = true;
+    ok &= install(jet::FlipSolver3::builder().withResolution({8, 8, 8}).makeShared());
+    ok &= install(jet::PicSolver3::builder().withResolution({8, 8, 8}).makeShared());
+    ok &= install(jet::GridSmokeSolver3::builder().withResolution({8, 8, 8}).makeShared());
+    ok &= install(jet::LevelSetLiquidSolver3::builder().withResolution({8, 8, 8}).makeShared());
+    jetgpu_jet::GpuFractionalSinglePhasePressureSolver3 s;
+    ok &= std::dynamic_pointer_cast<jet::GridFractionalBoundaryConditionSolver3>(
+              s.suggestedBoundaryConditionSolver()) != nullptr;
+    std::printf("%s %s\n", ok ? "installed" : "FAILED", jetgpu_version());
+    return ok ? 0 : 1;
+}
+"""
+
+
+def test_cpp_adapter_installs_into_jet_solvers(tmp_path):
+    if not os.path.isdir(os.path.join(REF, "include", "jet")):
+        pytest.skip("reference headers not present on this machine")
+    import oracle
+    from jetgpu import _build
+    lib = _build.build()
+    oracle.build_reference()
+    ref_a = os.path.join(REPO, "oracle", "_ref", "libjet_ref.a")
+    assert os.path.exists(ref_a)
+    main = tmp_path / "main.cpp"
+    main.write_text(MAIN)
+    exe = tmp_path / "install"
+    plugin = os.path.join(PKG, "jet_plugin")
+    cmd = ["g++", "-std=c++17", "-O1", "-fopenmp", "-DJET_TASKING_OPENMP",
+           "-include", "cstdint", "-w",
+           "-I" + os.path.join(REF, "include"),
+           "-I" + os.path.join(REF, "external"),
+           "-I" + os.path.join(REPO, "include"), "-I" + plugin,
+           str(main), os.path.join(plugin, "gpu_fractional_pressure_solver3.cpp"),
+           ref_a, lib, "-Wl,-rpath," + os.path.dirname(lib), "-o", str(exe)]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr[-3000:]
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=120)
+    assert r.returncode == 0 and "installed" in r.stdout, r.stdout + r.stderr
