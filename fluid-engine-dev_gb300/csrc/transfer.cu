@@ -16,6 +16,8 @@
 
 #include "ctx.h"
 
+#include <mutex>
+
 namespace jg {
 namespace {
 
@@ -276,3 +278,93 @@ jetgpu_status g2p_pic(Ctx* c, const GridDesc& g, long np, const double* pos,
 }
 
 }  // namespace jg
+
+// ---------------------------------------------------------------------------
+// Allocation-free P2G (jetgpu_p2g_device_noalloc). Its only scratch, the
+// per-face weight sums, is this fixed array. In host code the name is only a
+// host-side stand-in, so the device address is looked up once per device
+// with cudaGetSymbolAddress and handed to the kernels.
+
+namespace {
+
+constexpr size_t kNoAllocFaces = JETGPU_P2G_NOALLOC_MAX_FACES;
+__device__ __align__(256) double g_p2g_noalloc_wsum[kNoAllocFaces];
+
+constexpr int kMaxDevices = 64;
+std::mutex g_noalloc_mu;
+double* g_noalloc_ptr[kMaxDevices] = {};
+int g_noalloc_sms[kMaxDevices] = {};
+
+}  // namespace
+
+extern "C" jetgpu_status jetgpu_p2g_device_noalloc(
+    void* stream, const jetgpu_grid* grid, long np, const double* pos,
+    const double* vel, double* u, double* v, double* w, unsigned char* mu,
+    unsigned char* mv, unsigned char* mw, float* su, float* sv, float* sw) {
+    using namespace jg;
+    if (!grid || !u || !v || !w) return JETGPU_BAD_INPUT;
+    if (np < 0 || (np > 0 && (!pos || !vel))) return JETGPU_BAD_INPUT;
+    for (int a = 0; a < 3; ++a)
+        if (grid->res[a] < 1 || !(grid->spacing[a] > 0.0))
+            return JETGPU_BAD_INPUT;
+    GridDesc g;
+    for (int a = 0; a < 3; ++a) {
+        g.res[a] = grid->res[a];
+        g.spacing[a] = grid->spacing[a];
+        g.origin[a] = grid->origin[a];
+    }
+    const FaceSet fs = face_set(g);
+    const size_t n[3] = {(size_t)fs.s[0].count(), (size_t)fs.s[1].count(),
+                         (size_t)fs.s[2].count()};
+    const size_t faces = n[0] + n[1] + n[2];
+    if (faces > kNoAllocFaces) return JETGPU_CAPACITY_EXCEEDED;
+
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMaxDevices)
+        return JETGPU_CUDA_ERROR;
+    double* wsum = nullptr;
+    int sms = 0;
+    {
+        std::lock_guard<std::mutex> lock(g_noalloc_mu);
+        if (!g_noalloc_ptr[dev]) {
+            void* p = nullptr;
+            if (cudaGetSymbolAddress(&p, g_p2g_noalloc_wsum) != cudaSuccess ||
+                !p)
+                return JETGPU_CUDA_ERROR;
+            int count = 0;
+            if (cudaDeviceGetAttribute(&count, cudaDevAttrMultiProcessorCount,
+                                       dev) != cudaSuccess)
+                return JETGPU_CUDA_ERROR;
+            g_noalloc_sms[dev] = count;
+            g_noalloc_ptr[dev] = static_cast<double*>(p);
+        }
+        wsum = g_noalloc_ptr[dev];
+        sms = g_noalloc_sms[dev];
+    }
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    double* grids[3] = {u, v, w};
+    unsigned char* mark[3] = {mu, mv, mw};
+    float* snap[3] = {su, sv, sw};
+    // The array keeps the previous call's sums: clear the part used here.
+    if (cudaMemsetAsync(wsum, 0, faces * sizeof(double), st) != cudaSuccess)
+        return JETGPU_CUDA_ERROR;
+    for (int a = 0; a < 3; ++a) {
+        if (cudaMemsetAsync(grids[a], 0, n[a] * sizeof(double), st) !=
+            cudaSuccess)
+            return JETGPU_CUDA_ERROR;
+        if (mark[a] && cudaMemsetAsync(mark[a], 0, n[a], st) != cudaSuccess)
+            return JETGPU_CUDA_ERROR;
+    }
+    if (np > 0)
+        k_p2g_scatter<<<blocks_for(np, kThreads, sms * 16), kThreads, 0, st>>>(
+            np, pos, vel, fs, 1.0 / g.spacing[0], 1.0 / g.spacing[1],
+            1.0 / g.spacing[2], u, v, w, wsum, wsum + n[0], wsum + n[0] + n[1],
+            mu, mv, mw);
+    size_t off = 0;
+    for (int a = 0; a < 3; ++a) {
+        k_p2g_normalize<<<blocks_for((long)n[a]), kThreads, 0, st>>>(
+            grids[a], wsum + off, snap[a], (long)n[a]);
+        off += n[a];
+    }
+    return cudaGetLastError() == cudaSuccess ? JETGPU_OK : JETGPU_CUDA_ERROR;
+}

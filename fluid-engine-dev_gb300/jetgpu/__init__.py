@@ -92,7 +92,7 @@ class SolveStats(C.Structure):
 
 STATUS = {0: "OK", 1: "NOT_CONVERGED", 2: "STALLED_FALLBACK_USED",
           3: "BAD_INPUT", 4: "CUDA_ERROR", 5: "OUT_OF_MEMORY",
-          6: "NUMERICAL_ERROR"}
+          6: "NUMERICAL_ERROR", 7: "CAPACITY_EXCEEDED"}
 PRECISION = {"fp32": 0, "fp64": 1, "mixed": 2, "bf16": 2}
 
 # Symbols include/jetgpu.h declares (checked by the CPU test suite).
@@ -103,7 +103,7 @@ EXPORTS = (
     "jetgpu_p2g_device", "jetgpu_g2p_flip_device", "jetgpu_g2p_pic_device",
     "jetgpu_p2g", "jetgpu_g2p_flip", "jetgpu_g2p_pic", "jetgpu_get_level",
     "jetgpu_version", "jetgpu_get_stream", "jetgpu_profile",
-    "jetgpu_profile_read",
+    "jetgpu_profile_read", "jetgpu_p2g_device_noalloc",
 )
 
 
@@ -162,6 +162,8 @@ def library() -> C.CDLL:
     L.jetgpu_p2g.restype = C.c_int
     L.jetgpu_p2g_device.argtypes = p2g_args
     L.jetgpu_p2g_device.restype = C.c_int
+    L.jetgpu_p2g_device_noalloc.argtypes = p2g_args
+    L.jetgpu_p2g_device_noalloc.restype = C.c_int
     flip_args = [vp, C.POINTER(Grid), C.c_long, dp, dp, dp, dp, dp, fp, fp, fp,
                  C.c_double]
     L.jetgpu_g2p_flip.argtypes = flip_args

@@ -39,7 +39,10 @@ typedef enum jetgpu_status {
     JETGPU_CUDA_ERROR = 4,
     JETGPU_OUT_OF_MEMORY = 5,
     /* A NaN or Inf appeared in a reduction (input or breakdown). */
-    JETGPU_NUMERICAL_ERROR = 6
+    JETGPU_NUMERICAL_ERROR = 6,
+    /* The problem is larger than the fixed capacity of an entry point that
+     * works without allocating (jetgpu_p2g_device_noalloc). */
+    JETGPU_CAPACITY_EXCEEDED = 7
 } jetgpu_status;
 
 /* Arithmetic of the Krylov iteration. In every mode the global r.z and p.Ap
@@ -211,6 +214,36 @@ jetgpu_status jetgpu_g2p_pic_device(struct jetgpu_ctx* ctx,
                                     long num_particles, const double* pos,
                                     double* vel, const double* u,
                                     const double* v, const double* w);
+
+/* P2G that allocates nothing. No counterpart in the reference.
+ *
+ * For callers that must not allocate device memory while they run: a host
+ * engine or plugin that owns the GPU's memory budget and forbids hidden
+ * allocations, or a real-time loop in which cudaMalloc's implicit device
+ * synchronisation is not allowed. It computes the same result as
+ * jetgpu_p2g_device (same DEVICE-pointer arguments) but needs no context:
+ * its only scratch, the per-face weight sums, lives in a fixed array in the
+ * library's device memory of JETGPU_P2G_NOALLOC_MAX_FACES doubles (6.4 MB,
+ * the faces of a 64^3 grid), which every GPU that loads the library holds
+ * until the process exits. Grids whose u+v+w face count exceeds it are
+ * rejected with JETGPU_CAPACITY_EXCEEDED before any GPU work.
+ *
+ * The work is queued on `stream` (a cudaStream_t; NULL = the default
+ * stream) and the call returns without waiting for it. The first call on a
+ * device, with that device current, looks up the scratch array's device
+ * address; make that first call before any stream capture. All calls share
+ * the one array: calls that overlap on the GPU (different streams, or
+ * different host threads, without ordering between them) race on it. Each
+ * call clears the part it uses before accumulating. No cudaMalloc, cudaFree
+ * or allocating library routine is called. */
+#define JETGPU_P2G_NOALLOC_MAX_FACES (3u * 65u * 64u * 64u)
+jetgpu_status jetgpu_p2g_device_noalloc(void* stream, const jetgpu_grid* grid,
+                                        long num_particles, const double* pos,
+                                        const double* vel, double* u,
+                                        double* v, double* w,
+                                        unsigned char* mu, unsigned char* mv,
+                                        unsigned char* mw, float* snap_u,
+                                        float* snap_v, float* snap_w);
 
 /* Host-pointer forms of the three transfers (copies inside the call). */
 jetgpu_status jetgpu_p2g(struct jetgpu_ctx* ctx, const jetgpu_grid* grid,
