@@ -296,6 +296,22 @@ jetgpu_status jetgpu_profile_read(struct jetgpu_ctx* ctx,
                                   jetgpu_kernel_stat* out, int capacity,
                                   int* count);
 
+/* ---- Learned preconditioner building blocks (no counterpart in the
+ * reference; Jet has no learned components). DEVICE pointers, queued on
+ * `stream` (a cudaStream_t) without waiting. Activations are BF16,
+ * channels-last ([cell][channel], cells i-fastest). */
+
+/* 3x3x3 convolution, stride 1, zero padding 1, on the tcgen05 tensor cores:
+ * out[v][co] = act(bias[co] + sum_{tap,ci} in[v+tap][ci] * w[tap][co][ci])
+ * with FP32 accumulation; tap = (dz+1)*9 + (dy+1)*3 + (dx+1). ci and co are
+ * multiples of 16 in [16, 128]. relu != 0 applies max(0, .). out (BF16)
+ * and/or out32 (FP32) receive the result. *err is or-ed with 1 if an
+ * internal wait gave up (it never should). */
+jetgpu_status jetgpu_conv3d(void* stream, const void* in, int ci,
+                            const void* w, const float* bias, int co,
+                            const int res[3], int relu, void* out,
+                            float* out32, unsigned int* err);
+
 /* Library version string. */
 const char* jetgpu_version(void);
 
