@@ -217,3 +217,189 @@ extern "C" jetgpu_status jetgpu_conv3d(void* stream, const void* in, int ci,
                   Dims{res[0], res[1], res[2]}, relu,
                   static_cast<__nv_bfloat16*>(out), out32, err);
 }
+
+// ---------------------------------------------------------------------------
+// K16 (training): weight gradient dW[t][co][ci] += sum_v dy[v][co] *
+// in[v + off(t)][ci] as a tensor-core GEMM with K = cells. Per 128-cell
+// K-tile the threads transpose dy (A: 128 rows = co padded with zeros, K =
+// cells) and the tap-shifted input (B: ci rows, K = cells) into K-major
+// operand tiles; one thread issues the MMAs of a group of taps, whose
+// accumulators sit side by side in TMEM (tg * ci <= 512 columns).
+// Persistent CTAs accumulate over their tiles and add the result into the
+// FP32 gradient with atomics at the end (the caller zeroes it).
+
+namespace jg {
+namespace {
+
+constexpr uint32_t kWgSbo = 16u * 128u;  // 128 K-columns = 16 core matrices
+
+struct WgradArgs {
+    const __nv_bfloat16* in;  // [V][ci]
+    const __nv_bfloat16* dy;  // [V][co]
+    float* dw;                // [27][co][ci]
+    Dims n;
+    int ci, co, t0, tg;
+    unsigned* err;
+};
+
+__host__ __device__ inline int wgrad_taps(int ci) {
+    int tg = 512 / ci;
+    return tg > 27 ? 27 : tg;
+}
+
+__host__ __device__ inline size_t wgrad_smem_bytes(int ci) {
+    // A (128 rows) + tg B tiles (ci rows each), 128 K-columns of BF16, plus
+    // barrier space; at least 120 KB so one CTA holds an SM's TMEM.
+    const size_t need = (size_t)128 * 256 + (size_t)wgrad_taps(ci) * ci * 256 + 64;
+    const size_t floor_bytes = 120 * 1024;
+    return need > floor_bytes ? need : floor_bytes;
+}
+
+// Writes the 8 channels of one cell (16 bytes) into column `col` of rows
+// r0..r0+7 of a K-major operand tile.
+__device__ __forceinline__ void scatter8(unsigned char* tile, int r0, int col,
+                                         uint4 chunk) {
+    const __nv_bfloat16* h = reinterpret_cast<const __nv_bfloat16*>(&chunk);
+    unsigned char* base = tile + (r0 >> 3) * kWgSbo + (col >> 3) * 128 + (col & 7) * 2;
+#pragma unroll
+    for (int q = 0; q < 8; ++q)
+        *reinterpret_cast<__nv_bfloat16*>(base + q * 16) = h[q];
+}
+
+__global__ void __launch_bounds__(128) k_conv3d_wgrad_tc(WgradArgs a) {
+    extern __shared__ __align__(128) unsigned char smem[];
+    const int ci = a.ci, co = a.co, tg = a.tg;
+    unsigned char* A = smem;
+    unsigned char* B = smem + 128 * 256;
+    const uint32_t bstride = (uint32_t)ci * 256u;
+    uint64_t* mbar = reinterpret_cast<uint64_t*>(B + (size_t)tg * bstride);
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(mbar + 1);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const long V = a.n.count();
+    const long tiles = (V + 127) / 128;
+    uint32_t need = (uint32_t)(tg * ci), ncols = 32;
+    while (ncols < need) ncols <<= 1;
+
+    if (warp == 0) tc::tmem_alloc(tslot, ncols);
+    if (tid == 0) {
+        tc::mbar_init(&mbar[0], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    // Rows co..127 of A stay zero.
+    for (int q = tid; q < 128 * 256 / 16; q += 128)
+        reinterpret_cast<uint4*>(A)[q] = make_uint4(0, 0, 0, 0);
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = *tslot;
+    const uint32_t idesc = tc::idesc_bf16_f32(128, ci);
+    uint32_t phase = 0;
+    bool ok = true;
+    long done = 0;
+    for (long tile = blockIdx.x; tile < tiles; tile += gridDim.x, ++done) {
+        const long v = tile * 128 + tid;
+        const bool vok = v < V;
+        int vi = 0, vj = 0, vk = 0;
+        if (vok) cell_ijk(v, a.n, vi, vj, vk);
+        for (int c8 = 0; c8 < co; c8 += 8) {
+            uint4 chunk = make_uint4(0, 0, 0, 0);
+            if (vok) chunk = *reinterpret_cast<const uint4*>(a.dy + v * co + c8);
+            scatter8(A, c8, tid, chunk);
+        }
+        for (int g = 0; g < tg; ++g) {
+            const int t = a.t0 + g;
+            const int dz = t / 9 - 1, dyy = (t / 3) % 3 - 1, dx = t % 3 - 1;
+            const int ii = vi + dx, jj = vj + dyy, kk = vk + dz;
+            const bool ok2 = vok && ii >= 0 && ii < a.n.x && jj >= 0 &&
+                             jj < a.n.y && kk >= 0 && kk < a.n.z;
+            const __nv_bfloat16* src =
+                ok2 ? a.in + lin(ii, jj, kk, a.n.x, a.n.y) * ci : nullptr;
+            for (int c8 = 0; c8 < ci; c8 += 8) {
+                uint4 chunk = make_uint4(0, 0, 0, 0);
+                if (ok2) chunk = *reinterpret_cast<const uint4*>(src + c8);
+                scatter8(B + g * bstride, c8, tid, chunk);
+            }
+        }
+        tc::fence_proxy_async();
+        __syncthreads();
+        if (tid == 0) {
+            tc::fence_after_sync();
+            const uint32_t ab = tc::smem_u32(A), bb = tc::smem_u32(B);
+            for (int g = 0; g < tg; ++g)
+                for (int k16 = 0; k16 < 8; ++k16) {
+                    const uint64_t ad = tc::smem_desc(ab + k16 * 256, 128, kWgSbo);
+                    const uint64_t bd =
+                        tc::smem_desc(bb + g * bstride + k16 * 256, 128, kWgSbo);
+                    tc::mma_bf16(tmem + (uint32_t)(g * ci), ad, bd, idesc,
+                                 (done > 0 || k16 > 0) ? 1u : 0u);
+                }
+            tc::mma_commit(&mbar[0]);
+        }
+        // The next tile overwrites the operand tiles: wait for the MMAs.
+        ok &= tc::mbar_wait(&mbar[0], phase);
+        phase ^= 1u;
+        tc::fence_after_sync();
+    }
+    if (!ok && a.err) atomicOr(a.err, 1u);
+    if (done > 0 && warp * 32 < co) {
+        const int row = warp * 32 + (tid & 31);
+        const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
+        for (int g = 0; g < tg; ++g)
+            for (int c0 = 0; c0 < ci; c0 += 16) {
+                float val[16];
+                tc::tmem_ld16(trow + (uint32_t)(g * ci + c0), val);
+                if (row < co) {
+                    float* dst = a.dw + ((long)(a.t0 + g) * co + row) * ci + c0;
+#pragma unroll
+                    for (int q = 0; q < 16; ++q) atomicAdd(dst + q, val[q]);
+                }
+            }
+    }
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tmem, ncols);
+}
+
+}  // namespace
+
+jetgpu_status conv3d_wgrad(cudaStream_t st, const __nv_bfloat16* in, int ci,
+                           const __nv_bfloat16* dy, int co, Dims n, float* dw,
+                           unsigned* err, int sms) {
+    static bool attr_set = false;
+    if (!attr_set) {
+        if (cudaFuncSetAttribute(k_conv3d_wgrad_tc,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 200 * 1024) != cudaSuccess)
+            return JETGPU_CUDA_ERROR;
+        attr_set = true;
+    }
+    const long tiles = (n.count() + 127) / 128;
+    const int grid = (int)(tiles < sms ? tiles : sms);
+    const int tg = wgrad_taps(ci);
+    for (int t0 = 0; t0 < 27; t0 += tg) {
+        WgradArgs a{in, dy, dw, n, ci, co, t0, t0 + tg <= 27 ? tg : 27 - t0, err};
+        k_conv3d_wgrad_tc<<<grid, 128, wgrad_smem_bytes(ci), st>>>(a);
+    }
+    return cudaGetLastError() == cudaSuccess ? JETGPU_OK : JETGPU_CUDA_ERROR;
+}
+
+}  // namespace jg
+
+extern "C" jetgpu_status jetgpu_conv3d_wgrad(void* stream, const void* in,
+                                             int ci, const void* dy, int co,
+                                             const int res[3], float* dw,
+                                             unsigned* err) {
+    using namespace jg;
+    if (!in || !dy || !dw || !res) return JETGPU_BAD_INPUT;
+    if (ci < 16 || ci > 128 || ci % 16 || co < 16 || co > 128 || co % 16)
+        return JETGPU_BAD_INPUT;
+    int dev = 0, sms = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=
+            cudaSuccess)
+        return JETGPU_CUDA_ERROR;
+    return conv3d_wgrad(static_cast<cudaStream_t>(stream),
+                        static_cast<const __nv_bfloat16*>(in), ci,
+                        static_cast<const __nv_bfloat16*>(dy), co,
+                        Dims{res[0], res[1], res[2]}, dw, err, sms);
+}

@@ -104,6 +104,7 @@ EXPORTS = (
     "jetgpu_p2g", "jetgpu_g2p_flip", "jetgpu_g2p_pic", "jetgpu_get_level",
     "jetgpu_version", "jetgpu_get_stream", "jetgpu_profile",
     "jetgpu_profile_read", "jetgpu_p2g_device_noalloc", "jetgpu_conv3d",
+    "jetgpu_conv3d_wgrad",
 )
 
 
@@ -183,6 +184,9 @@ def library() -> C.CDLL:
     L.jetgpu_conv3d.argtypes = [vp, vp, C.c_int, vp, vp, C.c_int,
                                 C.POINTER(C.c_int), C.c_int, vp, vp, vp]
     L.jetgpu_conv3d.restype = C.c_int
+    L.jetgpu_conv3d_wgrad.argtypes = [vp, vp, C.c_int, vp, C.c_int,
+                                      C.POINTER(C.c_int), vp, vp]
+    L.jetgpu_conv3d_wgrad.restype = C.c_int
     L.jetgpu_get_stream.argtypes = [vp, C.POINTER(C.c_void_p)]
     L.jetgpu_get_stream.restype = C.c_int
     L.jetgpu_profile.argtypes = [vp, C.c_int]

@@ -312,6 +312,14 @@ jetgpu_status jetgpu_conv3d(void* stream, const void* in, int ci,
                             const int res[3], int relu, void* out,
                             float* out32, unsigned int* err);
 
+/* Weight gradient of jetgpu_conv3d (no bias, no activation):
+ * dw[tap][co][ci] += sum_v dy[v][co] * in[v+tap][ci], FP32, on the tensor
+ * cores. The caller zeroes dw first. The input gradient is jetgpu_conv3d of
+ * dy with the weights flipped in tap and transposed in (co, ci). */
+jetgpu_status jetgpu_conv3d_wgrad(void* stream, const void* in, int ci,
+                                  const void* dy, int co, const int res[3],
+                                  float* dw, unsigned int* err);
+
 /* Library version string. */
 const char* jetgpu_version(void);
 
