@@ -20,6 +20,13 @@ jetgpu_status fail(Ctx* c, jetgpu_status s, const std::string& msg) {
 
 namespace {
 
+// A solve whose result is applied: converged, capped, or finished by the
+// multigrid fallback after the learned preconditioner stalled.
+bool usable(jetgpu_status s) {
+    return s == JETGPU_OK || s == JETGPU_NOT_CONVERGED ||
+           s == JETGPU_STALLED_FALLBACK_USED;
+}
+
 template <typename T>
 cudaError_t alloc(T** p, size_t count) {
     *p = nullptr;
@@ -58,6 +65,7 @@ void free_buffers(Ctx* c) {
     release(&c->kd);
     release(&c->kq);
     release(&c->kz);
+    release(&c->kz2);
     release(&c->dx);
     release(&c->dr);
     release(&c->dd);
@@ -85,7 +93,7 @@ jetgpu_status check_config(Ctx* c, const jetgpu_config* cfg) {
                     "only red-black smoothing is provided on the GPU");
     if (cfg->precision < 0 || cfg->precision > 2)
         return fail(c, JETGPU_BAD_INPUT, "unknown precision");
-    if (cfg->preconditioner < 0 || cfg->preconditioner > 1)
+    if (cfg->preconditioner < 0 || cfg->preconditioner > 2)
         return fail(c, JETGPU_BAD_INPUT, "unknown preconditioner");
     return JETGPU_OK;
 }
@@ -219,6 +227,7 @@ jetgpu_status ensure_buffers(Ctx* c, Dims n, unsigned max_levels) {
     JG_CUDA(c, alloc(&c->kd, N));
     JG_CUDA(c, alloc(&c->kq, N));
     JG_CUDA(c, alloc(&c->kz, N));
+    JG_CUDA(c, alloc(&c->kz2, N));
     JG_CUDA(c, alloc(&c->dd, N));
     JG_CUDA(c, alloc(&c->dq, N));
     c->n0 = n;
@@ -248,7 +257,7 @@ static jetgpu_status solve_pressure_dev(
     const double setup = ms_since(t0);
     auto t1 = std::chrono::steady_clock::now();
     jetgpu_status solve_status = mgpcg_solve(c, st);
-    if (solve_status != JETGPU_OK && solve_status != JETGPU_NOT_CONVERGED)
+    if (!usable(solve_status))
         return solve_status;
     const double solve = ms_since(t1);
     // The reference applies the gradient whatever the solver returned
@@ -345,6 +354,8 @@ void jetgpu_destroy(jetgpu_ctx* c) {
     release(&c->counters);
     release(&c->stage);
     release(&c->pscratch);
+    net_destroy(c->unet);
+    c->unet = nullptr;
     if (c->h_scal) cudaFreeHost(c->h_scal);
     if (c->host_stage) cudaFreeHost(c->host_stage);
     for (auto& e : c->ev)
@@ -459,7 +470,7 @@ jetgpu_status jetgpu_solve_pressure(
     jetgpu_status solve_status = solve_pressure_dev(
         c, grid, du, dv, dw, boundary_sdf, db, fluid_sdf, df, dsu, dsv, dsw,
         ou, ov, ow, out_pressure ? dp : nullptr, &local);
-    if (solve_status != JETGPU_OK && solve_status != JETGPU_NOT_CONVERGED) {
+    if (!usable(solve_status)) {
         if (stats) *stats = local;
         return solve_status;
     }
@@ -523,7 +534,7 @@ jetgpu_status jetgpu_mgpcg_solve_system(jetgpu_ctx* c, const int res0[3],
     auto t1 = std::chrono::steady_clock::now();
     jetgpu_status solve_status = mgpcg_solve(c, &local);
     local.solve_ms = ms_since(t1);
-    if (solve_status == JETGPU_OK || solve_status == JETGPU_NOT_CONVERGED) {
+    if (usable(solve_status)) {
         JG_CUDA(c, cudaMemcpyAsync(x, c->x64, (size_t)N0 * 8, cudaMemcpyDeviceToHost, st));
         JG_CUDA(c, cudaStreamSynchronize(st));
     }
@@ -864,6 +875,58 @@ jetgpu_status jetgpu_profile_read(jetgpu_ctx* c, jetgpu_kernel_stat* out,
         ++n;
     }
     *count = n;
+    return JETGPU_OK;
+}
+
+}  // extern "C"
+
+// ---- learned preconditioner ------------------------------------------------
+
+extern "C" {
+
+size_t jetgpu_net_param_count(void) { return net_param_count(); }
+
+jetgpu_status jetgpu_load_unet(jetgpu_ctx* c, const float* params,
+                               size_t count) {
+    if (!c || !params) return JETGPU_BAD_INPUT;
+    JG_CUDA(c, cudaSetDevice(c->device));
+    return net_load(c, params, count);
+}
+
+jetgpu_status jetgpu_harvest(jetgpu_ctx* c, unsigned int max_pairs,
+                             float* r_out, float* z_out, unsigned int* count) {
+    if (!c || !r_out || !z_out || !count) return JETGPU_BAD_INPUT;
+    if (c->built_levels == 0)
+        return fail(c, JETGPU_BAD_INPUT, "no system: run a pressure solve first");
+    JG_CUDA(c, cudaSetDevice(c->device));
+    return harvest_pairs(c, max_pairs, r_out, z_out, count);
+}
+
+jetgpu_status jetgpu_net_features(jetgpu_ctx* c, const float* r, void* feat) {
+    if (!c || !r || !feat) return JETGPU_BAD_INPUT;
+    if (c->built_levels == 0)
+        return fail(c, JETGPU_BAD_INPUT, "no system: run a pressure solve first");
+    JG_CUDA(c, cudaSetDevice(c->device));
+    jetgpu_status s = norm2f(c, r, c->levels[0].n.count(), S_MEAN);
+    if (s != JETGPU_OK) return s;
+    s = net_features(c, r, c->scal + S_MEAN, feat);
+    if (s != JETGPU_OK) return s;
+    JG_CUDA(c, cudaStreamSynchronize(c->stream));
+    return JETGPU_OK;
+}
+
+jetgpu_status jetgpu_net_apply(jetgpu_ctx* c, const float* r, float* z) {
+    if (!c || !r || !z) return JETGPU_BAD_INPUT;
+    if (c->built_levels == 0 || !net_supported(c))
+        return fail(c, JETGPU_BAD_INPUT,
+                    "needs a solved system with resolution divisible by 8 and "
+                    "a loaded network");
+    JG_CUDA(c, cudaSetDevice(c->device));
+    jetgpu_status s = norm2f(c, r, c->levels[0].n.count(), S_MEAN);
+    if (s != JETGPU_OK) return s;
+    s = net_apply(c, r, c->scal + S_MEAN, z);
+    if (s != JETGPU_OK) return s;
+    JG_CUDA(c, cudaStreamSynchronize(c->stream));
     return JETGPU_OK;
 }
 

@@ -107,6 +107,7 @@ struct Ctx {
     float* kd = nullptr;
     float* kq = nullptr;
     float* kz = nullptr;
+    float* kz2 = nullptr;  // previous z (flexible PCG)
     // Krylov vectors (FP64 mode).
     double* dx = nullptr;
     double* dr = nullptr;
@@ -220,6 +221,32 @@ jetgpu_status vcycle(Ctx* c, const float* r, float* z, float* alt,
                      float** result);
 // One-time kernel attributes (dynamic shared memory limits).
 jetgpu_status init_kernels(Ctx* c);
+
+// ---- unet.cu --------------------------------------------------------------
+struct NetLayer {
+    int ci, co, relu, level;
+};
+constexpr int kNetLayerCount = 14;
+extern const NetLayer kNetLayers[kNetLayerCount];
+size_t net_param_count();
+jetgpu_status net_load(Ctx* c, const float* params, size_t count);
+bool net_supported(const Ctx* c);
+jetgpu_status net_features(Ctx* c, const float* r, const double* rr,
+                           void* feat);
+jetgpu_status net_apply(Ctx* c, const float* r, const double* rr, float* z);
+void net_destroy(void* net);
+jetgpu_status conv3d(cudaStream_t st, const __nv_bfloat16* in, int ci,
+                     const __nv_bfloat16* w, const float* bias, int co,
+                     Dims n, int relu, __nv_bfloat16* out, float* out32,
+                     unsigned* err);
+
+// ---- mgpcg.cu (learned path) ----------------------------------------------
+// Records up to max_pairs (r_k, z_k = V-cycle(r_k)) pairs of an MGPCG run on
+// the current system into device arrays of max_pairs * N floats.
+jetgpu_status harvest_pairs(Ctx* c, unsigned max_pairs, float* r_out,
+                            float* z_out, unsigned* count);
+// sum(r^2) of an FP32 vector into scal[target] (device).
+jetgpu_status norm2f(Ctx* c, const float* r, long n, int target);
 
 // ---- transfer.cu ----------------------------------------------------------
 jetgpu_status p2g(Ctx* c, const GridDesc& g, long np, const double* pos,

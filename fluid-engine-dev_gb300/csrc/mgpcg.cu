@@ -800,7 +800,11 @@ static jetgpu_status pcg_f32(Ctx* c, double target, unsigned max_it,
     double rr = 0;
     while (it < max_it) {
         float* z = nullptr;
-        if (jetgpu_status vs = vcycle(c, c->kr, c->kz, L0.x2, &z)) return vs;
+        if (c->cfg.preconditioner == JETGPU_PRECOND_NONE) {
+            z = c->kr;  // plain CG: z = r
+        } else if (jetgpu_status vs = vcycle(c, c->kr, c->kz, L0.x2, &z)) {
+            return vs;
+        }
         {
             Prof pr(c, K_DOT_RZ, 8.0 * N);
             k_dot_rz<float, float><<<G, kThreads, 0, c->stream>>>(
@@ -887,6 +891,171 @@ static jetgpu_status pcg_f64(Ctx* c, double target, unsigned max_it,
     return JETGPU_OK;
 }
 
+// ---------------------------------------------------------------------------
+// Flexible PCG with the learned preconditioner (K18).
+
+namespace {
+
+// r.z_new -> scal[S_RZ], r.z_old -> scal[S_AUX] (FP64), one pass.
+__global__ void __launch_bounds__(kThreads)
+    k_dot_pr(const float* __restrict__ r, const float* __restrict__ z,
+             const float* __restrict__ zold, long N, double* partials,
+             unsigned* counters, double* scal) {
+    __shared__ double smem[32];
+    double a = 0.0, b = 0.0;
+    for (long c = blockIdx.x * (long)kThreads + threadIdx.x; c < N;
+         c += (long)gridDim.x * kThreads) {
+        const double rv = r[c];
+        a += rv * (double)z[c];
+        b += rv * (double)zold[c];
+    }
+    reduce_finish<kThreads>(a, 5, S_RZ, FIN_NONE, partials, counters, scal,
+                            smem);
+    __syncthreads();
+    reduce_finish<kThreads>(b, 6, S_AUX, FIN_NONE, partials, counters, scal,
+                            smem);
+}
+
+// Polak-Ribiere beta = r_k.(z_k - z_{k-1}) / (r_{k-1}.z_{k-1}); rolls r.z.
+__global__ void k_pr_beta(double* scal, int first) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        const double rz = scal[S_RZ], old = scal[S_RZ_OLD];
+        scal[S_BETA] = (first || old == 0.0) ? 0.0 : (rz - scal[S_AUX]) / old;
+        scal[S_RZ_OLD] = rz;
+    }
+}
+
+__global__ void __launch_bounds__(kThreads)
+    k_norm2f(const float* __restrict__ v, long N, double* partials,
+             unsigned* counters, double* scal, int target) {
+    __shared__ double smem[32];
+    double acc = 0.0;
+    for (long c = blockIdx.x * (long)kThreads + threadIdx.x; c < N;
+         c += (long)gridDim.x * kThreads)
+        acc += (double)v[c] * (double)v[c];
+    reduce_finish<kThreads>(acc, 7, target, FIN_NONE, partials, counters,
+                            scal, smem);
+}
+
+}  // namespace
+
+jetgpu_status norm2f(Ctx* c, const float* r, long n, int target) {
+    k_norm2f<<<red_blocks(c, n), kThreads, 0, c->stream>>>(
+        r, n, c->partials, c->counters, c->scal, target);
+    JG_CUDA(c, cudaGetLastError());
+    return JETGPU_OK;
+}
+
+// FPCG on the FP32 rows for a correction e with A e = r (r = kr on entry,
+// its squared norm in scal[S_R64]). Stops at ||r|| <= target, after max_it
+// iterations, or when progress stalls (*stalled = true; x so far is kept).
+static jetgpu_status fpcg_f32(Ctx* c, double target, unsigned max_it,
+                              unsigned* it_out, double* rr_out,
+                              bool* stalled) {
+    const Level& L0 = c->levels[0];
+    const Dims n = L0.n;
+    const long N = n.count();
+    const int G = red_blocks(c, N);
+    RowsF M{L0.A};
+    *stalled = false;
+    k_init_scalars<<<1, 32, 0, c->stream>>>(c->scal);
+    k_zero<float><<<grid_for(c, N), kThreads, 0, c->stream>>>(c->kz2, N);
+    float* z = c->kz;
+    float* zold = c->kz2;
+    std::vector<double> hist;
+    unsigned it = 0;
+    double rr = 0;
+    while (it < max_it) {
+        const double* rrp = c->scal + (it == 0 ? S_R64 : S_RR);
+        if (jetgpu_status s = net_apply(c, c->kr, rrp, z)) return s;
+        {
+            Prof pr(c, K_DOT_RZ, 12.0 * N);
+            k_dot_pr<<<G, kThreads, 0, c->stream>>>(c->kr, z, zold, N,
+                                                    c->partials, c->counters,
+                                                    c->scal);
+        }
+        k_pr_beta<<<1, 32, 0, c->stream>>>(c->scal, it == 0 ? 1 : 0);
+        {
+            Prof pr(c, K_UPDATE_D, 12.0 * N);
+            k_update_d<float, float><<<G, kThreads, 0, c->stream>>>(c->kd, z,
+                                                                    N, c->scal);
+        }
+        {
+            Prof pr(c, K_SPMV, 24.0 * N);
+            k_spmv_dot<float, RowsF><<<G, kThreads, 0, c->stream>>>(
+                M, c->kd, c->kq, n, c->partials, c->counters, c->scal);
+        }
+        {
+            Prof pr(c, K_UPDATE_XR, 24.0 * N);
+            k_update_xr<float><<<G, kThreads, 0, c->stream>>>(
+                c->kx, c->kr, c->kd, c->kq, nullptr, N, c->partials,
+                c->counters, c->scal);
+        }
+        std::swap(z, zold);
+        ++it;
+        jetgpu_status s = read_scalars(c);
+        if (s != JETGPU_OK) return s;
+        rr = c->h_scal[S_RR];
+        const double rz = c->h_scal[S_RZ];
+        if (!std::isfinite(rr) || !std::isfinite(rz) || rz <= 0.0) {
+            // A non-positive r.z means the network is not acting as a
+            // positive preconditioner here: stop and let multigrid finish.
+            *stalled = true;
+            break;
+        }
+        hist.push_back(std::sqrt(rr));
+        if (std::sqrt(rr) <= target) break;
+        const size_t k = hist.size();
+        if (k >= 6 && hist[k - 1] > 0.8 * hist[k - 4]) {
+            *stalled = true;
+            break;
+        }
+    }
+    if (*stalled && !std::isfinite(rr)) {
+        // Discard a non-finite correction.
+        k_zero<float><<<grid_for(c, N), kThreads, 0, c->stream>>>(c->kx, N);
+    }
+    *it_out = it;
+    *rr_out = rr;
+    return JETGPU_OK;
+}
+
+jetgpu_status harvest_pairs(Ctx* c, unsigned max_pairs, float* r_out,
+                            float* z_out, unsigned* count) {
+    const Level& L0 = c->levels[0];
+    const Dims n = L0.n;
+    const long N = n.count();
+    const int G = red_blocks(c, N);
+    RowsF M{L0.A};
+    // r = b (x = 0), FP32 image.
+    k_zero<double><<<grid_for(c, N), kThreads, 0, c->stream>>>(c->x64, N);
+    k_residual64<<<G, kThreads, 0, c->stream>>>(
+        c->A64, c->x64, c->b64, c->r64, c->kr, c->kx, n, c->partials,
+        c->counters, c->scal, S_R64);
+    k_init_scalars<<<1, 32, 0, c->stream>>>(c->scal);
+    unsigned k = 0;
+    for (; k < max_pairs; ++k) {
+        float* z = nullptr;
+        if (jetgpu_status vs = vcycle(c, c->kr, c->kz, L0.x2, &z)) return vs;
+        JG_CUDA(c, cudaMemcpyAsync(r_out + (size_t)k * N, c->kr, N * sizeof(float),
+                                   cudaMemcpyDeviceToDevice, c->stream));
+        JG_CUDA(c, cudaMemcpyAsync(z_out + (size_t)k * N, z, N * sizeof(float),
+                                   cudaMemcpyDeviceToDevice, c->stream));
+        k_dot_rz<float, float><<<G, kThreads, 0, c->stream>>>(
+            c->kr, z, N, c->partials, c->counters, c->scal);
+        k_update_d<float, float><<<G, kThreads, 0, c->stream>>>(c->kd, z, N,
+                                                                c->scal);
+        k_spmv_dot<float, RowsF><<<G, kThreads, 0, c->stream>>>(
+            M, c->kd, c->kq, n, c->partials, c->counters, c->scal);
+        k_update_xr<float><<<G, kThreads, 0, c->stream>>>(
+            c->kx, c->kr, c->kd, c->kq, nullptr, N, c->partials, c->counters,
+            c->scal);
+    }
+    JG_CUDA(c, cudaStreamSynchronize(c->stream));
+    *count = k;
+    return JETGPU_OK;
+}
+
 jetgpu_status mgpcg_solve(Ctx* c, jetgpu_solve_stats* st) {
     const Level& L0 = c->levels[0];
     const Dims n = L0.n;
@@ -911,6 +1080,12 @@ jetgpu_status mgpcg_solve(Ctx* c, jetgpu_solve_stats* st) {
     st->relative_residual = 0.0;
     if (bnorm == 0.0) return JETGPU_OK;
 
+    const bool learned = cfg.preconditioner == JETGPU_PRECOND_LEARNED;
+    if (learned && (fp64 || !net_supported(c)))
+        return fail(c, JETGPU_BAD_INPUT,
+                    "learned preconditioner needs a loaded network, FP32 "
+                    "Krylov vectors and a resolution divisible by 8");
+    bool fell_back = false;
     const double goal = cfg.tolerance * bnorm;
     double rnorm = bnorm;
     unsigned total = 0;
@@ -943,7 +1118,17 @@ jetgpu_status mgpcg_solve(Ctx* c, jetgpu_solve_stats* st) {
             // deliver; the FP64 pass loop does the rest.
             double eta = 0.5 * goal / rnorm;
             if (eta < 1e-4) eta = 1e-4;
-            s = pcg_f32(c, eta * rnorm, cfg.max_cg_iter - total, &it, &rr);
+            if (learned && !fell_back) {
+                bool stalled = false;
+                s = fpcg_f32(c, eta * rnorm, cfg.max_cg_iter - total, &it, &rr,
+                             &stalled);
+                if (stalled) {
+                    fell_back = true;
+                    st->fallback_used = 1;
+                }
+            } else {
+                s = pcg_f32(c, eta * rnorm, cfg.max_cg_iter - total, &it, &rr);
+            }
             if (s == JETGPU_OK) {
                 Prof pr(c, K_ACCUMULATE, 20.0 * N);
                 k_accumulate<<<grid_for(c, N), kThreads, 0, c->stream>>>(
@@ -968,7 +1153,7 @@ jetgpu_status mgpcg_solve(Ctx* c, jetgpu_solve_stats* st) {
             return fail(c, JETGPU_NOT_CONVERGED,
                         "tolerance not reached within the iteration cap");
     }
-    return JETGPU_OK;
+    return fell_back ? JETGPU_STALLED_FALLBACK_USED : JETGPU_OK;
 }
 
 }  // namespace jg

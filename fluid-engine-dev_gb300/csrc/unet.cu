@@ -403,3 +403,322 @@ extern "C" jetgpu_status jetgpu_conv3d_wgrad(void* stream, const void* in,
                         static_cast<const __nv_bfloat16*>(dy), co,
                         Dims{res[0], res[1], res[2]}, dw, err, sms);
 }
+
+// ---------------------------------------------------------------------------
+// K17: the preconditioner network. A 3-D U-Net with 4 levels (16, 32, 48,
+// 64 channels), two 3x3x3 convolutions per level and side, 2x2x2 average
+// pooling, nearest-neighbour upsampling and skip concatenation
+// [upsampled | skip]. Input: 16 channels of per-cell features of the
+// residual and the system (net_features below). Output: channel 0 of the
+// last convolution, scaled back to the residual's units.
+
+namespace jg {
+
+const NetLayer kNetLayers[kNetLayerCount] = {
+    {16, 16, 1, 0},  {16, 16, 1, 0},   // encoder, level 0
+    {16, 32, 1, 1},  {32, 32, 1, 1},   // level 1
+    {32, 48, 1, 2},  {48, 48, 1, 2},   // level 2
+    {48, 64, 1, 3},  {64, 64, 1, 3},   // level 3
+    {112, 48, 1, 2}, {48, 48, 1, 2},   // decoder, level 2 ([up(64) | 48])
+    {80, 32, 1, 1},  {32, 32, 1, 1},   // level 1 ([up(48) | 32])
+    {48, 16, 1, 0},  {16, 16, 0, 0}};  // level 0 ([up(32) | 16]), output
+
+size_t net_param_count() {
+    size_t n = 0;
+    for (int l = 0; l < kNetLayerCount; ++l)
+        n += (size_t)27 * kNetLayers[l].ci * kNetLayers[l].co + kNetLayers[l].co;
+    return n;
+}
+
+namespace {
+
+// Input features of cell c (16 channels, BF16): residual / rms(residual),
+// the six face weights of the cell, fluid indicator, diagonal * h^2 / 6.
+__global__ void k_net_features(const float* __restrict__ r,
+                               const double* __restrict__ rr, long N,
+                               const float* __restrict__ uw,
+                               const float* __restrict__ vw,
+                               const float* __restrict__ ww,
+                               const float* __restrict__ phi,
+                               const float4* __restrict__ A, float h2, Dims n,
+                               __nv_bfloat16* __restrict__ feat) {
+    const double ms = rr[0] / (double)N;
+    const float inv = ms > 0.0 ? (float)(1.0 / sqrt(ms)) : 0.0f;
+    for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < N;
+         c += (long)gridDim.x * blockDim.x) {
+        int i, j, k;
+        cell_ijk(c, n, i, j, k);
+        float f[16];
+        f[0] = r[c] * inv;
+        f[1] = uw[lin(i, j, k, n.x + 1, n.y)];
+        f[2] = uw[lin(i + 1, j, k, n.x + 1, n.y)];
+        f[3] = vw[lin(i, j, k, n.x, n.y + 1)];
+        f[4] = vw[lin(i, j + 1, k, n.x, n.y + 1)];
+        f[5] = ww[lin(i, j, k, n.x, n.y)];
+        f[6] = ww[lin(i, j, k + 1, n.x, n.y)];
+        f[7] = phi[c] < 0.0f ? 1.0f : 0.0f;
+        f[8] = A[c].x * h2 * (1.0f / 6.0f);
+#pragma unroll
+        for (int q = 9; q < 16; ++q) f[q] = 0.0f;
+        __align__(16) __nv_bfloat16 h[16];
+#pragma unroll
+        for (int q = 0; q < 16; ++q) h[q] = __float2bfloat16_rn(f[q]);
+        uint4* dst = reinterpret_cast<uint4*>(feat + c * 16);
+        dst[0] = reinterpret_cast<const uint4*>(h)[0];
+        dst[1] = reinterpret_cast<const uint4*>(h)[1];
+    }
+}
+
+// 2x2x2 average pooling, channels-last BF16 (FP32 sum, one rounding).
+__global__ void k_pool2(const __nv_bfloat16* __restrict__ in, Dims fine,
+                        int C, __nv_bfloat16* __restrict__ out) {
+    const Dims cs{fine.x / 2, fine.y / 2, fine.z / 2};
+    const long total = cs.count() * C;
+    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < total;
+         e += (long)gridDim.x * blockDim.x) {
+        const long c = e / C;
+        const int ch = (int)(e - c * C);
+        int i, j, k;
+        cell_ijk(c, cs, i, j, k);
+        float s = 0.0f;
+        for (int dz = 0; dz < 2; ++dz)
+            for (int dy = 0; dy < 2; ++dy)
+                for (int dx = 0; dx < 2; ++dx)
+                    s += __bfloat162float(
+                        in[lin(2 * i + dx, 2 * j + dy, 2 * k + dz, fine.x, fine.y) * C + ch]);
+        out[e] = __float2bfloat16_rn(0.125f * s);
+    }
+}
+
+// out[v] = [ coarse[v / 2] (C1 channels) | skip[v] (C2 channels) ].
+__global__ void k_up_concat(const __nv_bfloat16* __restrict__ coarse, int C1,
+                            const __nv_bfloat16* __restrict__ skip, int C2,
+                            Dims fine, __nv_bfloat16* __restrict__ out) {
+    const int C = C1 + C2;
+    const Dims cs{fine.x / 2, fine.y / 2, fine.z / 2};
+    const long total = fine.count() * C;
+    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < total;
+         e += (long)gridDim.x * blockDim.x) {
+        const long c = e / C;
+        const int ch = (int)(e - c * C);
+        int i, j, k;
+        cell_ijk(c, fine, i, j, k);
+        out[e] = ch < C1 ? coarse[lin(i >> 1, j >> 1, k >> 1, cs.x, cs.y) * C1 + ch]
+                         : skip[c * C2 + (ch - C1)];
+    }
+}
+
+// z[c] = out32[c][0] * rms(residual) * h^2 on fluid cells, 0 elsewhere.
+__global__ void k_net_output(const float* __restrict__ out32,
+                             const double* __restrict__ rr, long N, float h2,
+                             const float* __restrict__ phi,
+                             float* __restrict__ z) {
+    const double ms = rr[0] / (double)N;
+    const float scale = (float)sqrt(ms > 0.0 ? ms : 0.0) * h2;
+    for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < N;
+         c += (long)gridDim.x * blockDim.x)
+        z[c] = phi[c] < 0.0f ? out32[c * 16] * scale : 0.0f;
+}
+
+template <typename T>
+cudaError_t nalloc(T** p, size_t count) {
+    return cudaMalloc((void**)p, count * sizeof(T));
+}
+
+}  // namespace
+
+struct Net {
+    Dims n0{0, 0, 0};
+    __nv_bfloat16* w[kNetLayerCount] = {};
+    float* b[kNetLayerCount] = {};
+    // Activations per level.
+    __nv_bfloat16 *feat = nullptr, *t0 = nullptr, *e0 = nullptr, *u0 = nullptr,
+                  *d0 = nullptr;
+    __nv_bfloat16 *p1 = nullptr, *t1 = nullptr, *e1 = nullptr, *u1 = nullptr,
+                  *d1 = nullptr;
+    __nv_bfloat16 *p2 = nullptr, *t2 = nullptr, *e2 = nullptr, *u2 = nullptr,
+                  *d2 = nullptr;
+    __nv_bfloat16 *p3 = nullptr, *t3 = nullptr, *e3 = nullptr;
+    float* out32 = nullptr;
+    unsigned* err = nullptr;
+    bool loaded = false;
+};
+
+void net_free_acts(Net* net) {
+    __nv_bfloat16** acts[] = {&net->feat, &net->t0, &net->e0, &net->u0, &net->d0,
+                              &net->p1,   &net->t1, &net->e1, &net->u1, &net->d1,
+                              &net->p2,   &net->t2, &net->e2, &net->u2, &net->d2,
+                              &net->p3,   &net->t3, &net->e3};
+    for (auto p : acts) {
+        if (*p) cudaFree(*p);
+        *p = nullptr;
+    }
+    if (net->out32) cudaFree(net->out32);
+    net->out32 = nullptr;
+    net->n0 = Dims{0, 0, 0};
+}
+
+void net_destroy(void* p) {
+    Net* net = static_cast<Net*>(p);
+    if (!net) return;
+    net_free_acts(net);
+    for (int l = 0; l < kNetLayerCount; ++l) {
+        if (net->w[l]) cudaFree(net->w[l]);
+        if (net->b[l]) cudaFree(net->b[l]);
+    }
+    if (net->err) cudaFree(net->err);
+    delete net;
+}
+
+namespace {
+
+__global__ void k_f32_to_bf16(const float* __restrict__ in,
+                              __nv_bfloat16* __restrict__ out, long n) {
+    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < n;
+         e += (long)gridDim.x * blockDim.x)
+        out[e] = __float2bfloat16_rn(in[e]);
+}
+
+}  // namespace
+
+// Uploads FP32 parameters in the canonical order: per layer w[27][co][ci]
+// then b[co].
+jetgpu_status net_load(Ctx* c, const float* params, size_t count) {
+    if (count != net_param_count())
+        return fail(c, JETGPU_BAD_INPUT, "parameter count does not match the network");
+    Net* net = static_cast<Net*>(c->unet);
+    if (!net) {
+        net = new Net();
+        c->unet = net;
+        JG_CUDA(c, nalloc(&net->err, 1));
+        for (int l = 0; l < kNetLayerCount; ++l) {
+            const NetLayer& L = kNetLayers[l];
+            JG_CUDA(c, nalloc(&net->w[l], (size_t)27 * L.ci * L.co));
+            JG_CUDA(c, nalloc(&net->b[l], (size_t)L.co));
+        }
+    }
+    float* tmp = nullptr;
+    JG_CUDA(c, nalloc(&tmp, count));
+    JG_CUDA(c, cudaMemcpyAsync(tmp, params, count * sizeof(float),
+                               cudaMemcpyHostToDevice, c->stream));
+    size_t off = 0;
+    for (int l = 0; l < kNetLayerCount; ++l) {
+        const NetLayer& L = kNetLayers[l];
+        const long nw = 27L * L.ci * L.co;
+        k_f32_to_bf16<<<blocks_for(nw), kThreads, 0, c->stream>>>(tmp + off,
+                                                                  net->w[l], nw);
+        off += nw;
+        JG_CUDA(c, cudaMemcpyAsync(net->b[l], tmp + off, L.co * sizeof(float),
+                                   cudaMemcpyDeviceToDevice, c->stream));
+        off += L.co;
+    }
+    JG_CUDA(c, cudaStreamSynchronize(c->stream));
+    cudaFree(tmp);
+    JG_CUDA(c, cudaMemsetAsync(net->err, 0, sizeof(unsigned), c->stream));
+    net->loaded = true;
+    return JETGPU_OK;
+}
+
+static jetgpu_status net_ensure_acts(Ctx* c, Net* net, Dims n) {
+    if (net->n0.x == n.x && net->n0.y == n.y && net->n0.z == n.z) return JETGPU_OK;
+    net_free_acts(net);
+    const size_t V0 = n.count(), V1 = V0 / 8, V2 = V1 / 8, V3 = V2 / 8;
+    JG_CUDA(c, nalloc(&net->feat, V0 * 16));
+    JG_CUDA(c, nalloc(&net->t0, V0 * 16));
+    JG_CUDA(c, nalloc(&net->e0, V0 * 16));
+    JG_CUDA(c, nalloc(&net->u0, V0 * 48));
+    JG_CUDA(c, nalloc(&net->d0, V0 * 16));
+    JG_CUDA(c, nalloc(&net->p1, V1 * 16));
+    JG_CUDA(c, nalloc(&net->t1, V1 * 32));
+    JG_CUDA(c, nalloc(&net->e1, V1 * 32));
+    JG_CUDA(c, nalloc(&net->u1, V1 * 80));
+    JG_CUDA(c, nalloc(&net->d1, V1 * 32));
+    JG_CUDA(c, nalloc(&net->p2, V2 * 32));
+    JG_CUDA(c, nalloc(&net->t2, V2 * 48));
+    JG_CUDA(c, nalloc(&net->e2, V2 * 48));
+    JG_CUDA(c, nalloc(&net->u2, V2 * 112));
+    JG_CUDA(c, nalloc(&net->d2, V2 * 48));
+    JG_CUDA(c, nalloc(&net->p3, V3 * 48));
+    JG_CUDA(c, nalloc(&net->t3, V3 * 64));
+    JG_CUDA(c, nalloc(&net->e3, V3 * 64));
+    JG_CUDA(c, nalloc(&net->out32, V0 * 16));
+    net->n0 = n;
+    return JETGPU_OK;
+}
+
+bool net_supported(const Ctx* c) {
+    const Net* net = static_cast<const Net*>(c->unet);
+    const Dims n = c->levels.empty() ? Dims{0, 0, 0} : c->levels[0].n;
+    return net && net->loaded && n.x % 8 == 0 && n.y % 8 == 0 && n.z % 8 == 0 &&
+           n.x >= 8 && n.y >= 8 && n.z >= 8;
+}
+
+// Builds the 16 input channels of residual r on the current level-0 system.
+// rr: device pointer to sum(r^2).
+jetgpu_status net_features(Ctx* c, const float* r, const double* rr,
+                           void* feat) {
+    const Level& L = c->levels[0];
+    const float h2 = (float)(L.h[0] * L.h[0]);
+    k_net_features<<<blocks_for(L.n.count()), kThreads, 0, c->stream>>>(
+        r, rr, L.n.count(), L.uw, L.vw, L.ww, L.phi, L.A, h2, L.n,
+        static_cast<__nv_bfloat16*>(feat));
+    JG_CUDA(c, cudaGetLastError());
+    return JETGPU_OK;
+}
+
+// z = net(r) on the current level-0 system; rr = device sum(r^2).
+jetgpu_status net_apply(Ctx* c, const float* r, const double* rr, float* z) {
+    Net* net = static_cast<Net*>(c->unet);
+    const Level& L0 = c->levels[0];
+    const Dims n0 = L0.n, n1{n0.x / 2, n0.y / 2, n0.z / 2},
+               n2{n1.x / 2, n1.y / 2, n1.z / 2}, n3{n2.x / 2, n2.y / 2, n2.z / 2};
+    jetgpu_status s = net_ensure_acts(c, net, n0);
+    if (s != JETGPU_OK) return s;
+    Prof pr(c, K_UNET, 0.0);
+    cudaStream_t st = c->stream;
+    s = net_features(c, r, rr, net->feat);
+    if (s != JETGPU_OK) return s;
+    auto conv = [&](int l, const __nv_bfloat16* in, Dims n, __nv_bfloat16* out,
+                    float* out32) {
+        const NetLayer& Ly = kNetLayers[l];
+        return conv3d(st, in, Ly.ci, net->w[l], net->b[l], Ly.co, n, Ly.relu,
+                      out, out32, net->err);
+    };
+    auto pool = [&](const __nv_bfloat16* in, Dims fine, int C, __nv_bfloat16* out) {
+        k_pool2<<<blocks_for(fine.count() / 8 * C), kThreads, 0, st>>>(in, fine, C, out);
+    };
+    auto upcat = [&](const __nv_bfloat16* coarse, int C1, const __nv_bfloat16* skip,
+                     int C2, Dims fine, __nv_bfloat16* out) {
+        k_up_concat<<<blocks_for(fine.count() * (C1 + C2)), kThreads, 0, st>>>(
+            coarse, C1, skip, C2, fine, out);
+    };
+    jetgpu_status e = JETGPU_OK;
+    auto chk = [&](jetgpu_status x) { if (x != JETGPU_OK) e = x; };
+    chk(conv(0, net->feat, n0, net->t0, nullptr));
+    chk(conv(1, net->t0, n0, net->e0, nullptr));
+    pool(net->e0, n0, 16, net->p1);
+    chk(conv(2, net->p1, n1, net->t1, nullptr));
+    chk(conv(3, net->t1, n1, net->e1, nullptr));
+    pool(net->e1, n1, 32, net->p2);
+    chk(conv(4, net->p2, n2, net->t2, nullptr));
+    chk(conv(5, net->t2, n2, net->e2, nullptr));
+    pool(net->e2, n2, 48, net->p3);
+    chk(conv(6, net->p3, n3, net->t3, nullptr));
+    chk(conv(7, net->t3, n3, net->e3, nullptr));
+    upcat(net->e3, 64, net->e2, 48, n2, net->u2);
+    chk(conv(8, net->u2, n2, net->t2, nullptr));
+    chk(conv(9, net->t2, n2, net->d2, nullptr));
+    upcat(net->d2, 48, net->e1, 32, n1, net->u1);
+    chk(conv(10, net->u1, n1, net->t1, nullptr));
+    chk(conv(11, net->t1, n1, net->d1, nullptr));
+    upcat(net->d1, 32, net->e0, 16, n0, net->u0);
+    chk(conv(12, net->u0, n0, net->d0, nullptr));
+    chk(conv(13, net->d0, n0, nullptr, net->out32));
+    if (e != JETGPU_OK) return fail(c, e, "convolution launch failed");
+    k_net_output<<<blocks_for(n0.count()), kThreads, 0, st>>>(
+        net->out32, rr, n0.count(), (float)(L0.h[0] * L0.h[0]), L0.phi, z);
+    JG_CUDA(c, cudaGetLastError());
+    return JETGPU_OK;
+}
+
+}  // namespace jg

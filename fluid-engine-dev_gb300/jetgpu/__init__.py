@@ -94,6 +94,8 @@ STATUS = {0: "OK", 1: "NOT_CONVERGED", 2: "STALLED_FALLBACK_USED",
           3: "BAD_INPUT", 4: "CUDA_ERROR", 5: "OUT_OF_MEMORY",
           6: "NUMERICAL_ERROR", 7: "CAPACITY_EXCEEDED"}
 PRECISION = {"fp32": 0, "fp64": 1, "mixed": 2, "bf16": 2}
+PRECONDITIONER = {"multigrid": 0, "learned": 1, "none": 2}
+SOLVED = (0, 1, 2)  # OK, NOT_CONVERGED (last iterate applied), fallback used
 
 # Symbols include/jetgpu.h declares (checked by the CPU test suite).
 EXPORTS = (
@@ -104,7 +106,8 @@ EXPORTS = (
     "jetgpu_p2g", "jetgpu_g2p_flip", "jetgpu_g2p_pic", "jetgpu_get_level",
     "jetgpu_version", "jetgpu_get_stream", "jetgpu_profile",
     "jetgpu_profile_read", "jetgpu_p2g_device_noalloc", "jetgpu_conv3d",
-    "jetgpu_conv3d_wgrad",
+    "jetgpu_conv3d_wgrad", "jetgpu_net_param_count", "jetgpu_load_unet",
+    "jetgpu_harvest", "jetgpu_net_features", "jetgpu_net_apply",
 )
 
 
@@ -187,6 +190,16 @@ def library() -> C.CDLL:
     L.jetgpu_conv3d_wgrad.argtypes = [vp, vp, C.c_int, vp, C.c_int,
                                       C.POINTER(C.c_int), vp, vp]
     L.jetgpu_conv3d_wgrad.restype = C.c_int
+    L.jetgpu_net_param_count.argtypes = []
+    L.jetgpu_net_param_count.restype = C.c_size_t
+    L.jetgpu_load_unet.argtypes = [vp, vp, C.c_size_t]
+    L.jetgpu_load_unet.restype = C.c_int
+    L.jetgpu_harvest.argtypes = [vp, C.c_uint, vp, vp, C.POINTER(C.c_uint)]
+    L.jetgpu_harvest.restype = C.c_int
+    L.jetgpu_net_features.argtypes = [vp, vp, vp]
+    L.jetgpu_net_features.restype = C.c_int
+    L.jetgpu_net_apply.argtypes = [vp, vp, vp]
+    L.jetgpu_net_apply.restype = C.c_int
     L.jetgpu_get_stream.argtypes = [vp, C.POINTER(C.c_void_p)]
     L.jetgpu_get_stream.restype = C.c_int
     L.jetgpu_profile.argtypes = [vp, C.c_int]
@@ -305,7 +318,8 @@ class FdmMgpcgSolver3:
                  numberOfRestrictionIter=2, numberOfCorrectionIter=2,
                  numberOfCoarsestIter=10, numberOfFinalIter=2,
                  maxTolerance=1e-6, sorFactor=1.0, useRedBlackOrdering=True,
-                 precision="fp32", device=0, maxRefinements=6):
+                 precision="fp32", device=0, maxRefinements=6,
+                 preconditioner="multigrid"):
         if not useRedBlackOrdering:
             raise ValueError("the GPU smoother is red-black; the lexicographic "
                              "Gauss-Seidel sweep is serial by construction")
@@ -323,6 +337,7 @@ class FdmMgpcgSolver3:
         cfg.sor = sorFactor
         cfg.red_black = 1
         cfg.precision = PRECISION[precision]
+        cfg.preconditioner = PRECONDITIONER[preconditioner]
         cfg.max_refinements = maxRefinements
         self._ctx = None
         self.last_stats = SolveStats()
@@ -347,6 +362,12 @@ class FdmMgpcgSolver3:
             self.close()
         except Exception:
             pass
+
+    def load_network(self, params: np.ndarray) -> None:
+        """Uploads preconditioner-network parameters (flat FP32, the order
+        of jetgpu_net_param_count) for preconditioner='learned'."""
+        p = np.ascontiguousarray(params, np.float32).reshape(-1)
+        self.check(library().jetgpu_load_unet(self.context(), _p(p), p.size))
 
     def stream(self) -> int:
         """The context's cudaStream_t as an integer handle."""
@@ -397,7 +418,7 @@ class FdmMgpcgSolver3:
         st = library().jetgpu_mgpcg_solve_system(
             self.context(), res0, len(system.A), _p(A), _p(b), _p(x),
             C.byref(self.last_stats))
-        self.check(st, allow=(0, 1))
+        self.check(st, allow=SOLVED)
         system.x[0][...] = x
         return st == 0
 
@@ -472,7 +493,7 @@ class GridFractionalSinglePhasePressureSolver3:
             C.byref(fs), _p(su), _p(sv), _p(sw), _p(output.u), _p(output.v),
             _p(output.w), _p(p), C.byref(self.last_stats))
         solver.last_stats = self.last_stats
-        solver.check(st, allow=(0, 1))
+        solver.check(st, allow=SOLVED)
         self._pressure = p
         return st
 
@@ -510,7 +531,7 @@ def solve_pressure_device(solver: FdmMgpcgSolver3, grid: Grid, u, v, w,
         C.byref(fluid), _p(solid[0]), _p(solid[1]), _p(solid[2]), _p(out_u),
         _p(out_v), _p(out_w), _p(out_p), C.byref(stats))
     solver.last_stats = stats
-    return solver.check(st, allow=(0, 1))
+    return solver.check(st, allow=SOLVED)
 
 
 # ---------------------------------------------------------------------------

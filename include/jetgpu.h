@@ -63,7 +63,9 @@ typedef enum jetgpu_preconditioner {
     /* Learned U-Net preconditioner in flexible PCG, with the multigrid
      * preconditioner as fallback when iterations stall. Requires weights
      * loaded with jetgpu_load_unet(). */
-    JETGPU_PRECOND_LEARNED = 1
+    JETGPU_PRECOND_LEARNED = 1,
+    /* No preconditioner (plain CG); for comparisons. */
+    JETGPU_PRECOND_NONE = 2
 } jetgpu_preconditioner;
 
 /* Solver configuration. The first nine fields mirror the FdmMgpcgSolver3
@@ -319,6 +321,33 @@ jetgpu_status jetgpu_conv3d(void* stream, const void* in, int ci,
 jetgpu_status jetgpu_conv3d_wgrad(void* stream, const void* in, int ci,
                                   const void* dy, int co, const int res[3],
                                   float* dw, unsigned int* err);
+
+/* Number of FP32 parameters of the preconditioner network: per layer,
+ * w[27][co][ci] then b[co], for the 14 layers of the 4-level U-Net
+ * (16/32/48/64 channels). */
+size_t jetgpu_net_param_count(void);
+
+/* Loads network parameters (HOST pointer, FP32, the order above) into the
+ * context; stored as BF16 weights and FP32 biases. Enables
+ * preconditioner = JETGPU_PRECOND_LEARNED (flexible PCG). */
+jetgpu_status jetgpu_load_unet(struct jetgpu_ctx* ctx, const float* params,
+                               size_t count);
+
+/* Training data from the solver itself: runs multigrid PCG on the system of
+ * the context's last pressure solve and records, for each of up to
+ * max_pairs iterations, the residual r_k and the V-cycle correction
+ * z_k = M r_k (DEVICE arrays of max_pairs * cells floats each). */
+jetgpu_status jetgpu_harvest(struct jetgpu_ctx* ctx, unsigned int max_pairs,
+                             float* r_out, float* z_out,
+                             unsigned int* count);
+
+/* The network's 16 input channels (BF16, channels-last) for residual r on
+ * the last solved system, and the network's output z = net(r). DEVICE
+ * pointers; synchronous. */
+jetgpu_status jetgpu_net_features(struct jetgpu_ctx* ctx, const float* r,
+                                  void* feat);
+jetgpu_status jetgpu_net_apply(struct jetgpu_ctx* ctx, const float* r,
+                               float* z);
 
 /* Library version string. */
 const char* jetgpu_version(void);
