@@ -50,8 +50,6 @@ def parse_args():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=256)
-    ap.add_argument("--precision", default="fp32",
-                    choices=["fp32", "fp64", "mixed"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
     return ap.parse_args()
 
@@ -151,15 +149,28 @@ def workload(n: int):
                                      sphere=((0.6, 0.2, 0.5), 0.15))
 
 
-def solver_params(precision: str):
-    """GPU MGPCG settings: FdmMgpcgSolver3(200, 6, 2, 2, 10, 2, 1e-6, 1.0,
+def solver_params(precision: str, preconditioner: str = "multigrid"):
+    """GPU solver settings: FdmMgpcgSolver3(200, 6, 2, 2, 10, 2, 1e-6, 1.0,
     true). Two symmetric red-black sweeps per level and a masked coarse
     residual give mesh-independent convergence (5-8 iterations)."""
     return dict(numberOfCgIter=200, maxNumberOfLevels=6,
                 numberOfRestrictionIter=2, numberOfCorrectionIter=2,
                 numberOfCoarsestIter=10, numberOfFinalIter=2,
                 maxTolerance=TOL, sorFactor=1.0, useRedBlackOrdering=True,
-                precision=precision)
+                precision=precision, preconditioner=preconditioner,
+                maxRefinements=8)
+
+
+# The solver variants the metric compares, all to the same 1e-6 relative
+# true residual: plain MGPCG (FP32 Krylov and V-cycle, FP64-accurate
+# reductions and refinement), the mixed-precision V-cycle (BF16 rows), and
+# the learned U-Net preconditioner in flexible PCG over the mixed V-cycle
+# fallback (when trained weights are present).
+VARIANTS = {
+    "plain_mgpcg": ("fp32", "multigrid"),
+    "mixed_mgpcg": ("mixed", "multigrid"),
+    "learned_fpcg": ("mixed", "learned"),
+}
 
 
 def peaks() -> dict:
@@ -184,7 +195,6 @@ def traffic_per_launch(kernel: str, n: int):
 
 
 def run_ours(args, rank, world, local, pg):
-    import ctypes as C
     import numpy as np
     import torch
     import jetgpu
@@ -194,8 +204,6 @@ def run_ours(args, rank, world, local, pg):
     n = args.n
     h = 1.0 / n
     sc = workload(n)
-    solver = jetgpu.FdmMgpcgSolver3(**solver_params(args.precision),
-                                    device=local)
     grid = jetgpu.Grid()
     grid.res[:] = (n, n, n)
     grid.spacing[:] = (h, h, h)
@@ -218,42 +226,88 @@ def run_ours(args, rank, world, local, pg):
         return f
 
     bsdf, fsdf = field(d["boundary_sdf"]), field(d["fluid_sdf"])
-    stats = jetgpu.SolveStats()
-
-    def solve_device():
-        return jetgpu.solve_pressure_device(solver, grid, d["u"], d["v"],
-                                            d["w"], bsdf, fsdf, out["u"],
-                                            out["v"], out["w"], p_out,
-                                            stats=stats)
-
-    for _ in range(args.warmup):
-        solve_device()
-    stream = torch.cuda.ExternalStream(solver.stream(), device=dev)
-    clocks = Clocks(local)
-    iters, rel = [], []
-    barrier(pg, local)
-    torch.cuda.synchronize()
-    clocks.start()
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(args.steps):
-        solve_device()
-        iters.append(stats.iterations)
-        rel.append(stats.relative_residual)
-    e1.record(stream)
-    torch.cuda.synchronize()
-    ck = clocks.stop()
-    barrier(pg, local)
-    ms = e0.elapsed_time(e1) / args.steps
-    ms = max_over_ranks(pg, ms, local)
-    setup_ms, solve_ms = stats.setup_ms, stats.solve_ms
+
+    def make_solver(name):
+        prec, pre = VARIANTS[name]
+        solver = jetgpu.FdmMgpcgSolver3(**solver_params(prec, pre),
+                                        device=local)
+        if pre == "learned":
+            from jetgpu import learned
+            if not os.path.exists(learned.WEIGHTS):
+                solver.close()
+                return None
+            solver.load_network(learned.flatten(learned.load()))
+        return solver
+
+    def timed(solver, steps, warmup, clocks=None):
+        """Device-API solves timed with CUDA events on the library stream."""
+        stats = jetgpu.SolveStats()
+
+        def solve_device():
+            return jetgpu.solve_pressure_device(
+                solver, grid, d["u"], d["v"], d["w"], bsdf, fsdf, out["u"],
+                out["v"], out["w"], p_out, stats=stats)
+
+        for _ in range(warmup):
+            solve_device()
+        stream = torch.cuda.ExternalStream(solver.stream(), device=dev)
+        iters, rel = [], []
+        barrier(pg, local)
+        torch.cuda.synchronize()
+        if clocks:
+            clocks.start()
+        e0.record(stream)
+        for _ in range(steps):
+            solve_device()
+            iters.append(stats.iterations)
+            rel.append(stats.relative_residual)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ck = clocks.stop() if clocks else None
+        barrier(pg, local)
+        ms = max_over_ranks(pg, e0.elapsed_time(e1) / steps, local)
+        return dict(ms=ms, iters=iters, rel=rel, clocks=ck,
+                    setup_ms=stats.setup_ms, solve_ms=stats.solve_ms,
+                    fallback=stats.fallback_used, stream=stream,
+                    solve=solve_device)
+
+    variants = {}
+    results = {}
+    for name in VARIANTS:
+        solver = make_solver(name)
+        if solver is None:
+            variants[name] = {"status": "skipped: no trained weights"}
+            continue
+        r = timed(solver, args.steps, args.warmup, Clocks(local))
+        ok = max(r["rel"]) <= TOL
+        variants[name] = {
+            "ms_per_solve": round(r["ms"], 3),
+            "steps_per_s": round(1000.0 / r["ms"], 2),
+            "iterations_per_solve": r["iters"][-1],
+            "relative_residual": max(r["rel"]),
+            "reached_tolerance": ok,
+            "setup_ms": round(r["setup_ms"], 3),
+            "solve_ms": round(r["solve_ms"], 3),
+        }
+        if VARIANTS[name][1] == "learned":
+            variants[name]["multigrid_fallback_used"] = bool(r["fallback"])
+        results[name] = (solver, r, ok)
+    # Headline: the fastest variant that reached the tolerance.
+    head = min((k for k in results if results[k][2]),
+               key=lambda k: results[k][1]["ms"])
+    solver, r, _ = results[head]
+    for k, (s_, _, _) in results.items():
+        if k != head:
+            s_.close()
+    ms, ck = r["ms"], r["clocks"]
 
     # Second pass of the same K solves with every launch bracketed by events
     # on the library stream: per-kernel durations and launch counts.
     solver.profile(True)
     for _ in range(args.steps):
-        solve_device()
+        r["solve"]()
     prof = solver.profile_read()
     solver.profile(False)
     launches = sum(k["launches"] for k in prof)
@@ -291,6 +345,7 @@ def run_ours(args, rank, world, local, pg):
     cg = lambda t: jetgpu.CellCenteredScalarGrid3((n, n, n), (h, h, h),
                                                   (0, 0, 0), t.numpy())
     bg, fg = cg(pin["boundary_sdf"]), cg(pin["fluid_sdf"])
+    stream = r["stream"]
     for _ in range(max(1, args.warmup)):
         ps.solve(vel, 1 / 60, outg, bg, None, fg)
     barrier(pg, local)
@@ -303,10 +358,12 @@ def run_ours(args, rank, world, local, pg):
     e2e_ms = max_over_ranks(pg, e0.elapsed_time(e1) / args.steps, local)
     h2d = sum(pin[k].numel() * 8 for k in pin)
     d2h = sum(hout[k].numel() * 8 for k in hout) + n ** 3 * 8
+    solver.close()
     return dict(ms=ms, e2e_ms=e2e_ms, h2d=h2d, d2h=d2h, clocks=ck,
-                iters=iters, rel=rel, roofline=roofline, launches=launches,
-                whole_gbs=whole, solve_bytes=solve_bytes, profile=prof,
-                setup_ms=setup_ms, solve_ms=solve_ms, peak=pk)
+                iters=r["iters"], rel=r["rel"], roofline=roofline,
+                launches=launches, whole_gbs=whole, solve_bytes=solve_bytes,
+                profile=prof, setup_ms=r["setup_ms"], solve_ms=r["solve_ms"],
+                peak=pk, head=head, variants=variants)
 
 
 def cpu_reference():
@@ -419,22 +476,23 @@ def main():
         "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": round(r["ms"], 3), "higher_is_better": False,
         "scaling": "weak", "vs_baseline": None,
-        "dtype": {"fp32": "f32 (f64 reductions/refinement)",
-                  "fp64": "f64 (f32 V-cycle)",
-                  "mixed": "f32/bf16 (f64 reductions/refinement)"}[args.precision],
+        "dtype": {"fp32": "f32 (f64-accurate reductions/refinement)",
+                  "mixed": "f32 Krylov, bf16 V-cycle rows (f64-accurate "
+                           "reductions/refinement)"}[VARIANTS[r["head"]][0]],
         "data": "synthetic (seeded scene, no dataset)",
         "config": {
             "workload": f"{args.n}^3 FLIP dam break, first sub-step pressure "
                         "solve (weights + system + MGPCG + gradient), sphere "
                         "obstacle",
-            "grid": args.n, "tolerance": TOL, "precision": args.precision,
-            "solver": "MGPCG(200,6,2,2,10,2,1e-6,1.0,red-black), masked "
-                      "symmetric V-cycle",
+            "grid": args.n, "tolerance": TOL,
+            "solver": r["head"] + ": MGPCG(200,6,2,2,10,2,1e-6,1.0,"
+                      "red-black), masked symmetric V-cycle",
             "parallelism": f"replicas x{world}",
             "l2": "inputs and solver state >> L2 (no flush)",
             "roofline_timing": "per-launch CUDA events on the library stream "
                                "over a second pass of the K solves",
         },
+        "variants": r["variants"],
         "iterations_per_solve": iters[-1] if iters else None,
         "relative_residual": max(r["rel"]) if r["rel"] else None,
         "steps_per_s": round(1000.0 / r["ms"], 2),

@@ -47,12 +47,11 @@ void free_buffers(Ctx* c) {
         release(&L.vw);
         release(&L.ww);
         release(&L.A);
+        release(&L.Ah);
         release(&L.x);
         release(&L.x2);
         release(&L.b);
         release(&L.r);
-        release(&L.xh);
-        release(&L.bh);
         release(&L.Ah);
     }
     c->levels.clear();
@@ -60,6 +59,9 @@ void free_buffers(Ctx* c) {
     release(&c->b64);
     release(&c->x64);
     release(&c->r64);
+    release(&c->Alo);
+    release(&c->bdf);
+    release(&c->xdf);
     release(&c->kx);
     release(&c->kr);
     release(&c->kd);
@@ -211,6 +213,7 @@ jetgpu_status ensure_buffers(Ctx* c, Dims n, unsigned max_levels) {
         JG_CUDA(c, alloc(&L.vw, (size_t)s.x * (s.y + 1) * s.z));
         JG_CUDA(c, alloc(&L.ww, (size_t)s.x * s.y * (s.z + 1)));
         JG_CUDA(c, alloc(&L.A, N));
+        JG_CUDA(c, alloc(&L.Ah, N));
         JG_CUDA(c, alloc(&L.x, N));
         JG_CUDA(c, alloc(&L.x2, N));
         JG_CUDA(c, alloc(&L.b, N));
@@ -222,6 +225,9 @@ jetgpu_status ensure_buffers(Ctx* c, Dims n, unsigned max_levels) {
     JG_CUDA(c, alloc(&c->b64, N));
     JG_CUDA(c, alloc(&c->x64, N));
     JG_CUDA(c, alloc(&c->r64, N));
+    JG_CUDA(c, alloc(&c->Alo, N));
+    JG_CUDA(c, alloc(&c->bdf, N));
+    JG_CUDA(c, alloc(&c->xdf, N));
     JG_CUDA(c, alloc(&c->kx, N));
     JG_CUDA(c, alloc(&c->kr, N));
     JG_CUDA(c, alloc(&c->kd, N));
@@ -525,6 +531,8 @@ jetgpu_status jetgpu_mgpcg_solve_system(jetgpu_ctx* c, const int res0[3],
         off += N;
     }
     JG_CUDA(c, cudaGetLastError());
+    s = split_system(c);
+    if (s != JETGPU_OK) return s;
     s = prepare_levels(c);
     if (s != JETGPU_OK) return s;
     jetgpu_solve_stats local;

@@ -14,6 +14,7 @@
 #include "ctx.h"
 
 #include <cfloat>
+#include <cmath>
 #include <cstring>
 #include <map>
 #include <utility>
@@ -49,6 +50,85 @@ __device__ __forceinline__ void barycentric(double x, int iHigh, int* i,
 
 __device__ __forceinline__ double lerpd(double a, double b, double f) {
     return (1.0 - f) * a + f * b;
+}
+
+// GB300 issues FP64 at a small fraction of its FP32/integer rate, so the
+// exact replays below take integer-pipe shortcuts wherever they provably give
+// the bit pattern the double arithmetic gives.
+
+// phi < 0 for a double: sign bit set, not a zero, not a NaN (the word
+// moves of common.cuh keep these tests on the integer pipe).
+__device__ __forceinline__ bool neg_d(double x) {
+    unsigned lo, hi;
+    dwords(x, lo, hi);
+    const unsigned m = hi & 0x7fffffffu;
+    return (hi >> 31) != 0u && (m | lo) != 0u &&
+           (m < 0x7ff00000u || (m == 0x7ff00000u && lo == 0u));
+}
+__device__ __forceinline__ unsigned expo_d(double x) {
+    unsigned lo, hi;
+    dwords(x, lo, hi);
+    return (hi >> 20) & 0x7ffu;
+}
+// x * 0.5 exactly by an exponent decrement when x and x/2 are normal.
+__device__ __forceinline__ double half_d(double x) {
+    unsigned lo, hi;
+    dwords(x, lo, hi);
+    const unsigned e = (hi >> 20) & 0x7ffu;
+    if (e > 1u && e < 0x7ffu) return djoin(lo, hi - 0x100000u);
+    return x * 0.5;
+}
+// x * 2^k exactly by an exponent add when x and the result are normal;
+// zeros pass through; anything else multiplies by the FP64 scale.
+__device__ __forceinline__ double scale_pow2(double x, int k, double scale) {
+    unsigned lo, hi;
+    dwords(x, lo, hi);
+    const int e = (int)((hi >> 20) & 0x7ffu);
+    if (((hi & 0x7fffffffu) | lo) == 0u) return x;
+    if (e > 0 && e < 0x7ff && e + k > 0 && e + k < 0x7ff)
+        return djoin(lo, hi + ((unsigned)k << 20));
+    return x * scale;
+}
+// -x exactly by a sign flip, except that -(+0) stays +0 as 0.0 - 0.0 does.
+__device__ __forceinline__ double zero_minus(double x) {
+    unsigned lo, hi;
+    dwords(x, lo, hi);
+    if (((hi & 0x7fffffffu) | lo) == 0u) return djoin(0u, 0u);
+    return djoin(lo, hi ^ 0x80000000u);
+}
+// lerp(a, b, f) = (1 - f) * a + f * b (include/jet/detail/math_utils-inl.h)
+// with the fraction classes that dominate buildWeights' samples:
+//  * f = 0.5: both products are exact halvings, so the result is the one
+//    rounding of (a + b) / 2, i.e. half(a + b) — exact whenever a and b are
+//    zero or have exponent fields in [2, 0x7fd] (no overflow of a + b, no
+//    underflow of a / 2);
+//  * f = 0: the result is a + (0 * b), which is a itself when a is non-zero
+//    and b finite;
+//  * f = 1: (0 * a) + b, which is b when b is non-zero and a finite.
+// Everything else takes the reference's expression.
+constexpr long long kHalfBits = 0x3FE0000000000000LL;
+constexpr long long kOneBits = 0x3FF0000000000000LL;
+__device__ __forceinline__ bool half_ok(double x) {
+    unsigned lo, hi;
+    dwords(x, lo, hi);
+    const unsigned e = (hi >> 20) & 0x7ffu;
+    return (e >= 2u && e <= 0x7fdu) || ((hi & 0x7fffffffu) | lo) == 0u;
+}
+__device__ __forceinline__ bool nonzero_d(double x) {
+    unsigned lo, hi;
+    dwords(x, lo, hi);
+    return ((hi & 0x7fffffffu) | lo) != 0u;
+}
+__device__ __forceinline__ double lerp_c(double a, double b, double f,
+                                         long long fb) {
+    if (fb == kHalfBits) {
+        if (half_ok(a) && half_ok(b)) return half_d(a + b);
+    } else if (fb == 0LL) {
+        if (nonzero_d(a) && expo_d(b) != 0x7ffu) return a;
+    } else if (fb == kOneBits) {
+        if (nonzero_d(b) && expo_d(a) != 0x7ffu) return b;
+    }
+    return lerpd(a, b, f);
 }
 
 __device__ double sample_field(const FieldDesc& F, double x, double y,
@@ -97,7 +177,8 @@ __device__ __forceinline__ void cycle4(double* a) {
 }
 
 // Marching-squares area of the inside region of a face (fractionInside).
-__device__ double frac_inside(double bl, double br, double tl, double tr) {
+__device__ __noinline__ double frac_inside(double bl, double br, double tl,
+                                           double tr) {
     const int n = (bl < 0) + (tl < 0) + (br < 0) + (tr < 0);
     double l[4] = {bl, br, tr, tl};
     const double half = 0.5;  // 0.5f widened, exact
@@ -148,6 +229,11 @@ __device__ double frac_inside(double bl, double br, double tl, double tr) {
 
 __device__ __forceinline__ float face_weight(double p0, double p1, double p2,
                                              double p3) {
+    // All four corners on one side: fractionInside is exactly 1 (weight 0)
+    // or 0 (weight 1); decided with integer sign tests.
+    const int nin = neg_d(p0) + neg_d(p1) + neg_d(p2) + neg_d(p3);
+    if (nin == 4) return 0.0f;
+    if (nin == 0) return 1.0f;
     const double frac = frac_inside(p0, p1, p2, p3);
     double w = 1.0 - frac;
     w = (w < 0.0) ? 0.0 : ((w > 1.0) ? 1.0 : w);
@@ -161,9 +247,8 @@ __global__ void k_sample_fluid(float* __restrict__ phi, Dims n, GridDesc g,
     const long N = n.count();
     for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < N;
          c += (long)gridDim.x * blockDim.x) {
-        const int i = (int)(c % n.x);
-        const int j = (int)((c / n.x) % n.y);
-        const int k = (int)(c / ((long)n.x * n.y));
+        int i, j, k;
+        cell_ijk(c, n, i, j, k);
         // Grid3::cellCenterPosition (src/jet/grid3.cpp:32-38).
         const double px = g.origin[0] + g.spacing[0] * ((double)i + 0.5);
         const double py = g.origin[1] + g.spacing[1] * ((double)j + 0.5);
@@ -184,9 +269,8 @@ __global__ void k_face_weights(float* __restrict__ wgt, int axis, Dims fn,
     const double oz = g.origin[2] + 0.5 * (axis == 2 ? 0.0 : hz);
     for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < N;
          c += (long)gridDim.x * blockDim.x) {
-        const int i = (int)(c % fn.x);
-        const int j = (int)((c / fn.x) % fn.y);
-        const int k = (int)(c / ((long)fn.x * fn.y));
+        int i, j, k;
+        cell_ijk(c, fn, i, j, k);
         const double px = ox + hx * (double)i;
         const double py = oy + hy * (double)j;
         const double pz = oz + hz * (double)k;
@@ -225,9 +309,8 @@ __global__ void k_restrict_f32(const float* __restrict__ fine, Dims fs,
     const float stg[4] = {0.f, 1.f, 0.f, 0.f};
     for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < N;
          c += (long)gridDim.x * blockDim.x) {
-        const int i = (int)(c % cs.x);
-        const int j = (int)((c / cs.x) % cs.y);
-        const int k = (int)(c / ((long)cs.x * cs.y));
+        int i, j, k;
+        cell_ijk(c, cs, i, j, k);
         int iI[4], jI[4], kI[4];
         auto taps = [](int ks, int q, int nq, int* o) {
             o[0] = (q > 0) ? 2 * q - 1 : 2 * q;
@@ -257,11 +340,30 @@ __global__ void k_restrict_f32(const float* __restrict__ fine, Dims fs,
     }
 }
 
+// Air-side term of buildSingleSystem: term / max(theta, 0.01) with theta =
+// fractionInsideSdf(phi_c, phi_n). Out of line, so warps without a
+// free-surface face never issue its FP64 divisions.
+__device__ __noinline__ double air_term(double term, double cphi, double np) {
+    return term / fmax(frac_sdf(cphi, np), 0.01);
+}
+
+// Spacing factors of one level: 1/h and 1/h^2 per axis and, when they are
+// powers of two (h = 2^-m, the usual unit-cube grids), their exponents, so
+// that products with them become exact exponent adds (scale_pow2).
+struct SpacingInv {
+    double ih[3], ih2[3];
+    int k[3], k2[3];
+    int pow2;
+};
+
 // K4: buildSingleSystem (:117-267). Writes the FP32 rows of every level;
 // on the finest level also the exact FP64 rows and rhs. u/v/w are the input
 // velocity (finest level only; coarse right-hand sides are dead, overwritten
-// by restriction in the V-cycle, include/jet/detail/mg-inl.h:28-30).
-__global__ void k_build_system(Dims n, double hx, double hy, double hz,
+// by restriction in the V-cycle, include/jet/detail/mg-inl.h:28-30). Every
+// FP64 sum and product is the reference's, in its order; what changes is how
+// the exact ones are issued: classification on the FP32 SDF, exact widening
+// and power-of-two scaling on the integer pipe, divisions out of line.
+__global__ void k_build_system(Dims n, SpacingInv S,
                                const float* __restrict__ phi,
                                const float* __restrict__ uw,
                                const float* __restrict__ vw,
@@ -274,99 +376,72 @@ __global__ void k_build_system(Dims n, double hx, double hy, double hz,
                                const double* __restrict__ sw,
                                double* __restrict__ A64,
                                double* __restrict__ b64,
-                               float4* __restrict__ A32) {
+                               float4* __restrict__ A32,
+                               float4* __restrict__ Alo,
+                               float2* __restrict__ bdf) {
     const long N = n.count();
-    const double ihx = 1.0 / hx, ihy = 1.0 / hy, ihz = 1.0 / hz;
-    const double ihx2 = ihx * ihx, ihy2 = ihy * ihy, ihz2 = ihz * ihz;
     const int ux = n.x + 1;  // u-face row length
+    const bool pw = S.pow2 != 0;
     for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < N;
          c += (long)gridDim.x * blockDim.x) {
-        const int i = (int)(c % n.x);
-        const int j = (int)((c / n.x) % n.y);
-        const int k = (int)(c / ((long)n.x * n.y));
+        int i, j, k;
+        cell_ijk(c, n, i, j, k);
         double center = 0.0, right = 0.0, up = 0.0, front = 0.0, bb = 0.0;
-        const double cphi = phi[c];
-        if (inside(cphi)) {
+        const float cphf = phi[c];
+        bool fluid = false;
+        if (cphf < 0.0f) {  // the same test as on the exact widening
+            fluid = true;
+            const double cphi = widen_f32(cphf);
             const long uR = lin(i + 1, j, k, ux, n.y), uL = lin(i, j, k, ux, n.y);
             const long vU = lin(i, j + 1, k, n.x, n.y + 1),
                        vD = lin(i, j, k, n.x, n.y + 1);
             const long wF = lin(i, j, k + 1, n.x, n.y), wB = lin(i, j, k, n.x, n.y);
             const long sy = n.x, sz = (long)n.x * n.y;
-            double term;
-            if (i + 1 < n.x) {
-                term = (double)uw[uR] * ihx2;
-                const double np = phi[c + 1];
-                if (inside(np)) {
-                    center += term;
-                    right -= term;
-                } else {
-                    center += term / fmax(frac_sdf(cphi, np), 0.01);
+            // One face: the centre term (or the air-side term), the
+            // off-diagonal of a fluid neighbour on the upper side, and the
+            // rhs term (weighted inside, unweighted on the domain boundary).
+            auto face = [&](bool has, const float* wts, long f, long nbc, int a,
+                            const double* vel, bool plus, double* off) {
+                if (has) {
+                    const double wd = widen_f32(wts[f]);
+                    const double term = pw ? scale_pow2(wd, S.k2[a], S.ih2[a])
+                                           : wd * S.ih2[a];
+                    const float npf = phi[nbc];
+                    if (npf < 0.0f) {
+                        center += term;
+                        if (off) *off = zero_minus(term);  // 0.0 - term
+                    } else {
+                        center += air_term(term, cphi, widen_f32(npf));
+                    }
+                    if (vel) {
+                        const double p = wd * vel[f];
+                        const double t = pw ? scale_pow2(p, S.k[a], S.ih[a])
+                                            : p * S.ih[a];
+                        bb = plus ? bb + t : bb - t;
+                    }
+                } else if (vel) {
+                    const double t = pw ? scale_pow2(vel[f], S.k[a], S.ih[a])
+                                        : vel[f] * S.ih[a];
+                    bb = plus ? bb + t : bb - t;
                 }
-                if (u) bb += (double)uw[uR] * u[uR] * ihx;
-            } else if (u) {
-                bb += u[uR] * ihx;
-            }
-            if (i > 0) {
-                term = (double)uw[uL] * ihx2;
-                const double np = phi[c - 1];
-                if (inside(np)) center += term;
-                else center += term / fmax(frac_sdf(cphi, np), 0.01);
-                if (u) bb -= (double)uw[uL] * u[uL] * ihx;
-            } else if (u) {
-                bb -= u[uL] * ihx;
-            }
-            if (j + 1 < n.y) {
-                term = (double)vw[vU] * ihy2;
-                const double np = phi[c + sy];
-                if (inside(np)) {
-                    center += term;
-                    up -= term;
-                } else {
-                    center += term / fmax(frac_sdf(cphi, np), 0.01);
-                }
-                if (u) bb += (double)vw[vU] * v[vU] * ihy;
-            } else if (u) {
-                bb += v[vU] * ihy;
-            }
-            if (j > 0) {
-                term = (double)vw[vD] * ihy2;
-                const double np = phi[c - sy];
-                if (inside(np)) center += term;
-                else center += term / fmax(frac_sdf(cphi, np), 0.01);
-                if (u) bb -= (double)vw[vD] * v[vD] * ihy;
-            } else if (u) {
-                bb -= v[vD] * ihy;
-            }
-            if (k + 1 < n.z) {
-                term = (double)ww[wF] * ihz2;
-                const double np = phi[c + sz];
-                if (inside(np)) {
-                    center += term;
-                    front -= term;
-                } else {
-                    center += term / fmax(frac_sdf(cphi, np), 0.01);
-                }
-                if (u) bb += (double)ww[wF] * w[wF] * ihz;
-            } else if (u) {
-                bb += w[wF] * ihz;
-            }
-            if (k > 0) {
-                term = (double)ww[wB] * ihz2;
-                const double np = phi[c - sz];
-                if (inside(np)) center += term;
-                else center += term / fmax(frac_sdf(cphi, np), 0.01);
-                if (u) bb -= (double)ww[wB] * w[wB] * ihz;
-            } else if (u) {
-                bb -= w[wB] * ihz;
-            }
+            };
+            face(i + 1 < n.x, uw, uR, c + 1, 0, u, true, &right);
+            face(i > 0, uw, uL, c - 1, 0, u, false, nullptr);
+            face(j + 1 < n.y, vw, vU, c + sy, 1, v, true, &up);
+            face(j > 0, vw, vD, c - sy, 1, v, false, nullptr);
+            face(k + 1 < n.z, ww, wF, c + sz, 2, w, true, &front);
+            face(k > 0, ww, wB, c - sz, 2, w, false, nullptr);
             if (u && !su && !sv && !sw) {
                 // Static collider: every term of the moving-boundary sum is
                 // (1 - w) * 0 * invH = +0, so the sum is +0 and adding it
                 // only turns -0 into +0 — exactly what this does.
-                bb = bb + 0.0;
+                unsigned lo, hi;
+                dwords(bb, lo, hi);
+                if (hi == 0x80000000u && lo == 0u) bb = djoin(0u, 0u);
             } else if (u) {
                 // Moving-boundary contribution (:241-255), evaluated as the
                 // reference's single left-to-right expression.
+                const double ihx = S.ih[0], ihy = S.ih[1], ihz = S.ih[2];
                 const double sR = su ? su[uR] : 0.0, sL = su ? su[uL] : 0.0;
                 const double sU = sv ? sv[vU] : 0.0, sD = sv ? sv[vD] : 0.0;
                 const double sF = sw ? sw[wF] : 0.0, sB = sw ? sw[wB] : 0.0;
@@ -378,7 +453,13 @@ __global__ void k_build_system(Dims n, double hx, double hy, double hz,
                                        (1.0 - (double)ww[wB]) * sB * ihz;
                 bb += contrib;
             }
-            if (center < DBL_EPSILON) {  // kEpsilonD (:259-262)
+            // center < kEpsilonD (:259-262); center is a sum of non-negative
+            // terms, so its bit pattern orders like its value.
+            unsigned clo, chi;
+            dwords(center, clo, chi);
+            const unsigned long long cbits =
+                ((unsigned long long)chi << 32) | clo;
+            if (cbits < 0x3CB0000000000000ULL) {  // DBL_EPSILON
                 center = 1.0;
                 bb = 0.0;
             }
@@ -392,15 +473,62 @@ __global__ void k_build_system(Dims n, double hx, double hy, double hz,
             A64[4 * c + 3] = front;
         }
         if (b64) b64[c] = bb;
-        A32[c] = make_float4((float)center, (float)right, (float)up,
-                             (float)front);
+        // FP32 rows (= the FP32 rounding of the exact rows) and, on the
+        // finest level, the low parts that make hi + lo carry ~48 bits of
+        // each coefficient and of b for the double-float true residual.
+        float4 hi4, lo4;
+        float bh, bl;
+        if (fluid) {
+            split_f64(center, hi4.x, lo4.x);
+            split_f64(right, hi4.y, lo4.y);
+            split_f64(up, hi4.z, lo4.z);
+            split_f64(front, hi4.w, lo4.w);
+            split_f64(bb, bh, bl);
+        } else {
+            hi4 = make_float4(1.0f, 0.0f, 0.0f, 0.0f);
+            lo4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+            bh = bl = 0.0f;
+        }
+        A32[c] = hi4;
+        if (Alo) Alo[c] = lo4;
+        if (bdf) bdf[c] = make_float2(bh, bl);
     }
 }
 
-// K12: applyPressureGradient (:715-765). Each face i+1/j+1/k+1 of cell c is
-// written only by the thread of cell c, which also reads it, so the output
-// may alias the input.
-__global__ void k_apply_gradient(Dims n, double ihx, double ihy, double ihz,
+// Double-float image of a caller-built finest-level system (the FP32 rows
+// are written by the caller's conversion; this adds the low parts and b).
+__global__ void k_split_system(const double* __restrict__ A64,
+                               const double* __restrict__ b64,
+                               float4* __restrict__ Alo,
+                               float2* __restrict__ bdf, long N) {
+    for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < N;
+         c += (long)gridDim.x * blockDim.x) {
+        float4 hi4, lo4;
+        split_f64(A64[4 * c + 0], hi4.x, lo4.x);
+        split_f64(A64[4 * c + 1], hi4.y, lo4.y);
+        split_f64(A64[4 * c + 2], hi4.z, lo4.z);
+        split_f64(A64[4 * c + 3], hi4.w, lo4.w);
+        Alo[c] = lo4;
+        float bh, bl;
+        split_f64(b64[c], bh, bl);
+        bdf[c] = make_float2(bh, bl);
+    }
+}
+
+// Gradient coefficient invH / max(theta, 0.01) of a face with an air side
+// (out of line: only free-surface faces issue the FP64 divisions).
+__device__ __noinline__ double grad_coef(double ih, float cphf, float npf) {
+    return ih / fmax(frac_sdf(widen_f32(cphf), widen_f32(npf)), 0.01);
+}
+
+// K12: applyPressureGradient (:715-765). The output starts as a copy of the
+// input (grid_fluid_solver3.cpp:245-250); faces with a positive weight and a
+// fluid side get u + invH / max(theta, 0.01) * (x_n - x_c). The thread of
+// cell c owns the faces i+1/j+1/k+1 of c, and the cells on the lower domain
+// boundary also own faces 0, so every output face is written once; with
+// `copy` false (output aliasing the input) untouched faces are skipped.
+// Between two fluid cells theta = 1 and invH / 1 = invH exactly.
+__global__ void k_apply_gradient(Dims n, SpacingInv S,
                                  const float* __restrict__ phi,
                                  const float* __restrict__ uw,
                                  const float* __restrict__ vw,
@@ -408,39 +536,41 @@ __global__ void k_apply_gradient(Dims n, double ihx, double ihy, double ihz,
                                  const double* __restrict__ x,
                                  const double* u, const double* v,
                                  const double* w, double* ou, double* ov,
-                                 double* ow) {
+                                 double* ow, int copy) {
     const long N = n.count();
     const int ux = n.x + 1;
+    const long sz = (long)n.x * n.y;
+    const bool pw = S.pow2 != 0;
     for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < N;
          c += (long)gridDim.x * blockDim.x) {
-        const int i = (int)(c % n.x);
-        const int j = (int)((c / n.x) % n.y);
-        const int k = (int)(c / ((long)n.x * n.y));
-        const double cphi = phi[c];
-        if (i + 1 < n.x) {
-            const long f = lin(i + 1, j, k, ux, n.y);
-            const double np = phi[c + 1];
-            if ((double)uw[f] > 0.0 && (inside(cphi) || inside(np))) {
-                const double th = fmax(frac_sdf(cphi, np), 0.01);
-                ou[f] = u[f] + ihx / th * (x[c + 1] - x[c]);
+        int i, j, k;
+        cell_ijk(c, n, i, j, k);
+        const float cphf = phi[c];
+        const bool cin = cphf < 0.0f;
+        auto face = [&](bool inner, const float* wts, long f, long nbc, int a,
+                        const double* in, double* out) {
+            if (inner) {
+                const float npf = phi[nbc];
+                if (wts[f] > 0.0f && (cin || npf < 0.0f)) {
+                    const double dx = x[nbc] - x[c];
+                    double g;
+                    if (cin && npf < 0.0f)
+                        g = pw ? scale_pow2(dx, S.k[a], S.ih[a]) : S.ih[a] * dx;
+                    else
+                        g = grad_coef(S.ih[a], cphf, npf) * dx;
+                    out[f] = in[f] + g;
+                    return;
+                }
             }
-        }
-        if (j + 1 < n.y) {
-            const long f = lin(i, j + 1, k, n.x, n.y + 1);
-            const double np = phi[c + n.x];
-            if ((double)vw[f] > 0.0 && (inside(cphi) || inside(np))) {
-                const double th = fmax(frac_sdf(cphi, np), 0.01);
-                ov[f] = v[f] + ihy / th * (x[c + n.x] - x[c]);
-            }
-        }
-        if (k + 1 < n.z) {
-            const long sz = (long)n.x * n.y;
-            const long f = lin(i, j, k + 1, n.x, n.y);
-            const double np = phi[c + sz];
-            if ((double)ww[f] > 0.0 && (inside(cphi) || inside(np))) {
-                const double th = fmax(frac_sdf(cphi, np), 0.01);
-                ow[f] = w[f] + ihz / th * (x[c + sz] - x[c]);
-            }
+            if (copy) out[f] = in[f];
+        };
+        face(i + 1 < n.x, uw, lin(i + 1, j, k, ux, n.y), c + 1, 0, u, ou);
+        face(j + 1 < n.y, vw, lin(i, j + 1, k, n.x, n.y + 1), c + n.x, 1, v, ov);
+        face(k + 1 < n.z, ww, lin(i, j, k + 1, n.x, n.y), c + sz, 2, w, ow);
+        if (copy) {
+            if (i == 0) ou[lin(0, j, k, ux, n.y)] = u[lin(0, j, k, ux, n.y)];
+            if (j == 0) ov[lin(i, 0, k, n.x, n.y + 1)] = v[lin(i, 0, k, n.x, n.y + 1)];
+            if (k == 0) ow[lin(i, j, 0, n.x, n.y)] = w[lin(i, j, 0, n.x, n.y)];
         }
     }
 }
@@ -477,9 +607,17 @@ __device__ __forceinline__ double trilerp_at(const double* __restrict__ d,
     const double f010 = d[lin(i, jp1, k, rx, ry)], f110 = d[lin(ip1, jp1, k, rx, ry)];
     const double f001 = d[lin(i, j, kp1, rx, ry)], f101 = d[lin(ip1, j, kp1, rx, ry)];
     const double f011 = d[lin(i, jp1, kp1, rx, ry)], f111 = d[lin(ip1, jp1, kp1, rx, ry)];
-    const double b0 = lerpd(lerpd(f000, f100, fx), lerpd(f010, f110, fx), fy);
-    const double b1 = lerpd(lerpd(f001, f101, fx), lerpd(f011, f111, fx), fy);
-    return lerpd(b0, b1, fz);
+    auto cls = [](double f) {
+        unsigned lo, hi;
+        dwords(f, lo, hi);
+        return (long long)(((unsigned long long)hi << 32) | lo);
+    };
+    const long long bx = cls(fx), by = cls(fy), bz = cls(fz);
+    const double b0 = lerp_c(lerp_c(f000, f100, fx, bx),
+                             lerp_c(f010, f110, fx, bx), fy, by);
+    const double b1 = lerp_c(lerp_c(f001, f101, fx, bx),
+                             lerp_c(f011, f111, fx, bx), fy, by);
+    return lerp_c(b0, b1, fz, bz);
 }
 
 struct TabLayout {
@@ -528,8 +666,8 @@ __global__ void k_node_grid(FieldDesc B, const int* __restrict__ sidx,
     const long N = (long)S.x * S.y * S.z;
     for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < N;
          c += (long)gridDim.x * blockDim.x) {
-        const int a = (int)(c % S.x), b = (int)((c / S.x) % S.y),
-                  z = (int)(c / ((long)S.x * S.y));
+        int a, b, z;
+        cell_ijk(c, Dims{S.x, S.y, S.z}, a, b, z);
         node[c] = trilerp_at(B.data, B.res, sidx[soff.x + a], sfrac[soff.x + a],
                              sidx[soff.y + b], sfrac[soff.y + b],
                              sidx[soff.z + z], sfrac[soff.z + z]);
@@ -544,9 +682,8 @@ __global__ void k_face_weights_nodes(float* __restrict__ wgt, int axis,
     const long N = fn.count();
     for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < N;
          c += (long)gridDim.x * blockDim.x) {
-        const int i = (int)(c % fn.x);
-        const int j = (int)((c / fn.x) % fn.y);
-        const int k = (int)(c / ((long)fn.x * fn.y));
+        int i, j, k;
+        cell_ijk(c, fn, i, j, k);
         // Lower/upper slot along each axis: N for the normal axis (same for
         // both), M/P for the tangential axes.
         const int q[3] = {i, j, k};
@@ -592,12 +729,14 @@ __global__ void k_sample_fluid_tab(float* __restrict__ phi, Dims n,
     const int ox = L.off[0][3], oy = L.off[1][3], oz = L.off[2][3];
     for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < N;
          c += (long)gridDim.x * blockDim.x) {
-        const int i = (int)(c % n.x);
-        const int j = (int)((c / n.x) % n.y);
-        const int k = (int)(c / ((long)n.x * n.y));
-        phi[c] = (float)trilerp_at(F.data, F.res, idx[ox + i], frac[ox + i],
-                                   idx[oy + j], frac[oy + j], idx[oz + k],
-                                   frac[oz + k]);
+        int i, j, k;
+        cell_ijk(c, n, i, j, k);
+        float hi, lo;
+        split_f64(trilerp_at(F.data, F.res, idx[ox + i], frac[ox + i],
+                             idx[oy + j], frac[oy + j], idx[oz + k],
+                             frac[oz + k]),
+                  hi, lo);
+        phi[c] = hi;  // == (float) of the sample
     }
 }
 
@@ -797,6 +936,25 @@ jetgpu_status build_weights(Ctx* c, const GridDesc& g, const FieldDesc& bsdf,
     return JETGPU_OK;
 }
 
+// 1/h and 1/h^2 as the kernel's double arithmetic forms them, with their
+// power-of-two exponents when every factor is an exact power of two.
+SpacingInv spacing_inv(double hx, double hy, double hz) {
+    SpacingInv S;
+    const double h[3] = {hx, hy, hz};
+    S.pow2 = 1;
+    for (int a = 0; a < 3; ++a) {
+        S.ih[a] = 1.0 / h[a];
+        S.ih2[a] = S.ih[a] * S.ih[a];
+        int e1 = 0, e2 = 0;
+        const double m1 = std::frexp(S.ih[a], &e1);
+        const double m2 = std::frexp(S.ih2[a], &e2);
+        S.k[a] = e1 - 1;
+        S.k2[a] = e2 - 1;
+        if (m1 != 0.5 || m2 != 0.5) S.pow2 = 0;
+    }
+    return S;
+}
+
 jetgpu_status build_system(Ctx* c, const GridDesc& g, const double* u,
                            const double* v, const double* w,
                            const double* su, const double* sv,
@@ -816,11 +974,21 @@ jetgpu_status build_system(Ctx* c, const GridDesc& g, const double* u,
         Prof pr(c, K_SYSTEM, (top ? 16.0 + 32.0 + 8.0 + 24.0 : 16.0 + 16.0) *
                                 (double)L.n.count());
         k_build_system<<<blocks_for(L.n.count()), kThreads, 0, c->stream>>>(
-            L.n, hx, hy, hz, L.phi, L.uw, L.vw, L.ww, top ? u : nullptr,
+            L.n, spacing_inv(hx, hy, hz), L.phi, L.uw, L.vw, L.ww,
+            top ? u : nullptr,
             top ? v : nullptr, top ? w : nullptr, top ? su : nullptr,
             top ? sv : nullptr, top ? sw : nullptr, top ? c->A64 : nullptr,
-            top ? c->b64 : nullptr, L.A);
+            top ? c->b64 : nullptr, L.A, top ? c->Alo : nullptr,
+            top ? c->bdf : nullptr);
     }
+    JG_CUDA(c, cudaGetLastError());
+    return JETGPU_OK;
+}
+
+jetgpu_status split_system(Ctx* c) {
+    const long N = c->levels[0].n.count();
+    k_split_system<<<blocks_for(N), kThreads, 0, c->stream>>>(
+        c->A64, c->b64, c->Alo, c->bdf, N);
     JG_CUDA(c, cudaGetLastError());
     return JETGPU_OK;
 }
@@ -830,21 +998,14 @@ jetgpu_status apply_gradient(Ctx* c, const GridDesc& g, const double* u,
                              double* ov, double* ow) {
     const Level& L = c->levels[0];
     const Dims n = L.n;
-    const long nu = (long)(n.x + 1) * n.y * n.z, nv = (long)n.x * (n.y + 1) * n.z,
-               nw = (long)n.x * n.y * (n.z + 1);
-    if (ou != u)
-        JG_CUDA(c, cudaMemcpyAsync(ou, u, nu * 8, cudaMemcpyDeviceToDevice,
-                                   c->stream));
-    if (ov != v)
-        JG_CUDA(c, cudaMemcpyAsync(ov, v, nv * 8, cudaMemcpyDeviceToDevice,
-                                   c->stream));
-    if (ow != w)
-        JG_CUDA(c, cudaMemcpyAsync(ow, w, nw * 8, cudaMemcpyDeviceToDevice,
-                                   c->stream));
+    const bool alias = (ou == u) && (ov == v) && (ow == w);
+    if (!alias && ((ou == u) || (ov == v) || (ow == w)))
+        return fail(c, JETGPU_BAD_INPUT,
+                    "output faces must all alias the input or none");
     Prof pr(c, K_GRADIENT, (4.0 + 12.0 + 8.0 + 48.0) * (double)n.count());
     k_apply_gradient<<<blocks_for(n.count()), kThreads, 0, c->stream>>>(
-        n, 1.0 / g.spacing[0], 1.0 / g.spacing[1], 1.0 / g.spacing[2], L.phi,
-        L.uw, L.vw, L.ww, c->x64, u, v, w, ou, ov, ow);
+        n, spacing_inv(g.spacing[0], g.spacing[1], g.spacing[2]), L.phi, L.uw,
+        L.vw, L.ww, c->x64, u, v, w, ou, ov, ow, alias ? 0 : 1);
     JG_CUDA(c, cudaGetLastError());
     return JETGPU_OK;
 }

@@ -5,6 +5,7 @@
 #include <cuda_bf16.h>
 
 #include <string>
+#include <unordered_map>
 #include <vector>
 
 #include "../../include/jetgpu.h"
@@ -25,9 +26,7 @@ struct Level {
     float* x2 = nullptr;         // ping-pong partner of x (fused smoother)
     float* b = nullptr;          // V-cycle rhs
     float* r = nullptr;          // residual scratch
-    __nv_bfloat16* xh = nullptr; // BF16 storage (mixed mode)
-    __nv_bfloat16* bh = nullptr;
-    uint2* Ah = nullptr;         // BF16 matrix rows (4 x bf16)
+    uint2* Ah = nullptr;         // BF16 rows of the mixed-precision V-cycle
 };
 
 // Kernel classes of the live per-kernel profile (jetgpu_profile_read).
@@ -45,7 +44,7 @@ enum KernelClass : int {
     K_DOT_RZ,         // r.z
     K_UPDATE_D,       // d = z + b d
     K_RESIDUAL64,     // FP64 true residual
-    K_ACCUMULATE,     // x64 += e
+    K_ACCUMULATE,     // x += e (double-float) / x64 += e
     K_WEIGHTS,        // fluid SDF sampling + face weights
     K_PYRAMID,        // restriction of the weight/SDF pyramid
     K_SYSTEM,         // matrix rows + rhs
@@ -87,6 +86,8 @@ struct Ctx {
     jetgpu_config cfg;
     int device = 0;
     int num_sms = 0;
+    int col_blocks_per_sm = 1;  // resident blocks of the fused sweep per SM
+    std::unordered_map<const void*, int> occupancy;  // blocks/SM per kernel
     cudaStream_t stream = nullptr;
     std::string err;
 
@@ -100,6 +101,12 @@ struct Ctx {
     double* b64 = nullptr;
     double* x64 = nullptr;
     double* r64 = nullptr;
+    // Double-float image of the finest-level system and iterate (FP32
+    // modes): the exact rows and rhs as hi + lo FP32 pairs (hi = the FP32
+    // rows of level 0), and the solution accumulated as a pair.
+    float4* Alo = nullptr;
+    float2* bdf = nullptr;
+    float2* xdf = nullptr;
 
     // Krylov vectors (FP32 modes).
     float* kx = nullptr;
@@ -201,6 +208,8 @@ jetgpu_status build_system(Ctx* c, const GridDesc& g, const double* u,
                            const double* v, const double* w,
                            const double* su, const double* sv,
                            const double* sw);
+// Low parts of a caller-built finest-level system (jetgpu_mgpcg_solve_system).
+jetgpu_status split_system(Ctx* c);
 jetgpu_status apply_gradient(Ctx* c, const GridDesc& g, const double* u,
                              const double* v, const double* w, double* ou,
                              double* ov, double* ow);

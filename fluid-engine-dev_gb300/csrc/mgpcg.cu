@@ -8,9 +8,13 @@
 //
 // Design (GB300-first):
 //   * Krylov vectors FP32 (or FP64), matrix rows as one aligned float4 per
-//     cell, V-cycle in FP32; every global reduction is FP64, deterministic
-//     (fixed grid, per-block partials summed in block order by the last block
-//     to finish; no block ever waits on another).
+//     cell, V-cycle in FP32; every global reduction is FP64-accurate and
+//     deterministic (fixed grid, per-block partials summed in FP64 in block
+//     order by the last block to finish; no block ever waits on another).
+//     Over FP32 vectors each thread accumulates its products exactly split
+//     into a double-float pair on the FP32 pipe (common.cuh, DF): GB300
+//     issues FP64 at a small fraction of the FP32 rate, and a per-element
+//     FP64 multiply-add made these streaming kernels FP64-issue-bound.
 //   * alpha and beta never leave the device: the last block of each reduction
 //     computes them, the next kernel reads them. The host reads one scalar per
 //     iteration (the residual norm) for the stopping test.
@@ -24,6 +28,7 @@
 
 #include "ctx.h"
 
+#include <algorithm>
 #include <chrono>
 #include <cmath>
 #include <cstring>
@@ -83,6 +88,16 @@ struct RowsF {
     const float4* A;
     __device__ __forceinline__ float4 row(long c) const { return A[c]; }
 };
+// BF16 rows (mixed mode): {center | right << 16, up | front << 16}.
+__device__ __forceinline__ float bf_lo(unsigned u) { return __uint_as_float(u << 16); }
+__device__ __forceinline__ float bf_hi(unsigned u) { return __uint_as_float(u & 0xffff0000u); }
+__device__ __forceinline__ float4 bf_row(uint2 r) {
+    return make_float4(bf_lo(r.x), bf_hi(r.x), bf_lo(r.y), bf_hi(r.y));
+}
+struct RowsB {
+    const uint2* A;
+    __device__ __forceinline__ float4 row(long c) const { return bf_row(__ldg(A + c)); }
+};
 struct RowsD {
     const double* A;
     __device__ __forceinline__ double4 row(long c) const {
@@ -115,17 +130,17 @@ __global__ void __launch_bounds__(kThreads)
                double* partials, unsigned* counters, double* scal) {
     __shared__ double smem[32];
     const long N = n.count();
-    double acc = 0.0;
+    typename AccOf<V>::type acc;
     for (long c = blockIdx.x * (long)kThreads + threadIdx.x; c < N;
          c += (long)gridDim.x * kThreads) {
         int i, j, k;
         cell_ijk(c, n, i, j, k);
         const V qv = apply7<V>(M, d, c, i, j, k, n);
         q[c] = qv;
-        acc += (double)d[c] * (double)qv;
+        acc.add(d[c], qv);
     }
-    reduce_finish<kThreads>(acc, 0, S_DQ, FIN_ALPHA, partials, counters, scal,
-                            smem);
+    reduce_finish<kThreads>(acc.value(), 0, S_DQ, FIN_ALPHA, partials,
+                            counters, scal, smem);
 }
 
 // K7a: x += alpha d; r -= alpha q; r.r (FP64). Optionally writes an FP32
@@ -137,17 +152,17 @@ __global__ void __launch_bounds__(kThreads)
                 double* partials, unsigned* counters, double* scal) {
     __shared__ double smem[32];
     const V alpha = (V)scal[S_ALPHA];
-    double acc = 0.0;
+    typename AccOf<V>::type acc;
     for (long c = blockIdx.x * (long)kThreads + threadIdx.x; c < N;
          c += (long)gridDim.x * kThreads) {
         x[c] += alpha * d[c];
         const V rv = r[c] - alpha * q[c];
         r[c] = rv;
         if (r32) r32[c] = (float)rv;
-        acc += (double)rv * (double)rv;
+        acc.add(rv, rv);
     }
-    reduce_finish<kThreads>(acc, 1, S_RR, FIN_NONE, partials, counters, scal,
-                            smem);
+    reduce_finish<kThreads>(acc.value(), 1, S_RR, FIN_NONE, partials,
+                            counters, scal, smem);
 }
 
 // K7b: r.z (FP64), finishing beta.
@@ -156,12 +171,12 @@ __global__ void __launch_bounds__(kThreads)
     k_dot_rz(const V* __restrict__ r, const Z* __restrict__ z, long N,
              double* partials, unsigned* counters, double* scal) {
     __shared__ double smem[32];
-    double acc = 0.0;
+    typename AccOf<V>::type acc;
     for (long c = blockIdx.x * (long)kThreads + threadIdx.x; c < N;
          c += (long)gridDim.x * kThreads)
-        acc += (double)r[c] * (double)z[c];
-    reduce_finish<kThreads>(acc, 2, S_RZ, FIN_BETA, partials, counters, scal,
-                            smem);
+        acc.add(r[c], (V)z[c]);
+    reduce_finish<kThreads>(acc.value(), 2, S_RZ, FIN_BETA, partials,
+                            counters, scal, smem);
 }
 
 // K7c: d = z + beta d.
@@ -200,6 +215,111 @@ __global__ void __launch_bounds__(kThreads)
     }
     reduce_finish<kThreads>(acc, 3, target, FIN_NONE, partials, counters,
                             scal, smem);
+}
+
+// Double-float true residual (FP32 modes): r = b - A x with the exact rows,
+// rhs and iterate held as hi + lo FP32 pairs (about 48 significant bits),
+// evaluated with exact product splitting and TwoSum on the FP32 pipe. Writes
+// the FP32 image of r (the next correction's right-hand side), zeroes the
+// FP32 correction and reduces ||r||^2 into scal[target].
+__global__ void __launch_bounds__(kThreads)
+    k_residual_df(const float4* __restrict__ Ahi,
+                  const float4* __restrict__ Alo,
+                  const float2* __restrict__ x, const float2* __restrict__ b,
+                  float* __restrict__ r32, float* __restrict__ zero32, Dims n,
+                  double* partials, unsigned* counters, double* scal,
+                  int target) {
+    __shared__ double smem[32];
+    const long N = n.count();
+    const long sy = n.x, sz = (long)n.x * n.y;
+    AccF acc;
+    for (long c = blockIdx.x * (long)kThreads + threadIdx.x; c < N;
+         c += (long)gridDim.x * kThreads) {
+        int i, j, k;
+        cell_ijk(c, n, i, j, k);
+        const float4 h = Ahi[c], l = Alo[c];
+        const float2 xc = x[c], bc = b[c];
+        DF r;
+        r.hi = bc.x;
+        r.lo = bc.y;
+        r = df_sub_prod(r, h.x, l.x, xc.x, xc.y);
+        if (i > 0) {
+            const float2 xn = x[c - 1];
+            r = df_sub_prod(r, Ahi[c - 1].y, Alo[c - 1].y, xn.x, xn.y);
+        }
+        if (i + 1 < n.x) {
+            const float2 xn = x[c + 1];
+            r = df_sub_prod(r, h.y, l.y, xn.x, xn.y);
+        }
+        if (j > 0) {
+            const float2 xn = x[c - sy];
+            r = df_sub_prod(r, Ahi[c - sy].z, Alo[c - sy].z, xn.x, xn.y);
+        }
+        if (j + 1 < n.y) {
+            const float2 xn = x[c + sy];
+            r = df_sub_prod(r, h.z, l.z, xn.x, xn.y);
+        }
+        if (k > 0) {
+            const float2 xn = x[c - sz];
+            r = df_sub_prod(r, Ahi[c - sz].w, Alo[c - sz].w, xn.x, xn.y);
+        }
+        if (k + 1 < n.z) {
+            const float2 xn = x[c + sz];
+            r = df_sub_prod(r, h.w, l.w, xn.x, xn.y);
+        }
+        const float rv = __fadd_rn(r.hi, r.lo);
+        r32[c] = rv;
+        zero32[c] = 0.0f;
+        acc.add(rv, rv);
+    }
+    reduce_finish<kThreads>(acc.value(), 3, target, FIN_NONE, partials,
+                            counters, scal, smem);
+}
+
+// Start of the FP32-mode solve from x = 0: r = b (its FP32 image is b's hi
+// part, the FP32 rounding of b), correction and iterate zeroed, ||b||^2 from
+// the double-float b into scal[S_B64].
+__global__ void __launch_bounds__(kThreads)
+    k_start_df(const float2* __restrict__ b, float* __restrict__ r32,
+               float* __restrict__ zero32, float2* __restrict__ x, long N,
+               double* partials, unsigned* counters, double* scal) {
+    __shared__ double smem[32];
+    AccF acc;
+    for (long c = blockIdx.x * (long)kThreads + threadIdx.x; c < N;
+         c += (long)gridDim.x * kThreads) {
+        const float2 bc = b[c];
+        r32[c] = bc.x;
+        zero32[c] = 0.0f;
+        x[c] = make_float2(0.0f, 0.0f);
+        acc.add(bc.x, bc.x);
+        acc.add(2.0f * bc.x, bc.y);
+    }
+    reduce_finish<kThreads>(acc.value(), 4, S_R64, FIN_NONE, partials,
+                            counters, scal, smem);
+}
+
+// x += e on the double-float iterate.
+__global__ void k_accumulate_df(float2* __restrict__ x,
+                                const float* __restrict__ e, long N) {
+    for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < N;
+         c += (long)gridDim.x * blockDim.x) {
+        const float2 v = x[c];
+        DF a;
+        a.hi = v.x;
+        a.lo = v.y;
+        a = df_add_f(a, e[c]);
+        x[c] = make_float2(a.hi, a.lo);
+    }
+}
+
+// x64 = hi + lo (exact widening on the integer pipe, one FP64 add).
+__global__ void k_df_to_f64(const float2* __restrict__ x,
+                            double* __restrict__ x64, long N) {
+    for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < N;
+         c += (long)gridDim.x * blockDim.x) {
+        const float2 v = x[c];
+        x64[c] = widen_f32(v.x) + widen_f32(v.y);
+    }
 }
 
 // x64 += e (FP32 correction).
@@ -249,9 +369,9 @@ __global__ void k_zero(V* __restrict__ p, long N) {
 // pair of cells along i; `color` 0 updates (i+j+k) even cells. With ZERO the
 // whole vector is taken as zero on entry: the updated colour gets
 // omega*b/center and the other colour is written 0 (no read of x).
-template <bool ZERO>
+template <bool ZERO, typename R>
 __global__ void __launch_bounds__(kThreads)
-    k_rb_half(const float4* __restrict__ A, const float* __restrict__ b,
+    k_rb_half(R A, const float* __restrict__ b,
               float* __restrict__ x, Dims n, int color, float omega) {
     const int hx = (n.x + 1) >> 1;
     const long N = (long)hx * n.y * n.z;
@@ -268,7 +388,7 @@ __global__ void __launch_bounds__(kThreads)
         if (ZERO) {
             if (i < n.x) {
                 const long c = base + off;
-                const float4 r = A[c];
+                const float4 r = A.row(c);
                 x[c] = omega * b[c] / r.x;
             }
             const int io = 2 * p + (off ^ 1);
@@ -276,13 +396,13 @@ __global__ void __launch_bounds__(kThreads)
         } else {
             if (i >= n.x) continue;
             const long c = base + off;
-            const float4 r = A[c];
+            const float4 r = A.row(c);
             float s = 0.0f;
-            if (i > 0) s += A[c - 1].y * x[c - 1];
+            if (i > 0) s += A.row(c - 1).y * x[c - 1];
             if (i + 1 < n.x) s += r.y * x[c + 1];
-            if (j > 0) s += A[c - sy].z * x[c - sy];
+            if (j > 0) s += A.row(c - sy).z * x[c - sy];
             if (j + 1 < n.y) s += r.z * x[c + sy];
-            if (k > 0) s += A[c - sz].w * x[c - sz];
+            if (k > 0) s += A.row(c - sz).w * x[c - sz];
             if (k + 1 < n.z) s += r.w * x[c + sz];
             x[c] = (1.0f - omega) * x[c] + omega * (b[c] - s) / r.x;
         }
@@ -291,216 +411,255 @@ __global__ void __launch_bounds__(kThreads)
 
 // K8 (fused): one full red-black SOR sweep in a single pass over memory.
 //
-// A block owns a 64 x 8 (i, j) tile and marches through a slab of k planes
-// (2.5-D blocking). x is read from `xin` and the swept x written to `xout`
-// (ping-pong), so blocks never see each other's updates: each block redoes
-// the first-colour update on a one-cell ring around its tile, from old
-// values, exactly as the sequential sweep would produce them. Per plane the
-// block stages x with a two-cell ring, the matrix rows and b with cp.async
-// 16-byte copies (zero-filled outside the domain), then
-//   (1) updates the first colour of plane t+1 on tile + ring (in shared
-//       memory; the 7-point neighbours of a cell all have the other colour),
-//   (2) updates the second colour of plane t on the tile, reading first-
-//       colour values of planes t-1, t, t+1 that (1) produced, and writes
-//       both colours of plane t to global memory as one float2 per thread.
-// HBM traffic per sweep: x, b and A read once, x written once — 28 B/cell —
-// plus ring re-reads that mostly hit L2. Requires nx % 4 == 0.
-namespace fused {
-constexpr int TX = 64, TY = 8;          // tile (cells)
-constexpr int SX = TX + 8, SY = TY + 4; // staged plane: i0-4 .. i0+67, j0-2 .. j0+9
-constexpr int PLANE = SX * SY;          // 864 cells
-// Ring depths (planes): in use at step t are x t-1..t+2, A t-1..t+1 and
-// b t..t+1; PD more slots each hold the prefetches for steps t+1..t+PD, so
-// every block keeps PD planes of loads in flight while it computes.
-constexpr int PD = 2;
-constexpr int XS = 4 + PD, AS = 3 + PD, BS = 2 + PD;
-constexpr size_t SMEM = (size_t)PLANE * (XS * 4 + AS * 16 + BS * 4);
+// Register-column design. A block owns a tile of 32 cell pairs (64 cells)
+// in i by 8 rows in j and marches through k. Each thread holds the k-column
+// of one pair (cells 2m, 2m+1 of a row) in registers: at every plane a pair
+// has exactly one cell of each colour, and the cells directly below and
+// above a cell have the other colour, so the column neighbours of every
+// update are the thread's own registers. Only in-plane neighbours go through
+// shared memory (one float2 of x and of the two "up" coefficients, one float
+// of the pair's "right" coefficient and one of its first-colour result per
+// pair and plane), which keeps shared-memory traffic at a few words per
+// cell. Step t of the march
+//   (1) updates the first colour F of plane t+1 from old values (tile plus
+//       a one-pair / one-row ring, so the tile's second-colour cells have
+//       all their new F neighbours; ring rows also load x of the next row
+//       out, which their update reads),
+//   (2) updates the second colour S of plane t from the new F values of
+//       planes t-1, t, t+1 and writes both colours of plane t as one float2.
+// x is read from `xin` and written to `xout` (ping-pong), so blocks never
+// observe each other's updates: the result is exactly the sequential
+// red-then-black sweep, deterministic, with no inter-block synchronisation.
+// Global loads are issued two planes ahead into registers. Cells outside the
+// domain load as x = 0 and a zero row, which reproduces the reference's
+// guarded neighbour terms (FdmBlas3::mvm, fdm_linear_system3.cpp:79-96), and
+// are never written. Work items are (k-slab, tile) pairs ordered slab-major
+// and dealt round-robin to a persistent grid, so the blocks working at the
+// same time hold neighbouring tiles of the same slab: the ring rows and the
+// two warm-up planes a column re-reads were loaded moments earlier by a
+// neighbour and come from L2, not HBM.
+// HBM traffic per sweep: x, b and A read once, x written once — 28 B/cell
+// (24 B/cell from a zero start) — plus ring re-reads that mostly hit L2.
+// Requires an even nx.
+namespace col {
+constexpr int TXP = 32;            // pairs per tile row (64 cells)
+constexpr int TY = 8;              // rows per tile
+constexpr int PX = TXP + 2;        // pairs per row including the ring
+constexpr int PY = TY + 2;         // rows including the ring
+constexpr int NW = PX * PY;        // working threads (340)
+constexpr int BLOCK = 352;         // 11 warps
+constexpr int TCX = 2 * TXP;       // tile width in cells
+}  // namespace col
 
-__device__ __forceinline__ int ring(int p, int m) { return ((p % m) + m) % m; }
+// The two matrix rows of a cell pair as loaded (decoded where used).
+template <typename R> struct PairRows;
+template <> struct PairRows<RowsF> {
+    float4 a0, a1;
+    __device__ __forceinline__ void zero() {
+        a0 = a1 = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    __device__ __forceinline__ void load(const RowsF& M, int idx) {
+        a0 = __ldg(M.A + idx);
+        a1 = __ldg(M.A + idx + 1);
+    }
+    __device__ __forceinline__ float4 r0() const { return a0; }
+    __device__ __forceinline__ float4 r1() const { return a1; }
+};
+template <> struct PairRows<RowsB> {
+    uint4 raw;  // both BF16 rows: one aligned 16-byte load (idx is even)
+    __device__ __forceinline__ void zero() { raw = make_uint4(0u, 0u, 0u, 0u); }
+    __device__ __forceinline__ void load(const RowsB& M, int idx) {
+        raw = __ldg(reinterpret_cast<const uint4*>(M.A + idx));
+    }
+    __device__ __forceinline__ float4 r0() const {
+        return bf_row(make_uint2(raw.x, raw.y));
+    }
+    __device__ __forceinline__ float4 r1() const {
+        return bf_row(make_uint2(raw.z, raw.w));
+    }
+};
 
-__device__ __forceinline__ void cp16(void* smem, const void* gmem, bool valid) {
-    const unsigned s = (unsigned)__cvta_generic_to_shared(smem);
-    const int src = valid ? 16 : 0;
-    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(s),
-                 "l"(gmem), "r"(src));
-}
-__device__ __forceinline__ void cp_commit() {
-    asm volatile("cp.async.commit_group;\n" ::);
-}
-// Waits until at most `pending` committed groups are still in flight.
-template <int pending>
-__device__ __forceinline__ void cp_wait() {
-    asm volatile("cp.async.wait_group %0;\n" ::"n"(pending));
-}
-}  // namespace fused
+template <typename R>
+struct ColPlane {
+    float2 x;          // old x of the pair
+    PairRows<R> a;     // rows of the pair's two cells
+    float2 b;          // rhs of the pair
+    float2 xe;         // ring rows: old x of the row beyond
+    float2 ue;         // top ring row: "up" coefficients of the row beyond
+};
 
-__global__ void __launch_bounds__(256)
-    k_rb_sweep_fused(const float4* __restrict__ A, const float* __restrict__ b,
-                     const float* __restrict__ xin, float* __restrict__ xout,
-                     Dims n, int first, float omega, int kz) {
-    using namespace fused;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    float* sx = reinterpret_cast<float*>(smem_raw);               // XS planes
-    float4* sA = reinterpret_cast<float4*>(sx + XS * PLANE);      // AS planes
-    float* sb = reinterpret_cast<float*>(sA + AS * PLANE);        // BS planes
+template <bool ZERO, typename R>
+__global__ void __launch_bounds__(col::BLOCK, 2)
+    k_rb_sweep_col(R A, const float* __restrict__ b,
+                   const float* __restrict__ xin, float* __restrict__ xout,
+                   Dims n, int first, float omega, int tiles_x, int tiles,
+                   int kz, int items) {
+    using namespace col;
+    __shared__ float2 sX[PY + 2][PX];      // x of plane t+1, rows -2..TY+1
+    __shared__ float sYF[2][PY][PX];       // F result per pair, by plane parity
+    __shared__ float sAr[2][PY][PX];       // "right" of the pair's cell 1
+    __shared__ float2 sAu[2][PY + 1][PX];  // "up" of both cells, rows -2..TY-1
     const int tid = threadIdx.x;
-    const int i0 = blockIdx.x * TX, j0 = blockIdx.y * TY;
-    const int k0 = blockIdx.z * kz;
-    const int k1 = min(n.z, k0 + kz);
-    const long sy = n.x, sz = (long)n.x * n.y;
-    const int second = first ^ 1;
+    const bool worker = tid < NW;
+    const int py = worker ? tid / PX : 0;  // tile row py - 1
+    const int px = worker ? tid - py * PX : 0;
+    const int sz = n.x * n.y;  // grids hold < 2^31 cells
+    const bool ring_lo = py == 0, ring_hi = py == PY - 1;
+    const bool interior = worker && px > 0 && px < PX - 1 && !ring_lo &&
+                          !ring_hi;
 
-    // Per-thread copy descriptors. The in-plane offsets of a thread's 16-byte
-    // chunks are the same for every plane, so their index arithmetic is done
-    // once here; a plane load only adds the plane base.
-    // x and b: PLANE/4 = 216 chunks of 4 floats, one per thread below 216.
-    int vgo = 0, vso = 0;
-    bool vok = false;
-    if (tid < PLANE / 4) {
-        const int r = tid / (SX / 4), c4 = tid - r * (SX / 4);
-        const int gi = i0 - 4 + 4 * c4, gj = j0 - 2 + r;
-        vok = gi >= 0 && gi < n.x && gj >= 0 && gj < n.y;
-        vgo = vok ? gi + n.x * gj : 0;
-        vso = r * SX + 4 * c4;
-    }
-    // A: PLANE rows of 16 bytes, up to AM per thread.
-    constexpr int AM = (PLANE + 255) / 256;
-    int ago[AM];
-    bool aok[AM];
-#pragma unroll
-    for (int m = 0; m < AM; ++m) {
-        const int f = tid + 256 * m;
-        const int r = f / SX, c = f - r * SX;
-        const int gi = i0 - 4 + c, gj = j0 - 2 + r;
-        aok[m] = f < PLANE && gi >= 0 && gi < n.x && gj >= 0 && gj < n.y;
-        ago[m] = aok[m] ? gi + n.x * gj : 0;
-    }
+    for (int item = blockIdx.x; item < items; item += gridDim.x) {
+        const int slab = item / tiles;
+        const int tile = item - slab * tiles;
+        const int k0 = slab * kz;
+        const int k1 = min(n.z, k0 + kz);
+        const int i0 = (tile % tiles_x) * TCX;
+        const int j0 = (tile / tiles_x) * TY;
+        const int gi = i0 + 2 * (px - 1);
+        const int gj = j0 + py - 1;
+        const bool colv = worker && gi >= 0 && gi < n.x && gj >= 0 && gj < n.y;
+        const int ej = ring_lo ? gj - 1 : gj + 1;
+        const bool exv = worker && (ring_lo || ring_hi) && gi >= 0 &&
+                         gi < n.x && ej >= 0 && ej < n.y;
+        const bool uev = exv && ring_lo;
+        const int cb = colv ? gi + n.x * gj : 0;
+        const int eb = exv ? gi + n.x * ej : 0;
 
-    // Stage plane p of x / A / b (zero-filled outside the domain, so the
-    // update below needs no bounds tests: an outside neighbour has x = 0 and
-    // a zero matrix row, exactly the reference's guarded terms,
-    // FdmBlas3::mvm, fdm_linear_system3.cpp:79-96).
-    auto load_x = [&](int p) {
-        float* dst = sx + ring(p, XS) * PLANE;
-        if (xin == nullptr || p < 0 || p >= n.z) {
-            for (int q = tid; q < PLANE; q += 256) dst[q] = 0.0f;
-            return;
-        }
-        if (tid < PLANE / 4) {
-            const float* base = xin + sz * p;
-            cp16(dst + vso, vok ? base + vgo : xin, vok);
-        }
-    };
-    auto load_A = [&](int p) {
-        float4* dst = sA + ring(p, AS) * PLANE;
-        const bool pin = p >= 0 && p < n.z;
-        const float4* base = A + (pin ? sz * p : 0);
-#pragma unroll
-        for (int m = 0; m < AM; ++m) {
-            const int f = tid + 256 * m;
-            if (f < PLANE) cp16(dst + f, base + ago[m], pin && aok[m]);
-        }
-    };
-    auto load_b = [&](int p) {
-        float* dst = sb + ring(p, BS) * PLANE;
-        const bool pin = p >= 0 && p < n.z;
-        if (tid < PLANE / 4) {
-            const float* base = b + (pin ? sz * p : 0);
-            cp16(dst + vso, base + vgo, pin && vok);
-        }
-    };
-    // SOR update at staged index s: xc/Ac/bc this plane, xdn/Adn the plane
-    // below, xup the plane above.
-    auto relax = [&](const float* xc, const float* xdn, const float* xup,
-                     const float4* Ac, const float4* Adn, const float* bc,
-                     int s) -> float {
-        const float4 row = Ac[s];
-        const float acc = Ac[s - 1].y * xc[s - 1] + row.y * xc[s + 1] +
-                          Ac[s - SX].z * xc[s - SX] + row.z * xc[s + SX] +
-                          Adn[s].w * xdn[s] + row.w * xup[s];
-        return (1.0f - omega) * xc[s] + omega * __fdividef(bc[s] - acc, row.x);
-    };
-
-    // Step t needs x planes t..t+2, A planes t..t+1 and b plane t+1 staged.
-    // Group g holds the loads of step t0+g; groups for steps t+1..t+PD are
-    // in flight while step t computes (empty groups keep the count uniform).
-    const int t0 = k0 - 2;
-    load_x(t0);
-    load_x(t0 + 1);
-    load_A(t0);
-    for (int q = 0; q < PD; ++q) {
-        if (t0 + q < k1) {
-            load_x(t0 + q + 2);
-            load_A(t0 + q + 1);
-            load_b(t0 + q + 1);
-        }
-        fused::cp_commit();
-    }
-    for (int t = t0; t < k1; ++t) {
-        if (t + PD < k1) {
-            load_x(t + PD + 2);
-            load_A(t + PD + 1);
-            load_b(t + PD + 1);
-        }
-        fused::cp_commit();
-        fused::cp_wait<PD>();
-        __syncthreads();
-        // Slot pointers of the planes this step touches.
-        float* xm1 = sx + ring(t - 1, XS) * PLANE;
-        float* x0 = sx + ring(t, XS) * PLANE;
-        float* x1 = sx + ring(t + 1, XS) * PLANE;
-        const float* x2 = sx + ring(t + 2, XS) * PLANE;
-        const float4* am1 = sA + ring(t - 1, AS) * PLANE;
-        const float4* a0 = sA + ring(t, AS) * PLANE;
-        const float4* a1 = sA + ring(t + 1, AS) * PLANE;
-        const float* b0 = sb + ring(t, BS) * PLANE;
-        const float* b1 = sb + ring(t + 1, BS) * PLANE;
-        // (1) first colour of plane t+1 on tile + 1-cell ring.
-        const int p1 = t + 1;
-        if (p1 >= k0 - 1 && p1 <= k1 && p1 >= 0 && p1 < n.z) {
-            const int par = (first - p1 + 1) & 1;
-            for (int q = tid; q < 33 * (TY + 2); q += 256) {
-                const int row = q / 33;
-                const int jj = row - 1;
-                const int ii = -1 + 2 * (q - 33 * row) + ((par - jj) & 1);
-                const int gi = i0 + ii, gj = j0 + jj;
-                if (gi < 0 || gi >= n.x || gj < 0 || gj >= n.y) continue;
-                const int s = (jj + 2) * SX + (ii + 4);
-                x1[s] = relax(x1, x0, x2, a1, a0, b1, s);
+        // Loads of plane p (zeros outside the domain or beyond `need`).
+        auto load = [&](int p, bool need_x, bool need_rest) {
+            ColPlane<R> q;
+            q.x = make_float2(0.f, 0.f);
+            q.xe = make_float2(0.f, 0.f);
+            q.a.zero();
+            q.b = make_float2(0.f, 0.f);
+            q.ue = make_float2(0.f, 0.f);
+            if (p < 0 || p >= n.z) return q;
+            const int pb = sz * p;
+            if (!ZERO && need_x) {
+                if (colv) q.x = __ldg(reinterpret_cast<const float2*>(xin + pb + cb));
             }
-        }
-        __syncthreads();
-        // (2) second colour of plane t on the tile; write plane t.
-        if (t >= k0) {
-            const int tx = tid & 31, ty = tid >> 5;
-            const int ii = 2 * tx, jj = ty;
-            const int gi = i0 + ii, gj = j0 + jj;
-            if (gi < n.x && gj < n.y) {
-                const int odd = ((ii + jj + t) & 1) != second;  // S cell at ii+odd
-                const float* xp = x0;
-                const int s = (jj + 2) * SX + (ii + 4);
-                float2 out;
-                const float vs = relax(x0, xm1, x1, a0, am1, b0, s + odd);
-                if (odd) {
-                    out.x = xp[s];
-                    out.y = vs;
-                } else {
-                    out.x = vs;
-                    out.y = xp[s + 1];
+            if (need_rest) {
+                if (!ZERO && exv)
+                    q.xe = __ldg(reinterpret_cast<const float2*>(xin + pb + eb));
+                if (colv) {
+                    q.a.load(A, pb + cb);
+                    q.b = __ldg(reinterpret_cast<const float2*>(b + pb + cb));
                 }
-                *reinterpret_cast<float2*>(xout + gi + sy * gj + sz * t) = out;
+                if (uev)
+                    q.ue = make_float2(A.row(pb + eb).z, A.row(pb + eb + 1).z);
             }
+            return q;
+        };
+
+        // Register column. Planes: X t..t+2, A t-1 (front) .. t+1, b t..t+1.
+        const int t0 = k0 - 2;
+        ColPlane<R> P0 = load(t0, true, true);      // x(t), A(t)
+        ColPlane<R> P1 = load(t0 + 1, true, true);  // x(t+1), A(t+1), b(t+1)
+        float2 x2 = load(t0 + 2, true, false).x;    // x(t+2)
+        ColPlane<R> Q1 = load(t0 + 2, false, true); // A, b, ring of t+2
+        float2 qx1 = load(t0 + 3, true, false).x;  // x(t+3)
+        float2 amf = make_float2(0.f, 0.f);        // fronts of plane t-1
+        float yfm = 0.f, yf0 = 0.f;                // F results of t-1, t
+
+        for (int t = t0; t < k1; ++t) {
+            // Prefetch: A, b, ring of t+3 and x of t+4.
+            ColPlane<R> Q2 = load(t + 3, false, t + 3 <= k1);
+            const float2 qx2v = load(t + 4, t + 4 <= k1 + 1, false).x;
+
+            const int p1 = t + 1;
+            const int par1 = p1 & 1, par0 = t & 1;
+            if (worker) {
+                sX[py + 1][px] = P1.x;
+                if (ring_lo) sX[0][px] = P1.xe;
+                if (ring_hi) sX[PY + 1][px] = P1.xe;
+                const float4 r0 = P1.a.r0(), r1 = P1.a.r1();
+                sAr[par1][py][px] = r1.y;
+                sAu[par1][py + 1][px] = make_float2(r0.z, r1.z);
+                if (ring_lo) sAu[par1][0][px] = P1.ue;
+            }
+            __syncthreads();
+
+            // (1) First colour of plane t+1.
+            float yf1 = 0.f;
+            if (colv && p1 >= 0 && p1 < n.z) {
+                const int e = (first + gj + p1) & 1;  // F cell of the pair
+                const bool skip = (px == 0 && e == 0) || (px == PX - 1 && e == 1);
+                if (!skip) {
+                    const float4 p10 = P1.a.r0(), p11 = P1.a.r1();
+                    const float4 r = e ? p11 : p10;
+                    const float xold = e ? P1.x.y : P1.x.x;
+                    const float xl = e ? P1.x.x : sX[py + 1][px - 1].y;
+                    const float xr = e ? sX[py + 1][px + 1].x : P1.x.y;
+                    const float2 xd2 = sX[py][px], xu2 = sX[py + 2][px];
+                    const float xd = e ? xd2.y : xd2.x;
+                    const float xu = e ? xu2.y : xu2.x;
+                    const float xb = e ? P0.x.y : P0.x.x;
+                    const float xf = e ? x2.y : x2.x;
+                    const float cl = e ? p10.y : sAr[par1][py][px - 1];
+                    const float2 dn2 = sAu[par1][py][px];
+                    const float cd = e ? dn2.y : dn2.x;
+                    const float cb_ = e ? P0.a.r1().w : P0.a.r0().w;
+                    const float bb = e ? P1.b.y : P1.b.x;
+                    const float acc = cl * xl + r.y * xr + cd * xd + r.z * xu +
+                                      cb_ * xb + r.w * xf;
+                    yf1 = (1.0f - omega) * xold +
+                          omega * __fdividef(bb - acc, r.x);
+                }
+            }
+            if (worker) sYF[par1][py][px] = yf1;
+
+            // (2) Second colour of plane t; write plane t.
+            if (interior && colv && t >= k0) {
+                const int eF = (first + gj + t) & 1;
+                const int e = eF ^ 1;  // S cell of the pair
+                const float4 p00 = P0.a.r0(), p01 = P0.a.r1();
+                const float4 r = e ? p01 : p00;
+                const float xold = e ? P0.x.y : P0.x.x;
+                const float yl = e ? yf0 : sYF[par0][py][px - 1];
+                const float yr = e ? sYF[par0][py][px + 1] : yf0;
+                const float yd = sYF[par0][py - 1][px];
+                const float yu = sYF[par0][py + 1][px];
+                const float cl = e ? p00.y : sAr[par0][py][px - 1];
+                const float2 dn2 = sAu[par0][py][px];
+                const float cd = e ? dn2.y : dn2.x;
+                const float cbk = e ? amf.y : amf.x;
+                const float bb = e ? P0.b.y : P0.b.x;
+                const float acc = cl * yl + r.y * yr + cd * yd + r.z * yu +
+                                  cbk * yfm + r.w * yf1;
+                const float ys = (1.0f - omega) * xold +
+                                 omega * __fdividef(bb - acc, r.x);
+                float2 out;
+                out.x = e ? yf0 : ys;
+                out.y = e ? ys : yf0;
+                *reinterpret_cast<float2*>(xout + (sz * t + cb)) = out;
+            }
+
+            // Rotate the column.
+            amf = make_float2(P0.a.r0().w, P0.a.r1().w);
+            P0.x = P1.x;
+            P0.a = P1.a;
+            P0.b = P1.b;
+            P1.x = x2;
+            P1.a = Q1.a;
+            P1.b = Q1.b;
+            P1.xe = Q1.xe;
+            P1.ue = Q1.ue;
+            x2 = qx1;
+            qx1 = qx2v;
+            Q1 = Q2;
+            yfm = yf0;
+            yf0 = yf1;
+            __syncthreads();
         }
-        __syncthreads();
     }
 }
 
 // K9a: r = b - A x (FP32).
+template <typename R>
 __global__ void __launch_bounds__(kThreads)
-    k_residual32(const float4* __restrict__ A, const float* __restrict__ x,
+    k_residual32(R M, const float* __restrict__ x,
                  const float* __restrict__ b, float* __restrict__ r, Dims n) {
     const long N = n.count();
-    RowsF M{A};
     for (long c = blockIdx.x * (long)kThreads + threadIdx.x; c < N;
          c += (long)gridDim.x * kThreads) {
         int i, j, k;
@@ -587,8 +746,9 @@ __global__ void __launch_bounds__(kThreads)
 // forward red-black sweeps followed by `sweeps` sweeps in reverse colour
 // order (symmetric), starting from x = 0.
 constexpr int kCoarsestMaxCells = 4096;
+template <typename R>
 __global__ void __launch_bounds__(1024)
-    k_coarsest(const float4* __restrict__ A, const float* __restrict__ b,
+    k_coarsest(R A, const float* __restrict__ b,
                float* __restrict__ x, Dims n, int sweeps, float omega) {
     __shared__ float sx[kCoarsestMaxCells];
     __shared__ float sb[kCoarsestMaxCells];
@@ -605,13 +765,13 @@ __global__ void __launch_bounds__(1024)
             for (int c = threadIdx.x; c < N; c += blockDim.x) {
                 const int i = c % n.x, j = (c / n.x) % n.y, k = c / sz;
                 if (((i + j + k) & 1) != color) continue;
-                const float4 r = A[c];
+                const float4 r = A.row(c);
                 float s = 0.0f;
-                if (i > 0) s += A[c - 1].y * sx[c - 1];
+                if (i > 0) s += A.row(c - 1).y * sx[c - 1];
                 if (i + 1 < n.x) s += r.y * sx[c + 1];
-                if (j > 0) s += A[c - sy].z * sx[c - sy];
+                if (j > 0) s += A.row(c - sy).z * sx[c - sy];
                 if (j + 1 < n.y) s += r.z * sx[c + sy];
-                if (k > 0) s += A[c - sz].w * sx[c - sz];
+                if (k > 0) s += A.row(c - sz).w * sx[c - sz];
                 if (k + 1 < n.z) s += r.w * sx[c + sz];
                 sx[c] = (1.0f - omega) * sx[c] + omega * (sb[c] - s) / r.x;
             }
@@ -623,6 +783,64 @@ __global__ void __launch_bounds__(1024)
 
 // ---------------------------------------------------------------------------
 
+// Grid of a reduction (or streaming) kernel over n elements: every block
+// resident at once (SM count x the kernel's occupancy), so the grid-stride
+// work is one wave with no tail; fixed per kernel and device, which keeps the
+// block-ordered reductions deterministic.
+template <typename K>
+int rgrid(Ctx* c, K kernel, long n) {
+    const void* key = reinterpret_cast<const void*>(kernel);
+    auto it = c->occupancy.find(key);
+    int occ = 0;
+    if (it == c->occupancy.end()) {
+        if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, kernel,
+                                                          kThreads, 0) !=
+                cudaSuccess ||
+            occ < 1)
+            occ = 1;
+        c->occupancy[key] = occ;
+    } else {
+        occ = it->second;
+    }
+    long g = (long)c->num_sms * occ;
+    if (g > kMaxRedBlocks) g = kMaxRedBlocks;
+    return blocks_for(n, kThreads, (int)g);
+}
+
+// BF16 rows for the mixed-precision V-cycle: the diagonal rounded up and the
+// off-diagonals rounded toward zero, so a row that is diagonally dominant in
+// FP32 stays so in BF16 (the V-cycle remains a convergent SPD
+// preconditioner); x, b and all arithmetic stay FP32.
+__device__ __forceinline__ unsigned bf_trunc(float v) {
+    return __float_as_uint(v) >> 16;
+}
+__device__ __forceinline__ unsigned bf_up(float v) {
+    const unsigned u = __float_as_uint(v);
+    const unsigned t = u >> 16;
+    return (v > 0.0f && (u & 0xffffu) != 0u) ? t + 1u : t;
+}
+__global__ void k_rows_to_bf16(const float4* __restrict__ A,
+                               uint2* __restrict__ Ah, long N) {
+    for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < N;
+         c += (long)gridDim.x * blockDim.x) {
+        const float4 r = A[c];
+        Ah[c] = make_uint2(bf_up(r.x) | (bf_trunc(r.y) << 16),
+                           bf_trunc(r.z) | (bf_trunc(r.w) << 16));
+    }
+}
+
+bool mixed(const Ctx* c) {
+    return c->cfg.precision == JETGPU_PRECISION_MIXED_BF16;
+}
+// Calls f with the V-cycle rows of level L: BF16 in mixed mode, else FP32.
+template <typename F>
+void with_rows(const Ctx* c, const Level& L, F&& f) {
+    if (mixed(c)) f(RowsB{L.Ah});
+    else f(RowsF{L.A});
+}
+// Bytes per cell of a stored V-cycle row.
+double row_bytes(const Ctx* c) { return mixed(c) ? 8.0 : 16.0; }
+
 int grid_for(const Ctx* c, long work) {
     int cap = c->num_sms * 8;
     return blocks_for(work, kThreads, cap);
@@ -632,29 +850,48 @@ void rb_half(Ctx* c, const Level& L, const float* b, float* x, int color,
              bool zero, int cls) {
     const long pairs = (long)((L.n.x + 1) / 2) * L.n.y * L.n.z;
     const float w = (float)c->cfg.sor;
-    Prof pr(c, cls, 14.0 * L.n.count());
-    if (zero)
-        k_rb_half<true><<<grid_for(c, pairs), kThreads, 0, c->stream>>>(
-            L.A, b, x, L.n, color, w);
-    else
-        k_rb_half<false><<<grid_for(c, pairs), kThreads, 0, c->stream>>>(
-            L.A, b, x, L.n, color, w);
+    Prof pr(c, cls, (6.0 + 0.5 * row_bytes(c)) * L.n.count());
+    with_rows(c, L, [&](auto M) {
+        if (zero)
+            k_rb_half<true><<<grid_for(c, pairs), kThreads, 0, c->stream>>>(
+                M, b, x, L.n, color, w);
+        else
+            k_rb_half<false><<<grid_for(c, pairs), kThreads, 0, c->stream>>>(
+                M, b, x, L.n, color, w);
+    });
 }
 
 bool fused_ok(const Level& L) {
-    return L.n.x % 4 == 0 && L.n.x >= 64 && L.n.y >= 8 && L.n.z >= 2;
+    return L.n.x % 2 == 0 && L.n.x >= 64 && L.n.y >= 4 && L.n.z >= 2;
 }
 
-// Slab depth of the fused sweep: about two waves of resident blocks.
-int fused_kz(const Ctx* c, const Level& L) {
-    const long tiles = (long)((L.n.x + fused::TX - 1) / fused::TX) *
-                       ((L.n.y + fused::TY - 1) / fused::TY);
-    const long resident = (long)c->num_sms * 2;
-    long kz = (long)L.n.z * tiles / (2 * resident);
-    if (kz < 8) kz = 8;
-    if (kz > 64) kz = 64;
-    if (kz > L.n.z) kz = L.n.z;
-    return (int)kz;
+// Launch shape of the fused sweep: a persistent grid of at most the resident
+// block count, and the slab depth kz (planes per work item) that minimises
+// the makespan in planes, rounds x (kz + 2 warm-up planes).
+struct ColLaunch {
+    int grid, tiles_x, tiles, kz, items;
+};
+ColLaunch col_launch(const Ctx* c, const Level& L) {
+    ColLaunch r;
+    r.tiles_x = (L.n.x + col::TCX - 1) / col::TCX;
+    r.tiles = r.tiles_x * ((L.n.y + col::TY - 1) / col::TY);
+    const long G = (long)c->num_sms * c->col_blocks_per_sm;
+    long best = -1;
+    r.kz = L.n.z;
+    for (int kz = 4; kz <= 64; ++kz) {
+        const long slabs = (L.n.z + kz - 1) / kz;
+        const long items = slabs * r.tiles;
+        const long rounds = (items + G - 1) / G;
+        const long span = rounds * (kz + 2);
+        if (best < 0 || span < best) {
+            best = span;
+            r.kz = kz;
+        }
+        if (kz >= L.n.z) break;
+    }
+    r.items = (int)(((L.n.z + r.kz - 1) / r.kz) * r.tiles);
+    r.grid = (int)std::min<long>(G, r.items);
+    return r;
 }
 
 // `sweeps` red-black sweeps (colour order reversed when `reverse`) starting
@@ -670,18 +907,27 @@ float* smooth(Ctx* c, const Level& L, const float* b, float* x, float* alt,
         return x;
     }
     if (alt != nullptr && fused_ok(L)) {
-        const int kz = fused_kz(c, L);
-        dim3 grid((L.n.x + fused::TX - 1) / fused::TX,
-                  (L.n.y + fused::TY - 1) / fused::TY, (L.n.z + kz - 1) / kz);
+        const ColLaunch cl = col_launch(c, L);
         float* cur = x;
         float* oth = alt;
         for (unsigned s = 0; s < sweeps; ++s) {
             const bool z0 = zero && s == 0;
             Prof pr(c, l == 0 ? K_SWEEP_L0 : K_SWEEP_COARSE,
-                    (z0 ? 24.0 : 28.0) * L.n.count());
-            k_rb_sweep_fused<<<grid, 256, fused::SMEM, c->stream>>>(
-                L.A, b, z0 ? nullptr : cur, oth, L.n, first, (float)c->cfg.sor,
-                kz);
+                    ((z0 ? 8.0 : 12.0) + row_bytes(c)) * L.n.count());
+            with_rows(c, L, [&](auto M) {
+                using R = decltype(M);
+                if (z0)
+                    k_rb_sweep_col<true, R>
+                        <<<cl.grid, col::BLOCK, 0, c->stream>>>(
+                            M, b, nullptr, oth, L.n, first,
+                            (float)c->cfg.sor, cl.tiles_x, cl.tiles, cl.kz,
+                            cl.items);
+                else
+                    k_rb_sweep_col<false, R>
+                        <<<cl.grid, col::BLOCK, 0, c->stream>>>(
+                            M, b, cur, oth, L.n, first, (float)c->cfg.sor,
+                            cl.tiles_x, cl.tiles, cl.kz, cl.items);
+            });
             std::swap(cur, oth);
         }
         return cur;
@@ -703,10 +949,12 @@ float* vcycle_level(Ctx* c, unsigned l, const float* b, float* x, float* alt) {
     if (l + 1 == nl) {
         if (L.n.count() <= kCoarsestMaxCells) {
             int nt = (int)std::min<long>(1024, ((L.n.count() + 31) / 32) * 32);
-            Prof pr(c, K_COARSEST, 28.0 * L.n.count());
-            k_coarsest<<<1, nt, 0, c->stream>>>(L.A, b, x, L.n,
-                                                (int)cfg.coarsest_iter,
-                                                (float)cfg.sor);
+            Prof pr(c, K_COARSEST, (12.0 + row_bytes(c)) * L.n.count());
+            with_rows(c, L, [&](auto M) {
+                k_coarsest<<<1, nt, 0, c->stream>>>(M, b, x, L.n,
+                                                    (int)cfg.coarsest_iter,
+                                                    (float)cfg.sor);
+            });
             return x;
         }
         float* cur = smooth(c, L, b, x, alt, cfg.coarsest_iter, false, true, l);
@@ -717,9 +965,11 @@ float* vcycle_level(Ctx* c, unsigned l, const float* b, float* x, float* alt) {
     float* cur = smooth(c, L, b, x, alt, cfg.restrict_iter, false, true, l);
     float* other = (cur == x) ? alt : x;
     {
-        Prof pr(c, K_RESIDUAL, 28.0 * L.n.count());
-        k_residual32<<<grid_for(c, L.n.count()), kThreads, 0, c->stream>>>(
-            L.A, cur, b, L.r, L.n);
+        Prof pr(c, K_RESIDUAL, (12.0 + row_bytes(c)) * L.n.count());
+        with_rows(c, L, [&](auto M) {
+            k_residual32<<<grid_for(c, L.n.count()), kThreads, 0,
+                           c->stream>>>(M, cur, b, L.r, L.n);
+        });
     }
     {
         Prof pr(c, K_RESTRICT, 4.0 * L.n.count() + 8.0 * C.n.count());
@@ -775,14 +1025,30 @@ jetgpu_status vcycle(Ctx* c, const float* r, float* z, float* alt,
 }
 
 jetgpu_status prepare_levels(Ctx* c) {
-    (void)c;
+    if (!mixed(c)) return JETGPU_OK;
+    for (unsigned l = 0; l < c->built_levels; ++l) {
+        const Level& L = c->levels[l];
+        const long N = L.n.count();
+        Prof pr(c, K_SYSTEM, 24.0 * N);
+        k_rows_to_bf16<<<grid_for(c, N), kThreads, 0, c->stream>>>(L.A, L.Ah,
+                                                                   N);
+    }
+    JG_CUDA(c, cudaGetLastError());
     return JETGPU_OK;
 }
 
 jetgpu_status init_kernels(Ctx* c) {
-    JG_CUDA(c, cudaFuncSetAttribute(k_rb_sweep_fused,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)fused::SMEM));
+    int occ[4] = {0, 0, 0, 0};
+    JG_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                   &occ[0], k_rb_sweep_col<true, RowsF>, col::BLOCK, 0));
+    JG_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                   &occ[1], k_rb_sweep_col<false, RowsF>, col::BLOCK, 0));
+    JG_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                   &occ[2], k_rb_sweep_col<true, RowsB>, col::BLOCK, 0));
+    JG_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                   &occ[3], k_rb_sweep_col<false, RowsB>, col::BLOCK, 0));
+    c->col_blocks_per_sm =
+        std::max(1, std::min(std::min(occ[0], occ[1]), std::min(occ[2], occ[3])));
     return JETGPU_OK;
 }
 
@@ -793,7 +1059,6 @@ static jetgpu_status pcg_f32(Ctx* c, double target, unsigned max_it,
     const Level& L0 = c->levels[0];
     const Dims n = L0.n;
     const long N = n.count();
-    const int G = red_blocks(c, N);
     RowsF M{L0.A};
     k_init_scalars<<<1, 32, 0, c->stream>>>(c->scal);
     unsigned it = 0;
@@ -807,22 +1072,26 @@ static jetgpu_status pcg_f32(Ctx* c, double target, unsigned max_it,
         }
         {
             Prof pr(c, K_DOT_RZ, 8.0 * N);
-            k_dot_rz<float, float><<<G, kThreads, 0, c->stream>>>(
+            k_dot_rz<float, float><<<rgrid(c, k_dot_rz<float, float>, N), kThreads, 0,
+            c->stream>>>(
                 c->kr, z, N, c->partials, c->counters, c->scal);
         }
         {
             Prof pr(c, K_UPDATE_D, 12.0 * N);
-            k_update_d<float, float><<<G, kThreads, 0, c->stream>>>(c->kd, z,
+            k_update_d<float, float><<<rgrid(c, k_update_d<float, float>, N), kThreads, 0,
+            c->stream>>>(c->kd, z,
                                                                     N, c->scal);
         }
         {
             Prof pr(c, K_SPMV, 24.0 * N);
-            k_spmv_dot<float, RowsF><<<G, kThreads, 0, c->stream>>>(
+            k_spmv_dot<float, RowsF><<<rgrid(c, k_spmv_dot<float, RowsF>, N), kThreads, 0,
+            c->stream>>>(
                 M, c->kd, c->kq, n, c->partials, c->counters, c->scal);
         }
         {
             Prof pr(c, K_UPDATE_XR, 24.0 * N);
-            k_update_xr<float><<<G, kThreads, 0, c->stream>>>(
+            k_update_xr<float><<<rgrid(c, k_update_xr<float>, N), kThreads, 0,
+            c->stream>>>(
                 c->kx, c->kr, c->kd, c->kq, nullptr, N, c->partials,
                 c->counters, c->scal);
         }
@@ -846,7 +1115,6 @@ static jetgpu_status pcg_f64(Ctx* c, double target, unsigned max_it,
     const Level& L0 = c->levels[0];
     const Dims n = L0.n;
     const long N = n.count();
-    const int G = red_blocks(c, N);
     RowsD M{c->A64};
     k_init_scalars<<<1, 32, 0, c->stream>>>(c->scal);
     unsigned it = 0;
@@ -858,22 +1126,26 @@ static jetgpu_status pcg_f64(Ctx* c, double target, unsigned max_it,
         if (jetgpu_status vs = vcycle(c, r32, L0.x, L0.x2, &z)) return vs;
         {
             Prof pr(c, K_DOT_RZ, 12.0 * N);
-            k_dot_rz<double, float><<<G, kThreads, 0, c->stream>>>(
+            k_dot_rz<double, float><<<rgrid(c, k_dot_rz<double, float>, N), kThreads, 0,
+            c->stream>>>(
                 c->r64, z, N, c->partials, c->counters, c->scal);
         }
         {
             Prof pr(c, K_UPDATE_D, 20.0 * N);
-            k_update_d<double, float><<<G, kThreads, 0, c->stream>>>(
+            k_update_d<double, float><<<rgrid(c, k_update_d<double, float>, N), kThreads, 0,
+            c->stream>>>(
                 c->dd, z, N, c->scal);
         }
         {
             Prof pr(c, K_SPMV, 48.0 * N);
-            k_spmv_dot<double, RowsD><<<G, kThreads, 0, c->stream>>>(
+            k_spmv_dot<double, RowsD><<<rgrid(c, k_spmv_dot<double, RowsD>, N), kThreads, 0,
+            c->stream>>>(
                 M, c->dd, c->dq, n, c->partials, c->counters, c->scal);
         }
         {
             Prof pr(c, K_UPDATE_XR, 52.0 * N);
-            k_update_xr<double><<<G, kThreads, 0, c->stream>>>(
+            k_update_xr<double><<<rgrid(c, k_update_xr<double>, N), kThreads, 0,
+            c->stream>>>(
                 c->x64, c->r64, c->dd, c->dq, r32, N, c->partials,
                 c->counters, c->scal);
         }
@@ -902,18 +1174,18 @@ __global__ void __launch_bounds__(kThreads)
              const float* __restrict__ zold, long N, double* partials,
              unsigned* counters, double* scal) {
     __shared__ double smem[32];
-    double a = 0.0, b = 0.0;
+    AccF a, b;
     for (long c = blockIdx.x * (long)kThreads + threadIdx.x; c < N;
          c += (long)gridDim.x * kThreads) {
-        const double rv = r[c];
-        a += rv * (double)z[c];
-        b += rv * (double)zold[c];
+        const float rv = r[c];
+        a.add(rv, z[c]);
+        b.add(rv, zold[c]);
     }
-    reduce_finish<kThreads>(a, 5, S_RZ, FIN_NONE, partials, counters, scal,
-                            smem);
+    reduce_finish<kThreads>(a.value(), 5, S_RZ, FIN_NONE, partials, counters,
+                            scal, smem);
     __syncthreads();
-    reduce_finish<kThreads>(b, 6, S_AUX, FIN_NONE, partials, counters, scal,
-                            smem);
+    reduce_finish<kThreads>(b.value(), 6, S_AUX, FIN_NONE, partials, counters,
+                            scal, smem);
 }
 
 // Polak-Ribiere beta = r_k.(z_k - z_{k-1}) / (r_{k-1}.z_{k-1}); rolls r.z.
@@ -929,18 +1201,18 @@ __global__ void __launch_bounds__(kThreads)
     k_norm2f(const float* __restrict__ v, long N, double* partials,
              unsigned* counters, double* scal, int target) {
     __shared__ double smem[32];
-    double acc = 0.0;
+    AccF acc;
     for (long c = blockIdx.x * (long)kThreads + threadIdx.x; c < N;
          c += (long)gridDim.x * kThreads)
-        acc += (double)v[c] * (double)v[c];
-    reduce_finish<kThreads>(acc, 7, target, FIN_NONE, partials, counters,
-                            scal, smem);
+        acc.add(v[c], v[c]);
+    reduce_finish<kThreads>(acc.value(), 7, target, FIN_NONE, partials,
+                            counters, scal, smem);
 }
 
 }  // namespace
 
 jetgpu_status norm2f(Ctx* c, const float* r, long n, int target) {
-    k_norm2f<<<red_blocks(c, n), kThreads, 0, c->stream>>>(
+    k_norm2f<<<rgrid(c, k_norm2f, n), kThreads, 0, c->stream>>>(
         r, n, c->partials, c->counters, c->scal, target);
     JG_CUDA(c, cudaGetLastError());
     return JETGPU_OK;
@@ -955,7 +1227,6 @@ static jetgpu_status fpcg_f32(Ctx* c, double target, unsigned max_it,
     const Level& L0 = c->levels[0];
     const Dims n = L0.n;
     const long N = n.count();
-    const int G = red_blocks(c, N);
     RowsF M{L0.A};
     *stalled = false;
     k_init_scalars<<<1, 32, 0, c->stream>>>(c->scal);
@@ -970,24 +1241,28 @@ static jetgpu_status fpcg_f32(Ctx* c, double target, unsigned max_it,
         if (jetgpu_status s = net_apply(c, c->kr, rrp, z)) return s;
         {
             Prof pr(c, K_DOT_RZ, 12.0 * N);
-            k_dot_pr<<<G, kThreads, 0, c->stream>>>(c->kr, z, zold, N,
+            k_dot_pr<<<rgrid(c, k_dot_pr, N), kThreads, 0,
+            c->stream>>>(c->kr, z, zold, N,
                                                     c->partials, c->counters,
                                                     c->scal);
         }
         k_pr_beta<<<1, 32, 0, c->stream>>>(c->scal, it == 0 ? 1 : 0);
         {
             Prof pr(c, K_UPDATE_D, 12.0 * N);
-            k_update_d<float, float><<<G, kThreads, 0, c->stream>>>(c->kd, z,
+            k_update_d<float, float><<<rgrid(c, k_update_d<float, float>, N), kThreads, 0,
+            c->stream>>>(c->kd, z,
                                                                     N, c->scal);
         }
         {
             Prof pr(c, K_SPMV, 24.0 * N);
-            k_spmv_dot<float, RowsF><<<G, kThreads, 0, c->stream>>>(
+            k_spmv_dot<float, RowsF><<<rgrid(c, k_spmv_dot<float, RowsF>, N), kThreads, 0,
+            c->stream>>>(
                 M, c->kd, c->kq, n, c->partials, c->counters, c->scal);
         }
         {
             Prof pr(c, K_UPDATE_XR, 24.0 * N);
-            k_update_xr<float><<<G, kThreads, 0, c->stream>>>(
+            k_update_xr<float><<<rgrid(c, k_update_xr<float>, N), kThreads, 0,
+            c->stream>>>(
                 c->kx, c->kr, c->kd, c->kq, nullptr, N, c->partials,
                 c->counters, c->scal);
         }
@@ -1025,11 +1300,11 @@ jetgpu_status harvest_pairs(Ctx* c, unsigned max_pairs, float* r_out,
     const Level& L0 = c->levels[0];
     const Dims n = L0.n;
     const long N = n.count();
-    const int G = red_blocks(c, N);
     RowsF M{L0.A};
     // r = b (x = 0), FP32 image.
     k_zero<double><<<grid_for(c, N), kThreads, 0, c->stream>>>(c->x64, N);
-    k_residual64<<<G, kThreads, 0, c->stream>>>(
+    k_residual64<<<rgrid(c, k_residual64, N), kThreads, 0,
+            c->stream>>>(
         c->A64, c->x64, c->b64, c->r64, c->kr, c->kx, n, c->partials,
         c->counters, c->scal, S_R64);
     k_init_scalars<<<1, 32, 0, c->stream>>>(c->scal);
@@ -1041,13 +1316,17 @@ jetgpu_status harvest_pairs(Ctx* c, unsigned max_pairs, float* r_out,
                                    cudaMemcpyDeviceToDevice, c->stream));
         JG_CUDA(c, cudaMemcpyAsync(z_out + (size_t)k * N, z, N * sizeof(float),
                                    cudaMemcpyDeviceToDevice, c->stream));
-        k_dot_rz<float, float><<<G, kThreads, 0, c->stream>>>(
+        k_dot_rz<float, float><<<rgrid(c, k_dot_rz<float, float>, N), kThreads, 0,
+            c->stream>>>(
             c->kr, z, N, c->partials, c->counters, c->scal);
-        k_update_d<float, float><<<G, kThreads, 0, c->stream>>>(c->kd, z, N,
+        k_update_d<float, float><<<rgrid(c, k_update_d<float, float>, N), kThreads, 0,
+            c->stream>>>(c->kd, z, N,
                                                                 c->scal);
-        k_spmv_dot<float, RowsF><<<G, kThreads, 0, c->stream>>>(
+        k_spmv_dot<float, RowsF><<<rgrid(c, k_spmv_dot<float, RowsF>, N), kThreads, 0,
+            c->stream>>>(
             M, c->kd, c->kq, n, c->partials, c->counters, c->scal);
-        k_update_xr<float><<<G, kThreads, 0, c->stream>>>(
+        k_update_xr<float><<<rgrid(c, k_update_xr<float>, N), kThreads, 0,
+            c->stream>>>(
             c->kx, c->kr, c->kd, c->kq, nullptr, N, c->partials, c->counters,
             c->scal);
     }
@@ -1060,17 +1339,26 @@ jetgpu_status mgpcg_solve(Ctx* c, jetgpu_solve_stats* st) {
     const Level& L0 = c->levels[0];
     const Dims n = L0.n;
     const long N = n.count();
-    const int G = red_blocks(c, N);
     const jetgpu_config& cfg = c->cfg;
     const bool fp64 = (cfg.precision == JETGPU_PRECISION_FP64);
 
-    // ||b||, x64 = 0.
-    k_norm2<<<G, kThreads, 0, c->stream>>>(c->b64, N, c->partials,
-                                           c->counters, c->scal, S_B64);
-    k_zero<double><<<grid_for(c, N), kThreads, 0, c->stream>>>(c->x64, N);
+    // FP64 mode: x64 = 0 and ||b|| in FP64. FP32 modes: the double-float
+    // start (r = b, x = 0, ||b||) in one pass.
+    if (fp64) {
+        k_norm2<<<rgrid(c, k_norm2, N), kThreads, 0,
+            c->stream>>>(c->b64, N, c->partials,
+                                               c->counters, c->scal, S_B64);
+        k_zero<double><<<grid_for(c, N), kThreads, 0, c->stream>>>(c->x64, N);
+    } else {
+        Prof pr(c, K_RESIDUAL64, 24.0 * N);
+        k_start_df<<<rgrid(c, k_start_df, N), kThreads, 0,
+            c->stream>>>(c->bdf, c->kr, c->kx, c->xdf,
+                                                  N, c->partials, c->counters,
+                                                  c->scal);
+    }
     jetgpu_status s = read_scalars(c);
     if (s != JETGPU_OK) return s;
-    const double bnorm = std::sqrt(c->h_scal[S_B64]);
+    const double bnorm = std::sqrt(c->h_scal[fp64 ? S_B64 : S_R64]);
     if (!std::isfinite(bnorm))
         return fail(c, JETGPU_NUMERICAL_ERROR, "non-finite right-hand side");
     st->b_norm = bnorm;
@@ -1078,7 +1366,20 @@ jetgpu_status mgpcg_solve(Ctx* c, jetgpu_solve_stats* st) {
     st->refinements = 0;
     st->residual = 0.0;
     st->relative_residual = 0.0;
-    if (bnorm == 0.0) return JETGPU_OK;
+    // The FP64 solution of the FP32 modes (from the double-float iterate).
+    auto finish_x = [&]() -> jetgpu_status {
+        if (!fp64) {
+            Prof pr(c, K_ACCUMULATE, 16.0 * N);
+            k_df_to_f64<<<grid_for(c, N), kThreads, 0, c->stream>>>(c->xdf,
+                                                                    c->x64, N);
+            JG_CUDA(c, cudaGetLastError());
+        }
+        return JETGPU_OK;
+    };
+    if (bnorm == 0.0) {
+        if (fp64) return JETGPU_OK;
+        return finish_x();
+    }
 
     const bool learned = cfg.preconditioner == JETGPU_PRECOND_LEARNED;
     if (learned && (fp64 || !net_supported(c)))
@@ -1090,23 +1391,41 @@ jetgpu_status mgpcg_solve(Ctx* c, jetgpu_solve_stats* st) {
     double rnorm = bnorm;
     unsigned total = 0;
     const unsigned max_pass = cfg.max_refinements > 0 ? cfg.max_refinements : 1;
-    for (unsigned pass = 0; pass < max_pass && total < cfg.max_cg_iter;
-         ++pass) {
-        // True FP64 residual r64 = b - A x64 (and its FP32 image).
-        float* r32 = fp64 ? L0.b : c->kr;
-        {
+    // True residual b - A x (FP64 rows): FP64 in FP64 mode, double-float in
+    // the FP32 modes; its FP32 image feeds the next correction solve.
+    auto true_residual = [&](float* r32, float* zero32) -> jetgpu_status {
+        if (fp64) {
             Prof pr(c, K_RESIDUAL64, 60.0 * N);
-            k_residual64<<<G, kThreads, 0, c->stream>>>(
-                c->A64, c->x64, c->b64, c->r64, r32, fp64 ? nullptr : c->kx,
-                n, c->partials, c->counters, c->scal, S_R64);
+            k_residual64<<<rgrid(c, k_residual64, N), kThreads, 0,
+            c->stream>>>(
+                c->A64, c->x64, c->b64, c->r64, r32, zero32, n, c->partials,
+                c->counters, c->scal, S_R64);
+        } else {
+            Prof pr(c, K_RESIDUAL64, 56.0 * N);
+            k_residual_df<<<rgrid(c, k_residual_df, N), kThreads, 0,
+            c->stream>>>(
+                L0.A, c->Alo, c->xdf, c->bdf, r32, zero32, n, c->partials,
+                c->counters, c->scal, S_R64);
         }
-        s = read_scalars(c);
-        if (s != JETGPU_OK) return s;
+        JG_CUDA(c, cudaGetLastError());
+        jetgpu_status rs = read_scalars(c);
+        if (rs != JETGPU_OK) return rs;
         rnorm = std::sqrt(c->h_scal[S_R64]);
         st->residual = rnorm;
         st->relative_residual = rnorm / bnorm;
         if (!std::isfinite(rnorm))
             return fail(c, JETGPU_NUMERICAL_ERROR, "non-finite residual");
+        return JETGPU_OK;
+    };
+    for (unsigned pass = 0; pass < max_pass && total < cfg.max_cg_iter;
+         ++pass) {
+        if (fp64 || pass > 0) {
+            s = true_residual(fp64 ? L0.b : c->kr, fp64 ? nullptr : c->kx);
+            if (s != JETGPU_OK) return s;
+        } else {
+            st->residual = rnorm;
+            st->relative_residual = 1.0;
+        }
         if (rnorm <= goal) break;
         st->refinements = pass + 1;
         unsigned it = 0;
@@ -1115,7 +1434,7 @@ jetgpu_status mgpcg_solve(Ctx* c, jetgpu_solve_stats* st) {
             s = pcg_f64(c, goal * 0.5, cfg.max_cg_iter - total, &it, &rr);
         } else {
             // Inner FP32 solve to a relative reduction the FP32 operator can
-            // deliver; the FP64 pass loop does the rest.
+            // deliver; the refinement loop does the rest.
             double eta = 0.5 * goal / rnorm;
             if (eta < 1e-4) eta = 1e-4;
             if (learned && !fell_back) {
@@ -1131,8 +1450,8 @@ jetgpu_status mgpcg_solve(Ctx* c, jetgpu_solve_stats* st) {
             }
             if (s == JETGPU_OK) {
                 Prof pr(c, K_ACCUMULATE, 20.0 * N);
-                k_accumulate<<<grid_for(c, N), kThreads, 0, c->stream>>>(
-                    c->x64, c->kx, N);
+                k_accumulate_df<<<grid_for(c, N), kThreads, 0, c->stream>>>(
+                    c->xdf, c->kx, N);
             }
         }
         if (s != JETGPU_OK) return s;
@@ -1141,18 +1460,17 @@ jetgpu_status mgpcg_solve(Ctx* c, jetgpu_solve_stats* st) {
     }
     if (st->relative_residual > cfg.tolerance) {
         // Final check after the last pass.
-        k_residual64<<<G, kThreads, 0, c->stream>>>(
-            c->A64, c->x64, c->b64, c->r64, nullptr, nullptr, n, c->partials,
-            c->counters, c->scal, S_R64);
-        s = read_scalars(c);
+        s = true_residual(fp64 ? nullptr : c->kr, fp64 ? nullptr : c->kx);
         if (s != JETGPU_OK) return s;
-        rnorm = std::sqrt(c->h_scal[S_R64]);
-        st->residual = rnorm;
-        st->relative_residual = rnorm / bnorm;
-        if (rnorm > goal)
+        if (rnorm > goal) {
+            jetgpu_status fs = finish_x();
+            if (fs != JETGPU_OK) return fs;
             return fail(c, JETGPU_NOT_CONVERGED,
                         "tolerance not reached within the iteration cap");
+        }
     }
+    s = finish_x();
+    if (s != JETGPU_OK) return s;
     return fell_back ? JETGPU_STALLED_FALLBACK_USED : JETGPU_OK;
 }
 

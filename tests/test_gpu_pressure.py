@@ -57,7 +57,7 @@ def check_levels(ps, g, res):
     assert np.array_equal(ps.level(0, "b"), g["L0_b"].reshape(-1))
 
 
-@pytest.mark.parametrize("precision", ["fp32", "fp64"])
+@pytest.mark.parametrize("precision", ["fp32", "fp64", "mixed"])
 def test_sphere_union_16(precision):
     g = golden("sphere_union_16.npz")
     n, h = 16, (1 / 16,) * 3
@@ -96,8 +96,9 @@ def test_known_answer_free_surface():
         assert np.abs(getattr(out, k)).max() < 1e-6
 
 
-@pytest.mark.parametrize("n", [32, 64])
-def test_sphere_union_vs_port(port, n):
+@pytest.mark.parametrize("n,precision", [(32, "fp32"), (64, "fp32"),
+                                         (64, "mixed")])
+def test_sphere_union_vs_port(port, n, precision):
     h = (1.0 / n,) * 3
     sc = scenes.sphere_union_scene(n, seed=1)
     ref = port.pressure_solve((n,) * 3, h, (0, 0, 0), sc["u"], sc["v"], sc["w"],
@@ -105,7 +106,7 @@ def test_sphere_union_vs_port(port, n):
                               oracle.MgParams(400, 5, 3, 3, 20, 20, 1e-13, 1.5,
                                               True))
     ps, out, st = solve((n,) * 3, h, sc["u"], sc["v"], sc["w"],
-                        sc["boundary_sdf"], sc["fluid_sdf"])
+                        sc["boundary_sdf"], sc["fluid_sdf"], precision)
     assert st == 0
     for what in ("fluid", "uw", "vw", "ww"):
         assert np.array_equal(ps.level(0, what),
@@ -115,7 +116,8 @@ def test_sphere_union_vs_port(port, n):
     assert rel_l2(ps.pressure(), ref["p"]) < P_REL_L2
 
 
-def test_flip_substep_64_vs_port(port):
+@pytest.mark.parametrize("precision", ["fp32", "mixed"])
+def test_flip_substep_64_vs_port(port, precision):
     n = 64
     h = (1.0 / n,) * 3
     sc = scenes.flip_first_substep(n, box_hi=(0.25, 0.75, 1.0))
@@ -124,7 +126,7 @@ def test_flip_substep_64_vs_port(port):
                               oracle.MgParams(400, 5, 3, 3, 20, 20, 1e-13, 1.5,
                                               True))
     ps, out, st = solve((n,) * 3, h, sc["u"], sc["v"], sc["w"],
-                        sc["boundary_sdf"], sc["fluid_sdf"])
+                        sc["boundary_sdf"], sc["fluid_sdf"], precision)
     assert st == 0
     assert ps.last_stats.relative_residual <= TOL
     assert rel_l2(ps.pressure(), ref["p"]) < P_REL_L2
