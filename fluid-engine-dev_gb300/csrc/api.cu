@@ -52,7 +52,6 @@ void free_buffers(Ctx* c) {
         release(&L.x2);
         release(&L.b);
         release(&L.r);
-        release(&L.Ah);
     }
     c->levels.clear();
     release(&c->A64);
@@ -158,12 +157,11 @@ long field_count(const jetgpu_scalar_field* f) {
     return f->kind == 1 ? (long)f->res[0] * f->res[1] * f->res[2] : 0;
 }
 
-__global__ void k_rows_to_f32(const double* __restrict__ A, float4* __restrict__ out,
+__global__ void k_rows_to_f32(const double* __restrict__ A, float* __restrict__ out,
                               long N) {
     for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < N;
          c += (long)gridDim.x * blockDim.x)
-        out[c] = make_float4((float)A[4 * c], (float)A[4 * c + 1],
-                             (float)A[4 * c + 2], (float)A[4 * c + 3]);
+        for (int k = 0; k < 4; ++k) out[k * N + c] = (float)A[4 * c + k];
 }
 
 __global__ void k_fill_f32(float* __restrict__ p, float v, long N) {
@@ -172,15 +170,14 @@ __global__ void k_fill_f32(float* __restrict__ p, float v, long N) {
         p[c] = v;
 }
 
-__global__ void k_rows_f32_to_f64(const float4* __restrict__ A,
+__global__ void k_rows_f32_to_f64(const float* __restrict__ A,
                                   double* __restrict__ out, long N) {
     for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < N;
          c += (long)gridDim.x * blockDim.x) {
-        const float4 r = A[c];
-        out[4 * c] = r.x;
-        out[4 * c + 1] = r.y;
-        out[4 * c + 2] = r.z;
-        out[4 * c + 3] = r.w;
+        out[4 * c] = A[c];
+        out[4 * c + 1] = A[N + c];
+        out[4 * c + 2] = A[2 * N + c];
+        out[4 * c + 3] = A[3 * N + c];
     }
 }
 
@@ -212,8 +209,8 @@ jetgpu_status ensure_buffers(Ctx* c, Dims n, unsigned max_levels) {
         JG_CUDA(c, alloc(&L.uw, (size_t)(s.x + 1) * s.y * s.z));
         JG_CUDA(c, alloc(&L.vw, (size_t)s.x * (s.y + 1) * s.z));
         JG_CUDA(c, alloc(&L.ww, (size_t)s.x * s.y * (s.z + 1)));
-        JG_CUDA(c, alloc(&L.A, N));
-        JG_CUDA(c, alloc(&L.Ah, N));
+        JG_CUDA(c, alloc(&L.A, 4 * (size_t)N));
+        JG_CUDA(c, alloc(&L.Ah, 4 * (size_t)N));
         JG_CUDA(c, alloc(&L.x, N));
         JG_CUDA(c, alloc(&L.x2, N));
         JG_CUDA(c, alloc(&L.b, N));

@@ -119,6 +119,12 @@ __device__ __forceinline__ bool nonzero_d(double x) {
     dwords(x, lo, hi);
     return ((hi & 0x7fffffffu) | lo) != 0u;
 }
+// The reference's lerp, out of line: the exact shortcuts below cover the
+// common fractions, and a call keeps the compiler from predicating this
+// FP64 expression into every sample.
+__device__ __noinline__ double lerp_slow(double a, double b, double f) {
+    return lerpd(a, b, f);
+}
 __device__ __forceinline__ double lerp_c(double a, double b, double f,
                                          long long fb) {
     if (fb == kHalfBits) {
@@ -128,7 +134,7 @@ __device__ __forceinline__ double lerp_c(double a, double b, double f,
     } else if (fb == kOneBits) {
         if (nonzero_d(b) && expo_d(a) != 0x7ffu) return b;
     }
-    return lerpd(a, b, f);
+    return lerp_slow(a, b, f);
 }
 
 __device__ double sample_field(const FieldDesc& F, double x, double y,
@@ -168,63 +174,81 @@ __device__ __forceinline__ double frac_sdf(double p0, double p1) {
     return 0.0;
 }
 
-__device__ __forceinline__ void cycle4(double* a) {
-    double t = a[0];
-    a[0] = a[1];
-    a[1] = a[2];
-    a[2] = a[3];
-    a[3] = t;
+// (l0, l1, l2, l3) rotated left by k (0..3) with constant register moves.
+__device__ __forceinline__ void rot4(double& l0, double& l1, double& l2,
+                                     double& l3, int k) {
+#pragma unroll
+    for (int r = 0; r < 3; ++r) {
+        if (r < k) {
+            const double t = l0;
+            l0 = l1;
+            l1 = l2;
+            l2 = l3;
+            l3 = t;
+        }
+    }
 }
 
 // Marching-squares area of the inside region of a face (fractionInside).
+// The corners are visited counter-clockwise from bottom-left; each case
+// rotates them (the reference's cycleArray) until its anchor corner comes
+// first: the rotation count is the first r at which the rotated view stops
+// satisfying the reference's loop condition (4 rotations = none).
 __device__ __noinline__ double frac_inside(double bl, double br, double tl,
                                            double tr) {
-    const int n = (bl < 0) + (tl < 0) + (br < 0) + (tr < 0);
-    double l[4] = {bl, br, tr, tl};
+    const double v[4] = {bl, br, tr, tl};
+    const bool in[4] = {bl < 0, br < 0, tr < 0, tl < 0};
+    const bool ge[4] = {bl >= 0, br >= 0, tr >= 0, tl >= 0};  // NaN: neither
+    const int n = in[0] + in[1] + in[2] + in[3];
     const double half = 0.5;  // 0.5f widened, exact
     const double quarter = 0.25;
     if (n == 4) return 1.0;
+    if (n == 0) return 0.0;
+    int k = 0;
+#pragma unroll
+    for (int r = 3; r >= 0; --r) {
+        bool go;  // the reference's loop condition on the view rotated by r
+        if (n == 3) go = in[r];
+        else if (n == 2) go = ge[r] || !(in[(r + 1) & 3] || in[(r + 2) & 3]);
+        else go = ge[r];
+        if (!go) k = r;
+    }
+    double l0 = v[0], l1 = v[1], l2 = v[2], l3 = v[3];
+    rot4(l0, l1, l2, l3, k);
     if (n == 3) {
-        for (int r = 0; r < 4 && l[0] < 0; ++r) cycle4(l);
-        const double s0 = 1.0 - frac_sdf(l[0], l[3]);
-        const double s1 = 1.0 - frac_sdf(l[0], l[1]);
+        const double s0 = 1.0 - frac_sdf(l0, l3);
+        const double s1 = 1.0 - frac_sdf(l0, l1);
         return 1.0 - half * s0 * s1;
     }
     if (n == 2) {
-        for (int r = 0; r < 4 && (l[0] >= 0 || !(l[1] < 0 || l[2] < 0)); ++r)
-            cycle4(l);
-        if (l[1] < 0) {
-            const double sl = frac_sdf(l[0], l[3]);
-            const double sr = frac_sdf(l[1], l[2]);
+        if (l1 < 0) {
+            const double sl = frac_sdf(l0, l3);
+            const double sr = frac_sdf(l1, l2);
             return half * (sl + sr);
         }
-        const double mid = quarter * (l[0] + l[1] + l[2] + l[3]);
+        const double mid = quarter * (l0 + l1 + l2 + l3);
         if (mid < 0) {
             double area = 0.0;
-            const double s1 = 1.0 - frac_sdf(l[0], l[3]);
-            const double s3 = 1.0 - frac_sdf(l[2], l[3]);
+            const double s1 = 1.0 - frac_sdf(l0, l3);
+            const double s3 = 1.0 - frac_sdf(l2, l3);
             area += half * s1 * s3;
-            const double s2 = 1.0 - frac_sdf(l[2], l[1]);
-            const double s0 = 1.0 - frac_sdf(l[0], l[1]);
+            const double s2 = 1.0 - frac_sdf(l2, l1);
+            const double s0 = 1.0 - frac_sdf(l0, l1);
             area += half * s0 * s2;
             return 1.0 - area;
         }
         double area = 0.0;
-        const double s0 = frac_sdf(l[0], l[1]);
-        const double s1 = frac_sdf(l[0], l[3]);
+        const double s0 = frac_sdf(l0, l1);
+        const double s1 = frac_sdf(l0, l3);
         area += half * s0 * s1;
-        const double s2 = frac_sdf(l[2], l[1]);
-        const double s3 = frac_sdf(l[2], l[3]);
+        const double s2 = frac_sdf(l2, l1);
+        const double s3 = frac_sdf(l2, l3);
         area += half * s2 * s3;
         return area;
     }
-    if (n == 1) {
-        for (int r = 0; r < 4 && l[0] >= 0; ++r) cycle4(l);
-        const double s0 = frac_sdf(l[0], l[3]);
-        const double s1 = frac_sdf(l[0], l[1]);
-        return half * s0 * s1;
-    }
-    return 0.0;
+    const double s0 = frac_sdf(l0, l3);
+    const double s1 = frac_sdf(l0, l1);
+    return half * s0 * s1;
 }
 
 __device__ __forceinline__ float face_weight(double p0, double p1, double p2,
@@ -376,7 +400,7 @@ __global__ void k_build_system(Dims n, SpacingInv S,
                                const double* __restrict__ sw,
                                double* __restrict__ A64,
                                double* __restrict__ b64,
-                               float4* __restrict__ A32,
+                               float* __restrict__ A32,
                                float4* __restrict__ Alo,
                                float2* __restrict__ bdf) {
     const long N = n.count();
@@ -489,7 +513,10 @@ __global__ void k_build_system(Dims n, SpacingInv S,
             lo4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
             bh = bl = 0.0f;
         }
-        A32[c] = hi4;
+        A32[c] = hi4.x;  // structure of arrays: center, right, up, front
+        A32[N + c] = hi4.y;
+        A32[2 * N + c] = hi4.z;
+        A32[3 * N + c] = hi4.w;
         if (Alo) Alo[c] = lo4;
         if (bdf) bdf[c] = make_float2(bh, bl);
     }

@@ -21,12 +21,15 @@ struct Level {
     float* uw = nullptr;         // face weights
     float* vw = nullptr;
     float* ww = nullptr;
-    float4* A = nullptr;         // FP32 matrix rows
+    // Matrix rows as a structure of arrays: the center, right, up and front
+    // coefficients in four planes of N values each (FP32 in A; BF16 in Ah
+    // for the mixed-precision V-cycle).
+    float* A = nullptr;
     float* x = nullptr;          // V-cycle solution
     float* x2 = nullptr;         // ping-pong partner of x (fused smoother)
     float* b = nullptr;          // V-cycle rhs
     float* r = nullptr;          // residual scratch
-    uint2* Ah = nullptr;         // BF16 rows of the mixed-precision V-cycle
+    unsigned short* Ah = nullptr;
 };
 
 // Kernel classes of the live per-kernel profile (jetgpu_profile_read).
@@ -86,7 +89,7 @@ struct Ctx {
     jetgpu_config cfg;
     int device = 0;
     int num_sms = 0;
-    int col_blocks_per_sm = 1;  // resident blocks of the fused sweep per SM
+    int col_blocks_per_sm[2] = {1, 1};  // fused sweep blocks/SM: FP32, BF16 rows
     std::unordered_map<const void*, int> occupancy;  // blocks/SM per kernel
     cudaStream_t stream = nullptr;
     std::string err;

@@ -84,19 +84,28 @@ __device__ __forceinline__ void reduce_finish(double partial, int slot,
 // ---------------------------------------------------------------------------
 // Matrix access: FP32 rows (float4) or the exact FP64 rows (4 doubles).
 
+// Rows of one level as a structure of arrays (center, right, up, front
+// planes of N values).
 struct RowsF {
-    const float4* A;
-    __device__ __forceinline__ float4 row(long c) const { return A[c]; }
+    const float* A;
+    long N;
+    __device__ __forceinline__ float4 row(long c) const {
+        return make_float4(__ldg(A + c), __ldg(A + N + c), __ldg(A + 2 * N + c),
+                           __ldg(A + 3 * N + c));
+    }
 };
-// BF16 rows (mixed mode): {center | right << 16, up | front << 16}.
-__device__ __forceinline__ float bf_lo(unsigned u) { return __uint_as_float(u << 16); }
-__device__ __forceinline__ float bf_hi(unsigned u) { return __uint_as_float(u & 0xffff0000u); }
-__device__ __forceinline__ float4 bf_row(uint2 r) {
-    return make_float4(bf_lo(r.x), bf_hi(r.x), bf_lo(r.y), bf_hi(r.y));
+// BF16 rows (mixed mode), same layout.
+__device__ __forceinline__ float bf_dec(unsigned short u) {
+    return __uint_as_float((unsigned)u << 16);
 }
 struct RowsB {
-    const uint2* A;
-    __device__ __forceinline__ float4 row(long c) const { return bf_row(__ldg(A + c)); }
+    const unsigned short* A;
+    long N;
+    __device__ __forceinline__ float4 row(long c) const {
+        return make_float4(bf_dec(__ldg(A + c)), bf_dec(__ldg(A + N + c)),
+                           bf_dec(__ldg(A + 2 * N + c)),
+                           bf_dec(__ldg(A + 3 * N + c)));
+    }
 };
 struct RowsD {
     const double* A;
@@ -223,8 +232,7 @@ __global__ void __launch_bounds__(kThreads)
 // the FP32 image of r (the next correction's right-hand side), zeroes the
 // FP32 correction and reduces ||r||^2 into scal[target].
 __global__ void __launch_bounds__(kThreads)
-    k_residual_df(const float4* __restrict__ Ahi,
-                  const float4* __restrict__ Alo,
+    k_residual_df(RowsF Ahi, const float4* __restrict__ Alo,
                   const float2* __restrict__ x, const float2* __restrict__ b,
                   float* __restrict__ r32, float* __restrict__ zero32, Dims n,
                   double* partials, unsigned* counters, double* scal,
@@ -237,7 +245,7 @@ __global__ void __launch_bounds__(kThreads)
          c += (long)gridDim.x * kThreads) {
         int i, j, k;
         cell_ijk(c, n, i, j, k);
-        const float4 h = Ahi[c], l = Alo[c];
+        const float4 h = Ahi.row(c), l = Alo[c];
         const float2 xc = x[c], bc = b[c];
         DF r;
         r.hi = bc.x;
@@ -245,7 +253,7 @@ __global__ void __launch_bounds__(kThreads)
         r = df_sub_prod(r, h.x, l.x, xc.x, xc.y);
         if (i > 0) {
             const float2 xn = x[c - 1];
-            r = df_sub_prod(r, Ahi[c - 1].y, Alo[c - 1].y, xn.x, xn.y);
+            r = df_sub_prod(r, Ahi.row(c - 1).y, Alo[c - 1].y, xn.x, xn.y);
         }
         if (i + 1 < n.x) {
             const float2 xn = x[c + 1];
@@ -253,7 +261,7 @@ __global__ void __launch_bounds__(kThreads)
         }
         if (j > 0) {
             const float2 xn = x[c - sy];
-            r = df_sub_prod(r, Ahi[c - sy].z, Alo[c - sy].z, xn.x, xn.y);
+            r = df_sub_prod(r, Ahi.row(c - sy).z, Alo[c - sy].z, xn.x, xn.y);
         }
         if (j + 1 < n.y) {
             const float2 xn = x[c + sy];
@@ -261,7 +269,7 @@ __global__ void __launch_bounds__(kThreads)
         }
         if (k > 0) {
             const float2 xn = x[c - sz];
-            r = df_sub_prod(r, Ahi[c - sz].w, Alo[c - sz].w, xn.x, xn.y);
+            r = df_sub_prod(r, Ahi.row(c - sz).w, Alo[c - sz].w, xn.x, xn.y);
         }
         if (k + 1 < n.z) {
             const float2 xn = x[c + sz];
@@ -411,36 +419,32 @@ __global__ void __launch_bounds__(kThreads)
 
 // K8 (fused): one full red-black SOR sweep in a single pass over memory.
 //
-// Register-column design. A block owns a tile of 32 cell pairs (64 cells)
-// in i by 8 rows in j and marches through k. Each thread holds the k-column
-// of one pair (cells 2m, 2m+1 of a row) in registers: at every plane a pair
-// has exactly one cell of each colour, and the cells directly below and
-// above a cell have the other colour, so the column neighbours of every
-// update are the thread's own registers. Only in-plane neighbours go through
-// shared memory (one float2 of x and of the two "up" coefficients, one float
-// of the pair's "right" coefficient and one of its first-colour result per
-// pair and plane), which keeps shared-memory traffic at a few words per
-// cell. Step t of the march
-//   (1) updates the first colour F of plane t+1 from old values (tile plus
-//       a one-pair / one-row ring, so the tile's second-colour cells have
-//       all their new F neighbours; ring rows also load x of the next row
-//       out, which their update reads),
+// A block owns a tile of 32 cell pairs (64 cells) in i by 8 rows in j and
+// marches through k; each thread owns one pair (cells 2m, 2m+1 of a row).
+// At every plane a pair holds one cell of each colour, and the cells
+// directly below and above a cell have the other colour, so a thread's
+// column neighbours are its own pair one plane away. Planes of x, of the
+// four row components (structure of arrays) and of b are staged into
+// shared-memory rings by cp.async, two planes ahead of their first use, each
+// thread copying its own pair (zero-filled outside the domain); every read
+// then is a conflict-free word of a consecutive-pair array. Step t of the
+// march
+//   (1) updates the first colour F of plane t+1 from old values, on the tile
+//       plus a one-pair / one-row ring (ring rows also stage x of the row
+//       beyond, which their update reads),
 //   (2) updates the second colour S of plane t from the new F values of
-//       planes t-1, t, t+1 and writes both colours of plane t as one float2.
+//       planes t-1, t, t+1 (the thread's own results of the previous, this
+//       and the next plane, and the neighbours' from shared memory) and
+//       writes both colours of plane t as one float2.
 // x is read from `xin` and written to `xout` (ping-pong), so blocks never
 // observe each other's updates: the result is exactly the sequential
 // red-then-black sweep, deterministic, with no inter-block synchronisation.
-// Global loads are issued two planes ahead into registers. Cells outside the
-// domain load as x = 0 and a zero row, which reproduces the reference's
-// guarded neighbour terms (FdmBlas3::mvm, fdm_linear_system3.cpp:79-96), and
-// are never written. Work items are (k-slab, tile) pairs ordered slab-major
-// and dealt round-robin to a persistent grid, so the blocks working at the
-// same time hold neighbouring tiles of the same slab: the ring rows and the
-// two warm-up planes a column re-reads were loaded moments earlier by a
-// neighbour and come from L2, not HBM.
-// HBM traffic per sweep: x, b and A read once, x written once — 28 B/cell
-// (24 B/cell from a zero start) — plus ring re-reads that mostly hit L2.
-// Requires an even nx.
+// Outside the domain x = 0 and the rows are zero, which reproduces the
+// reference's guarded neighbour terms (FdmBlas3::mvm,
+// fdm_linear_system3.cpp:79-96). The grid is persistent: each block walks a
+// contiguous range of the (tile, plane) work list. HBM traffic per sweep: x, b and the rows read once,
+// x written once — 12 B/cell plus 16 (FP32) or 8 (BF16) B/cell of rows —
+// plus ring re-reads, mostly from L2. Requires an even nx.
 namespace col {
 constexpr int TXP = 32;            // pairs per tile row (64 cells)
 constexpr int TY = 8;              // rows per tile
@@ -449,209 +453,246 @@ constexpr int PY = TY + 2;         // rows including the ring
 constexpr int NW = PX * PY;        // working threads (340)
 constexpr int BLOCK = 352;         // 11 warps
 constexpr int TCX = 2 * TXP;       // tile width in cells
+constexpr int XR = 5, AR = 5, BR = 4;  // ring depths in planes
+constexpr int XROWS = PY + 2;      // x rows -2 .. TY+1
+constexpr int UROWS = PY + 1;      // "up" rows -2 .. TY
 }  // namespace col
 
-// The two matrix rows of a cell pair as loaded (decoded where used).
-template <typename R> struct PairRows;
-template <> struct PairRows<RowsF> {
-    float4 a0, a1;
-    __device__ __forceinline__ void zero() {
-        a0 = a1 = make_float4(0.f, 0.f, 0.f, 0.f);
+template <int BYTES>
+__device__ __forceinline__ void cpa(void* smem, const void* gmem, bool valid) {
+    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
+    asm volatile("cp.async.ca.shared.global [%0], [%1], %2, %3;\n" ::"r"(sa),
+                 "l"(gmem), "n"(BYTES), "r"(valid ? BYTES : 0));
+}
+__device__ __forceinline__ void cpa_commit() {
+    asm volatile("cp.async.commit_group;\n" ::);
+}
+template <int N>
+__device__ __forceinline__ void cpa_wait() {
+    asm volatile("cp.async.wait_group %0;\n" ::"n"(N));
+}
+
+// Storage of one row component in shared memory: FP32, or BF16 kept as its
+// 16 bits (decoded with a shift). Staged per pair (8 or 4 bytes).
+template <typename R> struct ColTraits;
+template <> struct ColTraits<RowsF> {
+    using E = float;
+    static constexpr int bytes = 8;
+    __device__ static float get(const E* p) { return *p; }
+    __device__ static const void* src(const RowsF& M, int k, long idx) {
+        return M.A + k * M.N + idx;
     }
-    __device__ __forceinline__ void load(const RowsF& M, int idx) {
-        a0 = __ldg(M.A + idx);
-        a1 = __ldg(M.A + idx + 1);
-    }
-    __device__ __forceinline__ float4 r0() const { return a0; }
-    __device__ __forceinline__ float4 r1() const { return a1; }
 };
-template <> struct PairRows<RowsB> {
-    uint4 raw;  // both BF16 rows: one aligned 16-byte load (idx is even)
-    __device__ __forceinline__ void zero() { raw = make_uint4(0u, 0u, 0u, 0u); }
-    __device__ __forceinline__ void load(const RowsB& M, int idx) {
-        raw = __ldg(reinterpret_cast<const uint4*>(M.A + idx));
+template <> struct ColTraits<RowsB> {
+    using E = unsigned short;
+    static constexpr int bytes = 4;
+    __device__ static float get(const E* p) {
+        return __uint_as_float((unsigned)*p << 16);
     }
-    __device__ __forceinline__ float4 r0() const {
-        return bf_row(make_uint2(raw.x, raw.y));
-    }
-    __device__ __forceinline__ float4 r1() const {
-        return bf_row(make_uint2(raw.z, raw.w));
+    __device__ static const void* src(const RowsB& M, int k, long idx) {
+        return M.A + k * M.N + idx;
     }
 };
 
+// Shared-memory rings. Every row is a flat run of CW = 2 * PX cells (the
+// tile's 64 cells plus one ring pair each side), so a cell's in-row
+// neighbours are the adjacent elements and its j-neighbours the same
+// element of the adjacent rows.
+namespace col {
+constexpr int CW = 2 * PX;  // cells per staged row (68)
+}
 template <typename R>
-struct ColPlane {
-    float2 x;          // old x of the pair
-    PairRows<R> a;     // rows of the pair's two cells
-    float2 b;          // rhs of the pair
-    float2 xe;         // ring rows: old x of the row beyond
-    float2 ue;         // top ring row: "up" coefficients of the row beyond
+struct ColSmem {
+    using E = typename ColTraits<R>::E;
+    float x[col::XR][col::XROWS][col::CW];
+    E c[col::AR][col::PY][col::CW];
+    E r[col::AR][col::PY][col::CW];
+    E f[col::AR][col::PY][col::CW];
+    E u[col::AR][col::UROWS][col::CW];
+    float b[col::BR][col::PY][col::CW];
+    float yf[2][col::PY][col::CW];  // new first-colour values, by plane parity
 };
 
 template <bool ZERO, typename R>
 __global__ void __launch_bounds__(col::BLOCK, 2)
-    k_rb_sweep_col(R A, const float* __restrict__ b,
+    k_rb_sweep_col(R M, const float* __restrict__ b,
                    const float* __restrict__ xin, float* __restrict__ xout,
-                   Dims n, int first, float omega, int tiles_x, int tiles,
-                   int kz, int items) {
+                   Dims n, int first, float omega, int tiles_x,
+                   long total, long per_block) {
     using namespace col;
-    __shared__ float2 sX[PY + 2][PX];      // x of plane t+1, rows -2..TY+1
-    __shared__ float sYF[2][PY][PX];       // F result per pair, by plane parity
-    __shared__ float sAr[2][PY][PX];       // "right" of the pair's cell 1
-    __shared__ float2 sAu[2][PY + 1][PX];  // "up" of both cells, rows -2..TY-1
+    using T = ColTraits<R>;
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    ColSmem<R>& S = *reinterpret_cast<ColSmem<R>*>(smem_raw);
     const int tid = threadIdx.x;
     const bool worker = tid < NW;
     const int py = worker ? tid / PX : 0;  // tile row py - 1
     const int px = worker ? tid - py * PX : 0;
     const int sz = n.x * n.y;  // grids hold < 2^31 cells
-    const bool ring_lo = py == 0, ring_hi = py == PY - 1;
-    const bool interior = worker && px > 0 && px < PX - 1 && !ring_lo &&
-                          !ring_hi;
+    const bool ring_lo = worker && py == 0, ring_hi = worker && py == PY - 1;
+    const bool interior = worker && px > 0 && px < PX - 1 && py > 0 &&
+                          py < PY - 1;
+    auto slot = [](int p, int D) { return ((p % D) + D) % D; };
+    if (ZERO) {  // x = 0 everywhere: the x ring is zeroed once, never staged
+        float* xs = &S.x[0][0][0];
+        for (int q = tid; q < XR * XROWS * CW; q += BLOCK) xs[q] = 0.f;
+    }
 
-    for (int item = blockIdx.x; item < items; item += gridDim.x) {
-        const int slab = item / tiles;
-        const int tile = item - slab * tiles;
-        const int k0 = slab * kz;
-        const int k1 = min(n.z, k0 + kz);
+    // This block's contiguous range of the (tile, plane) work list, in
+    // segments of consecutive planes of one tile.
+    long w = (long)blockIdx.x * per_block;
+    const long wend = min(total, w + per_block);
+    while (w < wend) {
+        const int tile = (int)(w / n.z);
+        const int k0 = (int)(w - (long)tile * n.z);
+        const int k1 = (int)min((long)n.z, k0 + (wend - w));
+        w += k1 - k0;
         const int i0 = (tile % tiles_x) * TCX;
         const int j0 = (tile / tiles_x) * TY;
         const int gi = i0 + 2 * (px - 1);
         const int gj = j0 + py - 1;
         const bool colv = worker && gi >= 0 && gi < n.x && gj >= 0 && gj < n.y;
         const int ej = ring_lo ? gj - 1 : gj + 1;
-        const bool exv = worker && (ring_lo || ring_hi) && gi >= 0 &&
-                         gi < n.x && ej >= 0 && ej < n.y;
-        const bool uev = exv && ring_lo;
+        const bool exv = (ring_lo || ring_hi) && gi >= 0 && gi < n.x &&
+                         ej >= 0 && ej < n.y;
         const int cb = colv ? gi + n.x * gj : 0;
         const int eb = exv ? gi + n.x * ej : 0;
 
-        // Loads of plane p (zeros outside the domain or beyond `need`).
-        auto load = [&](int p, bool need_x, bool need_rest) {
-            ColPlane<R> q;
-            q.x = make_float2(0.f, 0.f);
-            q.xe = make_float2(0.f, 0.f);
-            q.a.zero();
-            q.b = make_float2(0.f, 0.f);
-            q.ue = make_float2(0.f, 0.f);
-            if (p < 0 || p >= n.z) return q;
-            const int pb = sz * p;
-            if (!ZERO && need_x) {
-                if (colv) q.x = __ldg(reinterpret_cast<const float2*>(xin + pb + cb));
+        // Stage x of plane p (own row, plus the row beyond for ring rows).
+        const int pc = 2 * px;  // this pair's first cell in a staged row
+        auto stage_x = [&](int p) {
+            if (ZERO || !worker) return;
+            const bool pin = p >= 0 && p < n.z;
+            const int sl = slot(p, XR);
+            const int off = pin ? sz * p : 0;
+            cpa<8>(&S.x[sl][py + 1][pc], xin + (colv && pin ? off + cb : 0),
+                   colv && pin);
+            if (ring_lo)
+                cpa<8>(&S.x[sl][0][pc], xin + (exv && pin ? off + eb : 0),
+                       exv && pin);
+            if (ring_hi)
+                cpa<8>(&S.x[sl][PY + 1][pc], xin + (exv && pin ? off + eb : 0),
+                       exv && pin);
+        };
+        // Stage the row components and b of plane p.
+        auto stage_ab = [&](int p) {
+            if (!worker) return;
+            const bool pin = p >= 0 && p < n.z;
+            const int sa = slot(p, AR), sb = slot(p, BR);
+            const long off = pin ? (long)sz * p : 0;
+            const bool v = colv && pin;
+            const long idx = v ? off + cb : 0;
+            cpa<T::bytes>(&S.c[sa][py][pc], T::src(M, 0, idx), v);
+            cpa<T::bytes>(&S.r[sa][py][pc], T::src(M, 1, idx), v);
+            cpa<T::bytes>(&S.u[sa][py + 1][pc], T::src(M, 2, idx), v);
+            cpa<T::bytes>(&S.f[sa][py][pc], T::src(M, 3, idx), v);
+            if (ring_lo) {
+                const bool ve = exv && pin;
+                cpa<T::bytes>(&S.u[sa][0][pc], T::src(M, 2, ve ? off + eb : 0),
+                              ve);
             }
-            if (need_rest) {
-                if (!ZERO && exv)
-                    q.xe = __ldg(reinterpret_cast<const float2*>(xin + pb + eb));
-                if (colv) {
-                    q.a.load(A, pb + cb);
-                    q.b = __ldg(reinterpret_cast<const float2*>(b + pb + cb));
-                }
-                if (uev)
-                    q.ue = make_float2(A.row(pb + eb).z, A.row(pb + eb + 1).z);
-            }
-            return q;
+            cpa<8>(&S.b[sb][py][pc], b + idx, v);
         };
 
-        // Register column. Planes: X t..t+2, A t-1 (front) .. t+1, b t..t+1.
+        __syncthreads();  // the previous segment's reads of the rings are done
         const int t0 = k0 - 2;
-        ColPlane<R> P0 = load(t0, true, true);      // x(t), A(t)
-        ColPlane<R> P1 = load(t0 + 1, true, true);  // x(t+1), A(t+1), b(t+1)
-        float2 x2 = load(t0 + 2, true, false).x;    // x(t+2)
-        ColPlane<R> Q1 = load(t0 + 2, false, true); // A, b, ring of t+2
-        float2 qx1 = load(t0 + 3, true, false).x;  // x(t+3)
-        float2 amf = make_float2(0.f, 0.f);        // fronts of plane t-1
-        float yfm = 0.f, yf0 = 0.f;                // F results of t-1, t
+        stage_x(t0);
+        stage_x(t0 + 1);
+        stage_x(t0 + 2);
+        stage_ab(t0 - 1);
+        stage_ab(t0);
+        stage_ab(t0 + 1);
+        cpa_commit();
+        stage_x(t0 + 3);
+        stage_ab(t0 + 2);
+        cpa_commit();
+        float yfm = 0.f, yf0 = 0.f;  // own F results of planes t-1, t
 
+        // Ring slots of the planes step t touches, advanced once per step.
+        int xs0 = slot(t0, XR), as0 = slot(t0, AR), bs0 = slot(t0, BR);
+        auto nx = [](int q, int D) { return q + 1 == D ? 0 : q + 1; };
+        auto pv = [](int q, int D) { return q == 0 ? D - 1 : q - 1; };
         for (int t = t0; t < k1; ++t) {
-            // Prefetch: A, b, ring of t+3 and x of t+4.
-            ColPlane<R> Q2 = load(t + 3, false, t + 3 <= k1);
-            const float2 qx2v = load(t + 4, t + 4 <= k1 + 1, false).x;
-
-            const int p1 = t + 1;
-            const int par1 = p1 & 1, par0 = t & 1;
-            if (worker) {
-                sX[py + 1][px] = P1.x;
-                if (ring_lo) sX[0][px] = P1.xe;
-                if (ring_hi) sX[PY + 1][px] = P1.xe;
-                const float4 r0 = P1.a.r0(), r1 = P1.a.r1();
-                sAr[par1][py][px] = r1.y;
-                sAu[par1][py + 1][px] = make_float2(r0.z, r1.z);
-                if (ring_lo) sAu[par1][0][px] = P1.ue;
-            }
+            cpa_wait<1>();
             __syncthreads();
+            // Two planes ahead: x of t+4, rows and b of t+3 (the slots of
+            // planes the previous step was the last to read).
+            if (t + 4 <= k1 + 1) stage_x(t + 4);
+            if (t + 3 <= k1) stage_ab(t + 3);
+            cpa_commit();
+            const int xs1 = nx(xs0, XR), xs2 = nx(xs1, XR);
+            const int as1 = nx(as0, AR), asm1 = pv(as0, AR);
+            const int bs1 = nx(bs0, BR);
 
-            // (1) First colour of plane t+1.
+            // (1) First colour of plane t+1 at staged cell cf of this pair.
+            const int p1 = t + 1;
             float yf1 = 0.f;
+            const int eF1 = (first + gj + p1) & 1;
+            const int cf = pc + eF1;
             if (colv && p1 >= 0 && p1 < n.z) {
-                const int e = (first + gj + p1) & 1;  // F cell of the pair
-                const bool skip = (px == 0 && e == 0) || (px == PX - 1 && e == 1);
+                const bool skip = (px == 0 && eF1 == 0) || (px == PX - 1 && eF1 == 1);
                 if (!skip) {
-                    const float4 p10 = P1.a.r0(), p11 = P1.a.r1();
-                    const float4 r = e ? p11 : p10;
-                    const float xold = e ? P1.x.y : P1.x.x;
-                    const float xl = e ? P1.x.x : sX[py + 1][px - 1].y;
-                    const float xr = e ? sX[py + 1][px + 1].x : P1.x.y;
-                    const float2 xd2 = sX[py][px], xu2 = sX[py + 2][px];
-                    const float xd = e ? xd2.y : xd2.x;
-                    const float xu = e ? xu2.y : xu2.x;
-                    const float xb = e ? P0.x.y : P0.x.x;
-                    const float xf = e ? x2.y : x2.x;
-                    const float cl = e ? p10.y : sAr[par1][py][px - 1];
-                    const float2 dn2 = sAu[par1][py][px];
-                    const float cd = e ? dn2.y : dn2.x;
-                    const float cb_ = e ? P0.a.r1().w : P0.a.r0().w;
-                    const float bb = e ? P1.b.y : P1.b.x;
-                    const float acc = cl * xl + r.y * xr + cd * xd + r.z * xu +
-                                      cb_ * xb + r.w * xf;
+                    const float* xr1 = &S.x[xs1][py + 1][cf];
+                    const float xold = xr1[0];
+                    const float xl = xr1[-1];
+                    const float xr = xr1[1];
+                    const float xd = S.x[xs1][py][cf];
+                    const float xu = S.x[xs1][py + 2][cf];
+                    const float xb = S.x[xs0][py + 1][cf];
+                    const float xf = S.x[xs2][py + 1][cf];
+                    const auto* rr = &S.r[as1][py][cf];
+                    const float center = T::get(&S.c[as1][py][cf]);
+                    const float right = T::get(rr);
+                    const float cl = T::get(rr - 1);
+                    const float up = T::get(&S.u[as1][py + 1][cf]);
+                    const float cd = T::get(&S.u[as1][py][cf]);
+                    const float front = T::get(&S.f[as1][py][cf]);
+                    const float cbk = T::get(&S.f[as0][py][cf]);
+                    const float bb = S.b[bs1][py][cf];
+                    const float acc = cl * xl + right * xr + cd * xd + up * xu +
+                                      cbk * xb + front * xf;
                     yf1 = (1.0f - omega) * xold +
-                          omega * __fdividef(bb - acc, r.x);
+                          omega * __fdividef(bb - acc, center);
                 }
             }
-            if (worker) sYF[par1][py][px] = yf1;
+            if (worker) S.yf[p1 & 1][py][cf] = yf1;
 
-            // (2) Second colour of plane t; write plane t.
+            // (2) Second colour of plane t at staged cell cs; write plane t.
             if (interior && colv && t >= k0) {
-                const int eF = (first + gj + t) & 1;
-                const int e = eF ^ 1;  // S cell of the pair
-                const float4 p00 = P0.a.r0(), p01 = P0.a.r1();
-                const float4 r = e ? p01 : p00;
-                const float xold = e ? P0.x.y : P0.x.x;
-                const float yl = e ? yf0 : sYF[par0][py][px - 1];
-                const float yr = e ? sYF[par0][py][px + 1] : yf0;
-                const float yd = sYF[par0][py - 1][px];
-                const float yu = sYF[par0][py + 1][px];
-                const float cl = e ? p00.y : sAr[par0][py][px - 1];
-                const float2 dn2 = sAu[par0][py][px];
-                const float cd = e ? dn2.y : dn2.x;
-                const float cbk = e ? amf.y : amf.x;
-                const float bb = e ? P0.b.y : P0.b.x;
-                const float acc = cl * yl + r.y * yr + cd * yd + r.z * yu +
-                                  cbk * yfm + r.w * yf1;
+                // The S cell of plane t sits under the F cell of plane t+1.
+                const int eS = eF1;
+                const int cs0 = cf;
+                const float* yr0 = &S.yf[t & 1][py][cs0];
+                const auto* rr = &S.r[as0][py][cs0];
+                const float center = T::get(&S.c[as0][py][cs0]);
+                const float right = T::get(rr);
+                const float cl = T::get(rr - 1);
+                const float up = T::get(&S.u[as0][py + 1][cs0]);
+                const float cd = T::get(&S.u[as0][py][cs0]);
+                const float front = T::get(&S.f[as0][py][cs0]);
+                const float cbk = T::get(&S.f[asm1][py][cs0]);
+                const float bb = S.b[bs0][py][cs0];
+                const float xold = S.x[xs0][py + 1][cs0];
+                const float yl = yr0[-1];
+                const float yr = yr0[1];
+                const float yd = S.yf[t & 1][py - 1][cs0];
+                const float yu = S.yf[t & 1][py + 1][cs0];
+                const float acc = cl * yl + right * yr + cd * yd + up * yu +
+                                  cbk * yfm + front * yf1;
                 const float ys = (1.0f - omega) * xold +
-                                 omega * __fdividef(bb - acc, r.x);
+                                 omega * __fdividef(bb - acc, center);
                 float2 out;
-                out.x = e ? yf0 : ys;
-                out.y = e ? ys : yf0;
+                out.x = eS ? yf0 : ys;
+                out.y = eS ? ys : yf0;
                 *reinterpret_cast<float2*>(xout + (sz * t + cb)) = out;
             }
-
-            // Rotate the column.
-            amf = make_float2(P0.a.r0().w, P0.a.r1().w);
-            P0.x = P1.x;
-            P0.a = P1.a;
-            P0.b = P1.b;
-            P1.x = x2;
-            P1.a = Q1.a;
-            P1.b = Q1.b;
-            P1.xe = Q1.xe;
-            P1.ue = Q1.ue;
-            x2 = qx1;
-            qx1 = qx2v;
-            Q1 = Q2;
             yfm = yf0;
             yf0 = yf1;
-            __syncthreads();
+            xs0 = xs1;
+            as0 = as1;
+            bs0 = bs1;
         }
     }
+    cpa_wait<0>();
 }
 
 // K9a: r = b - A x (FP32).
@@ -819,13 +860,14 @@ __device__ __forceinline__ unsigned bf_up(float v) {
     const unsigned t = u >> 16;
     return (v > 0.0f && (u & 0xffffu) != 0u) ? t + 1u : t;
 }
-__global__ void k_rows_to_bf16(const float4* __restrict__ A,
-                               uint2* __restrict__ Ah, long N) {
+__global__ void k_rows_to_bf16(const float* __restrict__ A,
+                               unsigned short* __restrict__ Ah, long N) {
     for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < N;
          c += (long)gridDim.x * blockDim.x) {
-        const float4 r = A[c];
-        Ah[c] = make_uint2(bf_up(r.x) | (bf_trunc(r.y) << 16),
-                           bf_trunc(r.z) | (bf_trunc(r.w) << 16));
+        Ah[c] = (unsigned short)bf_up(A[c]);
+        Ah[N + c] = (unsigned short)bf_trunc(A[N + c]);
+        Ah[2 * N + c] = (unsigned short)bf_trunc(A[2 * N + c]);
+        Ah[3 * N + c] = (unsigned short)bf_trunc(A[3 * N + c]);
     }
 }
 
@@ -835,8 +877,8 @@ bool mixed(const Ctx* c) {
 // Calls f with the V-cycle rows of level L: BF16 in mixed mode, else FP32.
 template <typename F>
 void with_rows(const Ctx* c, const Level& L, F&& f) {
-    if (mixed(c)) f(RowsB{L.Ah});
-    else f(RowsF{L.A});
+    if (mixed(c)) f(RowsB{L.Ah, L.n.count()});
+    else f(RowsF{L.A, L.n.count()});
 }
 // Bytes per cell of a stored V-cycle row.
 double row_bytes(const Ctx* c) { return mixed(c) ? 8.0 : 16.0; }
@@ -866,31 +908,49 @@ bool fused_ok(const Level& L) {
 }
 
 // Launch shape of the fused sweep: a persistent grid of at most the resident
-// block count, and the slab depth kz (planes per work item) that minimises
-// the makespan in planes, rounds x (kz + 2 warm-up planes).
+// block count, with at least 8 planes of work per block so the warm-up of a
+// column segment stays small.
 struct ColLaunch {
-    int grid, tiles_x, tiles, kz, items;
+    int grid, tiles_x;
+    long total, per_block;
 };
 ColLaunch col_launch(const Ctx* c, const Level& L) {
     ColLaunch r;
     r.tiles_x = (L.n.x + col::TCX - 1) / col::TCX;
-    r.tiles = r.tiles_x * ((L.n.y + col::TY - 1) / col::TY);
-    const long G = (long)c->num_sms * c->col_blocks_per_sm;
-    long best = -1;
-    r.kz = L.n.z;
-    for (int kz = 4; kz <= 64; ++kz) {
-        const long slabs = (L.n.z + kz - 1) / kz;
-        const long items = slabs * r.tiles;
-        const long rounds = (items + G - 1) / G;
-        const long span = rounds * (kz + 2);
-        if (best < 0 || span < best) {
-            best = span;
-            r.kz = kz;
-        }
-        if (kz >= L.n.z) break;
+    const long tiles = (long)r.tiles_x * ((L.n.y + col::TY - 1) / col::TY);
+    r.total = tiles * L.n.z;
+    long g = (long)c->num_sms * c->col_blocks_per_sm[mixed(c) ? 1 : 0];
+    const long by_work = (r.total + 7) / 8;
+    if (g > by_work) g = by_work;
+    if (g < 1) g = 1;
+    // Blocks that hold neighbouring tiles should stage the same plane at the
+    // same time: the ring rows and the partial lines at a tile's i-edges are
+    // then read from L2, where the neighbour just brought them. When every
+    // tile fits in one wave, each tile's column is split into m equal
+    // segments (m = resident blocks / tiles), one per block, all marching in
+    // lock-step.
+    if (tiles <= g) {
+        const long m = g / tiles;
+        r.per_block = (L.n.z + m - 1) / m;
+        r.grid = (int)((r.total + r.per_block - 1) / r.per_block);
+        return r;
     }
-    r.items = (int)(((L.n.z + r.kz - 1) / r.kz) * r.tiles);
-    r.grid = (int)std::min<long>(G, r.items);
+    // Otherwise, among range lengths up to 15% above the even split, take
+    // the one that keeps j-neighbouring tiles (tiles_x * nz items apart in
+    // the work list) nearest to the same plane.
+    const long p0 = (r.total + g - 1) / g;
+    const long stride = (long)r.tiles_x * L.n.z;
+    long best = p0, bestd = -1;
+    for (long p = p0; p <= p0 + p0 / 7 + 1; ++p) {
+        const long off = stride % p;
+        const long d = std::min(off, p - off);
+        if (bestd < 0 || d < bestd) {
+            bestd = d;
+            best = p;
+        }
+    }
+    r.per_block = best;
+    r.grid = (int)((r.total + r.per_block - 1) / r.per_block);
     return r;
 }
 
@@ -916,17 +976,18 @@ float* smooth(Ctx* c, const Level& L, const float* b, float* x, float* alt,
                     ((z0 ? 8.0 : 12.0) + row_bytes(c)) * L.n.count());
             with_rows(c, L, [&](auto M) {
                 using R = decltype(M);
+                constexpr size_t smem = sizeof(ColSmem<R>);
                 if (z0)
                     k_rb_sweep_col<true, R>
-                        <<<cl.grid, col::BLOCK, 0, c->stream>>>(
+                        <<<cl.grid, col::BLOCK, smem, c->stream>>>(
                             M, b, nullptr, oth, L.n, first,
-                            (float)c->cfg.sor, cl.tiles_x, cl.tiles, cl.kz,
-                            cl.items);
+                            (float)c->cfg.sor, cl.tiles_x, cl.total,
+                            cl.per_block);
                 else
                     k_rb_sweep_col<false, R>
-                        <<<cl.grid, col::BLOCK, 0, c->stream>>>(
+                        <<<cl.grid, col::BLOCK, smem, c->stream>>>(
                             M, b, cur, oth, L.n, first, (float)c->cfg.sor,
-                            cl.tiles_x, cl.tiles, cl.kz, cl.items);
+                            cl.tiles_x, cl.total, cl.per_block);
             });
             std::swap(cur, oth);
         }
@@ -1038,17 +1099,30 @@ jetgpu_status prepare_levels(Ctx* c) {
 }
 
 jetgpu_status init_kernels(Ctx* c) {
+    const size_t smf = sizeof(ColSmem<RowsF>), smb = sizeof(ColSmem<RowsB>);
+    JG_CUDA(c, cudaFuncSetAttribute(k_rb_sweep_col<true, RowsF>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)smf));
+    JG_CUDA(c, cudaFuncSetAttribute(k_rb_sweep_col<false, RowsF>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)smf));
+    JG_CUDA(c, cudaFuncSetAttribute(k_rb_sweep_col<true, RowsB>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)smb));
+    JG_CUDA(c, cudaFuncSetAttribute(k_rb_sweep_col<false, RowsB>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    (int)smb));
     int occ[4] = {0, 0, 0, 0};
     JG_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                   &occ[0], k_rb_sweep_col<true, RowsF>, col::BLOCK, 0));
+                   &occ[0], k_rb_sweep_col<true, RowsF>, col::BLOCK, smf));
     JG_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                   &occ[1], k_rb_sweep_col<false, RowsF>, col::BLOCK, 0));
+                   &occ[1], k_rb_sweep_col<false, RowsF>, col::BLOCK, smf));
     JG_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                   &occ[2], k_rb_sweep_col<true, RowsB>, col::BLOCK, 0));
+                   &occ[2], k_rb_sweep_col<true, RowsB>, col::BLOCK, smb));
     JG_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                   &occ[3], k_rb_sweep_col<false, RowsB>, col::BLOCK, 0));
-    c->col_blocks_per_sm =
-        std::max(1, std::min(std::min(occ[0], occ[1]), std::min(occ[2], occ[3])));
+                   &occ[3], k_rb_sweep_col<false, RowsB>, col::BLOCK, smb));
+    c->col_blocks_per_sm[0] = std::max(1, std::min(occ[0], occ[1]));
+    c->col_blocks_per_sm[1] = std::max(1, std::min(occ[2], occ[3]));
     return JETGPU_OK;
 }
 
@@ -1059,7 +1133,7 @@ static jetgpu_status pcg_f32(Ctx* c, double target, unsigned max_it,
     const Level& L0 = c->levels[0];
     const Dims n = L0.n;
     const long N = n.count();
-    RowsF M{L0.A};
+    RowsF M{L0.A, N};
     k_init_scalars<<<1, 32, 0, c->stream>>>(c->scal);
     unsigned it = 0;
     double rr = 0;
@@ -1227,7 +1301,7 @@ static jetgpu_status fpcg_f32(Ctx* c, double target, unsigned max_it,
     const Level& L0 = c->levels[0];
     const Dims n = L0.n;
     const long N = n.count();
-    RowsF M{L0.A};
+    RowsF M{L0.A, N};
     *stalled = false;
     k_init_scalars<<<1, 32, 0, c->stream>>>(c->scal);
     k_zero<float><<<grid_for(c, N), kThreads, 0, c->stream>>>(c->kz2, N);
@@ -1300,7 +1374,7 @@ jetgpu_status harvest_pairs(Ctx* c, unsigned max_pairs, float* r_out,
     const Level& L0 = c->levels[0];
     const Dims n = L0.n;
     const long N = n.count();
-    RowsF M{L0.A};
+    RowsF M{L0.A, N};
     // r = b (x = 0), FP32 image.
     k_zero<double><<<grid_for(c, N), kThreads, 0, c->stream>>>(c->x64, N);
     k_residual64<<<rgrid(c, k_residual64, N), kThreads, 0,
@@ -1404,7 +1478,8 @@ jetgpu_status mgpcg_solve(Ctx* c, jetgpu_solve_stats* st) {
             Prof pr(c, K_RESIDUAL64, 56.0 * N);
             k_residual_df<<<rgrid(c, k_residual_df, N), kThreads, 0,
             c->stream>>>(
-                L0.A, c->Alo, c->xdf, c->bdf, r32, zero32, n, c->partials,
+                RowsF{L0.A, N}, c->Alo, c->xdf, c->bdf, r32, zero32, n,
+                c->partials,
                 c->counters, c->scal, S_R64);
         }
         JG_CUDA(c, cudaGetLastError());

@@ -3,8 +3,10 @@ kernels of libjetgpu.
 
 The network maps the 16 input channels libjetgpu builds for a residual r
 (``jetgpu_net_features``: r / rms(r), the six face weights of each cell,
-fluid indicator, scaled diagonal) to z / (rms(r) h^2), where z = M r is the
-multigrid V-cycle's correction. Pairs (r_k, z_k) come from the solver's own
+fluid indicator, scaled diagonal) to NET_GAIN * z / rms(r), where z = M r is
+the multigrid V-cycle's correction. For the smooth modes that dominate a
+preconditioned residual z is about r / (3 pi^2) at any grid spacing, so the
+target is O(1) and independent of the resolution. Pairs (r_k, z_k) come from the solver's own
 MGPCG iterations (``jetgpu_harvest``). Every convolution of the forward and
 backward passes runs on libjetgpu's tcgen05 kernels (``jetgpu_conv3d`` and
 ``jetgpu_conv3d_wgrad``); PyTorch supplies device memory, the optimizer and
@@ -29,6 +31,8 @@ LAYERS = [(16, 16, 1), (16, 16, 1), (16, 32, 1), (32, 32, 1), (32, 48, 1),
           (48, 48, 1), (48, 64, 1), (64, 64, 1), (112, 48, 1), (48, 48, 1),
           (80, 32, 1), (32, 32, 1), (48, 16, 1), (16, 16, 0)]
 
+NET_GAIN = 32.0  # kNetGain in unet.cu
+
 WEIGHTS = os.path.join(os.path.dirname(os.path.abspath(__file__)), "weights",
                        "unet_pressure.npz")
 
@@ -43,7 +47,7 @@ def init_params(seed: int = 0):
     for l, (ci, co, _) in enumerate(LAYERS):
         std = np.sqrt(2.0 / (27 * ci))
         if l == len(LAYERS) - 1:
-            std *= 0.1
+            std *= 0.01  # start near z = 0: a large initial loss kills ReLUs
         params.append((rng.standard_normal((27, co, ci)).astype(np.float32) * std,
                        np.zeros(co, np.float32)))
     return params
@@ -219,7 +223,7 @@ def harvest(solver: FdmMgpcgSolver3, sc: dict, n: int, pairs: int):
         rms = torch.sqrt(torch.mean(R[k].double() ** 2)).float()
         if rms <= 0:
             continue
-        target = (Z[k] / (rms * h * h)).reshape(n, n, n)
+        target = (Z[k] * (NET_GAIN / rms)).reshape(n, n, n)
         mask = feat[..., 7].float()
         samples.append((feat, target, mask))
     del fluid
@@ -255,8 +259,12 @@ def train(n: int = 64, scenes_count: int = 24, pairs: int = 6,
     P = [(torch.tensor(w, device=dev, requires_grad=True),
           torch.tensor(b, device=dev, requires_grad=True))
          for w, b in init_params(seed)]
-    opt = torch.optim.Adam([t for p in P for t in p], lr=lr)
-    sched = torch.optim.lr_scheduler.CosineAnnealingLR(opt, steps)
+    flat_params = [t for p in P for t in p]
+    opt = torch.optim.Adam(flat_params, lr=lr)
+    warm = max(1, min(200, steps // 10))
+    sched = torch.optim.lr_scheduler.LambdaLR(
+        opt, lambda s: min(1.0, (s + 1) / warm) *
+        0.5 * (1.0 + np.cos(np.pi * min(s, steps) / steps)))
     rng = np.random.default_rng(seed)
     hist = []
     for step in range(steps):
@@ -266,6 +274,7 @@ def train(n: int = 64, scenes_count: int = 24, pairs: int = 6,
         loss = (err * err).sum() / ((target * mask) ** 2).sum().clamp_min(1e-30)
         opt.zero_grad()
         loss.backward()
+        torch.nn.utils.clip_grad_norm_(flat_params, 1.0)
         opt.step()
         sched.step()
         hist.append(float(loss.detach()))
