@@ -34,6 +34,7 @@ enum Scalar : int {
     S_R64 = 5,     // ||b - A x||^2 (FP64 true residual)
     S_MEAN = 6,    // sum used for mean removal
     S_AUX = 7,
+    S_WAIT = 15,   // set to 1 by a kernel whose bounded stage wait ran out
     S_COUNT = 16
 };
 

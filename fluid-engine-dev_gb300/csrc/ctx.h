@@ -89,7 +89,8 @@ struct Ctx {
     jetgpu_config cfg;
     int device = 0;
     int num_sms = 0;
-    int col_blocks_per_sm[2] = {1, 1};  // fused sweep blocks/SM: FP32, BF16 rows
+    int tma_blocks_per_sm[2] = {0, 0};  // fused sweep blocks/SM, FP32 / BF16
+                                        // rows (0: not usable on this device)
     std::unordered_map<const void*, int> occupancy;  // blocks/SM per kernel
     cudaStream_t stream = nullptr;
     std::string err;

@@ -27,10 +27,11 @@
 //     from zero, so it is a fixed SPD preconditioner for CG.
 
 #include "ctx.h"
+#include "sweep_tma.cuh"
 
 #include <algorithm>
-#include <chrono>
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 
 namespace jg {
@@ -330,13 +331,6 @@ __global__ void k_df_to_f64(const float2* __restrict__ x,
     }
 }
 
-// x64 += e (FP32 correction).
-__global__ void k_accumulate(double* __restrict__ x, const float* __restrict__ e,
-                             long N) {
-    for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < N;
-         c += (long)gridDim.x * blockDim.x)
-        x[c] += (double)e[c];
-}
 
 // ||v||^2 (FP64).
 __global__ void __launch_bounds__(kThreads)
@@ -415,284 +409,6 @@ __global__ void __launch_bounds__(kThreads)
             x[c] = (1.0f - omega) * x[c] + omega * (b[c] - s) / r.x;
         }
     }
-}
-
-// K8 (fused): one full red-black SOR sweep in a single pass over memory.
-//
-// A block owns a tile of 32 cell pairs (64 cells) in i by 8 rows in j and
-// marches through k; each thread owns one pair (cells 2m, 2m+1 of a row).
-// At every plane a pair holds one cell of each colour, and the cells
-// directly below and above a cell have the other colour, so a thread's
-// column neighbours are its own pair one plane away. Planes of x, of the
-// four row components (structure of arrays) and of b are staged into
-// shared-memory rings by cp.async, two planes ahead of their first use, each
-// thread copying its own pair (zero-filled outside the domain); every read
-// then is a conflict-free word of a consecutive-pair array. Step t of the
-// march
-//   (1) updates the first colour F of plane t+1 from old values, on the tile
-//       plus a one-pair / one-row ring (ring rows also stage x of the row
-//       beyond, which their update reads),
-//   (2) updates the second colour S of plane t from the new F values of
-//       planes t-1, t, t+1 (the thread's own results of the previous, this
-//       and the next plane, and the neighbours' from shared memory) and
-//       writes both colours of plane t as one float2.
-// x is read from `xin` and written to `xout` (ping-pong), so blocks never
-// observe each other's updates: the result is exactly the sequential
-// red-then-black sweep, deterministic, with no inter-block synchronisation.
-// Outside the domain x = 0 and the rows are zero, which reproduces the
-// reference's guarded neighbour terms (FdmBlas3::mvm,
-// fdm_linear_system3.cpp:79-96). The grid is persistent: each block walks a
-// contiguous range of the (tile, plane) work list. HBM traffic per sweep: x, b and the rows read once,
-// x written once — 12 B/cell plus 16 (FP32) or 8 (BF16) B/cell of rows —
-// plus ring re-reads, mostly from L2. Requires an even nx.
-namespace col {
-constexpr int TXP = 32;            // pairs per tile row (64 cells)
-constexpr int TY = 8;              // rows per tile
-constexpr int PX = TXP + 2;        // pairs per row including the ring
-constexpr int PY = TY + 2;         // rows including the ring
-constexpr int NW = PX * PY;        // working threads (340)
-constexpr int BLOCK = 352;         // 11 warps
-constexpr int TCX = 2 * TXP;       // tile width in cells
-constexpr int XR = 5, AR = 5, BR = 4;  // ring depths in planes
-constexpr int XROWS = PY + 2;      // x rows -2 .. TY+1
-constexpr int UROWS = PY + 1;      // "up" rows -2 .. TY
-}  // namespace col
-
-template <int BYTES>
-__device__ __forceinline__ void cpa(void* smem, const void* gmem, bool valid) {
-    const unsigned sa = (unsigned)__cvta_generic_to_shared(smem);
-    asm volatile("cp.async.ca.shared.global [%0], [%1], %2, %3;\n" ::"r"(sa),
-                 "l"(gmem), "n"(BYTES), "r"(valid ? BYTES : 0));
-}
-__device__ __forceinline__ void cpa_commit() {
-    asm volatile("cp.async.commit_group;\n" ::);
-}
-template <int N>
-__device__ __forceinline__ void cpa_wait() {
-    asm volatile("cp.async.wait_group %0;\n" ::"n"(N));
-}
-
-// Storage of one row component in shared memory: FP32, or BF16 kept as its
-// 16 bits (decoded with a shift). Staged per pair (8 or 4 bytes).
-template <typename R> struct ColTraits;
-template <> struct ColTraits<RowsF> {
-    using E = float;
-    static constexpr int bytes = 8;
-    __device__ static float get(const E* p) { return *p; }
-    __device__ static const void* src(const RowsF& M, int k, long idx) {
-        return M.A + k * M.N + idx;
-    }
-};
-template <> struct ColTraits<RowsB> {
-    using E = unsigned short;
-    static constexpr int bytes = 4;
-    __device__ static float get(const E* p) {
-        return __uint_as_float((unsigned)*p << 16);
-    }
-    __device__ static const void* src(const RowsB& M, int k, long idx) {
-        return M.A + k * M.N + idx;
-    }
-};
-
-// Shared-memory rings. Every row is a flat run of CW = 2 * PX cells (the
-// tile's 64 cells plus one ring pair each side), so a cell's in-row
-// neighbours are the adjacent elements and its j-neighbours the same
-// element of the adjacent rows.
-namespace col {
-constexpr int CW = 2 * PX;  // cells per staged row (68)
-}
-template <typename R>
-struct ColSmem {
-    using E = typename ColTraits<R>::E;
-    float x[col::XR][col::XROWS][col::CW];
-    E c[col::AR][col::PY][col::CW];
-    E r[col::AR][col::PY][col::CW];
-    E f[col::AR][col::PY][col::CW];
-    E u[col::AR][col::UROWS][col::CW];
-    float b[col::BR][col::PY][col::CW];
-    float yf[2][col::PY][col::CW];  // new first-colour values, by plane parity
-};
-
-template <bool ZERO, typename R>
-__global__ void __launch_bounds__(col::BLOCK, 2)
-    k_rb_sweep_col(R M, const float* __restrict__ b,
-                   const float* __restrict__ xin, float* __restrict__ xout,
-                   Dims n, int first, float omega, int tiles_x,
-                   long total, long per_block) {
-    using namespace col;
-    using T = ColTraits<R>;
-    extern __shared__ __align__(16) unsigned char smem_raw[];
-    ColSmem<R>& S = *reinterpret_cast<ColSmem<R>*>(smem_raw);
-    const int tid = threadIdx.x;
-    const bool worker = tid < NW;
-    const int py = worker ? tid / PX : 0;  // tile row py - 1
-    const int px = worker ? tid - py * PX : 0;
-    const int sz = n.x * n.y;  // grids hold < 2^31 cells
-    const bool ring_lo = worker && py == 0, ring_hi = worker && py == PY - 1;
-    const bool interior = worker && px > 0 && px < PX - 1 && py > 0 &&
-                          py < PY - 1;
-    auto slot = [](int p, int D) { return ((p % D) + D) % D; };
-    if (ZERO) {  // x = 0 everywhere: the x ring is zeroed once, never staged
-        float* xs = &S.x[0][0][0];
-        for (int q = tid; q < XR * XROWS * CW; q += BLOCK) xs[q] = 0.f;
-    }
-
-    // This block's contiguous range of the (tile, plane) work list, in
-    // segments of consecutive planes of one tile.
-    long w = (long)blockIdx.x * per_block;
-    const long wend = min(total, w + per_block);
-    while (w < wend) {
-        const int tile = (int)(w / n.z);
-        const int k0 = (int)(w - (long)tile * n.z);
-        const int k1 = (int)min((long)n.z, k0 + (wend - w));
-        w += k1 - k0;
-        const int i0 = (tile % tiles_x) * TCX;
-        const int j0 = (tile / tiles_x) * TY;
-        const int gi = i0 + 2 * (px - 1);
-        const int gj = j0 + py - 1;
-        const bool colv = worker && gi >= 0 && gi < n.x && gj >= 0 && gj < n.y;
-        const int ej = ring_lo ? gj - 1 : gj + 1;
-        const bool exv = (ring_lo || ring_hi) && gi >= 0 && gi < n.x &&
-                         ej >= 0 && ej < n.y;
-        const int cb = colv ? gi + n.x * gj : 0;
-        const int eb = exv ? gi + n.x * ej : 0;
-
-        // Stage x of plane p (own row, plus the row beyond for ring rows).
-        const int pc = 2 * px;  // this pair's first cell in a staged row
-        auto stage_x = [&](int p) {
-            if (ZERO || !worker) return;
-            const bool pin = p >= 0 && p < n.z;
-            const int sl = slot(p, XR);
-            const int off = pin ? sz * p : 0;
-            cpa<8>(&S.x[sl][py + 1][pc], xin + (colv && pin ? off + cb : 0),
-                   colv && pin);
-            if (ring_lo)
-                cpa<8>(&S.x[sl][0][pc], xin + (exv && pin ? off + eb : 0),
-                       exv && pin);
-            if (ring_hi)
-                cpa<8>(&S.x[sl][PY + 1][pc], xin + (exv && pin ? off + eb : 0),
-                       exv && pin);
-        };
-        // Stage the row components and b of plane p.
-        auto stage_ab = [&](int p) {
-            if (!worker) return;
-            const bool pin = p >= 0 && p < n.z;
-            const int sa = slot(p, AR), sb = slot(p, BR);
-            const long off = pin ? (long)sz * p : 0;
-            const bool v = colv && pin;
-            const long idx = v ? off + cb : 0;
-            cpa<T::bytes>(&S.c[sa][py][pc], T::src(M, 0, idx), v);
-            cpa<T::bytes>(&S.r[sa][py][pc], T::src(M, 1, idx), v);
-            cpa<T::bytes>(&S.u[sa][py + 1][pc], T::src(M, 2, idx), v);
-            cpa<T::bytes>(&S.f[sa][py][pc], T::src(M, 3, idx), v);
-            if (ring_lo) {
-                const bool ve = exv && pin;
-                cpa<T::bytes>(&S.u[sa][0][pc], T::src(M, 2, ve ? off + eb : 0),
-                              ve);
-            }
-            cpa<8>(&S.b[sb][py][pc], b + idx, v);
-        };
-
-        __syncthreads();  // the previous segment's reads of the rings are done
-        const int t0 = k0 - 2;
-        stage_x(t0);
-        stage_x(t0 + 1);
-        stage_x(t0 + 2);
-        stage_ab(t0 - 1);
-        stage_ab(t0);
-        stage_ab(t0 + 1);
-        cpa_commit();
-        stage_x(t0 + 3);
-        stage_ab(t0 + 2);
-        cpa_commit();
-        float yfm = 0.f, yf0 = 0.f;  // own F results of planes t-1, t
-
-        // Ring slots of the planes step t touches, advanced once per step.
-        int xs0 = slot(t0, XR), as0 = slot(t0, AR), bs0 = slot(t0, BR);
-        auto nx = [](int q, int D) { return q + 1 == D ? 0 : q + 1; };
-        auto pv = [](int q, int D) { return q == 0 ? D - 1 : q - 1; };
-        for (int t = t0; t < k1; ++t) {
-            cpa_wait<1>();
-            __syncthreads();
-            // Two planes ahead: x of t+4, rows and b of t+3 (the slots of
-            // planes the previous step was the last to read).
-            if (t + 4 <= k1 + 1) stage_x(t + 4);
-            if (t + 3 <= k1) stage_ab(t + 3);
-            cpa_commit();
-            const int xs1 = nx(xs0, XR), xs2 = nx(xs1, XR);
-            const int as1 = nx(as0, AR), asm1 = pv(as0, AR);
-            const int bs1 = nx(bs0, BR);
-
-            // (1) First colour of plane t+1 at staged cell cf of this pair.
-            const int p1 = t + 1;
-            float yf1 = 0.f;
-            const int eF1 = (first + gj + p1) & 1;
-            const int cf = pc + eF1;
-            if (colv && p1 >= 0 && p1 < n.z) {
-                const bool skip = (px == 0 && eF1 == 0) || (px == PX - 1 && eF1 == 1);
-                if (!skip) {
-                    const float* xr1 = &S.x[xs1][py + 1][cf];
-                    const float xold = xr1[0];
-                    const float xl = xr1[-1];
-                    const float xr = xr1[1];
-                    const float xd = S.x[xs1][py][cf];
-                    const float xu = S.x[xs1][py + 2][cf];
-                    const float xb = S.x[xs0][py + 1][cf];
-                    const float xf = S.x[xs2][py + 1][cf];
-                    const auto* rr = &S.r[as1][py][cf];
-                    const float center = T::get(&S.c[as1][py][cf]);
-                    const float right = T::get(rr);
-                    const float cl = T::get(rr - 1);
-                    const float up = T::get(&S.u[as1][py + 1][cf]);
-                    const float cd = T::get(&S.u[as1][py][cf]);
-                    const float front = T::get(&S.f[as1][py][cf]);
-                    const float cbk = T::get(&S.f[as0][py][cf]);
-                    const float bb = S.b[bs1][py][cf];
-                    const float acc = cl * xl + right * xr + cd * xd + up * xu +
-                                      cbk * xb + front * xf;
-                    yf1 = (1.0f - omega) * xold +
-                          omega * __fdividef(bb - acc, center);
-                }
-            }
-            if (worker) S.yf[p1 & 1][py][cf] = yf1;
-
-            // (2) Second colour of plane t at staged cell cs; write plane t.
-            if (interior && colv && t >= k0) {
-                // The S cell of plane t sits under the F cell of plane t+1.
-                const int eS = eF1;
-                const int cs0 = cf;
-                const float* yr0 = &S.yf[t & 1][py][cs0];
-                const auto* rr = &S.r[as0][py][cs0];
-                const float center = T::get(&S.c[as0][py][cs0]);
-                const float right = T::get(rr);
-                const float cl = T::get(rr - 1);
-                const float up = T::get(&S.u[as0][py + 1][cs0]);
-                const float cd = T::get(&S.u[as0][py][cs0]);
-                const float front = T::get(&S.f[as0][py][cs0]);
-                const float cbk = T::get(&S.f[asm1][py][cs0]);
-                const float bb = S.b[bs0][py][cs0];
-                const float xold = S.x[xs0][py + 1][cs0];
-                const float yl = yr0[-1];
-                const float yr = yr0[1];
-                const float yd = S.yf[t & 1][py - 1][cs0];
-                const float yu = S.yf[t & 1][py + 1][cs0];
-                const float acc = cl * yl + right * yr + cd * yd + up * yu +
-                                  cbk * yfm + front * yf1;
-                const float ys = (1.0f - omega) * xold +
-                                 omega * __fdividef(bb - acc, center);
-                float2 out;
-                out.x = eS ? yf0 : ys;
-                out.y = eS ? ys : yf0;
-                *reinterpret_cast<float2*>(xout + (sz * t + cb)) = out;
-            }
-            yfm = yf0;
-            yf0 = yf1;
-            xs0 = xs1;
-            as0 = as1;
-            bs0 = bs1;
-        }
-    }
-    cpa_wait<0>();
 }
 
 // K9a: r = b - A x (FP32).
@@ -903,10 +619,6 @@ void rb_half(Ctx* c, const Level& L, const float* b, float* x, int color,
     });
 }
 
-bool fused_ok(const Level& L) {
-    return L.n.x % 2 == 0 && L.n.x >= 64 && L.n.y >= 4 && L.n.z >= 2;
-}
-
 // Launch shape of the fused sweep: a persistent grid of at most the resident
 // block count, with at least 8 planes of work per block so the warm-up of a
 // column segment stays small.
@@ -914,12 +626,13 @@ struct ColLaunch {
     int grid, tiles_x;
     long total, per_block;
 };
-ColLaunch col_launch(const Ctx* c, const Level& L) {
+ColLaunch col_launch(const Ctx* c, const Level& L, int tcx, int ty,
+                     int blocks_per_sm) {
     ColLaunch r;
-    r.tiles_x = (L.n.x + col::TCX - 1) / col::TCX;
-    const long tiles = (long)r.tiles_x * ((L.n.y + col::TY - 1) / col::TY);
+    r.tiles_x = (L.n.x + tcx - 1) / tcx;
+    const long tiles = (long)r.tiles_x * ((L.n.y + ty - 1) / ty);
     r.total = tiles * L.n.z;
-    long g = (long)c->num_sms * c->col_blocks_per_sm[mixed(c) ? 1 : 0];
+    long g = (long)c->num_sms * blocks_per_sm;
     const long by_work = (r.total + 7) / 8;
     if (g > by_work) g = by_work;
     if (g < 1) g = 1;
@@ -954,6 +667,127 @@ ColLaunch col_launch(const Ctx* c, const Level& L) {
     return r;
 }
 
+// ---- TMA sweep (sweep_tma.cuh): tensor maps and launch --------------------
+
+// Row element and prefetch distance (planes) of the TMA sweep. Two planes
+// keep two blocks per SM with FP32 rows; deeper prefetch measured no faster.
+template <typename R> struct TmaCfg;
+template <> struct TmaCfg<RowsF> {
+    using E = float;
+    static constexpr int D = 2;
+};
+template <> struct TmaCfg<RowsB> {
+    using E = unsigned short;
+    static constexpr int D = 2;
+};
+
+PFN_cuTensorMapEncodeTiled_v12000 tma_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p,
+                                             12000, cudaEnableDefault,
+                                             &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            p = nullptr;
+        return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }();
+    return fn;
+}
+
+bool tma_ok(const Ctx* c, const Level& L) {
+    return c->tma_blocks_per_sm[mixed(c) ? 1 : 0] > 0 && L.n.x % 8 == 0 &&
+           L.n.x >= 64;
+}
+
+// Tiled map over `rank` dims (innermost first) of a dense array at p.
+bool encode_map(CUtensorMap* m, CUtensorMapDataType dt, int esize, int rank,
+                const void* p, const long* dims, const unsigned* box) {
+    cuuint64_t gd[4], gs[3];
+    cuuint32_t bx[4], es[4] = {1, 1, 1, 1};
+    long stride = esize;
+    for (int d = 0; d < rank; ++d) {
+        gd[d] = (cuuint64_t)dims[d];
+        bx[d] = box[d];
+        if (d > 0) gs[d - 1] = (cuuint64_t)stride;
+        stride *= dims[d];
+    }
+    return tma_encoder()(m, dt, (cuuint32_t)rank, const_cast<void*>(p), gd, gs,
+                         bx, es, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                         CU_TENSOR_MAP_SWIZZLE_NONE,
+                         CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                         CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// Tensor maps of one smoothing call: b, the rows, and the two ping-pong x
+// buffers (the sweeps alternate between them).
+struct TmaMaps {
+    CUtensorMap b, r, x[2];
+};
+
+template <typename R>
+bool tma_maps(TmaMaps* m, const R& M, const float* b, const float* x0,
+              const float* x1, Dims n) {
+    using E = typename TmaCfg<R>::E;
+    using Lt = tsw::Layout<E, TmaCfg<R>::D>;
+    const long d3[3] = {n.x, n.y, n.z};
+    const long d4[4] = {n.x, n.y, n.z, 4};
+    const unsigned bx[3] = {tsw::XW, tsw::XH, 1};
+    const unsigned bb[3] = {tsw::XW, tsw::BH, 1};
+    const unsigned br[4] = {Lt::RW, tsw::RH, 1, 4};
+    return encode_map(&m->b, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, 3, b, d3,
+                      bb) &&
+           encode_map(&m->r, tsw::Elem<E>::dtype, (int)sizeof(E), 4, M.A, d4,
+                      br) &&
+           encode_map(&m->x[0], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, 3, x0, d3,
+                      bx) &&
+           encode_map(&m->x[1], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, 3, x1, d3,
+                      bx);
+}
+
+// One TMA-staged fused sweep from x[src] (or from zero) into xout.
+template <typename R>
+void launch_tma(Ctx* c, const ColLaunch& cl, const TmaMaps& m, int src,
+                bool zero, float* xout, Dims n, int first) {
+    using E = typename TmaCfg<R>::E;
+    constexpr int D = TmaCfg<R>::D;
+    constexpr int smem = tsw::Layout<E, D>::TOTAL;
+    double* err = c->scal + S_WAIT;
+    if (zero)
+        tsw::k_rb_sweep_tma<true, E, D>
+            <<<cl.grid, tsw::BLOCK, smem, c->stream>>>(
+                m.b, m.r, m.b, xout, n, first, (float)c->cfg.sor, cl.tiles_x,
+                cl.total, cl.per_block, err);
+    else
+        tsw::k_rb_sweep_tma<false, E, D>
+            <<<cl.grid, tsw::BLOCK, smem, c->stream>>>(
+                m.x[src], m.r, m.b, xout, n, first, (float)c->cfg.sor,
+                cl.tiles_x, cl.total, cl.per_block, err);
+}
+
+// Shared-memory limit and resident blocks per SM of both TMA sweep variants
+// with rows R (0 when they cannot run).
+template <typename R>
+jetgpu_status tma_prepare(Ctx* c, int* blocks) {
+    using E = typename TmaCfg<R>::E;
+    constexpr int D = TmaCfg<R>::D;
+    const int smem = tsw::Layout<E, D>::TOTAL;
+    int occ[2] = {0, 0};
+    JG_CUDA(c, cudaFuncSetAttribute(tsw::k_rb_sweep_tma<true, E, D>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    smem));
+    JG_CUDA(c, cudaFuncSetAttribute(tsw::k_rb_sweep_tma<false, E, D>,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    smem));
+    JG_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                   &occ[0], tsw::k_rb_sweep_tma<true, E, D>, tsw::BLOCK, smem));
+    JG_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                   &occ[1], tsw::k_rb_sweep_tma<false, E, D>, tsw::BLOCK, smem));
+    *blocks = tma_encoder() ? std::min(occ[0], occ[1]) : 0;
+    return JETGPU_OK;
+}
+
+
 // `sweeps` red-black sweeps (colour order reversed when `reverse`) starting
 // from x = 0 when `zero`, else from *x. Levels the fused kernel serves
 // ping-pong between x and alt; the return value holds the result.
@@ -966,32 +800,28 @@ float* smooth(Ctx* c, const Level& L, const float* b, float* x, float* alt,
                             c->stream>>>(x, L.n.count());
         return x;
     }
-    if (alt != nullptr && fused_ok(L)) {
-        const ColLaunch cl = col_launch(c, L);
-        float* cur = x;
-        float* oth = alt;
-        for (unsigned s = 0; s < sweeps; ++s) {
-            const bool z0 = zero && s == 0;
-            Prof pr(c, l == 0 ? K_SWEEP_L0 : K_SWEEP_COARSE,
-                    ((z0 ? 8.0 : 12.0) + row_bytes(c)) * L.n.count());
-            with_rows(c, L, [&](auto M) {
-                using R = decltype(M);
-                constexpr size_t smem = sizeof(ColSmem<R>);
-                if (z0)
-                    k_rb_sweep_col<true, R>
-                        <<<cl.grid, col::BLOCK, smem, c->stream>>>(
-                            M, b, nullptr, oth, L.n, first,
-                            (float)c->cfg.sor, cl.tiles_x, cl.total,
-                            cl.per_block);
-                else
-                    k_rb_sweep_col<false, R>
-                        <<<cl.grid, col::BLOCK, smem, c->stream>>>(
-                            M, b, cur, oth, L.n, first, (float)c->cfg.sor,
-                            cl.tiles_x, cl.total, cl.per_block);
-            });
-            std::swap(cur, oth);
-        }
-        return cur;
+    if (alt != nullptr && tma_ok(c, L)) {
+        const ColLaunch cl = col_launch(c, L, tsw::TX, tsw::TY,
+                                        c->tma_blocks_per_sm[mixed(c) ? 1 : 0]);
+        bool done = false;
+        float* out = x;
+        with_rows(c, L, [&](auto M) {
+            using R = decltype(M);
+            TmaMaps maps;
+            if (!tma_maps(&maps, M, b, x, alt, L.n)) return;  // half sweeps
+            float* buf[2] = {x, alt};
+            int cur = 0;
+            for (unsigned s = 0; s < sweeps; ++s) {
+                const bool z0 = zero && s == 0;
+                Prof pr(c, l == 0 ? K_SWEEP_L0 : K_SWEEP_COARSE,
+                        ((z0 ? 8.0 : 12.0) + row_bytes(c)) * L.n.count());
+                launch_tma<R>(c, cl, maps, cur, z0, buf[1 - cur], L.n, first);
+                cur = 1 - cur;
+            }
+            out = buf[cur];
+            done = true;
+        });
+        if (done) return out;
     }
     const int cls = l == 0 ? K_HALF_L0 : K_HALF_COARSE;
     for (unsigned s = 0; s < sweeps; ++s) {
@@ -1047,17 +877,17 @@ float* vcycle_level(Ctx* c, unsigned l, const float* b, float* x, float* alt) {
                   l == 0 ? cfg.final_iter : cfg.correct_iter, true, false, l);
 }
 
-double now_ms() {
-    using namespace std::chrono;
-    return duration<double, std::milli>(
-               steady_clock::now().time_since_epoch())
-        .count();
-}
-
 jetgpu_status read_scalars(Ctx* c) {
     JG_CUDA(c, cudaMemcpyAsync(c->h_scal, c->scal, S_COUNT * sizeof(double),
                                cudaMemcpyDeviceToHost, c->stream));
     JG_CUDA(c, cudaStreamSynchronize(c->stream));
+    if (c->h_scal[S_WAIT] != 0.0) {
+        JG_CUDA(c, cudaMemsetAsync(c->scal + S_WAIT, 0, sizeof(double),
+                                   c->stream));
+        c->err = "a shared-memory stage of the red-black sweep did not arrive "
+                 "within its wait limit";
+        return JETGPU_CUDA_ERROR;
+    }
     return JETGPU_OK;
 }
 
@@ -1099,30 +929,11 @@ jetgpu_status prepare_levels(Ctx* c) {
 }
 
 jetgpu_status init_kernels(Ctx* c) {
-    const size_t smf = sizeof(ColSmem<RowsF>), smb = sizeof(ColSmem<RowsB>);
-    JG_CUDA(c, cudaFuncSetAttribute(k_rb_sweep_col<true, RowsF>,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)smf));
-    JG_CUDA(c, cudaFuncSetAttribute(k_rb_sweep_col<false, RowsF>,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)smf));
-    JG_CUDA(c, cudaFuncSetAttribute(k_rb_sweep_col<true, RowsB>,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)smb));
-    JG_CUDA(c, cudaFuncSetAttribute(k_rb_sweep_col<false, RowsB>,
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                    (int)smb));
-    int occ[4] = {0, 0, 0, 0};
-    JG_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                   &occ[0], k_rb_sweep_col<true, RowsF>, col::BLOCK, smf));
-    JG_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                   &occ[1], k_rb_sweep_col<false, RowsF>, col::BLOCK, smf));
-    JG_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                   &occ[2], k_rb_sweep_col<true, RowsB>, col::BLOCK, smb));
-    JG_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                   &occ[3], k_rb_sweep_col<false, RowsB>, col::BLOCK, smb));
-    c->col_blocks_per_sm[0] = std::max(1, std::min(occ[0], occ[1]));
-    c->col_blocks_per_sm[1] = std::max(1, std::min(occ[2], occ[3]));
+    jetgpu_status st;
+    if ((st = tma_prepare<RowsF>(c, &c->tma_blocks_per_sm[0])) != JETGPU_OK)
+        return st;
+    if ((st = tma_prepare<RowsB>(c, &c->tma_blocks_per_sm[1])) != JETGPU_OK)
+        return st;
     return JETGPU_OK;
 }
 

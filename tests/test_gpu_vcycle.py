@@ -138,6 +138,8 @@ def scene(res, seed):
                          [((64, 64, 64), 1.0, 5, "fp32"),
                           ((96, 40, 48), 1.2, 6, "fp32"),
                           ((128, 128, 128), 1.0, 6, "fp32"),
+                          ((72, 36, 40), 1.2, 6, "fp32"),
+                          ((72, 36, 40), 1.0, 6, "mixed"),
                           ((96, 40, 48), 1.0, 6, "mixed"),
                           ((128, 128, 128), 1.0, 6, "mixed")])
 def test_vcycle_matches_numpy_model(res, sor, max_levels, precision):
