@@ -51,6 +51,9 @@ def parse_args():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=256)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--variants", default=",".join(VARIANTS),
+                    help="comma-separated solver variants to run "
+                         "(plain_mgpcg, mixed_mgpcg, learned_fpcg)")
     return ap.parse_args()
 
 
@@ -181,14 +184,14 @@ def peaks() -> dict:
     return {"hbm_gbs": 6800.0, "source": "fallback"}
 
 
-def traffic_per_launch(kernel: str, n: int):
-    """DRAM bytes per launch of `kernel` from the committed ncu summary
-    (profiles/traffic.json), scaled by cells to this resolution; None when
-    no capture covers the kernel."""
+def traffic_per_launch(kernel: str, variant: str, n: int):
+    """DRAM bytes per launch of `kernel` in solver `variant` from the
+    committed ncu summary (profiles/traffic.json), scaled by cells to this
+    resolution; None when no capture covers the kernel."""
     path = os.path.join(REPO, "profiles", "traffic.json")
     if not os.path.exists(path):
         return None
-    rec = json.load(open(path)).get(kernel)
+    rec = json.load(open(path)).get(kernel, {}).get(variant)
     if not rec:
         return None
     return rec["dram_bytes_per_launch"] * (n ** 3) / float(rec["cells"])
@@ -275,7 +278,9 @@ def run_ours(args, rank, world, local, pg):
 
     variants = {}
     results = {}
-    for name in VARIANTS:
+    for name in args.variants.split(","):
+        if name not in VARIANTS:
+            raise SystemExit(f"unknown variant {name!r}")
         solver = make_solver(name)
         if solver is None:
             variants[name] = {"status": "skipped: no trained weights"}
@@ -316,7 +321,7 @@ def run_ours(args, rank, world, local, pg):
     pk = peaks()
     achieved = (top["bytes"] / top["launches"]) / (
         top["total_ms"] / top["launches"] * 1e-3) / 1e9
-    traffic = traffic_per_launch(top["name"], n)
+    traffic = traffic_per_launch(top["name"], head, n)
     roofline = {
         "kernel": top["name"], "bound": "hbm",
         "achieved": round(achieved, 1), "peak": pk["hbm_gbs"],
