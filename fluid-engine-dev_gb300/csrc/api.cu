@@ -357,6 +357,8 @@ void jetgpu_destroy(jetgpu_ctx* c) {
     release(&c->counters);
     release(&c->stage);
     release(&c->pscratch);
+    release(&c->bc_tmp);
+    release(&c->bc_valid);
     net_destroy(c->unet);
     c->unet = nullptr;
     if (c->h_scal) cudaFreeHost(c->h_scal);
@@ -798,6 +800,79 @@ jetgpu_status jetgpu_g2p_pic(jetgpu_ctx* c, const jetgpu_grid* grid, long np,
     return JETGPU_OK;
 }
 
+jetgpu_status jetgpu_constrain_velocity_device(
+    jetgpu_ctx* c, const jetgpu_grid* grid, double* u, double* v, double* w,
+    const jetgpu_scalar_field* sdf, const jetgpu_collider* col, int closed,
+    unsigned int depth) {
+    if (!c) return JETGPU_BAD_INPUT;
+    jetgpu_status s;
+    if ((s = check_grid(c, grid)) != JETGPU_OK) return s;
+    if ((s = check_field(c, sdf, "collider_sdf")) != JETGPU_OK) return s;
+    if (!u || !v || !w) return fail(c, JETGPU_BAD_INPUT, "null velocity arrays");
+    JG_CUDA(c, cudaSetDevice(c->device));
+    return constrain_velocity(c, to_desc(grid), u, v, w, to_desc(sdf, sdf->data),
+                              col, closed, depth);
+}
+
+jetgpu_status jetgpu_constrain_velocity(
+    jetgpu_ctx* c, const jetgpu_grid* grid, double* u, double* v, double* w,
+    const jetgpu_scalar_field* sdf, const jetgpu_collider* col, int closed,
+    unsigned int depth) {
+    if (!c) return JETGPU_BAD_INPUT;
+    jetgpu_status s;
+    if ((s = check_grid(c, grid)) != JETGPU_OK) return s;
+    if ((s = check_field(c, sdf, "collider_sdf")) != JETGPU_OK) return s;
+    if (!u || !v || !w) return fail(c, JETGPU_BAD_INPUT, "null velocity arrays");
+    JG_CUDA(c, cudaSetDevice(c->device));
+    size_t n[3];
+    face_counts(grid, n);
+    const size_t nf = n[0] + n[1] + n[2];
+    const size_t ns = (size_t)field_count(sdf);
+    s = grow_stage(c, (nf + ns) * 8 + 64);
+    if (s != JETGPU_OK) return s;
+    double* dg = reinterpret_cast<double*>(c->stage);
+    double* ds = dg + nf;
+    cudaStream_t st = c->stream;
+    double* io[3] = {u, v, w};
+    size_t off = 0;
+    for (int a = 0; a < 3; ++a) {
+        JG_CUDA(c, cudaMemcpyAsync(dg + off, io[a], n[a] * 8,
+                                   cudaMemcpyHostToDevice, st));
+        off += n[a];
+    }
+    if (ns)
+        JG_CUDA(c, cudaMemcpyAsync(ds, sdf->data, ns * 8,
+                                   cudaMemcpyHostToDevice, st));
+    s = constrain_velocity(c, to_desc(grid), dg, dg + n[0], dg + n[0] + n[1],
+                           to_desc(sdf, ns ? ds : nullptr), col, closed, depth);
+    if (s != JETGPU_OK) return s;
+    off = 0;
+    for (int a = 0; a < 3; ++a) {
+        JG_CUDA(c, cudaMemcpyAsync(io[a], dg + off, n[a] * 8,
+                                   cudaMemcpyDeviceToHost, st));
+        off += n[a];
+    }
+    JG_CUDA(c, cudaStreamSynchronize(st));
+    return JETGPU_OK;
+}
+
+jetgpu_status jetgpu_extrapolate_to_region_device(jetgpu_ctx* c,
+                                                  const int res[3],
+                                                  double* data,
+                                                  const unsigned char* valid,
+                                                  unsigned int iterations) {
+    if (!c) return JETGPU_BAD_INPUT;
+    if (!res || !data || !valid)
+        return fail(c, JETGPU_BAD_INPUT, "null argument");
+    for (int a = 0; a < 3; ++a)
+        if (res[a] < 1) return fail(c, JETGPU_BAD_INPUT, "resolution < 1");
+    if ((double)res[0] * res[1] * res[2] > 2147483647.0)
+        return fail(c, JETGPU_BAD_INPUT, "grid too large");
+    JG_CUDA(c, cudaSetDevice(c->device));
+    return extrapolate_region(c, Dims{res[0], res[1], res[2]}, data, valid,
+                              iterations);
+}
+
 }  // extern "C"
 
 // ---- live per-kernel profile -------------------------------------------------
@@ -811,7 +886,7 @@ const char* kernel_class_name(int cls) {
         "correct", "spmv_dot", "update_xr", "dot_rz", "update_d",
         "residual64", "accumulate", "weights", "pyramid", "system",
         "gradient", "p2g", "g2p",
-        "unet"};
+        "unet", "boundary"};
     return (cls >= 0 && cls < K_CLASS_COUNT) ? names[cls] : "?";
 }
 

@@ -1,0 +1,366 @@
+// Boundary conditions on the face-centred velocity (the first widening of
+// the pressure path: these run right after every projection and around the
+// particle transfers of a FLIP/PIC step).
+//
+// constrain_velocity replaces
+// GridFractionalBoundaryConditionSolver3::constrainVelocity
+// (src/jet/grid_fractional_boundary_condition_solver3.cpp:26-233):
+//   K19a  faces whose collider fraction 1 - fractionInsideSdf(phi(x - h/2),
+//         phi(x + h/2)) is 0 take the collider velocity and are marked
+//         invalid (:51-100);
+//   K19b  extrapolateToRegion from the valid faces, `depth` Jacobi passes
+//         (include/jet/detail/array_utils-inl.h:172-244; a pass writes only
+//         cells invalid at its start and reads only cells valid at its start,
+//         so it is order-independent and runs in place);
+//   K19c  faces inside the collider get the velocity sampled there projected
+//         onto the collider's tangent plane with friction
+//         (projectAndApplyFriction, src/jet/physics_helpers.h:34-45), the
+//         normal from the collider SDF's gradient (ScalarGrid3::gradient,
+//         src/jet/scalar_grid3.cpp:89-102, over gradient3,
+//         src/jet/fdm_utils.cpp:49-67), into a temporary (:110-175);
+//   K19d  copy back and zero the normal velocity on closed domain faces
+//         (:177-232).
+// The unit is built with -fmad=false and evaluates every expression in the
+// reference's order, so results are bit-identical to the reference.
+// Bound: HBM (K19a reads 16 B of SDF samples per face from L2-resident
+// neighbourhoods; K19b reads 7 values + validity per invalid face per pass).
+
+#include "ctx.h"
+#include "sampling.cuh"
+
+namespace jg {
+namespace {
+
+using namespace smp;
+
+struct ColliderDesc {
+    int present;
+    double lin[3], ang[3], centre[3];
+    double friction;
+};
+
+// RigidBodyCollider3::velocityAt (src/jet/rigid_body_collider3.cpp:25-28)
+// with Vector3::cross (include/jet/detail/vector3-inl.h:125-127).
+__device__ __forceinline__ void collider_vel(const ColliderDesc& c,
+                                             const double p[3], double o[3]) {
+    if (!c.present) {
+        o[0] = o[1] = o[2] = 0.0;
+        return;
+    }
+    const double r0 = p[0] - c.centre[0], r1 = p[1] - c.centre[1],
+                 r2 = p[2] - c.centre[2];
+    o[0] = c.lin[0] + (c.ang[1] * r2 - r1 * c.ang[2]);
+    o[1] = c.lin[1] + (c.ang[2] * r0 - r2 * c.ang[0]);
+    o[2] = c.lin[2] + (c.ang[0] * r1 - r0 * c.ang[1]);
+}
+
+// CellCenteredScalarGrid3::sample (LinearArraySampler3::operator()).
+__device__ double sample_sdf(const FieldDesc& F, double x, double y,
+                             double z) {
+    if (F.kind == 0) return F.value;
+    const Dims s{F.res[0], F.res[1], F.res[2]};
+    return sample_face<double, double>(F.data, s,
+                                       (x - F.origin[0]) / F.spacing[0],
+                                       (y - F.origin[1]) / F.spacing[1],
+                                       (z - F.origin[2]) / F.spacing[2]);
+}
+
+// std::max's rule (the first argument unless it is less than the second).
+__device__ __forceinline__ double dmax(double a, double b) {
+    return a < b ? b : a;
+}
+
+__device__ __forceinline__ double frac_inside_sdf(double p0, double p1) {
+    const bool i0 = p0 < 0.0, i1 = p1 < 0.0;
+    if (i0 && i1) return 1.0;
+    if (i0 && !i1) return p0 / (p0 - p1);
+    if (!i0 && i1) return p1 / (p1 - p0);
+    return 0.0;
+}
+
+__device__ __forceinline__ void face_pos(const FaceSet& fs, int a,
+                                         const double h[3], int i, int j,
+                                         int k, double p[3]) {
+    p[0] = fs.o[a][0] + h[0] * (double)i;
+    p[1] = fs.o[a][1] + h[1] * (double)j;
+    p[2] = fs.o[a][2] + h[2] * (double)k;
+}
+
+struct H3 {
+    double v[3];
+};
+
+// K19a
+__global__ void k_bc_mark(FaceSet fs, int a, H3 h, FieldDesc sdf,
+                          ColliderDesc col, double* __restrict__ vel,
+                          unsigned char* __restrict__ valid) {
+    const Dims s = fs.s[a];
+    const long n = s.count();
+    for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < n;
+         c += (long)gridDim.x * blockDim.x) {
+        int i, j, k;
+        cell_ijk(c, s, i, j, k);
+        double p[3], q0[3], q1[3];
+        face_pos(fs, a, h.v, i, j, k, p);
+        for (int d = 0; d < 3; ++d) {
+            const double off = d == a ? 0.5 * h.v[d] : 0.0;
+            q0[d] = p[d] - off;
+            q1[d] = p[d] + off;
+        }
+        double frac = frac_inside_sdf(sample_sdf(sdf, q0[0], q0[1], q0[2]),
+                                      sample_sdf(sdf, q1[0], q1[1], q1[2]));
+        frac = 1.0 - (frac < 0.0 ? 0.0 : (frac > 1.0 ? 1.0 : frac));
+        if (frac > 0.0) {
+            valid[c] = 1;
+        } else {
+            double cv[3];
+            collider_vel(col, p, cv);
+            vel[c] = cv[a];
+            valid[c] = 0;
+        }
+    }
+}
+
+// K19b: one extrapolation pass, in place on `data`.
+__global__ void k_extrapolate(Dims s, double* __restrict__ data,
+                              const unsigned char* __restrict__ v0,
+                              unsigned char* __restrict__ v1) {
+    const long n = s.count();
+    const long sy = s.x, sz = (long)s.x * s.y;
+    for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < n;
+         c += (long)gridDim.x * blockDim.x) {
+        if (v0[c]) {
+            v1[c] = 1;
+            continue;
+        }
+        int i, j, k;
+        cell_ijk(c, s, i, j, k);
+        double sum = 0.0;
+        unsigned count = 0;
+        if (i + 1 < s.x && v0[c + 1]) { sum += data[c + 1]; ++count; }
+        if (i > 0 && v0[c - 1]) { sum += data[c - 1]; ++count; }
+        if (j + 1 < s.y && v0[c + sy]) { sum += data[c + sy]; ++count; }
+        if (j > 0 && v0[c - sy]) { sum += data[c - sy]; ++count; }
+        if (k + 1 < s.z && v0[c + sz]) { sum += data[c + sz]; ++count; }
+        if (k > 0 && v0[c - sz]) { sum += data[c - sz]; ++count; }
+        if (count > 0) {
+            data[c] = sum / (double)count;
+            v1[c] = 1;
+        } else {
+            v1[c] = 0;
+        }
+    }
+}
+
+// ScalarGrid3::gradient at p: trilinear weights of the cell-centred sampler
+// (coordinates scaled by the inverse spacing, as getCoordinatesAndWeights
+// does) over the clamped central differences of gradient3.
+__device__ void sdf_gradient(const FieldDesc& F, const double inv[3],
+                             const double p[3], double g[3]) {
+    g[0] = g[1] = g[2] = 0.0;
+    if (F.kind == 0) return;
+    const Dims s{F.res[0], F.res[1], F.res[2]};
+    int i, j, k;
+    double fx, fy, fz;
+    bary<double>((p[0] - F.origin[0]) * inv[0], s.x - 1, &i, &fx);
+    bary<double>((p[1] - F.origin[1]) * inv[1], s.y - 1, &j, &fy);
+    bary<double>((p[2] - F.origin[2]) * inv[2], s.z - 1, &k, &fz);
+    const int ip1 = min(i + 1, s.x - 1), jp1 = min(j + 1, s.y - 1),
+              kp1 = min(k + 1, s.z - 1);
+    const int ci[8] = {i, ip1, i, ip1, i, ip1, i, ip1};
+    const int cj[8] = {j, j, jp1, jp1, j, j, jp1, jp1};
+    const int ck[8] = {k, k, k, k, kp1, kp1, kp1, kp1};
+    const double w[8] = {(1 - fx) * (1 - fy) * (1 - fz), fx * (1 - fy) * (1 - fz),
+                         (1 - fx) * fy * (1 - fz),       fx * fy * (1 - fz),
+                         (1 - fx) * (1 - fy) * fz,       fx * (1 - fy) * fz,
+                         (1 - fx) * fy * fz,             fx * fy * fz};
+    const double* d = F.data;
+#pragma unroll
+    for (int n = 0; n < 8; ++n) {
+        const int x = ci[n], y = cj[n], z = ck[n];
+        const double l = d[lin(x > 0 ? x - 1 : x, y, z, s.x, s.y)];
+        const double r = d[lin(x + 1 < s.x ? x + 1 : x, y, z, s.x, s.y)];
+        const double dn = d[lin(x, y > 0 ? y - 1 : y, z, s.x, s.y)];
+        const double up = d[lin(x, y + 1 < s.y ? y + 1 : y, z, s.x, s.y)];
+        const double bk = d[lin(x, y, z > 0 ? z - 1 : z, s.x, s.y)];
+        const double fr = d[lin(x, y, z + 1 < s.z ? z + 1 : z, s.x, s.y)];
+        const double gx = 0.5 * (r - l) / F.spacing[0];
+        const double gy = 0.5 * (up - dn) / F.spacing[1];
+        const double gz = 0.5 * (fr - bk) / F.spacing[2];
+        g[0] = g[0] + w[n] * gx;
+        g[1] = g[1] + w[n] * gy;
+        g[2] = g[2] + w[n] * gz;
+    }
+}
+
+// K19c
+__global__ void k_bc_project(FaceSet fs, int a, H3 h, H3 inv, FieldDesc sdf,
+                             ColliderDesc col, const double* __restrict__ u,
+                             const double* __restrict__ v,
+                             const double* __restrict__ w,
+                             double* __restrict__ tmp) {
+    const Dims s = fs.s[a];
+    const long n = s.count();
+    const double* vel[3] = {u, v, w};
+    for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < n;
+         c += (long)gridDim.x * blockDim.x) {
+        int i, j, k;
+        cell_ijk(c, s, i, j, k);
+        double p[3];
+        face_pos(fs, a, h.v, i, j, k, p);
+        if (!(sample_sdf(sdf, p[0], p[1], p[2]) < 0.0)) {
+            tmp[c] = vel[a][c];
+            continue;
+        }
+        double cv[3], fv[3], g[3];
+        collider_vel(col, p, cv);
+        for (int b = 0; b < 3; ++b)  // FaceCenteredGrid3::sample
+            fv[b] = sample_face<double, double>(vel[b], fs.s[b],
+                                                (p[0] - fs.o[b][0]) / h.v[0],
+                                                (p[1] - fs.o[b][1]) / h.v[1],
+                                                (p[2] - fs.o[b][2]) / h.v[2]);
+        sdf_gradient(sdf, inv.v, p, g);
+        if (g[0] * g[0] + g[1] * g[1] + g[2] * g[2] > 0.0) {
+            const double len = sqrt(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]);
+            const double nn[3] = {g[0] / len, g[1] / len, g[2] / len};
+            const double vr[3] = {fv[0] - cv[0], fv[1] - cv[1], fv[2] - cv[2]};
+            const double dn = vr[0] * nn[0] + vr[1] * nn[1] + vr[2] * nn[2];
+            double vt[3] = {vr[0] - nn[0] * dn, vr[1] - nn[1] * dn,
+                            vr[2] - nn[2] * dn};
+            const double l2 = vt[0] * vt[0] + vt[1] * vt[1] + vt[2] * vt[2];
+            if (l2 > 0.0) {
+                const double veln = dmax(-dn, 0.0);
+                const double sc =
+                    dmax(1.0 - col.friction * veln / sqrt(l2), 0.0);
+                vt[0] = vt[0] * sc;
+                vt[1] = vt[1] * sc;
+                vt[2] = vt[2] * sc;
+            }
+            tmp[c] = vt[a] + cv[a];
+        } else {
+            tmp[c] = cv[a];
+        }
+    }
+}
+
+// K19d
+__global__ void k_bc_store(Dims s, int a, int closed,
+                           const double* __restrict__ tmp,
+                           double* __restrict__ vel) {
+    const long n = s.count();
+    const int lo = 1 << (2 * a), hi = 1 << (2 * a + 1);
+    const int ext = a == 0 ? s.x : (a == 1 ? s.y : s.z);
+    for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < n;
+         c += (long)gridDim.x * blockDim.x) {
+        int i, j, k;
+        cell_ijk(c, s, i, j, k);
+        const int t = a == 0 ? i : (a == 1 ? j : k);
+        const bool zero = ((closed & lo) && t == 0) ||
+                          ((closed & hi) && t == ext - 1);
+        vel[c] = zero ? 0.0 : tmp[c];
+    }
+}
+
+// Scratch for the passes: two validity planes and one temporary of `n`
+// elements (bytes + doubles), grown on demand.
+jetgpu_status bc_scratch(Ctx* c, size_t n) {
+    if (c->bc_cap >= n) return JETGPU_OK;
+    JG_CUDA(c, cudaStreamSynchronize(c->stream));
+    if (c->bc_tmp) cudaFree(c->bc_tmp);
+    if (c->bc_valid) cudaFree(c->bc_valid);
+    c->bc_tmp = nullptr;
+    c->bc_valid = nullptr;
+    c->bc_cap = 0;
+    JG_CUDA(c, cudaMalloc((void**)&c->bc_tmp, n * sizeof(double)));
+    JG_CUDA(c, cudaMalloc((void**)&c->bc_valid, 2 * n));
+    c->bc_cap = n;
+    return JETGPU_OK;
+}
+
+// `iters` passes on one array whose validity starts in v0; returns the
+// plane that holds the final validity.
+unsigned char* extrapolate_passes(Ctx* c, Dims s, double* data,
+                                  unsigned char* v0, unsigned char* v1,
+                                  unsigned iters) {
+    for (unsigned it = 0; it < iters; ++it) {
+        Prof pr(c, K_BOUNDARY, 10.0 * s.count());
+        k_extrapolate<<<blocks_for(s.count(), kThreads, c->num_sms * 8), kThreads, 0, c->stream>>>(
+            s, data, v0, v1);
+        std::swap(v0, v1);
+    }
+    return v0;
+}
+
+}  // namespace
+
+jetgpu_status constrain_velocity(Ctx* c, const GridDesc& g, double* u,
+                                 double* v, double* w, const FieldDesc& sdf,
+                                 const jetgpu_collider* col, int closed,
+                                 unsigned depth) {
+    const FaceSet fs = face_set(g);
+    size_t nmax = 0;
+    for (int a = 0; a < 3; ++a)
+        nmax = std::max(nmax, (size_t)fs.s[a].count());
+    if (jetgpu_status s = bc_scratch(c, 3 * nmax)) return s;
+    ColliderDesc cd{};
+    if (col) {
+        cd.present = 1;
+        for (int d = 0; d < 3; ++d) {
+            cd.lin[d] = col->linear_velocity[d];
+            cd.ang[d] = col->angular_velocity[d];
+            cd.centre[d] = col->centre[d];
+        }
+        cd.friction = col->friction;
+    }
+    H3 h{{g.spacing[0], g.spacing[1], g.spacing[2]}};
+    H3 inv{{0, 0, 0}};
+    if (sdf.kind == 1)
+        for (int d = 0; d < 3; ++d) inv.v[d] = 1.0 / sdf.spacing[d];
+    double* vel[3] = {u, v, w};
+    double* tmp[3];
+    unsigned char* va[3];
+    unsigned char* vb[3];
+    for (int a = 0; a < 3; ++a) {
+        tmp[a] = c->bc_tmp + a * nmax;
+        va[a] = c->bc_valid + a * nmax;
+        vb[a] = c->bc_valid + (3 + a) * nmax;
+    }
+    for (int a = 0; a < 3; ++a) {
+        const long n = fs.s[a].count();
+        Prof pr(c, K_BOUNDARY, 17.0 * n);
+        k_bc_mark<<<blocks_for(n, kThreads, c->num_sms * 8), kThreads, 0, c->stream>>>(
+            fs, a, h, sdf, cd, vel[a], va[a]);
+    }
+    for (int a = 0; a < 3; ++a)
+        extrapolate_passes(c, fs.s[a], vel[a], va[a], vb[a], depth);
+    for (int a = 0; a < 3; ++a) {
+        const long n = fs.s[a].count();
+        Prof pr(c, K_BOUNDARY, 16.0 * n);
+        k_bc_project<<<blocks_for(n, kThreads, c->num_sms * 8), kThreads, 0, c->stream>>>(
+            fs, a, h, inv, sdf, cd, u, v, w, tmp[a]);
+    }
+    for (int a = 0; a < 3; ++a) {
+        const long n = fs.s[a].count();
+        Prof pr(c, K_BOUNDARY, 16.0 * n);
+        k_bc_store<<<blocks_for(n, kThreads, c->num_sms * 8), kThreads, 0, c->stream>>>(
+            fs.s[a], a, closed, tmp[a], vel[a]);
+    }
+    JG_CUDA(c, cudaGetLastError());
+    return JETGPU_OK;
+}
+
+jetgpu_status extrapolate_region(Ctx* c, Dims s, double* data,
+                                 const unsigned char* valid, unsigned iters) {
+    const size_t n = (size_t)s.count();
+    if (jetgpu_status st = bc_scratch(c, n)) return st;
+    // The caller's validity stays untouched: passes ping-pong in scratch.
+    unsigned char* v0 = c->bc_valid;
+    unsigned char* v1 = c->bc_valid + n;
+    JG_CUDA(c, cudaMemcpyAsync(v0, valid, n, cudaMemcpyDeviceToDevice,
+                               c->stream));
+    extrapolate_passes(c, s, data, v0, v1, iters);
+    JG_CUDA(c, cudaGetLastError());
+    return JETGPU_OK;
+}
+
+}  // namespace jg

@@ -55,6 +55,7 @@ enum KernelClass : int {
     K_P2G,
     K_G2P,
     K_UNET,
+    K_BOUNDARY,       // boundary conditions / extrapolation
     K_CLASS_COUNT
 };
 const char* kernel_class_name(int cls);
@@ -141,6 +142,12 @@ struct Ctx {
     // Particle-transfer scratch.
     size_t pscratch_bytes = 0;
     unsigned char* pscratch = nullptr;
+
+    // Boundary-condition scratch (boundary.cu): bc_cap doubles and 2 x bc_cap
+    // validity bytes.
+    size_t bc_cap = 0;
+    double* bc_tmp = nullptr;
+    unsigned char* bc_valid = nullptr;
 
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
 
@@ -262,6 +269,13 @@ jetgpu_status harvest_pairs(Ctx* c, unsigned max_pairs, float* r_out,
 jetgpu_status norm2f(Ctx* c, const float* r, long n, int target);
 
 // ---- transfer.cu ----------------------------------------------------------
+jetgpu_status constrain_velocity(Ctx* c, const GridDesc& g, double* u,
+                                 double* v, double* w, const FieldDesc& sdf,
+                                 const jetgpu_collider* col, int closed,
+                                 unsigned depth);
+jetgpu_status extrapolate_region(Ctx* c, Dims s, double* data,
+                                 const unsigned char* valid, unsigned iters);
+
 jetgpu_status p2g(Ctx* c, const GridDesc& g, long np, const double* pos,
                   const double* vel, double* u, double* v, double* w,
                   unsigned char* mu, unsigned char* mv, unsigned char* mw,

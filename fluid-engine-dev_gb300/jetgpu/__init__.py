@@ -108,7 +108,36 @@ EXPORTS = (
     "jetgpu_profile_read", "jetgpu_p2g_device_noalloc", "jetgpu_conv3d",
     "jetgpu_conv3d_wgrad", "jetgpu_net_param_count", "jetgpu_load_unet",
     "jetgpu_harvest", "jetgpu_net_features", "jetgpu_net_apply",
+    "jetgpu_constrain_velocity_device", "jetgpu_constrain_velocity",
+    "jetgpu_extrapolate_to_region_device",
 )
+
+# closedDomainBoundaryFlag bits (include/jet/constants.h:312-335).
+kDirectionLeft, kDirectionRight, kDirectionDown = 1, 2, 4
+kDirectionUp, kDirectionBack, kDirectionFront = 8, 16, 32
+kDirectionAll = 63
+
+
+class Collider(C.Structure):
+    """jetgpu_collider: a rigid collider's surface velocity
+    linear + angular x (p - centre) and friction coefficient
+    (RigidBodyCollider3, src/jet/rigid_body_collider3.cpp:25-28)."""
+    _fields_ = [
+        ("linear_velocity", C.c_double * 3),
+        ("angular_velocity", C.c_double * 3),
+        ("centre", C.c_double * 3),
+        ("friction", C.c_double),
+    ]
+
+    @staticmethod
+    def make(linear=(0, 0, 0), angular=(0, 0, 0), centre=(0, 0, 0),
+             friction=0.0) -> "Collider":
+        c = Collider()
+        c.linear_velocity[:] = tuple(float(x) for x in linear)
+        c.angular_velocity[:] = tuple(float(x) for x in angular)
+        c.centre[:] = tuple(float(x) for x in centre)
+        c.friction = float(friction)
+        return c
 
 
 class KernelStat(C.Structure):
@@ -179,6 +208,15 @@ def library() -> C.CDLL:
     L.jetgpu_g2p_pic.restype = C.c_int
     L.jetgpu_g2p_pic_device.argtypes = pic_args
     L.jetgpu_g2p_pic_device.restype = C.c_int
+    bc_args = [vp, C.POINTER(Grid), vp, vp, vp, C.POINTER(ScalarField),
+               C.POINTER(Collider), C.c_int, C.c_uint]
+    L.jetgpu_constrain_velocity.argtypes = bc_args
+    L.jetgpu_constrain_velocity.restype = C.c_int
+    L.jetgpu_constrain_velocity_device.argtypes = bc_args
+    L.jetgpu_constrain_velocity_device.restype = C.c_int
+    L.jetgpu_extrapolate_to_region_device.argtypes = [
+        vp, C.POINTER(C.c_int), vp, vp, C.c_uint]
+    L.jetgpu_extrapolate_to_region_device.restype = C.c_int
     L.jetgpu_get_level.argtypes = [vp, C.c_int, C.c_int, vp, C.c_size_t,
                                    C.POINTER(C.c_size_t)]
     L.jetgpu_get_level.restype = C.c_int
@@ -589,6 +627,78 @@ def pic_transfer_from_grids_to_particles(solver: FdmMgpcgSolver3,
                                   _p(grid.v), _p(grid.w))
     solver.check(st)
     return velocities
+
+
+class GridFractionalBoundaryConditionSolver3:
+    """Mirror of GridFractionalBoundaryConditionSolver3
+    (src/jet/grid_fractional_boundary_condition_solver3.cpp) on the GPU.
+
+    updateCollider(collider_sdf, collider) installs the collider: its SDF as
+    a CellCenteredScalarGrid3 on the velocity grid (what colliderSdf() holds;
+    None = no collider) and a ``Collider`` for its surface velocity and
+    friction. constrainVelocity(velocity, extrapolationDepth) then matches the
+    reference bit for bit. The GPU context is borrowed from ``owner`` (an
+    FdmMgpcgSolver3), or a private one is created."""
+
+    def __init__(self, owner: "FdmMgpcgSolver3 | None" = None):
+        self._owner = owner if owner is not None else FdmMgpcgSolver3()
+        self._sdf = ConstantScalarField3(kMaxD)
+        self._collider = None
+        self._closed = kDirectionAll
+
+    def updateCollider(self, collider_sdf=None, collider: Collider = None):
+        self._sdf = collider_sdf if collider_sdf is not None \
+            else ConstantScalarField3(kMaxD)
+        self._collider = collider
+
+    def colliderSdf(self):
+        return self._sdf
+
+    def setClosedDomainBoundaryFlag(self, flag: int):
+        self._closed = int(flag)
+
+    def closedDomainBoundaryFlag(self) -> int:
+        return self._closed
+
+    def constrainVelocity(self, velocity: FaceCenteredGrid3,
+                          extrapolationDepth: int = 5):
+        """In place on velocity.u/v/w (host arrays)."""
+        for a in (velocity.u, velocity.v, velocity.w):
+            if not (a.dtype == np.float64 and a.flags.c_contiguous):
+                raise ValueError("velocity arrays must be C-contiguous float64")
+        keep = []
+        f = _field(self._sdf, keep)
+        g = velocity.c_grid()
+        col = C.byref(self._collider) if self._collider is not None else None
+        st = library().jetgpu_constrain_velocity(
+            self._owner.context(), C.byref(g), _p(velocity.u), _p(velocity.v),
+            _p(velocity.w), C.byref(f), col, self._closed,
+            int(extrapolationDepth))
+        self._owner.check(st)
+        return velocity
+
+
+def constrain_velocity_device(solver: "FdmMgpcgSolver3", grid: Grid, u, v, w,
+                              collider_sdf: ScalarField,
+                              collider: Collider = None,
+                              closed: int = kDirectionAll, depth: int = 5):
+    """jetgpu_constrain_velocity_device on device tensors (in place)."""
+    col = C.byref(collider) if collider is not None else None
+    st = library().jetgpu_constrain_velocity_device(
+        solver.context(), C.byref(grid), _p(u), _p(v), _p(w),
+        C.byref(collider_sdf), col, int(closed), int(depth))
+    solver.check(st)
+
+
+def extrapolate_to_region_device(solver: "FdmMgpcgSolver3", data, valid,
+                                 iterations: int):
+    """extrapolateToRegion on a device tensor (nz,ny,nx) in place from the
+    cells whose byte in ``valid`` (uint8 tensor, same shape) is non-zero."""
+    nz, ny, nx = data.shape
+    res = (C.c_int * 3)(nx, ny, nz)
+    st = library().jetgpu_extrapolate_to_region_device(
+        solver.context(), res, _p(data), _p(valid), int(iterations))
+    solver.check(st)
 
 
 def version() -> str:

@@ -247,6 +247,60 @@ jetgpu_status jetgpu_p2g_device_noalloc(void* stream, const jetgpu_grid* grid,
                                         unsigned char* mw, float* snap_u,
                                         float* snap_v, float* snap_w);
 
+/* A rigid collider: surface velocity linear + angular x (p - centre)
+ * (RigidBodyCollider3::velocityAt, src/jet/rigid_body_collider3.cpp:25-28;
+ * centre = the surface transform's translation) and the friction
+ * coefficient (Collider3::frictionCoefficient, src/jet/collider3.h). */
+typedef struct jetgpu_collider {
+    double linear_velocity[3];
+    double angular_velocity[3];
+    double centre[3];
+    double friction;
+} jetgpu_collider;
+
+/* Closed-domain bits of closedDomainBoundaryFlag()
+ * (include/jet/constants.h:312-335). */
+#define JETGPU_DIRECTION_LEFT 1
+#define JETGPU_DIRECTION_RIGHT 2
+#define JETGPU_DIRECTION_DOWN 4
+#define JETGPU_DIRECTION_UP 8
+#define JETGPU_DIRECTION_BACK 16
+#define JETGPU_DIRECTION_FRONT 32
+#define JETGPU_DIRECTION_ALL 63
+
+/* GridFractionalBoundaryConditionSolver3::constrainVelocity
+ * (src/jet/grid_fractional_boundary_condition_solver3.cpp:26-233), in place
+ * on the face velocity u/v/w. DEVICE pointers (collider_sdf->data too).
+ * collider_sdf: the solver's colliderSdf() (a cell-centred grid of the
+ * velocity grid's resolution; kind 0 = no collider). collider: NULL = none.
+ * closed_domain_flags: JETGPU_DIRECTION_* bits. extrapolation_depth: the
+ * free-slip extrapolation depth (GridFluidSolver3 passes ceil(maxCfl)).
+ * Bit-identical to the reference. Queued on the context's stream; returns
+ * without waiting. */
+jetgpu_status jetgpu_constrain_velocity_device(
+    struct jetgpu_ctx* ctx, const jetgpu_grid* grid, double* u, double* v,
+    double* w, const jetgpu_scalar_field* collider_sdf,
+    const jetgpu_collider* collider, int closed_domain_flags,
+    unsigned int extrapolation_depth);
+
+/* Host-pointer form of jetgpu_constrain_velocity_device (copies inside the
+ * call; synchronous). */
+jetgpu_status jetgpu_constrain_velocity(
+    struct jetgpu_ctx* ctx, const jetgpu_grid* grid, double* u, double* v,
+    double* w, const jetgpu_scalar_field* collider_sdf,
+    const jetgpu_collider* collider, int closed_domain_flags,
+    unsigned int extrapolation_depth);
+
+/* extrapolateToRegion (include/jet/detail/array_utils-inl.h:172-244), as
+ * PicSolver3::extrapolateVelocityToAir (src/jet/pic_solver3.cpp:284-294)
+ * applies it to each face array with the P2G markers: `iterations` passes
+ * in place on data (res[0]*res[1]*res[2] doubles, i fastest) from the cells
+ * whose valid byte is non-zero. DEVICE pointers; valid is not modified.
+ * Bit-identical to the reference. */
+jetgpu_status jetgpu_extrapolate_to_region_device(
+    struct jetgpu_ctx* ctx, const int res[3], double* data,
+    const unsigned char* valid, unsigned int iterations);
+
 /* Host-pointer forms of the three transfers (copies inside the call). */
 jetgpu_status jetgpu_p2g(struct jetgpu_ctx* ctx, const jetgpu_grid* grid,
                          long num_particles, const double* pos,

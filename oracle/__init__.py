@@ -54,6 +54,15 @@ class OrcMgParams(C.Structure):
     ]
 
 
+class OrcCollider(C.Structure):
+    _fields_ = [
+        ("lin", C.c_double * 3),
+        ("ang", C.c_double * 3),
+        ("centre", C.c_double * 3),
+        ("friction", C.c_double),
+    ]
+
+
 class OrcGrid(C.Structure):
     _fields_ = [
         ("res", C.c_int * 3),
@@ -165,6 +174,13 @@ class Oracle:
         L.orc_g2p_pic.argtypes = [C.POINTER(OrcGrid), C.c_long, _dp, _dp,
                                   _dp, _dp, _dp]
         L.orc_set_threads.argtypes = [C.c_int]
+        L.orc_constrain_velocity.argtypes = [
+            C.POINTER(OrcGrid), _dp, _dp, _dp, C.POINTER(OrcField),
+            C.POINTER(OrcCollider), C.c_int, C.c_uint]
+        L.orc_extrapolate.argtypes = [C.POINTER(C.c_int), _dp, _cp, C.c_uint]
+        if hasattr(L, "orc_sphere_collider_sdf"):
+            L.orc_sphere_collider_sdf.argtypes = [C.POINTER(OrcGrid), _dp,
+                                                  C.c_double, _dp]
 
     def set_threads(self, n: int = 0) -> None:
         self.lib.orc_set_threads(int(n))
@@ -323,6 +339,56 @@ class Oracle:
         self.lib.orc_g2p_pic(C.byref(g), pos.shape[0], _ptr(pos), _ptr(vel),
                              *[_ptr(a) for a in grids])
         return vel
+
+
+    # -- boundary conditions ------------------------------------------------
+    @staticmethod
+    def _grid(res, spacing, origin) -> OrcGrid:
+        g = OrcGrid()
+        g.res[:] = tuple(res)
+        g.spacing[:] = tuple(spacing)
+        g.origin[:] = tuple(origin)
+        return g
+
+    def constrain_velocity(self, res, spacing, origin, u, v, w, collider_sdf,
+                           collider=None, closed=63, depth=5):
+        """GridFractionalBoundaryConditionSolver3::constrainVelocity on copies
+        of u/v/w. collider_sdf: constant or cell-centred grid (nz,ny,nx).
+        collider: dict(lin, ang, centre, friction) or None."""
+        g = self._grid(res, spacing, origin)
+        data_origin = tuple(o + 0.5 * h for o, h in zip(origin, spacing))
+        f, keep = field(collider_sdf, spacing, data_origin)
+        out = [np.ascontiguousarray(a, np.float64).copy() for a in (u, v, w)]
+        col = None
+        if collider is not None:
+            col = OrcCollider()
+            col.lin[:] = tuple(collider.get("lin", (0, 0, 0)))
+            col.ang[:] = tuple(collider.get("ang", (0, 0, 0)))
+            col.centre[:] = tuple(collider.get("centre", (0, 0, 0)))
+            col.friction = float(collider.get("friction", 0.0))
+        self.lib.orc_constrain_velocity(
+            C.byref(g), *[_ptr(a) for a in out], C.byref(f),
+            C.byref(col) if col is not None else None, int(closed), int(depth))
+        del keep
+        return out
+
+    def extrapolate(self, data, valid, iterations):
+        """extrapolateToRegion on a copy of data (nz,ny,nx) from valid cells."""
+        d = np.ascontiguousarray(data, np.float64).copy()
+        m = np.ascontiguousarray(valid, np.int8)
+        r = (C.c_int * 3)(d.shape[2], d.shape[1], d.shape[0])
+        self.lib.orc_extrapolate(r, _ptr(d), _ptr(m, _cp), int(iterations))
+        return d
+
+    def sphere_collider_sdf(self, res, spacing, origin, centre, radius):
+        """Reference harness only: the collider SDF the reference builds for
+        a sphere collider on this grid (cell-centred, (nz,ny,nx))."""
+        g = self._grid(res, spacing, origin)
+        out = np.zeros((res[2], res[1], res[0]))
+        c = np.ascontiguousarray(centre, np.float64)
+        self.lib.orc_sphere_collider_sdf(C.byref(g), _ptr(c), float(radius),
+                                         _ptr(out))
+        return out
 
 
 _cache: dict = {}

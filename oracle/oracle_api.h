@@ -118,6 +118,39 @@ void orc_g2p_flip(const orc_grid* g, long np, const double* pos, double* vel,
 void orc_g2p_pic(const orc_grid* g, long np, const double* pos, double* vel,
                  const double* u, const double* v, const double* w);
 
+/* A rigid collider's surface velocity v(p) = lin + ang x (p - centre)
+ * (RigidBodyCollider3::velocityAt, src/jet/rigid_body_collider3.cpp:25-28)
+ * and its friction coefficient (Collider3::frictionCoefficient). */
+typedef struct orc_collider {
+    double lin[3];
+    double ang[3];
+    double centre[3];
+    double friction;
+} orc_collider;
+
+/* GridFractionalBoundaryConditionSolver3::constrainVelocity
+ * (src/jet/grid_fractional_boundary_condition_solver3.cpp:26-233) in place on
+ * u/v/w. sdf: the solver's collider SDF (a cell-centred grid of the velocity
+ * grid's resolution, colliderSdf()). col: the collider (NULL = none).
+ * closed: closedDomainBoundaryFlag() bits (kDirectionLeft = 1 ... Front = 32,
+ * include/jet/constants.h:312-335). depth: extrapolation depth. */
+void orc_constrain_velocity(const orc_grid* g, double* u, double* v,
+                            double* w, const orc_field* sdf,
+                            const orc_collider* col, int closed,
+                            unsigned int depth);
+
+/* extrapolateToRegion (include/jet/detail/array_utils-inl.h:172-244) in
+ * place on data (res cells) from the cells whose valid byte is non-zero. */
+void orc_extrapolate(const int res[3], double* data, const char* valid,
+                     unsigned int iterations);
+
+/* Reference harness only: the collider SDF that
+ * GridFractionalBoundaryConditionSolver3::onColliderUpdated (:244-281)
+ * builds for a sphere collider (cell-centred samples of the surface's signed
+ * distance). out: res cells. */
+void orc_sphere_collider_sdf(const orc_grid* g, const double centre[3],
+                             double radius, double* out);
+
 /* Port only: additionally stop MGPCG once the true relative residual
  * ||b - A x|| / ||b|| falls to `rel` (0 disables). Used to state the CPU
  * baseline at the GPU solver's accuracy. */

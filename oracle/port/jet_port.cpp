@@ -1096,6 +1096,209 @@ void orc_g2p_flip(const orc_grid* g, long np, const double* pos, double* vel,
     }
 }
 
+// GridFractionalBoundaryConditionSolver3::constrainVelocity
+// (src/jet/grid_fractional_boundary_condition_solver3.cpp:26-233).
+void orc_constrain_velocity(const orc_grid* g, double* u, double* v,
+                            double* w, const orc_field* sdf,
+                            const orc_collider* col, int closed,
+                            unsigned int depth) {
+    FaceGeom fg[3];
+    faceGeoms(g, fg);
+    const double* h = g->spacing;
+    double* vel[3] = {u, v, w};
+    Field F{sdf};
+    // RigidBodyCollider3::velocityAt (rigid_body_collider3.cpp:25-28) and
+    // Vector3::cross (include/jet/detail/vector3-inl.h:125-127).
+    auto colVel = [&](const double p[3], double out[3]) {
+        if (col == nullptr) {
+            out[0] = out[1] = out[2] = 0.0;
+            return;
+        }
+        const double* a = col->ang;
+        const double r[3] = {p[0] - col->centre[0], p[1] - col->centre[1],
+                             p[2] - col->centre[2]};
+        const double cr[3] = {a[1] * r[2] - r[1] * a[2],
+                              a[2] * r[0] - r[2] * a[0],
+                              a[0] * r[1] - r[0] * a[1]};
+        for (int d = 0; d < 3; ++d) out[d] = col->lin[d] + cr[d];
+    };
+    auto facePos = [&](int a, long i, long j, long k, double p[3]) {
+        p[0] = fg[a].o[0] + h[0] * (double)i;
+        p[1] = fg[a].o[1] + h[1] * (double)j;
+        p[2] = fg[a].o[2] + h[2] * (double)k;
+    };
+    // Collider velocity and markers (:51-100).
+    std::vector<char> marker[3];
+    for (int a = 0; a < 3; ++a) {
+        const Size3 s = fg[a].s;
+        marker[a].assign(s.count(), 1);
+#pragma omp parallel for schedule(static)
+        for (long k = 0; k < s.z; ++k)
+            for (long j = 0; j < s.y; ++j)
+                for (long i = 0; i < s.x; ++i) {
+                    double p[3], q0[3], q1[3];
+                    facePos(a, i, j, k, p);
+                    for (int d = 0; d < 3; ++d) {
+                        const double off = d == a ? 0.5 * h[d] : 0.0;
+                        q0[d] = p[d] - off;
+                        q1[d] = p[d] + off;
+                    }
+                    double frac = fracInsideSdf(F.sample(q0[0], q0[1], q0[2]),
+                                                F.sample(q1[0], q1[1], q1[2]));
+                    frac = 1.0 - (frac < 0.0 ? 0.0 : frac > 1.0 ? 1.0 : frac);
+                    const long c = lin(s, i, j, k);
+                    if (frac > 0.0) {
+                        marker[a][c] = 1;
+                    } else {
+                        double cv[3];
+                        colVel(p, cv);
+                        vel[a][c] = cv[a];
+                        marker[a][c] = 0;
+                    }
+                }
+    }
+    // Free slip: extrapolate into the collider (:102-108).
+    for (int a = 0; a < 3; ++a) {
+        const int res[3] = {(int)fg[a].s.x, (int)fg[a].s.y, (int)fg[a].s.z};
+        orc_extrapolate(res, vel[a], marker[a].data(), depth);
+    }
+    // ScalarGrid3::gradient (src/jet/scalar_grid3.cpp:89-102) over the
+    // central differences of gradient3 (src/jet/fdm_utils.cpp:49-67).
+    auto gradient = [&](const double p[3], double gout[3]) {
+        gout[0] = gout[1] = gout[2] = 0.0;
+        if (sdf == nullptr || sdf->kind == 0) return;
+        const Size3 s{sdf->res[0], sdf->res[1], sdf->res[2]};
+        Stencil st;
+        coordsAndWeights(s, sdf->origin[0], sdf->origin[1], sdf->origin[2],
+                         1.0 / sdf->spacing[0], 1.0 / sdf->spacing[1],
+                         1.0 / sdf->spacing[2], p[0], p[1], p[2], &st);
+        const double* d = sdf->data;
+        for (int n = 0; n < 8; ++n) {
+            const long c = st.idx[n];
+            const long i = c % s.x, j = (c / s.x) % s.y, k = c / (s.x * s.y);
+            const double l = d[lin(s, i > 0 ? i - 1 : i, j, k)];
+            const double r = d[lin(s, i + 1 < s.x ? i + 1 : i, j, k)];
+            const double dn = d[lin(s, i, j > 0 ? j - 1 : j, k)];
+            const double up = d[lin(s, i, j + 1 < s.y ? j + 1 : j, k)];
+            const double b = d[lin(s, i, j, k > 0 ? k - 1 : k)];
+            const double f = d[lin(s, i, j, k + 1 < s.z ? k + 1 : k)];
+            const double gv[3] = {0.5 * (r - l) / sdf->spacing[0],
+                                  0.5 * (up - dn) / sdf->spacing[1],
+                                  0.5 * (f - b) / sdf->spacing[2]};
+            for (int q = 0; q < 3; ++q) gout[q] = gout[q] + st.w[n] * gv[q];
+        }
+    };
+    // No flux: project onto the collider's tangent plane (:110-175), reading
+    // the extrapolated field, writing temporaries.
+    std::vector<double> tmp[3];
+    for (int a = 0; a < 3; ++a) {
+        const Size3 s = fg[a].s;
+        tmp[a].resize(s.count());
+#pragma omp parallel for schedule(static)
+        for (long k = 0; k < s.z; ++k)
+            for (long j = 0; j < s.y; ++j)
+                for (long i = 0; i < s.x; ++i) {
+                    const long c = lin(s, i, j, k);
+                    double p[3];
+                    facePos(a, i, j, k, p);
+                    if (!inside(F.sample(p[0], p[1], p[2]))) {
+                        tmp[a][c] = vel[a][c];
+                        continue;
+                    }
+                    double cv[3], fv[3], gd[3];
+                    colVel(p, cv);
+                    for (int b = 0; b < 3; ++b) {  // FaceCenteredGrid3::sample
+                        const double nx = (p[0] - fg[b].o[0]) / h[0];
+                        const double ny = (p[1] - fg[b].o[1]) / h[1];
+                        const double nz = (p[2] - fg[b].o[2]) / h[2];
+                        fv[b] = trilinear<double, double>(vel[b], fg[b].s, nx,
+                                                          ny, nz);
+                    }
+                    gradient(p, gd);
+                    if (gd[0] * gd[0] + gd[1] * gd[1] + gd[2] * gd[2] > 0.0) {
+                        const double len =
+                            std::sqrt(gd[0] * gd[0] + gd[1] * gd[1] + gd[2] * gd[2]);
+                        const double n[3] = {gd[0] / len, gd[1] / len, gd[2] / len};
+                        const double vr[3] = {fv[0] - cv[0], fv[1] - cv[1],
+                                              fv[2] - cv[2]};
+                        // projectAndApplyFriction (src/jet/physics_helpers.h:34-45).
+                        const double dn = vr[0] * n[0] + vr[1] * n[1] + vr[2] * n[2];
+                        double vt[3] = {vr[0] - n[0] * dn, vr[1] - n[1] * dn,
+                                        vr[2] - n[2] * dn};
+                        const double l2 = vt[0] * vt[0] + vt[1] * vt[1] + vt[2] * vt[2];
+                        if (l2 > 0) {
+                            const double veln = std::max(-dn, 0.0);
+                            const double fr = col ? col->friction : 0.0;
+                            const double sc = std::max(
+                                1.0 - fr * veln / std::sqrt(l2), 0.0);
+                            for (int q = 0; q < 3; ++q) vt[q] = vt[q] * sc;
+                        }
+                        tmp[a][c] = vt[a] + cv[a];
+                    } else {
+                        tmp[a][c] = cv[a];
+                    }
+                }
+    }
+    // Transfer results, then zero the normal velocity on closed domain
+    // faces (:177-232).
+    for (int a = 0; a < 3; ++a) {
+        std::memcpy(vel[a], tmp[a].data(), sizeof(double) * tmp[a].size());
+        const Size3 s = fg[a].s;
+        const int lo = 1 << (2 * a), hi = 1 << (2 * a + 1);
+        const long ext[3] = {s.x, s.y, s.z};
+        for (long k = 0; k < s.z; ++k)
+            for (long j = 0; j < s.y; ++j)
+                for (long i = 0; i < s.x; ++i) {
+                    const long idx[3] = {i, j, k};
+                    if (((closed & lo) && idx[a] == 0) ||
+                        ((closed & hi) && idx[a] == ext[a] - 1))
+                        vel[a][lin(s, i, j, k)] = 0.0;
+                }
+    }
+}
+
+// extrapolateToRegion (include/jet/detail/array_utils-inl.h:172-244). An
+// iteration writes only cells invalid at its start and reads only cells
+// valid at its start, so it is order-independent.
+void orc_extrapolate(const int res[3], double* data, const char* valid,
+                     unsigned int iterations) {
+    const Size3 s{res[0], res[1], res[2]};
+    std::vector<char> v0(valid, valid + s.count()), v1(s.count(), 0);
+    for (unsigned it = 0; it < iterations; ++it) {
+#pragma omp parallel for schedule(static)
+        for (long k = 0; k < s.z; ++k)
+            for (long j = 0; j < s.y; ++j)
+                for (long i = 0; i < s.x; ++i) {
+                    const long c = lin(s, i, j, k);
+                    if (v0[c]) {
+                        v1[c] = 1;
+                        continue;
+                    }
+                    double sum = 0.0;
+                    unsigned count = 0;
+                    auto take = [&](bool ok, long n) {
+                        if (ok && v0[n]) {
+                            sum += data[n];
+                            ++count;
+                        }
+                    };
+                    take(i + 1 < s.x, c + 1);
+                    take(i > 0, c - 1);
+                    take(j + 1 < s.y, c + s.x);
+                    take(j > 0, c - s.x);
+                    take(k + 1 < s.z, c + s.x * s.y);
+                    take(k > 0, c - s.x * s.y);
+                    if (count > 0) {
+                        data[c] = sum / (double)count;
+                        v1[c] = 1;
+                    } else {
+                        v1[c] = 0;
+                    }
+                }
+        v0.swap(v1);
+    }
+}
+
 void orc_g2p_pic(const orc_grid* g, long np, const double* pos, double* vel,
                  const double* u, const double* v, const double* w) {
     FaceGeom fg[3];

@@ -407,4 +407,73 @@ void orc_g2p_pic(const orc_grid* g, long np, const double* pos, double* vel,
     }
 }
 
+namespace {
+// A rigid sphere collider, so that Collider3::velocityAt and
+// frictionCoefficient answer as `col` says (the surface only sets the
+// rotation centre; the solver's SDF is replaced by the caller's grid).
+std::shared_ptr<RigidBodyCollider3> makeCollider(const orc_collider* col,
+                                                 double radius) {
+    auto sphere = std::make_shared<Sphere3>(Vector3D(), radius);
+    if (col)
+        sphere->transform.setTranslation(
+            Vector3D(col->centre[0], col->centre[1], col->centre[2]));
+    auto c = std::make_shared<RigidBodyCollider3>(sphere);
+    if (col) {
+        c->linearVelocity = Vector3D(col->lin[0], col->lin[1], col->lin[2]);
+        c->angularVelocity = Vector3D(col->ang[0], col->ang[1], col->ang[2]);
+        c->setFrictionCoefficient(col->friction);
+    }
+    return c;
+}
+}  // namespace
+
+void orc_constrain_velocity(const orc_grid* g, double* u, double* v,
+                            double* w, const orc_field* sdf,
+                            const orc_collider* col, int closed,
+                            unsigned int depth) {
+    Logging::mute();
+    const Size3 res(g->res[0], g->res[1], g->res[2]);
+    const Vector3D h(g->spacing[0], g->spacing[1], g->spacing[2]);
+    const Vector3D o(g->origin[0], g->origin[1], g->origin[2]);
+    FaceCenteredGrid3 vel(res, h, o);
+    fillGrid(&vel, u, v, w);
+    GridFractionalBoundaryConditionSolver3 bc;
+    bc.updateCollider(col ? makeCollider(col, 0.1) : nullptr, res, h, o);
+    // Replace the collider SDF with the caller's samples (same grid).
+    if (sdf && sdf->kind == 1) {
+        auto acc = bc._colliderSdf->dataAccessor();
+        std::memcpy(acc.data(), sdf->data,
+                    sizeof(double) * res.x * res.y * res.z);
+    } else {
+        bc._colliderSdf->fill(sdf ? sdf->value : kMaxD);
+    }
+    bc.setClosedDomainBoundaryFlag(closed);
+    bc.constrainVelocity(&vel, depth);
+    readGrid(vel, u, v, w);
+}
+
+void orc_extrapolate(const int res[3], double* data, const char* valid,
+                     unsigned int iterations) {
+    const Size3 s(res[0], res[1], res[2]);
+    Array3<double> in(s), out(s);
+    Array3<char> mk(s);
+    std::memcpy(in.data(), data, sizeof(double) * s.x * s.y * s.z);
+    std::memcpy(mk.data(), valid, s.x * s.y * s.z);
+    extrapolateToRegion(in.constAccessor(), mk.constAccessor(), iterations,
+                        out.accessor());
+    std::memcpy(data, out.data(), sizeof(double) * s.x * s.y * s.z);
+}
+
+void orc_sphere_collider_sdf(const orc_grid* g, const double centre[3],
+                             double radius, double* out) {
+    const Size3 res(g->res[0], g->res[1], g->res[2]);
+    const Vector3D h(g->spacing[0], g->spacing[1], g->spacing[2]);
+    const Vector3D o(g->origin[0], g->origin[1], g->origin[2]);
+    orc_collider c{{0, 0, 0}, {0, 0, 0}, {centre[0], centre[1], centre[2]}, 0};
+    GridFractionalBoundaryConditionSolver3 bc;
+    bc.updateCollider(makeCollider(&c, radius), res, h, o);
+    auto acc = bc._colliderSdf->constDataAccessor();
+    std::memcpy(out, acc.data(), sizeof(double) * res.x * res.y * res.z);
+}
+
 }  // extern "C"

@@ -18,6 +18,12 @@ Every fixture holds inputs and the reference's outputs for one small case:
   src/tests/unit_tests/fdm_mgpcg_solver3_tests.cpp:13-60 and its solution.
 * transfer_16.npz — P2G (grids, markers, FLIP snapshot) and G2P (FLIP, FLIP
   with PIC blending, PIC) for 3,000 particles on a 16^3 grid.
+* boundary_20x16x12.npz — GridFractionalBoundaryConditionSolver3::
+  constrainVelocity on an anisotropic 20x16x12 grid with the reference's own
+  sphere-collider SDF: a moving, rotating collider with friction and all
+  walls closed; the same inputs with three walls closed, no friction and a
+  shallower extrapolation; and no collider at all. Plus extrapolateToRegion
+  of a random field from 15% valid cells.
 * rng_streams.npz — the first doubles of std::mt19937(seed) +
   std::uniform_real_distribution<double>(0,1) for seeds 0, 1, 2, produced by
   a C++ program compiled here.
@@ -172,6 +178,35 @@ int main() {
 """
 
 
+def boundary(ref):
+    res = (20, 16, 12)
+    nx, ny, nz = res
+    h = (0.05, 0.0625, 0.08)
+    org = (0.1, -0.2, 0.05)
+    rng = np.random.default_rng(7)
+    centre = (org[0] + 0.55 * nx * h[0], org[1] + 0.4 * ny * h[1],
+              org[2] + 0.5 * nz * h[2])
+    sdf = ref.sphere_collider_sdf(res, h, org, centre, 0.3)
+    u = rng.uniform(-1, 1, (nz, ny, nx + 1))
+    v = rng.uniform(-1, 1, (nz, ny + 1, nx))
+    w = rng.uniform(-1, 1, (nz + 1, ny, nx))
+    moving = dict(lin=(0.3, -0.2, 0.1), ang=(0.5, -1.0, 0.7), centre=centre,
+                  friction=0.4)
+    still = dict(lin=(0, 0, 0), ang=(0, 0, 0), centre=centre, friction=0.0)
+    a = ref.constrain_velocity(res, h, org, u, v, w, sdf, moving, 63, 5)
+    b = ref.constrain_velocity(res, h, org, u, v, w, sdf, still, 1 + 8 + 32, 3)
+    c = ref.constrain_velocity(res, h, org, u, v, w, KMAX, None, 63, 5)
+    data = rng.standard_normal((nz, ny, nx))
+    valid = (rng.uniform(size=data.shape) < 0.15).astype(np.int8)
+    ext = ref.extrapolate(data, valid, 4)
+    save("boundary_20x16x12.npz", res=np.array(res), h=np.array(h),
+         origin=np.array(org), centre=np.array(centre), sdf=sdf, u=u, v=v, w=w,
+         moving=np.array(moving["lin"] + moving["ang"] + (moving["friction"],)),
+         a_u=a[0], a_v=a[1], a_w=a[2], b_u=b[0], b_v=b[1], b_w=b[2],
+         c_u=c[0], c_v=c[1], c_w=c[2], ext_in=data, ext_valid=valid,
+         ext_out=ext)
+
+
 def rng_streams():
     with tempfile.TemporaryDirectory() as td:
         src = os.path.join(td, "rng.cpp")
@@ -195,6 +230,7 @@ def main():
     noncubic(ref)
     mgpcg_poisson(ref)
     transfers(ref)
+    boundary(ref)
     rng_streams()
 
 

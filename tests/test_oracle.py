@@ -159,3 +159,64 @@ def test_port_matches_reference_random(port, reference):
         for k in ("u", "v", "w", "p"):
             assert np.array_equal(a[k], b[k]), k
         assert a["iters"] == b["iters"]
+
+
+def _boundary_golden():
+    g = golden("boundary_20x16x12.npz")
+    res = tuple(int(x) for x in g["res"])
+    m = g["moving"]
+    moving = dict(lin=tuple(m[:3]), ang=tuple(m[3:6]), centre=tuple(g["centre"]),
+                  friction=float(m[6]))
+    still = dict(lin=(0, 0, 0), ang=(0, 0, 0), centre=tuple(g["centre"]),
+                 friction=0.0)
+    cases = [("a", g["sdf"], moving, 63, 5), ("b", g["sdf"], still, 41, 3),
+             ("c", KMAX, None, 63, 5)]
+    return g, res, tuple(g["h"]), tuple(g["origin"]), cases
+
+
+def test_constrain_velocity_bit_exact(port):
+    """GridFractionalBoundaryConditionSolver3::constrainVelocity
+    (grid_fractional_boundary_condition_solver3.cpp:26-233): moving rotating
+    collider with friction, partly closed walls, no collider."""
+    g, res, h, org, cases = _boundary_golden()
+    for tag, sdf, col, closed, depth in cases:
+        out = port.constrain_velocity(res, h, org, g["u"], g["v"], g["w"], sdf,
+                                      col, closed, depth)
+        for a, k in enumerate("uvw"):
+            assert np.array_equal(out[a], g[f"{tag}_{k}"]), (tag, k)
+
+
+def test_extrapolate_to_region_bit_exact(port):
+    """extrapolateToRegion (include/jet/detail/array_utils-inl.h:172-244)."""
+    g = golden("boundary_20x16x12.npz")
+    out = port.extrapolate(g["ext_in"], g["ext_valid"], 4)
+    assert np.array_equal(out, g["ext_out"])
+
+
+def test_port_boundary_matches_reference_random(port, reference):
+    """Fresh random collider scenes through both libraries (needs the
+    reference)."""
+    rng = np.random.default_rng(23)
+    for res, closed, fr in (((16, 16, 16), 63, 0.0), ((24, 16, 20), 45, 0.3),
+                            ((12, 20, 8), 0, 0.9)):
+        nx, ny, nz = res
+        h = 1.0 / max(res)
+        sp, org = (h, h, h), (0.1, -0.05, 0.0)
+        centre = (org[0] + 0.55 * nx * h, org[1] + 0.45 * ny * h,
+                  org[2] + 0.5 * nz * h)
+        sdf = reference.sphere_collider_sdf(res, sp, org, centre,
+                                            0.3 * min(res) * h)
+        u = rng.uniform(-1, 1, (nz, ny, nx + 1))
+        v = rng.uniform(-1, 1, (nz, ny + 1, nx))
+        w = rng.uniform(-1, 1, (nz + 1, ny, nx))
+        col = dict(lin=(0.2, -0.1, 0.05), ang=(0.3, 0.7, -0.4), centre=centre,
+                   friction=fr)
+        a = reference.constrain_velocity(res, sp, org, u, v, w, sdf, col,
+                                         closed, 5)
+        b = port.constrain_velocity(res, sp, org, u, v, w, sdf, col, closed, 5)
+        for x, y in zip(a, b):
+            assert np.array_equal(x, y)
+        d = rng.standard_normal((nz, ny, nx))
+        m = (rng.uniform(size=d.shape) < 0.2).astype(np.int8)
+        assert np.array_equal(reference.extrapolate(d, m, 4),
+                              port.extrapolate(d, m, 4))
