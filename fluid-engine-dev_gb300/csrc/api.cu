@@ -856,6 +856,67 @@ jetgpu_status jetgpu_constrain_velocity(
     return JETGPU_OK;
 }
 
+jetgpu_status jetgpu_move_particles_device(
+    jetgpu_ctx* c, const jetgpu_grid* grid, long np, double* pos, double* vel,
+    const double* u, const double* v, const double* w, double dt,
+    double max_cfl, int closed, const jetgpu_collider* col,
+    const jetgpu_sphere* sph) {
+    jetgpu_status s = check_transfer(c, grid, np, pos, vel);
+    if (s != JETGPU_OK) return s;
+    if (!u || !v || !w) return fail(c, JETGPU_BAD_INPUT, "null grid arrays");
+    if (!std::isfinite(dt) || !std::isfinite(max_cfl))
+        return fail(c, JETGPU_BAD_INPUT, "non-finite time step or CFL");
+    if (sph && !(sph->radius >= 0.0))
+        return fail(c, JETGPU_BAD_INPUT, "sphere radius must be >= 0");
+    JG_CUDA(c, cudaSetDevice(c->device));
+    return move_particles(c, to_desc(grid), np, pos, vel, u, v, w, dt, max_cfl,
+                          closed, col, sph);
+}
+
+jetgpu_status jetgpu_move_particles(
+    jetgpu_ctx* c, const jetgpu_grid* grid, long np, double* pos, double* vel,
+    const double* u, const double* v, const double* w, double dt,
+    double max_cfl, int closed, const jetgpu_collider* col,
+    const jetgpu_sphere* sph) {
+    jetgpu_status s = check_transfer(c, grid, np, pos, vel);
+    if (s != JETGPU_OK) return s;
+    if (!u || !v || !w) return fail(c, JETGPU_BAD_INPUT, "null grid arrays");
+    if (!std::isfinite(dt) || !std::isfinite(max_cfl))
+        return fail(c, JETGPU_BAD_INPUT, "non-finite time step or CFL");
+    if (sph && !(sph->radius >= 0.0))
+        return fail(c, JETGPU_BAD_INPUT, "sphere radius must be >= 0");
+    JG_CUDA(c, cudaSetDevice(c->device));
+    size_t n[3];
+    face_counts(grid, n);
+    const size_t nf = n[0] + n[1] + n[2];
+    s = grow_stage(c, (size_t)np * 48 + nf * 8 + 64);
+    if (s != JETGPU_OK) return s;
+    unsigned char* p = c->stage;
+    double* dpos = reinterpret_cast<double*>(p); p += (size_t)np * 24;
+    double* dvel = reinterpret_cast<double*>(p); p += (size_t)np * 24;
+    double* dg = reinterpret_cast<double*>(p);
+    cudaStream_t st = c->stream;
+    const double* ins[3] = {u, v, w};
+    if (np) {
+        JG_CUDA(c, cudaMemcpyAsync(dpos, pos, np * 24, cudaMemcpyHostToDevice, st));
+        JG_CUDA(c, cudaMemcpyAsync(dvel, vel, np * 24, cudaMemcpyHostToDevice, st));
+    }
+    size_t off = 0;
+    for (int a = 0; a < 3; ++a) {
+        JG_CUDA(c, cudaMemcpyAsync(dg + off, ins[a], n[a] * 8, cudaMemcpyHostToDevice, st));
+        off += n[a];
+    }
+    s = move_particles(c, to_desc(grid), np, dpos, dvel, dg, dg + n[0],
+                       dg + n[0] + n[1], dt, max_cfl, closed, col, sph);
+    if (s != JETGPU_OK) return s;
+    if (np) {
+        JG_CUDA(c, cudaMemcpyAsync(pos, dpos, np * 24, cudaMemcpyDeviceToHost, st));
+        JG_CUDA(c, cudaMemcpyAsync(vel, dvel, np * 24, cudaMemcpyDeviceToHost, st));
+    }
+    JG_CUDA(c, cudaStreamSynchronize(st));
+    return JETGPU_OK;
+}
+
 jetgpu_status jetgpu_extrapolate_to_region_device(jetgpu_ctx* c,
                                                   const int res[3],
                                                   double* data,

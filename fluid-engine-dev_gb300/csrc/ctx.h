@@ -276,6 +276,12 @@ jetgpu_status constrain_velocity(Ctx* c, const GridDesc& g, double* u,
 jetgpu_status extrapolate_region(Ctx* c, Dims s, double* data,
                                  const unsigned char* valid, unsigned iters);
 
+jetgpu_status move_particles(Ctx* c, const GridDesc& g, long np, double* pos,
+                             double* vel, const double* u, const double* v,
+                             const double* w, double dt, double max_cfl,
+                             int closed, const jetgpu_collider* col,
+                             const jetgpu_sphere* sph);
+
 jetgpu_status p2g(Ctx* c, const GridDesc& g, long np, const double* pos,
                   const double* vel, double* u, double* v, double* w,
                   unsigned char* mu, unsigned char* mv, unsigned char* mw,

@@ -148,7 +148,186 @@ __global__ void k_g2p_pic(long np, const double* __restrict__ pos,
     }
 }
 
+// K20: PicSolver3::moveParticles (src/jet/pic_solver3.cpp:206-282) and,
+// with a sphere collider, Collider3::resolveCollision
+// (src/jet/collider3.cpp:19-73, radius 0, restitution 0) through the
+// transformed Sphere3 queries (src/jet/sphere3.cpp:25-39,
+// src/jet/surface3.cpp:23-79, include/jet/detail/transform3-inl.h:45-79).
+// One thread per particle; every expression in the reference's order.
+struct SphereDesc {
+    int present;
+    double center[3], radius;
+    int flipped;
+    double orient[9], inv[9];
+    double t[3];  // translation = collider centre
+    double lin[3], ang[3], friction;
+};
+
+__device__ __forceinline__ void mat3(const double* m, const double v[3],
+                                     double o[3]) {
+    o[0] = m[0] * v[0] + m[1] * v[1] + m[2] * v[2];
+    o[1] = m[3] * v[0] + m[4] * v[1] + m[5] * v[2];
+    o[2] = m[6] * v[0] + m[7] * v[1] + m[8] * v[2];
+}
+
+__device__ __forceinline__ double dmax(double a, double b) {
+    return a < b ? b : a;
+}
+
+__device__ void resolve_sphere(const SphereDesc& S, double p[3],
+                               double vv[3]) {
+    const double dp[3] = {p[0] - S.t[0], p[1] - S.t[1], p[2] - S.t[2]};
+    double pl[3];
+    mat3(S.inv, dp, pl);
+    const double* c = S.center;
+    double nl[3];
+    const double eps = 2.220446049250313e-16;  // numeric_limits::epsilon()
+    if (fabs(c[0] - pl[0]) < eps && fabs(c[1] - pl[1]) < eps &&
+        fabs(c[2] - pl[2]) < eps) {
+        nl[0] = 1.0;
+        nl[1] = 0.0;
+        nl[2] = 0.0;
+    } else {
+        const double d0 = pl[0] - c[0], d1 = pl[1] - c[1], d2 = pl[2] - c[2];
+        const double l = sqrt(d0 * d0 + d1 * d1 + d2 * d2);
+        nl[0] = d0 / l;
+        nl[1] = d1 / l;
+        nl[2] = d2 / l;
+    }
+    const double r = S.radius;
+    const double cpl[3] = {r * nl[0] + c[0], r * nl[1] + c[1],
+                           r * nl[2] + c[2]};
+    const double e0 = c[0] - pl[0], e1 = c[1] - pl[1], e2 = c[2] - pl[2];
+    const double dist = fabs(sqrt(e0 * e0 + e1 * e1 + e2 * e2) - r);
+    const double o0 = pl[0] - cpl[0], o1 = pl[1] - cpl[1], o2 = pl[2] - cpl[2];
+    const bool in_local = o0 * nl[0] + o1 * nl[1] + o2 * nl[2] < 0.0;
+    const bool is_in = (S.flipped != 0) == !in_local;
+    if (!(is_in || dist < 0.0)) return;
+    double cpw[3], nw[3];
+    mat3(S.orient, cpl, cpw);
+    for (int d = 0; d < 3; ++d) cpw[d] = cpw[d] + S.t[d];
+    mat3(S.orient, nl, nw);
+    const double fl = S.flipped ? -1.0 : 1.0;
+    for (int d = 0; d < 3; ++d) nw[d] *= fl;
+    const double* a = S.ang;
+    const double r0 = p[0] - S.t[0], r1 = p[1] - S.t[1], r2 = p[2] - S.t[2];
+    const double cv[3] = {S.lin[0] + (a[1] * r2 - r1 * a[2]),
+                          S.lin[1] + (a[2] * r0 - r2 * a[0]),
+                          S.lin[2] + (a[0] * r1 - r0 * a[1])};
+    double tp[3];
+    for (int d = 0; d < 3; ++d) tp[d] = cpw[d] + 0.0 * nw[d];
+    const double rv[3] = {vv[0] - cv[0], vv[1] - cv[1], vv[2] - cv[2]};
+    const double ndv = nw[0] * rv[0] + nw[1] * rv[1] + nw[2] * rv[2];
+    double rn[3] = {ndv * nw[0], ndv * nw[1], ndv * nw[2]};
+    double rt[3] = {rv[0] - rn[0], rv[1] - rn[1], rv[2] - rn[2]};
+    if (ndv < 0.0) {
+        const double rest = 0.0;
+        const double dn[3] = {(-rest - 1.0) * rn[0], (-rest - 1.0) * rn[1],
+                              (-rest - 1.0) * rn[2]};
+        for (int d = 0; d < 3; ++d) rn[d] *= -rest;
+        const double lt2 = rt[0] * rt[0] + rt[1] * rt[1] + rt[2] * rt[2];
+        if (lt2 > 0.0) {
+            const double ldn = sqrt(dn[0] * dn[0] + dn[1] * dn[1] + dn[2] * dn[2]);
+            const double fs = dmax(1.0 - S.friction * ldn / sqrt(lt2), 0.0);
+            for (int d = 0; d < 3; ++d) rt[d] *= fs;
+        }
+        for (int d = 0; d < 3; ++d) vv[d] = rn[d] + rt[d] + cv[d];
+    }
+    for (int d = 0; d < 3; ++d) p[d] = tp[d];
+}
+
+__global__ void k_move_particles(long np, double* __restrict__ pos,
+                                 double* __restrict__ vel, FaceSet fs,
+                                 const double* __restrict__ u,
+                                 const double* __restrict__ v,
+                                 const double* __restrict__ w, double hx,
+                                 double hy, double hz, double sdt,
+                                 unsigned nsub, int closed, double lo0,
+                                 double lo1, double lo2, double hi0,
+                                 double hi1, double hi2, SphereDesc S) {
+    const double* grid[3] = {u, v, w};
+    const double lo[3] = {lo0, lo1, lo2}, hi[3] = {hi0, hi1, hi2};
+    for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < np;
+         q += (long)gridDim.x * blockDim.x) {
+        double p0[3] = {pos[3 * q], pos[3 * q + 1], pos[3 * q + 2]};
+        double p1[3] = {p0[0], p0[1], p0[2]};
+        double vv[3] = {vel[3 * q], vel[3 * q + 1], vel[3 * q + 2]};
+        for (unsigned t = 0; t < nsub; ++t) {
+            double v0[3], mid[3], vm[3];
+            for (int a = 0; a < 3; ++a)
+                v0[a] = sample_face<double, double>(
+                    grid[a], fs.s[a], (p0[0] - fs.o[a][0]) / hx,
+                    (p0[1] - fs.o[a][1]) / hy, (p0[2] - fs.o[a][2]) / hz);
+            const double hs = 0.5 * sdt;
+            for (int d = 0; d < 3; ++d) mid[d] = p0[d] + hs * v0[d];
+            for (int a = 0; a < 3; ++a)
+                vm[a] = sample_face<double, double>(
+                    grid[a], fs.s[a], (mid[0] - fs.o[a][0]) / hx,
+                    (mid[1] - fs.o[a][1]) / hy, (mid[2] - fs.o[a][2]) / hz);
+            for (int d = 0; d < 3; ++d) p1[d] = p0[d] + sdt * vm[d];
+            for (int d = 0; d < 3; ++d) p0[d] = p1[d];
+        }
+        for (int d = 0; d < 3; ++d) {
+            if ((closed & (1 << (2 * d))) && p1[d] <= lo[d]) {
+                p1[d] = lo[d];
+                vv[d] = 0.0;
+            }
+            if ((closed & (1 << (2 * d + 1))) && p1[d] >= hi[d]) {
+                p1[d] = hi[d];
+                vv[d] = 0.0;
+            }
+        }
+        if (S.present) resolve_sphere(S, p1, vv);
+        for (int d = 0; d < 3; ++d) {
+            pos[3 * q + d] = p1[d];
+            vel[3 * q + d] = vv[d];
+        }
+    }
+}
+
 }  // namespace
+
+jetgpu_status move_particles(Ctx* c, const GridDesc& g, long np, double* pos,
+                             double* vel, const double* u, const double* v,
+                             const double* w, double dt, double max_cfl,
+                             int closed, const jetgpu_collider* col,
+                             const jetgpu_sphere* sph) {
+    const FaceSet fs = face_set(g);
+    double lo[3], hi[3];  // Grid3::boundingBox (src/jet/grid3.cpp:77)
+    for (int d = 0; d < 3; ++d) {
+        const double e = g.origin[d] + g.spacing[d] * (double)g.res[d];
+        lo[d] = std::min(g.origin[d], e);
+        hi[d] = std::max(g.origin[d], e);
+    }
+    const unsigned nsub = (unsigned)std::max(max_cfl, 1.0);
+    SphereDesc S{};
+    if (col && sph) {
+        S.present = 1;
+        for (int d = 0; d < 3; ++d) {
+            S.center[d] = sph->center[d];
+            S.t[d] = col->centre[d];
+            S.lin[d] = col->linear_velocity[d];
+            S.ang[d] = col->angular_velocity[d];
+        }
+        S.radius = sph->radius;
+        S.flipped = sph->normal_flipped;
+        for (int i = 0; i < 9; ++i) {
+            S.orient[i] = sph->orientation[i];
+            S.inv[i] = sph->inverse_orientation[i];
+        }
+        S.friction = col->friction;
+    }
+    if (np > 0) {
+        Prof pr(c, K_G2P, 48.0 * np);
+        k_move_particles<<<blocks_for(np, kThreads, c->num_sms * 16), kThreads,
+                           0, c->stream>>>(
+            np, pos, vel, fs, u, v, w, g.spacing[0], g.spacing[1],
+            g.spacing[2], dt / nsub, nsub, closed, lo[0], lo[1], lo[2], hi[0],
+            hi[1], hi[2], S);
+    }
+    JG_CUDA(c, cudaGetLastError());
+    return JETGPU_OK;
+}
 
 jetgpu_status p2g(Ctx* c, const GridDesc& g, long np, const double* pos,
                   const double* vel, double* u, double* v, double* w,

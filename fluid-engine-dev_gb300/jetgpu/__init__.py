@@ -109,7 +109,8 @@ EXPORTS = (
     "jetgpu_conv3d_wgrad", "jetgpu_net_param_count", "jetgpu_load_unet",
     "jetgpu_harvest", "jetgpu_net_features", "jetgpu_net_apply",
     "jetgpu_constrain_velocity_device", "jetgpu_constrain_velocity",
-    "jetgpu_extrapolate_to_region_device",
+    "jetgpu_extrapolate_to_region_device", "jetgpu_move_particles_device",
+    "jetgpu_move_particles",
 )
 
 # closedDomainBoundaryFlag bits (include/jet/constants.h:312-335).
@@ -217,6 +218,12 @@ def library() -> C.CDLL:
     L.jetgpu_extrapolate_to_region_device.argtypes = [
         vp, C.POINTER(C.c_int), vp, vp, C.c_uint]
     L.jetgpu_extrapolate_to_region_device.restype = C.c_int
+    mp_args = [vp, C.POINTER(Grid), C.c_long, vp, vp, vp, vp, vp, C.c_double,
+               C.c_double, C.c_int, C.POINTER(Collider), C.POINTER(Sphere)]
+    L.jetgpu_move_particles.argtypes = mp_args
+    L.jetgpu_move_particles.restype = C.c_int
+    L.jetgpu_move_particles_device.argtypes = mp_args
+    L.jetgpu_move_particles_device.restype = C.c_int
     L.jetgpu_get_level.argtypes = [vp, C.c_int, C.c_int, vp, C.c_size_t,
                                    C.POINTER(C.c_size_t)]
     L.jetgpu_get_level.restype = C.c_int
@@ -627,6 +634,65 @@ def pic_transfer_from_grids_to_particles(solver: FdmMgpcgSolver3,
                                   _p(grid.v), _p(grid.w))
     solver.check(st)
     return velocities
+
+
+class Sphere(C.Structure):
+    """jetgpu_sphere: a Sphere3 collider surface under its Transform3
+    (orientation matrix and inverse, row-major)."""
+    _fields_ = [
+        ("center", C.c_double * 3),
+        ("radius", C.c_double),
+        ("normal_flipped", C.c_int),
+        ("orientation", C.c_double * 9),
+        ("inverse_orientation", C.c_double * 9),
+    ]
+
+    @staticmethod
+    def make(radius, center=(0, 0, 0), normal_flipped=False,
+             orientation=None, inverse_orientation=None) -> "Sphere":
+        s = Sphere()
+        s.center[:] = tuple(float(x) for x in center)
+        s.radius = float(radius)
+        s.normal_flipped = int(bool(normal_flipped))
+        eye = tuple(float(x) for x in np.eye(3).ravel())
+        s.orientation[:] = eye if orientation is None else \
+            tuple(float(x) for x in np.ravel(orientation))
+        s.inverse_orientation[:] = eye if inverse_orientation is None else \
+            tuple(float(x) for x in np.ravel(inverse_orientation))
+        return s
+
+
+def move_particles(solver: "FdmMgpcgSolver3", grid: FaceCenteredGrid3,
+                   positions, velocities, dt: float, maxCfl: float = 5.0,
+                   closed: int = kDirectionAll, collider: Collider = None,
+                   sphere: Sphere = None):
+    """PicSolver3::moveParticles (+ sphere collisions) in place on host
+    arrays (C-contiguous float64, shape (n, 3))."""
+    for a in (positions, velocities):
+        if not (a.dtype == np.float64 and a.flags.c_contiguous):
+            raise ValueError("positions/velocities must be C-contiguous float64")
+    g = grid.c_grid()
+    st = library().jetgpu_move_particles(
+        solver.context(), C.byref(g), positions.shape[0], _p(positions),
+        _p(velocities), _p(grid.u), _p(grid.v), _p(grid.w), float(dt),
+        float(maxCfl), int(closed),
+        C.byref(collider) if collider is not None else None,
+        C.byref(sphere) if sphere is not None else None)
+    solver.check(st)
+    return positions, velocities
+
+
+def move_particles_device(solver: "FdmMgpcgSolver3", grid: Grid, pos, vel, u,
+                          v, w, dt: float, maxCfl: float = 5.0,
+                          closed: int = kDirectionAll,
+                          collider: Collider = None, sphere: Sphere = None):
+    """jetgpu_move_particles_device on device tensors (in place)."""
+    st = library().jetgpu_move_particles_device(
+        solver.context(), C.byref(grid), pos.shape[0], _p(pos), _p(vel),
+        _p(u), _p(v), _p(w), float(dt), float(maxCfl), int(closed),
+        C.byref(collider) if collider is not None else None,
+        C.byref(sphere) if sphere is not None else None)
+    solver.check(st)
 
 
 class GridFractionalBoundaryConditionSolver3:

@@ -301,6 +301,40 @@ jetgpu_status jetgpu_extrapolate_to_region_device(
     struct jetgpu_ctx* ctx, const int res[3], double* data,
     const unsigned char* valid, unsigned int iterations);
 
+/* A Sphere3 collider surface (src/jet/sphere3.cpp) under its Transform3
+ * (include/jet/detail/transform3-inl.h): local centre and radius, normal
+ * flip (Surface3::isNormalFlipped), and the transform's orientation matrix
+ * and its inverse, row-major (Transform3 keeps both; identity for an
+ * unrotated sphere). The translation is the collider's `centre`. */
+typedef struct jetgpu_sphere {
+    double center[3];
+    double radius;
+    int normal_flipped;
+    double orientation[9];
+    double inverse_orientation[9];
+} jetgpu_sphere;
+
+/* PicSolver3::moveParticles (src/jet/pic_solver3.cpp:206-282): per
+ * particle, max(1, floor(max_cfl)) RK2 midpoint sub-steps of dt through the
+ * face velocity u/v/w, clamping to the closed domain walls
+ * (closed_domain_flags, JETGPU_DIRECTION_* bits) with the velocity component
+ * zeroed there; then, when both collider and sphere are non-NULL,
+ * Collider3::resolveCollision (src/jet/collider3.cpp:19-73) with radius 0
+ * and restitution 0 against the sphere. pos/vel: AoS xyz doubles, updated in
+ * place. DEVICE pointers. Bit-identical to the reference. */
+jetgpu_status jetgpu_move_particles_device(
+    struct jetgpu_ctx* ctx, const jetgpu_grid* grid, long num_particles,
+    double* pos, double* vel, const double* u, const double* v,
+    const double* w, double dt, double max_cfl, int closed_domain_flags,
+    const jetgpu_collider* collider, const jetgpu_sphere* sphere);
+
+/* Host-pointer form of jetgpu_move_particles_device (synchronous). */
+jetgpu_status jetgpu_move_particles(
+    struct jetgpu_ctx* ctx, const jetgpu_grid* grid, long num_particles,
+    double* pos, double* vel, const double* u, const double* v,
+    const double* w, double dt, double max_cfl, int closed_domain_flags,
+    const jetgpu_collider* collider, const jetgpu_sphere* sphere);
+
 /* Host-pointer forms of the three transfers (copies inside the call). */
 jetgpu_status jetgpu_p2g(struct jetgpu_ctx* ctx, const jetgpu_grid* grid,
                          long num_particles, const double* pos,

@@ -63,6 +63,17 @@ class OrcCollider(C.Structure):
     ]
 
 
+class OrcSphere(C.Structure):
+    _fields_ = [
+        ("center", C.c_double * 3),
+        ("radius", C.c_double),
+        ("normal_flipped", C.c_int),
+        ("orient", C.c_double * 9),
+        ("inv_orient", C.c_double * 9),
+        ("quat", C.c_double * 4),
+    ]
+
+
 class OrcGrid(C.Structure):
     _fields_ = [
         ("res", C.c_int * 3),
@@ -178,6 +189,14 @@ class Oracle:
             C.POINTER(OrcGrid), _dp, _dp, _dp, C.POINTER(OrcField),
             C.POINTER(OrcCollider), C.c_int, C.c_uint]
         L.orc_extrapolate.argtypes = [C.POINTER(C.c_int), _dp, _cp, C.c_uint]
+        L.orc_move_particles.argtypes = [
+            C.POINTER(OrcGrid), C.c_long, _dp, _dp, _dp, _dp, _dp, C.c_double,
+            C.c_double, C.c_int, C.POINTER(OrcCollider), C.POINTER(OrcSphere)]
+        L.orc_build_particle_sdf.argtypes = [
+            C.POINTER(OrcGrid), C.c_long, _dp, C.POINTER(OrcField), C.c_double,
+            _dp]
+        if hasattr(L, "orc_quaternion_matrices"):
+            L.orc_quaternion_matrices.argtypes = [_dp, _dp, _dp]
         if hasattr(L, "orc_sphere_collider_sdf"):
             L.orc_sphere_collider_sdf.argtypes = [C.POINTER(OrcGrid), _dp,
                                                   C.c_double, _dp]
@@ -359,13 +378,7 @@ class Oracle:
         data_origin = tuple(o + 0.5 * h for o, h in zip(origin, spacing))
         f, keep = field(collider_sdf, spacing, data_origin)
         out = [np.ascontiguousarray(a, np.float64).copy() for a in (u, v, w)]
-        col = None
-        if collider is not None:
-            col = OrcCollider()
-            col.lin[:] = tuple(collider.get("lin", (0, 0, 0)))
-            col.ang[:] = tuple(collider.get("ang", (0, 0, 0)))
-            col.centre[:] = tuple(collider.get("centre", (0, 0, 0)))
-            col.friction = float(collider.get("friction", 0.0))
+        col = self._collider(collider) if collider is not None else None
         self.lib.orc_constrain_velocity(
             C.byref(g), *[_ptr(a) for a in out], C.byref(f),
             C.byref(col) if col is not None else None, int(closed), int(depth))
@@ -379,6 +392,63 @@ class Oracle:
         r = (C.c_int * 3)(d.shape[2], d.shape[1], d.shape[0])
         self.lib.orc_extrapolate(r, _ptr(d), _ptr(m, _cp), int(iterations))
         return d
+
+    @staticmethod
+    def _collider(c):
+        col = OrcCollider()
+        col.lin[:] = tuple(c.get("lin", (0, 0, 0)))
+        col.ang[:] = tuple(c.get("ang", (0, 0, 0)))
+        col.centre[:] = tuple(c.get("centre", (0, 0, 0)))
+        col.friction = float(c.get("friction", 0.0))
+        return col
+
+    def quaternion_matrices(self, q):
+        """Reference harness only: Transform3's orientation matrix and its
+        inverse for quaternion q = (w, x, y, z), row-major."""
+        o, i = np.zeros(9), np.zeros(9)
+        self.lib.orc_quaternion_matrices(
+            _ptr(np.ascontiguousarray(q, np.float64)), _ptr(o), _ptr(i))
+        return o, i
+
+    def move_particles(self, res, spacing, origin, pos, vel, grids, dt,
+                       max_cfl=5.0, closed=63, collider=None, sphere=None):
+        """PicSolver3::moveParticles (+ sphere collisions) on copies.
+        sphere: dict(center, radius, normal_flipped, orient, inv_orient,
+        quat)."""
+        g = self._grid(res, spacing, origin)
+        pos = np.ascontiguousarray(pos, np.float64).copy()
+        vel = np.ascontiguousarray(vel, np.float64).copy()
+        grids = [np.ascontiguousarray(a, np.float64) for a in grids]
+        col = sph = None
+        if collider is not None and sphere is not None:
+            col = self._collider(collider)
+            sph = OrcSphere()
+            sph.center[:] = tuple(sphere.get("center", (0, 0, 0)))
+            sph.radius = float(sphere["radius"])
+            sph.normal_flipped = int(sphere.get("normal_flipped", 0))
+            sph.orient[:] = tuple(sphere.get("orient", np.eye(3).ravel()))
+            sph.inv_orient[:] = tuple(sphere.get("inv_orient", np.eye(3).ravel()))
+            sph.quat[:] = tuple(sphere.get("quat", (1, 0, 0, 0)))
+        self.lib.orc_move_particles(
+            C.byref(g), pos.shape[0], _ptr(pos), _ptr(vel),
+            *[_ptr(a) for a in grids], float(dt), float(max_cfl), int(closed),
+            C.byref(col) if col is not None else None,
+            C.byref(sph) if sph is not None else None)
+        return pos, vel
+
+    def build_particle_sdf(self, res, spacing, origin, pos, collider_sdf,
+                           max_cfl=5.0):
+        """PicSolver3::buildSignedDistanceField (+ extrapolation into the
+        collider); returns the cell-centred SDF (nz,ny,nx)."""
+        g = self._grid(res, spacing, origin)
+        data_origin = tuple(o + 0.5 * h for o, h in zip(origin, spacing))
+        f, keep = field(collider_sdf, spacing, data_origin)
+        pos = np.ascontiguousarray(pos, np.float64)
+        out = np.zeros((res[2], res[1], res[0]))
+        self.lib.orc_build_particle_sdf(C.byref(g), pos.shape[0], _ptr(pos),
+                                        C.byref(f), float(max_cfl), _ptr(out))
+        del keep
+        return out
 
     def sphere_collider_sdf(self, res, spacing, origin, centre, radius):
         """Reference harness only: the collider SDF the reference builds for

@@ -144,6 +144,46 @@ void orc_constrain_velocity(const orc_grid* g, double* u, double* v,
 void orc_extrapolate(const int res[3], double* data, const char* valid,
                      unsigned int iterations);
 
+/* A Sphere3 collider surface (src/jet/sphere3.cpp) under its Transform3
+ * (include/jet/detail/transform3-inl.h): local centre and radius, normal
+ * flip, the orientation matrix and its inverse (row-major; Transform3 keeps
+ * both), and the orientation quaternion (w, x, y, z) they came from (used by
+ * the reference harness to build the same transform). The translation is the
+ * collider's `centre`. */
+typedef struct orc_sphere {
+    double center[3];
+    double radius;
+    int normal_flipped;
+    double orient[9];
+    double inv_orient[9];
+    double quat[4];
+} orc_sphere;
+
+/* PicSolver3::moveParticles (src/jet/pic_solver3.cpp:206-282): RK2
+ * midpoint sub-steps through the face velocity, clamping to closed domain
+ * walls, then Collider3::resolveCollision (src/jet/collider3.cpp:19-73) of
+ * every particle against the sphere collider (col and sphere both non-NULL).
+ * pos/vel: AoS xyz doubles, updated in place. */
+void orc_move_particles(const orc_grid* g, long np, double* pos, double* vel,
+                        const double* u, const double* v, const double* w,
+                        double dt, double max_cfl, int closed,
+                        const orc_collider* col, const orc_sphere* sphere);
+
+/* PicSolver3::buildSignedDistanceField (src/jet/pic_solver3.cpp:296-317):
+ * at every cell centre the distance to the nearest particle within the band
+ * 2r (r = 1.2 max(h) / sqrt(2)) minus r (the band value where none is
+ * near), then extrapolateIntoCollider (src/jet/grid_fluid_solver3.cpp:
+ * 423-438) with depth ceil(max_cfl) from the cells outside collider_sdf.
+ * out: res cells. */
+void orc_build_particle_sdf(const orc_grid* g, long np, const double* pos,
+                            const orc_field* collider_sdf, double max_cfl,
+                            double* out);
+
+/* Reference harness only: Transform3's orientation matrix and its inverse
+ * for quaternion q = (w, x, y, z), row-major. */
+void orc_quaternion_matrices(const double q[4], double orient[9],
+                             double inv_orient[9]);
+
 /* Reference harness only: the collider SDF that
  * GridFractionalBoundaryConditionSolver3::onColliderUpdated (:244-281)
  * builds for a sphere collider (cell-centred samples of the surface's signed

@@ -1257,6 +1257,246 @@ void orc_constrain_velocity(const orc_grid* g, double* u, double* v,
     }
 }
 
+// PicSolver3::moveParticles (src/jet/pic_solver3.cpp:206-282) and
+// Collider3::resolveCollision (src/jet/collider3.cpp:19-73) with radius 0
+// and restitution 0 against a transformed Sphere3 (src/jet/sphere3.cpp:25-39,
+// src/jet/surface3.cpp:23-79, include/jet/detail/transform3-inl.h:45-79).
+void orc_move_particles(const orc_grid* g, long np, double* pos, double* vel,
+                        const double* u, const double* v, const double* w,
+                        double dt, double max_cfl, int closed,
+                        const orc_collider* col, const orc_sphere* sph) {
+    FaceGeom fg[3];
+    faceGeoms(g, fg);
+    const double* grids[3] = {u, v, w};
+    const double* h = g->spacing;
+    auto sample = [&](const double p[3], double out[3]) {
+        for (int a = 0; a < 3; ++a) {
+            const double nx = (p[0] - fg[a].o[0]) / h[0];
+            const double ny = (p[1] - fg[a].o[1]) / h[1];
+            const double nz = (p[2] - fg[a].o[2]) / h[2];
+            out[a] = trilinear<double, double>(grids[a], fg[a].s, nx, ny, nz);
+        }
+    };
+    double lo[3], hi[3];  // Grid3::boundingBox (src/jet/grid3.cpp:77)
+    for (int d = 0; d < 3; ++d) {
+        const double e = g->origin[d] + h[d] * (double)g->res[d];
+        lo[d] = std::min(g->origin[d], e);
+        hi[d] = std::max(g->origin[d], e);
+    }
+    const unsigned nsub = (unsigned)std::max(max_cfl, 1.0);
+    const double sdt = dt / nsub;
+    auto mat = [](const double* m, const double v[3], double o[3]) {
+        o[0] = m[0] * v[0] + m[1] * v[1] + m[2] * v[2];
+        o[1] = m[3] * v[0] + m[4] * v[1] + m[5] * v[2];
+        o[2] = m[6] * v[0] + m[7] * v[1] + m[8] * v[2];
+    };
+#pragma omp parallel for schedule(static)
+    for (long q = 0; q < np; ++q) {
+        double p0[3] = {pos[3 * q], pos[3 * q + 1], pos[3 * q + 2]};
+        double p1[3] = {p0[0], p0[1], p0[2]};
+        double vv[3] = {vel[3 * q], vel[3 * q + 1], vel[3 * q + 2]};
+        for (unsigned t = 0; t < nsub; ++t) {
+            double v0[3], mid[3], vm[3];
+            sample(p0, v0);
+            const double hs = 0.5 * sdt;
+            for (int d = 0; d < 3; ++d) mid[d] = p0[d] + hs * v0[d];
+            sample(mid, vm);
+            for (int d = 0; d < 3; ++d) p1[d] = p0[d] + sdt * vm[d];
+            for (int d = 0; d < 3; ++d) p0[d] = p1[d];
+        }
+        for (int d = 0; d < 3; ++d) {
+            if ((closed & (1 << (2 * d))) && p1[d] <= lo[d]) {
+                p1[d] = lo[d];
+                vv[d] = 0.0;
+            }
+            if ((closed & (1 << (2 * d + 1))) && p1[d] >= hi[d]) {
+                p1[d] = hi[d];
+                vv[d] = 0.0;
+            }
+        }
+        if (col && sph) {
+            // World -> local: inverse orientation of (p - translation).
+            const double* t = col->centre;
+            const double dp[3] = {p1[0] - t[0], p1[1] - t[1], p1[2] - t[2]};
+            double pl[3];
+            mat(sph->inv_orient, dp, pl);
+            const double* c = sph->center;
+            // closestNormalLocal (sphere3.cpp:33-39).
+            double nl[3];
+            if (std::fabs(c[0] - pl[0]) < kEpsD &&
+                std::fabs(c[1] - pl[1]) < kEpsD &&
+                std::fabs(c[2] - pl[2]) < kEpsD) {
+                nl[0] = 1;
+                nl[1] = 0;
+                nl[2] = 0;
+            } else {
+                const double dd[3] = {pl[0] - c[0], pl[1] - c[1], pl[2] - c[2]};
+                const double l = std::sqrt(dd[0] * dd[0] + dd[1] * dd[1] +
+                                           dd[2] * dd[2]);
+                nl[0] = dd[0] / l;
+                nl[1] = dd[1] / l;
+                nl[2] = dd[2] / l;
+            }
+            const double r = sph->radius;
+            const double cpl[3] = {r * nl[0] + c[0], r * nl[1] + c[1],
+                                   r * nl[2] + c[2]};
+            // closestDistanceLocal (sphere3.cpp:29-31).
+            const double e3[3] = {c[0] - pl[0], c[1] - pl[1], c[2] - pl[2]};
+            const double dist = std::fabs(
+                std::sqrt(e3[0] * e3[0] + e3[1] * e3[1] + e3[2] * e3[2]) - r);
+            // isInsideLocal (surface3.cpp:75-79) and isInside (:67-69).
+            const double off[3] = {pl[0] - cpl[0], pl[1] - cpl[1],
+                                   pl[2] - cpl[2]};
+            const bool inLocal =
+                off[0] * nl[0] + off[1] * nl[1] + off[2] * nl[2] < 0.0;
+            const bool isIn = (sph->normal_flipped != 0) == !inLocal;
+            if (isIn || dist < 0.0) {
+                // closestPoint / closestNormal in world space.
+                double cpw[3], nw[3];
+                mat(sph->orient, cpl, cpw);
+                for (int d = 0; d < 3; ++d) cpw[d] = cpw[d] + t[d];
+                mat(sph->orient, nl, nw);
+                const double fl = sph->normal_flipped ? -1.0 : 1.0;
+                for (int d = 0; d < 3; ++d) nw[d] *= fl;
+                // velocityAt(query point) (rigid_body_collider3.cpp:25-28).
+                const double* a = col->ang;
+                const double rr[3] = {p1[0] - t[0], p1[1] - t[1], p1[2] - t[2]};
+                const double cv[3] = {
+                    col->lin[0] + (a[1] * rr[2] - rr[1] * a[2]),
+                    col->lin[1] + (a[2] * rr[0] - rr[2] * a[0]),
+                    col->lin[2] + (a[0] * rr[1] - rr[0] * a[1])};
+                double tp[3];
+                for (int d = 0; d < 3; ++d) tp[d] = cpw[d] + 0.0 * nw[d];
+                const double rv[3] = {vv[0] - cv[0], vv[1] - cv[1],
+                                      vv[2] - cv[2]};
+                const double ndv = nw[0] * rv[0] + nw[1] * rv[1] + nw[2] * rv[2];
+                double rn[3] = {ndv * nw[0], ndv * nw[1], ndv * nw[2]};
+                double rt[3] = {rv[0] - rn[0], rv[1] - rn[1], rv[2] - rn[2]};
+                if (ndv < 0.0) {
+                    const double rest = 0.0;
+                    const double dn[3] = {(-rest - 1.0) * rn[0],
+                                          (-rest - 1.0) * rn[1],
+                                          (-rest - 1.0) * rn[2]};
+                    for (int d = 0; d < 3; ++d) rn[d] *= -rest;
+                    const double lt2 = rt[0] * rt[0] + rt[1] * rt[1] + rt[2] * rt[2];
+                    if (lt2 > 0.0) {
+                        const double ldn = std::sqrt(dn[0] * dn[0] + dn[1] * dn[1] +
+                                                     dn[2] * dn[2]);
+                        const double fs = std::max(
+                            1.0 - col->friction * ldn / std::sqrt(lt2), 0.0);
+                        for (int d = 0; d < 3; ++d) rt[d] *= fs;
+                    }
+                    for (int d = 0; d < 3; ++d) vv[d] = rn[d] + rt[d] + cv[d];
+                }
+                for (int d = 0; d < 3; ++d) p1[d] = tp[d];
+            }
+        }
+        for (int d = 0; d < 3; ++d) {
+            pos[3 * q + d] = p1[d];
+            vel[3 * q + d] = vv[d];
+        }
+    }
+}
+
+// PicSolver3::buildSignedDistanceField (src/jet/pic_solver3.cpp:296-317) and
+// GridFluidSolver3::extrapolateIntoCollider (grid_fluid_solver3.cpp:423-438).
+// The reference's hash-grid search visits exactly the particles whose
+// squared distance (x - p).(x - p) is <= band^2, and takes the minimum of
+// their distances, so any search that finds that set gives the same value;
+// this one bins particles into cells of the band size.
+void orc_build_particle_sdf(const orc_grid* g, long np, const double* pos,
+                            const orc_field* collider_sdf, double max_cfl,
+                            double* out) {
+    const Size3 s{g->res[0], g->res[1], g->res[2]};
+    const double* h = g->spacing;
+    const double maxH = std::max(std::max(h[0], h[1]), h[2]);
+    const double radius = 1.2 * maxH / std::sqrt(2.0);
+    const double band = 2.0 * radius;
+    const double band2 = band * band;
+    const double o[3] = {g->origin[0] + 0.5 * h[0], g->origin[1] + 0.5 * h[1],
+                         g->origin[2] + 0.5 * h[2]};
+    // Bins of edge `band` over the particles' bounding box.
+    double lo[3] = {0, 0, 0}, hi[3] = {0, 0, 0};
+    long nb[3] = {1, 1, 1};
+    std::vector<long> start, order;
+    auto binOf = [&](const double* p, long* b) {
+        for (int d = 0; d < 3; ++d) {
+            double f = std::floor((p[d] - lo[d]) / band);
+            if (!(f >= 0)) f = 0;
+            if (f > nb[d] - 1) f = (double)(nb[d] - 1);
+            b[d] = (long)f;
+        }
+    };
+    if (np > 0) {
+        for (int d = 0; d < 3; ++d) {
+            lo[d] = hi[d] = pos[d];
+            for (long q = 1; q < np; ++q) {
+                lo[d] = std::min(lo[d], pos[3 * q + d]);
+                hi[d] = std::max(hi[d], pos[3 * q + d]);
+            }
+            nb[d] = std::max(1L, std::min(1L << 20, (long)((hi[d] - lo[d]) / band) + 1));
+        }
+        const long nbin = nb[0] * nb[1] * nb[2];
+        std::vector<long> cnt(nbin + 1, 0), key(np);
+        for (long q = 0; q < np; ++q) {
+            long b[3];
+            binOf(pos + 3 * q, b);
+            key[q] = b[0] + nb[0] * (b[1] + nb[1] * b[2]);
+            ++cnt[key[q] + 1];
+        }
+        for (long b = 0; b < nbin; ++b) cnt[b + 1] += cnt[b];
+        start = cnt;
+        order.resize(np);
+        for (long q = 0; q < np; ++q) order[cnt[key[q]]++] = q;
+    }
+#pragma omp parallel for schedule(static)
+    for (long k = 0; k < s.z; ++k)
+        for (long j = 0; j < s.y; ++j)
+            for (long i = 0; i < s.x; ++i) {
+                const double pt[3] = {o[0] + h[0] * (double)i,
+                                      o[1] + h[1] * (double)j,
+                                      o[2] + h[2] * (double)k};
+                double minDist = band;
+                if (np > 0) {
+                    long b0[3], b1[3];
+                    const double plo[3] = {pt[0] - band, pt[1] - band, pt[2] - band};
+                    const double phi[3] = {pt[0] + band, pt[1] + band, pt[2] + band};
+                    binOf(plo, b0);
+                    binOf(phi, b1);
+                    for (long bz = b0[2]; bz <= b1[2]; ++bz)
+                        for (long by = b0[1]; by <= b1[1]; ++by)
+                            for (long bx = b0[0]; bx <= b1[0]; ++bx) {
+                                const long b = bx + nb[0] * (by + nb[1] * bz);
+                                for (long e = start[b]; e < start[b + 1]; ++e) {
+                                    const double* x = pos + 3 * order[e];
+                                    const double d0 = x[0] - pt[0], d1 = x[1] - pt[1],
+                                                 d2 = x[2] - pt[2];
+                                    if (d0 * d0 + d1 * d1 + d2 * d2 <= band2) {
+                                        const double e0 = pt[0] - x[0], e1 = pt[1] - x[1],
+                                                     e2 = pt[2] - x[2];
+                                        const double dist =
+                                            std::sqrt(e0 * e0 + e1 * e1 + e2 * e2);
+                                        minDist = std::min(minDist, dist);
+                                    }
+                                }
+                            }
+                }
+                out[lin(s, i, j, k)] = minDist - radius;
+            }
+    // extrapolateIntoCollider: valid where the collider SDF is not negative.
+    Field C{collider_sdf};
+    std::vector<char> valid(s.count());
+#pragma omp parallel for schedule(static)
+    for (long k = 0; k < s.z; ++k)
+        for (long j = 0; j < s.y; ++j)
+            for (long i = 0; i < s.x; ++i)
+                valid[lin(s, i, j, k)] =
+                    inside(C.sample(o[0] + h[0] * (double)i, o[1] + h[1] * (double)j,
+                                    o[2] + h[2] * (double)k)) ? 0 : 1;
+    const int res[3] = {(int)s.x, (int)s.y, (int)s.z};
+    orc_extrapolate(res, out, valid.data(), (unsigned)std::ceil(max_cfl));
+}
+
 // extrapolateToRegion (include/jet/detail/array_utils-inl.h:172-244). An
 // iteration writes only cells invalid at its start and reads only cells
 // valid at its start, so it is order-independent.

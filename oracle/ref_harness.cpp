@@ -464,6 +464,93 @@ void orc_extrapolate(const int res[3], double* data, const char* valid,
     std::memcpy(data, out.data(), sizeof(double) * s.x * s.y * s.z);
 }
 
+void orc_move_particles(const orc_grid* g, long np, double* pos, double* vel,
+                        const double* u, const double* v, const double* w,
+                        double dt, double max_cfl, int closed,
+                        const orc_collider* col, const orc_sphere* sph) {
+    Logging::mute();
+    auto s = std::make_unique<PicSolver3>(
+        Size3(g->res[0], g->res[1], g->res[2]),
+        Vector3D(g->spacing[0], g->spacing[1], g->spacing[2]),
+        Vector3D(g->origin[0], g->origin[1], g->origin[2]));
+    auto particles = s->particleSystemData();
+    Array1<Vector3D> P(np), V(np), F(np);
+    for (long i = 0; i < np; ++i) {
+        P[i] = Vector3D(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]);
+        V[i] = Vector3D(vel[3 * i], vel[3 * i + 1], vel[3 * i + 2]);
+    }
+    particles->addParticles(P.constAccessor(), V.constAccessor(),
+                            F.constAccessor());
+    fillGrid(s->gridSystemData()->velocity().get(), u, v, w);
+    s->setMaxCfl(max_cfl);
+    s->setClosedDomainBoundaryFlag(closed);
+    if (col && sph) {
+        auto sphere = std::make_shared<Sphere3>(
+            Vector3D(sph->center[0], sph->center[1], sph->center[2]),
+            sph->radius,
+            Transform3(Vector3D(col->centre[0], col->centre[1], col->centre[2]),
+                       QuaternionD(sph->quat[0], sph->quat[1], sph->quat[2],
+                                   sph->quat[3])),
+            sph->normal_flipped != 0);
+        auto c = std::make_shared<RigidBodyCollider3>(sphere);
+        c->linearVelocity = Vector3D(col->lin[0], col->lin[1], col->lin[2]);
+        c->angularVelocity = Vector3D(col->ang[0], col->ang[1], col->ang[2]);
+        c->setFrictionCoefficient(col->friction);
+        // Installed directly: setCollider would also rebuild the boundary
+        // solver, which moveParticles does not use.
+        s->_collider = c;
+    }
+    s->moveParticles(dt);
+    auto ps = s->particleSystemData()->positions();
+    auto vs = s->particleSystemData()->velocities();
+    for (long i = 0; i < np; ++i) {
+        for (int d = 0; d < 3; ++d) {
+            pos[3 * i + d] = ps[i][d];
+            vel[3 * i + d] = vs[i][d];
+        }
+    }
+}
+
+void orc_build_particle_sdf(const orc_grid* g, long np, const double* pos,
+                            const orc_field* collider_sdf, double max_cfl,
+                            double* out) {
+    Logging::mute();
+    const Size3 res(g->res[0], g->res[1], g->res[2]);
+    const Vector3D h(g->spacing[0], g->spacing[1], g->spacing[2]);
+    const Vector3D o(g->origin[0], g->origin[1], g->origin[2]);
+    auto s = std::make_unique<PicSolver3>(res, h, o);
+    auto particles = s->particleSystemData();
+    Array1<Vector3D> P(np), V(np), F(np);
+    for (long i = 0; i < np; ++i)
+        P[i] = Vector3D(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]);
+    particles->addParticles(P.constAccessor(), V.constAccessor(),
+                            F.constAccessor());
+    s->setMaxCfl(max_cfl);
+    // The collider SDF the boundary solver holds, replaced by the caller's.
+    auto bc = std::dynamic_pointer_cast<GridFractionalBoundaryConditionSolver3>(
+        s->_boundaryConditionSolver);
+    bc->updateCollider(nullptr, res, h, o);
+    if (collider_sdf && collider_sdf->kind == 1) {
+        auto acc = bc->_colliderSdf->dataAccessor();
+        std::memcpy(acc.data(), collider_sdf->data,
+                    sizeof(double) * res.x * res.y * res.z);
+    } else {
+        bc->_colliderSdf->fill(collider_sdf ? collider_sdf->value : kMaxD);
+    }
+    s->buildSignedDistanceField();
+    auto acc = s->signedDistanceField()->constDataAccessor();
+    std::memcpy(out, acc.data(), sizeof(double) * res.x * res.y * res.z);
+}
+
+void orc_quaternion_matrices(const double q[4], double orient[9],
+                             double inv_orient[9]) {
+    Transform3 t(Vector3D(), QuaternionD(q[0], q[1], q[2], q[3]));
+    for (int i = 0; i < 9; ++i) {
+        orient[i] = t._orientationMat3[i];
+        inv_orient[i] = t._inverseOrientationMat3[i];
+    }
+}
+
 void orc_sphere_collider_sdf(const orc_grid* g, const double centre[3],
                              double radius, double* out) {
     const Size3 res(g->res[0], g->res[1], g->res[2]);

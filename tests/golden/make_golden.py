@@ -24,6 +24,11 @@ Every fixture holds inputs and the reference's outputs for one small case:
   walls closed; the same inputs with three walls closed, no friction and a
   shallower extrapolation; and no collider at all. Plus extrapolateToRegion
   of a random field from 15% valid cells.
+* particles_20x12x16.npz — PicSolver3::moveParticles of 3,000 particles
+  (some starting outside the box) through a random face velocity: with a
+  rotated, moving sphere collider (friction 0.5, three walls closed,
+  maxCfl 3), with a normal-flipped sphere (all walls closed), and with no
+  collider (maxCfl 5); plus the Transform3 matrices the reference builds.
 * rng_streams.npz — the first doubles of std::mt19937(seed) +
   std::uniform_real_distribution<double>(0,1) for seeds 0, 1, 2, produced by
   a C++ program compiled here.
@@ -207,6 +212,40 @@ def boundary(ref):
          ext_out=ext)
 
 
+def particles(ref):
+    res = (20, 12, 16)
+    nx, ny, nz = res
+    h = 1.0 / 20
+    sp, org = (h, h, h), (0.05, 0.0, -0.1)
+    rng = np.random.default_rng(13)
+    grids = [rng.uniform(-2, 2, (nz, ny, nx + 1)),
+             rng.uniform(-2, 2, (nz, ny + 1, nx)),
+             rng.uniform(-2, 2, (nz + 1, ny, nx))]
+    lo = np.array(org)
+    hi = lo + h * np.array(res)
+    pos = lo + (hi - lo) * rng.uniform(-0.05, 1.05, (3000, 3))
+    vel = rng.uniform(-1, 1, (3000, 3))
+    q = np.array([0.9, 0.1, -0.3, 0.2])
+    q /= np.linalg.norm(q)
+    o, i = ref.quaternion_matrices(q)
+    centre = tuple(lo + (hi - lo) * np.array([0.5, 0.4, 0.55]))
+    col = dict(lin=(0.3, -0.2, 0.1), ang=(0.5, -1.0, 0.7), centre=centre,
+               friction=0.5)
+    sph = dict(center=(0.01, -0.02, 0.0), radius=0.2, normal_flipped=0,
+               orient=o, inv_orient=i, quat=q)
+    a = ref.move_particles(res, sp, org, pos, vel, grids, 0.01, 3.0, 45, col,
+                           sph)
+    sphf = dict(sph, normal_flipped=1, radius=0.3)
+    b = ref.move_particles(res, sp, org, pos, vel, grids, 0.02, 2.0, 63, col,
+                           sphf)
+    c = ref.move_particles(res, sp, org, pos, vel, grids, 0.01, 5.0, 63)
+    save("particles_20x12x16.npz", res=np.array(res), h=np.array(sp),
+         origin=np.array(org), u=grids[0], v=grids[1], w=grids[2], pos=pos,
+         vel=vel, quat=q, orient=o, inv_orient=i, centre=np.array(centre),
+         a_pos=a[0], a_vel=a[1], b_pos=b[0], b_vel=b[1], c_pos=c[0],
+         c_vel=c[1])
+
+
 def rng_streams():
     with tempfile.TemporaryDirectory() as td:
         src = os.path.join(td, "rng.cpp")
@@ -231,6 +270,7 @@ def main():
     mgpcg_poisson(ref)
     transfers(ref)
     boundary(ref)
+    particles(ref)
     rng_streams()
 
 
