@@ -359,6 +359,9 @@ void jetgpu_destroy(jetgpu_ctx* c) {
     release(&c->pscratch);
     release(&c->bc_tmp);
     release(&c->bc_valid);
+    release(&c->sdf_int);
+    release(&c->sdf_dbl);
+    release(&c->sdf_valid);
     net_destroy(c->unet);
     c->unet = nullptr;
     if (c->h_scal) cudaFreeHost(c->h_scal);
@@ -917,6 +920,63 @@ jetgpu_status jetgpu_move_particles(
     return JETGPU_OK;
 }
 
+jetgpu_status jetgpu_build_particle_sdf_device(
+    jetgpu_ctx* c, const jetgpu_grid* grid, long np, const double* pos,
+    const jetgpu_scalar_field* collider_sdf, double max_cfl, double* sdf) {
+    if (!c) return JETGPU_BAD_INPUT;
+    jetgpu_status s;
+    if ((s = check_grid(c, grid)) != JETGPU_OK) return s;
+    if ((s = check_field(c, collider_sdf, "collider_sdf")) != JETGPU_OK) return s;
+    if (np < 0 || (np > 0 && !pos) || !sdf)
+        return fail(c, JETGPU_BAD_INPUT, "bad particle or output arguments");
+    if (np > 2147483647L)
+        return fail(c, JETGPU_BAD_INPUT, "more than 2^31 - 1 particles");
+    if (!std::isfinite(max_cfl) || max_cfl < 0.0)
+        return fail(c, JETGPU_BAD_INPUT, "max_cfl must be finite and >= 0");
+    JG_CUDA(c, cudaSetDevice(c->device));
+    return build_particle_sdf(c, to_desc(grid), np, pos,
+                              to_desc(collider_sdf, collider_sdf->data),
+                              max_cfl, sdf);
+}
+
+jetgpu_status jetgpu_build_particle_sdf(jetgpu_ctx* c, const jetgpu_grid* grid,
+                                        long np, const double* pos,
+                                        const jetgpu_scalar_field* collider_sdf,
+                                        double max_cfl, double* sdf) {
+    if (!c) return JETGPU_BAD_INPUT;
+    jetgpu_status s;
+    if ((s = check_grid(c, grid)) != JETGPU_OK) return s;
+    if ((s = check_field(c, collider_sdf, "collider_sdf")) != JETGPU_OK) return s;
+    if (np < 0 || (np > 0 && !pos) || !sdf)
+        return fail(c, JETGPU_BAD_INPUT, "bad particle or output arguments");
+    if (np > 2147483647L)
+        return fail(c, JETGPU_BAD_INPUT, "more than 2^31 - 1 particles");
+    if (!std::isfinite(max_cfl) || max_cfl < 0.0)
+        return fail(c, JETGPU_BAD_INPUT, "max_cfl must be finite and >= 0");
+    JG_CUDA(c, cudaSetDevice(c->device));
+    const size_t cells = (size_t)grid->res[0] * grid->res[1] * grid->res[2];
+    const size_t ns = (size_t)field_count(collider_sdf);
+    s = grow_stage(c, (size_t)np * 24 + (cells + ns) * 8 + 64);
+    if (s != JETGPU_OK) return s;
+    unsigned char* p = c->stage;
+    double* dpos = reinterpret_cast<double*>(p); p += (size_t)np * 24;
+    double* dout = reinterpret_cast<double*>(p); p += cells * 8;
+    double* dcol = reinterpret_cast<double*>(p);
+    cudaStream_t st = c->stream;
+    if (np)
+        JG_CUDA(c, cudaMemcpyAsync(dpos, pos, np * 24, cudaMemcpyHostToDevice, st));
+    if (ns)
+        JG_CUDA(c, cudaMemcpyAsync(dcol, collider_sdf->data, ns * 8,
+                                   cudaMemcpyHostToDevice, st));
+    s = build_particle_sdf(c, to_desc(grid), np, dpos,
+                           to_desc(collider_sdf, ns ? dcol : nullptr), max_cfl,
+                           dout);
+    if (s != JETGPU_OK) return s;
+    JG_CUDA(c, cudaMemcpyAsync(sdf, dout, cells * 8, cudaMemcpyDeviceToHost, st));
+    JG_CUDA(c, cudaStreamSynchronize(st));
+    return JETGPU_OK;
+}
+
 jetgpu_status jetgpu_extrapolate_to_region_device(jetgpu_ctx* c,
                                                   const int res[3],
                                                   double* data,
@@ -947,7 +1007,7 @@ const char* kernel_class_name(int cls) {
         "correct", "spmv_dot", "update_xr", "dot_rz", "update_d",
         "residual64", "accumulate", "weights", "pyramid", "system",
         "gradient", "p2g", "g2p",
-        "unet", "boundary"};
+        "unet", "boundary", "particle_sdf", "move_particles"};
     return (cls >= 0 && cls < K_CLASS_COUNT) ? names[cls] : "?";
 }
 

@@ -56,6 +56,8 @@ enum KernelClass : int {
     K_G2P,
     K_UNET,
     K_BOUNDARY,       // boundary conditions / extrapolation
+    K_SDF,            // particle signed-distance field
+    K_MOVE,           // particle advection
     K_CLASS_COUNT
 };
 const char* kernel_class_name(int cls);
@@ -148,6 +150,12 @@ struct Ctx {
     size_t bc_cap = 0;
     double* bc_tmp = nullptr;
     unsigned char* bc_valid = nullptr;
+
+    // Particle-SDF scratch (sdf.cu): bins, keys, sorted particles, validity.
+    size_t sdf_int_cap = 0, sdf_dbl_cap = 0, sdf_valid_cap = 0;
+    int* sdf_int = nullptr;
+    double* sdf_dbl = nullptr;
+    unsigned char* sdf_valid = nullptr;
 
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
 
@@ -275,6 +283,10 @@ jetgpu_status constrain_velocity(Ctx* c, const GridDesc& g, double* u,
                                  unsigned depth);
 jetgpu_status extrapolate_region(Ctx* c, Dims s, double* data,
                                  const unsigned char* valid, unsigned iters);
+
+jetgpu_status build_particle_sdf(Ctx* c, const GridDesc& g, long np,
+                                 const double* pos, const FieldDesc& col,
+                                 double max_cfl, double* out);
 
 jetgpu_status move_particles(Ctx* c, const GridDesc& g, long np, double* pos,
                              double* vel, const double* u, const double* v,

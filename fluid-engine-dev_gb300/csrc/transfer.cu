@@ -318,7 +318,7 @@ jetgpu_status move_particles(Ctx* c, const GridDesc& g, long np, double* pos,
         S.friction = col->friction;
     }
     if (np > 0) {
-        Prof pr(c, K_G2P, 48.0 * np);
+        Prof pr(c, K_MOVE, 96.0 * np);
         k_move_particles<<<blocks_for(np, kThreads, c->num_sms * 16), kThreads,
                            0, c->stream>>>(
             np, pos, vel, fs, u, v, w, g.spacing[0], g.spacing[1],

@@ -110,7 +110,8 @@ EXPORTS = (
     "jetgpu_harvest", "jetgpu_net_features", "jetgpu_net_apply",
     "jetgpu_constrain_velocity_device", "jetgpu_constrain_velocity",
     "jetgpu_extrapolate_to_region_device", "jetgpu_move_particles_device",
-    "jetgpu_move_particles",
+    "jetgpu_move_particles", "jetgpu_build_particle_sdf_device",
+    "jetgpu_build_particle_sdf",
 )
 
 # closedDomainBoundaryFlag bits (include/jet/constants.h:312-335).
@@ -224,6 +225,12 @@ def library() -> C.CDLL:
     L.jetgpu_move_particles.restype = C.c_int
     L.jetgpu_move_particles_device.argtypes = mp_args
     L.jetgpu_move_particles_device.restype = C.c_int
+    sdf_args = [vp, C.POINTER(Grid), C.c_long, vp, C.POINTER(ScalarField),
+                C.c_double, vp]
+    L.jetgpu_build_particle_sdf.argtypes = sdf_args
+    L.jetgpu_build_particle_sdf.restype = C.c_int
+    L.jetgpu_build_particle_sdf_device.argtypes = sdf_args
+    L.jetgpu_build_particle_sdf_device.restype = C.c_int
     L.jetgpu_get_level.argtypes = [vp, C.c_int, C.c_int, vp, C.c_size_t,
                                    C.POINTER(C.c_size_t)]
     L.jetgpu_get_level.restype = C.c_int
@@ -692,6 +699,36 @@ def move_particles_device(solver: "FdmMgpcgSolver3", grid: Grid, pos, vel, u,
         _p(u), _p(v), _p(w), float(dt), float(maxCfl), int(closed),
         C.byref(collider) if collider is not None else None,
         C.byref(sphere) if sphere is not None else None)
+    solver.check(st)
+
+
+def build_signed_distance_field(solver: "FdmMgpcgSolver3",
+                                grid: FaceCenteredGrid3, positions,
+                                collider_sdf=None, maxCfl: float = 5.0):
+    """PicSolver3::buildSignedDistanceField (+ extrapolation into the
+    collider) from host particle positions (n, 3); returns the cell-centred
+    liquid SDF (nz, ny, nx) the pressure solve takes."""
+    pos = np.ascontiguousarray(positions, np.float64)
+    nx, ny, nz = grid.resolution
+    out = np.zeros((nz, ny, nx))
+    keep = []
+    f = _field(collider_sdf if collider_sdf is not None
+               else ConstantScalarField3(kMaxD), keep)
+    g = grid.c_grid()
+    st = library().jetgpu_build_particle_sdf(
+        solver.context(), C.byref(g), pos.shape[0], _p(pos), C.byref(f),
+        float(maxCfl), _p(out))
+    solver.check(st)
+    return out
+
+
+def build_signed_distance_field_device(solver: "FdmMgpcgSolver3", grid: Grid,
+                                       pos, collider_sdf: ScalarField, out,
+                                       maxCfl: float = 5.0):
+    """jetgpu_build_particle_sdf_device on device tensors."""
+    st = library().jetgpu_build_particle_sdf_device(
+        solver.context(), C.byref(grid), pos.shape[0], _p(pos),
+        C.byref(collider_sdf), float(maxCfl), _p(out))
     solver.check(st)
 
 

@@ -335,6 +335,25 @@ jetgpu_status jetgpu_move_particles(
     const double* w, double dt, double max_cfl, int closed_domain_flags,
     const jetgpu_collider* collider, const jetgpu_sphere* sphere);
 
+/* PicSolver3::buildSignedDistanceField (src/jet/pic_solver3.cpp:296-317)
+ * and GridFluidSolver3::extrapolateIntoCollider
+ * (src/jet/grid_fluid_solver3.cpp:423-438): the liquid SDF the pressure
+ * solve takes, at the cell centres of `grid` (res cells, i fastest) — the
+ * distance to the nearest particle within 2r minus r, r = 1.2 max(h) /
+ * sqrt(2) — then extrapolated ceil(max_cfl) cells into the collider
+ * (collider_sdf negative; kind 0 = no collider). pos: AoS xyz doubles.
+ * DEVICE pointers. Bit-identical to the reference. */
+jetgpu_status jetgpu_build_particle_sdf_device(
+    struct jetgpu_ctx* ctx, const jetgpu_grid* grid, long num_particles,
+    const double* pos, const jetgpu_scalar_field* collider_sdf,
+    double max_cfl, double* sdf_out);
+
+/* Host-pointer form of jetgpu_build_particle_sdf_device (synchronous). */
+jetgpu_status jetgpu_build_particle_sdf(
+    struct jetgpu_ctx* ctx, const jetgpu_grid* grid, long num_particles,
+    const double* pos, const jetgpu_scalar_field* collider_sdf,
+    double max_cfl, double* sdf_out);
+
 /* Host-pointer forms of the three transfers (copies inside the call). */
 jetgpu_status jetgpu_p2g(struct jetgpu_ctx* ctx, const jetgpu_grid* grid,
                          long num_particles, const double* pos,

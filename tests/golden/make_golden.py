@@ -29,6 +29,10 @@ Every fixture holds inputs and the reference's outputs for one small case:
   rotated, moving sphere collider (friction 0.5, three walls closed,
   maxCfl 3), with a normal-flipped sphere (all walls closed), and with no
   collider (maxCfl 5); plus the Transform3 matrices the reference builds.
+* particle_sdf_20x12x16.npz — PicSolver3::buildSignedDistanceField with
+  extrapolation into the collider for 3,000 particles on an anisotropic
+  grid, with the reference's sphere-collider SDF (maxCfl 2.5) and with no
+  collider (maxCfl 5).
 * rng_streams.npz — the first doubles of std::mt19937(seed) +
   std::uniform_real_distribution<double>(0,1) for seeds 0, 1, 2, produced by
   a C++ program compiled here.
@@ -246,6 +250,22 @@ def particles(ref):
          c_vel=c[1])
 
 
+def particle_sdf(ref):
+    res = (20, 12, 16)
+    h = (0.05, 0.0625, 0.055)
+    org = (0.1, 0.0, -0.05)
+    rng = np.random.default_rng(17)
+    lo = np.array(org)
+    hi = lo + np.array(h) * np.array(res)
+    pos = lo + (hi - lo) * rng.uniform(-0.1, 1.1, (3000, 3))
+    col = ref.sphere_collider_sdf(res, h, org, tuple(lo + (hi - lo) * 0.5),
+                                  0.25)
+    a = ref.build_particle_sdf(res, h, org, pos, col, 2.5)
+    b = ref.build_particle_sdf(res, h, org, pos, KMAX, 5.0)
+    save("particle_sdf_20x12x16.npz", res=np.array(res), h=np.array(h),
+         origin=np.array(org), pos=pos, collider_sdf=col, a=a, b=b)
+
+
 def rng_streams():
     with tempfile.TemporaryDirectory() as td:
         src = os.path.join(td, "rng.cpp")
@@ -271,6 +291,7 @@ def main():
     transfers(ref)
     boundary(ref)
     particles(ref)
+    particle_sdf(ref)
     rng_streams()
 
 

@@ -79,3 +79,52 @@ def test_move_particles_rejects_bad_inputs(solver):
     with pytest.raises(jetgpu.JetGpuError):
         jetgpu.move_particles(solver, grid, pos, vel, 0.01, 5.0, 63,
                               jetgpu.Collider.make(), jetgpu.Sphere.make(-1.0))
+
+
+def test_particle_sdf_matches_reference(solver):
+    g = golden("particle_sdf_20x12x16.npz")
+    res = tuple(int(x) for x in g["res"])
+    h, org = tuple(g["h"]), tuple(g["origin"])
+    grid = jetgpu.FaceCenteredGrid3(res, h, org)
+    col = jetgpu.CellCenteredScalarGrid3(res, h, org, g["collider_sdf"])
+    a = jetgpu.build_signed_distance_field(solver, grid, g["pos"], col, 2.5)
+    assert np.array_equal(a, g["a"])
+    b = jetgpu.build_signed_distance_field(solver, grid, g["pos"], None, 5.0)
+    assert np.array_equal(b, g["b"])
+
+
+@pytest.mark.parametrize("n", [64, 96])
+def test_particle_sdf_device_matches_port(solver, n):
+    """Dam-break particles at 8 per cell (the FLIP scenes' seeding) plus
+    particles on grid lines and outside the box, with a sphere collider."""
+    h = 1.0 / n
+    rng = np.random.default_rng(n)
+    m = n // 4
+    cells = np.stack(np.meshgrid(np.arange(m), np.arange(3 * m),
+                                 np.arange(n), indexing="ij"), -1).reshape(-1, 3)
+    pos = ((np.repeat(cells, 8, 0) + rng.uniform(size=(cells.shape[0] * 8, 3)))
+           * h)
+    pos = np.concatenate([pos, rng.integers(0, n, (5000, 3)) * h,
+                          rng.uniform(-0.05, 1.05, (5000, 3))])
+    k, j, i = np.indices((n, n, n))
+    col = np.sqrt(((i + .5) * h - .6) ** 2 + ((j + .5) * h - .2) ** 2 +
+                  ((k + .5) * h - .5) ** 2) - 0.15
+    ref = oracle.port().build_particle_sdf((n, n, n), (h, h, h), (0, 0, 0), pos,
+                                           col, 5.0)
+    dev = torch.device("cuda", 0)
+    tp = torch.from_numpy(np.ascontiguousarray(pos)).to(dev)
+    tcol = torch.from_numpy(col).to(dev)
+    out = torch.empty((n, n, n), dtype=torch.float64, device=dev)
+    grid = jetgpu.Grid()
+    grid.res[:] = (n, n, n)
+    grid.spacing[:] = (h, h, h)
+    grid.origin[:] = (0, 0, 0)
+    f = jetgpu.ScalarField()
+    f.kind = 1
+    f.data = tcol.data_ptr()
+    f.res[:] = (n, n, n)
+    f.origin[:] = (0.5 * h,) * 3
+    f.spacing[:] = (h, h, h)
+    jetgpu.build_signed_distance_field_device(solver, grid, tp, f, out, 5.0)
+    torch.cuda.synchronize()
+    assert np.array_equal(out.cpu().numpy(), ref)

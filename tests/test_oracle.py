@@ -273,3 +273,29 @@ def test_port_move_particles_matches_reference_random(port, reference):
         b = port.move_particles(res, sp, org, pos, vel, grids, 0.015, 4.0,
                                 closed, col, sph)
         assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+
+
+def test_particle_sdf_bit_exact(port):
+    """PicSolver3::buildSignedDistanceField (pic_solver3.cpp:296-317) and
+    extrapolateIntoCollider (grid_fluid_solver3.cpp:423-438)."""
+    g = golden("particle_sdf_20x12x16.npz")
+    res = tuple(int(x) for x in g["res"])
+    h, org = tuple(g["h"]), tuple(g["origin"])
+    a = port.build_particle_sdf(res, h, org, g["pos"], g["collider_sdf"], 2.5)
+    assert np.array_equal(a, g["a"])
+    b = port.build_particle_sdf(res, h, org, g["pos"], KMAX, 5.0)
+    assert np.array_equal(b, g["b"])
+
+
+def test_port_particle_sdf_matches_reference_random(port, reference):
+    rng = np.random.default_rng(41)
+    for res, h in (((16, 16, 16), (1 / 16,) * 3), ((24, 10, 14), (0.04, 0.07, 0.05))):
+        lo = np.zeros(3)
+        hi = np.array(h) * np.array(res)
+        pos = hi * rng.uniform(-0.1, 1.1, (4000, 3))
+        pos[::5] = hi * rng.integers(0, 8, (800, 3)) / 8.0  # on grid lines
+        col = reference.sphere_collider_sdf(res, h, (0, 0, 0), tuple(hi * 0.4),
+                                            0.2)
+        a = reference.build_particle_sdf(res, h, (0, 0, 0), pos, col, 3.0)
+        b = port.build_particle_sdf(res, h, (0, 0, 0), pos, col, 3.0)
+        assert np.array_equal(a, b)
