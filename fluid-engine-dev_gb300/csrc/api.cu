@@ -239,7 +239,7 @@ jetgpu_status ensure_buffers(Ctx* c, Dims n, unsigned max_levels) {
 }
 
 // The device-resident pipeline shared by the host and device entry points.
-static jetgpu_status solve_pressure_dev(
+jetgpu_status solve_pressure_dev(
     Ctx* c, const jetgpu_grid* grid, const double* u, const double* v,
     const double* w, const jetgpu_scalar_field* bsdf, const double* bdata,
     const jetgpu_scalar_field* fsdf, const double* fdata, const double* su,
@@ -362,6 +362,10 @@ void jetgpu_destroy(jetgpu_ctx* c) {
     release(&c->sdf_int);
     release(&c->sdf_dbl);
     release(&c->sdf_valid);
+    release(&c->flip_marks);
+    release(&c->flip_snap);
+    release(&c->flip_solid);
+    release(&c->flip_cfl);
     net_destroy(c->unet);
     c->unet = nullptr;
     if (c->h_scal) cudaFreeHost(c->h_scal);
@@ -975,6 +979,58 @@ jetgpu_status jetgpu_build_particle_sdf(jetgpu_ctx* c, const jetgpu_grid* grid,
     JG_CUDA(c, cudaMemcpyAsync(sdf, dout, cells * 8, cudaMemcpyDeviceToHost, st));
     JG_CUDA(c, cudaStreamSynchronize(st));
     return JETGPU_OK;
+}
+
+void jetgpu_flip_params_default(jetgpu_flip_params* p) {
+    if (!p) return;
+    p->gravity[0] = 0.0;
+    p->gravity[1] = -9.8;
+    p->gravity[2] = 0.0;
+    p->max_cfl = 5.0;
+    p->closed_domain_flags = JETGPU_DIRECTION_ALL;
+    p->flip = 1;
+    p->pic_blending = 0.0;
+}
+
+jetgpu_status jetgpu_fluid_cfl_device(jetgpu_ctx* c, const jetgpu_grid* grid,
+                                      const double* u, const double* v,
+                                      const double* w, double dt,
+                                      const double gravity[3], double* cfl) {
+    if (!c) return JETGPU_BAD_INPUT;
+    jetgpu_status s;
+    if ((s = check_grid(c, grid)) != JETGPU_OK) return s;
+    if (!u || !v || !w || !gravity || !cfl)
+        return fail(c, JETGPU_BAD_INPUT, "null argument");
+    JG_CUDA(c, cudaSetDevice(c->device));
+    return fluid_cfl(c, to_desc(grid), u, v, w, dt, gravity, cfl);
+}
+
+jetgpu_status jetgpu_flip_substep_device(
+    jetgpu_ctx* c, const jetgpu_grid* grid, long np, double* pos, double* vel,
+    double* u, double* v, double* w, double* fluid_sdf,
+    const jetgpu_scalar_field* collider_sdf, const jetgpu_collider* collider,
+    const jetgpu_sphere* sphere, const jetgpu_flip_params* prm, double dt,
+    jetgpu_solve_stats* stats) {
+    jetgpu_status s = check_transfer(c, grid, np, pos, vel);
+    if (s != JETGPU_OK) return s;
+    if ((s = check_field(c, collider_sdf, "collider_sdf")) != JETGPU_OK) return s;
+    if (!u || !v || !w || !fluid_sdf || !prm)
+        return fail(c, JETGPU_BAD_INPUT, "null argument");
+    if (np > 2147483647L)
+        return fail(c, JETGPU_BAD_INPUT, "more than 2^31 - 1 particles");
+    if (!std::isfinite(dt) || !(dt >= 0.0) || !std::isfinite(prm->max_cfl) ||
+        prm->max_cfl < 0.0)
+        return fail(c, JETGPU_BAD_INPUT, "bad time step or maxCfl");
+    if (sphere && !(sphere->radius >= 0.0))
+        return fail(c, JETGPU_BAD_INPUT, "sphere radius must be >= 0");
+    JG_CUDA(c, cudaSetDevice(c->device));
+    jetgpu_solve_stats local;
+    std::memset(&local, 0, sizeof(local));
+    s = flip_substep(c, to_desc(grid), np, pos, vel, u, v, w, fluid_sdf,
+                     to_desc(collider_sdf, collider_sdf->data), collider,
+                     sphere, *prm, dt, &local);
+    if (stats) *stats = local;
+    return s;
 }
 
 jetgpu_status jetgpu_extrapolate_to_region_device(jetgpu_ctx* c,

@@ -151,6 +151,15 @@ struct Ctx {
     double* bc_tmp = nullptr;
     unsigned char* bc_valid = nullptr;
 
+    // Device-resident FLIP step scratch (flip.cu): P2G markers, FLIP
+    // snapshot, collider face velocities, the CFL maximum.
+    size_t flip_marks_cap = 0, flip_snap_cap = 0, flip_solid_cap = 0,
+           flip_cfl_cap = 0;
+    unsigned char* flip_marks = nullptr;
+    float* flip_snap = nullptr;
+    double* flip_solid = nullptr;
+    unsigned long long* flip_cfl = nullptr;
+
     // Particle-SDF scratch (sdf.cu): bins, keys, sorted particles, validity.
     size_t sdf_int_cap = 0, sdf_dbl_cap = 0, sdf_valid_cap = 0;
     int* sdf_int = nullptr;
@@ -283,6 +292,26 @@ jetgpu_status constrain_velocity(Ctx* c, const GridDesc& g, double* u,
                                  unsigned depth);
 jetgpu_status extrapolate_region(Ctx* c, Dims s, double* data,
                                  const unsigned char* valid, unsigned iters);
+
+// GridFractionalSinglePhasePressureSolver3::solve on device arrays (api.cu):
+// the SDF descriptors' data pointers are replaced by bdata / fdata.
+jetgpu_status solve_pressure_dev(
+    Ctx* c, const jetgpu_grid* grid, const double* u, const double* v,
+    const double* w, const jetgpu_scalar_field* bsdf, const double* bdata,
+    const jetgpu_scalar_field* fsdf, const double* fdata, const double* su,
+    const double* sv, const double* sw, double* ou, double* ov, double* ow,
+    double* op, jetgpu_solve_stats* st);
+
+jetgpu_status fluid_cfl(Ctx* c, const GridDesc& g, const double* u,
+                        const double* v, const double* w, double dt,
+                        const double gravity[3], double* cfl);
+jetgpu_status flip_substep(Ctx* c, const GridDesc& g, long np, double* pos,
+                           double* vel, double* u, double* v, double* w,
+                           double* fluid_sdf, const FieldDesc& col_sdf,
+                           const jetgpu_collider* col,
+                           const jetgpu_sphere* sph,
+                           const jetgpu_flip_params& prm, double dt,
+                           jetgpu_solve_stats* stats);
 
 jetgpu_status build_particle_sdf(Ctx* c, const GridDesc& g, long np,
                                  const double* pos, const FieldDesc& col,

@@ -111,7 +111,8 @@ EXPORTS = (
     "jetgpu_constrain_velocity_device", "jetgpu_constrain_velocity",
     "jetgpu_extrapolate_to_region_device", "jetgpu_move_particles_device",
     "jetgpu_move_particles", "jetgpu_build_particle_sdf_device",
-    "jetgpu_build_particle_sdf",
+    "jetgpu_build_particle_sdf", "jetgpu_flip_params_default",
+    "jetgpu_fluid_cfl_device", "jetgpu_flip_substep_device",
 )
 
 # closedDomainBoundaryFlag bits (include/jet/constants.h:312-335).
@@ -231,6 +232,17 @@ def library() -> C.CDLL:
     L.jetgpu_build_particle_sdf.restype = C.c_int
     L.jetgpu_build_particle_sdf_device.argtypes = sdf_args
     L.jetgpu_build_particle_sdf_device.restype = C.c_int
+    L.jetgpu_flip_params_default.argtypes = [C.POINTER(FlipParams)]
+    L.jetgpu_flip_params_default.restype = None
+    L.jetgpu_fluid_cfl_device.argtypes = [vp, C.POINTER(Grid), vp, vp, vp,
+                                          C.c_double, C.POINTER(C.c_double),
+                                          C.POINTER(C.c_double)]
+    L.jetgpu_fluid_cfl_device.restype = C.c_int
+    L.jetgpu_flip_substep_device.argtypes = [
+        vp, C.POINTER(Grid), C.c_long, vp, vp, vp, vp, vp, vp,
+        C.POINTER(ScalarField), C.POINTER(Collider), C.POINTER(Sphere),
+        C.POINTER(FlipParams), C.c_double, C.POINTER(SolveStats)]
+    L.jetgpu_flip_substep_device.restype = C.c_int
     L.jetgpu_get_level.argtypes = [vp, C.c_int, C.c_int, vp, C.c_size_t,
                                    C.POINTER(C.c_size_t)]
     L.jetgpu_get_level.restype = C.c_int
@@ -730,6 +742,173 @@ def build_signed_distance_field_device(solver: "FdmMgpcgSolver3", grid: Grid,
         solver.context(), C.byref(grid), pos.shape[0], _p(pos),
         C.byref(collider_sdf), float(maxCfl), _p(out))
     solver.check(st)
+
+
+class FlipParams(C.Structure):
+    """jetgpu_flip_params (GridFluidSolver3 / FlipSolver3 settings)."""
+    _fields_ = [
+        ("gravity", C.c_double * 3),
+        ("max_cfl", C.c_double),
+        ("closed_domain_flags", C.c_int),
+        ("flip", C.c_int),
+        ("pic_blending", C.c_double),
+    ]
+
+
+class FlipSolver3:
+    """FlipSolver3 / PicSolver3 with particles and grid resident on the GPU
+    (src/jet/flip_solver3.cpp, src/jet/pic_solver3.cpp).
+
+    Particles are set with ``setParticles(positions, velocities)`` (host
+    arrays (n, 3)); ``update(frameInterval)`` advances one frame with the
+    reference's adaptive sub-stepping (PhysicsAnimation::onUpdate,
+    src/jet/physics_animation.cpp:98-122): while time remains, take
+    max(ceil(cfl / maxCfl), 1) equal sub-steps of the remaining time, each
+    one ``jetgpu_flip_substep_device``. The pressure projection uses
+    ``pressureSolver`` (an FdmMgpcgSolver3, which also owns the GPU
+    context). Device state: positions, velocities, the face velocity u/v/w and
+    the particle SDF, as torch tensors."""
+
+    def __init__(self, resolution, gridSpacing, origin=(0.0, 0.0, 0.0),
+                 pressureSolver: "FdmMgpcgSolver3 | None" = None,
+                 flip: bool = True, device: int = 0):
+        import torch
+        self._torch = torch
+        self.solver = pressureSolver if pressureSolver is not None \
+            else FdmMgpcgSolver3(device=device)
+        self.dev = torch.device("cuda", device)
+        nx, ny, nz = (int(r) for r in resolution)
+        if np.isscalar(gridSpacing):
+            gridSpacing = (float(gridSpacing),) * 3
+        self.resolution = (nx, ny, nz)
+        self.gridSpacing = tuple(float(h) for h in gridSpacing)
+        self.origin = tuple(float(o) for o in origin)
+        self.grid = Grid()
+        self.grid.res[:] = self.resolution
+        self.grid.spacing[:] = self.gridSpacing
+        self.grid.origin[:] = self.origin
+        f64 = dict(dtype=torch.float64, device=self.dev)
+        self.u = torch.zeros((nz, ny, nx + 1), **f64)
+        self.v = torch.zeros((nz, ny + 1, nx), **f64)
+        self.w = torch.zeros((nz + 1, ny, nx), **f64)
+        self.sdf = torch.zeros((nz, ny, nx), **f64)
+        self.pos = torch.zeros((0, 3), **f64)
+        self.vel = torch.zeros((0, 3), **f64)
+        self.params = FlipParams()
+        library().jetgpu_flip_params_default(C.byref(self.params))
+        self.params.flip = int(bool(flip))
+        self._col_sdf = None
+        self._collider = None
+        self._sphere = None
+        self.currentTimeInSeconds = 0.0
+        self.subSteps = 0
+        self.lastStats = SolveStats()
+        # The library works on its own stream; torch's uploads and reads of
+        # these tensors are ordered against it explicitly.
+        self._stream = torch.cuda.ExternalStream(self.solver.stream(),
+                                                 device=self.dev)
+
+    def _uploaded(self):
+        """Orders torch's writes to the state before library work."""
+        self._torch.cuda.current_stream(self.dev).synchronize()
+
+    def synchronize(self):
+        """Waits for the library's queued work on the state."""
+        self._stream.synchronize()
+
+    # -- settings (GridFluidSolver3 / FlipSolver3 accessors) ----------------
+    def setGravity(self, g):
+        self.params.gravity[:] = tuple(float(x) for x in g)
+
+    def setMaxCfl(self, cfl: float):
+        self.params.max_cfl = float(cfl)
+
+    def setClosedDomainBoundaryFlag(self, flag: int):
+        self.params.closed_domain_flags = int(flag)
+
+    def setPicBlendingFactor(self, f: float):
+        self.params.pic_blending = float(f)
+
+    def setCollider(self, collider_sdf, collider: Collider = None,
+                    sphere: Sphere = None):
+        """The collider: its SDF on this grid's cell centres (what the
+        reference's boundary solver builds from the surface; (nz,ny,nx)
+        array), and optionally its motion and sphere surface for particle
+        collisions."""
+        self.synchronize()
+        self._col_sdf = self._torch.as_tensor(
+            np.ascontiguousarray(collider_sdf, np.float64), device=self.dev)
+        self._collider = collider
+        self._sphere = sphere
+        self._uploaded()
+
+    def setParticles(self, positions, velocities=None):
+        pos = np.ascontiguousarray(positions, np.float64).reshape(-1, 3)
+        vel = np.zeros_like(pos) if velocities is None else \
+            np.ascontiguousarray(velocities, np.float64).reshape(-1, 3)
+        self.synchronize()
+        self.pos = self._torch.from_numpy(pos.copy()).to(self.dev)
+        self.vel = self._torch.from_numpy(vel.copy()).to(self.dev)
+        self._uploaded()
+
+    def positions(self) -> np.ndarray:
+        self.synchronize()
+        return self.pos.cpu().numpy()
+
+    def velocities(self) -> np.ndarray:
+        self.synchronize()
+        return self.vel.cpu().numpy()
+
+    # -- stepping ------------------------------------------------------------
+    def _col_field(self) -> ScalarField:
+        f = ScalarField()
+        if self._col_sdf is None:
+            f.kind = 0
+            f.value = kMaxD
+            return f
+        f.kind = 1
+        f.data = self._col_sdf.data_ptr()
+        f.res[:] = self.resolution
+        f.origin[:] = tuple(o + 0.5 * h for o, h in zip(self.origin,
+                                                        self.gridSpacing))
+        f.spacing[:] = self.gridSpacing
+        return f
+
+    def cfl(self, dt: float) -> float:
+        out = C.c_double(0.0)
+        g = (C.c_double * 3)(*self.params.gravity)
+        st = library().jetgpu_fluid_cfl_device(
+            self.solver.context(), C.byref(self.grid), _p(self.u), _p(self.v),
+            _p(self.w), float(dt), g, C.byref(out))
+        self.solver.check(st)
+        return out.value
+
+    def numberOfSubTimeSteps(self, dt: float) -> int:
+        return int(max(np.ceil(self.cfl(dt) / self.params.max_cfl), 1.0))
+
+    def advanceSubStep(self, dt: float):
+        f = self._col_field()
+        st = library().jetgpu_flip_substep_device(
+            self.solver.context(), C.byref(self.grid), self.pos.shape[0],
+            _p(self.pos), _p(self.vel), _p(self.u), _p(self.v), _p(self.w),
+            _p(self.sdf), C.byref(f),
+            C.byref(self._collider) if self._collider is not None else None,
+            C.byref(self._sphere) if self._sphere is not None else None,
+            C.byref(self.params), float(dt), C.byref(self.lastStats))
+        self.solver.check(st, allow=SOLVED)
+        self.subSteps += 1
+
+    def update(self, frameInterval: float):
+        """One frame (PhysicsAnimation::onUpdate's adaptive branch)."""
+        remaining = float(frameInterval)
+        eps = float(np.finfo(np.float64).eps)
+        while remaining > eps:
+            n = self.numberOfSubTimeSteps(remaining)
+            dt = remaining / float(n)
+            self.advanceSubStep(dt)
+            remaining -= dt
+            self.currentTimeInSeconds += dt
+        self.synchronize()  # the reference's update() returns when done
 
 
 class GridFractionalBoundaryConditionSolver3:

@@ -354,6 +354,49 @@ jetgpu_status jetgpu_build_particle_sdf(
     const double* pos, const jetgpu_scalar_field* collider_sdf,
     double max_cfl, double* sdf_out);
 
+/* Settings of a FLIP / PIC step (GridFluidSolver3 / FlipSolver3). */
+typedef struct jetgpu_flip_params {
+    double gravity[3];        /* GridFluidSolver3::gravity */
+    double max_cfl;           /* GridFluidSolver3::maxCfl */
+    int closed_domain_flags;  /* JETGPU_DIRECTION_* bits */
+    int flip;                 /* 1: FlipSolver3, 0: PicSolver3 */
+    double pic_blending;      /* FlipSolver3::picBlendingFactor */
+} jetgpu_flip_params;
+
+/* Fills the reference defaults (grid_fluid_solver3.h:269,
+ * flip_solver3.h:67): gravity (0,-9.8,0), maxCfl 5, all walls closed, FLIP,
+ * no PIC blending. */
+void jetgpu_flip_params_default(jetgpu_flip_params* params);
+
+/* GridFluidSolver3::cfl (src/jet/grid_fluid_solver3.cpp:360-378): the
+ * largest component (or 0) of the cell-centre velocity plus dt * gravity,
+ * times dt, over the smallest grid spacing; the adaptive sub-stepping of
+ * PhysicsAnimation::onUpdate (src/jet/physics_animation.cpp:98-122) takes
+ * max(ceil(cfl / maxCfl), 1) sub-steps. DEVICE velocity; synchronous. */
+jetgpu_status jetgpu_fluid_cfl_device(struct jetgpu_ctx* ctx,
+                                      const jetgpu_grid* grid, const double* u,
+                                      const double* v, const double* w,
+                                      double dt, const double gravity[3],
+                                      double* cfl);
+
+/* One GridFluidSolver3::onAdvanceTimeStep of FlipSolver3 / PicSolver3
+ * (src/jet/grid_fluid_solver3.cpp:179-210, src/jet/pic_solver3.cpp:63-112,
+ * src/jet/flip_solver3.cpp:27-99) on device-resident state: boundary
+ * conditions, P2G (+ FLIP snapshot), the particle SDF, extrapolation to air,
+ * gravity, the pressure projection of this library (its configured solver),
+ * G2P and particle advection with collisions, each stage in the
+ * reference's order. DEVICE pointers. pos/vel: AoS xyz doubles; u/v/w: the
+ * grid velocity (the solver's grid state, read and written); fluid_sdf: the
+ * particle SDF out (res cells). collider_sdf: colliderSdf() of the boundary
+ * solver (kind 0 = none); collider / sphere: NULL = none. stats: the
+ * pressure solve's. Returns the first error, or the pressure solve's status. */
+jetgpu_status jetgpu_flip_substep_device(
+    struct jetgpu_ctx* ctx, const jetgpu_grid* grid, long num_particles,
+    double* pos, double* vel, double* u, double* v, double* w,
+    double* fluid_sdf, const jetgpu_scalar_field* collider_sdf,
+    const jetgpu_collider* collider, const jetgpu_sphere* sphere,
+    const jetgpu_flip_params* params, double dt, jetgpu_solve_stats* stats);
+
 /* Host-pointer forms of the three transfers (copies inside the call). */
 jetgpu_status jetgpu_p2g(struct jetgpu_ctx* ctx, const jetgpu_grid* grid,
                          long num_particles, const double* pos,

@@ -195,6 +195,10 @@ class Oracle:
         L.orc_build_particle_sdf.argtypes = [
             C.POINTER(OrcGrid), C.c_long, _dp, C.POINTER(OrcField), C.c_double,
             _dp]
+        if hasattr(L, "orc_flip_run"):
+            L.orc_flip_run.argtypes = [
+                C.POINTER(OrcGrid), C.c_long, _dp, _dp, C.c_int, C.c_double,
+                C.c_double, C.c_int, _dp, C.c_int, C.POINTER(OrcMgParams)]
         if hasattr(L, "orc_quaternion_matrices"):
             L.orc_quaternion_matrices.argtypes = [_dp, _dp, _dp]
         if hasattr(L, "orc_sphere_collider_sdf"):
@@ -449,6 +453,22 @@ class Oracle:
                                         C.byref(f), float(max_cfl), _ptr(out))
         del keep
         return out
+
+    def flip_run(self, res, spacing, origin, pos, vel, frames, fps=60.0,
+                 max_cfl=5.0, closed=63, gravity=(0.0, -9.8, 0.0), flip=True,
+                 params: MgParams | None = None):
+        """Reference harness only: FlipSolver3 / PicSolver3 for `frames`
+        frames; returns the particles' (positions, velocities)."""
+        g = self._grid(res, spacing, origin)
+        pos = np.ascontiguousarray(pos, np.float64).copy()
+        vel = np.ascontiguousarray(vel, np.float64).copy()
+        prm = (params or MgParams()).c()
+        gr = np.ascontiguousarray(gravity, np.float64)
+        self.lib.orc_flip_run(C.byref(g), pos.shape[0], _ptr(pos), _ptr(vel),
+                              int(frames), float(fps), float(max_cfl),
+                              int(closed), _ptr(gr), int(bool(flip)),
+                              C.byref(prm))
+        return pos, vel
 
     def sphere_collider_sdf(self, res, spacing, origin, centre, radius):
         """Reference harness only: the collider SDF the reference builds for

@@ -179,6 +179,15 @@ void orc_build_particle_sdf(const orc_grid* g, long np, const double* pos,
                             const orc_field* collider_sdf, double max_cfl,
                             double* out);
 
+/* Reference harness only: FlipSolver3 (flip = 1) or PicSolver3 (0) with
+ * GridFractionalSinglePhasePressureSolver3 + FdmMgpcgSolver3(p), gravity g,
+ * maxCfl, closed walls and no collider, run for `frames` frames of 1/fps
+ * (update(Frame(i, 1/fps)), adaptive sub-steps) from the particles
+ * pos/vel, which are updated in place. */
+void orc_flip_run(const orc_grid* g, long np, double* pos, double* vel,
+                  int frames, double fps, double max_cfl, int closed,
+                  const double gravity[3], int flip, const orc_mg_params* p);
+
 /* Reference harness only: Transform3's orientation matrix and its inverse
  * for quaternion q = (w, x, y, z), row-major. */
 void orc_quaternion_matrices(const double q[4], double orient[9],

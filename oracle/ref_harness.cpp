@@ -542,6 +542,46 @@ void orc_build_particle_sdf(const orc_grid* g, long np, const double* pos,
     std::memcpy(out, acc.data(), sizeof(double) * res.x * res.y * res.z);
 }
 
+void orc_flip_run(const orc_grid* g, long np, double* pos, double* vel,
+                  int frames, double fps, double max_cfl, int closed,
+                  const double gravity[3], int flip, const orc_mg_params* p) {
+    Logging::mute();
+    const Size3 res(g->res[0], g->res[1], g->res[2]);
+    const Vector3D h(g->spacing[0], g->spacing[1], g->spacing[2]);
+    const Vector3D o(g->origin[0], g->origin[1], g->origin[2]);
+    std::shared_ptr<PicSolver3> s;
+    if (flip)
+        s = std::make_shared<FlipSolver3>(res, h, o);
+    else
+        s = std::make_shared<PicSolver3>(res, h, o);
+    auto particles = s->particleSystemData();
+    Array1<Vector3D> P(np), V(np), F(np);
+    for (long i = 0; i < np; ++i) {
+        P[i] = Vector3D(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]);
+        V[i] = Vector3D(vel[3 * i], vel[3 * i + 1], vel[3 * i + 2]);
+    }
+    particles->addParticles(P.constAccessor(), V.constAccessor(),
+                            F.constAccessor());
+    s->setGravity(Vector3D(gravity[0], gravity[1], gravity[2]));
+    s->setMaxCfl(max_cfl);
+    s->setClosedDomainBoundaryFlag(closed);
+    auto ps = std::make_shared<GridFractionalSinglePhasePressureSolver3>();
+    ps->setLinearSystemSolver(std::make_shared<FdmMgpcgSolver3>(
+        p->max_cg_iter, p->max_levels, p->restrict_iter, p->correct_iter,
+        p->coarsest_iter, p->final_iter, p->tolerance, p->sor,
+        p->red_black != 0));
+    s->setPressureSolver(ps);
+    for (Frame frame(0, 1.0 / fps); frame.index < frames; ++frame)
+        s->update(frame);
+    auto pp = s->particleSystemData()->positions();
+    auto vv = s->particleSystemData()->velocities();
+    for (long i = 0; i < np; ++i)
+        for (int d = 0; d < 3; ++d) {
+            pos[3 * i + d] = pp[i][d];
+            vel[3 * i + d] = vv[i][d];
+        }
+}
+
 void orc_quaternion_matrices(const double q[4], double orient[9],
                              double inv_orient[9]) {
     Transform3 t(Vector3D(), QuaternionD(q[0], q[1], q[2], q[3]));

@@ -33,6 +33,11 @@ Every fixture holds inputs and the reference's outputs for one small case:
   extrapolation into the collider for 3,000 particles on an anisotropic
   grid, with the reference's sphere-collider SDF (maxCfl 2.5) and with no
   collider (maxCfl 5).
+* flip_dam_break_24.npz — FlipSolver3 and PicSolver3 (the reference's
+  whole step: transfers, SDF, boundary conditions, gravity, pressure with
+  FdmMgpcgSolver3 at tolerance 1e-10, advection) for 3 frames of 1/60 s on
+  the 64^3 dam break's geometry at 24^3 (water box [0,.25]x[0,.75]x[0,1],
+  8 particles per cell from seed 0, closed walls, gravity (0,-9.8,0)).
 * rng_streams.npz — the first doubles of std::mt19937(seed) +
   std::uniform_real_distribution<double>(0,1) for seeds 0, 1, 2, produced by
   a C++ program compiled here.
@@ -266,6 +271,19 @@ def particle_sdf(ref):
          origin=np.array(org), pos=pos, collider_sdf=col, a=a, b=b)
 
 
+def flip_dam_break(ref):
+    n = 24
+    h = 1.0 / n
+    pos, vel = scenes.dam_break_particles(n, (0.25, 0.75, 1.0), seed=0)
+    p = oracle.MgParams(100, 5, 5, 5, 20, 20, 1e-10, 1.5, True)
+    fp, fv = ref.flip_run((n, n, n), (h, h, h), (0, 0, 0), pos, vel, 3,
+                          params=p)
+    pp, pv = ref.flip_run((n, n, n), (h, h, h), (0, 0, 0), pos, vel, 3,
+                          flip=False, params=p)
+    save("flip_dam_break_24.npz", flip_pos=fp, flip_vel=fv, pic_pos=pp,
+         pic_vel=pv)
+
+
 def rng_streams():
     with tempfile.TemporaryDirectory() as td:
         src = os.path.join(td, "rng.cpp")
@@ -292,6 +310,7 @@ def main():
     boundary(ref)
     particles(ref)
     particle_sdf(ref)
+    flip_dam_break(ref)
     rng_streams()
 
 
