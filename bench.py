@@ -51,6 +51,8 @@ def parse_args():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--n", type=int, default=256)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-flip", action="store_true",
+                    help="skip the whole-FLIP-frame measurements")
     ap.add_argument("--variants", default=",".join(VARIANTS),
                     help="comma-separated solver variants to run "
                          "(plain_mgpcg, mixed_mgpcg, learned_fpcg)")
@@ -371,6 +373,65 @@ def run_ours(args, rank, world, local, pg):
                 peak=pk, head=head, variants=variants)
 
 
+def run_flip(args, local, variant: str, frames: int):
+    """Whole FLIP frames on the GPU (jetgpu_flip_substep_device under the
+    reference's adaptive sub-stepping): the 256^3 dam break with the static
+    sphere obstacle (water box [0,.3]x[0,.8]x[0,1], 8 particles per cell
+    from seed 2, sphere r = .15 at (.6,.2,.5)) for `frames` frames of 1/60 s
+    after one warm-up frame, and the 64^3 dam break (box [0,.25]x[0,.75]x
+    [0,1], seed 0, closed box) for 60 frames. CUDA events on the library
+    stream; the particles never leave the device."""
+    import numpy as np
+    import torch
+    import jetgpu
+    from jetgpu import scenes
+    dev = torch.device("cuda", local)
+    out = {}
+    for tag, n, box, seed, sphere, nframes, warm in (
+            ("flip_256", args.n, (0.3, 0.8, 1.0), 2, True, frames, 1),
+            ("flip_64_dam_break", 64, (0.25, 0.75, 1.0), 0, False, 60, 0)):
+        prec, _ = VARIANTS[variant]
+        ps = jetgpu.FdmMgpcgSolver3(**solver_params(prec, "multigrid"),
+                                    device=local)
+        h = 1.0 / n
+        sim = jetgpu.FlipSolver3((n, n, n), h, (0, 0, 0), pressureSolver=ps,
+                                 device=local)
+        pos, _ = scenes.dam_break_particles(n, box, seed=seed)
+        sim.setParticles(pos)
+        if sphere:
+            X, Y, Z = scenes.cell_centres(n)
+            c, r = (0.6, 0.2, 0.5), 0.15
+            sdf = np.sqrt((X - c[0]) ** 2 + (Y - c[1]) ** 2 +
+                          (Z - c[2]) ** 2) - r
+            sim.setCollider(sdf, jetgpu.Collider.make(centre=c),
+                            jetgpu.Sphere.make(r))
+        for _ in range(warm):
+            sim.update(1.0 / 60)
+        stream = torch.cuda.ExternalStream(ps.stream(), device=dev)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        s0 = sim.subSteps
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(nframes):
+            sim.update(1.0 / 60)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1)
+        subs = sim.subSteps - s0
+        out[tag] = {
+            "grid": n, "particles": int(pos.shape[0]), "frames": nframes,
+            "substeps": subs, "ms_per_frame": round(ms / nframes, 3),
+            "ms_per_substep": round(ms / max(subs, 1), 3),
+            "substeps_per_s": round(1000.0 * subs / ms, 2),
+            "pressure_iterations_last": sim.lastStats.iterations,
+            "solver": variant, "collider": "sphere" if sphere else "none",
+        }
+        del sim
+        ps.close()
+    return out
+
+
 def cpu_reference():
     """The reference's CPU algorithm on this host: the compiled reference
     when it exists here, else the oracle port (bit-exact with it)."""
@@ -470,6 +531,9 @@ def main():
             print(json.dumps(line), flush=True)
         return
     r = run_ours(args, rank, world, local, pg)
+    flip = None
+    if not args.no_flip:
+        flip = run_flip(args, local, r["head"], frames=3)
     cb = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cb = cpu_baseline(args.n, steps=1)
@@ -514,6 +578,8 @@ def main():
                      "ms": round(k["total_ms"], 3)} for k in
                     sorted(r["profile"], key=lambda k: -k["total_ms"])],
     }
+    if flip is not None:
+        line["flip_steps"] = flip
     if cb is not None:
         line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores",
                                                    "kind", "sample")}

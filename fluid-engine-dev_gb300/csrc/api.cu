@@ -359,6 +359,7 @@ void jetgpu_destroy(jetgpu_ctx* c) {
     release(&c->pscratch);
     release(&c->bc_tmp);
     release(&c->bc_valid);
+    release(&c->bc_cls);
     release(&c->sdf_int);
     release(&c->sdf_dbl);
     release(&c->sdf_valid);

@@ -54,15 +54,19 @@ __device__ __forceinline__ void collider_vel(const ColliderDesc& c,
     o[2] = c.lin[2] + (c.ang[0] * r1 - r0 * c.ang[1]);
 }
 
-// CellCenteredScalarGrid3::sample (LinearArraySampler3::operator()).
-__device__ double sample_sdf(const FieldDesc& F, double x, double y,
-                             double z) {
+struct S3 {
+    Spacing s[3];
+};
+
+// CellCenteredScalarGrid3::sample (LinearArraySampler3::operator()); `fsp`
+// holds the field's spacings.
+__device__ double sample_sdf(const FieldDesc& F, const S3& fsp, double x,
+                             double y, double z) {
     if (F.kind == 0) return F.value;
     const Dims s{F.res[0], F.res[1], F.res[2]};
-    return sample_face<double, double>(F.data, s,
-                                       (x - F.origin[0]) / F.spacing[0],
-                                       (y - F.origin[1]) / F.spacing[1],
-                                       (z - F.origin[2]) / F.spacing[2]);
+    return sample_face<double, double>(F.data, s, fsp.s[0].div(x - F.origin[0]),
+                                       fsp.s[1].div(y - F.origin[1]),
+                                       fsp.s[2].div(z - F.origin[2]));
 }
 
 // std::max's rule (the first argument unless it is less than the second).
@@ -90,10 +94,16 @@ struct H3 {
     double v[3];
 };
 
-// K19a
-__global__ void k_bc_mark(FaceSet fs, int a, H3 h, FieldDesc sdf,
-                          ColliderDesc col, double* __restrict__ vel,
-                          unsigned char* __restrict__ valid) {
+// Face classes: bit 0 = the collider fraction 1 - fractionInsideSdf(phi at
+// the two ends of the face) is > 0 (a valid fluid face, :55-62); bit 1 = the
+// face position is inside the collider (:113). They depend only on the
+// collider SDF, so one pass serves every constrainVelocity call made while
+// the collider stands still (all calls of a sub-step).
+enum : unsigned char { kFaceValid = 1, kFaceInside = 2 };
+
+// K19a: classification.
+__global__ void k_bc_classify(FaceSet fs, int a, H3 h, FieldDesc sdf, S3 fsp,
+                              unsigned char* __restrict__ cls) {
     const Dims s = fs.s[a];
     const long n = s.count();
     for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < n;
@@ -107,17 +117,37 @@ __global__ void k_bc_mark(FaceSet fs, int a, H3 h, FieldDesc sdf,
             q0[d] = p[d] - off;
             q1[d] = p[d] + off;
         }
-        double frac = frac_inside_sdf(sample_sdf(sdf, q0[0], q0[1], q0[2]),
-                                      sample_sdf(sdf, q1[0], q1[1], q1[2]));
+        double frac =
+            frac_inside_sdf(sample_sdf(sdf, fsp, q0[0], q0[1], q0[2]),
+                            sample_sdf(sdf, fsp, q1[0], q1[1], q1[2]));
         frac = 1.0 - (frac < 0.0 ? 0.0 : (frac > 1.0 ? 1.0 : frac));
-        if (frac > 0.0) {
+        unsigned char f = frac > 0.0 ? kFaceValid : 0;
+        if (sample_sdf(sdf, fsp, p[0], p[1], p[2]) < 0.0) f |= kFaceInside;
+        cls[c] = f;
+    }
+}
+
+// K19a': faces that are not valid take the collider velocity (:63-67) and
+// start the extrapolation invalid.
+__global__ void k_bc_mark(FaceSet fs, int a, H3 h, ColliderDesc col,
+                          const unsigned char* __restrict__ cls,
+                          double* __restrict__ vel,
+                          unsigned char* __restrict__ valid) {
+    const Dims s = fs.s[a];
+    const long n = s.count();
+    for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < n;
+         c += (long)gridDim.x * blockDim.x) {
+        if (cls[c] & kFaceValid) {
             valid[c] = 1;
-        } else {
-            double cv[3];
-            collider_vel(col, p, cv);
-            vel[c] = cv[a];
-            valid[c] = 0;
+            continue;
         }
+        int i, j, k;
+        cell_ijk(c, s, i, j, k);
+        double p[3], cv[3];
+        face_pos(fs, a, h.v, i, j, k, p);
+        collider_vel(col, p, cv);
+        vel[c] = cv[a];
+        valid[c] = 0;
     }
 }
 
@@ -193,9 +223,11 @@ __device__ void sdf_gradient(const FieldDesc& F, const double inv[3],
     }
 }
 
-// K19c
-__global__ void k_bc_project(FaceSet fs, int a, H3 h, H3 inv, FieldDesc sdf,
-                             ColliderDesc col, const double* __restrict__ u,
+// K19c: faces inside the collider only (the others keep their value).
+__global__ void k_bc_project(FaceSet fs, int a, H3 h, S3 gsp, H3 inv,
+                             FieldDesc sdf, ColliderDesc col,
+                             const unsigned char* __restrict__ cls,
+                             const double* __restrict__ u,
                              const double* __restrict__ v,
                              const double* __restrict__ w,
                              double* __restrict__ tmp) {
@@ -204,21 +236,18 @@ __global__ void k_bc_project(FaceSet fs, int a, H3 h, H3 inv, FieldDesc sdf,
     const double* vel[3] = {u, v, w};
     for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < n;
          c += (long)gridDim.x * blockDim.x) {
+        if (!(cls[c] & kFaceInside)) continue;
         int i, j, k;
         cell_ijk(c, s, i, j, k);
         double p[3];
         face_pos(fs, a, h.v, i, j, k, p);
-        if (!(sample_sdf(sdf, p[0], p[1], p[2]) < 0.0)) {
-            tmp[c] = vel[a][c];
-            continue;
-        }
         double cv[3], fv[3], g[3];
         collider_vel(col, p, cv);
         for (int b = 0; b < 3; ++b)  // FaceCenteredGrid3::sample
-            fv[b] = sample_face<double, double>(vel[b], fs.s[b],
-                                                (p[0] - fs.o[b][0]) / h.v[0],
-                                                (p[1] - fs.o[b][1]) / h.v[1],
-                                                (p[2] - fs.o[b][2]) / h.v[2]);
+            fv[b] = sample_face<double, double>(
+                vel[b], fs.s[b], gsp.s[0].div(p[0] - fs.o[b][0]),
+                gsp.s[1].div(p[1] - fs.o[b][1]),
+                gsp.s[2].div(p[2] - fs.o[b][2]));
         sdf_gradient(sdf, inv.v, p, g);
         if (g[0] * g[0] + g[1] * g[1] + g[2] * g[2] > 0.0) {
             const double len = sqrt(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]);
@@ -243,8 +272,9 @@ __global__ void k_bc_project(FaceSet fs, int a, H3 h, H3 inv, FieldDesc sdf,
     }
 }
 
-// K19d
+// K19d: projected faces from the temporary; closed walls to zero.
 __global__ void k_bc_store(Dims s, int a, int closed,
+                           const unsigned char* __restrict__ cls,
                            const double* __restrict__ tmp,
                            double* __restrict__ vel) {
     const long n = s.count();
@@ -257,7 +287,10 @@ __global__ void k_bc_store(Dims s, int a, int closed,
         const int t = a == 0 ? i : (a == 1 ? j : k);
         const bool zero = ((closed & lo) && t == 0) ||
                           ((closed & hi) && t == ext - 1);
-        vel[c] = zero ? 0.0 : tmp[c];
+        if (zero)
+            vel[c] = 0.0;
+        else if (cls[c] & kFaceInside)
+            vel[c] = tmp[c];
     }
 }
 
@@ -293,10 +326,37 @@ unsigned char* extrapolate_passes(Ctx* c, Dims s, double* data,
 
 }  // namespace
 
-jetgpu_status constrain_velocity(Ctx* c, const GridDesc& g, double* u,
-                                 double* v, double* w, const FieldDesc& sdf,
-                                 const jetgpu_collider* col, int closed,
-                                 unsigned depth) {
+jetgpu_status bc_classify(Ctx* c, const GridDesc& g, const FieldDesc& sdf) {
+    const FaceSet fs = face_set(g);
+    size_t nf = 0;
+    for (int a = 0; a < 3; ++a) nf += (size_t)fs.s[a].count();
+    if (c->bc_cls_cap < nf) {
+        JG_CUDA(c, cudaStreamSynchronize(c->stream));
+        if (c->bc_cls) cudaFree(c->bc_cls);
+        c->bc_cls = nullptr;
+        c->bc_cls_cap = 0;
+        JG_CUDA(c, cudaMalloc((void**)&c->bc_cls, nf));
+        c->bc_cls_cap = nf;
+    }
+    H3 h{{g.spacing[0], g.spacing[1], g.spacing[2]}};
+    S3 fsp{{make_spacing(sdf.kind == 1 ? sdf.spacing[0] : 1.0),
+            make_spacing(sdf.kind == 1 ? sdf.spacing[1] : 1.0),
+            make_spacing(sdf.kind == 1 ? sdf.spacing[2] : 1.0)}};
+    size_t off = 0;
+    for (int a = 0; a < 3; ++a) {
+        const long n = fs.s[a].count();
+        Prof pr(c, K_BOUNDARY, 1.0 * n);
+        k_bc_classify<<<blocks_for(n, kThreads, c->num_sms * 8), kThreads, 0,
+                        c->stream>>>(fs, a, h, sdf, fsp, c->bc_cls + off);
+        off += n;
+    }
+    JG_CUDA(c, cudaGetLastError());
+    return JETGPU_OK;
+}
+
+jetgpu_status bc_apply(Ctx* c, const GridDesc& g, double* u, double* v,
+                       double* w, const FieldDesc& sdf,
+                       const jetgpu_collider* col, int closed, unsigned depth) {
     const FaceSet fs = face_set(g);
     size_t nmax = 0;
     for (int a = 0; a < 3; ++a)
@@ -313,6 +373,8 @@ jetgpu_status constrain_velocity(Ctx* c, const GridDesc& g, double* u,
         cd.friction = col->friction;
     }
     H3 h{{g.spacing[0], g.spacing[1], g.spacing[2]}};
+    S3 gsp{{make_spacing(g.spacing[0]), make_spacing(g.spacing[1]),
+            make_spacing(g.spacing[2])}};
     H3 inv{{0, 0, 0}};
     if (sdf.kind == 1)
         for (int d = 0; d < 3; ++d) inv.v[d] = 1.0 / sdf.spacing[d];
@@ -320,33 +382,46 @@ jetgpu_status constrain_velocity(Ctx* c, const GridDesc& g, double* u,
     double* tmp[3];
     unsigned char* va[3];
     unsigned char* vb[3];
+    const unsigned char* cls[3];
+    size_t off = 0;
     for (int a = 0; a < 3; ++a) {
         tmp[a] = c->bc_tmp + a * nmax;
         va[a] = c->bc_valid + a * nmax;
         vb[a] = c->bc_valid + (3 + a) * nmax;
+        cls[a] = c->bc_cls + off;
+        off += (size_t)fs.s[a].count();
     }
     for (int a = 0; a < 3; ++a) {
         const long n = fs.s[a].count();
-        Prof pr(c, K_BOUNDARY, 17.0 * n);
-        k_bc_mark<<<blocks_for(n, kThreads, c->num_sms * 8), kThreads, 0, c->stream>>>(
-            fs, a, h, sdf, cd, vel[a], va[a]);
+        Prof pr(c, K_BOUNDARY, 2.0 * n);
+        k_bc_mark<<<blocks_for(n, kThreads, c->num_sms * 8), kThreads, 0,
+                    c->stream>>>(fs, a, h, cd, cls[a], vel[a], va[a]);
     }
     for (int a = 0; a < 3; ++a)
         extrapolate_passes(c, fs.s[a], vel[a], va[a], vb[a], depth);
     for (int a = 0; a < 3; ++a) {
         const long n = fs.s[a].count();
-        Prof pr(c, K_BOUNDARY, 16.0 * n);
-        k_bc_project<<<blocks_for(n, kThreads, c->num_sms * 8), kThreads, 0, c->stream>>>(
-            fs, a, h, inv, sdf, cd, u, v, w, tmp[a]);
+        Prof pr(c, K_BOUNDARY, 1.0 * n);
+        k_bc_project<<<blocks_for(n, kThreads, c->num_sms * 8), kThreads, 0,
+                       c->stream>>>(fs, a, h, gsp, inv, sdf, cd, cls[a], u, v,
+                                    w, tmp[a]);
     }
     for (int a = 0; a < 3; ++a) {
         const long n = fs.s[a].count();
-        Prof pr(c, K_BOUNDARY, 16.0 * n);
-        k_bc_store<<<blocks_for(n, kThreads, c->num_sms * 8), kThreads, 0, c->stream>>>(
-            fs.s[a], a, closed, tmp[a], vel[a]);
+        Prof pr(c, K_BOUNDARY, 1.0 * n);
+        k_bc_store<<<blocks_for(n, kThreads, c->num_sms * 8), kThreads, 0,
+                     c->stream>>>(fs.s[a], a, closed, cls[a], tmp[a], vel[a]);
     }
     JG_CUDA(c, cudaGetLastError());
     return JETGPU_OK;
+}
+
+jetgpu_status constrain_velocity(Ctx* c, const GridDesc& g, double* u,
+                                 double* v, double* w, const FieldDesc& sdf,
+                                 const jetgpu_collider* col, int closed,
+                                 unsigned depth) {
+    if (jetgpu_status s = bc_classify(c, g, sdf)) return s;
+    return bc_apply(c, g, u, v, w, sdf, col, closed, depth);
 }
 
 jetgpu_status extrapolate_region(Ctx* c, Dims s, double* data,

@@ -150,6 +150,8 @@ struct Ctx {
     size_t bc_cap = 0;
     double* bc_tmp = nullptr;
     unsigned char* bc_valid = nullptr;
+    size_t bc_cls_cap = 0;
+    unsigned char* bc_cls = nullptr;  // face classes of the last bc_classify
 
     // Device-resident FLIP step scratch (flip.cu): P2G markers, FLIP
     // snapshot, collider face velocities, the CFL maximum.
@@ -290,6 +292,14 @@ jetgpu_status constrain_velocity(Ctx* c, const GridDesc& g, double* u,
                                  double* v, double* w, const FieldDesc& sdf,
                                  const jetgpu_collider* col, int closed,
                                  unsigned depth);
+// The two halves of constrain_velocity: bc_classify evaluates the collider
+// SDF at every face (cached in ctx->bc_cls), bc_apply does the rest with
+// those classes; a caller whose collider does not move between calls
+// classifies once.
+jetgpu_status bc_classify(Ctx* c, const GridDesc& g, const FieldDesc& sdf);
+jetgpu_status bc_apply(Ctx* c, const GridDesc& g, double* u, double* v,
+                       double* w, const FieldDesc& sdf,
+                       const jetgpu_collider* col, int closed, unsigned depth);
 jetgpu_status extrapolate_region(Ctx* c, Dims s, double* data,
                                  const unsigned char* valid, unsigned iters);
 

@@ -165,8 +165,11 @@ jetgpu_status flip_substep(Ctx* c, const GridDesc& g, long np, double* pos,
     const int res3[3][3] = {{fs.s[0].x, fs.s[0].y, fs.s[0].z},
                             {fs.s[1].x, fs.s[1].y, fs.s[1].z},
                             {fs.s[2].x, fs.s[2].y, fs.s[2].z}};
+    // The collider stands still within a sub-step: its faces are classified
+    // once for the five boundary-condition passes.
+    if (jetgpu_status s = bc_classify(c, g, col_sdf)) return s;
     auto bc = [&]() {
-        return constrain_velocity(c, g, u, v, w, col_sdf, col, closed, depth);
+        return bc_apply(c, g, u, v, w, col_sdf, col, closed, depth);
     };
     auto to_air = [&]() -> jetgpu_status {  // extrapolateVelocityToAir
         for (int a = 0; a < 3; ++a) {

@@ -9,10 +9,28 @@
 // face arrays (src/jet/face_centered_grid3.cpp:428-445).
 #pragma once
 
+#include <cmath>
+
 #include "common.cuh"
 
 namespace jg {
 namespace smp {
+
+// x / h for a grid spacing h. IEEE division and multiplication both return
+// the correctly rounded exact result, and when h is a power of two x / h and
+// x * (1 / h) are the same real number (x * 2^-k), so the multiply gives the
+// reference's quotient bit for bit at a fraction of an FP64 divide's cost.
+struct Spacing {
+    double h, inv;
+    int pow2;
+    __device__ __forceinline__ double div(double x) const {
+        return pow2 ? x * inv : x / h;
+    }
+};
+inline Spacing make_spacing(double h) {
+    int e = 0;
+    return Spacing{h, 1.0 / h, std::frexp(h, &e) == 0.5 ? 1 : 0};
+}
 
 template <typename T>
 __device__ __forceinline__ void bary(T x, int iHigh, int* i, T* f) {

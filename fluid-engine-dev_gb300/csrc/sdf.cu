@@ -37,6 +37,7 @@ struct SdfGeom {
     double band, band2, radius;
     int win[3];      // bin window half-width per axis
     float slack;     // FP32 error bound on a squared distance near the band
+    double inner2;   // (1.5 min h)^2, less a margin: the 3x3x3 bins' reach
 };
 
 __device__ __forceinline__ int bin_axis(double p, double o, double h, int n) {
@@ -181,25 +182,48 @@ __global__ void k_sdf_cells(SdfGeom G, const int* __restrict__ off,
         const int z0 = max(k - G.win[2], 0), z1 = min(k + G.win[2], G.n.z - 1);
         const int y0 = max(j - G.win[1], 0), y1 = min(j + G.win[1], G.n.y - 1);
         const int x0 = max(i - G.win[0], 0), x1 = min(i + G.win[0], G.n.x - 1);
-        for (int bz = z0; bz <= z1; ++bz)
-            for (int by = y0; by <= y1; ++by) {
-                const long row = (long)G.n.x * (by + (long)G.n.y * bz);
-                const int e0 = off[row + x0], e1 = off[row + x1 + 1];
-                for (int e = e0; e < e1; ++e) {
-                    const float4 p = sf[e];
-                    const float dx = p.x - cx, dy = p.y - cy, dz = p.z - cz;
-                    const float d2f = dx * dx + dy * dy + dz * dz;
-                    if (d2f > best_f + 2.0f * G.slack) continue;
-                    const double* x = sp + 3 * (long)e;
-                    const double d0 = x[0] - pt[0], d1 = x[1] - pt[1],
-                                 d2 = x[2] - pt[2];
-                    const double dd = d0 * d0 + d1 * d1 + d2 * d2;
-                    if (dd <= G.band2 && dd < best) {
-                        best = dd;
-                        best_f = fminf(best_f, d2f);
-                    }
+        // Particles of bins e0 .. e1 (a run of one row).
+        auto scan = [&](int e0, int e1) {
+            for (int e = e0; e < e1; ++e) {
+                const float4 p = sf[e];
+                const float dx = p.x - cx, dy = p.y - cy, dz = p.z - cz;
+                const float d2f = dx * dx + dy * dy + dz * dz;
+                if (d2f > best_f + 2.0f * G.slack) continue;
+                const double* x = sp + 3 * (long)e;
+                const double d0 = x[0] - pt[0], d1 = x[1] - pt[1],
+                             d2 = x[2] - pt[2];
+                const double dd = d0 * d0 + d1 * d1 + d2 * d2;
+                if (dd <= G.band2 && dd < best) {
+                    best = dd;
+                    best_f = fminf(best_f, d2f);
                 }
             }
+        };
+        // The 3x3x3 bins around the cell first. A particle in any other bin
+        // is at least 1.5 min(h) away along some axis (bins are cells, the
+        // centre sits mid-cell; clamping moves outside particles inwards
+        // only), so when the nearest found is closer than that the rest of
+        // the window cannot change the minimum.
+        const int ix0 = max(i - 1, 0), ix1 = min(i + 1, G.n.x - 1);
+        const int iy0 = max(j - 1, 0), iy1 = min(j + 1, G.n.y - 1);
+        const int iz0 = max(k - 1, 0), iz1 = min(k + 1, G.n.z - 1);
+        for (int bz = iz0; bz <= iz1; ++bz)
+            for (int by = iy0; by <= iy1; ++by) {
+                const long row = (long)G.n.x * (by + (long)G.n.y * bz);
+                scan(off[row + ix0], off[row + ix1 + 1]);
+            }
+        if (!(best < G.inner2)) {
+            for (int bz = z0; bz <= z1; ++bz)
+                for (int by = y0; by <= y1; ++by) {
+                    const long row = (long)G.n.x * (by + (long)G.n.y * bz);
+                    if (bz >= iz0 && bz <= iz1 && by >= iy0 && by <= iy1) {
+                        if (x0 < ix0) scan(off[row + x0], off[row + ix0]);
+                        if (ix1 < x1) scan(off[row + ix1 + 1], off[row + x1 + 1]);
+                    } else {
+                        scan(off[row + x0], off[row + x1 + 1]);
+                    }
+                }
+        }
         double minDist = G.band;
         if (best <= G.band2) {
             const double dist = sqrt(best);
@@ -264,6 +288,9 @@ jetgpu_status build_particle_sdf(Ctx* c, const GridDesc& g, long np,
     G.band2 = G.band * G.band;
     for (int d = 0; d < 3; ++d)
         G.win[d] = (int)std::ceil(G.band / G.h[d]);
+    const double minH = std::min(std::min(G.h[0], G.h[1]), G.h[2]);
+    // The margin covers the rounding of the bin index floor((x - o) / h).
+    G.inner2 = (1.5 * minH) * (1.5 * minH) * (1.0 - 1e-9);
     // FP32 error of a squared distance d^2 <= band^2 + slack between a
     // particle and a centre whose offsets from the origin are at most
     // L = extent + band: each rounded offset is off by <= u L (u = 2^-24), a

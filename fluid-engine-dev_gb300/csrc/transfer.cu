@@ -240,8 +240,8 @@ __global__ void k_move_particles(long np, double* __restrict__ pos,
                                  double* __restrict__ vel, FaceSet fs,
                                  const double* __restrict__ u,
                                  const double* __restrict__ v,
-                                 const double* __restrict__ w, double hx,
-                                 double hy, double hz, double sdt,
+                                 const double* __restrict__ w, Spacing hx,
+                                 Spacing hy, Spacing hz, double sdt,
                                  unsigned nsub, int closed, double lo0,
                                  double lo1, double lo2, double hi0,
                                  double hi1, double hi2, SphereDesc S) {
@@ -256,14 +256,14 @@ __global__ void k_move_particles(long np, double* __restrict__ pos,
             double v0[3], mid[3], vm[3];
             for (int a = 0; a < 3; ++a)
                 v0[a] = sample_face<double, double>(
-                    grid[a], fs.s[a], (p0[0] - fs.o[a][0]) / hx,
-                    (p0[1] - fs.o[a][1]) / hy, (p0[2] - fs.o[a][2]) / hz);
+                    grid[a], fs.s[a], hx.div(p0[0] - fs.o[a][0]),
+                    hy.div(p0[1] - fs.o[a][1]), hz.div(p0[2] - fs.o[a][2]));
             const double hs = 0.5 * sdt;
             for (int d = 0; d < 3; ++d) mid[d] = p0[d] + hs * v0[d];
             for (int a = 0; a < 3; ++a)
                 vm[a] = sample_face<double, double>(
-                    grid[a], fs.s[a], (mid[0] - fs.o[a][0]) / hx,
-                    (mid[1] - fs.o[a][1]) / hy, (mid[2] - fs.o[a][2]) / hz);
+                    grid[a], fs.s[a], hx.div(mid[0] - fs.o[a][0]),
+                    hy.div(mid[1] - fs.o[a][1]), hz.div(mid[2] - fs.o[a][2]));
             for (int d = 0; d < 3; ++d) p1[d] = p0[d] + sdt * vm[d];
             for (int d = 0; d < 3; ++d) p0[d] = p1[d];
         }
@@ -321,8 +321,9 @@ jetgpu_status move_particles(Ctx* c, const GridDesc& g, long np, double* pos,
         Prof pr(c, K_MOVE, 96.0 * np);
         k_move_particles<<<blocks_for(np, kThreads, c->num_sms * 16), kThreads,
                            0, c->stream>>>(
-            np, pos, vel, fs, u, v, w, g.spacing[0], g.spacing[1],
-            g.spacing[2], dt / nsub, nsub, closed, lo[0], lo[1], lo[2], hi[0],
+            np, pos, vel, fs, u, v, w, make_spacing(g.spacing[0]),
+            make_spacing(g.spacing[1]), make_spacing(g.spacing[2]), dt / nsub,
+            nsub, closed, lo[0], lo[1], lo[2], hi[0],
             hi[1], hi[2], S);
     }
     JG_CUDA(c, cudaGetLastError());
@@ -352,12 +353,14 @@ jetgpu_status p2g(Ctx* c, const GridDesc& g, long np, const double* pos,
         JG_CUDA(c, cudaMemsetAsync(grid[a], 0, n[a] * sizeof(double), c->stream));
         if (mark[a]) JG_CUDA(c, cudaMemsetAsync(mark[a], 0, n[a], c->stream));
     }
-    if (np > 0)
+    if (np > 0) {
+        Prof pr(c, K_P2G, 48.0 * np + 2.0 * 3 * 8.0 * (n[0] + n[1] + n[2]));
         k_p2g_scatter<<<blocks_for(np, kThreads, c->num_sms * 16), kThreads, 0,
                         c->stream>>>(np, pos, vel, fs, 1.0 / g.spacing[0],
                                      1.0 / g.spacing[1], 1.0 / g.spacing[2],
                                      u, v, w, wsum, wsum + n[0],
                                      wsum + n[0] + n[1], mu, mv, mw);
+    }
     long off = 0;
     for (int a = 0; a < 3; ++a) {
         k_p2g_normalize<<<blocks_for(n[a]), kThreads, 0, c->stream>>>(
@@ -378,11 +381,13 @@ jetgpu_status g2p_flip(Ctx* c, const GridDesc& g, long np, const double* pos,
     for (int a = 0; a < 3; ++a)
         k_flip_delta<<<blocks_for(fs.s[a].count()), kThreads, 0, c->stream>>>(
             grid[a], snap[a], fs.s[a].count());
-    if (np > 0)
+    if (np > 0) {
+        Prof pr(c, K_G2P, 48.0 * np);
         k_g2p_flip<<<blocks_for(np), kThreads, 0, c->stream>>>(
             np, pos, vel, fs, (float)g.spacing[0], (float)g.spacing[1],
             (float)g.spacing[2], su, sv, sw, u, v, w, g.spacing[0],
             g.spacing[1], g.spacing[2], blend);
+    }
     JG_CUDA(c, cudaGetLastError());
     return JETGPU_OK;
 }
