@@ -18,6 +18,13 @@ Arms:
   (about 10 s on 8 cores); the reference's MGPCG breaks down at 256^3 before
   1e-6, and the residual it reaches is reported.
 
+Also in the line (same rules, not the headline): `flip_steps` — whole
+FLIP frames resident on the GPU (transfers, particle SDF, boundary
+conditions, gravity, pressure, advection under the reference's adaptive
+sub-stepping) for the 256^3 dam break with the sphere (about 32M particles)
+and the 64^3 dam break (60 frames); `smoke_512_pressure` — the projection of
+the 512^3 smoke plume (all fluid, closed box).
+
 Timing: W warm-up solves, then K solves bracketed by a barrier and
 synchronize, timed with CUDA events on the library's own stream, max over
 ranks. The working set (0.5 GB of FP64 inputs, 3+ GB of solver state) is
@@ -53,6 +60,8 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-flip", action="store_true",
                     help="skip the whole-FLIP-frame measurements")
+    ap.add_argument("--no-smoke", action="store_true",
+                    help="skip the 512^3 smoke-plume projection")
     ap.add_argument("--variants", default=",".join(VARIANTS),
                     help="comma-separated solver variants to run "
                          "(plain_mgpcg, mixed_mgpcg, learned_fpcg)")
@@ -432,6 +441,64 @@ def run_flip(args, local, variant: str, frames: int):
     return out
 
 
+def run_smoke(args, local, variant: str, steps: int = 3):
+    """The projection of the 512^3 buoyant smoke plume (GridSmokeSolver3:
+    all fluid, closed box; the source sphere r = .05 at (.5,.1,.5) pushing
+    upward), one device-resident pressure solve per step to the same 1e-6
+    relative true residual, after one warm-up solve."""
+    import torch
+    import jetgpu
+    n = 512
+    h = 1.0 / n
+    dev = torch.device("cuda", local)
+    prec, _ = VARIANTS[variant]
+    solver = jetgpu.FdmMgpcgSolver3(**solver_params(prec, "multigrid"),
+                                    device=local)
+    f64 = dict(dtype=torch.float64, device=dev)
+    u = torch.zeros((n, n, n + 1), **f64)
+    w = torch.zeros((n + 1, n, n), **f64)
+    c = (torch.arange(n, **f64) + 0.5) * h
+    yf = torch.arange(n + 1, **f64) * h
+    r2 = ((c[None, None, :] - 0.5) ** 2 + (yf[None, :, None] - 0.1) ** 2 +
+          (c[:, None, None] - 0.5) ** 2)
+    v = (r2 < 0.05 ** 2).to(torch.float64)
+    v[:, 0, :] = 0
+    v[:, -1, :] = 0
+    del r2
+    out = [torch.empty_like(a) for a in (u, v, w)]
+    grid = jetgpu.Grid()
+    grid.res[:] = (n, n, n)
+    grid.spacing[:] = (h, h, h)
+    grid.origin[:] = (0, 0, 0)
+    fb, ff = jetgpu.ScalarField(), jetgpu.ScalarField()
+    fb.kind, fb.value = 0, jetgpu.kMaxD
+    ff.kind, ff.value = 0, -jetgpu.kMaxD
+    stats = jetgpu.SolveStats()
+
+    def solve():
+        jetgpu.solve_pressure_device(solver, grid, u, v, w, fb, ff, *out,
+                                     None, stats=stats)
+
+    solve()
+    stream = torch.cuda.ExternalStream(solver.stream(), device=dev)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(steps):
+        solve()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    res = {"grid": n, "cells": n ** 3, "ms_per_solve": round(ms, 3),
+           "solves": steps, "iterations_per_solve": stats.iterations,
+           "relative_residual": stats.relative_residual,
+           "setup_ms": round(stats.setup_ms, 3), "solver": variant,
+           "system": "all fluid, closed box (pure Neumann)"}
+    solver.close()
+    return res
+
+
 def cpu_reference():
     """The reference's CPU algorithm on this host: the compiled reference
     when it exists here, else the oracle port (bit-exact with it)."""
@@ -534,6 +601,9 @@ def main():
     flip = None
     if not args.no_flip:
         flip = run_flip(args, local, r["head"], frames=3)
+    smoke = None
+    if not args.no_smoke:
+        smoke = run_smoke(args, local, r["head"])
     cb = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cb = cpu_baseline(args.n, steps=1)
@@ -580,6 +650,8 @@ def main():
     }
     if flip is not None:
         line["flip_steps"] = flip
+    if smoke is not None:
+        line["smoke_512_pressure"] = smoke
     if cb is not None:
         line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores",
                                                    "kind", "sample")}
