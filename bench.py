@@ -416,6 +416,18 @@ def run_flip(args, local, variant: str, frames: int):
                             jetgpu.Sphere.make(r))
         for _ in range(warm):
             sim.update(1.0 / 60)
+        kernels = None
+        if tag == "flip_256":
+            # Per-kernel-class split of one profiled frame (events around
+            # every launch on the library stream), then the timed frames.
+            ps.profile(True)
+            s0 = sim.subSteps
+            sim.update(1.0 / 60)
+            prof = ps.profile_read()
+            ps.profile(False)
+            ns = max(sim.subSteps - s0, 1)
+            kernels = {k["name"]: round(k["total_ms"] / ns, 3) for k in
+                       sorted(prof, key=lambda k: -k["total_ms"])}
         stream = torch.cuda.ExternalStream(ps.stream(), device=dev)
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
@@ -436,6 +448,8 @@ def run_flip(args, local, variant: str, frames: int):
             "pressure_iterations_last": sim.lastStats.iterations,
             "solver": variant, "collider": "sphere" if sphere else "none",
         }
+        if kernels is not None:
+            out[tag]["ms_per_substep_by_kernel_class"] = kernels
         del sim
         ps.close()
     return out
