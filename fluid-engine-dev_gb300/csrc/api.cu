@@ -360,6 +360,8 @@ void jetgpu_destroy(jetgpu_ctx* c) {
     release(&c->bc_tmp);
     release(&c->bc_valid);
     release(&c->bc_cls);
+    release(&c->bc_list);
+    release(&c->bc_cnt);
     release(&c->sdf_int);
     release(&c->sdf_dbl);
     release(&c->sdf_valid);

@@ -101,9 +101,31 @@ struct H3 {
 // the collider stands still (all calls of a sub-step).
 enum : unsigned char { kFaceValid = 1, kFaceInside = 2 };
 
-// K19a: classification.
+// Appends face c to a list when `take`; one atomic per warp.
+__device__ __forceinline__ void push(int* __restrict__ lst,
+                                     unsigned* __restrict__ cnt, long c,
+                                     bool take) {
+    const unsigned active = __activemask();
+    const unsigned m = __ballot_sync(active, take);
+    if (!m) return;
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(m) - 1;
+    unsigned base = 0;
+    if (lane == leader) base = atomicAdd(cnt, (unsigned)__popc(m));
+    base = __shfl_sync(active, base, leader);
+    if (take) lst[base + __popc(m & ((1u << lane) - 1u))] = (int)c;
+}
+
+// K19a: classification, and the lists of the faces later passes touch:
+// those without a valid fraction (collider velocity, then extrapolated) and
+// those inside the collider (projected). List order is arbitrary; every
+// pass over a list is order-independent.
 __global__ void k_bc_classify(FaceSet fs, int a, H3 h, FieldDesc sdf, S3 fsp,
-                              unsigned char* __restrict__ cls) {
+                              unsigned char* __restrict__ cls,
+                              int* __restrict__ inv_list,
+                              unsigned* __restrict__ inv_cnt,
+                              int* __restrict__ in_list,
+                              unsigned* __restrict__ in_cnt) {
     const Dims s = fs.s[a];
     const long n = s.count();
     for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < n;
@@ -124,30 +146,68 @@ __global__ void k_bc_classify(FaceSet fs, int a, H3 h, FieldDesc sdf, S3 fsp,
         unsigned char f = frac > 0.0 ? kFaceValid : 0;
         if (sample_sdf(sdf, fsp, p[0], p[1], p[2]) < 0.0) f |= kFaceInside;
         cls[c] = f;
+        push(inv_list, inv_cnt, c, !(f & kFaceValid));
+        push(in_list, in_cnt, c, (f & kFaceInside) != 0);
     }
 }
 
-// K19a': faces that are not valid take the collider velocity (:63-67) and
-// start the extrapolation invalid.
+// K19a': the faces without a valid fraction take the collider velocity
+// (:63-67) and start the extrapolation invalid.
 __global__ void k_bc_mark(FaceSet fs, int a, H3 h, ColliderDesc col,
-                          const unsigned char* __restrict__ cls,
+                          const int* __restrict__ lst,
+                          const unsigned* __restrict__ cnt,
                           double* __restrict__ vel,
-                          unsigned char* __restrict__ valid) {
+                          unsigned char* __restrict__ st0) {
     const Dims s = fs.s[a];
-    const long n = s.count();
-    for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < n;
-         c += (long)gridDim.x * blockDim.x) {
-        if (cls[c] & kFaceValid) {
-            valid[c] = 1;
-            continue;
-        }
+    const long m = *cnt;
+    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < m;
+         t += (long)gridDim.x * blockDim.x) {
+        const long c = lst[t];
         int i, j, k;
         cell_ijk(c, s, i, j, k);
         double p[3], cv[3];
         face_pos(fs, a, h.v, i, j, k, p);
         collider_vel(col, p, cv);
         vel[c] = cv[a];
-        valid[c] = 0;
+        st0[c] = 0;
+    }
+}
+
+// K19b': one extrapolation pass over the listed (initially invalid) faces.
+// A face outside the list is valid by its class; a listed face is valid
+// when its state byte says so.
+__global__ void k_extrapolate_list(Dims s, const int* __restrict__ lst,
+                                   const unsigned* __restrict__ cnt,
+                                   double* __restrict__ data,
+                                   const unsigned char* __restrict__ cls,
+                                   const unsigned char* __restrict__ st0,
+                                   unsigned char* __restrict__ st1) {
+    const long m = *cnt;
+    const long sy = s.x, sz = (long)s.x * s.y;
+    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < m;
+         t += (long)gridDim.x * blockDim.x) {
+        const long c = lst[t];
+        if (st0[c]) {
+            st1[c] = 1;
+            continue;
+        }
+        int i, j, k;
+        cell_ijk(c, s, i, j, k);
+        auto ok = [&](long q) { return (cls[q] & kFaceValid) || st0[q]; };
+        double sum = 0.0;
+        unsigned count = 0;
+        if (i + 1 < s.x && ok(c + 1)) { sum += data[c + 1]; ++count; }
+        if (i > 0 && ok(c - 1)) { sum += data[c - 1]; ++count; }
+        if (j + 1 < s.y && ok(c + sy)) { sum += data[c + sy]; ++count; }
+        if (j > 0 && ok(c - sy)) { sum += data[c - sy]; ++count; }
+        if (k + 1 < s.z && ok(c + sz)) { sum += data[c + sz]; ++count; }
+        if (k > 0 && ok(c - sz)) { sum += data[c - sz]; ++count; }
+        if (count > 0) {
+            data[c] = sum / (double)count;
+            st1[c] = 1;
+        } else {
+            st1[c] = 0;
+        }
     }
 }
 
@@ -223,20 +283,22 @@ __device__ void sdf_gradient(const FieldDesc& F, const double inv[3],
     }
 }
 
-// K19c: faces inside the collider only (the others keep their value).
+// K19c: the listed faces inside the collider (the others keep their
+// value); tmp[t] receives the projection of list entry t.
 __global__ void k_bc_project(FaceSet fs, int a, H3 h, S3 gsp, H3 inv,
                              FieldDesc sdf, ColliderDesc col,
-                             const unsigned char* __restrict__ cls,
+                             const int* __restrict__ lst,
+                             const unsigned* __restrict__ cnt,
                              const double* __restrict__ u,
                              const double* __restrict__ v,
                              const double* __restrict__ w,
                              double* __restrict__ tmp) {
     const Dims s = fs.s[a];
-    const long n = s.count();
+    const long m = *cnt;
     const double* vel[3] = {u, v, w};
-    for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < n;
-         c += (long)gridDim.x * blockDim.x) {
-        if (!(cls[c] & kFaceInside)) continue;
+    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < m;
+         t += (long)gridDim.x * blockDim.x) {
+        const long c = lst[t];
         int i, j, k;
         cell_ijk(c, s, i, j, k);
         double p[3];
@@ -265,32 +327,44 @@ __global__ void k_bc_project(FaceSet fs, int a, H3 h, S3 gsp, H3 inv,
                 vt[1] = vt[1] * sc;
                 vt[2] = vt[2] * sc;
             }
-            tmp[c] = vt[a] + cv[a];
+            tmp[t] = vt[a] + cv[a];
         } else {
-            tmp[c] = cv[a];
+            tmp[t] = cv[a];
         }
     }
 }
 
-// K19d: projected faces from the temporary; closed walls to zero.
-__global__ void k_bc_store(Dims s, int a, int closed,
-                           const unsigned char* __restrict__ cls,
+// K19d: the projected faces from the temporary (:177-187) ...
+__global__ void k_bc_store(const int* __restrict__ lst,
+                           const unsigned* __restrict__ cnt,
                            const double* __restrict__ tmp,
                            double* __restrict__ vel) {
-    const long n = s.count();
-    const int lo = 1 << (2 * a), hi = 1 << (2 * a + 1);
+    const long m = *cnt;
+    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < m;
+         t += (long)gridDim.x * blockDim.x)
+        vel[lst[t]] = tmp[t];
+}
+
+// ... then zero on the closed domain walls (:189-232): the two planes of
+// axis a, plane 0 when `lo`, the last when `hi`.
+__global__ void k_bc_walls(Dims s, int a, int lo, int hi,
+                           double* __restrict__ vel) {
+    const int d1 = a == 0 ? s.y : s.x;            // the plane's two extents
+    const int d2 = a == 2 ? s.y : s.z;
     const int ext = a == 0 ? s.x : (a == 1 ? s.y : s.z);
-    for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < n;
-         c += (long)gridDim.x * blockDim.x) {
+    const long P = (long)d1 * d2;
+    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < 2 * P;
+         t += (long)gridDim.x * blockDim.x) {
+        const int side = (int)(t / P);
+        if ((side == 0 && !lo) || (side == 1 && !hi)) continue;
+        const long q = t - side * P;
+        const int p1 = (int)(q % d1), p2 = (int)(q / d1);
+        const int at = side == 0 ? 0 : ext - 1;
         int i, j, k;
-        cell_ijk(c, s, i, j, k);
-        const int t = a == 0 ? i : (a == 1 ? j : k);
-        const bool zero = ((closed & lo) && t == 0) ||
-                          ((closed & hi) && t == ext - 1);
-        if (zero)
-            vel[c] = 0.0;
-        else if (cls[c] & kFaceInside)
-            vel[c] = tmp[c];
+        if (a == 0) { i = at; j = p1; k = p2; }
+        else if (a == 1) { i = p1; j = at; k = p2; }
+        else { i = p1; j = p2; k = at; }
+        vel[lin(i, j, k, s.x, s.y)] = 0.0;
     }
 }
 
@@ -333,11 +407,16 @@ jetgpu_status bc_classify(Ctx* c, const GridDesc& g, const FieldDesc& sdf) {
     if (c->bc_cls_cap < nf) {
         JG_CUDA(c, cudaStreamSynchronize(c->stream));
         if (c->bc_cls) cudaFree(c->bc_cls);
+        if (c->bc_list) cudaFree(c->bc_list);
         c->bc_cls = nullptr;
+        c->bc_list = nullptr;
         c->bc_cls_cap = 0;
         JG_CUDA(c, cudaMalloc((void**)&c->bc_cls, nf));
+        JG_CUDA(c, cudaMalloc((void**)&c->bc_list, 2 * nf * sizeof(int)));
         c->bc_cls_cap = nf;
     }
+    if (!c->bc_cnt) JG_CUDA(c, cudaMalloc((void**)&c->bc_cnt, 6 * sizeof(unsigned)));
+    JG_CUDA(c, cudaMemsetAsync(c->bc_cnt, 0, 6 * sizeof(unsigned), c->stream));
     H3 h{{g.spacing[0], g.spacing[1], g.spacing[2]}};
     S3 fsp{{make_spacing(sdf.kind == 1 ? sdf.spacing[0] : 1.0),
             make_spacing(sdf.kind == 1 ? sdf.spacing[1] : 1.0),
@@ -346,8 +425,12 @@ jetgpu_status bc_classify(Ctx* c, const GridDesc& g, const FieldDesc& sdf) {
     for (int a = 0; a < 3; ++a) {
         const long n = fs.s[a].count();
         Prof pr(c, K_BOUNDARY, 1.0 * n);
+        // Lists: invalid faces of axis a at bc_list + off, inside faces at
+        // bc_list + nf + off; counts bc_cnt[a], bc_cnt[3 + a].
         k_bc_classify<<<blocks_for(n, kThreads, c->num_sms * 8), kThreads, 0,
-                        c->stream>>>(fs, a, h, sdf, fsp, c->bc_cls + off);
+                        c->stream>>>(fs, a, h, sdf, fsp, c->bc_cls + off,
+                                     c->bc_list + off, c->bc_cnt + a,
+                                     c->bc_list + nf + off, c->bc_cnt + 3 + a);
         off += n;
     }
     JG_CUDA(c, cudaGetLastError());
@@ -358,10 +441,9 @@ jetgpu_status bc_apply(Ctx* c, const GridDesc& g, double* u, double* v,
                        double* w, const FieldDesc& sdf,
                        const jetgpu_collider* col, int closed, unsigned depth) {
     const FaceSet fs = face_set(g);
-    size_t nmax = 0;
-    for (int a = 0; a < 3; ++a)
-        nmax = std::max(nmax, (size_t)fs.s[a].count());
-    if (jetgpu_status s = bc_scratch(c, 3 * nmax)) return s;
+    size_t nf = 0;
+    for (int a = 0; a < 3; ++a) nf += (size_t)fs.s[a].count();
+    if (jetgpu_status s = bc_scratch(c, nf)) return s;
     ColliderDesc cd{};
     if (col) {
         cd.present = 1;
@@ -379,38 +461,51 @@ jetgpu_status bc_apply(Ctx* c, const GridDesc& g, double* u, double* v,
     if (sdf.kind == 1)
         for (int d = 0; d < 3; ++d) inv.v[d] = 1.0 / sdf.spacing[d];
     double* vel[3] = {u, v, w};
-    double* tmp[3];
-    unsigned char* va[3];
-    unsigned char* vb[3];
-    const unsigned char* cls[3];
-    size_t off = 0;
+    // The list passes are sized for the worst case and read their counts on
+    // the device, so nothing here waits for the classification.
+    const int grid = c->num_sms * 8;
+    size_t off[3], o = 0;
     for (int a = 0; a < 3; ++a) {
-        tmp[a] = c->bc_tmp + a * nmax;
-        va[a] = c->bc_valid + a * nmax;
-        vb[a] = c->bc_valid + (3 + a) * nmax;
-        cls[a] = c->bc_cls + off;
-        off += (size_t)fs.s[a].count();
+        off[a] = o;
+        o += (size_t)fs.s[a].count();
     }
     for (int a = 0; a < 3; ++a) {
-        const long n = fs.s[a].count();
-        Prof pr(c, K_BOUNDARY, 2.0 * n);
-        k_bc_mark<<<blocks_for(n, kThreads, c->num_sms * 8), kThreads, 0,
-                    c->stream>>>(fs, a, h, cd, cls[a], vel[a], va[a]);
+        const int* inv_list = c->bc_list + off[a];
+        const unsigned* inv_cnt = c->bc_cnt + a;
+        const unsigned char* cls = c->bc_cls + off[a];
+        unsigned char* st0 = c->bc_valid + off[a];
+        unsigned char* st1 = c->bc_valid + nf + off[a];
+        {
+            Prof pr(c, K_BOUNDARY, 0.0);
+            k_bc_mark<<<grid, kThreads, 0, c->stream>>>(fs, a, h, cd, inv_list,
+                                                        inv_cnt, vel[a], st0);
+        }
+        for (unsigned it = 0; it < depth; ++it) {
+            Prof pr(c, K_BOUNDARY, 0.0);
+            k_extrapolate_list<<<grid, kThreads, 0, c->stream>>>(
+                fs.s[a], inv_list, inv_cnt, vel[a], cls, st0, st1);
+            std::swap(st0, st1);
+        }
     }
-    for (int a = 0; a < 3; ++a)
-        extrapolate_passes(c, fs.s[a], vel[a], va[a], vb[a], depth);
     for (int a = 0; a < 3; ++a) {
-        const long n = fs.s[a].count();
-        Prof pr(c, K_BOUNDARY, 1.0 * n);
-        k_bc_project<<<blocks_for(n, kThreads, c->num_sms * 8), kThreads, 0,
-                       c->stream>>>(fs, a, h, gsp, inv, sdf, cd, cls[a], u, v,
-                                    w, tmp[a]);
+        Prof pr(c, K_BOUNDARY, 0.0);
+        k_bc_project<<<grid, kThreads, 0, c->stream>>>(
+            fs, a, h, gsp, inv, sdf, cd, c->bc_list + nf + off[a],
+            c->bc_cnt + 3 + a, u, v, w, c->bc_tmp + off[a]);
     }
     for (int a = 0; a < 3; ++a) {
-        const long n = fs.s[a].count();
-        Prof pr(c, K_BOUNDARY, 1.0 * n);
-        k_bc_store<<<blocks_for(n, kThreads, c->num_sms * 8), kThreads, 0,
-                     c->stream>>>(fs.s[a], a, closed, cls[a], tmp[a], vel[a]);
+        Prof pr(c, K_BOUNDARY, 0.0);
+        k_bc_store<<<grid, kThreads, 0, c->stream>>>(
+            c->bc_list + nf + off[a], c->bc_cnt + 3 + a, c->bc_tmp + off[a],
+            vel[a]);
+        const int lo = closed & (1 << (2 * a)), hi = closed & (1 << (2 * a + 1));
+        if (lo || hi) {
+            const Dims s = fs.s[a];
+            const long P = a == 0 ? (long)s.y * s.z
+                                  : (a == 1 ? (long)s.x * s.z : (long)s.x * s.y);
+            k_bc_walls<<<blocks_for(2 * P, kThreads, c->num_sms * 8), kThreads,
+                         0, c->stream>>>(s, a, lo, hi, vel[a]);
+        }
     }
     JG_CUDA(c, cudaGetLastError());
     return JETGPU_OK;

@@ -152,6 +152,8 @@ struct Ctx {
     unsigned char* bc_valid = nullptr;
     size_t bc_cls_cap = 0;
     unsigned char* bc_cls = nullptr;  // face classes of the last bc_classify
+    int* bc_list = nullptr;           // its invalid / inside face lists
+    unsigned* bc_cnt = nullptr;       // their lengths per axis
 
     // Device-resident FLIP step scratch (flip.cu): P2G markers, FLIP
     // snapshot, collider face velocities, the CFL maximum.
