@@ -866,6 +866,33 @@ jetgpu_status jetgpu_constrain_velocity(
     return JETGPU_OK;
 }
 
+jetgpu_status jetgpu_apic_p2g_device(jetgpu_ctx* c, const jetgpu_grid* grid,
+                                     long np, const double* pos,
+                                     const double* vel, const double* affine,
+                                     double* u, double* v, double* w,
+                                     unsigned char* mu, unsigned char* mv,
+                                     unsigned char* mw) {
+    jetgpu_status s = check_transfer(c, grid, np, pos, vel);
+    if (s != JETGPU_OK) return s;
+    if (!u || !v || !w || (np > 0 && !affine))
+        return fail(c, JETGPU_BAD_INPUT, "null grid or affine arrays");
+    JG_CUDA(c, cudaSetDevice(c->device));
+    return apic_p2g(c, to_desc(grid), np, pos, vel, affine, u, v, w, mu, mv,
+                    mw);
+}
+
+jetgpu_status jetgpu_apic_g2p_device(jetgpu_ctx* c, const jetgpu_grid* grid,
+                                     long np, const double* pos, double* vel,
+                                     double* affine, const double* u,
+                                     const double* v, const double* w) {
+    jetgpu_status s = check_transfer(c, grid, np, pos, vel);
+    if (s != JETGPU_OK) return s;
+    if (!u || !v || !w || (np > 0 && !affine))
+        return fail(c, JETGPU_BAD_INPUT, "null grid or affine arrays");
+    JG_CUDA(c, cudaSetDevice(c->device));
+    return apic_g2p(c, to_desc(grid), np, pos, vel, affine, u, v, w);
+}
+
 jetgpu_status jetgpu_move_particles_device(
     jetgpu_ctx* c, const jetgpu_grid* grid, long np, double* pos, double* vel,
     const double* u, const double* v, const double* w, double dt,
@@ -1010,7 +1037,7 @@ jetgpu_status jetgpu_fluid_cfl_device(jetgpu_ctx* c, const jetgpu_grid* grid,
 
 jetgpu_status jetgpu_flip_substep_device(
     jetgpu_ctx* c, const jetgpu_grid* grid, long np, double* pos, double* vel,
-    double* u, double* v, double* w, double* fluid_sdf,
+    double* affine, double* u, double* v, double* w, double* fluid_sdf,
     const jetgpu_scalar_field* collider_sdf, const jetgpu_collider* collider,
     const jetgpu_sphere* sphere, const jetgpu_flip_params* prm, double dt,
     jetgpu_solve_stats* stats) {
@@ -1019,6 +1046,10 @@ jetgpu_status jetgpu_flip_substep_device(
     if ((s = check_field(c, collider_sdf, "collider_sdf")) != JETGPU_OK) return s;
     if (!u || !v || !w || !fluid_sdf || !prm)
         return fail(c, JETGPU_BAD_INPUT, "null argument");
+    if (prm->flip < 0 || prm->flip > 2)
+        return fail(c, JETGPU_BAD_INPUT, "flip must be 0 (PIC), 1 or 2 (APIC)");
+    if (prm->flip == 2 && np > 0 && !affine)
+        return fail(c, JETGPU_BAD_INPUT, "APIC needs the affine array");
     if (np > 2147483647L)
         return fail(c, JETGPU_BAD_INPUT, "more than 2^31 - 1 particles");
     if (!std::isfinite(dt) || !(dt >= 0.0) || !std::isfinite(prm->max_cfl) ||
@@ -1029,7 +1060,8 @@ jetgpu_status jetgpu_flip_substep_device(
     JG_CUDA(c, cudaSetDevice(c->device));
     jetgpu_solve_stats local;
     std::memset(&local, 0, sizeof(local));
-    s = flip_substep(c, to_desc(grid), np, pos, vel, u, v, w, fluid_sdf,
+    s = flip_substep(c, to_desc(grid), np, pos, vel, affine, u, v, w,
+                     fluid_sdf,
                      to_desc(collider_sdf, collider_sdf->data), collider,
                      sphere, *prm, dt, &local);
     if (stats) *stats = local;

@@ -318,7 +318,8 @@ jetgpu_status fluid_cfl(Ctx* c, const GridDesc& g, const double* u,
                         const double* v, const double* w, double dt,
                         const double gravity[3], double* cfl);
 jetgpu_status flip_substep(Ctx* c, const GridDesc& g, long np, double* pos,
-                           double* vel, double* u, double* v, double* w,
+                           double* vel, double* affine, double* u, double* v,
+                           double* w,
                            double* fluid_sdf, const FieldDesc& col_sdf,
                            const jetgpu_collider* col,
                            const jetgpu_sphere* sph,
@@ -328,6 +329,14 @@ jetgpu_status flip_substep(Ctx* c, const GridDesc& g, long np, double* pos,
 jetgpu_status build_particle_sdf(Ctx* c, const GridDesc& g, long np,
                                  const double* pos, const FieldDesc& col,
                                  double max_cfl, double* out);
+
+jetgpu_status apic_p2g(Ctx* c, const GridDesc& g, long np, const double* pos,
+                       const double* vel, const double* aff, double* u,
+                       double* v, double* w, unsigned char* mu,
+                       unsigned char* mv, unsigned char* mw);
+jetgpu_status apic_g2p(Ctx* c, const GridDesc& g, long np, const double* pos,
+                       double* vel, double* aff, const double* u,
+                       const double* v, const double* w);
 
 jetgpu_status move_particles(Ctx* c, const GridDesc& g, long np, double* pos,
                              double* vel, const double* u, const double* v,

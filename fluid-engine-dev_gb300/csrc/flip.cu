@@ -1,6 +1,8 @@
-// One device-resident FLIP / PIC sub-step: GridFluidSolver3::onAdvanceTimeStep
-// (src/jet/grid_fluid_solver3.cpp:179-210) as FlipSolver3 / PicSolver3 run it
-// (src/jet/pic_solver3.cpp:63-112, src/jet/flip_solver3.cpp:27-99), with no
+// One device-resident FLIP / PIC / APIC sub-step:
+// GridFluidSolver3::onAdvanceTimeStep (src/jet/grid_fluid_solver3.cpp:
+// 179-210) as FlipSolver3 / PicSolver3 / ApicSolver3 run it
+// (src/jet/pic_solver3.cpp:63-112, src/jet/flip_solver3.cpp:27-99,
+// src/jet/apic_solver3.cpp:26-228), with no
 // viscosity, emitter or advected scalar fields:
 //   beginAdvanceTimeStep        applyBoundaryCondition            (:137-160)
 //   onBeginAdvanceTimeStep      P2G (+ FLIP snapshot), particle SDF,
@@ -140,7 +142,8 @@ jetgpu_status fluid_cfl(Ctx* c, const GridDesc& g, const double* u,
 }
 
 jetgpu_status flip_substep(Ctx* c, const GridDesc& g, long np, double* pos,
-                           double* vel, double* u, double* v, double* w,
+                           double* vel, double* affine, double* u, double* v,
+                           double* w,
                            double* fluid_sdf, const FieldDesc& col_sdf,
                            const jetgpu_collider* col,
                            const jetgpu_sphere* sph,
@@ -184,10 +187,14 @@ jetgpu_status flip_substep(Ctx* c, const GridDesc& g, long np, double* pos,
     // beginAdvanceTimeStep
     if ((s = bc()) != JETGPU_OK) return s;
     // onBeginAdvanceTimeStep
-    if ((s = p2g(c, g, np, pos, vel, u, v, w, mk[0], mk[1], mk[2],
-                 prm.flip ? sn[0] : nullptr, prm.flip ? sn[1] : nullptr,
-                 prm.flip ? sn[2] : nullptr)) != JETGPU_OK)
-        return s;
+    const bool flip = prm.flip == 1, apic = prm.flip == 2;
+    if (apic)
+        s = apic_p2g(c, g, np, pos, vel, affine, u, v, w, mk[0], mk[1], mk[2]);
+    else
+        s = p2g(c, g, np, pos, vel, u, v, w, mk[0], mk[1], mk[2],
+                flip ? sn[0] : nullptr, flip ? sn[1] : nullptr,
+                flip ? sn[2] : nullptr);
+    if (s != JETGPU_OK) return s;
     if ((s = build_particle_sdf(c, g, np, pos, col_sdf, prm.max_cfl,
                                 fluid_sdf)) != JETGPU_OK)
         return s;
@@ -258,9 +265,11 @@ jetgpu_status flip_substep(Ctx* c, const GridDesc& g, long np, double* pos,
     // computeAdvection
     if ((s = to_air()) != JETGPU_OK) return s;
     if ((s = bc()) != JETGPU_OK) return s;
-    if (prm.flip)
+    if (flip)
         s = g2p_flip(c, g, np, pos, vel, u, v, w, sn[0], sn[1], sn[2],
                      prm.pic_blending);
+    else if (apic)
+        s = apic_g2p(c, g, np, pos, vel, affine, u, v, w);
     else
         s = g2p_pic(c, g, np, pos, vel, u, v, w);
     if (s != JETGPU_OK) return s;

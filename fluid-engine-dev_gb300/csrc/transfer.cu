@@ -148,6 +148,130 @@ __global__ void k_g2p_pic(long np, const double* __restrict__ pos,
     }
 }
 
+// APIC (ApicSolver3, src/jet/apic_solver3.cpp). Positions are clamped per
+// face grid: the two other coordinates half a cell inside the grid's box
+// (:55-62), with jet::clamp's rule.
+struct ApicBox {
+    double lo[3], hi[3];  // box +- half a cell
+};
+__device__ __forceinline__ double clamp_d(double v, double lo, double hi) {
+    return v < lo ? lo : (v > hi ? hi : v);
+}
+
+// K22a: the APIC scatter (:51-124): weights as P2G's, each sample carrying
+// vel_a + c_a . (x_face - x_clamped). FP64 atomics reorder the reference's
+// serial sums (rounding only).
+__global__ void k_apic_p2g_scatter(long np, const double* __restrict__ pos,
+                                   const double* __restrict__ vel,
+                                   const double* __restrict__ aff, FaceSet fs,
+                                   double hx, double hy, double hz, double ihx,
+                                   double ihy, double ihz, ApicBox box,
+                                   double* u, double* v, double* w,
+                                   double* wu, double* wv, double* ww,
+                                   unsigned char* mu, unsigned char* mv,
+                                   unsigned char* mw) {
+    double* grid[3] = {u, v, w};
+    double* wsum[3] = {wu, wv, ww};
+    unsigned char* mark[3] = {mu, mv, mw};
+    const double hs[3] = {hx, hy, hz};
+    for (long p = blockIdx.x * (long)blockDim.x + threadIdx.x; p < np;
+         p += (long)gridDim.x * blockDim.x) {
+        for (int a = 0; a < 3; ++a) {
+            double q[3];
+            for (int d = 0; d < 3; ++d)
+                q[d] = d == a ? pos[3 * p + d]
+                              : clamp_d(pos[3 * p + d], box.lo[d], box.hi[d]);
+            const Dims s = fs.s[a];
+            int i, j, k;
+            double fx, fy, fz;
+            bary<double>((q[0] - fs.o[a][0]) * ihx, s.x - 1, &i, &fx);
+            bary<double>((q[1] - fs.o[a][1]) * ihy, s.y - 1, &j, &fy);
+            bary<double>((q[2] - fs.o[a][2]) * ihz, s.z - 1, &k, &fz);
+            const int ip1 = min(i + 1, s.x - 1), jp1 = min(j + 1, s.y - 1),
+                      kp1 = min(k + 1, s.z - 1);
+            const int ci[8] = {i, ip1, i, ip1, i, ip1, i, ip1};
+            const int cj[8] = {j, j, jp1, jp1, j, j, jp1, jp1};
+            const int ck[8] = {k, k, k, k, kp1, kp1, kp1, kp1};
+            const double wt[8] = {(1 - fx) * (1 - fy) * (1 - fz), fx * (1 - fy) * (1 - fz),
+                                  (1 - fx) * fy * (1 - fz),       fx * fy * (1 - fz),
+                                  (1 - fx) * (1 - fy) * fz,       fx * (1 - fy) * fz,
+                                  (1 - fx) * fy * fz,             fx * fy * fz};
+            const double* C = aff + 9 * p + 3 * a;
+            const double va = vel[3 * p + a];
+            for (int n = 0; n < 8; ++n) {
+                const double g0 = fs.o[a][0] + hs[0] * (double)ci[n];
+                const double g1 = fs.o[a][1] + hs[1] * (double)cj[n];
+                const double g2 = fs.o[a][2] + hs[2] * (double)ck[n];
+                const double term = C[0] * (g0 - q[0]) + C[1] * (g1 - q[1]) +
+                                    C[2] * (g2 - q[2]);
+                const long idx = lin(ci[n], cj[n], ck[n], s.x, s.y);
+                atomicAdd(&grid[a][idx], wt[n] * (va + term));
+                atomicAdd(&wsum[a][idx], wt[n]);
+                if (mark[a]) mark[a][idx] = 1;
+            }
+        }
+    }
+}
+
+// K22b: the APIC gather (:148-228): the PIC velocity, then c_a = sum of the
+// gradient weights of getCoordinatesAndGradientWeights
+// (include/jet/detail/array_samplers3-inl.h:196-261) times the grid values.
+__global__ void k_apic_g2p(long np, const double* __restrict__ pos,
+                           double* __restrict__ vel, double* __restrict__ aff,
+                           FaceSet fs, Spacing sx, Spacing sy, Spacing sz,
+                           double ix, double iy, double iz, ApicBox box,
+                           const double* __restrict__ u,
+                           const double* __restrict__ v,
+                           const double* __restrict__ w) {
+    const double* g[3] = {u, v, w};
+    for (long p = blockIdx.x * (long)blockDim.x + threadIdx.x; p < np;
+         p += (long)gridDim.x * blockDim.x) {
+        const double px = pos[3 * p], py = pos[3 * p + 1], pz = pos[3 * p + 2];
+        for (int a = 0; a < 3; ++a)
+            vel[3 * p + a] = sample_face<double, double>(
+                g[a], fs.s[a], sx.div(px - fs.o[a][0]), sy.div(py - fs.o[a][1]),
+                sz.div(pz - fs.o[a][2]));
+        for (int a = 0; a < 3; ++a) {
+            double q[3];
+            for (int d = 0; d < 3; ++d)
+                q[d] = d == a ? pos[3 * p + d]
+                              : clamp_d(pos[3 * p + d], box.lo[d], box.hi[d]);
+            const Dims s = fs.s[a];
+            int i, j, k;
+            double fx, fy, fz;
+            bary<double>(sx.div(q[0] - fs.o[a][0]), s.x - 1, &i, &fx);
+            bary<double>(sy.div(q[1] - fs.o[a][1]), s.y - 1, &j, &fy);
+            bary<double>(sz.div(q[2] - fs.o[a][2]), s.z - 1, &k, &fz);
+            const int ip1 = min(i + 1, s.x - 1), jp1 = min(j + 1, s.y - 1),
+                      kp1 = min(k + 1, s.z - 1);
+            const long idx[8] = {lin(i, j, k, s.x, s.y),     lin(ip1, j, k, s.x, s.y),
+                                 lin(i, jp1, k, s.x, s.y),   lin(ip1, jp1, k, s.x, s.y),
+                                 lin(i, j, kp1, s.x, s.y),   lin(ip1, j, kp1, s.x, s.y),
+                                 lin(i, jp1, kp1, s.x, s.y), lin(ip1, jp1, kp1, s.x, s.y)};
+            const double gw[8][3] = {
+                {-ix * (1 - fy) * (1 - fz), -iy * (1 - fx) * (1 - fz), -iz * (1 - fx) * (1 - fy)},
+                {ix * (1 - fy) * (1 - fz), fx * (-iy) * (1 - fz), fx * (1 - fy) * (-iz)},
+                {(-ix) * fy * (1 - fz), (1 - fx) * iy * (1 - fz), (1 - fx) * fy * (-iz)},
+                {ix * fy * (1 - fz), fx * iy * (1 - fz), fx * fy * (-iz)},
+                {(-ix) * (1 - fy) * fz, (1 - fx) * (-iy) * fz, (1 - fx) * (1 - fy) * iz},
+                {ix * (1 - fy) * fz, fx * (-iy) * fz, fx * (1 - fy) * iz},
+                {(-ix) * fy * fz, (1 - fx) * iy * fz, (1 - fx) * fy * iz},
+                {ix * fy * fz, fx * iy * fz, fx * fy * iz}};
+            double C0 = 0.0, C1 = 0.0, C2 = 0.0;
+#pragma unroll
+            for (int n = 0; n < 8; ++n) {
+                const double val = g[a][idx[n]];
+                C0 = C0 + gw[n][0] * val;
+                C1 = C1 + gw[n][1] * val;
+                C2 = C2 + gw[n][2] * val;
+            }
+            aff[9 * p + 3 * a] = C0;
+            aff[9 * p + 3 * a + 1] = C1;
+            aff[9 * p + 3 * a + 2] = C2;
+        }
+    }
+}
+
 // K20: PicSolver3::moveParticles (src/jet/pic_solver3.cpp:206-282) and,
 // with a sphere collider, Collider3::resolveCollision
 // (src/jet/collider3.cpp:19-73, radius 0, restitution 0) through the
@@ -387,6 +511,75 @@ jetgpu_status g2p_flip(Ctx* c, const GridDesc& g, long np, const double* pos,
             np, pos, vel, fs, (float)g.spacing[0], (float)g.spacing[1],
             (float)g.spacing[2], su, sv, sw, u, v, w, g.spacing[0],
             g.spacing[1], g.spacing[2], blend);
+    }
+    JG_CUDA(c, cudaGetLastError());
+    return JETGPU_OK;
+}
+
+static ApicBox apic_box(const GridDesc& g) {
+    ApicBox b;
+    for (int d = 0; d < 3; ++d) {
+        const double e = g.origin[d] + g.spacing[d] * (double)g.res[d];
+        const double hh = g.spacing[d] / 2.0;
+        b.lo[d] = std::min(g.origin[d], e) + hh;
+        b.hi[d] = std::max(g.origin[d], e) - hh;
+    }
+    return b;
+}
+
+jetgpu_status apic_p2g(Ctx* c, const GridDesc& g, long np, const double* pos,
+                       const double* vel, const double* aff, double* u,
+                       double* v, double* w, unsigned char* mu,
+                       unsigned char* mv, unsigned char* mw) {
+    const FaceSet fs = face_set(g);
+    const long n[3] = {fs.s[0].count(), fs.s[1].count(), fs.s[2].count()};
+    const size_t need = (size_t)(n[0] + n[1] + n[2]) * sizeof(double);
+    if (need > c->pscratch_bytes) {
+        if (c->pscratch) cudaFree(c->pscratch);
+        c->pscratch = nullptr;
+        c->pscratch_bytes = 0;
+        JG_CUDA(c, cudaMalloc((void**)&c->pscratch, need));
+        c->pscratch_bytes = need;
+    }
+    double* wsum = reinterpret_cast<double*>(c->pscratch);
+    double* grid[3] = {u, v, w};
+    unsigned char* mark[3] = {mu, mv, mw};
+    JG_CUDA(c, cudaMemsetAsync(wsum, 0, need, c->stream));
+    for (int a = 0; a < 3; ++a) {
+        JG_CUDA(c, cudaMemsetAsync(grid[a], 0, n[a] * sizeof(double), c->stream));
+        if (mark[a]) JG_CUDA(c, cudaMemsetAsync(mark[a], 0, n[a], c->stream));
+    }
+    if (np > 0) {
+        Prof pr(c, K_P2G, 120.0 * np + 2.0 * 3 * 8.0 * (n[0] + n[1] + n[2]));
+        k_apic_p2g_scatter<<<blocks_for(np, kThreads, c->num_sms * 16),
+                             kThreads, 0, c->stream>>>(
+            np, pos, vel, aff, fs, g.spacing[0], g.spacing[1], g.spacing[2],
+            1.0 / g.spacing[0], 1.0 / g.spacing[1], 1.0 / g.spacing[2],
+            apic_box(g), u, v, w, wsum, wsum + n[0], wsum + n[0] + n[1], mu,
+            mv, mw);
+    }
+    long off = 0;
+    for (int a = 0; a < 3; ++a) {
+        k_p2g_normalize<<<blocks_for(n[a]), kThreads, 0, c->stream>>>(
+            grid[a], wsum + off, nullptr, n[a]);
+        off += n[a];
+    }
+    JG_CUDA(c, cudaGetLastError());
+    return JETGPU_OK;
+}
+
+jetgpu_status apic_g2p(Ctx* c, const GridDesc& g, long np, const double* pos,
+                       double* vel, double* aff, const double* u,
+                       const double* v, const double* w) {
+    const FaceSet fs = face_set(g);
+    if (np > 0) {
+        Prof pr(c, K_G2P, 120.0 * np);
+        k_apic_g2p<<<blocks_for(np, kThreads, c->num_sms * 16), kThreads, 0,
+                     c->stream>>>(
+            np, pos, vel, aff, fs, make_spacing(g.spacing[0]),
+            make_spacing(g.spacing[1]), make_spacing(g.spacing[2]),
+            1.0 / g.spacing[0], 1.0 / g.spacing[1], 1.0 / g.spacing[2],
+            apic_box(g), u, v, w);
     }
     JG_CUDA(c, cudaGetLastError());
     return JETGPU_OK;

@@ -113,6 +113,7 @@ EXPORTS = (
     "jetgpu_move_particles", "jetgpu_build_particle_sdf_device",
     "jetgpu_build_particle_sdf", "jetgpu_flip_params_default",
     "jetgpu_fluid_cfl_device", "jetgpu_flip_substep_device",
+    "jetgpu_apic_p2g_device", "jetgpu_apic_g2p_device",
 )
 
 # closedDomainBoundaryFlag bits (include/jet/constants.h:312-335).
@@ -232,6 +233,12 @@ def library() -> C.CDLL:
     L.jetgpu_build_particle_sdf.restype = C.c_int
     L.jetgpu_build_particle_sdf_device.argtypes = sdf_args
     L.jetgpu_build_particle_sdf_device.restype = C.c_int
+    L.jetgpu_apic_p2g_device.argtypes = [vp, C.POINTER(Grid), C.c_long, vp,
+                                         vp, vp, vp, vp, vp, vp, vp, vp]
+    L.jetgpu_apic_p2g_device.restype = C.c_int
+    L.jetgpu_apic_g2p_device.argtypes = [vp, C.POINTER(Grid), C.c_long, vp,
+                                         vp, vp, vp, vp, vp]
+    L.jetgpu_apic_g2p_device.restype = C.c_int
     L.jetgpu_flip_params_default.argtypes = [C.POINTER(FlipParams)]
     L.jetgpu_flip_params_default.restype = None
     L.jetgpu_fluid_cfl_device.argtypes = [vp, C.POINTER(Grid), vp, vp, vp,
@@ -239,7 +246,7 @@ def library() -> C.CDLL:
                                           C.POINTER(C.c_double)]
     L.jetgpu_fluid_cfl_device.restype = C.c_int
     L.jetgpu_flip_substep_device.argtypes = [
-        vp, C.POINTER(Grid), C.c_long, vp, vp, vp, vp, vp, vp,
+        vp, C.POINTER(Grid), C.c_long, vp, vp, vp, vp, vp, vp, vp,
         C.POINTER(ScalarField), C.POINTER(Collider), C.POINTER(Sphere),
         C.POINTER(FlipParams), C.c_double, C.POINTER(SolveStats)]
     L.jetgpu_flip_substep_device.restype = C.c_int
@@ -769,9 +776,12 @@ class FlipSolver3:
     context). Device state: positions, velocities, the face velocity u/v/w and
     the particle SDF, as torch tensors."""
 
+    TRANSFERS = {"pic": 0, "flip": 1, "apic": 2}
+
     def __init__(self, resolution, gridSpacing, origin=(0.0, 0.0, 0.0),
                  pressureSolver: "FdmMgpcgSolver3 | None" = None,
-                 flip: bool = True, device: int = 0):
+                 flip: bool = True, device: int = 0,
+                 transfer: str | None = None):
         import torch
         self._torch = torch
         self.solver = pressureSolver if pressureSolver is not None \
@@ -796,7 +806,12 @@ class FlipSolver3:
         self.vel = torch.zeros((0, 3), **f64)
         self.params = FlipParams()
         library().jetgpu_flip_params_default(C.byref(self.params))
-        self.params.flip = int(bool(flip))
+        # transfer: "flip" (FlipSolver3), "pic" (PicSolver3) or "apic"
+        # (ApicSolver3); `flip` chooses between the first two.
+        if transfer is None:
+            transfer = "flip" if flip else "pic"
+        self.params.flip = self.TRANSFERS[transfer]
+        self.affine = torch.zeros((0, 9), **f64)
         self._col_sdf = None
         self._collider = None
         self._sphere = None
@@ -849,6 +864,11 @@ class FlipSolver3:
         self.synchronize()
         self.pos = self._torch.from_numpy(pos.copy()).to(self.dev)
         self.vel = self._torch.from_numpy(vel.copy()).to(self.dev)
+        # APIC's affine matrices start at zero, as ApicSolver3's do once its
+        # first G2P has run (apic_solver3.cpp:160-165).
+        self.affine = self._torch.zeros((pos.shape[0], 9),
+                                        dtype=self._torch.float64,
+                                        device=self.dev)
         self._uploaded()
 
     def positions(self) -> np.ndarray:
@@ -890,7 +910,9 @@ class FlipSolver3:
         f = self._col_field()
         st = library().jetgpu_flip_substep_device(
             self.solver.context(), C.byref(self.grid), self.pos.shape[0],
-            _p(self.pos), _p(self.vel), _p(self.u), _p(self.v), _p(self.w),
+            _p(self.pos), _p(self.vel),
+            _p(self.affine) if self.params.flip == 2 else None,
+            _p(self.u), _p(self.v), _p(self.w),
             _p(self.sdf), C.byref(f),
             C.byref(self._collider) if self._collider is not None else None,
             C.byref(self._sphere) if self._sphere is not None else None,
@@ -909,6 +931,27 @@ class FlipSolver3:
             remaining -= dt
             self.currentTimeInSeconds += dt
         self.synchronize()  # the reference's update() returns when done
+
+
+def apic_transfer_from_particles_to_grids_device(solver: "FdmMgpcgSolver3",
+                                                 grid: Grid, pos, vel, affine,
+                                                 u, v, w, mu=None, mv=None,
+                                                 mw=None):
+    """ApicSolver3::transferFromParticlesToGrids on device tensors."""
+    st = library().jetgpu_apic_p2g_device(
+        solver.context(), C.byref(grid), pos.shape[0], _p(pos), _p(vel),
+        _p(affine), _p(u), _p(v), _p(w), _p(mu), _p(mv), _p(mw))
+    solver.check(st)
+
+
+def apic_transfer_from_grids_to_particles_device(solver: "FdmMgpcgSolver3",
+                                                 grid: Grid, pos, vel, affine,
+                                                 u, v, w):
+    """ApicSolver3::transferFromGridsToParticles on device tensors."""
+    st = library().jetgpu_apic_g2p_device(
+        solver.context(), C.byref(grid), pos.shape[0], _p(pos), _p(vel),
+        _p(affine), _p(u), _p(v), _p(w))
+    solver.check(st)
 
 
 class GridFractionalBoundaryConditionSolver3:

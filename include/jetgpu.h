@@ -359,7 +359,8 @@ typedef struct jetgpu_flip_params {
     double gravity[3];        /* GridFluidSolver3::gravity */
     double max_cfl;           /* GridFluidSolver3::maxCfl */
     int closed_domain_flags;  /* JETGPU_DIRECTION_* bits */
-    int flip;                 /* 1: FlipSolver3, 0: PicSolver3 */
+    int flip;                 /* 1: FlipSolver3, 0: PicSolver3,
+                                 2: ApicSolver3 */
     double pic_blending;      /* FlipSolver3::picBlendingFactor */
 } jetgpu_flip_params;
 
@@ -385,17 +386,42 @@ jetgpu_status jetgpu_fluid_cfl_device(struct jetgpu_ctx* ctx,
  * conditions, P2G (+ FLIP snapshot), the particle SDF, extrapolation to air,
  * gravity, the pressure projection of this library (its configured solver),
  * G2P and particle advection with collisions, each stage in the
- * reference's order. DEVICE pointers. pos/vel: AoS xyz doubles; u/v/w: the
- * grid velocity (the solver's grid state, read and written); fluid_sdf: the
+ * reference's order. DEVICE pointers. pos/vel: AoS xyz doubles; affine:
+ * the APIC particles' cX, cY, cZ (9 doubles each; read and written; NULL
+ * unless params->flip == 2); u/v/w: the grid velocity (the solver's grid
+ * state, read and written); fluid_sdf: the
  * particle SDF out (res cells). collider_sdf: colliderSdf() of the boundary
  * solver (kind 0 = none); collider / sphere: NULL = none. stats: the
  * pressure solve's. Returns the first error, or the pressure solve's status. */
 jetgpu_status jetgpu_flip_substep_device(
     struct jetgpu_ctx* ctx, const jetgpu_grid* grid, long num_particles,
-    double* pos, double* vel, double* u, double* v, double* w,
+    double* pos, double* vel, double* affine, double* u, double* v, double* w,
     double* fluid_sdf, const jetgpu_scalar_field* collider_sdf,
     const jetgpu_collider* collider, const jetgpu_sphere* sphere,
     const jetgpu_flip_params* params, double dt, jetgpu_solve_stats* stats);
+
+/* ApicSolver3::transferFromParticlesToGrids (src/jet/apic_solver3.cpp:
+ * 26-146): the affine particle-to-grid transfer. affine: each particle's
+ * cX, cY, cZ (9 doubles: cX.x, cX.y, cX.z, cY.x, ...). u/v/w and markers out
+ * as jetgpu_p2g_device. DEVICE pointers. The FP64 atomic scatter reorders the
+ * reference's serial sums (rounding only). */
+jetgpu_status jetgpu_apic_p2g_device(struct jetgpu_ctx* ctx,
+                                     const jetgpu_grid* grid,
+                                     long num_particles, const double* pos,
+                                     const double* vel, const double* affine,
+                                     double* u, double* v, double* w,
+                                     unsigned char* mu, unsigned char* mv,
+                                     unsigned char* mw);
+
+/* ApicSolver3::transferFromGridsToParticles (:148-228): vel (the PIC
+ * sample) and affine (the velocity gradients, 9 doubles per particle) out.
+ * DEVICE pointers. Bit-identical to the reference. */
+jetgpu_status jetgpu_apic_g2p_device(struct jetgpu_ctx* ctx,
+                                     const jetgpu_grid* grid,
+                                     long num_particles, const double* pos,
+                                     double* vel, double* affine,
+                                     const double* u, const double* v,
+                                     const double* w);
 
 /* Host-pointer forms of the three transfers (copies inside the call). */
 jetgpu_status jetgpu_p2g(struct jetgpu_ctx* ctx, const jetgpu_grid* grid,

@@ -192,6 +192,10 @@ class Oracle:
         L.orc_move_particles.argtypes = [
             C.POINTER(OrcGrid), C.c_long, _dp, _dp, _dp, _dp, _dp, C.c_double,
             C.c_double, C.c_int, C.POINTER(OrcCollider), C.POINTER(OrcSphere)]
+        L.orc_apic_p2g.argtypes = [C.POINTER(OrcGrid), C.c_long, _dp, _dp,
+                                   _dp, _dp, _dp, _dp, _cp, _cp, _cp]
+        L.orc_apic_g2p.argtypes = [C.POINTER(OrcGrid), C.c_long, _dp, _dp,
+                                   _dp, _dp, _dp, _dp]
         L.orc_build_particle_sdf.argtypes = [
             C.POINTER(OrcGrid), C.c_long, _dp, C.POINTER(OrcField), C.c_double,
             _dp]
@@ -397,6 +401,34 @@ class Oracle:
         self.lib.orc_extrapolate(r, _ptr(d), _ptr(m, _cp), int(iterations))
         return d
 
+    def apic_p2g(self, res, spacing, origin, pos, vel, affine):
+        """ApicSolver3::transferFromParticlesToGrids; affine (n, 9).
+        Returns (grids, markers)."""
+        g = self._grid(res, spacing, origin)
+        nx, ny, nz = res
+        shp = [(nz, ny, nx + 1), (nz, ny + 1, nx), (nz + 1, ny, nx)]
+        grids = [np.zeros(s) for s in shp]
+        marks = [np.zeros(s, np.int8) for s in shp]
+        pos = np.ascontiguousarray(pos, np.float64)
+        vel = np.ascontiguousarray(vel, np.float64)
+        aff = np.ascontiguousarray(affine, np.float64)
+        self.lib.orc_apic_p2g(C.byref(g), pos.shape[0], _ptr(pos), _ptr(vel),
+                              _ptr(aff), *[_ptr(a) for a in grids],
+                              *[_ptr(m, _cp) for m in marks])
+        return grids, marks
+
+    def apic_g2p(self, res, spacing, origin, pos, grids):
+        """ApicSolver3::transferFromGridsToParticles; returns (vel, affine
+        (n, 9))."""
+        g = self._grid(res, spacing, origin)
+        pos = np.ascontiguousarray(pos, np.float64)
+        vel = np.zeros_like(pos)
+        aff = np.zeros((pos.shape[0], 9))
+        grids = [np.ascontiguousarray(a, np.float64) for a in grids]
+        self.lib.orc_apic_g2p(C.byref(g), pos.shape[0], _ptr(pos), _ptr(vel),
+                              _ptr(aff), *[_ptr(a) for a in grids])
+        return vel, aff
+
     @staticmethod
     def _collider(c):
         col = OrcCollider()
@@ -466,7 +498,7 @@ class Oracle:
         gr = np.ascontiguousarray(gravity, np.float64)
         self.lib.orc_flip_run(C.byref(g), pos.shape[0], _ptr(pos), _ptr(vel),
                               int(frames), float(fps), float(max_cfl),
-                              int(closed), _ptr(gr), int(bool(flip)),
+                              int(closed), _ptr(gr), int(flip),
                               C.byref(prm))
         return pos, vel
 

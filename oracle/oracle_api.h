@@ -179,7 +179,8 @@ void orc_build_particle_sdf(const orc_grid* g, long np, const double* pos,
                             const orc_field* collider_sdf, double max_cfl,
                             double* out);
 
-/* Reference harness only: FlipSolver3 (flip = 1) or PicSolver3 (0) with
+/* Reference harness only: FlipSolver3 (flip = 1), PicSolver3 (0) or
+ * ApicSolver3 (2) with
  * GridFractionalSinglePhasePressureSolver3 + FdmMgpcgSolver3(p), gravity g,
  * maxCfl, closed walls and no collider, run for `frames` frames of 1/fps
  * (update(Frame(i, 1/fps)), adaptive sub-steps) from the particles
@@ -199,6 +200,18 @@ void orc_quaternion_matrices(const double q[4], double orient[9],
  * distance). out: res cells. */
 void orc_sphere_collider_sdf(const orc_grid* g, const double centre[3],
                              double radius, double* out);
+
+/* ApicSolver3::transferFromParticlesToGrids (src/jet/apic_solver3.cpp:
+ * 26-146). affine: the particles' cX, cY, cZ as 9 doubles each (cX.x, cX.y,
+ * cX.z, cY.x, ...). Grids and markers out as orc_p2g. */
+void orc_apic_p2g(const orc_grid* g, long np, const double* pos,
+                  const double* vel, const double* affine, double* u,
+                  double* v, double* w, char* mu, char* mv, char* mw);
+
+/* ApicSolver3::transferFromGridsToParticles (:148-228): vel and affine out. */
+void orc_apic_g2p(const orc_grid* g, long np, const double* pos, double* vel,
+                  double* affine, const double* u, const double* v,
+                  const double* w);
 
 /* Port only: additionally stop MGPCG once the true relative residual
  * ||b - A x|| / ||b|| falls to `rel` (0 disables). Used to state the CPU

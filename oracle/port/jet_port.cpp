@@ -1497,6 +1497,130 @@ void orc_build_particle_sdf(const orc_grid* g, long np, const double* pos,
     orc_extrapolate(res, out, valid.data(), (unsigned)std::ceil(max_cfl));
 }
 
+// The bounding box and half spacing ApicSolver3 clamps positions with
+// (apic_solver3.cpp:33-34), and jet::clamp (math_utils-inl.h:126-134).
+struct ApicFrame {
+    double lo[3], hi[3], hh[3];
+};
+ApicFrame apicFrame(const orc_grid* g) {
+    ApicFrame f;
+    for (int d = 0; d < 3; ++d) {
+        const double e = g->origin[d] + g->spacing[d] * (double)g->res[d];
+        f.lo[d] = std::min(g->origin[d], e);
+        f.hi[d] = std::max(g->origin[d], e);
+        f.hh[d] = g->spacing[d] / 2.0;
+    }
+    return f;
+}
+inline double clampd(double v, double lo, double hi) {
+    return v < lo ? lo : (v > hi ? hi : v);
+}
+// The position clamped for face grid a: the two other coordinates kept half
+// a cell inside the box.
+inline void apicClamp(const ApicFrame& f, int a, const double* p, double q[3]) {
+    for (int d = 0; d < 3; ++d)
+        q[d] = d == a ? p[d] : clampd(p[d], f.lo[d] + f.hh[d], f.hi[d] - f.hh[d]);
+}
+
+void orc_apic_p2g(const orc_grid* g, long np, const double* pos,
+                  const double* vel, const double* affine, double* u,
+                  double* v, double* w, char* mu, char* mv, char* mw) {
+    FaceGeom fg[3];
+    faceGeoms(g, fg);
+    const ApicFrame F = apicFrame(g);
+    const double* h = g->spacing;
+    double* grids[3] = {u, v, w};
+    char* marks[3] = {mu, mv, mw};
+    std::vector<double> wsum[3];
+    for (int a = 0; a < 3; ++a) {
+        const long n = fg[a].s.count();
+        std::fill(grids[a], grids[a] + n, 0.0);
+        wsum[a].assign(n, 0.0);
+        if (marks[a]) std::fill(marks[a], marks[a] + n, 0);
+    }
+    for (long p = 0; p < np; ++p) {  // serial, in index order
+        for (int a = 0; a < 3; ++a) {
+            double q[3];
+            apicClamp(F, a, pos + 3 * p, q);
+            Stencil st;
+            coordsAndWeights(fg[a].s, fg[a].o[0], fg[a].o[1], fg[a].o[2],
+                             1.0 / h[0], 1.0 / h[1], 1.0 / h[2], q[0], q[1],
+                             q[2], &st);
+            const double* C = affine + 9 * p + 3 * a;
+            const Size3 s = fg[a].s;
+            for (int n = 0; n < 8; ++n) {
+                const long c = st.idx[n];
+                const long i = c % s.x, j = (c / s.x) % s.y, k = c / (s.x * s.y);
+                const double gp[3] = {fg[a].o[0] + h[0] * (double)i,
+                                      fg[a].o[1] + h[1] * (double)j,
+                                      fg[a].o[2] + h[2] * (double)k};
+                const double term = C[0] * (gp[0] - q[0]) +
+                                    C[1] * (gp[1] - q[1]) +
+                                    C[2] * (gp[2] - q[2]);
+                grids[a][c] += st.w[n] * (vel[3 * p + a] + term);
+                wsum[a][c] += st.w[n];
+                if (marks[a]) marks[a][c] = 1;
+            }
+        }
+    }
+    for (int a = 0; a < 3; ++a)
+        for (long c = 0; c < fg[a].s.count(); ++c)
+            if (wsum[a][c] > 0.0) grids[a][c] /= wsum[a][c];
+}
+
+void orc_apic_g2p(const orc_grid* g, long np, const double* pos, double* vel,
+                  double* affine, const double* u, const double* v,
+                  const double* w) {
+    FaceGeom fg[3];
+    faceGeoms(g, fg);
+    const ApicFrame F = apicFrame(g);
+    const double* h = g->spacing;
+    const double* grids[3] = {u, v, w};
+    const double ih[3] = {1.0 / h[0], 1.0 / h[1], 1.0 / h[2]};
+#pragma omp parallel for schedule(static)
+    for (long p = 0; p < np; ++p) {
+        for (int a = 0; a < 3; ++a) {  // velocities[i] = flow->sample(x)
+            const double nx = (pos[3 * p] - fg[a].o[0]) / h[0];
+            const double ny = (pos[3 * p + 1] - fg[a].o[1]) / h[1];
+            const double nz = (pos[3 * p + 2] - fg[a].o[2]) / h[2];
+            vel[3 * p + a] = trilinear<double, double>(grids[a], fg[a].s, nx, ny, nz);
+        }
+        for (int a = 0; a < 3; ++a) {
+            double q[3];
+            apicClamp(F, a, pos + 3 * p, q);
+            // getCoordinatesAndGradientWeights (array_samplers3-inl.h:196-261).
+            const Size3 s = fg[a].s;
+            long i, j, k;
+            double fx, fy, fz;
+            barycentric<double>((q[0] - fg[a].o[0]) / h[0], s.x - 1, &i, &fx);
+            barycentric<double>((q[1] - fg[a].o[1]) / h[1], s.y - 1, &j, &fy);
+            barycentric<double>((q[2] - fg[a].o[2]) / h[2], s.z - 1, &k, &fz);
+            const long ip1 = std::min(i + 1, s.x - 1), jp1 = std::min(j + 1, s.y - 1),
+                       kp1 = std::min(k + 1, s.z - 1);
+            const long idx[8] = {lin(s, i, j, k),     lin(s, ip1, j, k),
+                                 lin(s, i, jp1, k),   lin(s, ip1, jp1, k),
+                                 lin(s, i, j, kp1),   lin(s, ip1, j, kp1),
+                                 lin(s, i, jp1, kp1), lin(s, ip1, jp1, kp1)};
+            const double ix = ih[0], iy = ih[1], iz = ih[2];
+            const double gw[8][3] = {
+                {-ix * (1 - fy) * (1 - fz), -iy * (1 - fx) * (1 - fz), -iz * (1 - fx) * (1 - fy)},
+                {ix * (1 - fy) * (1 - fz), fx * (-iy) * (1 - fz), fx * (1 - fy) * (-iz)},
+                {(-ix) * fy * (1 - fz), (1 - fx) * iy * (1 - fz), (1 - fx) * fy * (-iz)},
+                {ix * fy * (1 - fz), fx * iy * (1 - fz), fx * fy * (-iz)},
+                {(-ix) * (1 - fy) * fz, (1 - fx) * (-iy) * fz, (1 - fx) * (1 - fy) * iz},
+                {ix * (1 - fy) * fz, fx * (-iy) * fz, fx * (1 - fy) * iz},
+                {(-ix) * fy * fz, (1 - fx) * iy * fz, (1 - fx) * fy * iz},
+                {ix * fy * fz, fx * iy * fz, fx * fy * iz}};
+            double C[3] = {0.0, 0.0, 0.0};
+            for (int n = 0; n < 8; ++n) {
+                const double val = grids[a][idx[n]];
+                for (int d = 0; d < 3; ++d) C[d] = C[d] + gw[n][d] * val;
+            }
+            for (int d = 0; d < 3; ++d) affine[9 * p + 3 * a + d] = C[d];
+        }
+    }
+}
+
 // extrapolateToRegion (include/jet/detail/array_utils-inl.h:172-244). An
 // iteration writes only cells invalid at its start and reads only cells
 // valid at its start, so it is order-independent.

@@ -542,6 +542,65 @@ void orc_build_particle_sdf(const orc_grid* g, long np, const double* pos,
     std::memcpy(out, acc.data(), sizeof(double) * res.x * res.y * res.z);
 }
 
+namespace {
+std::unique_ptr<ApicSolver3> makeApic(const orc_grid* g, long np,
+                                      const double* pos, const double* vel) {
+    Logging::mute();
+    auto s = std::make_unique<ApicSolver3>(
+        Size3(g->res[0], g->res[1], g->res[2]),
+        Vector3D(g->spacing[0], g->spacing[1], g->spacing[2]),
+        Vector3D(g->origin[0], g->origin[1], g->origin[2]));
+    Array1<Vector3D> P(np), V(np), F(np);
+    for (long i = 0; i < np; ++i) {
+        P[i] = Vector3D(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]);
+        V[i] = Vector3D(vel[3 * i], vel[3 * i + 1], vel[3 * i + 2]);
+    }
+    s->particleSystemData()->addParticles(P.constAccessor(), V.constAccessor(),
+                                          F.constAccessor());
+    return s;
+}
+}  // namespace
+
+void orc_apic_p2g(const orc_grid* g, long np, const double* pos,
+                  const double* vel, const double* affine, double* u,
+                  double* v, double* w, char* mu, char* mv, char* mw) {
+    auto s = makeApic(g, np, pos, vel);
+    s->_cX.resize(np);
+    s->_cY.resize(np);
+    s->_cZ.resize(np);
+    for (long i = 0; i < np; ++i) {
+        const double* c = affine + 9 * i;
+        s->_cX[i] = Vector3D(c[0], c[1], c[2]);
+        s->_cY[i] = Vector3D(c[3], c[4], c[5]);
+        s->_cZ[i] = Vector3D(c[6], c[7], c[8]);
+    }
+    s->transferFromParticlesToGrids();
+    readGrid(*s->gridSystemData()->velocity(), u, v, w);
+    auto cpyc = [](const Array3<char>& a, char* d) {
+        if (d) std::memcpy(d, a.data(), a.size().x * a.size().y * a.size().z);
+    };
+    cpyc(s->_uMarkers, mu);
+    cpyc(s->_vMarkers, mv);
+    cpyc(s->_wMarkers, mw);
+}
+
+void orc_apic_g2p(const orc_grid* g, long np, const double* pos, double* vel,
+                  double* affine, const double* u, const double* v,
+                  const double* w) {
+    auto s = makeApic(g, np, pos, vel);
+    fillGrid(s->gridSystemData()->velocity().get(), u, v, w);
+    s->transferFromGridsToParticles();
+    auto vs = s->particleSystemData()->velocities();
+    for (long i = 0; i < np; ++i) {
+        for (int d = 0; d < 3; ++d) {
+            vel[3 * i + d] = vs[i][d];
+            affine[9 * i + d] = s->_cX[i][d];
+            affine[9 * i + 3 + d] = s->_cY[i][d];
+            affine[9 * i + 6 + d] = s->_cZ[i][d];
+        }
+    }
+}
+
 void orc_flip_run(const orc_grid* g, long np, double* pos, double* vel,
                   int frames, double fps, double max_cfl, int closed,
                   const double gravity[3], int flip, const orc_mg_params* p) {
@@ -550,8 +609,10 @@ void orc_flip_run(const orc_grid* g, long np, double* pos, double* vel,
     const Vector3D h(g->spacing[0], g->spacing[1], g->spacing[2]);
     const Vector3D o(g->origin[0], g->origin[1], g->origin[2]);
     std::shared_ptr<PicSolver3> s;
-    if (flip)
+    if (flip == 1)
         s = std::make_shared<FlipSolver3>(res, h, o);
+    else if (flip == 2)
+        s = std::make_shared<ApicSolver3>(res, h, o);
     else
         s = std::make_shared<PicSolver3>(res, h, o);
     auto particles = s->particleSystemData();

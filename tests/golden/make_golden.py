@@ -38,6 +38,10 @@ Every fixture holds inputs and the reference's outputs for one small case:
   FdmMgpcgSolver3 at tolerance 1e-10, advection) for 3 frames of 1/60 s on
   the 64^3 dam break's geometry at 24^3 (water box [0,.25]x[0,.75]x[0,1],
   8 particles per cell from seed 0, closed walls, gravity (0,-9.8,0)).
+* apic_20x12x16.npz — ApicSolver3's transfers for 2,000 particles (some
+  outside the box) on an anisotropic grid: P2G with random affine matrices,
+  G2P from a random grid; and ApicSolver3 for 3 frames of the 24^3 dam break
+  (as flip_dam_break_24.npz).
 * rng_streams.npz — the first doubles of std::mt19937(seed) +
   std::uniform_real_distribution<double>(0,1) for seeds 0, 1, 2, produced by
   a C++ program compiled here.
@@ -284,6 +288,33 @@ def flip_dam_break(ref):
          pic_vel=pv)
 
 
+def apic(ref):
+    res = (20, 12, 16)
+    nx, ny, nz = res
+    h = (0.05, 0.07, 0.06)
+    org = (0.1, -0.2, 0.05)
+    rng = np.random.default_rng(29)
+    lo = np.array(org)
+    hi = lo + np.array(h) * np.array(res)
+    pos = lo + (hi - lo) * rng.uniform(-0.05, 1.05, (2000, 3))
+    vel = rng.uniform(-1, 1, (2000, 3))
+    aff = rng.uniform(-2, 2, (2000, 9))
+    grids, marks = ref.apic_p2g(res, h, org, pos, vel, aff)
+    g2 = [rng.uniform(-1, 1, (nz, ny, nx + 1)), rng.uniform(-1, 1, (nz, ny + 1, nx)),
+          rng.uniform(-1, 1, (nz + 1, ny, nx))]
+    gv, ga = ref.apic_g2p(res, h, org, pos, g2)
+    n = 24
+    d0, dv0 = scenes.dam_break_particles(n, (0.25, 0.75, 1.0), seed=0)
+    p = oracle.MgParams(100, 5, 5, 5, 20, 20, 1e-10, 1.5, True)
+    ap, av = ref.flip_run((n, n, n), (1 / n,) * 3, (0, 0, 0), d0, dv0, 3,
+                          flip=2, params=p)
+    save("apic_20x12x16.npz", res=np.array(res), h=np.array(h),
+         origin=np.array(org), pos=pos, vel=vel, affine=aff, u=grids[0],
+         v=grids[1], w=grids[2], mu=marks[0], mv=marks[1], mw=marks[2],
+         gu=g2[0], gv=g2[1], gw=g2[2], g2p_vel=gv, g2p_affine=ga,
+         dam_pos=ap, dam_vel=av)
+
+
 def rng_streams():
     with tempfile.TemporaryDirectory() as td:
         src = os.path.join(td, "rng.cpp")
@@ -311,6 +342,7 @@ def main():
     particles(ref)
     particle_sdf(ref)
     flip_dam_break(ref)
+    apic(ref)
     rng_streams()
 
 
