@@ -1,6 +1,7 @@
 // GPU drop-in for Jet's GridPressureSolver3: argument marshalling onto the
 // C ABI of libjetgpu. See gpu_fractional_pressure_solver3.h.
 #include "gpu_fractional_pressure_solver3.h"
+#include "gpu_fractional_boundary_condition_solver3.h"
 
 #include <jet/cell_centered_scalar_grid3.h>
 #include <jet/constant_scalar_field3.h>
@@ -30,7 +31,9 @@ GpuFractionalSinglePhasePressureSolver3::
 GridBoundaryConditionSolver3Ptr
 GpuFractionalSinglePhasePressureSolver3::suggestedBoundaryConditionSolver()
     const {
-    return std::make_shared<GridFractionalBoundaryConditionSolver3>();
+    // The fractional boundary solver the reference suggests (:486-490),
+    // with constrainVelocity on the GPU.
+    return std::make_shared<GpuFractionalBoundaryConditionSolver3>(&_config);
 }
 
 jetgpu_scalar_field GpuFractionalSinglePhasePressureSolver3::describe(

@@ -53,8 +53,10 @@ class GpuFractionalSinglePhasePressureSolver3 : public jet::GridPressureSolver3 
                    jet::ConstantScalarField3(-jet::kMaxD),
                bool useCompressed = false) override;
 
-    //! GridFractionalBoundaryConditionSolver3, as the reference's fractional
-    //! solver suggests (grid_fractional_single_phase_pressure_solver3.cpp:486-490).
+    //! GpuFractionalBoundaryConditionSolver3 (a
+    //! GridFractionalBoundaryConditionSolver3 whose constrainVelocity runs on
+    //! the GPU), as the reference's fractional solver suggests its CPU class
+    //! (grid_fractional_single_phase_pressure_solver3.cpp:486-490).
     jet::GridBoundaryConditionSolver3Ptr suggestedBoundaryConditionSolver()
         const override;
 

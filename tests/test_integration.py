@@ -5,7 +5,9 @@ against the reference's own headers, links it with the reference library
 (oracle/_ref/libjet_ref.a) and libjetgpu.so, and runs a program that
 installs the GPU solver with setPressureSolver() on FlipSolver3, PicSolver3,
 GridSmokeSolver3 and LevelSetLiquidSolver3 — the reference's install point
-(src/jet/grid_fluid_solver3.cpp:110-121). No solve runs (no GPU here); the
+(src/jet/grid_fluid_solver3.cpp:110-121) — and checks that the GPU
+boundary-condition solver is the one it suggests (setPressureSolver installs
+the suggestion). No solve runs (no GPU here); the
 CUDA context is created lazily on the first solve. Skipped where the
 reference sources are absent.
 """
@@ -21,6 +23,7 @@ REF = "/root/reference"
 MAIN = r"""
 #include <jet/jet.h>
 #include "gpu_fractional_pressure_solver3.h"
+#include "gpu_fractional_boundary_condition_solver3.h"
 #include <cstdio>
 #include <memory>
 
@@ -41,6 +44,9 @@ int main() {
     jetgpu_jet::GpuFractionalSinglePhasePressureSolver3 s;
     ok &= std::dynamic_pointer_cast<jet::GridFractionalBoundaryConditionSolver3>(
               s.suggestedBoundaryConditionSolver()) != nullptr;
+    ok &= std::dynamic_pointer_cast<jetgpu_jet::GpuFractionalBoundaryConditionSolver3>(
+              s.suggestedBoundaryConditionSolver()) != nullptr;
+
     std::printf("%s %s\n", ok ? "installed" : "FAILED", jetgpu_version());
     return ok ? 0 : 1;
 }
@@ -66,6 +72,7 @@ def test_cpp_adapter_installs_into_jet_solvers(tmp_path):
            "-I" + os.path.join(REF, "external"),
            "-I" + os.path.join(REPO, "include"), "-I" + plugin,
            str(main), os.path.join(plugin, "gpu_fractional_pressure_solver3.cpp"),
+           os.path.join(plugin, "gpu_fractional_boundary_condition_solver3.cpp"),
            ref_a, lib, "-Wl,-rpath," + os.path.dirname(lib), "-o", str(exe)]
     r = subprocess.run(cmd, capture_output=True, text=True)
     assert r.returncode == 0, r.stderr[-3000:]
