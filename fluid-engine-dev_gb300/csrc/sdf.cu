@@ -12,12 +12,14 @@
 // a window that covers its band (K21d). Exactness: sqrt is correctly rounded
 // and monotone, so min over sqrt(d^2) = sqrt(min d^2); d^2 is formed in FP64
 // in the reference's order (this unit is built with -fmad=false) and filtered
-// with the reference's `<= band^2`. An FP32 copy of the coordinates rejects
-// the particles whose FP32 squared distance exceeds the band, or the best so
-// far, by more than a bound on the FP32 error (`slack`, computed on the host
-// from the grid's extent), so the FP64 work is spent on the few candidates
-// near the minimum only. Bound: FP32 issue over the 5x5x5 window (L1/L2
-// traffic), then HBM for the sort.
+// with the reference's `<= band^2`. An FP32 copy of the coordinates gives
+// the minimum squared distance to within a proven error bound (`slack`,
+// computed on the host from the grid's extent); the exact FP64 distance is
+// then formed only for the particles within that bound of the FP32 minimum
+// (one or two per cell), and the 5x5x5 window is scanned only when the 3x3x3
+// bins around the cell do not already hold a particle nearer than any
+// outside them. Bound: FP32 issue and L1 traffic over the bins, then HBM for
+// the sort.
 
 #include "ctx.h"
 #include "sampling.cuh"
@@ -178,25 +180,33 @@ __global__ void k_sdf_cells(SdfGeom G, const int* __restrict__ off,
         const float cx = (float)(pt[0] - G.o[0]), cy = (float)(pt[1] - G.o[1]),
                     cz = (float)(pt[2] - G.o[2]);
         double best = INFINITY;     // exact squared distance of the nearest
-        float best_f = band2f;      // FP32 estimate of min(band^2, best)
         const int z0 = max(k - G.win[2], 0), z1 = min(k + G.win[2], G.n.z - 1);
         const int y0 = max(j - G.win[1], 0), y1 = min(j + G.win[1], G.n.y - 1);
         const int x0 = max(i - G.win[0], 0), x1 = min(i + G.win[0], G.n.x - 1);
-        // Particles of bins e0 .. e1 (a run of one row).
-        auto scan = [&](int e0, int e1) {
+        // Two passes per region: the FP32 minimum mf of the squared
+        // distances, then the exact FP64 distance of the particles within
+        // 2 * slack of it. A particle skipped by the second pass is farther
+        // (exactly) than the one that set mf, so it cannot be the minimum,
+        // and if that one is outside the band so is it.
+        float mf = band2f;
+        auto min_f = [&](int e0, int e1) {
             for (int e = e0; e < e1; ++e) {
                 const float4 p = sf[e];
                 const float dx = p.x - cx, dy = p.y - cy, dz = p.z - cz;
-                const float d2f = dx * dx + dy * dy + dz * dz;
-                if (d2f > best_f + 2.0f * G.slack) continue;
+                mf = fminf(mf, dx * dx + dy * dy + dz * dz);
+            }
+        };
+        auto exact = [&](int e0, int e1) {
+            const float thr = mf + 2.0f * G.slack;
+            for (int e = e0; e < e1; ++e) {
+                const float4 p = sf[e];
+                const float dx = p.x - cx, dy = p.y - cy, dz = p.z - cz;
+                if (dx * dx + dy * dy + dz * dz > thr) continue;
                 const double* x = sp + 3 * (long)e;
                 const double d0 = x[0] - pt[0], d1 = x[1] - pt[1],
                              d2 = x[2] - pt[2];
                 const double dd = d0 * d0 + d1 * d1 + d2 * d2;
-                if (dd <= G.band2 && dd < best) {
-                    best = dd;
-                    best_f = fminf(best_f, d2f);
-                }
+                if (dd <= G.band2 && dd < best) best = dd;
             }
         };
         // The 3x3x3 bins around the cell first. A particle in any other bin
@@ -207,22 +217,32 @@ __global__ void k_sdf_cells(SdfGeom G, const int* __restrict__ off,
         const int ix0 = max(i - 1, 0), ix1 = min(i + 1, G.n.x - 1);
         const int iy0 = max(j - 1, 0), iy1 = min(j + 1, G.n.y - 1);
         const int iz0 = max(k - 1, 0), iz1 = min(k + 1, G.n.z - 1);
-        for (int bz = iz0; bz <= iz1; ++bz)
-            for (int by = iy0; by <= iy1; ++by) {
-                const long row = (long)G.n.x * (by + (long)G.n.y * bz);
-                scan(off[row + ix0], off[row + ix1 + 1]);
-            }
-        if (!(best < G.inner2)) {
+        auto inner = [&](auto&& f) {
+            for (int bz = iz0; bz <= iz1; ++bz)
+                for (int by = iy0; by <= iy1; ++by) {
+                    const long row = (long)G.n.x * (by + (long)G.n.y * bz);
+                    f(off[row + ix0], off[row + ix1 + 1]);
+                }
+        };
+        auto outer = [&](auto&& f) {
             for (int bz = z0; bz <= z1; ++bz)
                 for (int by = y0; by <= y1; ++by) {
                     const long row = (long)G.n.x * (by + (long)G.n.y * bz);
                     if (bz >= iz0 && bz <= iz1 && by >= iy0 && by <= iy1) {
-                        if (x0 < ix0) scan(off[row + x0], off[row + ix0]);
-                        if (ix1 < x1) scan(off[row + ix1 + 1], off[row + x1 + 1]);
+                        if (x0 < ix0) f(off[row + x0], off[row + ix0]);
+                        if (ix1 < x1) f(off[row + ix1 + 1], off[row + x1 + 1]);
                     } else {
-                        scan(off[row + x0], off[row + x1 + 1]);
+                        f(off[row + x0], off[row + x1 + 1]);
                     }
                 }
+        };
+        inner(min_f);
+        inner(exact);
+        if (!(best < G.inner2)) {
+            // A lower mf only shrinks the threshold, so the inner particles
+            // already checked cover every inner candidate.
+            outer(min_f);
+            outer(exact);
         }
         double minDist = G.band;
         if (best <= G.band2) {
