@@ -244,14 +244,16 @@ jetgpu_status solve_pressure_dev(
     const double* w, const jetgpu_scalar_field* bsdf, const double* bdata,
     const jetgpu_scalar_field* fsdf, const double* fdata, const double* su,
     const double* sv, const double* sw, double* ou, double* ov, double* ow,
-    double* op, jetgpu_solve_stats* st) {
+    double* op, jetgpu_solve_stats* st, const SolveIo* io) {
     auto t0 = std::chrono::steady_clock::now();
     const Dims n{grid->res[0], grid->res[1], grid->res[2]};
     jetgpu_status s = ensure_buffers(c, n, c->cfg.max_levels);
     if (s != JETGPU_OK) return s;
     const GridDesc g = to_desc(grid);
+    if (io) JG_CUDA(c, cudaStreamWaitEvent(c->stream, io->sdf_in, 0));
     s = build_weights(c, g, to_desc(bsdf, bdata), to_desc(fsdf, fdata));
     if (s != JETGPU_OK) return s;
+    if (io) JG_CUDA(c, cudaStreamWaitEvent(c->stream, io->vel_in, 0));
     s = build_system(c, g, u, v, w, su, sv, sw);
     if (s != JETGPU_OK) return s;
     s = prepare_levels(c);
@@ -263,10 +265,20 @@ jetgpu_status solve_pressure_dev(
     if (!usable(solve_status))
         return solve_status;
     const double solve = ms_since(t1);
+    if (io && io->host_p)
+        JG_CUDA(c, cudaEventRecord(io->x_final, c->stream));
     // The reference applies the gradient whatever the solver returned
     // (grid_fractional_single_phase_pressure_solver3.cpp:466-483).
     s = apply_gradient(c, g, u, v, w, ou, ov, ow);
     if (s != JETGPU_OK) return s;
+    // Issued after the gradient launch, so that a pageable destination
+    // (whose copy blocks the host) still overlaps the gradient kernel.
+    if (io && io->host_p) {
+        JG_CUDA(c, cudaStreamWaitEvent(io->copy, io->x_final, 0));
+        JG_CUDA(c, cudaMemcpyAsync(io->host_p, c->x64,
+                                   n.count() * sizeof(double),
+                                   cudaMemcpyDeviceToHost, io->copy));
+    }
     if (op)
         JG_CUDA(c, cudaMemcpyAsync(op, c->x64, n.count() * sizeof(double),
                                    cudaMemcpyDeviceToDevice, c->stream));
@@ -326,6 +338,10 @@ jetgpu_status jetgpu_create(const jetgpu_config* cfg, jetgpu_ctx** out) {
                                           c->device));
         JG_CUDA(c, cudaStreamCreateWithFlags(&c->stream,
                                              cudaStreamNonBlocking));
+        JG_CUDA(c, cudaStreamCreateWithFlags(&c->copy_stream,
+                                             cudaStreamNonBlocking));
+        for (auto& e : c->io_ev)
+            JG_CUDA(c, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
         JG_CUDA(c, cudaMalloc((void**)&c->scal, S_COUNT * sizeof(double)));
         JG_CUDA(c, cudaMemset(c->scal, 0, S_COUNT * sizeof(double)));
         JG_CUDA(c, cudaMalloc((void**)&c->partials,
@@ -351,6 +367,7 @@ void jetgpu_destroy(jetgpu_ctx* c) {
     if (!c) return;
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
+    if (c->copy_stream) cudaStreamSynchronize(c->copy_stream);
     free_buffers(c);
     release(&c->scal);
     release(&c->partials);
@@ -385,6 +402,9 @@ void jetgpu_destroy(jetgpu_ctx* c) {
         release(&T.sfrac);
         release(&T.node);
     }
+    for (auto& e : c->io_ev)
+        if (e) cudaEventDestroy(e);
+    if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
@@ -445,11 +465,12 @@ jetgpu_status jetgpu_solve_pressure(
     JG_CUDA(c, cudaSetDevice(c->device));
     const long nx = grid->res[0], ny = grid->res[1], nz = grid->res[2];
     const size_t nu = (size_t)(nx + 1) * ny * nz, nv = (size_t)nx * (ny + 1) * nz,
-                 nw = (size_t)nx * ny * (nz + 1), nc = (size_t)nx * ny * nz;
+                 nw = (size_t)nx * ny * (nz + 1);
     const size_t nb = field_count(boundary_sdf), nf = field_count(fluid_sdf);
     const size_t ns = (solid_u ? nu : 0) + (solid_v ? nv : 0) + (solid_w ? nw : 0);
-    // Device staging: inputs u,v,w | solid | sdf data | outputs u,v,w | p.
-    const size_t total = 2 * (nu + nv + nw) + ns + nb + nf + nc;
+    // Device staging: inputs u,v,w | solid | sdf data | outputs u,v,w (the
+    // pressure is downloaded from the solver's own buffer).
+    const size_t total = 2 * (nu + nv + nw) + ns + nb + nf;
     s = grow_stage(c, total * sizeof(double));
     if (s != JETGPU_OK) return s;
     double* base = reinterpret_cast<double*>(c->stage);
@@ -470,21 +491,38 @@ jetgpu_status jetgpu_solve_pressure(
     double* ou = p;
     double* ov = ou + nu;
     double* ow = ov + nv;
-    double* dp = ow + nw;
-    cudaStream_t st = c->stream;
-    JG_CUDA(c, cudaMemcpyAsync(du, u, nu * 8, cudaMemcpyHostToDevice, st));
-    JG_CUDA(c, cudaMemcpyAsync(dv, v, nv * 8, cudaMemcpyHostToDevice, st));
-    JG_CUDA(c, cudaMemcpyAsync(dw, w, nw * 8, cudaMemcpyHostToDevice, st));
-    if (dsu) JG_CUDA(c, cudaMemcpyAsync(dsu, solid_u, nu * 8, cudaMemcpyHostToDevice, st));
-    if (dsv) JG_CUDA(c, cudaMemcpyAsync(dsv, solid_v, nv * 8, cudaMemcpyHostToDevice, st));
-    if (dsw) JG_CUDA(c, cudaMemcpyAsync(dsw, solid_w, nw * 8, cudaMemcpyHostToDevice, st));
-    if (db) JG_CUDA(c, cudaMemcpyAsync(db, boundary_sdf->data, nb * 8, cudaMemcpyHostToDevice, st));
-    if (df) JG_CUDA(c, cudaMemcpyAsync(df, fluid_sdf->data, nf * 8, cudaMemcpyHostToDevice, st));
+    // Uploads run in order on the copy stream: the SDFs first (the weights
+    // build needs only them and starts as soon as they are in), then the
+    // velocities, which stream in under the weights build. The copy stream
+    // first waits for anything still queued on the compute stream.
+    cudaStream_t st = c->stream, cs = c->copy_stream;
+    struct Join {  // no exit leaves a copy in flight
+        cudaStream_t s;
+        ~Join() { cudaStreamSynchronize(s); }
+    } join{cs};
+    SolveIo io;
+    io.sdf_in = c->io_ev[1];
+    io.vel_in = c->io_ev[2];
+    io.x_final = c->io_ev[3];
+    io.copy = cs;
+    io.host_p = out_pressure;
+    JG_CUDA(c, cudaEventRecord(c->io_ev[0], st));
+    JG_CUDA(c, cudaStreamWaitEvent(cs, c->io_ev[0], 0));
+    if (db) JG_CUDA(c, cudaMemcpyAsync(db, boundary_sdf->data, nb * 8, cudaMemcpyHostToDevice, cs));
+    if (df) JG_CUDA(c, cudaMemcpyAsync(df, fluid_sdf->data, nf * 8, cudaMemcpyHostToDevice, cs));
+    JG_CUDA(c, cudaEventRecord(io.sdf_in, cs));
+    JG_CUDA(c, cudaMemcpyAsync(du, u, nu * 8, cudaMemcpyHostToDevice, cs));
+    JG_CUDA(c, cudaMemcpyAsync(dv, v, nv * 8, cudaMemcpyHostToDevice, cs));
+    JG_CUDA(c, cudaMemcpyAsync(dw, w, nw * 8, cudaMemcpyHostToDevice, cs));
+    if (dsu) JG_CUDA(c, cudaMemcpyAsync(dsu, solid_u, nu * 8, cudaMemcpyHostToDevice, cs));
+    if (dsv) JG_CUDA(c, cudaMemcpyAsync(dsv, solid_v, nv * 8, cudaMemcpyHostToDevice, cs));
+    if (dsw) JG_CUDA(c, cudaMemcpyAsync(dsw, solid_w, nw * 8, cudaMemcpyHostToDevice, cs));
+    JG_CUDA(c, cudaEventRecord(io.vel_in, cs));
     jetgpu_solve_stats local;
     std::memset(&local, 0, sizeof(local));
     jetgpu_status solve_status = solve_pressure_dev(
         c, grid, du, dv, dw, boundary_sdf, db, fluid_sdf, df, dsu, dsv, dsw,
-        ou, ov, ow, out_pressure ? dp : nullptr, &local);
+        ou, ov, ow, nullptr, &local, &io);
     if (!usable(solve_status)) {
         if (stats) *stats = local;
         return solve_status;
@@ -492,9 +530,8 @@ jetgpu_status jetgpu_solve_pressure(
     JG_CUDA(c, cudaMemcpyAsync(out_u, ou, nu * 8, cudaMemcpyDeviceToHost, st));
     JG_CUDA(c, cudaMemcpyAsync(out_v, ov, nv * 8, cudaMemcpyDeviceToHost, st));
     JG_CUDA(c, cudaMemcpyAsync(out_w, ow, nw * 8, cudaMemcpyDeviceToHost, st));
-    if (out_pressure)
-        JG_CUDA(c, cudaMemcpyAsync(out_pressure, dp, nc * 8, cudaMemcpyDeviceToHost, st));
     JG_CUDA(c, cudaStreamSynchronize(st));
+    JG_CUDA(c, cudaStreamSynchronize(cs));
     local.total_ms = ms_since(t0);
     if (stats) *stats = local;
     return solve_status;

@@ -96,6 +96,10 @@ struct Ctx {
                                         // rows (0: not usable on this device)
     std::unordered_map<const void*, int> occupancy;  // blocks/SM per kernel
     cudaStream_t stream = nullptr;
+    // Host-pointer solves move data on copy_stream, ordered against the
+    // compute stream by io_ev (see SolveIo).
+    cudaStream_t copy_stream = nullptr;
+    cudaEvent_t io_ev[4] = {nullptr, nullptr, nullptr, nullptr};
     std::string err;
 
     // Allocated geometry.
@@ -305,6 +309,18 @@ jetgpu_status bc_apply(Ctx* c, const GridDesc& g, double* u, double* v,
 jetgpu_status extrapolate_region(Ctx* c, Dims s, double* data,
                                  const unsigned char* valid, unsigned iters);
 
+// Overlap of a host-pointer solve's copies with its kernels. The compute
+// stream waits for sdf_in before the weights build (which needs only the
+// SDFs) and for vel_in before the system build, so the velocity upload runs
+// under the weights; once the solve is final, x_final is recorded and the
+// pressure is downloaded on `copy` straight into host_p while the gradient
+// kernel runs.
+struct SolveIo {
+    cudaEvent_t sdf_in = nullptr, vel_in = nullptr, x_final = nullptr;
+    cudaStream_t copy = nullptr;
+    double* host_p = nullptr;
+};
+
 // GridFractionalSinglePhasePressureSolver3::solve on device arrays (api.cu):
 // the SDF descriptors' data pointers are replaced by bdata / fdata.
 jetgpu_status solve_pressure_dev(
@@ -312,7 +328,7 @@ jetgpu_status solve_pressure_dev(
     const double* w, const jetgpu_scalar_field* bsdf, const double* bdata,
     const jetgpu_scalar_field* fsdf, const double* fdata, const double* su,
     const double* sv, const double* sw, double* ou, double* ov, double* ow,
-    double* op, jetgpu_solve_stats* st);
+    double* op, jetgpu_solve_stats* st, const SolveIo* io = nullptr);
 
 jetgpu_status fluid_cfl(Ctx* c, const GridDesc& g, const double* u,
                         const double* v, const double* w, double dt,

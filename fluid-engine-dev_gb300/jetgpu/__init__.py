@@ -557,7 +557,7 @@ class GridFractionalSinglePhasePressureSolver3:
             if a.shape != ref.shape or a.dtype != np.float64 or not a.flags.c_contiguous:
                 raise ValueError("output arrays must match the input layout")
         nx, ny, nz = input.resolution
-        p = np.zeros((nz, ny, nx))
+        p = self._pressure_buffer((nz, ny, nx))
         solver = self._solver
         st = library().jetgpu_solve_pressure(
             solver.context(), C.byref(g), _p(u), _p(v), _p(w), C.byref(bs),
@@ -567,6 +567,23 @@ class GridFractionalSinglePhasePressureSolver3:
         solver.check(st, allow=SOLVED)
         self._pressure = p
         return st
+
+    def _pressure_buffer(self, shape) -> np.ndarray:
+        """The pressure output, kept across solves in page-locked memory when
+        torch can provide it (the device-to-host copy then runs at full
+        bandwidth; a fresh pageable array per solve costs page faults and a
+        staged copy)."""
+        buf = getattr(self, "_pbuf", None)
+        if buf is None or buf.shape != tuple(shape):
+            try:
+                import torch
+                t = torch.empty(tuple(shape), dtype=torch.float64).pin_memory()
+                self._pbuf_owner = t
+                buf = t.numpy()
+            except Exception:  # no torch or no CUDA driver: pageable memory
+                buf = np.empty(tuple(shape))
+            self._pbuf = buf
+        return buf
 
     def level(self, level: int, what: str) -> np.ndarray:
         """Internal weights/system of the last solve (for parity checks)."""
