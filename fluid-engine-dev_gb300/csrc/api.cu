@@ -244,17 +244,19 @@ jetgpu_status solve_pressure_dev(
     const double* w, const jetgpu_scalar_field* bsdf, const double* bdata,
     const jetgpu_scalar_field* fsdf, const double* fdata, const double* su,
     const double* sv, const double* sw, double* ou, double* ov, double* ow,
-    double* op, jetgpu_solve_stats* st, const SolveIo* io) {
+    double* op, jetgpu_solve_stats* st, const SolveIo* io, bool blocked) {
     auto t0 = std::chrono::steady_clock::now();
     const Dims n{grid->res[0], grid->res[1], grid->res[2]};
     jetgpu_status s = ensure_buffers(c, n, c->cfg.max_levels);
     if (s != JETGPU_OK) return s;
     const GridDesc g = to_desc(grid);
     if (io) JG_CUDA(c, cudaStreamWaitEvent(c->stream, io->sdf_in, 0));
-    s = build_weights(c, g, to_desc(bsdf, bdata), to_desc(fsdf, fdata));
+    s = blocked ? blocked_markers(c, g, to_desc(bsdf, bdata), to_desc(fsdf, fdata))
+                : build_weights(c, g, to_desc(bsdf, bdata), to_desc(fsdf, fdata));
     if (s != JETGPU_OK) return s;
     if (io) JG_CUDA(c, cudaStreamWaitEvent(c->stream, io->vel_in, 0));
-    s = build_system(c, g, u, v, w, su, sv, sw);
+    s = blocked ? blocked_system(c, g, u, v, w)
+                : build_system(c, g, u, v, w, su, sv, sw);
     if (s != JETGPU_OK) return s;
     s = prepare_levels(c);
     if (s != JETGPU_OK) return s;
@@ -268,8 +270,10 @@ jetgpu_status solve_pressure_dev(
     if (io && io->host_p)
         JG_CUDA(c, cudaEventRecord(io->x_final, c->stream));
     // The reference applies the gradient whatever the solver returned
-    // (grid_fractional_single_phase_pressure_solver3.cpp:466-483).
-    s = apply_gradient(c, g, u, v, w, ou, ov, ow);
+    // (grid_fractional_single_phase_pressure_solver3.cpp:466-483,
+    // grid_single_phase_pressure_solver3.cpp:194-210).
+    s = blocked ? blocked_gradient(c, g, u, v, w, ou, ov, ow)
+                : apply_gradient(c, g, u, v, w, ou, ov, ow);
     if (s != JETGPU_OK) return s;
     // Issued after the gradient launch, so that a pageable destination
     // (whose copy blocks the host) still overlaps the gradient kernel.
@@ -382,6 +386,7 @@ void jetgpu_destroy(jetgpu_ctx* c) {
     release(&c->sdf_int);
     release(&c->sdf_dbl);
     release(&c->sdf_valid);
+    release(&c->blk_marks);
     release(&c->flip_marks);
     release(&c->flip_snap);
     release(&c->flip_solid);
@@ -423,13 +428,13 @@ jetgpu_status jetgpu_set_config(jetgpu_ctx* c, const jetgpu_config* cfg) {
     return JETGPU_OK;
 }
 
-jetgpu_status jetgpu_solve_pressure_device(
+static jetgpu_status solve_device(
     jetgpu_ctx* c, const jetgpu_grid* grid, const double* u, const double* v,
     const double* w, const jetgpu_scalar_field* boundary_sdf,
     const jetgpu_scalar_field* fluid_sdf, const double* solid_u,
     const double* solid_v, const double* solid_w, double* out_u,
     double* out_v, double* out_w, double* out_pressure,
-    jetgpu_solve_stats* stats) {
+    jetgpu_solve_stats* stats, bool blocked) {
     if (!c) return JETGPU_BAD_INPUT;
     jetgpu_status s = check_grid(c, grid);
     if (s != JETGPU_OK) return s;
@@ -442,18 +447,42 @@ jetgpu_status jetgpu_solve_pressure_device(
     std::memset(&local, 0, sizeof(local));
     s = solve_pressure_dev(c, grid, u, v, w, boundary_sdf, boundary_sdf->data,
                            fluid_sdf, fluid_sdf->data, solid_u, solid_v,
-                           solid_w, out_u, out_v, out_w, out_pressure, &local);
+                           solid_w, out_u, out_v, out_w, out_pressure, &local,
+                           nullptr, blocked);
     if (stats) *stats = local;
     return s;
 }
 
-jetgpu_status jetgpu_solve_pressure(
+jetgpu_status jetgpu_solve_pressure_device(
     jetgpu_ctx* c, const jetgpu_grid* grid, const double* u, const double* v,
     const double* w, const jetgpu_scalar_field* boundary_sdf,
     const jetgpu_scalar_field* fluid_sdf, const double* solid_u,
     const double* solid_v, const double* solid_w, double* out_u,
     double* out_v, double* out_w, double* out_pressure,
     jetgpu_solve_stats* stats) {
+    return solve_device(c, grid, u, v, w, boundary_sdf, fluid_sdf, solid_u,
+                        solid_v, solid_w, out_u, out_v, out_w, out_pressure,
+                        stats, false);
+}
+
+jetgpu_status jetgpu_solve_pressure_blocked_device(
+    jetgpu_ctx* c, const jetgpu_grid* grid, const double* u, const double* v,
+    const double* w, const jetgpu_scalar_field* boundary_sdf,
+    const jetgpu_scalar_field* fluid_sdf, double* out_u, double* out_v,
+    double* out_w, double* out_pressure, jetgpu_solve_stats* stats) {
+    return solve_device(c, grid, u, v, w, boundary_sdf, fluid_sdf, nullptr,
+                        nullptr, nullptr, out_u, out_v, out_w, out_pressure,
+                        stats, true);
+}
+
+// The host-pointer solve of either pressure solver (see solve_pressure_dev).
+static jetgpu_status solve_host(
+    jetgpu_ctx* c, const jetgpu_grid* grid, const double* u, const double* v,
+    const double* w, const jetgpu_scalar_field* boundary_sdf,
+    const jetgpu_scalar_field* fluid_sdf, const double* solid_u,
+    const double* solid_v, const double* solid_w, double* out_u,
+    double* out_v, double* out_w, double* out_pressure,
+    jetgpu_solve_stats* stats, bool blocked) {
     if (!c) return JETGPU_BAD_INPUT;
     auto t0 = std::chrono::steady_clock::now();
     jetgpu_status s = check_grid(c, grid);
@@ -522,7 +551,7 @@ jetgpu_status jetgpu_solve_pressure(
     std::memset(&local, 0, sizeof(local));
     jetgpu_status solve_status = solve_pressure_dev(
         c, grid, du, dv, dw, boundary_sdf, db, fluid_sdf, df, dsu, dsv, dsw,
-        ou, ov, ow, nullptr, &local, &io);
+        ou, ov, ow, nullptr, &local, &io, blocked);
     if (!usable(solve_status)) {
         if (stats) *stats = local;
         return solve_status;
@@ -535,6 +564,28 @@ jetgpu_status jetgpu_solve_pressure(
     local.total_ms = ms_since(t0);
     if (stats) *stats = local;
     return solve_status;
+}
+
+jetgpu_status jetgpu_solve_pressure(
+    jetgpu_ctx* c, const jetgpu_grid* grid, const double* u, const double* v,
+    const double* w, const jetgpu_scalar_field* boundary_sdf,
+    const jetgpu_scalar_field* fluid_sdf, const double* solid_u,
+    const double* solid_v, const double* solid_w, double* out_u,
+    double* out_v, double* out_w, double* out_pressure,
+    jetgpu_solve_stats* stats) {
+    return solve_host(c, grid, u, v, w, boundary_sdf, fluid_sdf, solid_u,
+                      solid_v, solid_w, out_u, out_v, out_w, out_pressure,
+                      stats, false);
+}
+
+jetgpu_status jetgpu_solve_pressure_blocked(
+    jetgpu_ctx* c, const jetgpu_grid* grid, const double* u, const double* v,
+    const double* w, const jetgpu_scalar_field* boundary_sdf,
+    const jetgpu_scalar_field* fluid_sdf, double* out_u, double* out_v,
+    double* out_w, double* out_pressure, jetgpu_solve_stats* stats) {
+    return solve_host(c, grid, u, v, w, boundary_sdf, fluid_sdf, nullptr,
+                      nullptr, nullptr, out_u, out_v, out_w, out_pressure,
+                      stats, true);
 }
 
 jetgpu_status jetgpu_mgpcg_solve_system(jetgpu_ctx* c, const int res0[3],

@@ -174,6 +174,11 @@ struct Ctx {
     double* sdf_dbl = nullptr;
     unsigned char* sdf_valid = nullptr;
 
+    // Blocked pressure solver (blocked.cu): cell markers of every level,
+    // finest first.
+    size_t blk_cap = 0;
+    unsigned char* blk_marks = nullptr;
+
     cudaEvent_t ev[4] = {nullptr, nullptr, nullptr, nullptr};
 
     // Learned preconditioner (opaque; see unet.cu).
@@ -250,6 +255,18 @@ jetgpu_status apply_gradient(Ctx* c, const GridDesc& g, const double* u,
                              const double* v, const double* w, double* ou,
                              double* ov, double* ow);
 
+// ---- blocked.cu ------------------------------------------------------------
+// GridSinglePhasePressureSolver3: markers of every level (and phi = -1 for
+// fluid, +1 otherwise, for the V-cycle's masked restriction), the rows of
+// every level with the finest-level rhs, and the pressure gradient.
+jetgpu_status blocked_markers(Ctx* c, const GridDesc& g, const FieldDesc& bsdf,
+                              const FieldDesc& fsdf);
+jetgpu_status blocked_system(Ctx* c, const GridDesc& g, const double* u,
+                             const double* v, const double* w);
+jetgpu_status blocked_gradient(Ctx* c, const GridDesc& g, const double* u,
+                               const double* v, const double* w, double* ou,
+                               double* ov, double* ow);
+
 // ---- mgpcg.cu -------------------------------------------------------------
 // Allocates the multigrid hierarchy and solver buffers for resolution n.
 jetgpu_status ensure_buffers(Ctx* c, Dims n, unsigned max_levels);
@@ -322,13 +339,16 @@ struct SolveIo {
 };
 
 // GridFractionalSinglePhasePressureSolver3::solve on device arrays (api.cu):
-// the SDF descriptors' data pointers are replaced by bdata / fdata.
+// the SDF descriptors' data pointers are replaced by bdata / fdata. With
+// `blocked`, GridSinglePhasePressureSolver3::solve instead (blocked.cu; the
+// solid velocities are ignored, as the reference ignores boundaryVelocity).
 jetgpu_status solve_pressure_dev(
     Ctx* c, const jetgpu_grid* grid, const double* u, const double* v,
     const double* w, const jetgpu_scalar_field* bsdf, const double* bdata,
     const jetgpu_scalar_field* fsdf, const double* fdata, const double* su,
     const double* sv, const double* sw, double* ou, double* ov, double* ow,
-    double* op, jetgpu_solve_stats* st, const SolveIo* io = nullptr);
+    double* op, jetgpu_solve_stats* st, const SolveIo* io = nullptr,
+    bool blocked = false);
 
 jetgpu_status fluid_cfl(Ctx* c, const GridDesc& g, const double* u,
                         const double* v, const double* w, double dt,

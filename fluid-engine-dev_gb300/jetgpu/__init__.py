@@ -101,7 +101,8 @@ SOLVED = (0, 1, 2)  # OK, NOT_CONVERGED (last iterate applied), fallback used
 EXPORTS = (
     "jetgpu_config_default", "jetgpu_create", "jetgpu_destroy",
     "jetgpu_last_error", "jetgpu_set_config", "jetgpu_solve_pressure",
-    "jetgpu_solve_pressure_device", "jetgpu_mgpcg_solve_system",
+    "jetgpu_solve_pressure_device", "jetgpu_solve_pressure_blocked",
+    "jetgpu_solve_pressure_blocked_device", "jetgpu_mgpcg_solve_system",
     "jetgpu_p2g_device", "jetgpu_g2p_flip_device", "jetgpu_g2p_pic_device",
     "jetgpu_p2g", "jetgpu_g2p_flip", "jetgpu_g2p_pic", "jetgpu_get_level",
     "jetgpu_version", "jetgpu_get_stream", "jetgpu_profile",
@@ -190,6 +191,13 @@ def library() -> C.CDLL:
     L.jetgpu_solve_pressure.restype = C.c_int
     L.jetgpu_solve_pressure_device.argtypes = solve_args
     L.jetgpu_solve_pressure_device.restype = C.c_int
+    blocked_args = [vp, C.POINTER(Grid), dp, dp, dp, C.POINTER(ScalarField),
+                    C.POINTER(ScalarField), dp, dp, dp, dp,
+                    C.POINTER(SolveStats)]
+    L.jetgpu_solve_pressure_blocked.argtypes = blocked_args
+    L.jetgpu_solve_pressure_blocked.restype = C.c_int
+    L.jetgpu_solve_pressure_blocked_device.argtypes = blocked_args
+    L.jetgpu_solve_pressure_blocked_device.restype = C.c_int
     L.jetgpu_mgpcg_solve_system.argtypes = [vp, C.POINTER(C.c_int), C.c_int,
                                             dp, dp, dp, C.POINTER(SolveStats)]
     L.jetgpu_mgpcg_solve_system.restype = C.c_int
@@ -606,6 +614,68 @@ class GridFractionalSinglePhasePressureSolver3:
                                 out.nbytes, C.byref(cnt))
         solver.check(st)
         return out
+
+
+class GridSinglePhasePressureSolver3(GridFractionalSinglePhasePressureSolver3):
+    """Drop-in GPU GridSinglePhasePressureSolver3, the blocked solver
+    (include/jet/grid_single_phase_pressure_solver3.h:30-118): cells are
+    fluid, air or boundary by the SDFs at their centres and the system is the
+    7-point Laplacian on those markers. The reference defaults to an
+    FdmIccgSolver3 (grid_single_phase_pressure_solver3.cpp:173-175); this
+    solver runs the GPU FdmMgpcgSolver3, whose multigrid levels get the
+    reference's majority-vote coarse markers (:270-317)."""
+
+    @staticmethod
+    def suggestedBoundaryConditionSolver() -> str:
+        # grid_single_phase_pressure_solver3.cpp:213-216
+        return "GridBlockedBoundaryConditionSolver3"
+
+    def solve(self, input: FaceCenteredGrid3, timeIntervalInSeconds: float,
+              output: FaceCenteredGrid3,
+              boundarySdf=ConstantScalarField3(kMaxD),
+              boundaryVelocity=None,
+              fluidSdf=ConstantScalarField3(-kMaxD),
+              useCompressed: bool = False) -> int:
+        """Projects ``input`` into ``output`` (host arrays). Like the
+        reference, the boundary velocity is not used (:191) and
+        ``useCompressed`` changes only the storage. Returns the C status."""
+        del timeIntervalInSeconds, boundaryVelocity, useCompressed
+        keep = []
+        bs = _field(boundarySdf, keep)
+        fs = _field(fluidSdf, keep)
+        g = input.c_grid()
+        u = np.ascontiguousarray(input.u, np.float64)
+        v = np.ascontiguousarray(input.v, np.float64)
+        w = np.ascontiguousarray(input.w, np.float64)
+        for a, ref in ((output.u, u), (output.v, v), (output.w, w)):
+            if a.shape != ref.shape or a.dtype != np.float64 or not a.flags.c_contiguous:
+                raise ValueError("output arrays must match the input layout")
+        nx, ny, nz = input.resolution
+        p = self._pressure_buffer((nz, ny, nx))
+        solver = self._solver
+        st = library().jetgpu_solve_pressure_blocked(
+            solver.context(), C.byref(g), _p(u), _p(v), _p(w), C.byref(bs),
+            C.byref(fs), _p(output.u), _p(output.v), _p(output.w), _p(p),
+            C.byref(self.last_stats))
+        solver.last_stats = self.last_stats
+        solver.check(st, allow=SOLVED)
+        self._pressure = p
+        return st
+
+
+def solve_pressure_blocked_device(solver: FdmMgpcgSolver3, grid: Grid, u, v,
+                                  w, boundary: ScalarField,
+                                  fluid: ScalarField, out_u, out_v, out_w,
+                                  out_p=None,
+                                  stats: SolveStats | None = None) -> int:
+    """Device-pointer form of the blocked solve (torch CUDA float64)."""
+    stats = stats if stats is not None else SolveStats()
+    st = library().jetgpu_solve_pressure_blocked_device(
+        solver.context(), C.byref(grid), _p(u), _p(v), _p(w), C.byref(boundary),
+        C.byref(fluid), _p(out_u), _p(out_v), _p(out_w), _p(out_p),
+        C.byref(stats))
+    solver.last_stats = stats
+    return solver.check(st, allow=SOLVED)
 
 
 def solve_pressure_device(solver: FdmMgpcgSolver3, grid: Grid, u, v, w,

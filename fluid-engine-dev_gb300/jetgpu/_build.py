@@ -22,7 +22,7 @@ LIB = os.path.join(PKG, "libjetgpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
           "--expt-relaxed-constexpr", "-I" + os.path.join(ROOT, "..", "include")]
-EXACT_UNITS = {"build.cu", "transfer.cu", "boundary.cu", "sdf.cu"}
+EXACT_UNITS = {"build.cu", "transfer.cu", "boundary.cu", "sdf.cu", "blocked.cu"}
 
 
 def _nvcc() -> str:

@@ -174,6 +174,28 @@ jetgpu_status jetgpu_solve_pressure_device(
     double* out_v, double* out_w, double* out_pressure,
     jetgpu_solve_stats* stats);
 
+/* GridSinglePhasePressureSolver3::solve, the blocked solver
+ * (src/jet/grid_single_phase_pressure_solver3.cpp:183-211), with an MGPCG
+ * linear solver installed: buildMarkers (:245-322; a cell is boundary,
+ * fluid or air by the SDFs at its centre, coarse levels by majority),
+ * buildSystem (:341-376), the MGPCG solve and applyPressureGradient
+ * (:378-405). The reference ignores boundaryVelocity (:191), so it is not an
+ * argument. HOST pointers; arguments otherwise as jetgpu_solve_pressure:
+ * faces the reference leaves untouched keep the input values, out_pressure
+ * is GridSinglePhasePressureSolver3::pressure() (:229-235) or NULL. */
+jetgpu_status jetgpu_solve_pressure_blocked(
+    struct jetgpu_ctx* ctx, const jetgpu_grid* grid, const double* u,
+    const double* v, const double* w, const jetgpu_scalar_field* boundary_sdf,
+    const jetgpu_scalar_field* fluid_sdf, double* out_u, double* out_v,
+    double* out_w, double* out_pressure, jetgpu_solve_stats* stats);
+
+/* jetgpu_solve_pressure_blocked with every array in DEVICE memory. */
+jetgpu_status jetgpu_solve_pressure_blocked_device(
+    struct jetgpu_ctx* ctx, const jetgpu_grid* grid, const double* u,
+    const double* v, const double* w, const jetgpu_scalar_field* boundary_sdf,
+    const jetgpu_scalar_field* fluid_sdf, double* out_u, double* out_v,
+    double* out_w, double* out_pressure, jetgpu_solve_stats* stats);
+
 /* FdmMgpcgSolver3::solve(FdmMgLinearSystem3*)
  * (src/jet/fdm_mgpcg_solver3.cpp:54-80) on a caller-built multigrid system.
  * HOST pointers. Levels are concatenated finest first; level l has

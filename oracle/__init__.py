@@ -163,6 +163,13 @@ class Oracle:
             C.POINTER(OrcGrid), _dp, _dp, _dp, C.POINTER(OrcField),
             C.POINTER(OrcField), _dp, _dp, _dp, C.POINTER(OrcMgParams),
             _dp, _dp, _dp, _dp, C.POINTER(C.c_uint), _dp]
+        L.orc_blocked_pressure_solve.restype = C.c_int
+        L.orc_blocked_pressure_solve.argtypes = [
+            C.POINTER(OrcGrid), _dp, _dp, _dp, C.POINTER(OrcField),
+            C.POINTER(OrcField), C.POINTER(OrcMgParams),
+            _dp, _dp, _dp, _dp, C.POINTER(C.c_uint), _dp]
+        L.orc_blocked_get_level.restype = C.c_long
+        L.orc_blocked_get_level.argtypes = [C.c_int, C.c_int, C.c_void_p]
         L.orc_level_count.restype = C.c_int
         L.orc_get_level.restype = C.c_long
         L.orc_get_level.argtypes = [C.c_int, C.c_int, C.c_void_p]
@@ -252,6 +259,50 @@ class Oracle:
         del bk, fk
         return dict(u=ou, v=ov, w=ow, p=p, iters=it.value, resid=rs.value,
                     ok=bool(ok))
+
+    def blocked_pressure_solve(self, res, spacing, origin, u, v, w,
+                               boundary_sdf, fluid_sdf, params: MgParams):
+        """GridSinglePhasePressureSolver3::solve + FdmMgpcgSolver3 (the
+        blocked solver); arguments and result as pressure_solve."""
+        g = OrcGrid()
+        g.res[:] = tuple(res)
+        g.spacing[:] = tuple(spacing)
+        g.origin[:] = tuple(origin)
+        data_origin = tuple(o + 0.5 * h for o, h in zip(origin, spacing))
+        bf, bk = field(boundary_sdf, spacing, data_origin)
+        ff, fk = field(fluid_sdf, spacing, data_origin)
+        u = np.ascontiguousarray(u, np.float64)
+        v = np.ascontiguousarray(v, np.float64)
+        w = np.ascontiguousarray(w, np.float64)
+        ou, ov, ow = u.copy(), v.copy(), w.copy()
+        nx, ny, nz = res
+        p = np.zeros((nz, ny, nx))
+        it = C.c_uint(0)
+        rs = C.c_double(0)
+        prm = params.c()
+        ok = self.lib.orc_blocked_pressure_solve(
+            C.byref(g), _ptr(u), _ptr(v), _ptr(w), C.byref(bf), C.byref(ff),
+            C.byref(prm), _ptr(ou), _ptr(ov), _ptr(ow), _ptr(p),
+            C.byref(it), C.byref(rs))
+        del bk, fk
+        return dict(u=ou, v=ov, w=ow, p=p, iters=it.value, resid=rs.value,
+                    ok=bool(ok))
+
+    def blocked_level(self, level: int, what: str, res0):
+        """State of the last blocked solve at `level`: "markers" (int8,
+        0 fluid / 1 air / 2 boundary), "A" (cells x 4 doubles) or "b"."""
+        nx, ny, nz = (r >> level for r in res0)
+        code = {"markers": 0, "A": 4, "b": 5}[what]
+        if what == "markers":
+            out = np.zeros((nz, ny, nx), np.int8)
+        elif what == "A":
+            out = np.zeros((nz, ny, nx, 4))
+        else:
+            out = np.zeros((nz, ny, nx))
+        n = self.lib.orc_blocked_get_level(level, code, out.ctypes.data)
+        if n < 0:
+            raise ValueError(f"no level {level}")
+        return out
 
     def level_count(self) -> int:
         return self.lib.orc_level_count()

@@ -213,6 +213,23 @@ void orc_apic_g2p(const orc_grid* g, long np, const double* pos, double* vel,
                   double* affine, const double* u, const double* v,
                   const double* w);
 
+/* GridSinglePhasePressureSolver3::solve (the blocked solver,
+ * src/jet/grid_single_phase_pressure_solver3.cpp:183-211) with an
+ * FdmMgpcgSolver3 installed. The boundary velocity is not an argument: the
+ * reference ignores it (:191). Output and return value as orc_pressure_solve. */
+int orc_blocked_pressure_solve(const orc_grid* g, const double* u,
+                               const double* v, const double* w,
+                               const orc_field* boundary_sdf,
+                               const orc_field* fluid_sdf,
+                               const orc_mg_params* p, double* out_u,
+                               double* out_v, double* out_w, double* out_p,
+                               unsigned int* iters, double* resid);
+
+/* A level of the last orc_blocked_pressure_solve: what 0 = cell markers
+ * (char: 0 fluid, 1 air, 2 boundary), 4 = matrix rows (4 doubles per cell),
+ * 5 = rhs b. Returns the number of cells copied, or -1. */
+long orc_blocked_get_level(int level, int what, void* dst);
+
 /* Port only: additionally stop MGPCG once the true relative residual
  * ||b - A x|| / ||b|| falls to `rel` (0 disables). Used to state the CPU
  * baseline at the GPU solver's accuracy. */

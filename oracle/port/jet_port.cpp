@@ -1681,3 +1681,246 @@ void orc_g2p_pic(const orc_grid* g, long np, const double* pos, double* vel,
 }
 
 }  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Blocked pressure solver (src/jet/grid_single_phase_pressure_solver3.cpp)
+// with an FdmMgpcgSolver3 installed: cells are marked fluid, air or boundary
+// at their centres, coarse levels take the majority marker of a 4x4x4 block,
+// and every level's matrix is the 7-point Laplacian on those markers.
+
+namespace {
+
+constexpr char kMFluid = 0, kMAir = 1, kMBoundary = 2;
+
+struct BlockedState {
+    std::vector<Size3> sizes;
+    std::vector<std::vector<char>> markers;
+    std::vector<Level> levels;
+};
+
+BlockedState g_blocked;
+
+// argmax3 (include/jet/detail/math_utils-inl.h:106-113).
+inline int argmax3i(int x, int y, int z) {
+    if (x > y) return (x > z) ? 0 : 2;
+    return (y > z) ? 1 : 2;
+}
+
+// buildMarkers (:245-322).
+void blockedMarkers(const orc_grid* g, const orc_field* bsdf,
+                    const orc_field* fsdf, unsigned maxLevels) {
+    BlockedState& S = g_blocked;
+    Size3 n{g->res[0], g->res[1], g->res[2]};
+    S.sizes = levelSizes(n, maxLevels);
+    S.markers.assign(S.sizes.size(), {});
+    for (size_t l = 0; l < S.sizes.size(); ++l)
+        S.markers[l].assign(S.sizes[l].count(), kMFluid);
+    Field B{bsdf}, F{fsdf};
+    std::vector<char>& m0 = S.markers[0];
+    const double hx = g->spacing[0], hy = g->spacing[1], hz = g->spacing[2];
+    const double ox = g->origin[0], oy = g->origin[1], oz = g->origin[2];
+#pragma omp parallel for schedule(static)
+    for (long k = 0; k < n.z; ++k)
+        for (long j = 0; j < n.y; ++j)
+            for (long i = 0; i < n.x; ++i) {
+                // Grid3::cellCenterPosition (src/jet/grid3.cpp:32-38).
+                const double x = ox + hx * ((double)i + 0.5);
+                const double y = oy + hy * ((double)j + 0.5);
+                const double z = oz + hz * ((double)k + 0.5);
+                char m;
+                if (inside(B.sample(x, y, z)))
+                    m = kMBoundary;
+                else if (inside(F.sample(x, y, z)))
+                    m = kMFluid;
+                else
+                    m = kMAir;
+                m0[lin(n, i, j, k)] = m;
+            }
+    for (size_t l = 1; l < S.sizes.size(); ++l) {
+        const Size3 f = S.sizes[l - 1], c = S.sizes[l];
+        const std::vector<char>& fine = S.markers[l - 1];
+        std::vector<char>& coarse = S.markers[l];
+#pragma omp parallel for schedule(static)
+        for (long k = 0; k < c.z; ++k)
+            for (long j = 0; j < c.y; ++j)
+                for (long i = 0; i < c.x; ++i) {
+                    const long kI[4] = {k > 0 ? 2 * k - 1 : 2 * k, 2 * k,
+                                        2 * k + 1,
+                                        k + 1 < c.z ? 2 * k + 2 : 2 * k + 1};
+                    const long jI[4] = {j > 0 ? 2 * j - 1 : 2 * j, 2 * j,
+                                        2 * j + 1,
+                                        j + 1 < c.y ? 2 * j + 2 : 2 * j + 1};
+                    const long iI[4] = {i > 0 ? 2 * i - 1 : 2 * i, 2 * i,
+                                        2 * i + 1,
+                                        i + 1 < c.x ? 2 * i + 2 : 2 * i + 1};
+                    int cnt[3] = {0, 0, 0};
+                    for (int z = 0; z < 4; ++z)
+                        for (int y = 0; y < 4; ++y)
+                            for (int x = 0; x < 4; ++x) {
+                                const char v = fine[lin(f, iI[x], jI[y], kI[z])];
+                                if (v == kMBoundary)
+                                    ++cnt[2];
+                                else if (v == kMFluid)
+                                    ++cnt[0];
+                                else
+                                    ++cnt[1];
+                            }
+                    coarse[lin(c, i, j, k)] =
+                        (char)argmax3i(cnt[0], cnt[1], cnt[2]);
+                }
+    }
+}
+
+// buildSingleSystem, FdmMatrix3 form (:26-76). `u` is NULL on coarse levels,
+// whose right-hand sides the multigrid overwrites by restriction
+// (include/jet/detail/mg-inl.h:28-30); b stays zero there.
+void blockedSystem(Level& L, const std::vector<char>& m, double hx, double hy,
+                   double hz, const double* u, const double* v,
+                   const double* w) {
+    const Size3 n = L.size;
+    L.A.assign(n.count(), Row{0, 0, 0, 0});
+    L.b.assign(n.count(), 0.0);
+    L.x.assign(n.count(), 0.0);
+    const double ihx = 1.0 / hx, ihy = 1.0 / hy, ihz = 1.0 / hz;
+    const double isx = ihx * ihx, isy = ihy * ihy, isz = ihz * ihz;
+    const Size3 us{n.x + 1, n.y, n.z}, vs{n.x, n.y + 1, n.z},
+        ws{n.x, n.y, n.z + 1};
+    const long sy = n.x, sz = n.x * n.y;
+#pragma omp parallel for schedule(static)
+    for (long k = 0; k < n.z; ++k)
+        for (long j = 0; j < n.y; ++j)
+            for (long i = 0; i < n.x; ++i) {
+                const long c = lin(n, i, j, k);
+                Row& r = L.A[c];
+                if (m[c] != kMFluid) {
+                    r.center = 1.0;
+                    continue;
+                }
+                if (u) {
+                    // FaceCenteredGrid3::divergenceAtCellCenter
+                    // (src/jet/face_centered_grid3.cpp:137-152).
+                    const double du = u[lin(us, i + 1, j, k)] - u[lin(us, i, j, k)];
+                    const double dv = v[lin(vs, i, j + 1, k)] - v[lin(vs, i, j, k)];
+                    const double dw = w[lin(ws, i, j, k + 1)] - w[lin(ws, i, j, k)];
+                    L.b[c] = du / hx + dv / hy + dw / hz;
+                }
+                if (i + 1 < n.x && m[c + 1] != kMBoundary) {
+                    r.center += isx;
+                    if (m[c + 1] == kMFluid) r.right -= isx;
+                }
+                if (i > 0 && m[c - 1] != kMBoundary) r.center += isx;
+                if (j + 1 < n.y && m[c + sy] != kMBoundary) {
+                    r.center += isy;
+                    if (m[c + sy] == kMFluid) r.up -= isy;
+                }
+                if (j > 0 && m[c - sy] != kMBoundary) r.center += isy;
+                if (k + 1 < n.z && m[c + sz] != kMBoundary) {
+                    r.center += isz;
+                    if (m[c + sz] == kMFluid) r.front -= isz;
+                }
+                if (k > 0 && m[c - sz] != kMBoundary) r.center += isz;
+            }
+}
+
+// applyPressureGradient (:378-405): only the +x/+y/+z faces of fluid cells
+// whose neighbour is not a boundary cell change; out_* start as copies of
+// the input.
+void blockedGradient(const orc_grid* g, const double* x, const double* u,
+                     const double* v, const double* w, double* ou,
+                     double* ov, double* ow) {
+    const std::vector<char>& m = g_blocked.markers[0];
+    const Size3 n{g->res[0], g->res[1], g->res[2]};
+    const Size3 us{n.x + 1, n.y, n.z}, vs{n.x, n.y + 1, n.z},
+        ws{n.x, n.y, n.z + 1};
+    const double ihx = 1.0 / g->spacing[0], ihy = 1.0 / g->spacing[1],
+                 ihz = 1.0 / g->spacing[2];
+    const long sy = n.x, sz = n.x * n.y;
+#pragma omp parallel for schedule(static)
+    for (long k = 0; k < n.z; ++k)
+        for (long j = 0; j < n.y; ++j)
+            for (long i = 0; i < n.x; ++i) {
+                const long c = lin(n, i, j, k);
+                if (m[c] != kMFluid) continue;
+                if (i + 1 < n.x && m[c + 1] != kMBoundary) {
+                    const long f = lin(us, i + 1, j, k);
+                    ou[f] = u[f] + ihx * (x[c + 1] - x[c]);
+                }
+                if (j + 1 < n.y && m[c + sy] != kMBoundary) {
+                    const long f = lin(vs, i, j + 1, k);
+                    ov[f] = v[f] + ihy * (x[c + sy] - x[c]);
+                }
+                if (k + 1 < n.z && m[c + sz] != kMBoundary) {
+                    const long f = lin(ws, i, j, k + 1);
+                    ow[f] = w[f] + ihz * (x[c + sz] - x[c]);
+                }
+            }
+}
+
+}  // namespace
+
+extern "C" {
+
+int orc_blocked_pressure_solve(const orc_grid* g, const double* u,
+                               const double* v, const double* w,
+                               const orc_field* boundary_sdf,
+                               const orc_field* fluid_sdf,
+                               const orc_mg_params* p, double* out_u,
+                               double* out_v, double* out_w, double* out_p,
+                               unsigned int* iters, double* resid) {
+    BlockedState& S = g_blocked;
+    blockedMarkers(g, boundary_sdf, fluid_sdf, p->max_levels);
+    const size_t nl = S.sizes.size();
+    S.levels.assign(nl, {});
+    // buildSystem (:341-376): coarse levels use the doubled spacing.
+    double hx = g->spacing[0], hy = g->spacing[1], hz = g->spacing[2];
+    for (size_t l = 0; l < nl; ++l) {
+        if (l > 0) {
+            hx *= 2.0;
+            hy *= 2.0;
+            hz *= 2.0;
+        }
+        S.levels[l].size = S.sizes[l];
+        blockedSystem(S.levels[l], S.markers[l], hx, hy, hz,
+                      l == 0 ? u : nullptr, l == 0 ? v : nullptr,
+                      l == 0 ? w : nullptr);
+    }
+    MgSolver solver{*p, &S.levels, {}, {}, {}};
+    unsigned it = 0;
+    double rs = 0;
+    const bool ok = solver.solve(&it, &rs);
+    if (iters) *iters = it;
+    if (resid) *resid = rs;
+    const Size3 n{g->res[0], g->res[1], g->res[2]};
+    const long nu = (n.x + 1) * n.y * n.z, nv = n.x * (n.y + 1) * n.z,
+               nw = n.x * n.y * (n.z + 1);
+    std::vector<double> cu(u, u + nu), cv(v, v + nv), cw(w, w + nw);
+    if (out_u != u) std::memcpy(out_u, u, nu * sizeof(double));
+    if (out_v != v) std::memcpy(out_v, v, nv * sizeof(double));
+    if (out_w != w) std::memcpy(out_w, w, nw * sizeof(double));
+    blockedGradient(g, S.levels[0].x.data(), cu.data(), cv.data(), cw.data(),
+                    out_u, out_v, out_w);
+    if (out_p)
+        std::memcpy(out_p, S.levels[0].x.data(), n.count() * sizeof(double));
+    return ok ? 1 : 0;
+}
+
+long orc_blocked_get_level(int level, int what, void* dst) {
+    BlockedState& S = g_blocked;
+    if (level < 0 || level >= (int)S.levels.size()) return -1;
+    const Level& L = S.levels[level];
+    switch (what) {
+        case 0:
+            std::memcpy(dst, S.markers[level].data(), S.markers[level].size());
+            return (long)S.markers[level].size();
+        case 4:
+            std::memcpy(dst, L.A.data(), L.A.size() * sizeof(Row));
+            return (long)L.A.size();
+        case 5:
+            std::memcpy(dst, L.b.data(), L.b.size() * sizeof(double));
+            return (long)L.b.size();
+        default:
+            return -1;
+    }
+}
+
+}  // extern "C"

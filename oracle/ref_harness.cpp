@@ -232,6 +232,65 @@ long orc_get_level(int level, int what, void* dst) {
     }
 }
 
+std::shared_ptr<GridSinglePhasePressureSolver3> g_blocked;
+
+int orc_blocked_pressure_solve(const orc_grid* g, const double* u,
+                               const double* v, const double* w,
+                               const orc_field* boundary_sdf,
+                               const orc_field* fluid_sdf,
+                               const orc_mg_params* p, double* out_u,
+                               double* out_v, double* out_w, double* out_p,
+                               unsigned int* iters, double* resid) {
+    Logging::mute();
+    Size3 res(g->res[0], g->res[1], g->res[2]);
+    Vector3D h(g->spacing[0], g->spacing[1], g->spacing[2]);
+    Vector3D o(g->origin[0], g->origin[1], g->origin[2]);
+    FaceCenteredGrid3 in(res, h, o);
+    fillGrid(&in, u, v, w);
+    FaceCenteredGrid3 out(in);
+    auto bsdf = makeField(boundary_sdf);
+    auto fsdf = makeField(fluid_sdf);
+    g_blocked = std::make_shared<GridSinglePhasePressureSolver3>();
+    auto mg = makeMgpcg(p);
+    g_blocked->setLinearSystemSolver(mg);
+    g_blocked->solve(in, 1.0, &out, *bsdf, ConstantVectorField3({0, 0, 0}),
+                     *fsdf, false);
+    readGrid(out, out_u, out_v, out_w);
+    if (out_p) copyOut(g_blocked->pressure(), out_p);
+    if (iters) *iters = mg->lastNumberOfIterations();
+    if (resid) *resid = mg->lastResidual();
+    bool ok = mg->lastResidual() <= mg->tolerance() ||
+              mg->lastNumberOfIterations() < mg->maxNumberOfIterations();
+    return ok ? 1 : 0;
+}
+
+long orc_blocked_get_level(int level, int what, void* dst) {
+    if (!g_blocked || level < 0 ||
+        level >= (int)g_blocked->_markers.size())
+        return -1;
+    switch (what) {
+        case 0: {
+            const auto& m = g_blocked->_markers[level];
+            long n = (long)(m.size().x * m.size().y * m.size().z);
+            std::memcpy(dst, m.data(), n);
+            return n;
+        }
+        case 4: {
+            const auto& A = g_blocked->_mgSystem.A.levels[level];
+            long n = (long)(A.size().x * A.size().y * A.size().z);
+            std::memcpy(dst, A.data(), n * sizeof(FdmMatrixRow3));
+            return n;
+        }
+        case 5: {
+            const auto& b = g_blocked->_mgSystem.b.levels[level];
+            long n = (long)(b.size().x * b.size().y * b.size().z);
+            std::memcpy(dst, b.data(), n * sizeof(double));
+            return n;
+        }
+        default: return -1;
+    }
+}
+
 int orc_mgpcg_system(const int res0[3], int levels, const double* A,
                      const double* b, const orc_mg_params* p, double* x0,
                      unsigned int* iters, double* resid) {

@@ -146,6 +146,59 @@ def noncubic(ref):
          spacing=np.array(h), params=params_array(p), **a)
 
 
+def blocked_case(ref, res, h, fields, params):
+    out = ref.blocked_pressure_solve(res, h, (0, 0, 0), fields["u"],
+                                     fields["v"], fields["w"],
+                                     fields["boundary_sdf"],
+                                     fields["fluid_sdf"], params)
+    arrays = dict(out_u=out["u"], out_v=out["v"], out_w=out["w"], p=out["p"],
+                  iters=np.array(out["iters"]), resid=np.array(out["resid"]))
+    levels = 0
+    while True:
+        try:
+            arrays[f"L{levels}_markers"] = ref.blocked_level(levels, "markers",
+                                                             res)
+        except ValueError:
+            break
+        arrays[f"L{levels}_A"] = ref.blocked_level(levels, "A", res)
+        levels += 1
+    arrays["L0_b"] = ref.blocked_level(0, "b", res)
+    arrays["levels"] = np.array(levels)
+    return arrays
+
+
+def blocked(ref):
+    """GridSinglePhasePressureSolver3 with MGPCG: a sphere-union scene on a
+    cubic power-of-two grid and a non-cubic grid with non-power-of-two
+    spacing (true divisions in the divergence)."""
+    n = 16
+    h = 1.0 / n
+    sc = scenes.sphere_union_scene(n, seed=4)
+    p = oracle.MgParams(200, 4, 5, 5, 20, 20, 1e-10, 1.5, True)
+    a = blocked_case(ref, (n, n, n), (h, h, h), sc, p)
+    save("blocked_sphere_union_16.npz", u=sc["u"], v=sc["v"], w=sc["w"],
+         fluid_sdf=sc["fluid_sdf"], boundary_sdf=sc["boundary_sdf"],
+         params=params_array(p), **a)
+    res = (12, 8, 16)
+    hh = (1.0 / 12, 0.8 / 8, 1.5 / 16)
+    nx, ny, nz = res
+    rng = np.random.default_rng(9)
+    cz, cy, cx = [(np.arange(m) + 0.5) * d for m, d in zip((nz, ny, nx),
+                                                           (hh[2], hh[1], hh[0]))]
+    Z, Y, X = np.meshgrid(cz, cy, cx, indexing="ij")
+    fluid = np.minimum(Y - 0.5, np.sqrt((X - .6) ** 2 + (Y - .6) ** 2 +
+                                        (Z - .7) ** 2) - 0.25)
+    solid = np.sqrt((X - 0.4) ** 2 + (Y - 0.3) ** 2 + (Z - 0.8) ** 2) - 0.2
+    u = rng.uniform(-1, 1, (nz, ny, nx + 1))
+    v = rng.uniform(-1, 1, (nz, ny + 1, nx))
+    w = rng.uniform(-1, 1, (nz + 1, ny, nx))
+    p = oracle.MgParams(200, 3, 5, 5, 20, 20, 1e-10, 1.5, True)
+    f = dict(u=u, v=v, w=w, boundary_sdf=solid, fluid_sdf=fluid)
+    a = blocked_case(ref, res, hh, f, p)
+    save("blocked_noncubic_12x8x16.npz", u=u, v=v, w=w, fluid_sdf=fluid,
+         boundary_sdf=solid, spacing=np.array(hh), params=params_array(p), **a)
+
+
 def mgpcg_poisson(ref):
     A, b = poisson_system()
     p = oracle.MgParams(50, 4, 5, 5, 10, 10, 1e-4, 1.5, False)
@@ -337,6 +390,7 @@ def main():
     sphere_union(ref)
     noncubic(ref)
     mgpcg_poisson(ref)
+    blocked(ref)
     transfers(ref)
     boundary(ref)
     particles(ref)

@@ -333,3 +333,103 @@ def test_port_apic_matches_reference_random(port, reference):
              rng.uniform(-1, 1, (nz + 1, ny, nx))]
     a, b = (o.apic_g2p(res, h, org, pos, grids) for o in (reference, port))
     assert np.array_equal(a[0], b[0]) and np.array_equal(a[1], b[1])
+
+
+# ---------------------------------------------------------------------------
+# Blocked pressure solver (GridSinglePhasePressureSolver3 + FdmMgpcgSolver3)
+
+
+def check_blocked_case(o, g, res, h):
+    out = o.blocked_pressure_solve(res, h, (0, 0, 0), g["u"], g["v"], g["w"],
+                                   g["boundary_sdf"], g["fluid_sdf"],
+                                   params_from(g["params"]))
+    assert out["iters"] == int(g["iters"])
+    for k in ("u", "v", "w"):
+        assert np.array_equal(out[k], g["out_" + k]), k
+    assert np.array_equal(out["p"], g["p"])
+    for l in range(int(g["levels"])):
+        assert np.array_equal(o.blocked_level(l, "markers", res),
+                              g[f"L{l}_markers"]), l
+        assert np.array_equal(o.blocked_level(l, "A", res), g[f"L{l}_A"]), l
+    assert np.array_equal(o.blocked_level(0, "b", res), g["L0_b"])
+
+
+def test_blocked_sphere_union_bit_exact(port):
+    g = golden("blocked_sphere_union_16.npz")
+    check_blocked_case(port, g, (16, 16, 16), (1.0 / 16,) * 3)
+
+
+def test_blocked_noncubic_bit_exact(port):
+    g = golden("blocked_noncubic_12x8x16.npz")
+    check_blocked_case(port, g, (12, 8, 16), tuple(g["spacing"]))
+
+
+def blocked_kat_case(kind):
+    """The scenes of grid_single_phase_pressure_solver3_tests.cpp: a 3^3
+    box with v = 1 on the interior y faces, alone (SolveSinglePhase, :14-67),
+    with a wall in the right-most column (…WithBoundary, :69-130), with air
+    in the top row (SolveFreeSurface, :132-189) or both
+    (SolveFreeSurfaceWithBoundary, :250-311)."""
+    n = 3
+    u = np.zeros((n, n, n + 1))
+    v = np.zeros((n, n + 1, n))
+    w = np.zeros((n + 1, n, n))
+    v[:, 1:3, :] = 1.0
+    c = np.arange(n) + 0.5
+    bs, fs = KMAX, -KMAX
+    if "boundary" in kind:
+        bs = np.broadcast_to((2.0 - c)[None, None, :], (n, n, n)).copy()
+    if "free_surface" in kind:
+        fs = np.broadcast_to((c - 2.0)[None, :, None], (n, n, n)).copy()
+    return u, v, w, bs, fs
+
+
+def check_blocked_kat(kind, out_u, out_v, out_w, p):
+    """The reference tests' expectations, with their 1e-6 tolerance."""
+    assert np.abs(out_u).max() < 1e-6
+    assert np.abs(out_w).max() < 1e-6
+    exp_v = np.zeros_like(out_v)
+    cols = slice(0, 3)
+    if "boundary" in kind:
+        exp_v[:, 1:3, 2] = 1.0  # the wall column keeps its velocity
+        cols = slice(0, 2)
+    assert np.abs(out_v - exp_v).max() < 1e-6
+    if "free_surface" in kind:
+        for j in range(2):
+            assert np.abs(p[:, j, cols] - (2.0 - j)).max() < 1e-6
+    else:
+        assert np.abs(p[:, 1:, cols] - p[:, :-1, cols] + 1.0).max() < 1e-6
+
+
+BLOCKED_KATS = ["plain", "boundary", "free_surface", "free_surface_boundary"]
+
+
+@pytest.mark.parametrize("kind", BLOCKED_KATS)
+def test_blocked_known_answers(port, kind):
+    u, v, w, bs, fs = blocked_kat_case(kind)
+    prm = oracle.MgParams(100, 5, 5, 5, 20, 20, 1e-12, 1.5, True)
+    out = port.blocked_pressure_solve((3, 3, 3), (1.0,) * 3, (0, 0, 0), u, v,
+                                      w, bs, fs, prm)
+    check_blocked_kat(kind, out["u"], out["v"], out["w"], out["p"])
+
+
+def test_port_blocked_matches_reference_random(port, reference):
+    """Fresh random scenes through both libraries (needs the reference)."""
+    rng = np.random.default_rng(23)
+    for n, levels in ((20, 3), (24, 4)):
+        h = 1.0 / n
+        X, Y, Z = scenes.cell_centres(n)
+        fl = np.minimum(Y - rng.uniform(0.3, 0.7),
+                        np.sqrt((X - .5) ** 2 + (Y - .5) ** 2 + (Z - .5) ** 2) - .2)
+        bs = np.sqrt((X - .3) ** 2 + (Y - .2) ** 2 + (Z - .6) ** 2) - .18
+        u = rng.uniform(-1, 1, (n, n, n + 1))
+        v = rng.uniform(-1, 1, (n, n + 1, n))
+        w = rng.uniform(-1, 1, (n + 1, n, n))
+        p = oracle.MgParams(100, levels, 3, 3, 10, 10, 1e-9, 1.5, True)
+        a = port.blocked_pressure_solve((n, n, n), (h, h, h), (0, 0, 0), u, v,
+                                        w, bs, fl, p)
+        b = reference.blocked_pressure_solve((n, n, n), (h, h, h), (0, 0, 0),
+                                             u, v, w, bs, fl, p)
+        for k in ("u", "v", "w", "p"):
+            assert np.array_equal(a[k], b[k]), k
+        assert a["iters"] == b["iters"]
