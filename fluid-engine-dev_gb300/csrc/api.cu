@@ -898,24 +898,48 @@ jetgpu_status jetgpu_g2p_pic(jetgpu_ctx* c, const jetgpu_grid* grid, long np,
     return JETGPU_OK;
 }
 
-jetgpu_status jetgpu_constrain_velocity_device(
+// The fractional or blocked constraint on device arrays.
+static jetgpu_status constrain_any(Ctx* c, const GridDesc& g, double* u,
+                                   double* v, double* w, const FieldDesc& f,
+                                   const jetgpu_collider* col, int closed,
+                                   unsigned depth, bool blocked) {
+    return blocked
+               ? constrain_velocity_blocked(c, g, u, v, w, f, col, closed, depth)
+               : constrain_velocity(c, g, u, v, w, f, col, closed, depth);
+}
+
+static jetgpu_status constrain_device(
     jetgpu_ctx* c, const jetgpu_grid* grid, double* u, double* v, double* w,
     const jetgpu_scalar_field* sdf, const jetgpu_collider* col, int closed,
-    unsigned int depth) {
+    unsigned int depth, bool blocked) {
     if (!c) return JETGPU_BAD_INPUT;
     jetgpu_status s;
     if ((s = check_grid(c, grid)) != JETGPU_OK) return s;
     if ((s = check_field(c, sdf, "collider_sdf")) != JETGPU_OK) return s;
     if (!u || !v || !w) return fail(c, JETGPU_BAD_INPUT, "null velocity arrays");
     JG_CUDA(c, cudaSetDevice(c->device));
-    return constrain_velocity(c, to_desc(grid), u, v, w, to_desc(sdf, sdf->data),
-                              col, closed, depth);
+    return constrain_any(c, to_desc(grid), u, v, w, to_desc(sdf, sdf->data),
+                         col, closed, depth, blocked);
 }
 
-jetgpu_status jetgpu_constrain_velocity(
+jetgpu_status jetgpu_constrain_velocity_device(
     jetgpu_ctx* c, const jetgpu_grid* grid, double* u, double* v, double* w,
     const jetgpu_scalar_field* sdf, const jetgpu_collider* col, int closed,
     unsigned int depth) {
+    return constrain_device(c, grid, u, v, w, sdf, col, closed, depth, false);
+}
+
+jetgpu_status jetgpu_constrain_velocity_blocked_device(
+    jetgpu_ctx* c, const jetgpu_grid* grid, double* u, double* v, double* w,
+    const jetgpu_scalar_field* sdf, const jetgpu_collider* col, int closed,
+    unsigned int depth) {
+    return constrain_device(c, grid, u, v, w, sdf, col, closed, depth, true);
+}
+
+static jetgpu_status constrain_host(
+    jetgpu_ctx* c, const jetgpu_grid* grid, double* u, double* v, double* w,
+    const jetgpu_scalar_field* sdf, const jetgpu_collider* col, int closed,
+    unsigned int depth, bool blocked) {
     if (!c) return JETGPU_BAD_INPUT;
     jetgpu_status s;
     if ((s = check_grid(c, grid)) != JETGPU_OK) return s;
@@ -941,8 +965,9 @@ jetgpu_status jetgpu_constrain_velocity(
     if (ns)
         JG_CUDA(c, cudaMemcpyAsync(ds, sdf->data, ns * 8,
                                    cudaMemcpyHostToDevice, st));
-    s = constrain_velocity(c, to_desc(grid), dg, dg + n[0], dg + n[0] + n[1],
-                           to_desc(sdf, ns ? ds : nullptr), col, closed, depth);
+    s = constrain_any(c, to_desc(grid), dg, dg + n[0], dg + n[0] + n[1],
+                      to_desc(sdf, ns ? ds : nullptr), col, closed, depth,
+                      blocked);
     if (s != JETGPU_OK) return s;
     off = 0;
     for (int a = 0; a < 3; ++a) {
@@ -952,6 +977,20 @@ jetgpu_status jetgpu_constrain_velocity(
     }
     JG_CUDA(c, cudaStreamSynchronize(st));
     return JETGPU_OK;
+}
+
+jetgpu_status jetgpu_constrain_velocity(
+    jetgpu_ctx* c, const jetgpu_grid* grid, double* u, double* v, double* w,
+    const jetgpu_scalar_field* sdf, const jetgpu_collider* col, int closed,
+    unsigned int depth) {
+    return constrain_host(c, grid, u, v, w, sdf, col, closed, depth, false);
+}
+
+jetgpu_status jetgpu_constrain_velocity_blocked(
+    jetgpu_ctx* c, const jetgpu_grid* grid, double* u, double* v, double* w,
+    const jetgpu_scalar_field* sdf, const jetgpu_collider* col, int closed,
+    unsigned int depth) {
+    return constrain_host(c, grid, u, v, w, sdf, col, closed, depth, true);
 }
 
 jetgpu_status jetgpu_apic_p2g_device(jetgpu_ctx* c, const jetgpu_grid* grid,

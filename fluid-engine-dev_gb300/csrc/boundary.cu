@@ -511,6 +511,77 @@ jetgpu_status bc_apply(Ctx* c, const GridDesc& g, double* u, double* v,
     return JETGPU_OK;
 }
 
+namespace {
+
+// GridBlockedBoundaryConditionSolver3's no-flux pass
+// (src/jet/grid_blocked_boundary_condition_solver3.cpp:29-66): a cell is a
+// collider cell when the collider SDF sample at the cell is negative
+// (onColliderUpdated, :79-90); each face between a collider cell and a
+// non-collider neighbour takes the collider velocity's normal component at
+// the face position. The collider side of such a face is unique, so the
+// cell's thread is the face's only writer.
+__global__ void k_bc_blocked(FaceSet fs, H3 h, Dims n, FieldDesc sdf,
+                             ColliderDesc col, double* __restrict__ u,
+                             double* __restrict__ v, double* __restrict__ w) {
+    const long N = n.count();
+    const long sy = n.x, sz = (long)n.x * n.y;
+    auto solid = [&](long c) {
+        return (sdf.kind == 1 ? sdf.data[c] : sdf.value) < 0.0;
+    };
+    for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < N;
+         c += (long)gridDim.x * blockDim.x) {
+        if (!solid(c)) continue;
+        int i, j, k;
+        cell_ijk(c, n, i, j, k);
+        double p[3], cv[3];
+        auto set = [&](int a, int fi, int fj, int fk, double* vel) {
+            face_pos(fs, a, h.v, fi, fj, fk, p);
+            collider_vel(col, p, cv);
+            vel[lin(fi, fj, fk, fs.s[a].x, fs.s[a].y)] = cv[a];
+        };
+        if (i > 0 && !solid(c - 1)) set(0, i, j, k, u);
+        if (i < n.x - 1 && !solid(c + 1)) set(0, i + 1, j, k, u);
+        if (j > 0 && !solid(c - sy)) set(1, i, j, k, v);
+        if (j < n.y - 1 && !solid(c + sy)) set(1, i, j + 1, k, v);
+        if (k > 0 && !solid(c - sz)) set(2, i, j, k, w);
+        if (k < n.z - 1 && !solid(c + sz)) set(2, i, j, k + 1, w);
+    }
+}
+
+}  // namespace
+
+jetgpu_status constrain_velocity_blocked(Ctx* c, const GridDesc& g, double* u,
+                                         double* v, double* w,
+                                         const FieldDesc& sdf,
+                                         const jetgpu_collider* col,
+                                         int closed, unsigned depth) {
+    if (sdf.kind == 1 && (sdf.res[0] != g.res[0] || sdf.res[1] != g.res[1] ||
+                          sdf.res[2] != g.res[2]))
+        return fail(c, JETGPU_BAD_INPUT,
+                    "the blocked constraint needs the collider SDF on the "
+                    "velocity grid's cells");
+    if (jetgpu_status s = constrain_velocity(c, g, u, v, w, sdf, col, closed,
+                                             depth))
+        return s;
+    ColliderDesc cd{};
+    if (col) {
+        cd.present = 1;
+        for (int d = 0; d < 3; ++d) {
+            cd.lin[d] = col->linear_velocity[d];
+            cd.ang[d] = col->angular_velocity[d];
+            cd.centre[d] = col->centre[d];
+        }
+        cd.friction = col->friction;
+    }
+    const Dims n{g.res[0], g.res[1], g.res[2]};
+    Prof pr(c, K_BOUNDARY, 8.0 * (double)n.count());
+    k_bc_blocked<<<blocks_for(n.count()), kThreads, 0, c->stream>>>(
+        face_set(g), H3{{g.spacing[0], g.spacing[1], g.spacing[2]}}, n, sdf,
+        cd, u, v, w);
+    JG_CUDA(c, cudaGetLastError());
+    return JETGPU_OK;
+}
+
 jetgpu_status constrain_velocity(Ctx* c, const GridDesc& g, double* u,
                                  double* v, double* w, const FieldDesc& sdf,
                                  const jetgpu_collider* col, int closed,

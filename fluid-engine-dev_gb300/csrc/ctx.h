@@ -315,6 +315,13 @@ jetgpu_status constrain_velocity(Ctx* c, const GridDesc& g, double* u,
                                  double* v, double* w, const FieldDesc& sdf,
                                  const jetgpu_collider* col, int closed,
                                  unsigned depth);
+// GridBlockedBoundaryConditionSolver3::constrainVelocity: constrain_velocity
+// plus the no-flux pass on the faces of collider cells (boundary.cu).
+jetgpu_status constrain_velocity_blocked(Ctx* c, const GridDesc& g, double* u,
+                                         double* v, double* w,
+                                         const FieldDesc& sdf,
+                                         const jetgpu_collider* col,
+                                         int closed, unsigned depth);
 // The two halves of constrain_velocity: bc_classify evaluates the collider
 // SDF at every face (cached in ctx->bc_cls), bc_apply does the rest with
 // those classes; a caller whose collider does not move between calls

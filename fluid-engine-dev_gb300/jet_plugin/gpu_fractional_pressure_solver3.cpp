@@ -2,6 +2,7 @@
 // C ABI of libjetgpu. See gpu_fractional_pressure_solver3.h.
 #include "gpu_fractional_pressure_solver3.h"
 #include "gpu_fractional_boundary_condition_solver3.h"
+#include "jet_marshal.h"
 
 #include <jet/cell_centered_scalar_grid3.h>
 #include <jet/constant_scalar_field3.h>
@@ -36,45 +37,6 @@ GpuFractionalSinglePhasePressureSolver3::suggestedBoundaryConditionSolver()
     return std::make_shared<GpuFractionalBoundaryConditionSolver3>(&_config);
 }
 
-jetgpu_scalar_field GpuFractionalSinglePhasePressureSolver3::describe(
-    const ScalarField3& field, const FaceCenteredGrid3& grid,
-    std::vector<double>* raster) const {
-    jetgpu_scalar_field f;
-    std::memset(&f, 0, sizeof(f));
-    if (auto c = dynamic_cast<const ConstantScalarField3*>(&field)) {
-        f.kind = 0;
-        f.value = c->sample(Vector3D());
-        return f;
-    }
-    const CellCenteredScalarGrid3* g =
-        dynamic_cast<const CellCenteredScalarGrid3*>(&field);
-    std::shared_ptr<CellCenteredScalarGrid3> owned;
-    if (!g) {
-        // Any other field: rasterise at the velocity grid's cell centres.
-        owned = std::make_shared<CellCenteredScalarGrid3>(
-            grid.resolution(), grid.gridSpacing(), grid.origin());
-        owned->fill([&](const Vector3D& x) { return field.sample(x); });
-        g = owned.get();
-    }
-    const Size3 r = g->resolution();
-    const size_t n = r.x * r.y * r.z;
-    auto acc = g->constDataAccessor();
-    raster->assign(acc.data(), acc.data() + n);
-    f.kind = 1;
-    f.data = raster->data();
-    f.res[0] = (int)r.x;
-    f.res[1] = (int)r.y;
-    f.res[2] = (int)r.z;
-    const Vector3D o = g->dataOrigin(), h = g->gridSpacing();
-    f.origin[0] = o.x;
-    f.origin[1] = o.y;
-    f.origin[2] = o.z;
-    f.spacing[0] = h.x;
-    f.spacing[1] = h.y;
-    f.spacing[2] = h.z;
-    return f;
-}
-
 void GpuFractionalSinglePhasePressureSolver3::solve(
     const FaceCenteredGrid3& input, double timeIntervalInSeconds,
     FaceCenteredGrid3* output, const ScalarField3& boundarySdf,
@@ -90,19 +52,11 @@ void GpuFractionalSinglePhasePressureSolver3::solve(
         }
     }
     const Size3 res = input.resolution();
-    const Vector3D h = input.gridSpacing(), o = input.origin();
-    jetgpu_grid g;
-    g.res[0] = (int)res.x;
-    g.res[1] = (int)res.y;
-    g.res[2] = (int)res.z;
-    g.spacing[0] = h.x;
-    g.spacing[1] = h.y;
-    g.spacing[2] = h.z;
-    g.origin[0] = o.x;
-    g.origin[1] = o.y;
-    g.origin[2] = o.z;
-    const jetgpu_scalar_field bsdf = describe(boundarySdf, input, &_boundaryRaster);
-    const jetgpu_scalar_field fsdf = describe(fluidSdf, input, &_fluidRaster);
+    const jetgpu_grid g = grid_of(input);
+    const jetgpu_scalar_field bsdf =
+        describe_field(boundarySdf, input, &_boundaryRaster);
+    const jetgpu_scalar_field fsdf =
+        describe_field(fluidSdf, input, &_fluidRaster);
 
     // Collider velocity: only the normal component at each face is used
     // (grid_fractional_single_phase_pressure_solver3.cpp:241-255).

@@ -76,10 +76,6 @@ class GpuFractionalSinglePhasePressureSolver3 : public jet::GridPressureSolver3 
     jetgpu_status _status = JETGPU_OK;
     std::vector<double> _fluidRaster, _boundaryRaster;
     std::vector<double> _solidU, _solidV, _solidW;
-
-    jetgpu_scalar_field describe(const jet::ScalarField3& field,
-                                 const jet::FaceCenteredGrid3& grid,
-                                 std::vector<double>* raster) const;
 };
 
 }  // namespace jetgpu_jet

@@ -110,6 +110,8 @@ EXPORTS = (
     "jetgpu_conv3d_wgrad", "jetgpu_net_param_count", "jetgpu_load_unet",
     "jetgpu_harvest", "jetgpu_net_features", "jetgpu_net_apply",
     "jetgpu_constrain_velocity_device", "jetgpu_constrain_velocity",
+    "jetgpu_constrain_velocity_blocked_device",
+    "jetgpu_constrain_velocity_blocked",
     "jetgpu_extrapolate_to_region_device", "jetgpu_move_particles_device",
     "jetgpu_move_particles", "jetgpu_build_particle_sdf_device",
     "jetgpu_build_particle_sdf", "jetgpu_flip_params_default",
@@ -226,6 +228,10 @@ def library() -> C.CDLL:
     L.jetgpu_constrain_velocity.restype = C.c_int
     L.jetgpu_constrain_velocity_device.argtypes = bc_args
     L.jetgpu_constrain_velocity_device.restype = C.c_int
+    L.jetgpu_constrain_velocity_blocked.argtypes = bc_args
+    L.jetgpu_constrain_velocity_blocked.restype = C.c_int
+    L.jetgpu_constrain_velocity_blocked_device.argtypes = bc_args
+    L.jetgpu_constrain_velocity_blocked_device.restype = C.c_int
     L.jetgpu_extrapolate_to_region_device.argtypes = [
         vp, C.POINTER(C.c_int), vp, vp, C.c_uint]
     L.jetgpu_extrapolate_to_region_device.restype = C.c_int
@@ -1052,6 +1058,8 @@ class GridFractionalBoundaryConditionSolver3:
     reference bit for bit. The GPU context is borrowed from ``owner`` (an
     FdmMgpcgSolver3), or a private one is created."""
 
+    _entry = "jetgpu_constrain_velocity"
+
     def __init__(self, owner: "FdmMgpcgSolver3 | None" = None):
         self._owner = owner if owner is not None else FdmMgpcgSolver3()
         self._sdf = ConstantScalarField3(kMaxD)
@@ -1082,7 +1090,7 @@ class GridFractionalBoundaryConditionSolver3:
         f = _field(self._sdf, keep)
         g = velocity.c_grid()
         col = C.byref(self._collider) if self._collider is not None else None
-        st = library().jetgpu_constrain_velocity(
+        st = getattr(library(), self._entry)(
             self._owner.context(), C.byref(g), _p(velocity.u), _p(velocity.v),
             _p(velocity.w), C.byref(f), col, self._closed,
             int(extrapolationDepth))
@@ -1090,13 +1098,37 @@ class GridFractionalBoundaryConditionSolver3:
         return velocity
 
 
+class GridBlockedBoundaryConditionSolver3(GridFractionalBoundaryConditionSolver3):
+    """Mirror of GridBlockedBoundaryConditionSolver3
+    (src/jet/grid_blocked_boundary_condition_solver3.cpp), the solver the
+    blocked pressure solver suggests: the fractional constraint, then the
+    faces between collider cells (colliderSdf() < 0 at the cell) and the
+    other cells take the collider velocity. Bit-identical to the reference."""
+
+    _entry = "jetgpu_constrain_velocity_blocked"
+
+    def marker(self, resolution) -> np.ndarray:
+        """The reference's cell markers (:69-71): 0 collider, 1 fluid."""
+        nx, ny, nz = resolution
+        sdf = self._sdf
+        if isinstance(sdf, CellCenteredScalarGrid3):
+            return np.where(np.asarray(sdf.data) < 0, 0, 1).astype(np.int8)
+        value = float(sdf.value)
+        return np.full((nz, ny, nx), 0 if value < 0 else 1, np.int8)
+
+
 def constrain_velocity_device(solver: "FdmMgpcgSolver3", grid: Grid, u, v, w,
                               collider_sdf: ScalarField,
                               collider: Collider = None,
-                              closed: int = kDirectionAll, depth: int = 5):
-    """jetgpu_constrain_velocity_device on device tensors (in place)."""
+                              closed: int = kDirectionAll, depth: int = 5,
+                              blocked: bool = False):
+    """jetgpu_constrain_velocity_device (or, with ``blocked``, the blocked
+    solver's jetgpu_constrain_velocity_blocked_device) on device tensors (in
+    place)."""
     col = C.byref(collider) if collider is not None else None
-    st = library().jetgpu_constrain_velocity_device(
+    fn = (library().jetgpu_constrain_velocity_blocked_device if blocked
+          else library().jetgpu_constrain_velocity_device)
+    st = fn(
         solver.context(), C.byref(grid), _p(u), _p(v), _p(w),
         C.byref(collider_sdf), col, int(closed), int(depth))
     solver.check(st)

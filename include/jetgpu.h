@@ -313,6 +313,27 @@ jetgpu_status jetgpu_constrain_velocity(
     const jetgpu_collider* collider, int closed_domain_flags,
     unsigned int extrapolation_depth);
 
+/* GridBlockedBoundaryConditionSolver3::constrainVelocity
+ * (src/jet/grid_blocked_boundary_condition_solver3.cpp:23-67), the
+ * boundary-condition solver GridSinglePhasePressureSolver3 suggests: the
+ * fractional constraint above, then every face between a collider cell
+ * (collider_sdf < 0 at the cell, :79-90) and a non-collider cell takes the
+ * collider velocity's normal component at the face position. collider_sdf,
+ * when a grid, must have the velocity grid's resolution. DEVICE pointers;
+ * queued on the context's stream. Bit-identical to the reference. */
+jetgpu_status jetgpu_constrain_velocity_blocked_device(
+    struct jetgpu_ctx* ctx, const jetgpu_grid* grid, double* u, double* v,
+    double* w, const jetgpu_scalar_field* collider_sdf,
+    const jetgpu_collider* collider, int closed_domain_flags,
+    unsigned int extrapolation_depth);
+
+/* Host-pointer form of jetgpu_constrain_velocity_blocked_device. */
+jetgpu_status jetgpu_constrain_velocity_blocked(
+    struct jetgpu_ctx* ctx, const jetgpu_grid* grid, double* u, double* v,
+    double* w, const jetgpu_scalar_field* collider_sdf,
+    const jetgpu_collider* collider, int closed_domain_flags,
+    unsigned int extrapolation_depth);
+
 /* extrapolateToRegion (include/jet/detail/array_utils-inl.h:172-244), as
  * PicSolver3::extrapolateVelocityToAir (src/jet/pic_solver3.cpp:284-294)
  * applies it to each face array with the P2G markers: `iterations` passes

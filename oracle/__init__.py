@@ -195,6 +195,8 @@ class Oracle:
         L.orc_constrain_velocity.argtypes = [
             C.POINTER(OrcGrid), _dp, _dp, _dp, C.POINTER(OrcField),
             C.POINTER(OrcCollider), C.c_int, C.c_uint]
+        L.orc_constrain_velocity_blocked.argtypes = \
+            L.orc_constrain_velocity.argtypes
         L.orc_extrapolate.argtypes = [C.POINTER(C.c_int), _dp, _cp, C.c_uint]
         L.orc_move_particles.argtypes = [
             C.POINTER(OrcGrid), C.c_long, _dp, _dp, _dp, _dp, _dp, C.c_double,
@@ -429,16 +431,19 @@ class Oracle:
         return g
 
     def constrain_velocity(self, res, spacing, origin, u, v, w, collider_sdf,
-                           collider=None, closed=63, depth=5):
-        """GridFractionalBoundaryConditionSolver3::constrainVelocity on copies
-        of u/v/w. collider_sdf: constant or cell-centred grid (nz,ny,nx).
+                           collider=None, closed=63, depth=5, blocked=False):
+        """GridFractionalBoundaryConditionSolver3::constrainVelocity (or, with
+        `blocked`, GridBlockedBoundaryConditionSolver3's) on copies of u/v/w.
+        collider_sdf: constant or cell-centred grid (nz,ny,nx).
         collider: dict(lin, ang, centre, friction) or None."""
         g = self._grid(res, spacing, origin)
         data_origin = tuple(o + 0.5 * h for o, h in zip(origin, spacing))
         f, keep = field(collider_sdf, spacing, data_origin)
         out = [np.ascontiguousarray(a, np.float64).copy() for a in (u, v, w)]
         col = self._collider(collider) if collider is not None else None
-        self.lib.orc_constrain_velocity(
+        fn = (self.lib.orc_constrain_velocity_blocked if blocked
+              else self.lib.orc_constrain_velocity)
+        fn(
             C.byref(g), *[_ptr(a) for a in out], C.byref(f),
             C.byref(col) if col is not None else None, int(closed), int(depth))
         del keep

@@ -213,6 +213,16 @@ void orc_apic_g2p(const orc_grid* g, long np, const double* pos, double* vel,
                   double* affine, const double* u, const double* v,
                   const double* w);
 
+/* GridBlockedBoundaryConditionSolver3::constrainVelocity
+ * (src/jet/grid_blocked_boundary_condition_solver3.cpp:23-67): as
+ * orc_constrain_velocity, then the faces between a collider cell (sdf < 0
+ * at the cell) and a non-collider cell take the collider velocity. With cells
+ * inside the collider, col must be given (the reference dereferences it). */
+void orc_constrain_velocity_blocked(const orc_grid* g, double* u, double* v,
+                                    double* w, const orc_field* sdf,
+                                    const orc_collider* col, int closed,
+                                    unsigned int depth);
+
 /* GridSinglePhasePressureSolver3::solve (the blocked solver,
  * src/jet/grid_single_phase_pressure_solver3.cpp:183-211) with an
  * FdmMgpcgSolver3 installed. The boundary velocity is not an argument: the

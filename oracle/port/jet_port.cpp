@@ -1924,3 +1924,80 @@ long orc_blocked_get_level(int level, int what, void* dst) {
 }
 
 }  // extern "C"
+
+extern "C" {
+
+// GridBlockedBoundaryConditionSolver3::constrainVelocity
+// (src/jet/grid_blocked_boundary_condition_solver3.cpp:23-67): the
+// fractional constraint, then every face between a collider cell (collider
+// SDF sample < 0 at the cell, :79-90) and a non-collider neighbour takes the
+// collider velocity's normal component at the face position. Each such face
+// has one collider side, so the pass is order-independent.
+void orc_constrain_velocity_blocked(const orc_grid* g, double* u, double* v,
+                                    double* w, const orc_field* sdf,
+                                    const orc_collider* col, int closed,
+                                    unsigned int depth) {
+    orc_constrain_velocity(g, u, v, w, sdf, col, closed, depth);
+    const Size3 n{g->res[0], g->res[1], g->res[2]};
+    const Size3 us{n.x + 1, n.y, n.z}, vs{n.x, n.y + 1, n.z},
+        ws{n.x, n.y, n.z + 1};
+    const double* h = g->spacing;
+    FaceGeom fg[3];
+    faceGeoms(g, fg);
+    auto solid = [&](long i, long j, long k) {
+        const double phi = sdf->kind == 1 ? sdf->data[lin(n, i, j, k)]
+                                          : sdf->value;
+        return inside(phi);
+    };
+    // RigidBodyCollider3::velocityAt (rigid_body_collider3.cpp:25-28).
+    auto colVel = [&](const double p[3], int a) {
+        if (col == nullptr) return 0.0;
+        const double* an = col->ang;
+        const double r[3] = {p[0] - col->centre[0], p[1] - col->centre[1],
+                             p[2] - col->centre[2]};
+        const double cr[3] = {an[1] * r[2] - r[1] * an[2],
+                              an[2] * r[0] - r[2] * an[0],
+                              an[0] * r[1] - r[0] * an[1]};
+        return col->lin[a] + cr[a];
+    };
+    // uPosition/vPosition/wPosition (src/jet/face_centered_grid3.cpp:
+    // 216-238): the face array's data origin + spacing * (i, j, k).
+    auto pos = [&](int a, long i, long j, long k, double p[3]) {
+        p[0] = fg[a].o[0] + h[0] * (double)i;
+        p[1] = fg[a].o[1] + h[1] * (double)j;
+        p[2] = fg[a].o[2] + h[2] * (double)k;
+    };
+#pragma omp parallel for schedule(static)
+    for (long k = 0; k < n.z; ++k)
+        for (long j = 0; j < n.y; ++j)
+            for (long i = 0; i < n.x; ++i) {
+                if (!solid(i, j, k)) continue;
+                double p[3];
+                if (i > 0 && !solid(i - 1, j, k)) {
+                    pos(0, i, j, k, p);
+                    u[lin(us, i, j, k)] = colVel(p, 0);
+                }
+                if (i < n.x - 1 && !solid(i + 1, j, k)) {
+                    pos(0, i + 1, j, k, p);
+                    u[lin(us, i + 1, j, k)] = colVel(p, 0);
+                }
+                if (j > 0 && !solid(i, j - 1, k)) {
+                    pos(1, i, j, k, p);
+                    v[lin(vs, i, j, k)] = colVel(p, 1);
+                }
+                if (j < n.y - 1 && !solid(i, j + 1, k)) {
+                    pos(1, i, j + 1, k, p);
+                    v[lin(vs, i, j + 1, k)] = colVel(p, 1);
+                }
+                if (k > 0 && !solid(i, j, k - 1)) {
+                    pos(2, i, j, k, p);
+                    w[lin(ws, i, j, k)] = colVel(p, 2);
+                }
+                if (k < n.z - 1 && !solid(i, j, k + 1)) {
+                    pos(2, i, j, k + 1, p);
+                    w[lin(ws, i, j, k + 1)] = colVel(p, 2);
+                }
+            }
+}
+
+}  // extern "C"

@@ -511,6 +511,38 @@ void orc_constrain_velocity(const orc_grid* g, double* u, double* v,
     readGrid(vel, u, v, w);
 }
 
+void orc_constrain_velocity_blocked(const orc_grid* g, double* u, double* v,
+                                    double* w, const orc_field* sdf,
+                                    const orc_collider* col, int closed,
+                                    unsigned int depth) {
+    Logging::mute();
+    const Size3 res(g->res[0], g->res[1], g->res[2]);
+    const Vector3D h(g->spacing[0], g->spacing[1], g->spacing[2]);
+    const Vector3D o(g->origin[0], g->origin[1], g->origin[2]);
+    FaceCenteredGrid3 vel(res, h, o);
+    fillGrid(&vel, u, v, w);
+    GridBlockedBoundaryConditionSolver3 bc;
+    bc.updateCollider(col ? makeCollider(col, 0.1) : nullptr, res, h, o);
+    // Replace the collider SDF with the caller's samples (same grid) and
+    // re-derive the cell markers from it with onColliderUpdated's rule
+    // (grid_blocked_boundary_condition_solver3.cpp:79-90).
+    if (sdf && sdf->kind == 1) {
+        auto acc = bc._colliderSdf->dataAccessor();
+        std::memcpy(acc.data(), sdf->data,
+                    sizeof(double) * res.x * res.y * res.z);
+    } else {
+        bc._colliderSdf->fill(sdf ? sdf->value : kMaxD);
+    }
+    const auto grid =
+        std::dynamic_pointer_cast<CellCenteredScalarGrid3>(bc.colliderSdf());
+    bc._marker.forEachIndex([&](size_t i, size_t j, size_t k) {
+        bc._marker(i, j, k) = isInsideSdf((*grid)(i, j, k)) ? 0 : 1;
+    });
+    bc.setClosedDomainBoundaryFlag(closed);
+    bc.constrainVelocity(&vel, depth);
+    readGrid(vel, u, v, w);
+}
+
 void orc_extrapolate(const int res[3], double* data, const char* valid,
                      unsigned int iterations) {
     const Size3 s(res[0], res[1], res[2]);

@@ -278,6 +278,26 @@ def boundary(ref):
          ext_out=ext)
 
 
+def boundary_blocked(ref):
+    """GridBlockedBoundaryConditionSolver3::constrainVelocity on the scene of
+    boundary(): the fractional constraint plus the no-flux pass on the faces
+    of collider cells."""
+    g = np.load(os.path.join(HERE, "boundary_20x16x12.npz"))
+    res = tuple(int(x) for x in g["res"])
+    h, org = tuple(g["h"]), tuple(g["origin"])
+    m = g["moving"]
+    centre = tuple(g["centre"])
+    moving = dict(lin=tuple(m[:3]), ang=tuple(m[3:6]), centre=centre,
+                  friction=float(m[6]))
+    still = dict(lin=(0, 0, 0), ang=(0, 0, 0), centre=centre, friction=0.0)
+    a = ref.constrain_velocity(res, h, org, g["u"], g["v"], g["w"], g["sdf"],
+                               moving, 63, 5, blocked=True)
+    b = ref.constrain_velocity(res, h, org, g["u"], g["v"], g["w"], g["sdf"],
+                               still, 1 + 8 + 32, 3, blocked=True)
+    save("boundary_blocked_20x16x12.npz", a_u=a[0], a_v=a[1], a_w=a[2],
+         b_u=b[0], b_v=b[1], b_w=b[2])
+
+
 def particles(ref):
     res = (20, 12, 16)
     nx, ny, nz = res
@@ -393,6 +413,7 @@ def main():
     blocked(ref)
     transfers(ref)
     boundary(ref)
+    boundary_blocked(ref)
     particles(ref)
     particle_sdf(ref)
     flip_dam_break(ref)

@@ -24,10 +24,13 @@ def solver():
     s.close()
 
 
-def gpu_constrain(solver, res, h, org, u, v, w, sdf, col, closed, depth):
+def gpu_constrain(solver, res, h, org, u, v, w, sdf, col, closed, depth,
+                  blocked=False):
     """Host-pointer path through the Python mirror class."""
     vel = jetgpu.FaceCenteredGrid3(res, h, org, u.copy(), v.copy(), w.copy())
-    bc = jetgpu.GridFractionalBoundaryConditionSolver3(solver)
+    cls = (jetgpu.GridBlockedBoundaryConditionSolver3 if blocked
+           else jetgpu.GridFractionalBoundaryConditionSolver3)
+    bc = cls(solver)
     sdf_f = (jetgpu.CellCenteredScalarGrid3(res, h, org, sdf)
              if isinstance(sdf, np.ndarray) else jetgpu.ConstantScalarField3(sdf))
     bc.updateCollider(sdf_f, None if col is None else jetgpu.Collider.make(
@@ -55,6 +58,26 @@ def test_constrain_velocity_matches_reference(solver):
             assert np.array_equal(out[a], g[f"{tag}_{k}"]), (tag, k)
 
 
+def test_constrain_velocity_blocked_matches_reference(solver):
+    """GridBlockedBoundaryConditionSolver3::constrainVelocity
+    (grid_blocked_boundary_condition_solver3.cpp:23-67)."""
+    g = golden("boundary_20x16x12.npz")
+    gb = golden("boundary_blocked_20x16x12.npz")
+    res = tuple(int(x) for x in g["res"])
+    h, org = tuple(g["h"]), tuple(g["origin"])
+    m = g["moving"]
+    centre = tuple(g["centre"])
+    cases = [("a", dict(lin=m[:3], ang=m[3:6], centre=centre,
+                        friction=float(m[6])), 63, 5),
+             ("b", dict(lin=(0, 0, 0), ang=(0, 0, 0), centre=centre,
+                        friction=0.0), 41, 3)]
+    for tag, col, closed, depth in cases:
+        out = gpu_constrain(solver, res, h, org, g["u"], g["v"], g["w"],
+                            g["sdf"], col, closed, depth, blocked=True)
+        for a, k in enumerate("uvw"):
+            assert np.array_equal(out[a], gb[f"{tag}_{k}"]), (tag, k)
+
+
 def test_extrapolate_matches_reference(solver):
     g = golden("boundary_20x16x12.npz")
     dev = torch.device("cuda", 0)
@@ -67,9 +90,11 @@ def test_extrapolate_matches_reference(solver):
     assert np.array_equal(valid.cpu().numpy(), g["ext_valid"].astype(np.uint8))
 
 
+@pytest.mark.parametrize("blocked", [False, True])
 @pytest.mark.parametrize("res,closed,fr,depth", [((64, 64, 64), 63, 0.25, 5),
                                                  ((72, 40, 56), 22, 0.0, 3)])
-def test_constrain_velocity_device_matches_port(solver, res, closed, fr, depth):
+def test_constrain_velocity_device_matches_port(solver, res, closed, fr, depth,
+                                                blocked):
     """The device-pointer entry on larger random scenes, against the oracle
     port (itself pinned to the reference)."""
     nx, ny, nz = res
@@ -85,7 +110,7 @@ def test_constrain_velocity_device_matches_port(solver, res, closed, fr, depth):
     w = rng.uniform(-1, 1, (nz + 1, ny, nx))
     col = dict(lin=(0.1, 0.2, -0.3), ang=(-0.6, 0.2, 0.9), centre=c, friction=fr)
     ref = oracle.port().constrain_velocity(res, h, org, u, v, w, sdf, col,
-                                           closed, depth)
+                                           closed, depth, blocked=blocked)
     dev = torch.device("cuda", 0)
     tu, tv, tw = (torch.from_numpy(a.copy()).to(dev) for a in (u, v, w))
     tsdf = torch.from_numpy(sdf).to(dev)
@@ -102,7 +127,7 @@ def test_constrain_velocity_device_matches_port(solver, res, closed, fr, depth):
     jetgpu.constrain_velocity_device(
         solver, grid, tu, tv, tw, f,
         jetgpu.Collider.make(col["lin"], col["ang"], col["centre"], fr),
-        closed, depth)
+        closed, depth, blocked=blocked)
     torch.cuda.synchronize()
     for a, t in enumerate((tu, tv, tw)):
         assert np.array_equal(t.cpu().numpy(), ref[a]), "uvw"[a]

@@ -186,6 +186,18 @@ def test_constrain_velocity_bit_exact(port):
             assert np.array_equal(out[a], g[f"{tag}_{k}"]), (tag, k)
 
 
+def test_constrain_velocity_blocked_bit_exact(port):
+    """GridBlockedBoundaryConditionSolver3::constrainVelocity
+    (grid_blocked_boundary_condition_solver3.cpp:23-67) on the same scenes."""
+    g, res, h, org, cases = _boundary_golden()
+    gb = golden("boundary_blocked_20x16x12.npz")
+    for tag, sdf, col, closed, depth in cases[:2]:
+        out = port.constrain_velocity(res, h, org, g["u"], g["v"], g["w"], sdf,
+                                      col, closed, depth, blocked=True)
+        for a, k in enumerate("uvw"):
+            assert np.array_equal(out[a], gb[f"{tag}_{k}"]), (tag, k)
+
+
 def test_extrapolate_to_region_bit_exact(port):
     """extrapolateToRegion (include/jet/detail/array_utils-inl.h:172-244)."""
     g = golden("boundary_20x16x12.npz")
@@ -214,6 +226,12 @@ def test_port_boundary_matches_reference_random(port, reference):
         a = reference.constrain_velocity(res, sp, org, u, v, w, sdf, col,
                                          closed, 5)
         b = port.constrain_velocity(res, sp, org, u, v, w, sdf, col, closed, 5)
+        for x, y in zip(a, b):
+            assert np.array_equal(x, y)
+        a = reference.constrain_velocity(res, sp, org, u, v, w, sdf, col,
+                                         closed, 5, blocked=True)
+        b = port.constrain_velocity(res, sp, org, u, v, w, sdf, col, closed, 5,
+                                    blocked=True)
         for x, y in zip(a, b):
             assert np.array_equal(x, y)
         d = rng.standard_normal((nz, ny, nx))
