@@ -23,7 +23,9 @@ FLIP frames resident on the GPU (transfers, particle SDF, boundary
 conditions, gravity, pressure, advection under the reference's adaptive
 sub-stepping) for the 256^3 dam break with the sphere (about 32M particles)
 and the 64^3 dam break (60 frames); `smoke_512_pressure` — the projection of
-the 512^3 smoke plume (all fluid, closed box).
+the 512^3 smoke plume (all fluid, closed box); `blocked_pressure` — the
+blocked solver (GridSinglePhasePressureSolver3) on the headline scene, with
+one solve of the reference's CPU algorithm beside it.
 
 Timing: W warm-up solves, then K solves bracketed by a barrier and
 synchronize, timed with CUDA events on the library's own stream, max over
@@ -60,6 +62,8 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-flip", action="store_true",
                     help="skip the whole-FLIP-frame measurements")
+    ap.add_argument("--no-blocked", action="store_true",
+                    help="skip the blocked pressure solver leg")
     ap.add_argument("--no-smoke", action="store_true",
                     help="skip the 512^3 smoke-plume projection")
     ap.add_argument("--variants", default=",".join(VARIANTS),
@@ -513,6 +517,86 @@ def run_smoke(args, local, variant: str, steps: int = 3):
     return res
 
 
+def run_blocked(args, local, variant: str, steps: int = 5, cpu: bool = True):
+    """The blocked pressure solver (GridSinglePhasePressureSolver3) on the
+    headline scene: device-resident solves to the same 1e-6 relative true
+    residual, K timed after one warm-up, and (rank 0, no --no-cpu-baseline)
+    one blocked solve of the reference's CPU algorithm on the host cores."""
+    import numpy as np
+    import torch
+    import jetgpu
+    n = args.n
+    h = 1.0 / n
+    dev = torch.device("cuda", local)
+    sc = workload(n)
+    prec, _ = VARIANTS[variant]
+    solver = jetgpu.FdmMgpcgSolver3(**solver_params(prec, "multigrid"),
+                                    device=local)
+    T = lambda a: torch.from_numpy(np.ascontiguousarray(a)).to(dev)
+    u, v, w = T(sc["u"]), T(sc["v"]), T(sc["w"])
+    bs, fs = T(sc["boundary_sdf"]), T(sc["fluid_sdf"])
+    out = [torch.empty_like(a) for a in (u, v, w)]
+    grid = jetgpu.Grid()
+    grid.res[:] = (n, n, n)
+    grid.spacing[:] = (h, h, h)
+    grid.origin[:] = (0, 0, 0)
+
+    def dfield(t):
+        f = jetgpu.ScalarField()
+        f.kind = 1
+        f.data = t.data_ptr()
+        f.res[:] = (n, n, n)
+        f.origin[:] = (0.5 * h,) * 3
+        f.spacing[:] = (h, h, h)
+        return f
+
+    fb, ff = dfield(bs), dfield(fs)
+    stats = jetgpu.SolveStats()
+    torch.cuda.synchronize()
+
+    def solve():
+        jetgpu.solve_pressure_blocked_device(solver, grid, u, v, w, fb, ff,
+                                             *out, None, stats=stats)
+
+    solve()
+    stream = torch.cuda.ExternalStream(solver.stream(), device=dev)
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(stream)
+    for _ in range(steps):
+        solve()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    ms = e0.elapsed_time(e1) / steps
+    res = {"grid": n, "ms_per_solve": round(ms, 3), "solves": steps,
+           "iterations_per_solve": stats.iterations,
+           "relative_residual": stats.relative_residual,
+           "setup_ms": round(stats.setup_ms, 3), "solver": variant,
+           "scene": "the headline 256^3 FLIP dam-break sub-step, cells "
+                    "marked fluid/air/boundary at their centres"}
+    solver.close()
+    if cpu and not args.no_cpu_baseline:
+        import oracle
+        o, kind, threads = cpu_reference()
+        m = max(n // 2, 8)  # a bounded sample: 1/8 of the cells
+        sm = workload(m)
+        t = time.perf_counter()
+        r = o.blocked_pressure_solve((m,) * 3, (1.0 / m,) * 3, (0, 0, 0),
+                                     sm["u"], sm["v"], sm["w"],
+                                     sm["boundary_sdf"], sm["fluid_sdf"],
+                                     oracle.MgParams(**REF_PARAMS))
+        dt = time.perf_counter() - t
+        res["cpu_reference"] = {
+            "grid": m, "ms_per_solve": round(dt * 1e3, 1), "cores": threads,
+            "kind": kind, "iterations": r["iters"],
+            "final_residual_norm": r["resid"],
+            "sample": f"one full {m}^3 blocked solve of the same scene with "
+                      "the reference's FdmMgpcgSolver3(100,5,5,5,20,20,1e-6,"
+                      "1.5,true) until its own stop"}
+    return res
+
+
 def cpu_reference():
     """The reference's CPU algorithm on this host: the compiled reference
     when it exists here, else the oracle port (bit-exact with it)."""
@@ -618,6 +702,10 @@ def main():
     smoke = None
     if not args.no_smoke:
         smoke = run_smoke(args, local, r["head"])
+    blocked = None
+    if not args.no_blocked:
+        blocked = run_blocked(args, local, r["head"],
+                              cpu=rank == 0 and world == 1)
     cb = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         cb = cpu_baseline(args.n, steps=1)
@@ -666,6 +754,8 @@ def main():
         line["flip_steps"] = flip
     if smoke is not None:
         line["smoke_512_pressure"] = smoke
+    if blocked is not None:
+        line["blocked_pressure"] = blocked
     if cb is not None:
         line["cpu_baseline"] = {k: cb[k] for k in ("value", "unit", "cores",
                                                    "kind", "sample")}
