@@ -50,6 +50,89 @@ __device__ __forceinline__ void bary(T x, int iHigh, int* i, T* f) {
     }
 }
 
+__host__ __device__ __forceinline__ unsigned long long dbits(double x) {
+#ifdef __CUDA_ARCH__
+    return (unsigned long long)__double_as_longlong(x);
+#else
+    unsigned long long b;
+    __builtin_memcpy(&b, &x, 8);
+    return b;
+#endif
+}
+
+__host__ __device__ __forceinline__ double bitsd(unsigned long long b) {
+#ifdef __CUDA_ARCH__
+    return __longlong_as_double((long long)b);
+#else
+    double x;
+    __builtin_memcpy(&x, &b, 8);
+    return x;
+#endif
+}
+
+// The same (i, f) as bary<double>, computed on the integer pipe from the bit
+// pattern (GB300 issues FP64 at a small fraction of its integer rate):
+//   x < 0 or -0     -> (0, +0)             (floor(x) < 0; -0 gives f = +0)
+//   x >= iHigh      -> (iHigh - 1, 1)      (floor(x) > iHigh - 1)
+//   0 <= x < iHigh  -> (trunc(x), x - trunc(x))
+// x - floor(x) is exact in IEEE arithmetic (its bits are the fraction bits
+// of x), so assembling it from those bits gives the FP64 subtraction's
+// result bit for bit. A NaN gives (0, NaN) as the FP64 form does (floor,
+// both tests false, int conversion of NaN = 0, NaN - NaN).
+__host__ __device__ __forceinline__ void bary_bits(double x, int iHigh,
+                                                    int* i, double* f) {
+    const unsigned long long X = dbits(x);
+    const unsigned ex = (unsigned)(X >> 52) & 0x7ffu;
+    if (iHigh == 0) {
+        *i = 0;
+        *f = 0.0;
+        return;
+    }
+    if (X >> 63) {  // negative, -0 or a negative NaN
+        *i = 0;
+        *f = (ex == 0x7ffu && (X << 12)) ? x : 0.0;
+        return;
+    }
+    if (ex == 0x7ffu && (X << 12)) {  // positive NaN
+        *i = 0;
+        *f = x;
+        return;
+    }
+    if (X >= dbits((double)iHigh)) {
+        *i = iHigh - 1;
+        *f = 1.0;
+        return;
+    }
+    const int e = (int)ex - 1023;  // x < iHigh <= 2^31, so e <= 30
+    if (e < 0) {                   // 0 <= x < 1
+        *i = 0;
+        *f = x;
+        return;
+    }
+    const unsigned long long M = (X & 0xfffffffffffffull) | (1ull << 52);
+    const int sh = 52 - e;         // fraction bits of x
+    *i = (int)(M >> sh);
+    const unsigned long long F = M & ((1ull << sh) - 1ull);
+    if (F == 0ull) {
+        *f = 0.0;
+        return;
+    }
+#ifdef __CUDA_ARCH__
+    const int p = 63 - __clzll((long long)F);  // top set bit of F
+#else
+    const int p = 63 - __builtin_clzll(F);
+#endif
+    // f = F * 2^-sh, top bit at p: exponent p - sh, mantissa F << (52 - p).
+    const unsigned long long be = (unsigned long long)(p - sh + 1023);
+    *f = bitsd((be << 52) | ((F << (52 - p)) & 0xfffffffffffffull));
+}
+
+template <>
+__device__ __forceinline__ void bary<double>(double x, int iHigh, int* i,
+                                             double* f) {
+    bary_bits(x, iHigh, i, f);
+}
+
 template <typename T>
 __device__ __forceinline__ T lerp_t(T a, T b, T f) {
     return ((T)1 - f) * a + f * b;
