@@ -168,13 +168,14 @@ def workload(n: int):
 
 
 def solver_params(precision: str, preconditioner: str = "multigrid"):
-    """GPU solver settings: FdmMgpcgSolver3(200, 6, 2, 2, 10, 2, 1e-6, 1.0,
-    true). Two symmetric red-black sweeps per level and a masked coarse
-    residual give mesh-independent convergence (5-8 iterations)."""
+    """GPU solver settings: FdmMgpcgSolver3(200, 6, 2, 2, 5, 2, 1e-6, 1.2,
+    true). Two symmetric red-black SOR sweeps per level (omega 1.2) and a
+    masked coarse residual give mesh-independent convergence (5-7
+    iterations)."""
     return dict(numberOfCgIter=200, maxNumberOfLevels=6,
                 numberOfRestrictionIter=2, numberOfCorrectionIter=2,
-                numberOfCoarsestIter=10, numberOfFinalIter=2,
-                maxTolerance=TOL, sorFactor=1.0, useRedBlackOrdering=True,
+                numberOfCoarsestIter=5, numberOfFinalIter=2,
+                maxTolerance=TOL, sorFactor=1.2, useRedBlackOrdering=True,
                 precision=precision, preconditioner=preconditioner,
                 maxRefinements=8)
 
@@ -726,7 +727,7 @@ def main():
                         "solve (weights + system + MGPCG + gradient), sphere "
                         "obstacle",
             "grid": args.n, "tolerance": TOL,
-            "solver": r["head"] + ": MGPCG(200,6,2,2,10,2,1e-6,1.0,"
+            "solver": r["head"] + ": MGPCG(200,6,2,2,5,2,1e-6,1.2,"
                       "red-black), masked symmetric V-cycle",
             "parallelism": f"replicas x{world}",
             "l2": "inputs and solver state >> L2 (no flush)",

@@ -307,13 +307,13 @@ void jetgpu_config_default(jetgpu_config* cfg) {
     std::memset(cfg, 0, sizeof(*cfg));
     cfg->device = 0;
     cfg->max_cg_iter = 100;
-    cfg->max_levels = 5;
+    cfg->max_levels = 6;
     cfg->restrict_iter = 2;
     cfg->correct_iter = 2;
-    cfg->coarsest_iter = 10;
+    cfg->coarsest_iter = 5;
     cfg->final_iter = 2;
     cfg->tolerance = 1e-6;
-    cfg->sor = 1.0;
+    cfg->sor = 1.2;
     cfg->red_black = 1;
     cfg->precision = JETGPU_PRECISION_FP32;
     cfg->preconditioner = JETGPU_PRECOND_MULTIGRID;

