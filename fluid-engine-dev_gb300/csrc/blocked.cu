@@ -46,7 +46,7 @@ __device__ __forceinline__ double sample(const FieldS& F, double x, double y,
                                          double z) {
     if (F.f.kind == 0) return F.f.value;
     const Dims s{F.f.res[0], F.f.res[1], F.f.res[2]};
-    return sample_face<double, double>(F.f.data, s,
+    return sample_face_grid(F.f.data, s,
                                        F.s[0].div(x - F.f.origin[0]),
                                        F.s[1].div(y - F.f.origin[1]),
                                        F.s[2].div(z - F.f.origin[2]));

@@ -64,7 +64,7 @@ __device__ double sample_sdf(const FieldDesc& F, const S3& fsp, double x,
                              double y, double z) {
     if (F.kind == 0) return F.value;
     const Dims s{F.res[0], F.res[1], F.res[2]};
-    return sample_face<double, double>(F.data, s, fsp.s[0].div(x - F.origin[0]),
+    return sample_face_grid(F.data, s, fsp.s[0].div(x - F.origin[0]),
                                        fsp.s[1].div(y - F.origin[1]),
                                        fsp.s[2].div(z - F.origin[2]));
 }
@@ -306,7 +306,7 @@ __global__ void k_bc_project(FaceSet fs, int a, H3 h, S3 gsp, H3 inv,
         double cv[3], fv[3], g[3];
         collider_vel(col, p, cv);
         for (int b = 0; b < 3; ++b)  // FaceCenteredGrid3::sample
-            fv[b] = sample_face<double, double>(
+            fv[b] = sample_face_grid(
                 vel[b], fs.s[b], gsp.s[0].div(p[0] - fs.o[b][0]),
                 gsp.s[1].div(p[1] - fs.o[b][1]),
                 gsp.s[2].div(p[2] - fs.o[b][2]));

@@ -387,7 +387,12 @@ struct SpacingInv {
 // FP64 sum and product is the reference's, in its order; what changes is how
 // the exact ones are issued: classification on the FP32 SDF, exact widening
 // and power-of-two scaling on the integer pipe, divisions out of line.
-__global__ void k_build_system(Dims n, SpacingInv S,
+//
+// Latency-bound at the 94 registers it would take freely (two blocks per
+// SM): capped at 64 for four blocks, with a few spilled values, it runs
+// 1.6x faster (1.21 -> 0.77 ms per 256^3 solve).
+__global__ void __launch_bounds__(kThreads, 4)
+    k_build_system(Dims n, SpacingInv S,
                                const float* __restrict__ phi,
                                const float* __restrict__ uw,
                                const float* __restrict__ vw,

@@ -50,9 +50,15 @@ __device__ __forceinline__ void bary(T x, int iHigh, int* i, T* f) {
     }
 }
 
+// The bit pattern of a double and back. On the device the words move
+// through PTX, which keeps the integer tests on them from being turned back
+// into FP64 compares and conversions (GB300 issues FP64 at a small fraction
+// of its integer rate).
 __host__ __device__ __forceinline__ unsigned long long dbits(double x) {
 #ifdef __CUDA_ARCH__
-    return (unsigned long long)__double_as_longlong(x);
+    unsigned lo, hi;
+    asm("mov.b64 {%0, %1}, %2;" : "=r"(lo), "=r"(hi) : "d"(x));
+    return ((unsigned long long)hi << 32) | lo;
 #else
     unsigned long long b;
     __builtin_memcpy(&b, &x, 8);
@@ -62,7 +68,11 @@ __host__ __device__ __forceinline__ unsigned long long dbits(double x) {
 
 __host__ __device__ __forceinline__ double bitsd(unsigned long long b) {
 #ifdef __CUDA_ARCH__
-    return __longlong_as_double((long long)b);
+    double x;
+    asm("mov.b64 %0, {%1, %2};"
+        : "=d"(x)
+        : "r"((unsigned)b), "r"((unsigned)(b >> 32)));
+    return x;
 #else
     double x;
     __builtin_memcpy(&x, &b, 8);
@@ -133,9 +143,93 @@ __device__ __forceinline__ void bary<double>(double x, int iHigh, int* i,
     bary_bits(x, iHigh, i, f);
 }
 
+// The reference's lerp (include/jet/detail/math_utils-inl.h),
+// (1 - f) * a + f * b, evaluated as the same IEEE operations.
+__host__ __device__ __forceinline__ double lerp_ref(double a, double b,
+                                                    double f) {
+    return (1.0 - f) * a + f * b;
+}
+
+// The same value with the fractions that grid-aligned samples produce taken
+// on the integer pipe:
+//  * f = 0.5: both products are exact halvings, so the result is the one
+//    rounding of (a + b) / 2 = half(RN(a + b)) — exact whenever a and b are
+//    zero or have exponent fields in [2, 0x7fd] (no overflow of a + b; a
+//    sum small enough for its half to be subnormal is exact, and so is that
+//    half);
+//  * f = 0: the result is 1 * a + 0 * b, which is a itself when a is
+//    non-zero and b finite;
+//  * f = 1: 0 * a + 1 * b, which is b when b is non-zero and a finite.
+// Anything else takes the reference's expression. fb is the bit pattern of
+// f (computed once per axis by the caller).
+__host__ __device__ __forceinline__ unsigned expo_bits(unsigned long long x) {
+    return (unsigned)(x >> 52) & 0x7ffu;
+}
+__host__ __device__ __forceinline__ bool half_safe(unsigned long long x) {
+    const unsigned e = expo_bits(x);
+    return (e >= 2u && e <= 0x7fdu) || (x << 1) == 0ull;
+}
+__host__ __device__ __forceinline__ double half_exact(double x) {
+    const unsigned long long b = dbits(x);
+    const unsigned e = expo_bits(b);
+    if (e > 1u && e < 0x7ffu) return bitsd(b - (1ull << 52));
+    return x * 0.5;
+}
+constexpr unsigned long long kHalfD = 0x3FE0000000000000ull;
+constexpr unsigned long long kOneD = 0x3FF0000000000000ull;
+__host__ __device__ __forceinline__ double lerp_fast(double a, double b,
+                                                     double f,
+                                                     unsigned long long fb) {
+    if (fb == kHalfD) {
+        const unsigned long long A = dbits(a), B = dbits(b);
+        if (half_safe(A) && half_safe(B)) return half_exact(a + b);
+    } else if (fb == 0ull) {
+        if ((dbits(a) << 1) != 0ull && expo_bits(dbits(b)) != 0x7ffu) return a;
+    } else if (fb == kOneD) {
+        if ((dbits(b) << 1) != 0ull && expo_bits(dbits(a)) != 0x7ffu) return b;
+    }
+    return lerp_ref(a, b, f);
+}
+
 template <typename T>
 __device__ __forceinline__ T lerp_t(T a, T b, T f) {
     return ((T)1 - f) * a + f * b;
+}
+
+// trilerp (include/jet/detail/math_utils-inl.h:177-211): x first, then y,
+// then z.
+template <typename T>
+__device__ __forceinline__ T trilerp(T f000, T f100, T f010, T f110, T f001,
+                                     T f101, T f011, T f111, T fx, T fy,
+                                     T fz) {
+    const T b0 = lerp_t(lerp_t(f000, f100, fx), lerp_t(f010, f110, fx), fy);
+    const T b1 = lerp_t(lerp_t(f001, f101, fx), lerp_t(f011, f111, fx), fy);
+    return lerp_t(b0, b1, fz);
+}
+// A fraction for which lerp_fast has an integer-pipe shortcut.
+__host__ __device__ __forceinline__ bool aligned_frac(unsigned long long fb) {
+    return fb == 0ull || fb == kHalfD || fb == kOneD;
+}
+// trilerp for samples taken at grid-aligned points of the sampled grid
+// (faces, nodes, cell centres): when all three fractions are 0, 1/2 or 1 the
+// lerps take the integer-pipe shortcuts; any other sample runs the
+// reference's lerps unchanged, with one test per sample.
+__device__ __forceinline__ double trilerp_grid(
+    double f000, double f100, double f010, double f110, double f001,
+    double f101, double f011, double f111, double fx, double fy, double fz) {
+    const unsigned long long bx = dbits(fx), by = dbits(fy), bz = dbits(fz);
+    if (aligned_frac(bx) && aligned_frac(by) && aligned_frac(bz)) {
+        const double b0 = lerp_fast(lerp_fast(f000, f100, fx, bx),
+                                    lerp_fast(f010, f110, fx, bx), fy, by);
+        const double b1 = lerp_fast(lerp_fast(f001, f101, fx, bx),
+                                    lerp_fast(f011, f111, fx, bx), fy, by);
+        return lerp_fast(b0, b1, fz, bz);
+    }
+    const double b0 = lerp_ref(lerp_ref(f000, f100, fx),
+                               lerp_ref(f010, f110, fx), fy);
+    const double b1 = lerp_ref(lerp_ref(f001, f101, fx),
+                               lerp_ref(f011, f111, fx), fy);
+    return lerp_ref(b0, b1, fz);
 }
 
 // Trilinear sample of a face array with the reference's operator() rule
@@ -153,9 +247,29 @@ __device__ T sample_face(const V* __restrict__ d, Dims s, T nx, T ny, T nz) {
     const T f010 = d[lin(i, jp1, k, s.x, s.y)], f110 = d[lin(ip1, jp1, k, s.x, s.y)];
     const T f001 = d[lin(i, j, kp1, s.x, s.y)], f101 = d[lin(ip1, j, kp1, s.x, s.y)];
     const T f011 = d[lin(i, jp1, kp1, s.x, s.y)], f111 = d[lin(ip1, jp1, kp1, s.x, s.y)];
-    const T b0 = lerp_t(lerp_t(f000, f100, fx), lerp_t(f010, f110, fx), fy);
-    const T b1 = lerp_t(lerp_t(f001, f101, fx), lerp_t(f011, f111, fx), fy);
-    return lerp_t(b0, b1, fz);
+    return trilerp<T>(f000, f100, f010, f110, f001, f101, f011, f111, fx, fy,
+                      fz);
+}
+
+// sample_face for points that usually sit on the sampled grid's lattice
+// (collider SDF at faces and cell centres, SDFs at nodes): same result, with
+// trilerp_grid's shortcuts. Particle positions use sample_face.
+__device__ __forceinline__ double sample_face_grid(const double* __restrict__ d,
+                                                   Dims s, double nx,
+                                                   double ny, double nz) {
+    int i, j, k;
+    double fx, fy, fz;
+    bary<double>(nx, s.x - 1, &i, &fx);
+    bary<double>(ny, s.y - 1, &j, &fy);
+    bary<double>(nz, s.z - 1, &k, &fz);
+    const int ip1 = min(i + 1, s.x - 1), jp1 = min(j + 1, s.y - 1),
+              kp1 = min(k + 1, s.z - 1);
+    return trilerp_grid(
+        d[lin(i, j, k, s.x, s.y)], d[lin(ip1, j, k, s.x, s.y)],
+        d[lin(i, jp1, k, s.x, s.y)], d[lin(ip1, jp1, k, s.x, s.y)],
+        d[lin(i, j, kp1, s.x, s.y)], d[lin(ip1, j, kp1, s.x, s.y)],
+        d[lin(i, jp1, kp1, s.x, s.y)], d[lin(ip1, jp1, kp1, s.x, s.y)], fx,
+        fy, fz);
 }
 
 struct FaceSet {

@@ -268,7 +268,7 @@ __global__ void k_sdf_valid(SdfGeom G, FieldDesc col,
             const double y = G.d0[1] + G.h[1] * (double)j;
             const double z = G.d0[2] + G.h[2] * (double)k;
             const Dims s{col.res[0], col.res[1], col.res[2]};
-            phi = sample_face<double, double>(col.data, s,
+            phi = sample_face_grid(col.data, s,
                                               (x - col.origin[0]) / col.spacing[0],
                                               (y - col.origin[1]) / col.spacing[1],
                                               (z - col.origin[2]) / col.spacing[2]);
