@@ -16,40 +16,6 @@
 namespace jg {
 namespace smp {
 
-// x / h for a grid spacing h. IEEE division and multiplication both return
-// the correctly rounded exact result, and when h is a power of two x / h and
-// x * (1 / h) are the same real number (x * 2^-k), so the multiply gives the
-// reference's quotient bit for bit at a fraction of an FP64 divide's cost.
-struct Spacing {
-    double h, inv;
-    int pow2;
-    __device__ __forceinline__ double div(double x) const {
-        return pow2 ? x * inv : x / h;
-    }
-};
-inline Spacing make_spacing(double h) {
-    int e = 0;
-    return Spacing{h, 1.0 / h, std::frexp(h, &e) == 0.5 ? 1 : 0};
-}
-
-template <typename T>
-__device__ __forceinline__ void bary(T x, int iHigh, int* i, T* f) {
-    T s = floor(x);
-    if (iHigh == 0) {
-        *i = 0;
-        *f = (T)0;
-    } else if (s < (T)0) {
-        *i = 0;
-        *f = (T)0;
-    } else if (s > (T)(iHigh - 1)) {
-        *i = iHigh - 1;
-        *f = (T)1;
-    } else {
-        *i = (int)s;
-        *f = x - s;
-    }
-}
-
 // The bit pattern of a double and back. On the device the words move
 // through PTX, which keeps the integer tests on them from being turned back
 // into FP64 compares and conversions (GB300 issues FP64 at a small fraction
@@ -78,6 +44,55 @@ __host__ __device__ __forceinline__ double bitsd(unsigned long long b) {
     __builtin_memcpy(&x, &b, 8);
     return x;
 #endif
+}
+
+// x * 2^k (scale = 2^k) exactly: an exponent add on the integer pipe when
+// x and the result are normal; zeros pass through; anything else takes the
+// FP64 multiply, which rounds the same way.
+__host__ __device__ __forceinline__ double scale_exact(double x, int k,
+                                                       double scale) {
+    const unsigned long long b = dbits(x);
+    if ((b << 1) == 0ull) return x;
+    const int e = (int)((b >> 52) & 0x7ffu);
+    if (e > 0 && e < 0x7ff && e + k > 0 && e + k < 0x7ff)
+        return bitsd(b + ((unsigned long long)(long long)k << 52));
+    return x * scale;
+}
+
+// x / h for a grid spacing h. IEEE division and multiplication both return
+// the correctly rounded exact result, and when h is a power of two x / h and
+// x * (1 / h) are the same real number (x * 2^k), so scaling the exponent
+// gives the reference's quotient bit for bit without an FP64 divide.
+struct Spacing {
+    double h, inv;
+    int pow2;
+    int k;  // inv = 2^k when pow2
+    __device__ __forceinline__ double div(double x) const {
+        return pow2 ? scale_exact(x, k, inv) : x / h;
+    }
+};
+inline Spacing make_spacing(double h) {
+    int e = 0;
+    const bool p2 = std::frexp(h, &e) == 0.5;  // h = 2^(e-1)
+    return Spacing{h, 1.0 / h, p2 ? 1 : 0, p2 ? 1 - e : 0};
+}
+
+template <typename T>
+__device__ __forceinline__ void bary(T x, int iHigh, int* i, T* f) {
+    T s = floor(x);
+    if (iHigh == 0) {
+        *i = 0;
+        *f = (T)0;
+    } else if (s < (T)0) {
+        *i = 0;
+        *f = (T)0;
+    } else if (s > (T)(iHigh - 1)) {
+        *i = iHigh - 1;
+        *f = (T)1;
+    } else {
+        *i = (int)s;
+        *f = x - s;
+    }
 }
 
 // The same (i, f) as bary<double>, computed on the integer pipe from the bit

@@ -376,18 +376,29 @@ __global__ void k_move_particles(long np, double* __restrict__ pos,
         double p0[3] = {pos[3 * q], pos[3 * q + 1], pos[3 * q + 2]};
         double p1[3] = {p0[0], p0[1], p0[2]};
         double vv[3] = {vel[3 * q], vel[3 * q + 1], vel[3 * q + 2]};
+        // The three face grids share their data origins axis by axis (the
+        // grid origin on a face's normal axis, origin + h/2 on the others),
+        // so each point needs six subtractions, not nine.
+        const Spacing sp[3] = {hx, hy, hz};
+        auto sample3 = [&](const double q[3], double out[3]) {
+            double nn[3], nt[3];
+#pragma unroll
+            for (int d = 0; d < 3; ++d) {
+                nn[d] = sp[d].div(q[d] - fs.o[d][d]);
+                nt[d] = sp[d].div(q[d] - fs.o[(d + 1) % 3][d]);
+            }
+#pragma unroll
+            for (int a = 0; a < 3; ++a)
+                out[a] = sample_face<double, double>(
+                    grid[a], fs.s[a], a == 0 ? nn[0] : nt[0],
+                    a == 1 ? nn[1] : nt[1], a == 2 ? nn[2] : nt[2]);
+        };
         for (unsigned t = 0; t < nsub; ++t) {
             double v0[3], mid[3], vm[3];
-            for (int a = 0; a < 3; ++a)
-                v0[a] = sample_face<double, double>(
-                    grid[a], fs.s[a], hx.div(p0[0] - fs.o[a][0]),
-                    hy.div(p0[1] - fs.o[a][1]), hz.div(p0[2] - fs.o[a][2]));
+            sample3(p0, v0);
             const double hs = 0.5 * sdt;
             for (int d = 0; d < 3; ++d) mid[d] = p0[d] + hs * v0[d];
-            for (int a = 0; a < 3; ++a)
-                vm[a] = sample_face<double, double>(
-                    grid[a], fs.s[a], hx.div(mid[0] - fs.o[a][0]),
-                    hy.div(mid[1] - fs.o[a][1]), hz.div(mid[2] - fs.o[a][2]));
+            sample3(mid, vm);
             for (int d = 0; d < 3; ++d) p1[d] = p0[d] + sdt * vm[d];
             for (int d = 0; d < 3; ++d) p0[d] = p1[d];
         }

@@ -1,6 +1,7 @@
-// Host check of smp::lerp_fast (csrc/sampling.cuh): the integer-pipe
-// shortcuts for the fractions 0, 1/2 and 1 must give the bits of the
-// reference's lerp, (1 - f) * a + f * b, for random values and random bit
+// Host check of smp::lerp_fast and smp::scale_exact (csrc/sampling.cuh):
+// the integer-pipe shortcuts for the fractions 0, 1/2 and 1 must give the
+// bits of the reference's lerp, (1 - f) * a + f * b, and the exponent add
+// the bits of the FP64 product x * 2^k, for random values and random bit
 // patterns (zeros of both signs, subnormals, values whose halves are
 // subnormal, infinities, NaN, values near overflow). Built and run by
 // tests/test_native.py with FP contraction off, like the reference.
@@ -65,6 +66,29 @@ int main() {
         const double b = -a * (1.0 + std::ldexp(U(g), -40));
         check(a, b, 0.5);
         check(b, a, 0.5);
+    }
+    // scale_exact(x, k, 2^k) against the FP64 product x * 2^k.
+    auto check_scale = [&](double x, int k) {
+        volatile double vx = x, vs = std::ldexp(1.0, k);
+        const double r = vx * vs;
+        const double q = scale_exact(x, k, std::ldexp(1.0, k));
+        ++n;
+        if (!(bits(r) == bits(q) || (std::isnan(r) && std::isnan(q)))) {
+            if (bad < 10)
+                std::printf("scale x=%.17g k=%d ref=%.17g fast=%.17g\n", x, k, r, q);
+            ++bad;
+        }
+    };
+    for (int k = -30; k <= 30; ++k) {
+        for (double x : special) check_scale(x, k);
+        for (int t = 0; t < 20000; ++t) {
+            const unsigned long long y = g();
+            double x;
+            std::memcpy(&x, &y, 8);
+            check_scale(x, k);
+            check_scale(U(g), k);
+            check_scale(std::ldexp(U(g), -1015 - (int)(g() % 12)), k);
+        }
     }
     std::printf("checked %ld, mismatches %ld\n", n, bad);
     return bad != 0;
