@@ -70,14 +70,17 @@ __device__ __forceinline__ unsigned expo_d(double x) {
     dwords(x, lo, hi);
     return (hi >> 20) & 0x7ffu;
 }
-// x * 0.5 exactly by an exponent decrement when x and x/2 are normal.
+// x * 0.5 exactly by an exponent decrement when x and x/2 are normal (the
+// FP64 fallback out of line, so that it is not predicated into every call).
+__device__ __noinline__ double half_slow(double x) { return x * 0.5; }
 __device__ __forceinline__ double half_d(double x) {
     unsigned lo, hi;
     dwords(x, lo, hi);
     const unsigned e = (hi >> 20) & 0x7ffu;
     if (e > 1u && e < 0x7ffu) return djoin(lo, hi - 0x100000u);
-    return x * 0.5;
+    return half_slow(x);
 }
+__device__ __noinline__ double scale_slow(double x, double s) { return x * s; }
 // x * 2^k exactly by an exponent add when x and the result are normal;
 // zeros pass through; anything else multiplies by the FP64 scale.
 __device__ __forceinline__ double scale_pow2(double x, int k, double scale) {
@@ -87,7 +90,7 @@ __device__ __forceinline__ double scale_pow2(double x, int k, double scale) {
     if (((hi & 0x7fffffffu) | lo) == 0u) return x;
     if (e > 0 && e < 0x7ff && e + k > 0 && e + k < 0x7ff)
         return djoin(lo, hi + ((unsigned)k << 20));
-    return x * scale;
+    return scale_slow(x, scale);
 }
 // -x exactly by a sign flip, except that -(+0) stays +0 as 0.0 - 0.0 does.
 __device__ __forceinline__ double zero_minus(double x) {

@@ -465,6 +465,53 @@ __global__ void __launch_bounds__(kThreads)
     }
 }
 
+// k_restrict for coarse rows of even length: a thread owns coarse cells
+// 2p and 2p+1 of a row, whose fine x taps 4p-1 .. 4p+4 (clamped as in
+// k_restrict) are one aligned 16-byte load and two scalar loads per fine
+// row instead of eight scalar loads. Same taps, weights and x-then-y-then-z
+// order as k_restrict.
+__global__ void __launch_bounds__(kThreads)
+    k_restrict2(const float* __restrict__ fine, float* __restrict__ coarse,
+                const float* __restrict__ coarse_phi, Dims c) {
+    const Dims q{c.x / 2, c.y, c.z};
+    const long G = q.count();
+    const int fx = 2 * c.x, fy = 2 * c.y;
+    const float kern[4] = {0.125f, 0.375f, 0.375f, 0.125f};
+    for (long t = blockIdx.x * (long)kThreads + threadIdx.x; t < G;
+         t += (long)gridDim.x * kThreads) {
+        int p, j, k;
+        cell_ijk(t, q, p, j, k);
+        const int jI[4] = {j > 0 ? 2 * j - 1 : 2 * j, 2 * j, 2 * j + 1,
+                           j + 1 < c.y ? 2 * j + 2 : 2 * j + 1};
+        const int kI[4] = {k > 0 ? 2 * k - 1 : 2 * k, 2 * k, 2 * k + 1,
+                           k + 1 < c.z ? 2 * k + 2 : 2 * k + 1};
+        const int xm = p > 0 ? 4 * p - 1 : 4 * p;
+        const int x4 = 2 * p + 2 < c.x ? 4 * p + 4 : 4 * p + 3;
+        float sum0 = 0.0f, sum1 = 0.0f;
+#pragma unroll
+        for (int z = 0; z < 4; ++z) {
+            float sy0 = 0.0f, sy1 = 0.0f;
+#pragma unroll
+            for (int y = 0; y < 4; ++y) {
+                const float* rowp = fine + lin(0, jI[y], kI[z], fx, fy);
+                const float4 f = *reinterpret_cast<const float4*>(rowp + 4 * p);
+                const float fm = rowp[xm], f4 = rowp[x4];
+                const float sx0 = kern[0] * fm + kern[1] * f.x +
+                                  kern[2] * f.y + kern[3] * f.z;
+                const float sx1 = kern[0] * f.y + kern[1] * f.z +
+                                  kern[2] * f.w + kern[3] * f4;
+                sy0 += kern[y] * sx0;
+                sy1 += kern[y] * sx1;
+            }
+            sum0 += kern[z] * sy0;
+            sum1 += kern[z] * sy1;
+        }
+        const long o = lin(2 * p, j, k, c.x, c.y);
+        coarse[o] = (coarse_phi[o] < 0.0f) ? sum0 : 0.0f;
+        coarse[o + 1] = (coarse_phi[o + 1] < 0.0f) ? sum1 : 0.0f;
+    }
+}
+
 // K10: FdmMgUtils3::correct (fdm_mg_linear_system3.cpp:100-179): fine +=
 // trilinear (1/4, 3/4) prolongation of coarse, clamped at the edges.
 __global__ void __launch_bounds__(kThreads)
@@ -496,6 +543,60 @@ __global__ void __launch_bounds__(kThreads)
         const float a0 = wj0 * (wi0 * c000 + wi1 * c100) + wj1 * (wi0 * c010 + wi1 * c110);
         const float a1 = wj0 * (wi0 * c001 + wi1 * c101) + wj1 * (wi0 * c011 + wi1 * c111);
         fine[t] += wk0 * a0 + wk1 * a1;
+    }
+}
+
+// k_correct for fine rows whose length is a multiple of 4: a thread owns 4
+// consecutive fine cells of a row (fine i = 4m..4m+3, coarse 2m and 2m+1),
+// so the 16 coarse values they share are loaded once, the index division is
+// done once, and the fine values move as one 16-byte load and store. Same
+// stencil, weights and x-then-y-then-z order as k_correct.
+__global__ void __launch_bounds__(kThreads)
+    k_correct4(const float* __restrict__ coarse, float* __restrict__ fine,
+               Dims c) {
+    const Dims n{2 * c.x, 2 * c.y, 2 * c.z};
+    const Dims q{n.x / 4, n.y, n.z};  // 4-cell groups
+    const long G = q.count();
+    for (long t = blockIdx.x * (long)kThreads + threadIdx.x; t < G;
+         t += (long)gridDim.x * kThreads) {
+        int m, j, k;
+        cell_ijk(t, q, m, j, k);
+        const int cj = j >> 1, ck = k >> 1;
+        int j0, j1, k0, k1;
+        float wj0, wj1, wk0, wk1;
+        if ((j & 1) == 0) { j0 = j > 1 ? cj - 1 : cj; j1 = cj; wj0 = 0.25f; wj1 = 0.75f; }
+        else { j0 = cj; j1 = j + 1 < n.y ? cj + 1 : cj; wj0 = 0.75f; wj1 = 0.25f; }
+        if ((k & 1) == 0) { k0 = k > 1 ? ck - 1 : ck; k1 = ck; wk0 = 0.25f; wk1 = 0.75f; }
+        else { k0 = ck; k1 = k + 1 < n.z ? ck + 1 : ck; wk0 = 0.75f; wk1 = 0.25f; }
+        // Coarse x columns 2m-1 .. 2m+2, clamped as k_correct clamps them.
+        const int x0 = 2 * m, xm = m > 0 ? x0 - 1 : x0,
+                  x2 = 4 * m + 4 < n.x ? x0 + 2 : x0 + 1;
+        float r[4][4];  // [row (j0,k0),(j1,k0),(j0,k1),(j1,k1)][fine cell]
+        const int rj[4] = {j0, j1, j0, j1}, rk[4] = {k0, k0, k1, k1};
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+            const float* row = coarse + lin(0, rj[e], rk[e], c.x, c.y);
+            const float cm = row[xm], c0 = row[x0], c1 = row[x0 + 1],
+                        c2 = row[x2];
+            r[e][0] = 0.25f * cm + 0.75f * c0;
+            r[e][1] = 0.75f * c0 + 0.25f * c1;
+            r[e][2] = 0.25f * c0 + 0.75f * c1;
+            r[e][3] = 0.75f * c1 + 0.25f * c2;
+        }
+        float4* f4 = reinterpret_cast<float4*>(fine + lin(4 * m, j, k, n.x, n.y));
+        float4 v = *f4;
+        float o[4];
+#pragma unroll
+        for (int l = 0; l < 4; ++l) {
+            const float a0 = wj0 * r[0][l] + wj1 * r[1][l];
+            const float a1 = wj0 * r[2][l] + wj1 * r[3][l];
+            o[l] = wk0 * a0 + wk1 * a1;
+        }
+        v.x += o[0];
+        v.y += o[1];
+        v.z += o[2];
+        v.w += o[3];
+        *f4 = v;
     }
 }
 
@@ -864,14 +965,22 @@ float* vcycle_level(Ctx* c, unsigned l, const float* b, float* x, float* alt) {
     }
     {
         Prof pr(c, K_RESTRICT, 4.0 * L.n.count() + 8.0 * C.n.count());
-        k_restrict<<<grid_for(c, C.n.count()), kThreads, 0, c->stream>>>(
-            L.r, C.b, C.phi, C.n);
+        if (C.n.x % 2 == 0)
+            k_restrict2<<<grid_for(c, C.n.count() / 2), kThreads, 0,
+                          c->stream>>>(L.r, C.b, C.phi, C.n);
+        else
+            k_restrict<<<grid_for(c, C.n.count()), kThreads, 0, c->stream>>>(
+                L.r, C.b, C.phi, C.n);
     }
     const float* xc = vcycle_level(c, l + 1, C.b, C.x, C.x2);
     {
         Prof pr(c, K_CORRECT, 8.0 * L.n.count() + 4.0 * C.n.count());
-        k_correct<<<grid_for(c, L.n.count()), kThreads, 0, c->stream>>>(
-            xc, cur, C.n);
+        if (L.n.x % 4 == 0)
+            k_correct4<<<grid_for(c, L.n.count() / 4), kThreads, 0,
+                         c->stream>>>(xc, cur, C.n);
+        else
+            k_correct<<<grid_for(c, L.n.count()), kThreads, 0, c->stream>>>(
+                xc, cur, C.n);
     }
     return smooth(c, L, b, cur, other,
                   l == 0 ? cfg.final_iter : cfg.correct_iter, true, false, l);

@@ -46,6 +46,13 @@ __host__ __device__ __forceinline__ double bitsd(unsigned long long b) {
 #endif
 }
 
+// The FP64 fallbacks of the shortcuts below, out of line: a call keeps the
+// compiler from predicating these FP64 instructions into every evaluation,
+// where they would occupy the FP64 pipe even when the shortcut is taken.
+static __host__ __device__ __noinline__ double mul_slow(double x, double y) {
+    return x * y;
+}
+
 // x * 2^k (scale = 2^k) exactly: an exponent add on the integer pipe when
 // x and the result are normal; zeros pass through; anything else takes the
 // FP64 multiply, which rounds the same way.
@@ -56,7 +63,7 @@ __host__ __device__ __forceinline__ double scale_exact(double x, int k,
     const int e = (int)((b >> 52) & 0x7ffu);
     if (e > 0 && e < 0x7ff && e + k > 0 && e + k < 0x7ff)
         return bitsd(b + ((unsigned long long)(long long)k << 52));
-    return x * scale;
+    return mul_slow(x, scale);
 }
 
 // x / h for a grid spacing h. IEEE division and multiplication both return
@@ -188,7 +195,11 @@ __host__ __device__ __forceinline__ double half_exact(double x) {
     const unsigned long long b = dbits(x);
     const unsigned e = expo_bits(b);
     if (e > 1u && e < 0x7ffu) return bitsd(b - (1ull << 52));
-    return x * 0.5;
+    return mul_slow(x, 0.5);
+}
+static __host__ __device__ __noinline__ double lerp_slow(double a, double b,
+                                                         double f) {
+    return lerp_ref(a, b, f);
 }
 constexpr unsigned long long kHalfD = 0x3FE0000000000000ull;
 constexpr unsigned long long kOneD = 0x3FF0000000000000ull;
@@ -203,7 +214,7 @@ __host__ __device__ __forceinline__ double lerp_fast(double a, double b,
     } else if (fb == kOneD) {
         if ((dbits(b) << 1) != 0ull && expo_bits(dbits(a)) != 0x7ffu) return b;
     }
-    return lerp_ref(a, b, f);
+    return lerp_slow(a, b, f);
 }
 
 template <typename T>
@@ -225,6 +236,16 @@ __device__ __forceinline__ T trilerp(T f000, T f100, T f010, T f110, T f001,
 __host__ __device__ __forceinline__ bool aligned_frac(unsigned long long fb) {
     return fb == 0ull || fb == kHalfD || fb == kOneD;
 }
+static __device__ __noinline__ double trilerp_slow(
+    double f000, double f100, double f010, double f110, double f001,
+    double f101, double f011, double f111, double fx, double fy, double fz) {
+    const double b0 = lerp_ref(lerp_ref(f000, f100, fx),
+                               lerp_ref(f010, f110, fx), fy);
+    const double b1 = lerp_ref(lerp_ref(f001, f101, fx),
+                               lerp_ref(f011, f111, fx), fy);
+    return lerp_ref(b0, b1, fz);
+}
+
 // trilerp for samples taken at grid-aligned points of the sampled grid
 // (faces, nodes, cell centres): when all three fractions are 0, 1/2 or 1 the
 // lerps take the integer-pipe shortcuts; any other sample runs the
@@ -240,11 +261,8 @@ __device__ __forceinline__ double trilerp_grid(
                                     lerp_fast(f011, f111, fx, bx), fy, by);
         return lerp_fast(b0, b1, fz, bz);
     }
-    const double b0 = lerp_ref(lerp_ref(f000, f100, fx),
-                               lerp_ref(f010, f110, fx), fy);
-    const double b1 = lerp_ref(lerp_ref(f001, f101, fx),
-                               lerp_ref(f011, f111, fx), fy);
-    return lerp_ref(b0, b1, fz);
+    return trilerp_slow(f000, f100, f010, f110, f001, f101, f011, f111, fx,
+                        fy, fz);
 }
 
 // Trilinear sample of a face array with the reference's operator() rule
