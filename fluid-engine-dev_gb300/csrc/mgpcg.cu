@@ -94,6 +94,13 @@ struct RowsF {
         return make_float4(__ldg(A + c), __ldg(A + N + c), __ldg(A + 2 * N + c),
                            __ldg(A + 3 * N + c));
     }
+    // Component p of cells c..c+3 (c and N multiples of 4).
+    __device__ __forceinline__ float4 quad(int p, long c) const {
+        return __ldg(reinterpret_cast<const float4*>(A + p * N + c));
+    }
+    __device__ __forceinline__ float one(int p, long c) const {
+        return __ldg(A + p * N + c);
+    }
 };
 // BF16 rows (mixed mode), same layout.
 __device__ __forceinline__ float bf_dec(unsigned short u) {
@@ -106,6 +113,16 @@ struct RowsB {
         return make_float4(bf_dec(__ldg(A + c)), bf_dec(__ldg(A + N + c)),
                            bf_dec(__ldg(A + 2 * N + c)),
                            bf_dec(__ldg(A + 3 * N + c)));
+    }
+    __device__ __forceinline__ float4 quad(int p, long c) const {
+        const uint2 w = __ldg(reinterpret_cast<const uint2*>(A + p * N + c));
+        return make_float4(__uint_as_float(w.x << 16),
+                           __uint_as_float(w.x & 0xffff0000u),
+                           __uint_as_float(w.y << 16),
+                           __uint_as_float(w.y & 0xffff0000u));
+    }
+    __device__ __forceinline__ float one(int p, long c) const {
+        return bf_dec(__ldg(A + p * N + c));
     }
 };
 struct RowsD {
@@ -131,6 +148,97 @@ __device__ __forceinline__ T apply7(const Rows& M, const V* __restrict__ v,
     if (k > 0) s += (T)M.row(c - sz).w * (T)v[c - sz];
     if (k + 1 < n.z) s += (T)r.w * (T)v[c + sz];
     return s;
+}
+
+__device__ __forceinline__ float4 ld4(const float* p) {
+    return *reinterpret_cast<const float4*>(p);
+}
+
+// apply7 for the four cells c..c+3 of a row (c and n.x multiples of 4) from
+// 16-byte loads: each cell's terms in apply7's order.
+template <typename R>
+__device__ __forceinline__ void apply7x4(const R& M,
+                                         const float* __restrict__ v, long c,
+                                         int i, int j, int k, Dims n,
+                                         float out[4]) {
+    const long sy = n.x, sz = (long)n.x * n.y;
+    const float4 cx = M.quad(0, c), cy = M.quad(1, c), cz = M.quad(2, c),
+                 cw = M.quad(3, c);
+    const float4 vc = ld4(v + c);
+    const bool hl = i > 0, hr = i + 4 < n.x, hd = j > 0, hu = j + 1 < n.y,
+               hb = k > 0, hf = k + 1 < n.z;
+    const float vl = hl ? v[c - 1] : 0.0f, yl = hl ? M.one(1, c - 1) : 0.0f;
+    const float vr = hr ? v[c + 4] : 0.0f;
+    const float4 z4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    const float4 vd = hd ? ld4(v + c - sy) : z4, zd = hd ? M.quad(2, c - sy) : z4;
+    const float4 vu = hu ? ld4(v + c + sy) : z4;
+    const float4 vb = hb ? ld4(v + c - sz) : z4, wb = hb ? M.quad(3, c - sz) : z4;
+    const float4 vf = hf ? ld4(v + c + sz) : z4;
+    const float V[6] = {vl, vc.x, vc.y, vc.z, vc.w, vr};
+    const float CX[4] = {cx.x, cx.y, cx.z, cx.w}, CY[4] = {cy.x, cy.y, cy.z, cy.w};
+    const float YL[4] = {yl, cy.x, cy.y, cy.z};
+    const float CZ[4] = {cz.x, cz.y, cz.z, cz.w}, ZD[4] = {zd.x, zd.y, zd.z, zd.w};
+    const float CW[4] = {cw.x, cw.y, cw.z, cw.w}, WB[4] = {wb.x, wb.y, wb.z, wb.w};
+    const float VD[4] = {vd.x, vd.y, vd.z, vd.w}, VU[4] = {vu.x, vu.y, vu.z, vu.w};
+    const float VB[4] = {vb.x, vb.y, vb.z, vb.w}, VF[4] = {vf.x, vf.y, vf.z, vf.w};
+#pragma unroll
+    for (int l = 0; l < 4; ++l) {
+        float s = CX[l] * V[l + 1];
+        if (l > 0 || hl) s += YL[l] * V[l];
+        if (l < 3 || hr) s += CY[l] * V[l + 2];
+        if (hd) s += ZD[l] * VD[l];
+        if (hu) s += CZ[l] * VU[l];
+        if (hb) s += WB[l] * VB[l];
+        if (hf) s += CW[l] * VF[l];
+        out[l] = s;
+    }
+}
+
+// k_residual32 over 4-cell groups (n.x a multiple of 4).
+template <typename R>
+__global__ void __launch_bounds__(kThreads)
+    k_residual32x4(R M, const float* __restrict__ x,
+                   const float* __restrict__ b, float* __restrict__ r, Dims n) {
+    const Dims q{n.x / 4, n.y, n.z};
+    const long G = q.count();
+    for (long t = blockIdx.x * (long)kThreads + threadIdx.x; t < G;
+         t += (long)gridDim.x * kThreads) {
+        int m, j, k;
+        cell_ijk(t, q, m, j, k);
+        const long c = lin(4 * m, j, k, n.x, n.y);
+        float ax[4];
+        apply7x4(M, x, c, 4 * m, j, k, n, ax);
+        const float4 bb = ld4(b + c);
+        *reinterpret_cast<float4*>(r + c) =
+            make_float4(bb.x - ax[0], bb.y - ax[1], bb.z - ax[2], bb.w - ax[3]);
+    }
+}
+
+// k_spmv_dot<float> over 4-cell groups (n.x a multiple of 4).
+template <typename R>
+__global__ void __launch_bounds__(kThreads)
+    k_spmv_dot4(R M, const float* __restrict__ d, float* __restrict__ q,
+                Dims n, double* partials, unsigned* counters, double* scal) {
+    __shared__ double smem[32];
+    const Dims g{n.x / 4, n.y, n.z};
+    const long G = g.count();
+    AccF acc;
+    for (long t = blockIdx.x * (long)kThreads + threadIdx.x; t < G;
+         t += (long)gridDim.x * kThreads) {
+        int m, j, k;
+        cell_ijk(t, g, m, j, k);
+        const long c = lin(4 * m, j, k, n.x, n.y);
+        float ad[4];
+        apply7x4(M, d, c, 4 * m, j, k, n, ad);
+        *reinterpret_cast<float4*>(q + c) = make_float4(ad[0], ad[1], ad[2], ad[3]);
+        const float4 dd = ld4(d + c);
+        acc.add(dd.x, ad[0]);
+        acc.add(dd.y, ad[1]);
+        acc.add(dd.z, ad[2]);
+        acc.add(dd.w, ad[3]);
+    }
+    reduce_finish<kThreads>(acc.value(), 0, S_DQ, FIN_ALPHA, partials,
+                            counters, scal, smem);
 }
 
 // K5: q = A d and d.q (FP64).
@@ -959,8 +1067,12 @@ float* vcycle_level(Ctx* c, unsigned l, const float* b, float* x, float* alt) {
     {
         Prof pr(c, K_RESIDUAL, (12.0 + row_bytes(c)) * L.n.count());
         with_rows(c, L, [&](auto M) {
-            k_residual32<<<grid_for(c, L.n.count()), kThreads, 0,
-                           c->stream>>>(M, cur, b, L.r, L.n);
+            if (L.n.x % 4 == 0)
+                k_residual32x4<<<grid_for(c, L.n.count() / 4), kThreads, 0,
+                                 c->stream>>>(M, cur, b, L.r, L.n);
+            else
+                k_residual32<<<grid_for(c, L.n.count()), kThreads, 0,
+                               c->stream>>>(M, cur, b, L.r, L.n);
         });
     }
     {
@@ -1046,6 +1158,19 @@ jetgpu_status init_kernels(Ctx* c) {
     return JETGPU_OK;
 }
 
+// q = A d and d.q on the FP32 Krylov vectors (kd -> kq).
+void spmv_f32(Ctx* c, const RowsF& M, Dims n) {
+    const long N = n.count();
+    if (n.x % 4 == 0)
+        k_spmv_dot4<RowsF><<<rgrid(c, k_spmv_dot4<RowsF>, N / 4), kThreads, 0,
+                             c->stream>>>(M, c->kd, c->kq, n, c->partials,
+                                          c->counters, c->scal);
+    else
+        k_spmv_dot<float, RowsF><<<rgrid(c, k_spmv_dot<float, RowsF>, N),
+                                   kThreads, 0, c->stream>>>(
+            M, c->kd, c->kq, n, c->partials, c->counters, c->scal);
+}
+
 // PCG on the FP32 rows for a correction e with A e = r (r = kr on entry).
 // Stops when ||r_k|| <= target or after max_it iterations.
 static jetgpu_status pcg_f32(Ctx* c, double target, unsigned max_it,
@@ -1078,9 +1203,7 @@ static jetgpu_status pcg_f32(Ctx* c, double target, unsigned max_it,
         }
         {
             Prof pr(c, K_SPMV, 24.0 * N);
-            k_spmv_dot<float, RowsF><<<rgrid(c, k_spmv_dot<float, RowsF>, N), kThreads, 0,
-            c->stream>>>(
-                M, c->kd, c->kq, n, c->partials, c->counters, c->scal);
+            spmv_f32(c, M, n);
         }
         {
             Prof pr(c, K_UPDATE_XR, 24.0 * N);
@@ -1249,9 +1372,7 @@ static jetgpu_status fpcg_f32(Ctx* c, double target, unsigned max_it,
         }
         {
             Prof pr(c, K_SPMV, 24.0 * N);
-            k_spmv_dot<float, RowsF><<<rgrid(c, k_spmv_dot<float, RowsF>, N), kThreads, 0,
-            c->stream>>>(
-                M, c->kd, c->kq, n, c->partials, c->counters, c->scal);
+            spmv_f32(c, M, n);
         }
         {
             Prof pr(c, K_UPDATE_XR, 24.0 * N);
@@ -1316,9 +1437,7 @@ jetgpu_status harvest_pairs(Ctx* c, unsigned max_pairs, float* r_out,
         k_update_d<float, float><<<rgrid(c, k_update_d<float, float>, N), kThreads, 0,
             c->stream>>>(c->kd, z, N,
                                                                 c->scal);
-        k_spmv_dot<float, RowsF><<<rgrid(c, k_spmv_dot<float, RowsF>, N), kThreads, 0,
-            c->stream>>>(
-            M, c->kd, c->kq, n, c->partials, c->counters, c->scal);
+        spmv_f32(c, M, n);
         k_update_xr<float><<<rgrid(c, k_update_xr<float>, N), kThreads, 0,
             c->stream>>>(
             c->kx, c->kr, c->kd, c->kq, nullptr, N, c->partials, c->counters,
