@@ -283,6 +283,79 @@ __global__ void __launch_bounds__(kThreads)
                             counters, scal, smem);
 }
 
+// k_update_xr<float> and k_dot_rz<float, float> over 4-element groups
+// (N a multiple of 4): 16-byte accesses, the same reductions.
+__global__ void __launch_bounds__(kThreads)
+    k_update_xr4(float* __restrict__ x, float* __restrict__ r,
+                 const float* __restrict__ d, const float* __restrict__ q,
+                 long N, double* partials, unsigned* counters, double* scal) {
+    __shared__ double smem[32];
+    const float alpha = (float)scal[S_ALPHA];
+    AccF acc;
+    const long G = N / 4;
+    for (long t = blockIdx.x * (long)kThreads + threadIdx.x; t < G;
+         t += (long)gridDim.x * kThreads) {
+        float4 xv = reinterpret_cast<float4*>(x)[t];
+        float4 rv = reinterpret_cast<float4*>(r)[t];
+        const float4 dv = reinterpret_cast<const float4*>(d)[t];
+        const float4 qv = reinterpret_cast<const float4*>(q)[t];
+        xv.x += alpha * dv.x;
+        xv.y += alpha * dv.y;
+        xv.z += alpha * dv.z;
+        xv.w += alpha * dv.w;
+        rv.x = rv.x - alpha * qv.x;
+        rv.y = rv.y - alpha * qv.y;
+        rv.z = rv.z - alpha * qv.z;
+        rv.w = rv.w - alpha * qv.w;
+        reinterpret_cast<float4*>(x)[t] = xv;
+        reinterpret_cast<float4*>(r)[t] = rv;
+        acc.add(rv.x, rv.x);
+        acc.add(rv.y, rv.y);
+        acc.add(rv.z, rv.z);
+        acc.add(rv.w, rv.w);
+    }
+    reduce_finish<kThreads>(acc.value(), 1, S_RR, FIN_NONE, partials,
+                            counters, scal, smem);
+}
+
+__global__ void __launch_bounds__(kThreads)
+    k_dot_rz4(const float* __restrict__ r, const float* __restrict__ z,
+              long N, double* partials, unsigned* counters, double* scal) {
+    __shared__ double smem[32];
+    AccF acc;
+    const long G = N / 4;
+    for (long t = blockIdx.x * (long)kThreads + threadIdx.x; t < G;
+         t += (long)gridDim.x * kThreads) {
+        const float4 rv = reinterpret_cast<const float4*>(r)[t];
+        const float4 zv = reinterpret_cast<const float4*>(z)[t];
+        acc.add(rv.x, zv.x);
+        acc.add(rv.y, zv.y);
+        acc.add(rv.z, zv.z);
+        acc.add(rv.w, zv.w);
+    }
+    reduce_finish<kThreads>(acc.value(), 2, S_RZ, FIN_BETA, partials,
+                            counters, scal, smem);
+}
+
+__global__ void __launch_bounds__(kThreads)
+    k_update_d4(float* __restrict__ d, const float* __restrict__ z, long N,
+                const double* scal) {
+    const float beta = (float)scal[S_BETA];
+    const long G = N / 4;
+    for (long t = blockIdx.x * (long)kThreads + threadIdx.x; t < G;
+         t += (long)gridDim.x * kThreads) {
+        const float4 zv = reinterpret_cast<const float4*>(z)[t];
+        if (beta == 0.0f) {
+            reinterpret_cast<float4*>(d)[t] = zv;
+        } else {
+            const float4 dv = reinterpret_cast<const float4*>(d)[t];
+            reinterpret_cast<float4*>(d)[t] =
+                make_float4(zv.x + beta * dv.x, zv.y + beta * dv.y,
+                            zv.z + beta * dv.z, zv.w + beta * dv.w);
+        }
+    }
+}
+
 // K7b: r.z (FP64), finishing beta.
 template <typename V, typename Z>
 __global__ void __launch_bounds__(kThreads)
@@ -1191,15 +1264,24 @@ static jetgpu_status pcg_f32(Ctx* c, double target, unsigned max_it,
         }
         {
             Prof pr(c, K_DOT_RZ, 8.0 * N);
-            k_dot_rz<float, float><<<rgrid(c, k_dot_rz<float, float>, N), kThreads, 0,
-            c->stream>>>(
-                c->kr, z, N, c->partials, c->counters, c->scal);
+            if (N % 4 == 0)
+                k_dot_rz4<<<rgrid(c, k_dot_rz4, N / 4), kThreads, 0,
+                            c->stream>>>(c->kr, z, N, c->partials,
+                                         c->counters, c->scal);
+            else
+                k_dot_rz<float, float><<<rgrid(c, k_dot_rz<float, float>, N),
+                                         kThreads, 0, c->stream>>>(
+                    c->kr, z, N, c->partials, c->counters, c->scal);
         }
         {
             Prof pr(c, K_UPDATE_D, 12.0 * N);
-            k_update_d<float, float><<<rgrid(c, k_update_d<float, float>, N), kThreads, 0,
-            c->stream>>>(c->kd, z,
-                                                                    N, c->scal);
+            if (N % 4 == 0)
+                k_update_d4<<<rgrid(c, k_update_d4, N / 4), kThreads, 0,
+                              c->stream>>>(c->kd, z, N, c->scal);
+            else
+                k_update_d<float, float><<<rgrid(c, k_update_d<float, float>, N),
+                                           kThreads, 0, c->stream>>>(
+                    c->kd, z, N, c->scal);
         }
         {
             Prof pr(c, K_SPMV, 24.0 * N);
@@ -1207,10 +1289,16 @@ static jetgpu_status pcg_f32(Ctx* c, double target, unsigned max_it,
         }
         {
             Prof pr(c, K_UPDATE_XR, 24.0 * N);
-            k_update_xr<float><<<rgrid(c, k_update_xr<float>, N), kThreads, 0,
-            c->stream>>>(
-                c->kx, c->kr, c->kd, c->kq, nullptr, N, c->partials,
-                c->counters, c->scal);
+            if (N % 4 == 0)
+                k_update_xr4<<<rgrid(c, k_update_xr4, N / 4), kThreads, 0,
+                               c->stream>>>(c->kx, c->kr, c->kd, c->kq, N,
+                                            c->partials, c->counters,
+                                            c->scal);
+            else
+                k_update_xr<float><<<rgrid(c, k_update_xr<float>, N),
+                                     kThreads, 0, c->stream>>>(
+                    c->kx, c->kr, c->kd, c->kq, nullptr, N, c->partials,
+                    c->counters, c->scal);
         }
         ++it;
         jetgpu_status s = read_scalars(c);
