@@ -466,6 +466,90 @@ __global__ void __launch_bounds__(kThreads)
                             counters, scal, smem);
 }
 
+// k_residual_df over 4-cell groups (n.x a multiple of 4): each cell's terms
+// in k_residual_df's order, from 16-byte loads of the row components and of
+// the double-float iterate and rhs; the low parts of the neighbours' rows are
+// read as single components.
+__global__ void __launch_bounds__(kThreads)
+    k_residual_df4(RowsF Ahi, const float4* __restrict__ Alo,
+                   const float2* __restrict__ x, const float2* __restrict__ b,
+                   float* __restrict__ r32, float* __restrict__ zero32, Dims n,
+                   double* partials, unsigned* counters, double* scal,
+                   int target) {
+    __shared__ double smem[32];
+    const Dims g{n.x / 4, n.y, n.z};
+    const long G = g.count();
+    const long sy = n.x, sz = (long)n.x * n.y;
+    const float* lo = reinterpret_cast<const float*>(Alo);
+    AccF acc;
+    for (long t = blockIdx.x * (long)kThreads + threadIdx.x; t < G;
+         t += (long)gridDim.x * kThreads) {
+        int m, j, k;
+        cell_ijk(t, g, m, j, k);
+        const int i = 4 * m;
+        const long c = lin(i, j, k, n.x, n.y);
+        const float4 hx = Ahi.quad(0, c), hy = Ahi.quad(1, c),
+                     hz = Ahi.quad(2, c), hw = Ahi.quad(3, c);
+        const float HX[4] = {hx.x, hx.y, hx.z, hx.w};
+        const float HY[4] = {hy.x, hy.y, hy.z, hy.w};
+        const float HZ[4] = {hz.x, hz.y, hz.z, hz.w};
+        const float HW[4] = {hw.x, hw.y, hw.z, hw.w};
+        const bool hl = i > 0, hr = i + 4 < n.x, hd = j > 0, hu = j + 1 < n.y,
+                   hb = k > 0, hf = k + 1 < n.z;
+        float4 zd = make_float4(0.f, 0.f, 0.f, 0.f), wb = zd;
+        if (hd) zd = Ahi.quad(2, c - sy);
+        if (hb) wb = Ahi.quad(3, c - sz);
+        const float ZD[4] = {zd.x, zd.y, zd.z, zd.w};
+        const float WB[4] = {wb.x, wb.y, wb.z, wb.w};
+        const float yl = hl ? Ahi.one(1, c - 1) : 0.0f;
+        const float yll = hl ? lo[4 * (c - 1) + 1] : 0.0f;
+        float rv[4];
+#pragma unroll
+        for (int l = 0; l < 4; ++l) {
+            const long cc = c + l;
+            const float4 L = Alo[cc];
+            const float2 xc = x[cc], bc = b[cc];
+            DF r;
+            r.hi = bc.x;
+            r.lo = bc.y;
+            r = df_sub_prod(r, HX[l], L.x, xc.x, xc.y);
+            if (l > 0 || hl) {
+                const float2 xn = x[cc - 1];
+                const float nh = l > 0 ? HY[l - 1] : yl;
+                const float nl = l > 0 ? lo[4 * (cc - 1) + 1] : yll;
+                r = df_sub_prod(r, nh, nl, xn.x, xn.y);
+            }
+            if (l < 3 || hr) {
+                const float2 xn = x[cc + 1];
+                r = df_sub_prod(r, HY[l], L.y, xn.x, xn.y);
+            }
+            if (hd) {
+                const float2 xn = x[cc - sy];
+                r = df_sub_prod(r, ZD[l], lo[4 * (cc - sy) + 2], xn.x, xn.y);
+            }
+            if (hu) {
+                const float2 xn = x[cc + sy];
+                r = df_sub_prod(r, HZ[l], L.z, xn.x, xn.y);
+            }
+            if (hb) {
+                const float2 xn = x[cc - sz];
+                r = df_sub_prod(r, WB[l], lo[4 * (cc - sz) + 3], xn.x, xn.y);
+            }
+            if (hf) {
+                const float2 xn = x[cc + sz];
+                r = df_sub_prod(r, HW[l], L.w, xn.x, xn.y);
+            }
+            rv[l] = __fadd_rn(r.hi, r.lo);
+        }
+        *reinterpret_cast<float4*>(r32 + c) = make_float4(rv[0], rv[1], rv[2], rv[3]);
+        *reinterpret_cast<float4*>(zero32 + c) = make_float4(0.f, 0.f, 0.f, 0.f);
+#pragma unroll
+        for (int l = 0; l < 4; ++l) acc.add(rv[l], rv[l]);
+    }
+    reduce_finish<kThreads>(acc.value(), 3, target, FIN_NONE, partials,
+                            counters, scal, smem);
+}
+
 // Start of the FP32-mode solve from x = 0: r = b (its FP32 image is b's hi
 // part, the FP32 rounding of b), correction and iterate zeroed, ||b||^2 from
 // the double-float b into scal[S_B64].
@@ -1603,11 +1687,16 @@ jetgpu_status mgpcg_solve(Ctx* c, jetgpu_solve_stats* st) {
                 c->counters, c->scal, S_R64);
         } else {
             Prof pr(c, K_RESIDUAL64, 56.0 * N);
-            k_residual_df<<<rgrid(c, k_residual_df, N), kThreads, 0,
-            c->stream>>>(
-                RowsF{L0.A, N}, c->Alo, c->xdf, c->bdf, r32, zero32, n,
-                c->partials,
-                c->counters, c->scal, S_R64);
+            if (n.x % 4 == 0)
+                k_residual_df4<<<rgrid(c, k_residual_df4, N / 4), kThreads, 0,
+                                 c->stream>>>(
+                    RowsF{L0.A, N}, c->Alo, c->xdf, c->bdf, r32, zero32, n,
+                    c->partials, c->counters, c->scal, S_R64);
+            else
+                k_residual_df<<<rgrid(c, k_residual_df, N), kThreads, 0,
+                                c->stream>>>(
+                    RowsF{L0.A, N}, c->Alo, c->xdf, c->bdf, r32, zero32, n,
+                    c->partials, c->counters, c->scal, S_R64);
         }
         JG_CUDA(c, cudaGetLastError());
         jetgpu_status rs = read_scalars(c);
