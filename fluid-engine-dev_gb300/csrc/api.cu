@@ -254,12 +254,25 @@ jetgpu_status solve_pressure_dev(
     s = blocked ? blocked_markers(c, g, to_desc(bsdf, bdata), to_desc(fsdf, fdata))
                 : build_weights(c, g, to_desc(bsdf, bdata), to_desc(fsdf, fdata));
     if (s != JETGPU_OK) return s;
-    if (io) JG_CUDA(c, cudaStreamWaitEvent(c->stream, io->vel_in, 0));
-    s = blocked ? blocked_system(c, g, u, v, w)
-                : build_system(c, g, u, v, w, su, sv, sw);
-    if (s != JETGPU_OK) return s;
-    s = prepare_levels(c);
-    if (s != JETGPU_OK) return s;
+    if (io && !blocked) {
+        // The coarse levels' rows need only the weights: built while the
+        // velocities are still uploading, level 0 (which reads them) after.
+        if ((s = build_system(c, g, nullptr, nullptr, nullptr, nullptr,
+                              nullptr, nullptr, 1)) != JETGPU_OK)
+            return s;
+        if ((s = prepare_levels(c, 1)) != JETGPU_OK) return s;
+        JG_CUDA(c, cudaStreamWaitEvent(c->stream, io->vel_in, 0));
+        if ((s = build_system(c, g, u, v, w, su, sv, sw, 0, 1)) != JETGPU_OK)
+            return s;
+        if ((s = prepare_levels(c, 0, 1)) != JETGPU_OK) return s;
+    } else {
+        if (io) JG_CUDA(c, cudaStreamWaitEvent(c->stream, io->vel_in, 0));
+        s = blocked ? blocked_system(c, g, u, v, w)
+                    : build_system(c, g, u, v, w, su, sv, sw);
+        if (s != JETGPU_OK) return s;
+        s = prepare_levels(c);
+        if (s != JETGPU_OK) return s;
+    }
     JG_CUDA(c, cudaStreamSynchronize(c->stream));
     const double setup = ms_since(t0);
     auto t1 = std::chrono::steady_clock::now();

@@ -1092,9 +1092,9 @@ SpacingInv spacing_inv(double hx, double hy, double hz) {
 jetgpu_status build_system(Ctx* c, const GridDesc& g, const double* u,
                            const double* v, const double* w,
                            const double* su, const double* sv,
-                           const double* sw) {
+                           const double* sw, unsigned lo, unsigned hi) {
     double hx = g.spacing[0], hy = g.spacing[1], hz = g.spacing[2];
-    for (unsigned l = 0; l < c->built_levels; ++l) {
+    for (unsigned l = 0; l < c->built_levels && l < hi; ++l) {
         Level& L = c->levels[l];
         if (l > 0) {
             hx *= 2.0;
@@ -1104,6 +1104,7 @@ jetgpu_status build_system(Ctx* c, const GridDesc& g, const double* u,
         L.h[0] = hx;
         L.h[1] = hy;
         L.h[2] = hz;
+        if (l < lo) continue;
         const bool top = (l == 0);
         Prof pr(c, K_SYSTEM, (top ? 16.0 + 32.0 + 8.0 + 24.0 : 16.0 + 16.0) *
                                 (double)L.n.count());

@@ -245,10 +245,12 @@ inline int red_blocks(const Ctx* c, long n) {
 // ---- build.cu -------------------------------------------------------------
 jetgpu_status build_weights(Ctx* c, const GridDesc& g, const FieldDesc& bsdf,
                             const FieldDesc& fsdf);
+// Levels [lo, hi) of the hierarchy; only level 0 reads the velocities.
 jetgpu_status build_system(Ctx* c, const GridDesc& g, const double* u,
                            const double* v, const double* w,
                            const double* su, const double* sv,
-                           const double* sw);
+                           const double* sw, unsigned lo = 0,
+                           unsigned hi = ~0u);
 // Low parts of a caller-built finest-level system (jetgpu_mgpcg_solve_system).
 jetgpu_status split_system(Ctx* c);
 jetgpu_status apply_gradient(Ctx* c, const GridDesc& g, const double* u,
@@ -270,8 +272,8 @@ jetgpu_status blocked_gradient(Ctx* c, const GridDesc& g, const double* u,
 // ---- mgpcg.cu -------------------------------------------------------------
 // Allocates the multigrid hierarchy and solver buffers for resolution n.
 jetgpu_status ensure_buffers(Ctx* c, Dims n, unsigned max_levels);
-// Derives FP32 (and BF16) matrices of every level from the built system.
-jetgpu_status prepare_levels(Ctx* c);
+// Derives FP32 (and BF16) matrices of levels [lo, hi) from the built system.
+jetgpu_status prepare_levels(Ctx* c, unsigned lo = 0, unsigned hi = ~0u);
 // Solves A64 x64 = b64 on the finest level; fills stats.
 jetgpu_status mgpcg_solve(Ctx* c, jetgpu_solve_stats* st);
 // Computes level count for resolution n (FdmMgUtils3::resizeArrayWithFinest).

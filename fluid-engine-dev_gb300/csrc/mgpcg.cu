@@ -1293,9 +1293,9 @@ jetgpu_status vcycle(Ctx* c, const float* r, float* z, float* alt,
     return JETGPU_OK;
 }
 
-jetgpu_status prepare_levels(Ctx* c) {
+jetgpu_status prepare_levels(Ctx* c, unsigned lo, unsigned hi) {
     if (!mixed(c)) return JETGPU_OK;
-    for (unsigned l = 0; l < c->built_levels; ++l) {
+    for (unsigned l = lo; l < c->built_levels && l < hi; ++l) {
         const Level& L = c->levels[l];
         const long N = L.n.count();
         Prof pr(c, K_SYSTEM, 24.0 * N);
