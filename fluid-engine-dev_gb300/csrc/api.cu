@@ -41,6 +41,10 @@ void release(T** p) {
 }
 
 void free_buffers(Ctx* c) {
+    if (c->vc_exec) {
+        cudaGraphExecDestroy(c->vc_exec);
+        c->vc_exec = nullptr;
+    }
     for (Level& L : c->levels) {
         release(&L.phi);
         release(&L.uw);

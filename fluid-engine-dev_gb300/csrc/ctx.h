@@ -174,6 +174,18 @@ struct Ctx {
     double* sdf_dbl = nullptr;
     unsigned char* sdf_valid = nullptr;
 
+    // The FP32 PCG's V-cycle captured as a CUDA graph (mgpcg.cu,
+    // vcycle_graph), with what it was captured for: its vectors, the level
+    // count and the smoother settings. Destroyed with the buffers.
+    cudaGraphExec_t vc_exec = nullptr;
+    const void* vc_key[3] = {nullptr, nullptr, nullptr};
+    unsigned vc_levels = 0;
+    unsigned vc_iters[4] = {0, 0, 0, 0};
+    double vc_sor = 0.0;
+    int vc_precision = -1;
+    float* vc_result = nullptr;
+    bool vc_disabled = false;
+
     // Blocked pressure solver (blocked.cu): cell markers of every level,
     // finest first.
     size_t blk_cap = 0;

@@ -1315,6 +1315,68 @@ jetgpu_status init_kernels(Ctx* c) {
     return JETGPU_OK;
 }
 
+// The V-cycle as one CUDA graph. A V-cycle is about 50 launches, most of
+// them on the small coarse levels, where launch latency rather than memory
+// bounds the time; replaying a captured graph removes the per-launch host
+// work and shortens the gaps between the kernels. The graph is captured on
+// first use and again whenever the vectors, the level count or the smoother
+// settings differ from the captured ones (the buffers' reallocation destroys
+// it). Launches bracketed by the live profile, and any failure to capture,
+// take the direct path.
+jetgpu_status vcycle_graph(Ctx* c, const float* r, float* z, float* alt,
+                           float** result) {
+    if (c->prof_on || c->vc_disabled) return vcycle(c, r, z, alt, result);
+    const jetgpu_config& f = c->cfg;
+    const bool same =
+        c->vc_exec && c->vc_key[0] == r && c->vc_key[1] == z &&
+        c->vc_key[2] == alt && c->vc_levels == c->built_levels &&
+        c->vc_iters[0] == f.restrict_iter && c->vc_iters[1] == f.correct_iter &&
+        c->vc_iters[2] == f.coarsest_iter && c->vc_iters[3] == f.final_iter &&
+        c->vc_sor == f.sor && c->vc_precision == f.precision;
+    if (!same) {
+        if (c->vc_exec) {
+            cudaGraphExecDestroy(c->vc_exec);
+            c->vc_exec = nullptr;
+        }
+        auto give_up = [&]() {
+            c->vc_disabled = true;
+            cudaGetLastError();
+            return vcycle(c, r, z, alt, result);
+        };
+        if (cudaStreamBeginCapture(c->stream,
+                                   cudaStreamCaptureModeThreadLocal) !=
+            cudaSuccess)
+            return give_up();
+        float* res = vcycle_level(c, 0, r, z, alt);
+        cudaGraph_t graph = nullptr;
+        const cudaError_t e = cudaStreamEndCapture(c->stream, &graph);
+        if (e != cudaSuccess || graph == nullptr) {
+            if (graph) cudaGraphDestroy(graph);
+            return give_up();
+        }
+        const cudaError_t ei = cudaGraphInstantiate(&c->vc_exec, graph, 0);
+        cudaGraphDestroy(graph);
+        if (ei != cudaSuccess) {
+            c->vc_exec = nullptr;
+            return give_up();
+        }
+        c->vc_key[0] = r;
+        c->vc_key[1] = z;
+        c->vc_key[2] = alt;
+        c->vc_levels = c->built_levels;
+        c->vc_iters[0] = f.restrict_iter;
+        c->vc_iters[1] = f.correct_iter;
+        c->vc_iters[2] = f.coarsest_iter;
+        c->vc_iters[3] = f.final_iter;
+        c->vc_sor = f.sor;
+        c->vc_precision = f.precision;
+        c->vc_result = res;
+    }
+    JG_CUDA(c, cudaGraphLaunch(c->vc_exec, c->stream));
+    *result = c->vc_result;
+    return JETGPU_OK;
+}
+
 // q = A d and d.q on the FP32 Krylov vectors (kd -> kq).
 void spmv_f32(Ctx* c, const RowsF& M, Dims n) {
     const long N = n.count();
@@ -1343,7 +1405,7 @@ static jetgpu_status pcg_f32(Ctx* c, double target, unsigned max_it,
         float* z = nullptr;
         if (c->cfg.preconditioner == JETGPU_PRECOND_NONE) {
             z = c->kr;  // plain CG: z = r
-        } else if (jetgpu_status vs = vcycle(c, c->kr, c->kz, L0.x2, &z)) {
+        } else if (jetgpu_status vs = vcycle_graph(c, c->kr, c->kz, L0.x2, &z)) {
             return vs;
         }
         {
