@@ -67,6 +67,9 @@ def parse_args():
                     help="skip the blocked pressure solver leg")
     ap.add_argument("--no-smoke", action="store_true",
                     help="skip the 512^3 smoke-plume projection")
+    ap.add_argument("--no-accuracy", action="store_true",
+                    help="skip the accuracy block (pressure rel-L2 and "
+                         "divergence against an FP64 answer)")
     ap.add_argument("--variants", default=",".join(VARIANTS),
                     help="comma-separated solver variants to run "
                          "(plain_mgpcg, mixed_mgpcg, learned_fpcg)")
@@ -396,6 +399,98 @@ def run_ours(args, rank, world, local, pg):
                 peak=pk, head=head, variants=variants)
 
 
+def residual_rows(A, x, b):
+    """||b - A x|| / ||b|| for 7-point rows {center, right, up, front}
+    ((nz,ny,nx,4) float64; the lower neighbours' couplings are the right/up/
+    front entries of the cell before), in numpy."""
+    import numpy as np
+    r = b - A[..., 0] * x
+    r[:, :, :-1] -= A[:, :, :-1, 1] * x[:, :, 1:]
+    r[:, :, 1:] -= A[:, :, :-1, 1] * x[:, :, :-1]
+    r[:, :-1, :] -= A[:, :-1, :, 2] * x[:, 1:, :]
+    r[:, 1:, :] -= A[:, :-1, :, 2] * x[:, :-1, :]
+    r[:-1] -= A[:-1, :, :, 3] * x[1:]
+    r[1:] -= A[:-1, :, :, 3] * x[:-1]
+    return float(np.linalg.norm(r) / np.linalg.norm(b))
+
+
+def run_accuracy(args, local, names):
+    """Per workload and solver variant, the error against an FP64 answer:
+    the same projection in the FP64 mode solved to a relative true residual
+    below 1e-12 (its residual recomputed here in numpy over the FP64 rows),
+    then each variant at the 1e-6 tolerance: relative L2 of the pressure and
+    the maximum over fluid cells of the cell-centre divergence
+    (FaceCenteredGrid3::divergenceAtCellCenter) of the projected velocity,
+    beside the FP64 answer's and their largest cell-wise difference. Host-
+    pointer solves through the public API; not timed."""
+    import numpy as np
+    import jetgpu
+    from jetgpu import scenes
+
+    def div(u, v, w, h):
+        return ((u[:, :, 1:] - u[:, :, :-1]) / h + (v[:, 1:, :] - v[:, :-1, :]) / h
+                + (w[1:] - w[:-1]) / h)
+
+    def solve(n, sc, prec, pre, tol, iters=200, refs=8):
+        h = 1.0 / n
+        prm = solver_params(prec, pre)
+        prm.update(maxTolerance=tol, numberOfCgIter=iters, maxRefinements=refs)
+        s = jetgpu.FdmMgpcgSolver3(**prm, device=local)
+        if pre == "learned":
+            from jetgpu import learned
+            if not os.path.exists(learned.WEIGHTS):
+                s.close()
+                return None
+            s.load_network(learned.flatten(learned.load()))
+        ps = jetgpu.GridFractionalSinglePhasePressureSolver3(s)
+        vel = jetgpu.FaceCenteredGrid3((n,) * 3, (h,) * 3, (0, 0, 0),
+                                       sc["u"], sc["v"], sc["w"])
+        out = vel.clone()
+        g = lambda d: jetgpu.CellCenteredScalarGrid3((n,) * 3, (h,) * 3,
+                                                     (0, 0, 0), d)
+        ps.solve(vel, 1 / 60, out, g(sc["boundary_sdf"]), None,
+                 g(sc["fluid_sdf"]))
+        return ps, out
+
+    result = {}
+    work = [("headline_%d" % args.n, args.n, workload(args.n),
+             [(k, VARIANTS[k]) for k in names]),
+            ("sphere_union_128", 128, scenes.sphere_union_scene(128, seed=1),
+             [("fp32", ("fp32", "multigrid")), ("fp64", ("fp64", "multigrid")),
+              ("mixed", ("mixed", "multigrid"))])]
+    for tag, n, sc, variants in work:
+        ps64, out64 = solve(n, sc, "fp64", "multigrid", 1e-12, iters=400,
+                            refs=20)
+        p64 = ps64.pressure().copy()
+        A = ps64.level(0, "A").reshape(n, n, n, 4)
+        b = ps64.level(0, "b").reshape(n, n, n)
+        fluid = ps64.level(0, "fluid").reshape(n, n, n) < 0
+        d64 = div(out64.u, out64.v, out64.w, 1.0 / n)
+        entry = {"fp64_answer": {
+            "relative_residual": ps64.last_stats.relative_residual,
+            "relative_residual_rechecked": residual_rows(A, p64, b),
+            "iterations": ps64.last_stats.iterations,
+            "max_div": float(np.abs(d64[fluid]).max())}}
+        ps64.linearSystemSolver.close()
+        for name, (prec, pre) in variants:
+            r = solve(n, sc, prec, pre, TOL)
+            if r is None:
+                entry[name] = {"status": "skipped: no trained weights"}
+                continue
+            ps, out = r
+            d = div(out.u, out.v, out.w, 1.0 / n)
+            p = ps.pressure()
+            entry[name] = {
+                "p_rel_l2": float(np.linalg.norm(p - p64) / np.linalg.norm(p64)),
+                "max_div": float(np.abs(d[fluid]).max()),
+                "max_div_diff": float(np.abs(d - d64)[fluid].max()),
+                "relative_residual": ps.last_stats.relative_residual,
+                "iterations": ps.last_stats.iterations}
+            ps.linearSystemSolver.close()
+        result[tag] = entry
+    return result
+
+
 def run_flip(args, local, variant: str, frames: int):
     """Whole FLIP frames on the GPU (jetgpu_flip_substep_device under the
     reference's adaptive sub-stepping): the 256^3 dam break with the static
@@ -706,6 +801,9 @@ def main():
             print(json.dumps(line), flush=True)
         return
     r = run_ours(args, rank, world, local, pg)
+    accuracy = None
+    if not args.no_accuracy and rank == 0:
+        accuracy = run_accuracy(args, local, r["variants"].keys())
     flip = None
     if not args.no_flip:
         flip = run_flip(args, local, r["head"], frames=3)
@@ -761,6 +859,8 @@ def main():
                      "ms": round(k["total_ms"], 3)} for k in
                     sorted(r["profile"], key=lambda k: -k["total_ms"])],
     }
+    if accuracy is not None:
+        line["accuracy"] = accuracy
     if flip is not None:
         line["flip_steps"] = flip
     if smoke is not None:

@@ -40,11 +40,17 @@ void release(T** p) {
     *p = nullptr;
 }
 
+// Frees the multigrid hierarchy. The captured V-cycle graph (vc_exec) bakes
+// in the level buffers' addresses and the TMA tensor maps made from them, so
+// it is destroyed here, and every path that reallocates level buffers must
+// come through this function. A capture that failed on the old buffers is
+// allowed again on the new ones.
 void free_buffers(Ctx* c) {
     if (c->vc_exec) {
         cudaGraphExecDestroy(c->vc_exec);
         c->vc_exec = nullptr;
     }
+    c->vc_disabled = false;
     for (Level& L : c->levels) {
         release(&L.phi);
         release(&L.uw);
@@ -196,6 +202,9 @@ jetgpu_status grow_stage(Ctx* c, size_t bytes) {
 
 }  // namespace
 
+// (Re)allocates the hierarchy for resolution n. Reallocation goes through
+// free_buffers, which also drops the captured V-cycle graph built on the old
+// buffers.
 jetgpu_status ensure_buffers(Ctx* c, Dims n, unsigned max_levels) {
     const unsigned nl = level_count(n, max_levels);
     if (c->n0.x == n.x && c->n0.y == n.y && c->n0.z == n.z &&
@@ -451,7 +460,8 @@ static jetgpu_status solve_device(
     const jetgpu_scalar_field* fluid_sdf, const double* solid_u,
     const double* solid_v, const double* solid_w, double* out_u,
     double* out_v, double* out_w, double* out_pressure,
-    jetgpu_solve_stats* stats, bool blocked) {
+    jetgpu_solve_stats* stats, bool blocked,
+    const jetgpu_collider* collider = nullptr) {
     if (!c) return JETGPU_BAD_INPUT;
     jetgpu_status s = check_grid(c, grid);
     if (s != JETGPU_OK) return s;
@@ -499,7 +509,8 @@ static jetgpu_status solve_host(
     const jetgpu_scalar_field* fluid_sdf, const double* solid_u,
     const double* solid_v, const double* solid_w, double* out_u,
     double* out_v, double* out_w, double* out_pressure,
-    jetgpu_solve_stats* stats, bool blocked) {
+    jetgpu_solve_stats* stats, bool blocked,
+    const jetgpu_collider* collider = nullptr) {
     if (!c) return JETGPU_BAD_INPUT;
     auto t0 = std::chrono::steady_clock::now();
     jetgpu_status s = check_grid(c, grid);
@@ -513,7 +524,13 @@ static jetgpu_status solve_host(
     const size_t nu = (size_t)(nx + 1) * ny * nz, nv = (size_t)nx * (ny + 1) * nz,
                  nw = (size_t)nx * ny * (nz + 1);
     const size_t nb = field_count(boundary_sdf), nf = field_count(fluid_sdf);
-    const size_t ns = (solid_u ? nu : 0) + (solid_v ? nv : 0) + (solid_w ? nw : 0);
+    // A moving rigid collider's face velocities are evaluated on the device
+    // into the solid part of the staging area (no host arrays).
+    const bool col_faces = collider_moves(collider);
+    if (col_faces) solid_u = solid_v = solid_w = nullptr;
+    const size_t ns = col_faces ? nu + nv + nw
+                                : (solid_u ? nu : 0) + (solid_v ? nv : 0) +
+                                      (solid_w ? nw : 0);
     // Device staging: inputs u,v,w | solid | sdf data | outputs u,v,w (the
     // pressure is downloaded from the solver's own buffer).
     const size_t total = 2 * (nu + nv + nw) + ns + nb + nf;
@@ -524,12 +541,12 @@ static jetgpu_status solve_host(
     double* dv = du + nu;
     double* dw = dv + nv;
     double* p = dw + nw;
-    double* dsu = solid_u ? p : nullptr;
-    p += solid_u ? nu : 0;
-    double* dsv = solid_v ? p : nullptr;
-    p += solid_v ? nv : 0;
-    double* dsw = solid_w ? p : nullptr;
-    p += solid_w ? nw : 0;
+    double* dsu = (solid_u || col_faces) ? p : nullptr;
+    p += dsu ? nu : 0;
+    double* dsv = (solid_v || col_faces) ? p : nullptr;
+    p += dsv ? nv : 0;
+    double* dsw = (solid_w || col_faces) ? p : nullptr;
+    p += dsw ? nw : 0;
     double* db = nb ? p : nullptr;
     p += nb;
     double* df = nf ? p : nullptr;
@@ -560,10 +577,20 @@ static jetgpu_status solve_host(
     JG_CUDA(c, cudaMemcpyAsync(du, u, nu * 8, cudaMemcpyHostToDevice, cs));
     JG_CUDA(c, cudaMemcpyAsync(dv, v, nv * 8, cudaMemcpyHostToDevice, cs));
     JG_CUDA(c, cudaMemcpyAsync(dw, w, nw * 8, cudaMemcpyHostToDevice, cs));
-    if (dsu) JG_CUDA(c, cudaMemcpyAsync(dsu, solid_u, nu * 8, cudaMemcpyHostToDevice, cs));
-    if (dsv) JG_CUDA(c, cudaMemcpyAsync(dsv, solid_v, nv * 8, cudaMemcpyHostToDevice, cs));
-    if (dsw) JG_CUDA(c, cudaMemcpyAsync(dsw, solid_w, nw * 8, cudaMemcpyHostToDevice, cs));
+    if (solid_u) JG_CUDA(c, cudaMemcpyAsync(dsu, solid_u, nu * 8, cudaMemcpyHostToDevice, cs));
+    if (solid_v) JG_CUDA(c, cudaMemcpyAsync(dsv, solid_v, nv * 8, cudaMemcpyHostToDevice, cs));
+    if (solid_w) JG_CUDA(c, cudaMemcpyAsync(dsw, solid_w, nw * 8, cudaMemcpyHostToDevice, cs));
     JG_CUDA(c, cudaEventRecord(io.vel_in, cs));
+    if (col_faces) {
+        GridDesc gd;
+        for (int a = 0; a < 3; ++a) {
+            gd.res[a] = grid->res[a];
+            gd.spacing[a] = grid->spacing[a];
+            gd.origin[a] = grid->origin[a];
+        }
+        if ((s = solid_face_velocities(c, gd, *collider, dsu)) != JETGPU_OK)
+            return s;
+    }
     jetgpu_solve_stats local;
     std::memset(&local, 0, sizeof(local));
     jetgpu_status solve_status = solve_pressure_dev(
@@ -593,6 +620,17 @@ jetgpu_status jetgpu_solve_pressure(
     return solve_host(c, grid, u, v, w, boundary_sdf, fluid_sdf, solid_u,
                       solid_v, solid_w, out_u, out_v, out_w, out_pressure,
                       stats, false);
+}
+
+jetgpu_status jetgpu_solve_pressure_collider(
+    jetgpu_ctx* c, const jetgpu_grid* grid, const double* u, const double* v,
+    const double* w, const jetgpu_scalar_field* boundary_sdf,
+    const jetgpu_scalar_field* fluid_sdf, const jetgpu_collider* collider,
+    double* out_u, double* out_v, double* out_w, double* out_pressure,
+    jetgpu_solve_stats* stats) {
+    return solve_host(c, grid, u, v, w, boundary_sdf, fluid_sdf, nullptr,
+                      nullptr, nullptr, out_u, out_v, out_w, out_pressure,
+                      stats, false, collider);
 }
 
 jetgpu_status jetgpu_solve_pressure_blocked(

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 #include <cuda_bf16.h>
 
+#include <mutex>
 #include <string>
 #include <unordered_map>
 #include <vector>
@@ -239,6 +240,29 @@ jetgpu_status fail(Ctx* c, jetgpu_status s, const std::string& msg);
         }                                                                   \
     } while (0)
 
+// Runs a set-up step (a kernel attribute, which CUDA keeps per device) once
+// on each device: the first call with a device current runs `f` and records
+// success for that device; later calls on it do nothing.
+class DeviceOnce {
+  public:
+    template <typename F>
+    bool run(F&& f) {
+        int dev = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= kMax)
+            return false;
+        std::lock_guard<std::mutex> lock(mu_);
+        if (done_[dev]) return true;
+        if (f() != cudaSuccess) return false;
+        done_[dev] = true;
+        return true;
+    }
+
+  private:
+    static constexpr int kMax = 64;
+    std::mutex mu_;
+    bool done_[kMax] = {};
+};
+
 // Number of blocks for a grid-stride kernel over n elements.
 inline int blocks_for(long n, int threads = kThreads, int cap = 1 << 30) {
     long b = (n + threads - 1) / threads;
@@ -370,6 +394,13 @@ jetgpu_status solve_pressure_dev(
     const double* sv, const double* sw, double* ou, double* ov, double* ow,
     double* op, jetgpu_solve_stats* st, const SolveIo* io = nullptr,
     bool blocked = false);
+
+// True when a rigid collider has a non-zero linear or angular velocity.
+bool collider_moves(const jetgpu_collider* col);
+// RigidBodyCollider3::velocityAt at every face of the grid: the u, v and w
+// face components one after the other in `out` (flip.cu).
+jetgpu_status solid_face_velocities(Ctx* c, const GridDesc& g,
+                                    const jetgpu_collider& col, double* out);
 
 jetgpu_status fluid_cfl(Ctx* c, const GridDesc& g, const double* u,
                         const double* v, const double* w, double dt,

@@ -47,15 +47,22 @@ __global__ void k_solid_faces(FaceSet fs, int a, double hx, double hy,
          c += (long)gridDim.x * blockDim.x) {
         int i, j, k;
         cell_ijk(c, s, i, j, k);
-        const double p0 = fs.o[a][0] + hx * (double)i;
-        const double p1 = fs.o[a][1] + hy * (double)j;
-        const double p2 = fs.o[a][2] + hz * (double)k;
+        // RigidBodyCollider3::velocityAt (src/jet/rigid_body_collider3.cpp:
+        // 25-28) at the face position (data origin + h * index); the _rn
+        // intrinsics keep every product and sum separately rounded, as the
+        // reference's double arithmetic is.
+        const double p0 = __dadd_rn(fs.o[a][0], __dmul_rn(hx, (double)i));
+        const double p1 = __dadd_rn(fs.o[a][1], __dmul_rn(hy, (double)j));
+        const double p2 = __dadd_rn(fs.o[a][2], __dmul_rn(hz, (double)k));
         const double* w = col.angular_velocity;
-        const double r0 = p0 - col.centre[0], r1 = p1 - col.centre[1],
-                     r2 = p2 - col.centre[2];
-        const double cr[3] = {w[1] * r2 - r1 * w[2], w[2] * r0 - r2 * w[0],
-                              w[0] * r1 - r0 * w[1]};
-        out[c] = col.linear_velocity[a] + cr[a];
+        const double r0 = __dsub_rn(p0, col.centre[0]),
+                     r1 = __dsub_rn(p1, col.centre[1]),
+                     r2 = __dsub_rn(p2, col.centre[2]);
+        const double cr[3] = {
+            __dsub_rn(__dmul_rn(w[1], r2), __dmul_rn(r1, w[2])),
+            __dsub_rn(__dmul_rn(w[2], r0), __dmul_rn(r2, w[0])),
+            __dsub_rn(__dmul_rn(w[0], r1), __dmul_rn(r0, w[1]))};
+        out[c] = __dadd_rn(col.linear_velocity[a], cr[a]);
     }
 }
 
@@ -118,6 +125,28 @@ bool usable(jetgpu_status s) {
 }
 
 }  // namespace
+
+bool collider_moves(const jetgpu_collider* col) {
+    if (!col) return false;
+    for (int d = 0; d < 3; ++d)
+        if (col->linear_velocity[d] != 0.0 || col->angular_velocity[d] != 0.0)
+            return true;
+    return false;
+}
+
+jetgpu_status solid_face_velocities(Ctx* c, const GridDesc& g,
+                                    const jetgpu_collider& col, double* out) {
+    const FaceSet fs = face_set(g);
+    for (int a = 0; a < 3; ++a) {
+        const long n = fs.s[a].count();
+        k_solid_faces<<<blocks_for(n, kThreads, c->num_sms * 8), kThreads, 0,
+                        c->stream>>>(fs, a, g.spacing[0], g.spacing[1],
+                                     g.spacing[2], col, out);
+        out += n;
+    }
+    JG_CUDA(c, cudaGetLastError());
+    return JETGPU_OK;
+}
 
 jetgpu_status fluid_cfl(Ctx* c, const GridDesc& g, const double* u,
                         const double* v, const double* w, double dt,
@@ -213,24 +242,16 @@ jetgpu_status flip_substep(Ctx* c, const GridDesc& g, long np, double* pos,
     }
     // computePressure: the collider SDF and velocity, the particle SDF.
     const double* solid[3] = {nullptr, nullptr, nullptr};
-    if (col) {
-        bool moving = false;
-        for (int d = 0; d < 3; ++d)
-            moving = moving || col->linear_velocity[d] != 0.0 ||
-                     col->angular_velocity[d] != 0.0;
-        if (moving) {
-            if ((s = grow(c, &c->flip_solid, &c->flip_solid_cap,
-                          (size_t)faces)) != JETGPU_OK)
-                return s;
-            double* sp = c->flip_solid;
-            for (int a = 0; a < 3; ++a) {
-                k_solid_faces<<<blocks_for(nf[a], kThreads, c->num_sms * 8),
-                                kThreads, 0, c->stream>>>(
-                    fs, a, g.spacing[0], g.spacing[1], g.spacing[2], *col, sp);
-                solid[a] = sp;
-                sp += nf[a];
-            }
-        }
+    if (collider_moves(col)) {
+        if ((s = grow(c, &c->flip_solid, &c->flip_solid_cap,
+                      (size_t)faces)) != JETGPU_OK)
+            return s;
+        if ((s = solid_face_velocities(c, g, *col, c->flip_solid)) !=
+            JETGPU_OK)
+            return s;
+        solid[0] = c->flip_solid;
+        solid[1] = solid[0] + nf[0];
+        solid[2] = solid[1] + nf[1];
     }
     {
         jetgpu_grid jg_grid;

@@ -635,9 +635,15 @@ extern "C" jetgpu_status jetgpu_p2g_device_noalloc(
     using namespace jg;
     if (!grid || !u || !v || !w) return JETGPU_BAD_INPUT;
     if (np < 0 || (np > 0 && (!pos || !vel))) return JETGPU_BAD_INPUT;
+    // The same grid checks as the context entry points: positive finite
+    // spacing, finite origin, and fewer than 2^31 cells, so that the face
+    // counts below cannot wrap before the capacity test.
     for (int a = 0; a < 3; ++a)
-        if (grid->res[a] < 1 || !(grid->spacing[a] > 0.0))
+        if (grid->res[a] < 1 || !(grid->spacing[a] > 0.0) ||
+            !std::isfinite(grid->spacing[a]) || !std::isfinite(grid->origin[a]))
             return JETGPU_BAD_INPUT;
+    if ((double)grid->res[0] * grid->res[1] * grid->res[2] > 2147483647.0)
+        return JETGPU_BAD_INPUT;
     GridDesc g;
     for (int a = 0; a < 3; ++a) {
         g.res[a] = grid->res[a];

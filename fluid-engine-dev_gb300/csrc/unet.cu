@@ -185,14 +185,13 @@ jetgpu_status conv3d(cudaStream_t st, const __nv_bfloat16* in, int ci,
                      unsigned* err) {
     ConvArgs a{in, w, bias, out, out32, n, ci, co, relu, err};
     const size_t smem = conv_smem_bytes(ci, co);
-    static bool attr_set = false;
-    if (!attr_set) {
-        if (cudaFuncSetAttribute(k_conv3d_tc,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 (int)conv_smem_bytes(128, 128)) != cudaSuccess)
-            return JETGPU_CUDA_ERROR;
-        attr_set = true;
-    }
+    static DeviceOnce attr;
+    if (!attr.run([] {
+            return cudaFuncSetAttribute(
+                k_conv3d_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                (int)conv_smem_bytes(128, 128));
+        }))
+        return JETGPU_CUDA_ERROR;
     const long blocks = (n.count() + kTile - 1) / kTile;
     k_conv3d_tc<<<(unsigned)blocks, 128, smem, st>>>(a);
     return cudaGetLastError() == cudaSuccess ? JETGPU_OK : JETGPU_CUDA_ERROR;
@@ -365,14 +364,13 @@ __global__ void __launch_bounds__(128) k_conv3d_wgrad_tc(WgradArgs a) {
 jetgpu_status conv3d_wgrad(cudaStream_t st, const __nv_bfloat16* in, int ci,
                            const __nv_bfloat16* dy, int co, Dims n, float* dw,
                            unsigned* err, int sms) {
-    static bool attr_set = false;
-    if (!attr_set) {
-        if (cudaFuncSetAttribute(k_conv3d_wgrad_tc,
-                                 cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 200 * 1024) != cudaSuccess)
-            return JETGPU_CUDA_ERROR;
-        attr_set = true;
-    }
+    static DeviceOnce attr;
+    if (!attr.run([] {
+            return cudaFuncSetAttribute(
+                k_conv3d_wgrad_tc,
+                cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+        }))
+        return JETGPU_CUDA_ERROR;
     const long tiles = (n.count() + 127) / 128;
     const int grid = (int)(tiles < sms ? tiles : sms);
     const int tg = wgrad_taps(ci);

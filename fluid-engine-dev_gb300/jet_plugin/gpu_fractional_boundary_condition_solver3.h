@@ -14,10 +14,42 @@
 #define JETGPU_JET_GPU_FRACTIONAL_BOUNDARY_CONDITION_SOLVER3_H_
 
 #include <jet/grid_fractional_boundary_condition_solver3.h>
+#include <jet/vector_field3.h>
+
+#include <memory>
 
 #include "jetgpu.h"
 
 namespace jetgpu_jet {
+
+//! The collider velocity field a GPU boundary-condition solver hands the
+//! pressure solver (GridFluidSolver3::computePressure passes
+//! colliderVelocityField(), src/jet/grid_fluid_solver3.cpp:243-253). It
+//! samples exactly as the reference's field does
+//! (grid_fractional_boundary_condition_solver3.cpp:265-278: the collider's
+//! velocityAt(x), zero without a collider), and it tells the GPU pressure
+//! solver which collider it stands for, so that a static collider costs no
+//! per-face host sampling and a moving rigid one is evaluated on the GPU.
+class GpuColliderVelocityField3 : public jet::VectorField3 {
+ public:
+    explicit GpuColliderVelocityField3(
+        const jet::GridBoundaryConditionSolver3* owner)
+        : _owner(owner) {}
+
+    jet::Vector3D sample(const jet::Vector3D& x) const override;
+    //! Zero for a rigid motion; a finite difference otherwise.
+    double divergence(const jet::Vector3D& x) const override;
+    //! Twice the angular velocity for a rigid motion.
+    jet::Vector3D curl(const jet::Vector3D& x) const override;
+    std::function<jet::Vector3D(const jet::Vector3D&)> sampler()
+        const override;
+
+    //! The owner's current collider (null when there is none).
+    const jet::Collider3Ptr& collider() const { return _owner->collider(); }
+
+ private:
+    const jet::GridBoundaryConditionSolver3* _owner;
+};
 
 class GpuFractionalBoundaryConditionSolver3
     : public jet::GridFractionalBoundaryConditionSolver3 {
@@ -40,9 +72,14 @@ class GpuFractionalBoundaryConditionSolver3
     void constrainVelocity(jet::FaceCenteredGrid3* velocity,
                            unsigned int extrapolationDepth = 5) override;
 
+    //! The collider's velocity as GpuColliderVelocityField3 (samples as the
+    //! reference's colliderVelocityField does).
+    jet::VectorField3Ptr colliderVelocityField() const override;
+
     jetgpu_status lastStatus() const { return _status; }
 
  private:
+    std::shared_ptr<GpuColliderVelocityField3> _velocityField;
     jetgpu_config _config;
     struct jetgpu_ctx* _ctx = nullptr;
     jetgpu_status _status = JETGPU_OK;

@@ -10,6 +10,7 @@
 #include <jet/face_centered_grid3.h>
 #include <jet/grid_fractional_boundary_condition_solver3.h>
 #include <jet/logging.h>
+#include <jet/rigid_body_collider3.h>
 
 #include <cstring>
 #include <memory>
@@ -59,13 +60,37 @@ void GpuFractionalSinglePhasePressureSolver3::solve(
         describe_field(fluidSdf, input, &_fluidRaster);
 
     // Collider velocity: only the normal component at each face is used
-    // (grid_fractional_single_phase_pressure_solver3.cpp:241-255).
+    // (grid_fractional_single_phase_pressure_solver3.cpp:241-255). The GPU
+    // boundary-condition solver (which setPressureSolver installs with this
+    // solver) passes a GpuColliderVelocityField3: no collider, or a rigid
+    // one standing still, means no moving-boundary term at all; a moving
+    // rigid collider's velocityAt is evaluated on the GPU. Any other field
+    // is sampled at every face position on the host.
     const double* su = nullptr;
     const double* sv = nullptr;
     const double* sw = nullptr;
-    auto cv = dynamic_cast<const ConstantVectorField3*>(&boundaryVelocity);
-    const bool still = cv && cv->sample(Vector3D()).lengthSquared() == 0.0;
-    if (!still) {
+    jetgpu_collider motion{};
+    bool moving_rigid = false;
+    bool sample_on_host = true;
+    if (auto gv = dynamic_cast<const GpuColliderVelocityField3*>(
+            &boundaryVelocity)) {
+        const Collider3Ptr& collider = gv->collider();
+        auto rigid = std::dynamic_pointer_cast<RigidBodyCollider3>(collider);
+        if (!collider) {
+            sample_on_host = false;
+        } else if (rigid) {
+            motion = rigid_motion(*rigid);
+            sample_on_host = false;
+            for (int d = 0; d < 3; ++d)
+                moving_rigid = moving_rigid ||
+                               motion.linear_velocity[d] != 0.0 ||
+                               motion.angular_velocity[d] != 0.0;
+        }
+    } else if (auto cv = dynamic_cast<const ConstantVectorField3*>(
+                   &boundaryVelocity)) {
+        sample_on_host = cv->sample(Vector3D()).lengthSquared() != 0.0;
+    }
+    if (sample_on_host) {
         auto sample = [&](std::vector<double>* out, const Size3& s,
                           VectorGrid3::DataPositionFunc pos, int axis) {
             out->resize(s.x * s.y * s.z);
@@ -90,10 +115,15 @@ void GpuFractionalSinglePhasePressureSolver3::solve(
     auto ou = output->uAccessor();
     auto ov = output->vAccessor();
     auto ow = output->wAccessor();
-    _status = jetgpu_solve_pressure(_ctx, &g, u.data(), v.data(), w.data(),
-                                    &bsdf, &fsdf, su, sv, sw, ou.data(),
-                                    ov.data(), ow.data(), _pressure.data(),
-                                    &_stats);
+    if (moving_rigid)
+        _status = jetgpu_solve_pressure_collider(
+            _ctx, &g, u.data(), v.data(), w.data(), &bsdf, &fsdf, &motion,
+            ou.data(), ov.data(), ow.data(), _pressure.data(), &_stats);
+    else
+        _status = jetgpu_solve_pressure(_ctx, &g, u.data(), v.data(),
+                                        w.data(), &bsdf, &fsdf, su, sv, sw,
+                                        ou.data(), ov.data(), ow.data(),
+                                        _pressure.data(), &_stats);
     if (_status != JETGPU_OK) {
         // The reference ignores its linear solver's result
         // (grid_fractional_single_phase_pressure_solver3.cpp:466-483); the

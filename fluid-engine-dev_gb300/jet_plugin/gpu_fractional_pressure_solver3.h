@@ -40,9 +40,13 @@ class GpuFractionalSinglePhasePressureSolver3 : public jet::GridPressureSolver3 
 
     //! GridPressureSolver3::solve (grid_pressure_solver3.h:58-64).
     //! CellCenteredScalarGrid3 and ConstantScalarField3 SDFs go to the GPU
-    //! as they are and are sampled there with Jet's exact trilinear rule;
-    //! other field types are rasterised at cell centres first. A moving
-    //! collider's velocity is sampled at every face position on the host.
+    //! as they are (the grid's own data, not a copy) and are sampled there
+    //! with Jet's exact trilinear rule; other field types are rasterised at
+    //! cell centres first. The collider velocity of the GPU
+    //! boundary-condition solver (GpuColliderVelocityField3) costs nothing
+    //! on the host: a missing or resting collider adds no moving-boundary
+    //! term, a moving RigidBodyCollider3 is evaluated on the GPU. Any other
+    //! velocity field is sampled at every face position on the host.
     void solve(const jet::FaceCenteredGrid3& input,
                double timeIntervalInSeconds, jet::FaceCenteredGrid3* output,
                const jet::ScalarField3& boundarySdf =

@@ -34,9 +34,10 @@ inline jetgpu_grid grid_of(const jet::FaceCenteredGrid3& grid) {
 }
 
 //! A ScalarField3 argument of GridPressureSolver3::solve. Constants and
-//! CellCenteredScalarGrid3 pass as they are (the GPU samples grids with Jet's
+//! CellCenteredScalarGrid3 pass as they are, the grid's own data pointer
+//! included (nothing is copied on the host; the GPU samples grids with Jet's
 //! exact trilinear rule); any other field is rasterised at the velocity
-//! grid's cell centres first. `raster` keeps the copied data alive.
+//! grid's cell centres into `raster`, which keeps that data alive.
 inline jetgpu_scalar_field describe_field(const jet::ScalarField3& field,
                                           const jet::FaceCenteredGrid3& grid,
                                           std::vector<double>* raster) {
@@ -58,11 +59,14 @@ inline jetgpu_scalar_field describe_field(const jet::ScalarField3& field,
         g = owned.get();
     }
     const Size3 r = g->resolution();
-    const size_t n = r.x * r.y * r.z;
     auto acc = g->constDataAccessor();
-    raster->assign(acc.data(), acc.data() + n);
     f.kind = 1;
-    f.data = raster->data();
+    if (owned) {
+        raster->assign(acc.data(), acc.data() + r.x * r.y * r.z);
+        f.data = raster->data();
+    } else {
+        f.data = acc.data();
+    }
     const Vector3D o = g->dataOrigin(), h = g->gridSpacing();
     for (int d = 0; d < 3; ++d) {
         f.res[d] = (int)r[d];
@@ -70,6 +74,21 @@ inline jetgpu_scalar_field describe_field(const jet::ScalarField3& field,
         f.spacing[d] = h[d];
     }
     return f;
+}
+
+//! The motion of a rigid collider as the C ABI takes it (velocityAt =
+//! linear + angular x (p - translation), src/jet/rigid_body_collider3.cpp:
+//! 25-28).
+inline jetgpu_collider rigid_motion(const jet::RigidBodyCollider3& rigid) {
+    jetgpu_collider col{};
+    const jet::Vector3D t = rigid.surface()->transform.translation();
+    for (int d = 0; d < 3; ++d) {
+        col.linear_velocity[d] = rigid.linearVelocity[d];
+        col.angular_velocity[d] = rigid.angularVelocity[d];
+        col.centre[d] = t[d];
+    }
+    col.friction = rigid.frictionCoefficient();
+    return col;
 }
 
 //! Creates the context on first use; throws when that fails.
@@ -110,13 +129,7 @@ inline void constrain_on_gpu(jet::GridFractionalBoundaryConditionSolver3& bc,
             throw std::invalid_argument(
                 "the GPU boundary-condition solvers take rigid colliders "
                 "(RigidBodyCollider3) only");
-        const Vector3D t = rigid->surface()->transform.translation();
-        for (int d = 0; d < 3; ++d) {
-            col.linear_velocity[d] = rigid->linearVelocity[d];
-            col.angular_velocity[d] = rigid->angularVelocity[d];
-            col.centre[d] = t[d];
-        }
-        col.friction = rigid->frictionCoefficient();
+        col = rigid_motion(*rigid);
         colp = &col;
     }
     ensure_context(cfg, ctx, status);

@@ -117,6 +117,7 @@ EXPORTS = (
     "jetgpu_build_particle_sdf", "jetgpu_flip_params_default",
     "jetgpu_fluid_cfl_device", "jetgpu_flip_substep_device",
     "jetgpu_apic_p2g_device", "jetgpu_apic_g2p_device",
+    "jetgpu_solve_pressure_collider",
 )
 
 # closedDomainBoundaryFlag bits (include/jet/constants.h:312-335).
@@ -193,6 +194,11 @@ def library() -> C.CDLL:
     L.jetgpu_solve_pressure.restype = C.c_int
     L.jetgpu_solve_pressure_device.argtypes = solve_args
     L.jetgpu_solve_pressure_device.restype = C.c_int
+    L.jetgpu_solve_pressure_collider.argtypes = [
+        vp, C.POINTER(Grid), dp, dp, dp, C.POINTER(ScalarField),
+        C.POINTER(ScalarField), C.POINTER(Collider), dp, dp, dp, dp,
+        C.POINTER(SolveStats)]
+    L.jetgpu_solve_pressure_collider.restype = C.c_int
     blocked_args = [vp, C.POINTER(Grid), dp, dp, dp, C.POINTER(ScalarField),
                     C.POINTER(ScalarField), dp, dp, dp, dp,
                     C.POINTER(SolveStats)]
@@ -551,8 +557,10 @@ class GridFractionalSinglePhasePressureSolver3:
               fluidSdf=ConstantScalarField3(-kMaxD),
               useCompressed: bool = False) -> int:
         """Projects ``input`` into ``output`` (host arrays). boundaryVelocity
-        is None (static collider) or a tuple of per-face normal components
-        (solid_u, solid_v, solid_w). ``useCompressed`` selects the
+        is None (static collider), a tuple of per-face normal components
+        (solid_u, solid_v, solid_w), or a rigid collider's motion
+        (``Collider``: RigidBodyCollider3::velocityAt evaluated on the GPU at
+        every face). ``useCompressed`` selects the
         reference's CSR storage; the GPU system is matrix-row based either
         way, so it has no effect. Returns the C status (0 or NOT_CONVERGED)."""
         del timeIntervalInSeconds, useCompressed  # unused, as in the reference
@@ -564,7 +572,10 @@ class GridFractionalSinglePhasePressureSolver3:
         v = np.ascontiguousarray(input.v, np.float64)
         w = np.ascontiguousarray(input.w, np.float64)
         su = sv = sw = None
-        if boundaryVelocity is not None:
+        collider = None
+        if isinstance(boundaryVelocity, Collider):
+            collider = boundaryVelocity
+        elif boundaryVelocity is not None:
             su, sv, sw = (None if a is None else np.ascontiguousarray(a, np.float64)
                           for a in boundaryVelocity)
         for a, ref in ((output.u, u), (output.v, v), (output.w, w)):
@@ -573,10 +584,17 @@ class GridFractionalSinglePhasePressureSolver3:
         nx, ny, nz = input.resolution
         p = self._pressure_buffer((nz, ny, nx))
         solver = self._solver
-        st = library().jetgpu_solve_pressure(
-            solver.context(), C.byref(g), _p(u), _p(v), _p(w), C.byref(bs),
-            C.byref(fs), _p(su), _p(sv), _p(sw), _p(output.u), _p(output.v),
-            _p(output.w), _p(p), C.byref(self.last_stats))
+        if collider is not None:
+            st = library().jetgpu_solve_pressure_collider(
+                solver.context(), C.byref(g), _p(u), _p(v), _p(w),
+                C.byref(bs), C.byref(fs), C.byref(collider), _p(output.u),
+                _p(output.v), _p(output.w), _p(p), C.byref(self.last_stats))
+        else:
+            st = library().jetgpu_solve_pressure(
+                solver.context(), C.byref(g), _p(u), _p(v), _p(w),
+                C.byref(bs), C.byref(fs), _p(su), _p(sv), _p(sw),
+                _p(output.u), _p(output.v), _p(output.w), _p(p),
+                C.byref(self.last_stats))
         solver.last_stats = self.last_stats
         solver.check(st, allow=SOLVED)
         self._pressure = p

@@ -249,10 +249,14 @@ jetgpu_status jetgpu_g2p_pic_device(struct jetgpu_ctx* ctx,
  * synchronisation is not allowed. It computes the same result as
  * jetgpu_p2g_device (same DEVICE-pointer arguments) but needs no context:
  * its only scratch, the per-face weight sums, lives in a fixed array in the
- * library's device memory of JETGPU_P2G_NOALLOC_MAX_FACES doubles (6.4 MB,
- * the faces of a 64^3 grid), which every GPU that loads the library holds
- * until the process exits. Grids whose u+v+w face count exceeds it are
- * rejected with JETGPU_CAPACITY_EXCEEDED before any GPU work.
+ * library's device memory of JETGPU_P2G_NOALLOC_MAX_FACES doubles (6.4 MB),
+ * which every GPU that loads the library holds until the process exits.
+ * The limit is on the face count, not on each axis: a grid (nx, ny, nz) is
+ * accepted when (nx+1)*ny*nz + nx*(ny+1)*nz + nx*ny*(nz+1) <=
+ * JETGPU_P2G_NOALLOC_MAX_FACES (a 64^3 grid fits exactly; so does
+ * 100 x 40 x 40) and rejected with JETGPU_CAPACITY_EXCEEDED, before any GPU
+ * work, otherwise. Grids with a non-finite origin or spacing, a spacing
+ * <= 0 or 2^31 cells or more get JETGPU_BAD_INPUT.
  *
  * The work is queued on `stream` (a cudaStream_t; NULL = the default
  * stream) and the call returns without waiting for it. The first call on a
@@ -281,6 +285,22 @@ typedef struct jetgpu_collider {
     double centre[3];
     double friction;
 } jetgpu_collider;
+
+/* jetgpu_solve_pressure with the collider velocity given as a rigid body's
+ * motion instead of sampled face arrays: the boundaryVelocity that
+ * GridFractionalBoundaryConditionSolver3::colliderVelocityField() hands the
+ * pressure solver (src/jet/grid_fractional_boundary_condition_solver3.cpp:
+ * 265-278) is RigidBodyCollider3::velocityAt
+ * (src/jet/rigid_body_collider3.cpp:25-28), which is evaluated here on the
+ * device at every face position. collider NULL, or one with zero linear and
+ * angular velocity, is a static collider (no moving-boundary term, as
+ * solid_u/v/w = NULL). HOST pointers; otherwise as jetgpu_solve_pressure. */
+jetgpu_status jetgpu_solve_pressure_collider(
+    struct jetgpu_ctx* ctx, const jetgpu_grid* grid, const double* u,
+    const double* v, const double* w, const jetgpu_scalar_field* boundary_sdf,
+    const jetgpu_scalar_field* fluid_sdf, const jetgpu_collider* collider,
+    double* out_u, double* out_v, double* out_w, double* out_pressure,
+    jetgpu_solve_stats* stats);
 
 /* Closed-domain bits of closedDomainBoundaryFlag()
  * (include/jet/constants.h:312-335). */

@@ -572,6 +572,18 @@ class Oracle:
 _cache: dict = {}
 
 
+def divergence_at_cell_center(u, v, w, spacing) -> np.ndarray:
+    """FaceCenteredGrid3::divergenceAtCellCenter at every cell
+    (src/jet/face_centered_grid3.cpp:137-151): (u(i+1)-u(i))/h.x +
+    (v(j+1)-v(j))/h.y + (w(k+1)-w(k))/h.z, summed in that order. u, v, w are
+    the (nz,ny,nx+1), (nz,ny+1,nx), (nz+1,ny,nx) face arrays; returns
+    (nz,ny,nx)."""
+    hx, hy, hz = spacing
+    return ((u[:, :, 1:] - u[:, :, :-1]) / hx +
+            (v[:, 1:, :] - v[:, :-1, :]) / hy +
+            (w[1:, :, :] - w[:-1, :, :]) / hz)
+
+
 def port() -> Oracle:
     if "port" not in _cache:
         if not os.path.exists(PORT_SO):

@@ -242,3 +242,59 @@ def test_gradient_paths_agree():
         solver.close()
     for a, b in zip(*outs):
         assert np.array_equal(a, b)
+
+
+def rigid_face_velocities(n, h, linear, angular, centre):
+    """RigidBodyCollider3::velocityAt (src/jet/rigid_body_collider3.cpp:
+    25-28) at every u/v/w face position (origin 0; face data origins
+    (0, h/2, h/2), (h/2, 0, h/2), (h/2, h/2, 0)), component a on axis-a
+    faces, in double arithmetic."""
+    out = []
+    for a, shape in enumerate([(n, n, n + 1), (n, n + 1, n), (n + 1, n, n)]):
+        k, j, i = np.indices(shape, dtype=np.float64)
+        o = [0.5 * h] * 3
+        o[a] = 0.0
+        p = (o[0] + h * i, o[1] + h * j, o[2] + h * k)
+        r = [p[d] - centre[d] for d in range(3)]
+        w = angular
+        cr = (w[1] * r[2] - r[1] * w[2], w[2] * r[0] - r[2] * w[0],
+              w[0] * r[1] - r[0] * w[1])
+        out.append(linear[a] + cr[a])
+    return out
+
+
+def test_moving_rigid_collider_on_device(port):
+    """jetgpu_solve_pressure_collider evaluates the collider's velocityAt on
+    the GPU: the same bits as passing the host-sampled face velocities to
+    jetgpu_solve_pressure, and the reference's answer for them."""
+    n = 32
+    h = 1.0 / n
+    sc = scenes.sphere_union_scene(n, seed=2)
+    lin, ang, ctr = (0.3, -0.2, 0.1), (0.5, 1.0, -0.7), (0.5, 0.3, 0.5)
+    solid = rigid_face_velocities(n, h, lin, ang, ctr)
+    ps_a, out_a, st = solve((n,) * 3, (h,) * 3, sc["u"], sc["v"], sc["w"],
+                            sc["boundary_sdf"], sc["fluid_sdf"],
+                            solid=tuple(solid))
+    assert st == 0
+    col = jetgpu.Collider.make(linear=lin, angular=ang, centre=ctr)
+    ps_b, out_b, st = solve((n,) * 3, (h,) * 3, sc["u"], sc["v"], sc["w"],
+                            sc["boundary_sdf"], sc["fluid_sdf"], solid=col)
+    assert st == 0
+    assert np.array_equal(ps_a.level(0, "b"), ps_b.level(0, "b"))
+    assert np.array_equal(ps_a.pressure(), ps_b.pressure())
+    for k in "uvw":
+        assert np.array_equal(getattr(out_a, k), getattr(out_b, k))
+    ref = port.pressure_solve((n,) * 3, (h,) * 3, (0, 0, 0), sc["u"], sc["v"],
+                              sc["w"], sc["boundary_sdf"], sc["fluid_sdf"],
+                              oracle.MgParams(400, 5, 3, 3, 20, 20, 1e-13, 1.5,
+                                              True), solid=tuple(solid))
+    assert np.array_equal(ps_b.level(0, "b"), port.level(0, "b", (n,) * 3).reshape(-1))
+    assert rel_l2(ps_b.pressure(), ref["p"]) < P_REL_L2
+    # A resting collider is a static one.
+    still = jetgpu.Collider.make(centre=ctr)
+    ps_c, out_c, st = solve((n,) * 3, (h,) * 3, sc["u"], sc["v"], sc["w"],
+                            sc["boundary_sdf"], sc["fluid_sdf"], solid=still)
+    ps_d, out_d, st2 = solve((n,) * 3, (h,) * 3, sc["u"], sc["v"], sc["w"],
+                             sc["boundary_sdf"], sc["fluid_sdf"])
+    assert st == 0 and st2 == 0
+    assert np.array_equal(ps_c.pressure(), ps_d.pressure())
