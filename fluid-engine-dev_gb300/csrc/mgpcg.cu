@@ -1035,16 +1035,20 @@ ColLaunch col_launch(const Ctx* c, const Level& L, int tcx, int ty,
 
 // ---- TMA sweep (sweep_tma.cuh): tensor maps and launch --------------------
 
-// Row element and prefetch distance (planes) of the TMA sweep. Two planes
-// keep two blocks per SM with FP32 rows; deeper prefetch measured no faster.
+// Row element, prefetch distance (planes) and resident blocks per SM the
+// register budget is set for, of the TMA sweep: with two planes in flight a
+// block holds 68 KB of shared memory with FP32 rows (three blocks per SM)
+// and 51 KB with BF16 rows (four).
 template <typename R> struct TmaCfg;
 template <> struct TmaCfg<RowsF> {
     using E = float;
     static constexpr int D = 2;
+    static constexpr int MINB = 3;
 };
 template <> struct TmaCfg<RowsB> {
     using E = unsigned short;
     static constexpr int D = 2;
+    static constexpr int MINB = 4;
 };
 
 PFN_cuTensorMapEncodeTiled_v12000 tma_encoder() {
@@ -1120,12 +1124,12 @@ void launch_tma(Ctx* c, const ColLaunch& cl, const TmaMaps& m, int src,
     constexpr int smem = tsw::Layout<E, D>::TOTAL;
     double* err = c->scal + S_WAIT;
     if (zero)
-        tsw::k_rb_sweep_tma<true, E, D>
+        tsw::k_rb_sweep_tma<true, E, D, TmaCfg<R>::MINB>
             <<<cl.grid, tsw::BLOCK, smem, c->stream>>>(
                 m.b, m.r, m.b, xout, n, first, (float)c->cfg.sor, cl.tiles_x,
                 cl.total, cl.per_block, err);
     else
-        tsw::k_rb_sweep_tma<false, E, D>
+        tsw::k_rb_sweep_tma<false, E, D, TmaCfg<R>::MINB>
             <<<cl.grid, tsw::BLOCK, smem, c->stream>>>(
                 m.x[src], m.r, m.b, xout, n, first, (float)c->cfg.sor,
                 cl.tiles_x, cl.total, cl.per_block, err);
@@ -1139,16 +1143,16 @@ jetgpu_status tma_prepare(Ctx* c, int* blocks) {
     constexpr int D = TmaCfg<R>::D;
     const int smem = tsw::Layout<E, D>::TOTAL;
     int occ[2] = {0, 0};
-    JG_CUDA(c, cudaFuncSetAttribute(tsw::k_rb_sweep_tma<true, E, D>,
+    JG_CUDA(c, cudaFuncSetAttribute(tsw::k_rb_sweep_tma<true, E, D, TmaCfg<R>::MINB>,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     smem));
-    JG_CUDA(c, cudaFuncSetAttribute(tsw::k_rb_sweep_tma<false, E, D>,
+    JG_CUDA(c, cudaFuncSetAttribute(tsw::k_rb_sweep_tma<false, E, D, TmaCfg<R>::MINB>,
                                     cudaFuncAttributeMaxDynamicSharedMemorySize,
                                     smem));
     JG_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                   &occ[0], tsw::k_rb_sweep_tma<true, E, D>, tsw::BLOCK, smem));
+                   &occ[0], tsw::k_rb_sweep_tma<true, E, D, TmaCfg<R>::MINB>, tsw::BLOCK, smem));
     JG_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                   &occ[1], tsw::k_rb_sweep_tma<false, E, D>, tsw::BLOCK, smem));
+                   &occ[1], tsw::k_rb_sweep_tma<false, E, D, TmaCfg<R>::MINB>, tsw::BLOCK, smem));
     *blocks = tma_encoder() ? std::min(occ[0], occ[1]) : 0;
     return JETGPU_OK;
 }

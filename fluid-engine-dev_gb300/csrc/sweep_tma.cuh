@@ -86,11 +86,14 @@ template <> struct Elem<unsigned short> {
 };
 
 // Shared-memory layout (byte offsets from a 128-byte aligned base). Ring
-// depths: a step t reads x of planes t..t+2 and stages x of t+2+D; rows of
-// t-1..t+1 and b of t..t+1, staging both of t+1+D.
+// depths: a step t reads x of planes t+1 (neighbours) and t+2 (own cells)
+// and stages x of t+2+D; it reads the rows and b of plane t+1 and stages
+// those of t+1+D. Everything a step needs from planes t and t-1 is held in
+// registers (see the kernel), so each ring holds the planes read plus those
+// in flight.
 template <typename E, int D>
 struct Layout {
-    static constexpr int XR = D + 3, AR = D + 3, BR = D + 2;
+    static constexpr int XR = D + 2, AR = D + 1;
     static constexpr int RW = TX + 2 * Elem<E>::H;
     static constexpr int X_BYTES = XH * XW * 4;
     static constexpr int R_BYTES = 4 * RH * RW * (int)sizeof(E);
@@ -101,7 +104,7 @@ struct Layout {
     static constexpr int X_OFF = GAP;  // ring entries, each after a guard
     static constexpr int R_OFF = X_OFF + XR * X_STEP;
     static constexpr int B_OFF = R_OFF + AR * R_STEP;
-    static constexpr int YF_OFF = B_OFF + BR * B_STEP;
+    static constexpr int YF_OFF = B_OFF + AR * B_STEP;
     static constexpr int YF_BYTES = 2 * FR * XW * 4;
     static constexpr int BAR_OFF = YF_OFF + up128(YF_BYTES) + GAP;
     static constexpr int TOTAL = BAR_OFF + 8 * (XR + AR) + 128;
@@ -136,103 +139,32 @@ __device__ __forceinline__ void tma4(void* dst, const CUtensorMap* m, int c0,
 __device__ __forceinline__ float4 lds4(const float* p) {
     return *reinterpret_cast<const float4*>(p);
 }
+// e ? b : a.
 __device__ __forceinline__ float sel(int e, float a, float b) {
     return e ? b : a;
 }
 
-// F update of the two cells at offsets e and e+2 of the group (e = 0 or 1,
-// per thread) of plane t+1. X0, X1, X2: x of planes t, t+1, t+2 at the
-// group; R1 / R0: rows of planes t+1 / t at the group; B1: b of plane t+1.
-// Neighbour products are summed in the order left, right, down, up, back,
-// front.
-template <bool ZERO, typename E>
-__device__ __forceinline__ float2 f_cells(int e, const float* X0,
-                                          const float* X1, const float* X2,
-                                          const E* R1, const E* R0,
-                                          const float* B1, float omega) {
-    using El = Elem<E>;
-    constexpr int RW = TX + 2 * El::H;
-    constexpr int RC = RH * RW;
-    const float4 cc = El::ld4(R1);
-    const float4 bb = lds4(B1);
-    const float cA = sel(e, cc.x, cc.y), cB = sel(e, cc.z, cc.w);
-    const float bA = sel(e, bb.x, bb.y), bB = sel(e, bb.z, bb.w);
-    if (ZERO)
-        return make_float2(omega * __fdividef(bA, cA),
-                           omega * __fdividef(bB, cB));
-    const float4 xc = lds4(X1);
-    const float xl = X1[-1], xr = X1[4];
-    const float4 xd = lds4(X1 - XW), xu = lds4(X1 + XW);
-    const float4 xb = lds4(X0), xf = lds4(X2);
-    const float4 rr = El::ld4(R1 + RC);
-    const float rl = El::ld1(R1 + RC - 1);
-    const float4 uu = El::ld4(R1 + 2 * RC);
-    const float4 ud = El::ld4(R1 + 2 * RC - RW);
-    const float4 ff = El::ld4(R1 + 3 * RC);
-    const float4 fb = El::ld4(R0 + 3 * RC);
-    const float accA = sel(e, rl, rr.x) * sel(e, xl, xc.x) +
-                       sel(e, rr.x, rr.y) * sel(e, xc.y, xc.z) +
-                       sel(e, ud.x, ud.y) * sel(e, xd.x, xd.y) +
-                       sel(e, uu.x, uu.y) * sel(e, xu.x, xu.y) +
-                       sel(e, fb.x, fb.y) * sel(e, xb.x, xb.y) +
-                       sel(e, ff.x, ff.y) * sel(e, xf.x, xf.y);
-    const float accB = sel(e, rr.y, rr.z) * sel(e, xc.y, xc.z) +
-                       sel(e, rr.z, rr.w) * sel(e, xc.w, xr) +
-                       sel(e, ud.z, ud.w) * sel(e, xd.z, xd.w) +
-                       sel(e, uu.z, uu.w) * sel(e, xu.z, xu.w) +
-                       sel(e, fb.z, fb.w) * sel(e, xb.z, xb.w) +
-                       sel(e, ff.z, ff.w) * sel(e, xf.z, xf.w);
-    return make_float2(
-        (1.0f - omega) * sel(e, xc.x, xc.y) + omega * __fdividef(bA - accA, cA),
-        (1.0f - omega) * sel(e, xc.z, xc.w) + omega * __fdividef(bB - accB, cB));
-}
-
-// S update of the two cells at offsets e and e+2 of plane t. Y: new F values
-// of plane t at the group (shared buffer); fm / fp: own F values of planes
-// t-1 / t+1 at the same cells; R0 / Rm: rows of planes t / t-1; B0: b of
-// plane t; X0: old x of plane t.
-template <bool ZERO, typename E>
-__device__ __forceinline__ float2 s_cells(int e, const float* Y, float2 fm,
-                                          float2 fp, const E* R0, const E* Rm,
-                                          const float* B0, const float* X0,
-                                          float omega) {
-    using El = Elem<E>;
-    constexpr int RW = TX + 2 * El::H;
-    constexpr int RC = RH * RW;
-    const float4 yc = lds4(Y);
-    const float yl = Y[-1], yr = Y[4];
-    const float4 yd = lds4(Y - XW), yu = lds4(Y + XW);
-    const float4 cc = El::ld4(R0);
-    const float4 rr = El::ld4(R0 + RC);
-    const float rl = El::ld1(R0 + RC - 1);
-    const float4 uu = El::ld4(R0 + 2 * RC);
-    const float4 ud = El::ld4(R0 + 2 * RC - RW);
-    const float4 ff = El::ld4(R0 + 3 * RC);
-    const float4 fb = El::ld4(Rm + 3 * RC);
-    const float4 bb = lds4(B0);
-    float xA = 0.f, xB = 0.f;
-    if (!ZERO) {
-        const float4 xc = lds4(X0);
-        xA = sel(e, xc.x, xc.y);
-        xB = sel(e, xc.z, xc.w);
+// One ring of staged planes: the slot and mbarrier phase of the next plane
+// to arrive, advanced one plane at a time (no division in the loop).
+struct Ring {
+    int slot = 0;
+    unsigned phase = 0;
+    template <int N>
+    __device__ __forceinline__ void advance() {
+        if (++slot == N) {
+            slot = 0;
+            phase ^= 1u;
+        }
     }
-    const float accA = sel(e, rl, rr.x) * sel(e, yl, yc.x) +
-                       sel(e, rr.x, rr.y) * sel(e, yc.y, yc.z) +
-                       sel(e, ud.x, ud.y) * sel(e, yd.x, yd.y) +
-                       sel(e, uu.x, uu.y) * sel(e, yu.x, yu.y) +
-                       sel(e, fb.x, fb.y) * fm.x + sel(e, ff.x, ff.y) * fp.x;
-    const float accB = sel(e, rr.y, rr.z) * sel(e, yc.y, yc.z) +
-                       sel(e, rr.z, rr.w) * sel(e, yc.w, yr) +
-                       sel(e, ud.z, ud.w) * sel(e, yd.z, yd.w) +
-                       sel(e, uu.z, uu.w) * sel(e, yu.z, yu.w) +
-                       sel(e, fb.z, fb.w) * fm.y + sel(e, ff.z, ff.w) * fp.y;
-    return make_float2((1.0f - omega) * xA +
-                           omega * __fdividef(sel(e, bb.x, bb.y) - accA,
-                                              sel(e, cc.x, cc.y)),
-                       (1.0f - omega) * xB +
-                           omega * __fdividef(sel(e, bb.z, bb.w) - accB,
-                                              sel(e, cc.z, cc.w)));
-}
+};
+
+// Rows and rhs a cell pair (offsets s and s+2 of a group) needs for its
+// second-colour update, picked out of the group's staged values when the
+// plane's first colour is updated one step earlier: centre, left, right,
+// down, up, front and back coefficients and b.
+struct PairRows {
+    float c[2], l[2], r[2], d[2], u[2], f[2], k[2], b[2];
+};
 
 // ZERO: the sweep starts from x = 0 (no x is staged). tm_x covers xin
 // (nx, ny, nz) FP32, box (XW, XH); tm_r the rows (nx, ny, nz, 4) of E, box
@@ -240,8 +172,19 @@ __device__ __forceinline__ float2 s_cells(int e, const float* Y, float2 fm,
 // to 1 when a copy did not arrive within the wait limit; the kernel then
 // stops waiting, finishes its loop on whatever the rings hold, and before it
 // exits waits (bounded) for the copies it issued.
-template <bool ZERO, typename E, int D>
-__global__ void __launch_bounds__(BLOCK, 1)
+//
+// Per thread, step t of the march over planes updates the F cells of plane
+// t+1 (offsets e and e+2 of its group) and the S cells of plane t (the same
+// offsets: the colour pattern flips with the plane). Values a thread uses at
+// two consecutive steps stay in registers: x of plane t+1 at its own group
+// (loaded as the front neighbour one step earlier), x of plane t at the
+// pair, the front coefficients of plane t, and the second-colour rows of
+// plane t (PairRows, picked while the same plane's first colour was
+// updated). Shared memory is read only for in-plane neighbours and for the
+// newly arrived planes. Neighbour products are summed in the order left,
+// right, down, up, back, front.
+template <bool ZERO, typename E, int D, int MINB>
+__global__ void __launch_bounds__(BLOCK, MINB)
     k_rb_sweep_tma(const __grid_constant__ CUtensorMap tm_x,
                    const __grid_constant__ CUtensorMap tm_r,
                    const __grid_constant__ CUtensorMap tm_b,
@@ -249,8 +192,9 @@ __global__ void __launch_bounds__(BLOCK, 1)
                    int tiles_x, long total, long per_block, double* err) {
     using Lt = Layout<E, D>;
     using El = Elem<E>;
-    constexpr int XR = Lt::XR, AR = Lt::AR, BR = Lt::BR;
+    constexpr int XR = Lt::XR, AR = Lt::AR;
     constexpr int RW = Lt::RW;
+    constexpr int RC = RH * RW;
     constexpr int H = El::H;
     extern __shared__ unsigned char smem_raw[];
     unsigned char* base = reinterpret_cast<unsigned char*>(
@@ -270,6 +214,7 @@ __global__ void __launch_bounds__(BLOCK, 1)
     const int xo = (ry + 1) * XW + 4 * gq;            // x: row j in the box
     const int bo = ry * XW + 4 * gq;                  // b and F buffer
     const int ro = (ry + 1) * RW + 4 * gq + (H - 4);  // rows: row j
+    const float w1 = 1.0f - omega;
 
     if (tid == 0) {
         for (int s = 0; s < XR + AR; ++s) tc::mbar_init(&barx[s], 1);
@@ -278,7 +223,10 @@ __global__ void __launch_bounds__(BLOCK, 1)
     __syncthreads();
 
     const int sz = n.x * n.y;  // levels hold < 2^31 cells
-    unsigned seq = 0;          // copies of each kind this block has issued
+    // Issue side (thread 0) and wait side (every thread) of each ring, and
+    // the number of copies thread 0 has issued into each.
+    Ring ix, ir, wx, wr;
+    unsigned nix = 0, nir = 0;
     bool bad = false;
     long w = (long)blockIdx.x * per_block;
     const long wend = min(total, w + per_block);
@@ -293,60 +241,75 @@ __global__ void __launch_bounds__(BLOCK, 1)
         const int gj = j0 - 1 + ry;
         const bool gv = worker && gi >= 0 && gi < n.x && gj >= 0 && gj < n.y;
         // Steps t0 .. k1-1; x of planes t0 .. k1+1 and rows + b of planes
-        // t0-1 .. k1 are staged, the same count of each.
+        // t0 .. k1 are staged, each once.
         const int t0 = k0 - 2;
-        auto qx = [&](int p) { return seq + (unsigned)(p - t0); };
-        auto qr = [&](int p) { return seq + (unsigned)(p - t0 + 1); };
-        auto xs = [&](int p) {
-            return reinterpret_cast<const float*>(
-                       base + Lt::X_OFF + (qx(p) % XR) * Lt::X_STEP) + xo;
-        };
-        auto rs = [&](int p) {
-            return reinterpret_cast<const E*>(
-                       base + Lt::R_OFF + (qr(p) % AR) * Lt::R_STEP) + ro;
-        };
-        auto bs = [&](int p) {
-            return reinterpret_cast<const float*>(
-                       base + Lt::B_OFF + (qr(p) % BR) * Lt::B_STEP) + bo;
-        };
         auto issue_x = [&](int p) {
-            const unsigned q = qx(p);
-            uint64_t* bar = &barx[q % XR];
+            uint64_t* bar = &barx[ix.slot];
             expect_tx(bar, Lt::X_BYTES);
-            tma3(base + Lt::X_OFF + (q % XR) * Lt::X_STEP, &tm_x, i0 - 4,
+            tma3(base + Lt::X_OFF + ix.slot * Lt::X_STEP, &tm_x, i0 - 4,
                  j0 - 2, p, bar);
+            ix.advance<XR>();
+            ++nix;
         };
         auto issue_r = [&](int p) {
-            const unsigned q = qr(p);
-            uint64_t* bar = &barr[q % AR];
+            uint64_t* bar = &barr[ir.slot];
             expect_tx(bar, Lt::R_BYTES + Lt::B_BYTES);
-            tma4(base + Lt::R_OFF + (q % AR) * Lt::R_STEP, &tm_r, i0 - H,
+            tma4(base + Lt::R_OFF + ir.slot * Lt::R_STEP, &tm_r, i0 - H,
                  j0 - 2, p, 0, bar);
-            tma3(base + Lt::B_OFF + (q % BR) * Lt::B_STEP, &tm_b, i0 - 4,
+            tma3(base + Lt::B_OFF + ir.slot * Lt::B_STEP, &tm_b, i0 - 4,
                  j0 - 1, p, bar);
+            ir.advance<AR>();
+            ++nir;
         };
-        auto wait_x = [&](int p) {  // after one timeout, wait no more
-            const unsigned q = qx(p);
-            if (!ZERO && !bad && !tc::mbar_wait(&barx[q % XR], (q / XR) & 1u))
-                bad = true;
+        // Waits for the next staged plane of a ring and returns its slot;
+        // after one timeout, waits no more.
+        auto wait_x = [&]() {
+            const int s = wx.slot;
+            if (!bad && !tc::mbar_wait(&barx[s], wx.phase)) bad = true;
+            wx.advance<XR>();
+            return s;
         };
-        auto wait_r = [&](int p) {
-            const unsigned q = qr(p);
-            if (!bad && !tc::mbar_wait(&barr[q % AR], (q / AR) & 1u))
-                bad = true;
+        auto wait_r = [&]() {
+            const int s = wr.slot;
+            if (!bad && !tc::mbar_wait(&barr[s], wr.phase)) bad = true;
+            wr.advance<AR>();
+            return s;
+        };
+        auto xs = [&](int slot) {
+            return reinterpret_cast<const float*>(base + Lt::X_OFF +
+                                                  slot * Lt::X_STEP) + xo;
+        };
+        auto rs = [&](int slot) {
+            return reinterpret_cast<const E*>(base + Lt::R_OFF +
+                                              slot * Lt::R_STEP) + ro;
+        };
+        auto bs = [&](int slot) {
+            return reinterpret_cast<const float*>(base + Lt::B_OFF +
+                                                  slot * Lt::B_STEP) + bo;
         };
 
         __syncthreads();  // the previous run's reads of every ring are done
         if (tid == 0) {
-            for (int p = t0; p <= min(k1 + 1, t0 + 1 + D); ++p)
-                if (!ZERO) issue_x(p);
-            for (int p = t0 - 1; p <= min(k1, t0 + D); ++p) issue_r(p);
+            if (!ZERO)
+                for (int p = t0; p <= min(k1 + 1, t0 + 1 + D); ++p) issue_x(p);
+            for (int p = t0; p <= min(k1, t0 + D); ++p) issue_r(p);
         }
-        wait_x(t0);
-        wait_x(t0 + 1);
-        wait_r(t0 - 1);
-        wait_r(t0);
-
+        // Prologue: x of planes t0 and t0+1 at the own group and the front
+        // coefficients of plane t0 into registers.
+        float4 xc = make_float4(0.f, 0.f, 0.f, 0.f);  // x(t+1), own group
+        float4 xp = xc;                                // x(t), own group
+        int sx1 = 0;                                   // slot of x(t+1)
+        if (!ZERO) {
+            const int s0 = wait_x();
+            sx1 = wait_x();
+            xp = lds4(xs(s0));
+            xc = lds4(xs(sx1));
+        }
+        float4 ffp = El::ld4(rs(wait_r()) + 3 * RC);  // front coeff. of t
+        // Pair of the first step (offsets of plane t0+1's first colour).
+        const int e0 = (first + gj + t0 + 1) & 1;
+        float xbA = sel(e0, xp.x, xp.y), xbB = sel(e0, xp.z, xp.w);
+        PairRows sp{};  // second-colour rows of plane t (set one step ahead)
         float2 fm = make_float2(0.f, 0.f);  // own F results of plane t-1
         float2 f0 = make_float2(0.f, 0.f);  // own F results of plane t
         for (int t = t0; t < k1; ++t) {
@@ -355,19 +318,49 @@ __global__ void __launch_bounds__(BLOCK, 1)
                 if (!ZERO && t + 2 + D <= k1 + 1) issue_x(t + 2 + D);
                 if (t + 1 + D <= k1) issue_r(t + 1 + D);
             }
-            wait_x(t + 2);
-            wait_r(t + 1);
+            const int sx2 = ZERO ? 0 : wait_x();
+            const int sr1 = wait_r();
 
             // (1) F cells of plane t+1 (offsets e and e+2 of the group).
             const int p1 = t + 1;
             const int e = (first + gj + p1) & 1;
+            const E* R1 = rs(sr1);
+            const float4 cc = El::ld4(R1);
+            const float4 rr = El::ld4(R1 + RC);
+            const float rl = El::ld1(R1 + RC - 1);
+            const float4 uu = El::ld4(R1 + 2 * RC);
+            const float4 ud = El::ld4(R1 + 2 * RC - RW);
+            const float4 ff = El::ld4(R1 + 3 * RC);
+            const float4 bb = lds4(bs(sr1));
+            float4 xf = make_float4(0.f, 0.f, 0.f, 0.f);  // x(t+2), own group
             float2 f1 = make_float2(0.f, 0.f);
+            if (!ZERO) xf = lds4(xs(sx2));
             if (gv && p1 >= 0 && p1 < n.z) {
-                const float* X0 = ZERO ? nullptr : xs(t);
-                const float* X1 = ZERO ? nullptr : xs(t + 1);
-                const float* X2 = ZERO ? nullptr : xs(t + 2);
-                f1 = f_cells<ZERO, E>(e, X0, X1, X2, rs(t + 1), rs(t),
-                                      bs(t + 1), omega);
+                const float cA = sel(e, cc.x, cc.y), cB = sel(e, cc.z, cc.w);
+                const float bA = sel(e, bb.x, bb.y), bB = sel(e, bb.z, bb.w);
+                if (ZERO) {
+                    f1 = make_float2(omega * __fdividef(bA, cA),
+                                     omega * __fdividef(bB, cB));
+                } else {
+                    const float* X1 = xs(sx1);
+                    const float xl = X1[-1], xr = X1[4];
+                    const float4 xd = lds4(X1 - XW), xu = lds4(X1 + XW);
+                    const float accA = sel(e, rl, rr.x) * sel(e, xl, xc.x) +
+                                       sel(e, rr.x, rr.y) * sel(e, xc.y, xc.z) +
+                                       sel(e, ud.x, ud.y) * sel(e, xd.x, xd.y) +
+                                       sel(e, uu.x, uu.y) * sel(e, xu.x, xu.y) +
+                                       sel(e, ffp.x, ffp.y) * xbA +
+                                       sel(e, ff.x, ff.y) * sel(e, xf.x, xf.y);
+                    const float accB = sel(e, rr.y, rr.z) * sel(e, xc.y, xc.z) +
+                                       sel(e, rr.z, rr.w) * sel(e, xc.w, xr) +
+                                       sel(e, ud.z, ud.w) * sel(e, xd.z, xd.w) +
+                                       sel(e, uu.z, uu.w) * sel(e, xu.z, xu.w) +
+                                       sel(e, ffp.z, ffp.w) * xbB +
+                                       sel(e, ff.z, ff.w) * sel(e, xf.z, xf.w);
+                    f1 = make_float2(
+                        w1 * sel(e, xc.x, xc.y) + omega * __fdividef(bA - accA, cA),
+                        w1 * sel(e, xc.z, xc.w) + omega * __fdividef(bB - accB, cB));
+                }
             }
             if (worker) {
                 float4 o;
@@ -378,12 +371,26 @@ __global__ void __launch_bounds__(BLOCK, 1)
                 *reinterpret_cast<float4*>(yfb + (p1 & 1) * FR * XW + bo) = o;
             }
 
-            // (2) S cells of plane t (the offsets of F in planes t+-1).
+            // (2) S cells of plane t: the same offsets e, e+2.
             if (tile_thr && gv && t >= k0) {
                 const float* Y = yfb + (t & 1) * FR * XW + bo;
-                const float* X0 = ZERO ? nullptr : xs(t);
-                const float2 sv = s_cells<ZERO, E>(e, Y, fm, f1, rs(t),
-                                                   rs(t - 1), bs(t), X0, omega);
+                const float4 yc = lds4(Y);
+                const float yl = Y[-1], yr = Y[4];
+                const float4 yd = lds4(Y - XW), yu = lds4(Y + XW);
+                const float accA = sp.l[0] * sel(e, yl, yc.x) +
+                                   sp.r[0] * sel(e, yc.y, yc.z) +
+                                   sp.d[0] * sel(e, yd.x, yd.y) +
+                                   sp.u[0] * sel(e, yu.x, yu.y) +
+                                   sp.k[0] * fm.x + sp.f[0] * f1.x;
+                const float accB = sp.l[1] * sel(e, yc.y, yc.z) +
+                                   sp.r[1] * sel(e, yc.w, yr) +
+                                   sp.d[1] * sel(e, yd.z, yd.w) +
+                                   sp.u[1] * sel(e, yu.z, yu.w) +
+                                   sp.k[1] * fm.y + sp.f[1] * f1.y;
+                const float xA = ZERO ? 0.f : xbA, xB = ZERO ? 0.f : xbB;
+                const float2 sv = make_float2(
+                    w1 * xA + omega * __fdividef(sp.b[0] - accA, sp.c[0]),
+                    w1 * xB + omega * __fdividef(sp.b[1] - accB, sp.c[1]));
                 float4 o;  // F of plane t sits at offsets 1-e and 3-e
                 o.x = e ? f0.x : sv.x;
                 o.y = e ? sv.x : f0.x;
@@ -392,18 +399,44 @@ __global__ void __launch_bounds__(BLOCK, 1)
                 *reinterpret_cast<float4*>(xout + ((size_t)sz * t + gi +
                                                    (size_t)n.x * gj)) = o;
             }
+
+            // Carry plane t+1 to the next step: its second-colour cells are
+            // the offsets s = 1-e.
+            const int s = 1 - e;
+            sp.c[0] = sel(s, cc.x, cc.y);
+            sp.c[1] = sel(s, cc.z, cc.w);
+            sp.l[0] = sel(s, rl, rr.x);
+            sp.r[0] = sel(s, rr.x, rr.y);
+            sp.l[1] = sel(s, rr.y, rr.z);
+            sp.r[1] = sel(s, rr.z, rr.w);
+            sp.d[0] = sel(s, ud.x, ud.y);
+            sp.d[1] = sel(s, ud.z, ud.w);
+            sp.u[0] = sel(s, uu.x, uu.y);
+            sp.u[1] = sel(s, uu.z, uu.w);
+            sp.f[0] = sel(s, ff.x, ff.y);
+            sp.f[1] = sel(s, ff.z, ff.w);
+            sp.k[0] = sel(s, ffp.x, ffp.y);
+            sp.k[1] = sel(s, ffp.z, ffp.w);
+            sp.b[0] = sel(s, bb.x, bb.y);
+            sp.b[1] = sel(s, bb.z, bb.w);
+            xbA = sel(s, xc.x, xc.y);
+            xbB = sel(s, xc.z, xc.w);
+            xc = xf;
+            ffp = ff;
+            sx1 = sx2;
             fm = f0;
             f0 = f1;
         }
-        seq += (unsigned)(k1 - t0 + 2);
     }
     if (bad) {
         err[0] = 1.0;
-        // Let every copy this block issued land before the block exits.
+        // Let every copy this block issued land before the block exits: the
+        // last XR (AR) copies of a ring are the only ones that can still be
+        // in flight; wait (bounded) for the latest phase of each.
         if (tid == 0) {
-            for (unsigned q = seq > (unsigned)XR ? seq - XR : 0u; q < seq; ++q)
-                if (!ZERO) tc::mbar_wait(&barx[q % XR], (q / XR) & 1u);
-            for (unsigned q = seq > (unsigned)AR ? seq - AR : 0u; q < seq; ++q)
+            for (unsigned q = nix > (unsigned)XR ? nix - XR : 0u; q < nix; ++q)
+                tc::mbar_wait(&barx[q % XR], (q / XR) & 1u);
+            for (unsigned q = nir > (unsigned)AR ? nir - AR : 0u; q < nir; ++q)
                 tc::mbar_wait(&barr[q % AR], (q / AR) & 1u);
         }
     }
