@@ -67,6 +67,8 @@ def parse_args():
                     help="skip the blocked pressure solver leg")
     ap.add_argument("--no-smoke", action="store_true",
                     help="skip the 512^3 smoke-plume projection")
+    ap.add_argument("--flip-frames", type=int, default=30,
+                    help="timed frames of the 256^3 FLIP dam break")
     ap.add_argument("--no-accuracy", action="store_true",
                     help="skip the accuracy block (pressure rel-L2 and "
                          "divergence against an FP64 answer)")
@@ -319,9 +321,14 @@ def run_ours(args, rank, world, local, pg):
         if VARIANTS[name][1] == "learned":
             variants[name]["multigrid_fallback_used"] = bool(r["fallback"])
         results[name] = (solver, r, ok)
-    # Headline: the fastest variant that reached the tolerance.
-    head = min((k for k in results if results[k][2]),
-               key=lambda k: results[k][1]["ms"])
+    # Headline: plain MGPCG, the method the metric measures the learned
+    # variant against (the other variants are in `variants`); the fastest
+    # variant that reached the tolerance if plain was not run.
+    if "plain_mgpcg" in results and results["plain_mgpcg"][2]:
+        head = "plain_mgpcg"
+    else:
+        head = min((k for k in results if results[k][2]),
+                   key=lambda k: results[k][1]["ms"])
     solver, r, _ = results[head]
     for k, (s_, _, _) in results.items():
         if k != head:
@@ -491,23 +498,28 @@ def run_accuracy(args, local, names):
     return result
 
 
-def run_flip(args, local, variant: str, frames: int):
+def run_flip(args, local, variant: str, frames: int, small: bool = True):
     """Whole FLIP frames on the GPU (jetgpu_flip_substep_device under the
     reference's adaptive sub-stepping): the 256^3 dam break with the static
     sphere obstacle (water box [0,.3]x[0,.8]x[0,1], 8 particles per cell
     from seed 2, sphere r = .15 at (.6,.2,.5)) for `frames` frames of 1/60 s
     after one warm-up frame, and the 64^3 dam break (box [0,.25]x[0,.75]x
     [0,1], seed 0, closed box) for 60 frames. CUDA events on the library
-    stream; the particles never leave the device."""
+    stream; the particles never leave the device. The pressure projections
+    of the timed frames are also timed one by one (SolveStats.setup_ms +
+    solve_ms: CUDA events around the weights, system and MGPCG kernels of
+    each solve) and averaged over the run's solves."""
     import numpy as np
     import torch
     import jetgpu
     from jetgpu import scenes
     dev = torch.device("cuda", local)
     out = {}
-    for tag, n, box, seed, sphere, nframes, warm in (
-            ("flip_256", args.n, (0.3, 0.8, 1.0), 2, True, frames, 1),
-            ("flip_64_dam_break", 64, (0.25, 0.75, 1.0), 0, False, 60, 0)):
+    legs = [("flip_256", args.n, (0.3, 0.8, 1.0), 2, True, frames, 1)]
+    if small:
+        legs.append(("flip_64_dam_break", 64, (0.25, 0.75, 1.0), 0, False,
+                     60, 0))
+    for tag, n, box, seed, sphere, nframes, warm in legs:
         prec, _ = VARIANTS[variant]
         ps = jetgpu.FdmMgpcgSolver3(**solver_params(prec, "multigrid"),
                                     device=local)
@@ -541,6 +553,7 @@ def run_flip(args, local, variant: str, frames: int):
         e0 = torch.cuda.Event(enable_timing=True)
         e1 = torch.cuda.Event(enable_timing=True)
         s0 = sim.subSteps
+        p0, i0 = sim.pressureMs, sim.pressureIterations
         torch.cuda.synchronize()
         e0.record(stream)
         for _ in range(nframes):
@@ -555,6 +568,9 @@ def run_flip(args, local, variant: str, frames: int):
             "ms_per_substep": round(ms / max(subs, 1), 3),
             "substeps_per_s": round(1000.0 * subs / ms, 2),
             "pressure_iterations_last": sim.lastStats.iterations,
+            "pressure_ms_per_solve": round((sim.pressureMs - p0) / max(subs, 1), 3),
+            "pressure_iterations_per_solve": round(
+                (sim.pressureIterations - i0) / max(subs, 1), 2),
             "solver": variant, "collider": "sphere" if sphere else "none",
         }
         if kernels is not None:
@@ -564,7 +580,7 @@ def run_flip(args, local, variant: str, frames: int):
     return out
 
 
-def run_smoke(args, local, variant: str, steps: int = 3):
+def run_smoke(args, local, variant: str, steps: int = 3, cpu: bool = False):
     """The projection of the 512^3 buoyant smoke plume (GridSmokeSolver3:
     all fluid, closed box; the source sphere r = .05 at (.5,.1,.5) pushing
     upward), one device-resident pressure solve per step to the same 1e-6
@@ -619,7 +635,40 @@ def run_smoke(args, local, variant: str, steps: int = 3):
            "setup_ms": round(stats.setup_ms, 3), "solver": variant,
            "system": "all fluid, closed box (pure Neumann)"}
     solver.close()
+    if cpu and not args.no_cpu_baseline:
+        res["cpu_reference"] = smoke_cpu_sample(n)
     return res
+
+
+def smoke_cpu_sample(n: int, iterations: int = 2):
+    """A bounded sample of the reference's CPU solve of the same 512^3
+    smoke projection on all host cores: weights, system build and the first
+    `iterations` MGPCG iterations of FdmMgpcgSolver3(., 5, 5, 5, 20, 20,
+    1e-6, 1.5, true) (the whole solve takes minutes at this size)."""
+    import numpy as np
+    import oracle
+    o, kind, threads = cpu_reference()
+    h = 1.0 / n
+    c = (np.arange(n) + 0.5) * h
+    yf = np.arange(n + 1) * h
+    v = ((c[None, None, :] - 0.5) ** 2 + (yf[None, :, None] - 0.1) ** 2 +
+         (c[:, None, None] - 0.5) ** 2 < 0.05 ** 2).astype(np.float64)
+    v[:, 0, :] = 0
+    v[:, -1, :] = 0
+    u = np.zeros((n, n, n + 1))
+    w = np.zeros((n + 1, n, n))
+    kmax = float(np.finfo(np.float64).max)
+    prm = dict(REF_PARAMS, max_cg_iter=iterations)
+    t = time.perf_counter()
+    r = o.pressure_solve((n,) * 3, (h,) * 3, (0, 0, 0), u, v, w, kmax, -kmax,
+                         oracle.MgParams(**prm))
+    dt = time.perf_counter() - t
+    return {"grid": n, "ms": round(dt * 1e3, 1), "cores": threads,
+            "kind": kind, "iterations": r["iters"],
+            "residual_norm": r["resid"],
+            "sample": f"weights + system build + the first {iterations} "
+                      f"MGPCG iterations of one {n}^3 reference solve "
+                      "(FdmMgpcgSolver3(100,5,5,5,20,20,1e-6,1.5,true))"}
 
 
 def run_blocked(args, local, variant: str, steps: int = 5, cpu: bool = True):
@@ -806,10 +855,17 @@ def main():
         accuracy = run_accuracy(args, local, r["variants"].keys())
     flip = None
     if not args.no_flip:
-        flip = run_flip(args, local, r["head"], frames=3)
+        # The 256^3 dam break for 30 frames with each MGPCG variant (the
+        # plain and the mixed-precision V-cycle), the 64^3 one for 60.
+        flip = {}
+        for name in ("plain_mgpcg", "mixed_mgpcg"):
+            res = run_flip(args, local, name, frames=args.flip_frames,
+                           small=name == r["head"])
+            for tag, val in res.items():
+                flip[tag if tag != "flip_256" else f"flip_256_{name}"] = val
     smoke = None
     if not args.no_smoke:
-        smoke = run_smoke(args, local, r["head"])
+        smoke = run_smoke(args, local, r["head"], cpu=rank == 0 and world == 1)
     blocked = None
     if not args.no_blocked:
         blocked = run_blocked(args, local, r["head"],

@@ -263,6 +263,9 @@ jetgpu_status solve_pressure_dev(
     jetgpu_status s = ensure_buffers(c, n, c->cfg.max_levels);
     if (s != JETGPU_OK) return s;
     const GridDesc g = to_desc(grid);
+    // Set-up and solve times come from events on the stream, so the host
+    // never waits between the set-up kernels and the solve.
+    JG_CUDA(c, cudaEventRecord(c->ev[0], c->stream));
     if (io) JG_CUDA(c, cudaStreamWaitEvent(c->stream, io->sdf_in, 0));
     s = blocked ? blocked_markers(c, g, to_desc(bsdf, bdata), to_desc(fsdf, fdata))
                 : build_weights(c, g, to_desc(bsdf, bdata), to_desc(fsdf, fdata));
@@ -286,13 +289,11 @@ jetgpu_status solve_pressure_dev(
         s = prepare_levels(c);
         if (s != JETGPU_OK) return s;
     }
-    JG_CUDA(c, cudaStreamSynchronize(c->stream));
-    const double setup = ms_since(t0);
-    auto t1 = std::chrono::steady_clock::now();
+    JG_CUDA(c, cudaEventRecord(c->ev[1], c->stream));
     jetgpu_status solve_status = mgpcg_solve(c, st);
     if (!usable(solve_status))
         return solve_status;
-    const double solve = ms_since(t1);
+    JG_CUDA(c, cudaEventRecord(c->ev[2], c->stream));
     if (io && io->host_p)
         JG_CUDA(c, cudaEventRecord(io->x_final, c->stream));
     // The reference applies the gradient whatever the solver returned
@@ -313,6 +314,9 @@ jetgpu_status solve_pressure_dev(
         JG_CUDA(c, cudaMemcpyAsync(op, c->x64, n.count() * sizeof(double),
                                    cudaMemcpyDeviceToDevice, c->stream));
     JG_CUDA(c, cudaStreamSynchronize(c->stream));
+    float setup = 0.0f, solve = 0.0f;
+    JG_CUDA(c, cudaEventElapsedTime(&setup, c->ev[0], c->ev[1]));
+    JG_CUDA(c, cudaEventElapsedTime(&solve, c->ev[1], c->ev[2]));
     st->levels = c->built_levels;
     st->setup_ms = setup;
     st->solve_ms = solve;
@@ -738,6 +742,11 @@ jetgpu_status jetgpu_get_level(jetgpu_ctx* c, int level, int what, void* dst,
             if (level != 0)
                 return fail(c, JETGPU_BAD_INPUT, "b is kept on level 0 only");
             src = c->b64; elems = s.count(); esize = 8; break;
+        case 6:
+            if (level != 0)
+                return fail(c, JETGPU_BAD_INPUT,
+                            "the pressure is kept on level 0 only");
+            src = c->x64; elems = s.count(); esize = 8; break;
         default:
             return fail(c, JETGPU_BAD_INPUT, "unknown field selector");
     }

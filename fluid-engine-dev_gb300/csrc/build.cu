@@ -1001,7 +1001,7 @@ TabLayout layout_of(const SampleTables& T) {
 }  // namespace
 
 jetgpu_status build_weights(Ctx* c, const GridDesc& g, const FieldDesc& bsdf,
-                            const FieldDesc& fsdf) {
+                            const FieldDesc& fsdf, bool pyramid) {
     const unsigned nl = c->built_levels;
     Level& L0 = c->levels[0];
     const Dims n = L0.n;
@@ -1049,6 +1049,12 @@ jetgpu_status build_weights(Ctx* c, const GridDesc& g, const FieldDesc& bsdf,
                 L0.ww, 2, fw, g, bsdf);
         }
     }
+    JG_CUDA(c, cudaGetLastError());
+    return pyramid ? build_pyramid(c) : JETGPU_OK;
+}
+
+jetgpu_status build_pyramid(Ctx* c) {
+    const unsigned nl = c->built_levels;
     Prof pyr(c, K_PYRAMID, 0.0);
     for (unsigned l = 1; l < nl; ++l) {
         const Level& F = c->levels[l - 1];

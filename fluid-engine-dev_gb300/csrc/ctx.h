@@ -279,8 +279,11 @@ inline int red_blocks(const Ctx* c, long n) {
 }
 
 // ---- build.cu -------------------------------------------------------------
+// The finest level's fluid SDF and face weights, then (with `pyramid`) the
+// coarser levels' (build_pyramid).
 jetgpu_status build_weights(Ctx* c, const GridDesc& g, const FieldDesc& bsdf,
-                            const FieldDesc& fsdf);
+                            const FieldDesc& fsdf, bool pyramid = true);
+jetgpu_status build_pyramid(Ctx* c);
 // Levels [lo, hi) of the hierarchy; only level 0 reads the velocities.
 jetgpu_status build_system(Ctx* c, const GridDesc& g, const double* u,
                            const double* v, const double* w,

@@ -929,6 +929,11 @@ class FlipSolver3:
         self.currentTimeInSeconds = 0.0
         self.subSteps = 0
         self.lastStats = SolveStats()
+        # Sum over sub-steps of the pressure projection's device time
+        # (weights, system and MGPCG solve: SolveStats.setup_ms + solve_ms,
+        # CUDA events around those kernels) and iterations.
+        self.pressureMs = 0.0
+        self.pressureIterations = 0
         # The library works on its own stream; torch's uploads and reads of
         # these tensors are ordered against it explicitly.
         self._stream = torch.cuda.ExternalStream(self.solver.stream(),
@@ -986,6 +991,17 @@ class FlipSolver3:
         self.synchronize()
         return self.pos.cpu().numpy()
 
+    def pressure(self) -> np.ndarray:
+        """The last sub-step's pressure ((nz, ny, nx); the reference's
+        GridFractionalSinglePhasePressureSolver3::pressure())."""
+        self.synchronize()
+        nx, ny, nz = self.resolution
+        out = np.zeros(nx * ny * nz)
+        cnt = C.c_size_t(0)
+        self.solver.check(library().jetgpu_get_level(
+            self.solver.context(), 0, 6, _p(out), out.nbytes, C.byref(cnt)))
+        return out.reshape(nz, ny, nx)
+
     def velocities(self) -> np.ndarray:
         self.synchronize()
         return self.vel.cpu().numpy()
@@ -1030,6 +1046,8 @@ class FlipSolver3:
             C.byref(self.params), float(dt), C.byref(self.lastStats))
         self.solver.check(st, allow=SOLVED)
         self.subSteps += 1
+        self.pressureMs += self.lastStats.setup_ms + self.lastStats.solve_ms
+        self.pressureIterations += self.lastStats.iterations
 
     def update(self, frameInterval: float):
         """One frame (PhysicsAnimation::onUpdate's adaptive branch)."""

@@ -130,8 +130,8 @@ typedef struct jetgpu_solve_stats {
     double residual;             /* ||b - A x||_2, FP64, reference operator */
     double relative_residual;    /* residual / ||b||_2 */
     double b_norm;               /* ||b||_2 */
-    double setup_ms;             /* weights + system build */
-    double solve_ms;             /* Krylov solve */
+    double setup_ms;             /* weights + system build (device time) */
+    double solve_ms;             /* Krylov solve (device time) */
     double total_ms;             /* whole call, including copies */
     int fallback_used;           /* learned preconditioner fell back */
 } jetgpu_solve_stats;
@@ -510,7 +510,9 @@ jetgpu_status jetgpu_g2p_pic(struct jetgpu_ctx* ctx, const jetgpu_grid* grid,
  * (grid_fractional_single_phase_pressure_solver3.h:103-115).
  * what: 0 fluid SDF (float, cells), 1/2/3 u/v/w weights (float, faces),
  *       4 matrix rows (4 doubles per cell; level 0 exact FP64, coarse levels
- *       as stored in FP32 and widened), 5 rhs b (doubles, level 0 only).
+ *       as stored in FP32 and widened), 5 rhs b (doubles, level 0 only),
+ *       6 the pressure of the last solve (doubles, level 0 only; after a
+ *       jetgpu_flip_substep_device, that sub-step's pressure).
  * Returns the element count via *count. */
 jetgpu_status jetgpu_get_level(struct jetgpu_ctx* ctx, int level, int what,
                                void* dst, size_t capacity, size_t* count);

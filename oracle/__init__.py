@@ -212,6 +212,11 @@ class Oracle:
             L.orc_flip_run.argtypes = [
                 C.POINTER(OrcGrid), C.c_long, _dp, _dp, C.c_int, C.c_double,
                 C.c_double, C.c_int, _dp, C.c_int, C.POINTER(OrcMgParams)]
+        if hasattr(L, "orc_flip_run_record"):
+            L.orc_flip_run_record.argtypes = [
+                C.POINTER(OrcGrid), C.c_long, _dp, _dp, C.c_int, C.c_double,
+                C.c_double, C.c_int, _dp, C.c_int, C.POINTER(OrcMgParams),
+                C.c_int, C.POINTER(C.c_int), _dp]
         if hasattr(L, "orc_quaternion_matrices"):
             L.orc_quaternion_matrices.argtypes = [_dp, _dp, _dp]
         if hasattr(L, "orc_sphere_collider_sdf"):
@@ -557,6 +562,29 @@ class Oracle:
                               int(closed), _ptr(gr), int(flip),
                               C.byref(prm))
         return pos, vel
+
+    def flip_run_record(self, res, spacing, origin, pos, vel, frames,
+                        record_frames, fps=60.0, max_cfl=5.0, closed=63,
+                        gravity=(0.0, -9.8, 0.0), flip=True,
+                        params: MgParams | None = None):
+        """flip_run that also returns the pressure solver's pressure() after
+        each frame count in `record_frames` (ascending, 1..frames):
+        (positions, velocities, pressures (len(record_frames), nz, ny,
+        nx))."""
+        g = self._grid(res, spacing, origin)
+        pos = np.ascontiguousarray(pos, np.float64).copy()
+        vel = np.ascontiguousarray(vel, np.float64).copy()
+        prm = (params or MgParams()).c()
+        gr = np.ascontiguousarray(gravity, np.float64)
+        rec = (C.c_int * len(record_frames))(*record_frames)
+        nx, ny, nz = res
+        p = np.zeros((len(record_frames), nz, ny, nx))
+        self.lib.orc_flip_run_record(C.byref(g), pos.shape[0], _ptr(pos),
+                                     _ptr(vel), int(frames), float(fps),
+                                     float(max_cfl), int(closed), _ptr(gr),
+                                     int(flip), C.byref(prm),
+                                     len(record_frames), rec, _ptr(p))
+        return pos, vel, p
 
     def sphere_collider_sdf(self, res, spacing, origin, centre, radius):
         """Reference harness only: the collider SDF the reference builds for

@@ -188,6 +188,14 @@ void orc_build_particle_sdf(const orc_grid* g, long np, const double* pos,
 void orc_flip_run(const orc_grid* g, long np, double* pos, double* vel,
                   int frames, double fps, double max_cfl, int closed,
                   const double gravity[3], int flip, const orc_mg_params* p);
+/* orc_flip_run that also copies the pressure solver's pressure() (the last
+ * sub-step's pressure, cells) after each frame listed in rec_frames (frame
+ * counts 1..frames, ascending) into p_out (nrec x cells). */
+void orc_flip_run_record(const orc_grid* g, long np, double* pos, double* vel,
+                         int frames, double fps, double max_cfl, int closed,
+                         const double gravity[3], int flip,
+                         const orc_mg_params* p, int nrec,
+                         const int* rec_frames, double* p_out);
 
 /* Reference harness only: Transform3's orientation matrix and its inverse
  * for quaternion q = (w, x, y, z), row-major. */

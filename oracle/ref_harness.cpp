@@ -695,6 +695,15 @@ void orc_apic_g2p(const orc_grid* g, long np, const double* pos, double* vel,
 void orc_flip_run(const orc_grid* g, long np, double* pos, double* vel,
                   int frames, double fps, double max_cfl, int closed,
                   const double gravity[3], int flip, const orc_mg_params* p) {
+    orc_flip_run_record(g, np, pos, vel, frames, fps, max_cfl, closed,
+                        gravity, flip, p, 0, nullptr, nullptr);
+}
+
+void orc_flip_run_record(const orc_grid* g, long np, double* pos, double* vel,
+                         int frames, double fps, double max_cfl, int closed,
+                         const double gravity[3], int flip,
+                         const orc_mg_params* p, int nrec,
+                         const int* rec_frames, double* p_out) {
     Logging::mute();
     const Size3 res(g->res[0], g->res[1], g->res[2]);
     const Vector3D h(g->spacing[0], g->spacing[1], g->spacing[2]);
@@ -723,8 +732,17 @@ void orc_flip_run(const orc_grid* g, long np, double* pos, double* vel,
         p->coarsest_iter, p->final_iter, p->tolerance, p->sor,
         p->red_black != 0));
     s->setPressureSolver(ps);
-    for (Frame frame(0, 1.0 / fps); frame.index < frames; ++frame)
+    const size_t cells = res.x * res.y * res.z;
+    int next = 0;
+    for (Frame frame(0, 1.0 / fps); frame.index < frames; ++frame) {
         s->update(frame);
+        if (next < nrec && rec_frames[next] == frame.index + 1) {
+            const FdmVector3& pr = ps->pressure();
+            std::memcpy(p_out + cells * next, pr.data(),
+                        sizeof(double) * cells);
+            ++next;
+        }
+    }
     auto pp = s->particleSystemData()->positions();
     auto vv = s->particleSystemData()->velocities();
     for (long i = 0; i < np; ++i)

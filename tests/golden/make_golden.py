@@ -38,6 +38,11 @@ Every fixture holds inputs and the reference's outputs for one small case:
   FdmMgpcgSolver3 at tolerance 1e-10, advection) for 3 frames of 1/60 s on
   the 64^3 dam break's geometry at 24^3 (water box [0,.25]x[0,.75]x[0,1],
   8 particles per cell from seed 0, closed walls, gravity (0,-9.8,0)).
+* flip_dam_break_64.npz — FlipSolver3 for BASELINE config 1 at its own
+  size: 64^3, 60 frames of the same dam break (393,216 particles), pressure
+  to an absolute 1e-10; the pressure after frames 1, 10, 30 and 60
+  (float32), every 16th particle's final position and velocity, and the
+  mean / standard deviation of all final positions.
 * apic_20x12x16.npz — ApicSolver3's transfers for 2,000 particles (some
   outside the box) on an anisotropic grid: P2G with random affine matrices,
   G2P from a random grid; and ApicSolver3 for 3 frames of the 24^3 dam break
@@ -361,6 +366,44 @@ def flip_dam_break(ref):
          pic_vel=pv)
 
 
+# Frames after which the 64^3 dam break's pressure is kept, and the particle
+# stride of the kept final positions (the whole set is 393,216 particles).
+DAM64_FRAMES = (1, 10, 30, 60)
+DAM64_STRIDE = 16
+
+
+def dam64_pressure(pr):
+    """The kept pressure fields in float32, with the values of air cells
+    (|p| below 1e-9 of the frame's maximum: what the solve leaves in the
+    identity rows) set to zero so that the fixture compresses."""
+    out = pr.astype(np.float32)
+    for f in range(out.shape[0]):
+        small = np.abs(pr[f]) < 1e-9 * np.abs(pr[f]).max()
+        out[f][small] = 0.0
+    return out
+
+
+def flip_dam_break_64(ref):
+    """BASELINE config 1 at its own size: FlipSolver3, 64^3 over the unit
+    cube, the water box [0,.25]x[0,.75]x[0,1] at 8 particles per cell from
+    seed 0, gravity (0,-9.8,0), closed walls, maxCfl 5, 60 frames of 1/60 s,
+    the pressure solved with FdmMgpcgSolver3 to an absolute 1e-10. Kept: the
+    pressure after frames DAM64_FRAMES (float32), every DAM64_STRIDE-th
+    particle's final position and velocity, and the mean and standard
+    deviation of all final positions."""
+    n = 64
+    h = 1.0 / n
+    pos, vel = scenes.dam_break_particles(n, (0.25, 0.75, 1.0), seed=0)
+    p = oracle.MgParams(100, 5, 5, 5, 20, 20, 1e-10, 1.5, True)
+    fp, fv, pr = ref.flip_run_record((n, n, n), (h, h, h), (0, 0, 0), pos,
+                                     vel, 60, DAM64_FRAMES, params=p)
+    save("flip_dam_break_64.npz", frames=np.array(DAM64_FRAMES),
+         pressure=dam64_pressure(pr), stride=np.array(DAM64_STRIDE),
+         pos=fp[::DAM64_STRIDE], vel=fv[::DAM64_STRIDE],
+         pos_mean=fp.mean(axis=0), pos_std=fp.std(axis=0),
+         count=np.array(fp.shape[0]))
+
+
 def apic(ref):
     res = (20, 12, 16)
     nx, ny, nz = res
@@ -406,6 +449,10 @@ def main():
         raise SystemExit("the reference harness is required (reference sources "
                          "not found)")
     ref.set_threads(0)
+    if len(sys.argv) > 1:  # named cases only
+        for name in sys.argv[1:]:
+            globals()[name](ref)
+        return
     kat_free_surface(ref)
     sphere_union(ref)
     noncubic(ref)
@@ -417,6 +464,7 @@ def main():
     particles(ref)
     particle_sdf(ref)
     flip_dam_break(ref)
+    flip_dam_break_64(ref)
     apic(ref)
     rng_streams()
 
