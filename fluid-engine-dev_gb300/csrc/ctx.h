@@ -1,6 +1,8 @@
 // Host-side context of libjetgpu: device buffers, stream, launch helpers.
 #pragma once
 
+#include <cuda.h>
+#include <cudaTypedefs.h>
 #include <cuda_runtime.h>
 #include <cuda_bf16.h>
 
@@ -309,6 +311,8 @@ jetgpu_status blocked_gradient(Ctx* c, const GridDesc& g, const double* u,
                                double* ov, double* ow);
 
 // ---- mgpcg.cu -------------------------------------------------------------
+// The driver's cuTensorMapEncodeTiled (null when the driver lacks it).
+PFN_cuTensorMapEncodeTiled_v12000 tma_encoder();
 // Allocates the multigrid hierarchy and solver buffers for resolution n.
 jetgpu_status ensure_buffers(Ctx* c, Dims n, unsigned max_levels);
 // Derives FP32 (and BF16) matrices of levels [lo, hi) from the built system.

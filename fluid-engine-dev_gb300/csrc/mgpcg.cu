@@ -1051,20 +1051,6 @@ template <> struct TmaCfg<RowsB> {
     static constexpr int MINB = 4;
 };
 
-PFN_cuTensorMapEncodeTiled_v12000 tma_encoder() {
-    static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
-        void* p = nullptr;
-        cudaDriverEntryPointQueryResult q;
-        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p,
-                                             12000, cudaEnableDefault,
-                                             &q) != cudaSuccess ||
-            q != cudaDriverEntryPointSuccess)
-            p = nullptr;
-        return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
-    }();
-    return fn;
-}
-
 bool tma_ok(const Ctx* c, const Level& L) {
     return c->tma_blocks_per_sm[mixed(c) ? 1 : 0] > 0 && L.n.x % 8 == 0 &&
            L.n.x >= 64;
@@ -1274,6 +1260,20 @@ jetgpu_status read_scalars(Ctx* c) {
 }
 
 }  // namespace
+
+PFN_cuTensorMapEncodeTiled_v12000 tma_encoder() {
+    static PFN_cuTensorMapEncodeTiled_v12000 fn = [] {
+        void* p = nullptr;
+        cudaDriverEntryPointQueryResult q;
+        if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p,
+                                             12000, cudaEnableDefault,
+                                             &q) != cudaSuccess ||
+            q != cudaDriverEntryPointSuccess)
+            p = nullptr;
+        return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    }();
+    return fn;
+}
 
 unsigned level_count(Dims n, unsigned max_levels) {
     unsigned i = 1;

@@ -177,12 +177,272 @@ __global__ void __launch_bounds__(128) k_conv3d_tc(ConvArgs a) {
     if (warp == 0) tc::tmem_dealloc(tmem, ncols);
 }
 
+// ---------------------------------------------------------------------------
+// K15 on rows of 128 cells (nx a multiple of 128): the input brick of a tile
+// staged once, all 27 taps read from it.
+//
+// A persistent CTA takes output tiles of 128 consecutive cells along i (one
+// (j, k) row segment, the MMA's M). Per tile and per chunk of 16 input
+// channels, one thread stages the brick the tile's 27 taps read — cells
+// i0-1 .. i0+128 of rows j-1 .. j+1 of planes k-1 .. k+1 — with two TMA
+// copies (channels 0-7 and 8-15 of the chunk; cells outside the grid arrive
+// as zeros, which is the convolution's zero padding). In shared memory each
+// copy is a run of 16-byte cells, so the A operand of tap (dx, dy, dz) is
+// the same run started at that tap's cell offset: 128 consecutive rows 16
+// bytes apart (8-row core matrices 128 bytes apart), the two channel halves
+// one copy apart. The CTA's weights, all taps and channels, are loaded once
+// into shared memory as K-major B tiles. Bricks are double-buffered: the
+// copy of the next chunk (or of the next tile's first chunk) runs under the
+// MMAs of the current one. Accumulators in TMEM (128 lanes x C_out FP32
+// columns); the epilogue adds the bias, applies the ReLU and stores BF16 or
+// FP32 rows of the channels-last output.
+
+constexpr int kBrickX = 130;                  // cells i0-1 .. i0+128
+constexpr int kBrickCells = kBrickX * 3 * 3;  // rows j-1..j+1, planes k-1..k+1
+constexpr uint32_t kHalfBytes = 18816;        // 16 B x 1170 cells, 128-aligned
+static_assert(kHalfBytes >= 16u * kBrickCells && kHalfBytes % 128u == 0u,
+              "brick half");
+
+__host__ __device__ inline size_t brick_weight_bytes(int ci, int co) {
+    return (size_t)27 * co * ci * 2;
+}
+__host__ __device__ inline size_t brick_smem_bytes(int ci, int co) {
+    // weights | 2 stages x 2 channel halves | barriers, TMEM slot; plus
+    // alignment slack for the 128-byte aligned base
+    return brick_weight_bytes(ci, co) + 4 * (size_t)kHalfBytes + 64 + 128;
+}
+
+struct BrickArgs {
+    const __nv_bfloat16* w;  // [27][co][ci]
+    const float* bias;       // [co] or null
+    __nv_bfloat16* out;      // [V][co] or null
+    float* out32;            // [V][co] or null
+    Dims n;
+    int ci, co, relu;
+    unsigned* err;
+};
+
+__global__ void __launch_bounds__(128)
+    k_conv3d_brick(const __grid_constant__ CUtensorMap tm_in, BrickArgs a) {
+    extern __shared__ unsigned char smem_raw[];
+    unsigned char* base = reinterpret_cast<unsigned char*>(
+        (reinterpret_cast<uintptr_t>(smem_raw) + 127) & ~uintptr_t(127));
+    const int ci = a.ci, co = a.co, nk = ci / 16;
+    unsigned char* W = base;
+    unsigned char* brick = base + brick_weight_bytes(ci, co);
+    uint64_t* full = reinterpret_cast<uint64_t*>(brick + 4 * kHalfBytes);
+    uint64_t* empty = full + 2;
+    uint64_t* accf = full + 4;
+    uint32_t* tslot = reinterpret_cast<uint32_t*>(full + 5);
+    const int tid = threadIdx.x, warp = tid >> 5;
+    const int tx = a.n.x / 128;
+    const long ntiles = (long)tx * a.n.y * a.n.z;
+    uint32_t ncols = 32;
+    while (ncols < (uint32_t)co) ncols <<= 1;
+
+    if (warp == 0) tc::tmem_alloc(tslot, ncols);
+    if (tid == 0) {
+        for (int q = 0; q < 5; ++q) tc::mbar_init(&full[q], 1);
+        asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    }
+    // Weights, K-major B tiles per (chunk, tap): [kc][t][half][co][8 ch].
+    {
+        const int groups = ci / 8;
+        const long pieces = 27L * co * groups;
+        for (long q = tid; q < pieces; q += 128) {
+            const int g = (int)(q % groups);
+            const long tn = q / groups;
+            const int nn = (int)(tn % co), t = (int)(tn / co);
+            const uint4 v = __ldg(reinterpret_cast<const uint4*>(
+                a.w + ((long)t * co + nn) * ci + 8 * g));
+            const long off = ((((long)(g >> 1) * 27 + t) * 2 + (g & 1)) * co + nn) * 16;
+            *reinterpret_cast<uint4*>(W + off) = v;
+        }
+    }
+    tc::fence_proxy_async();  // generic-proxy writes seen by the MMAs
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    const uint32_t tmem = *tslot;
+    const uint32_t idesc = tc::idesc_bf16_f32(128, co);
+    const uint32_t wbase = tc::smem_u32(W), bbase = tc::smem_u32(brick);
+    const uint32_t wstep = (uint32_t)co * 32u;  // one (chunk, tap) B tile
+    bool ok = true;
+
+    // Chunk q of this CTA's sequence: tile blockIdx.x + (q / nk) * gridDim.x,
+    // input channels 16 (q % nk) ...
+    const long my_tiles = ntiles > blockIdx.x
+        ? (ntiles - 1 - blockIdx.x) / gridDim.x + 1 : 0;
+    const long nq = my_tiles * nk;
+    auto issue = [&](long q) {
+        const long tile = blockIdx.x + (q / nk) * (long)gridDim.x;
+        const int kc = (int)(q % nk);
+        const int i0 = (int)(tile % tx) * 128;
+        const long r = tile / tx;
+        const int j = (int)(r % a.n.y), k = (int)(r / a.n.y);
+        const int st = (int)(q & 1);
+        uint64_t* bar = &full[st];
+        asm volatile(
+            "mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(
+                tc::smem_u32(bar)),
+            "r"(2u * 16u * kBrickCells)
+            : "memory");
+        for (int h = 0; h < 2; ++h) {
+            unsigned char* dst = brick + (st * 2 + h) * kHalfBytes;
+            asm volatile(
+                "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::"
+                "complete_tx::bytes [%0], [%1, {%2, %3, %4, %5}], [%6];\n" ::"r"(
+                    tc::smem_u32(dst)),
+                "l"(reinterpret_cast<uint64_t>(&tm_in)), "r"(16 * kc + 8 * h),
+                "r"(i0 - 1), "r"(j - 1), "r"(k - 1), "r"(tc::smem_u32(bar))
+                : "memory");
+        }
+    };
+    // Thread 0 stages bricks one chunk ahead of the MMAs; thread 32 issues
+    // the MMAs as each brick lands. A stage is reloaded once the MMAs of the
+    // chunk that last used it have completed (`empty`).
+    if (tid == 0 && nq > 0) issue(0);
+    long q0 = 0;  // first chunk of the current tile
+    for (long lt = 0; lt < my_tiles; ++lt, q0 += nk) {
+        const long tile = blockIdx.x + lt * (long)gridDim.x;
+        if (tid == 0) {
+            for (int kc = 0; kc < nk; ++kc) {
+                const long q = q0 + kc;
+                if (q + 1 < nq) {
+                    if (q >= 1)
+                        ok &= tc::mbar_wait(&empty[(q + 1) & 1],
+                                            (uint32_t)(((q - 1) >> 1) & 1));
+                    issue(q + 1);
+                }
+            }
+        } else if (tid == 32) {
+            tc::fence_after_sync();
+            for (int kc = 0; kc < nk; ++kc) {
+                const long q = q0 + kc;
+                ok &= tc::mbar_wait(&full[q & 1], (uint32_t)((q >> 1) & 1));
+                const uint32_t half0 = bbase + (uint32_t)(q & 1) * 2u * kHalfBytes;
+                for (int t = 0; t < 27; ++t) {
+                    const uint32_t cell =
+                        (uint32_t)((((t / 9) * 3 + (t / 3) % 3) * kBrickX) + t % 3);
+                    const uint64_t ad = tc::smem_desc(half0 + cell * 16u,
+                                                      kHalfBytes, 128);
+                    const uint64_t bd = tc::smem_desc(
+                        wbase + (uint32_t)(kc * 27 + t) * wstep, (uint32_t)co * 16u,
+                        128);
+                    tc::mma_bf16(tmem, ad, bd, idesc,
+                                 (kc > 0 || t > 0) ? 1u : 0u);
+                }
+                tc::mma_commit(&empty[q & 1]);
+            }
+            tc::mma_commit(accf);
+        }
+        __syncwarp();
+        ok &= tc::mbar_wait(accf, (uint32_t)(lt & 1));
+        __syncwarp();  // tcgen05.ld below is warp-collective
+        tc::fence_after_sync();
+        // Epilogue: warp w holds cells i0 + 32 w + lane.
+        const int i0 = (int)(tile % tx) * 128;
+        const long r = tile / tx;
+        const int j = (int)(r % a.n.y), k = (int)(r / a.n.y);
+        const long v = lin(i0 + 32 * warp + (tid & 31), j, k, a.n.x, a.n.y);
+        const uint32_t trow = tmem + ((uint32_t)(warp * 32) << 16);
+        for (int c0 = 0; c0 < co; c0 += 16) {
+            float val[16];
+            tc::tmem_ld16(trow + (uint32_t)c0, val);
+#pragma unroll
+            for (int qq = 0; qq < 16; ++qq) {
+                float x = val[qq] + (a.bias ? a.bias[c0 + qq] : 0.0f);
+                if (a.relu) x = fmaxf(x, 0.0f);
+                val[qq] = x;
+            }
+            if (a.out) {
+                __align__(16) __nv_bfloat16 hb[16];
+#pragma unroll
+                for (int qq = 0; qq < 16; ++qq) hb[qq] = __float2bfloat16_rn(val[qq]);
+                uint4* dst = reinterpret_cast<uint4*>(a.out + v * co + c0);
+                dst[0] = reinterpret_cast<const uint4*>(hb)[0];
+                dst[1] = reinterpret_cast<const uint4*>(hb)[1];
+            }
+            if (a.out32) {
+                float4* dst = reinterpret_cast<float4*>(a.out32 + v * co + c0);
+#pragma unroll
+                for (int qq = 0; qq < 4; ++qq)
+                    dst[qq] = make_float4(val[4 * qq], val[4 * qq + 1],
+                                          val[4 * qq + 2], val[4 * qq + 3]);
+            }
+        }
+        // The next tile's MMAs overwrite the accumulators.
+        tc::fence_before_sync();
+        __syncthreads();
+    }
+    if (!ok && a.err) atomicOr(a.err, 1u);
+    if (__syncthreads_or(!ok) && tid == 32 && nq > 0) {
+        // A wait gave up: let the last copies and MMAs land (bounded)
+        // before the CTA releases its shared memory and TMEM.
+        for (long q = nq >= 2 ? nq - 2 : 0; q < nq; ++q)
+            tc::mbar_wait(&full[q & 1], (uint32_t)((q >> 1) & 1));
+        tc::mbar_wait(accf, (uint32_t)((my_tiles - 1) & 1));
+    }
+    tc::fence_after_sync();
+    __syncthreads();
+    if (warp == 0) tc::tmem_dealloc(tmem, ncols);
+}
+
+// Tensor map of a channels-last BF16 activation [nz][ny][nx][ci] with the
+// brick box (8 channels x 130 x 3 x 3).
+bool brick_map(CUtensorMap* m, const __nv_bfloat16* in, int ci, Dims n) {
+    auto enc = tma_encoder();
+    if (!enc) return false;
+    cuuint64_t gd[4] = {(cuuint64_t)ci, (cuuint64_t)n.x, (cuuint64_t)n.y,
+                        (cuuint64_t)n.z};
+    cuuint64_t gs[3] = {(cuuint64_t)ci * 2, (cuuint64_t)n.x * ci * 2,
+                        (cuuint64_t)n.y * n.x * ci * 2};
+    cuuint32_t bx[4] = {8, (cuuint32_t)kBrickX, 3, 3}, es[4] = {1, 1, 1, 1};
+    return enc(m, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 4,
+               const_cast<__nv_bfloat16*>(in), gd, gs, bx, es,
+               CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+               CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+               CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+constexpr size_t kMaxConvSmem = 227 * 1024;
+
 }  // namespace
 
 jetgpu_status conv3d(cudaStream_t st, const __nv_bfloat16* in, int ci,
                      const __nv_bfloat16* w, const float* bias, int co,
                      Dims n, int relu, __nv_bfloat16* out, float* out32,
                      unsigned* err) {
+    // Rows of 128 cells and a CTA's weights within shared memory: the
+    // brick kernel; otherwise the per-tap gather kernel below.
+    const size_t bsmem = brick_smem_bytes(ci, co);
+    CUtensorMap tm;
+    if (n.x % 128 == 0 && bsmem <= kMaxConvSmem &&
+        (reinterpret_cast<uintptr_t>(in) & 15u) == 0 && brick_map(&tm, in, ci, n)) {
+        static DeviceOnce battr;
+        if (!battr.run([] {
+                return cudaFuncSetAttribute(
+                    k_conv3d_brick, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                    (int)kMaxConvSmem);
+            }))
+            return JETGPU_CUDA_ERROR;
+        int dev = 0, sms = 0, occ = 0;
+        if (cudaGetDevice(&dev) != cudaSuccess ||
+            cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) !=
+                cudaSuccess ||
+            cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_conv3d_brick,
+                                                          128, bsmem) !=
+                cudaSuccess)
+            return JETGPU_CUDA_ERROR;
+        if (occ < 1) occ = 1;
+        if (occ > 2) occ = 2;  // TMEM: <= 2 x 256 columns per SM
+        const long tiles = (long)(n.x / 128) * n.y * n.z;
+        long grid = (long)sms * occ;
+        if (grid > tiles) grid = tiles;
+        BrickArgs ba{w, bias, out, out32, n, ci, co, relu, err};
+        k_conv3d_brick<<<(unsigned)grid, 128, bsmem, st>>>(tm, ba);
+        return cudaGetLastError() == cudaSuccess ? JETGPU_OK : JETGPU_CUDA_ERROR;
+    }
     ConvArgs a{in, w, bias, out, out32, n, ci, co, relu, err};
     const size_t smem = conv_smem_bytes(ci, co);
     static DeviceOnce attr;

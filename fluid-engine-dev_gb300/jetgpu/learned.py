@@ -230,6 +230,174 @@ def harvest(solver: FdmMgpcgSolver3, sc: dict, n: int, pairs: int):
     return samples
 
 
+def device_scene(n: int, seed: int, device):
+    """The 16-sphere union scene of ``scenes.sphere_union_scene`` built on
+    the GPU (torch tensors): sphere centres and radii from the same
+    std::mt19937(seed) stream, the SDFs evaluated on the device. The face
+    velocities are U[-1, 1] from torch's generator seeded with `seed` (not
+    the reference's stream: training data only needs their distribution).
+    Returns dict(u, v, w, fluid_sdf, boundary_sdf)."""
+    torch = _torch()
+    rng = scenes.Mt19937Uniform(seed)
+    cs, rs = [], []
+    for _ in range(16):
+        cs.append(rng.uniform(0.2, 0.8, 3))
+        rs.append(rng.uniform(0.05, 0.2, 1)[0])
+    f64 = dict(dtype=torch.float64, device=device)
+    c = (torch.arange(n, **f64) + 0.5) / n
+    Z, Y, X = torch.meshgrid(c, c, c, indexing="ij")
+    fluid = torch.full((n, n, n), float("inf"), **f64)
+    for cc, r in zip(cs, rs):
+        d = torch.sqrt((X - cc[0]) ** 2 + (Y - cc[1]) ** 2 + (Z - cc[2]) ** 2) - r
+        fluid = torch.minimum(fluid, d)
+    walls = torch.minimum(torch.minimum(torch.minimum(X, 1 - X),
+                                        torch.minimum(Y, 1 - Y)),
+                          torch.minimum(Z, 1 - Z))
+    ball = torch.sqrt((X - 0.5) ** 2 + (Y - 0.3) ** 2 + (Z - 0.5) ** 2) - 0.15
+    gen = torch.Generator(device=device)
+    gen.manual_seed(int(seed))
+    u = torch.rand((n, n, n + 1), generator=gen, **f64) * 2 - 1
+    v = torch.rand((n, n + 1, n), generator=gen, **f64) * 2 - 1
+    w = torch.rand((n + 1, n, n), generator=gen, **f64) * 2 - 1
+    return dict(u=u, v=v, w=w, fluid_sdf=fluid.contiguous(),
+                boundary_sdf=torch.minimum(walls, ball).contiguous())
+
+
+def harvest_device(solver: FdmMgpcgSolver3, sc: dict, n: int, pairs: int):
+    """harvest() for a scene already on the device (device_scene): the
+    projection through jetgpu_solve_pressure_device, then `pairs` samples of
+    the MGPCG iterations on that system."""
+    torch = _torch()
+    from . import Grid, ScalarField, solve_pressure_device
+    L = library()
+    h = 1.0 / n
+    g = Grid()
+    g.res[:] = (n, n, n)
+    g.spacing[:] = (h, h, h)
+    g.origin[:] = (0.0, 0.0, 0.0)
+
+    def field(t):
+        f = ScalarField()
+        f.kind = 1
+        f.data = t.data_ptr()
+        f.res[:] = (n, n, n)
+        f.origin[:] = (0.5 * h,) * 3
+        f.spacing[:] = (h, h, h)
+        return f
+
+    out = [torch.empty_like(sc[k]) for k in ("u", "v", "w")]
+    torch.cuda.synchronize()
+    solve_pressure_device(solver, g, sc["u"], sc["v"], sc["w"],
+                          field(sc["boundary_sdf"]), field(sc["fluid_sdf"]),
+                          *out)
+    dev = sc["u"].device
+    N = n ** 3
+    R = torch.empty((pairs, N), dtype=torch.float32, device=dev)
+    Z = torch.empty((pairs, N), dtype=torch.float32, device=dev)
+    cnt = C.c_uint(0)
+    solver.check(L.jetgpu_harvest(solver.context(), pairs, R.data_ptr(),
+                                  Z.data_ptr(), C.byref(cnt)))
+    samples = []
+    for k in range(cnt.value):
+        feat = torch.empty((n, n, n, 16), dtype=torch.bfloat16, device=dev)
+        solver.check(L.jetgpu_net_features(solver.context(), R[k].data_ptr(),
+                                           feat.data_ptr()))
+        rms = torch.sqrt(torch.mean(R[k].double() ** 2)).float()
+        if rms <= 0:
+            continue
+        target = (Z[k] * (NET_GAIN / rms)).reshape(n, n, n)
+        samples.append((feat, target, feat[..., 7].float()))
+    return samples
+
+
+def level0_rows(solver: FdmMgpcgSolver3, n: int, device):
+    """The finest level's matrix rows {center, right, up, front} of the
+    solver's last system as an FP32 (n, n, n, 4) device tensor."""
+    torch = _torch()
+    L = library()
+    rows = np.zeros(n ** 3 * 4)
+    cnt = C.c_size_t(0)
+    solver.check(L.jetgpu_get_level(solver.context(), 0, 4,
+                                    rows.ctypes.data_as(C.c_void_p),
+                                    rows.nbytes, C.byref(cnt)))
+    return torch.from_numpy(rows.reshape(n, n, n, 4).astype(np.float32)).to(device)
+
+
+def apply_rows(A, x):
+    """y = A x for 7-point rows (FdmBlas3::mvm, fdm_linear_system3.cpp:
+    79-96) on torch tensors (differentiable)."""
+    y = A[..., 0] * x
+    y = y + _torch().nn.functional.pad(A[:, :, :-1, 1] * x[:, :, :-1], (1, 0))
+    y = y + _torch().nn.functional.pad(A[:, :, :-1, 1] * x[:, :, 1:], (0, 1))
+    y = y + _torch().nn.functional.pad(A[:, :-1, :, 2] * x[:, :-1, :], (0, 0, 1, 0))
+    y = y + _torch().nn.functional.pad(A[:, :-1, :, 2] * x[:, 1:, :], (0, 0, 0, 1))
+    y = y + _torch().nn.functional.pad(A[:-1, :, :, 3] * x[:-1], (0, 0, 0, 0, 1, 0))
+    y = y + _torch().nn.functional.pad(A[:-1, :, :, 3] * x[1:], (0, 0, 0, 0, 0, 1))
+    return y
+
+
+def step_energy(A, r, z):
+    """Energy (A-norm squared of the error) that the exact line search
+    along z removes from residual r: (r.z)^2 / (z.A z)."""
+    return (r * z).sum() ** 2 / (z * apply_rows(A, z)).sum().clamp_min(1e-30)
+
+
+def train_stream(n: int = 128, seeds=range(100, 2100), pairs: int = 2,
+                 lr: float = 2e-3, seed: int = 0, init=None, log=print,
+                 loss_kind: str = "energy"):
+    """Training at the scale of BASELINE's learned-preconditioner config:
+    one sphere-union scene per seed (by default 2,000 scenes at 128^3, seeds
+    100-2099), each solved on the GPU, `pairs` (residual, V-cycle
+    correction) samples harvested from its MGPCG iterations and used for one
+    optimiser step each, then discarded (a 128^3 sample is 64 MB of BF16
+    features). Every convolution forward and backward runs on libjetgpu's
+    tensor-core kernels. Returns (params, loss history)."""
+    torch = _torch()
+    conv = make_conv_fn()
+    solver = FdmMgpcgSolver3(200, 6, 2, 2, 10, 2, 1e-6, 1.0, True)
+    dev = torch.device("cuda", solver.config.device)
+    start = init if init is not None else init_params(seed)
+    P = [(torch.tensor(w, device=dev, requires_grad=True),
+          torch.tensor(b, device=dev, requires_grad=True)) for w, b in start]
+    flat_params = [t for p in P for t in p]
+    seeds = list(seeds)
+    steps = len(seeds) * pairs
+    opt = torch.optim.Adam(flat_params, lr=lr)
+    warm = max(1, min(200, steps // 10))
+    sched = torch.optim.lr_scheduler.LambdaLR(
+        opt, lambda s: min(1.0, (s + 1) / warm) *
+        0.5 * (1.0 + np.cos(np.pi * min(s, steps) / steps)))
+    hist = []
+    for si, sd in enumerate(seeds):
+        sc = device_scene(n, sd, dev)
+        samples = harvest_device(solver, sc, n, pairs)
+        A = level0_rows(solver, n, dev) if loss_kind == "energy" else None
+        for feat, target, mask in samples:
+            pred = forward(conv, P, feat)
+            if loss_kind == "energy":
+                # One minus the energy a step along the network's output
+                # removes, relative to the V-cycle's step (scale-free).
+                r = feat[..., 0].float() * mask
+                z = pred * mask
+                loss = 1.0 - step_energy(A, r, z) / step_energy(
+                    A, r, target * mask).detach()
+            else:
+                err = (pred - target) * mask
+                loss = (err * err).sum() / ((target * mask) ** 2).sum().clamp_min(1e-30)
+            opt.zero_grad()
+            loss.backward()
+            torch.nn.utils.clip_grad_norm_(flat_params, 1.0)
+            opt.step()
+            sched.step()
+            hist.append(float(loss.detach()))
+        del sc
+        if si % 100 == 0 or si == len(seeds) - 1:
+            log(f"scene {si} (seed {sd}) loss {np.mean(hist[-2 * pairs * 50:]):.4f}")
+    params = [(w.detach().cpu().numpy(), b.detach().cpu().numpy()) for w, b in P]
+    solver.close()
+    return params, hist
+
+
 def training_scenes(n: int, count: int, first_seed: int = 100):
     """Sphere-union scenes (16 spheres, seeds first_seed..) and FLIP first
     sub-step boxes of varying size."""
@@ -285,45 +453,68 @@ def train(n: int = 64, scenes_count: int = 24, pairs: int = 6,
     return params, hist
 
 
-def evaluate(params, n: int, seed: int, tolerance: float = 1e-6):
-    """Solves one held-out sphere-union scene with the learned, multigrid and
-    no preconditioner; returns {name: (status, iterations, relative residual,
-    fallback used)}."""
+def evaluate(params, n: int, seed: int, tolerance: float = 1e-6,
+             scene: str = "sphere_union"):
+    """Solves one held-out scene (the sphere union of a seed outside the
+    training range, or the FLIP dam-break sub-step) with the learned,
+    multigrid and no preconditioner; returns {name: dict(status,
+    iterations, relative residual, fallback used, ms)}, ms = the solve's
+    device time (weights, system and Krylov solve) of a second solve."""
     flat = flatten(params)
-    sc = scenes.sphere_union_scene(n, seed=seed)
+    if scene == "sphere_union":
+        sc = scenes.sphere_union_scene(n, seed=seed)
+    else:
+        sc = scenes.flip_first_substep(n, box_hi=(0.3, 0.8, 1.0),
+                                       sphere=((0.6, 0.2, 0.5), 0.15))
     h = (1.0 / n,) * 3
     out = {}
     for pre in ("learned", "multigrid", "none"):
-        s = FdmMgpcgSolver3(1000, 8, 2, 2, 10, 2, tolerance, 1.0, True,
+        s = FdmMgpcgSolver3(1000, 6, 2, 2, 5, 2, tolerance, 1.2, True,
                             preconditioner=pre, maxRefinements=8)
         if pre == "learned":
             s.load_network(flat)
         ps = GridFractionalSinglePhasePressureSolver3(s)
         vel = FaceCenteredGrid3((n,) * 3, h, (0, 0, 0), sc["u"], sc["v"], sc["w"])
         g = lambda d: CellCenteredScalarGrid3((n,) * 3, h, (0, 0, 0), d)
-        st = ps.solve(vel, 1 / 60, vel.clone(), g(sc["boundary_sdf"]), None,
-                      g(sc["fluid_sdf"]))
+        for _ in range(2):
+            st = ps.solve(vel, 1 / 60, vel.clone(), g(sc["boundary_sdf"]),
+                          None, g(sc["fluid_sdf"]))
         t = ps.last_stats
-        out[pre] = (st, t.iterations, t.relative_residual, t.fallback_used)
+        out[pre] = dict(status=st, iterations=t.iterations,
+                        relative_residual=t.relative_residual,
+                        fallback=bool(t.fallback_used),
+                        ms=round(t.setup_ms + t.solve_ms, 3))
         s.close()
     return out
 
 
 if __name__ == "__main__":
     import argparse
-    ap = argparse.ArgumentParser()
-    ap.add_argument("--n", type=int, default=64)
-    ap.add_argument("--scenes", type=int, default=24)
-    ap.add_argument("--pairs", type=int, default=6)
-    ap.add_argument("--steps", type=int, default=600)
+    import json
+    ap = argparse.ArgumentParser(
+        description="Trains the preconditioner network on the GPU: 2,000 "
+                    "sphere-union scenes at 128^3 (seeds 100-2099) by default")
+    ap.add_argument("--n", type=int, default=128)
+    ap.add_argument("--first-seed", type=int, default=100)
+    ap.add_argument("--scenes", type=int, default=2000)
+    ap.add_argument("--pairs", type=int, default=2)
     ap.add_argument("--lr", type=float, default=2e-3)
+    ap.add_argument("--loss", default="energy", choices=["energy", "mse"],
+                    help="energy: the error energy a step along the output "
+                         "removes, relative to the V-cycle's step; mse: "
+                         "relative squared error to the V-cycle's output")
     ap.add_argument("--out", default=WEIGHTS)
-    ap.add_argument("--eval", type=int, nargs="*", default=[64],
+    ap.add_argument("--eval", type=int, nargs="*", default=[128, 256],
                     help="grid sizes of the held-out evaluation solves")
     a = ap.parse_args()
-    params, hist = train(a.n, a.scenes, a.pairs, a.steps, lr=a.lr)
+    params, hist = train_stream(a.n, range(a.first_seed,
+                                           a.first_seed + a.scenes),
+                                a.pairs, lr=a.lr, loss_kind=a.loss)
     save(params, a.out)
-    print("saved", a.out, "final loss", np.mean(hist[-50:]))
+    print("saved", a.out, "final loss", np.mean(hist[-100:]))
     for n in a.eval:
         for seed in (9001, 9002):
-            print(f"held-out {n}^3 seed {seed}:", evaluate(params, n, seed))
+            print(json.dumps({"held_out": f"{n}^3 sphere union seed {seed}",
+                              **evaluate(params, n, seed)}), flush=True)
+        print(json.dumps({"held_out": f"{n}^3 FLIP dam-break sub-step",
+                          **evaluate(params, n, 0, scene="flip")}), flush=True)

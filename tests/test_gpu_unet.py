@@ -39,11 +39,19 @@ def run_conv(x, w, bias, relu):
     return out32.cpu().numpy(), out.float().cpu().numpy()
 
 
+# Shapes are (nz, ny, nx). Rows of 128 or 256 cells run on the brick kernel
+# (the input brick of a 128-cell row staged by TMA once, all taps from shared
+# memory), the others on the per-tap gather kernel.
 @pytest.mark.parametrize("ci,co,shape", [(16, 16, (9, 10, 12)),
                                          (32, 16, (8, 8, 8)),
                                          (16, 48, (5, 7, 11)),
                                          (112, 48, (6, 6, 6)),
-                                         (64, 64, (16, 16, 16))])
+                                         (64, 64, (16, 16, 16)),
+                                         (16, 16, (3, 4, 128)),
+                                         (48, 16, (4, 3, 128)),
+                                         (16, 32, (2, 3, 256)),
+                                         (80, 32, (3, 2, 128)),
+                                         (32, 80, (2, 2, 128))])
 def test_conv3d_matches_oracle(ci, co, shape):
     rng = np.random.default_rng(ci * 7 + co)
     x = conv_ref.bf16_round(rng.standard_normal(shape + (ci,)))
@@ -64,7 +72,8 @@ def test_conv3d_gradients_match_oracle():
     dev = torch.device("cuda", 0)
     rng = np.random.default_rng(3)
     for ci, co, shape in ((16, 16, (9, 10, 12)), (48, 32, (6, 7, 8)),
-                          (112, 48, (5, 6, 7)), (64, 64, (8, 8, 8))):
+                          (112, 48, (5, 6, 7)), (64, 64, (8, 8, 8)),
+                          (48, 16, (3, 2, 128)), (32, 80, (2, 3, 128))):
         x = conv_ref.bf16_round(rng.standard_normal(shape + (ci,)))
         w = conv_ref.bf16_round(rng.standard_normal((27, co, ci)) * 0.1)
         dy = conv_ref.bf16_round(rng.standard_normal(shape + (co,)))
