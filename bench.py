@@ -199,11 +199,66 @@ VARIANTS = {
 
 
 def peaks() -> dict:
+    """Roofline denominators: the measured copy bandwidth and cuBLAS BF16
+    burst throughput of the GB300s when MEASURED_PEAKS.json is
+    present, else the fallback figures (6.8 TB/s, 1.9 PFLOP/s)."""
     path = os.path.join(REPO, "MEASURED_PEAKS.json")
     if os.path.exists(path):
         d = json.load(open(path))
-        return {"hbm_gbs": d.get("hbm_gbs"), "source": "measured"}
-    return {"hbm_gbs": 6800.0, "source": "fallback"}
+        return {"hbm_gbs": d.get("hbm_gbs"), "source": "measured",
+                "bf16_tflops": d.get("bf16_tflops") or 1900.0,
+                "tensor_source": "measured" if d.get("bf16_tflops")
+                else "fallback"}
+    return {"hbm_gbs": 6800.0, "source": "fallback", "bf16_tflops": 1900.0,
+            "tensor_source": "fallback"}
+
+
+def run_unet(local, n: int = 128, reps: int = 10):
+    """Tensor-pipe roofline of the learned preconditioner's convolutions:
+    the level-0 layer (3x3x3, 16 -> 16 channels, BF16, FP32 accumulation)
+    at n^3 through jetgpu_conv3d, CUDA events over `reps` launches after
+    warm-up; FLOP = 2 * 27 * C_in * C_out per cell."""
+    import ctypes as C
+    import torch
+    import jetgpu
+    L = jetgpu.library()
+    dev = torch.device("cuda", local)
+    out = {}
+    for ci, co in ((16, 16), (48, 16)):
+        g = torch.Generator(device=dev)
+        g.manual_seed(0)
+        x = (torch.randn((n, n, n, ci), generator=g, device=dev) * 0.1).to(
+            torch.bfloat16)
+        w = (torch.randn((27, co, ci), generator=g, device=dev) * 0.05).to(
+            torch.bfloat16)
+        b = torch.zeros(co, device=dev)
+        y = torch.empty((n, n, n, co), dtype=torch.bfloat16, device=dev)
+        err = torch.zeros(1, dtype=torch.int32, device=dev)
+        res = (C.c_int * 3)(n, n, n)
+        s = torch.cuda.current_stream(dev).cuda_stream
+
+        def call():
+            st = L.jetgpu_conv3d(s, x.data_ptr(), ci, w.data_ptr(),
+                                 b.data_ptr(), co, res, 1, y.data_ptr(), None,
+                                 err.data_ptr())
+            if st != 0:
+                raise RuntimeError(f"jetgpu_conv3d failed ({st})")
+
+        for _ in range(3):
+            call()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record()
+        for _ in range(reps):
+            call()
+        e1.record()
+        torch.cuda.synchronize()
+        us = e0.elapsed_time(e1) / reps * 1e3
+        flop = 2.0 * 27 * ci * co * n ** 3
+        out[f"conv_{ci}_{co}_{n}"] = {"us": round(us, 1),
+                                      "tflops": round(flop / us / 1e6, 1)}
+    return out
 
 
 def traffic_per_launch(kernel: str, variant: str, n: int):
@@ -853,6 +908,7 @@ def main():
     accuracy = None
     if not args.no_accuracy and rank == 0:
         accuracy = run_accuracy(args, local, r["variants"].keys())
+    unet = run_unet(local) if rank == 0 else None
     flip = None
     if not args.no_flip:
         # The 256^3 dam break for 30 frames with each MGPCG variant (the
@@ -917,6 +973,15 @@ def main():
     }
     if accuracy is not None:
         line["accuracy"] = accuracy
+    if unet is not None:
+        pk = peaks()
+        top = unet["conv_16_16_128"]
+        line["roofline_tensor"] = {
+            "kernel": "conv3d 3x3x3 16->16 (U-Net level 0) at 128^3",
+            "bound": "tensor", "achieved": top["tflops"],
+            "peak": pk["bf16_tflops"], "unit": "TFLOP/s",
+            "frac": round(top["tflops"] / pk["bf16_tflops"], 3),
+            "peak_source": pk["tensor_source"], "layers": unet}
     if flip is not None:
         line["flip_steps"] = flip
     if smoke is not None:

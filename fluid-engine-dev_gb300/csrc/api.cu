@@ -50,7 +50,12 @@ void free_buffers(Ctx* c) {
         cudaGraphExecDestroy(c->vc_exec);
         c->vc_exec = nullptr;
     }
+    if (c->loop_exec) {
+        cudaGraphExecDestroy(c->loop_exec);
+        c->loop_exec = nullptr;
+    }
     c->vc_disabled = false;
+    c->loop_disabled = false;
     for (Level& L : c->levels) {
         release(&L.phi);
         release(&L.uw);
@@ -1394,6 +1399,26 @@ jetgpu_status jetgpu_net_features(jetgpu_ctx* c, const float* r, void* feat) {
     if (s != JETGPU_OK) return s;
     s = net_features(c, r, c->scal + S_MEAN, feat);
     if (s != JETGPU_OK) return s;
+    JG_CUDA(c, cudaStreamSynchronize(c->stream));
+    return JETGPU_OK;
+}
+
+jetgpu_status jetgpu_vcycle_apply(jetgpu_ctx* c, const float* r, float* z) {
+    if (!c || !r || !z) return JETGPU_BAD_INPUT;
+    if (c->built_levels == 0)
+        return fail(c, JETGPU_BAD_INPUT, "no system: run a pressure solve first");
+    JG_CUDA(c, cudaSetDevice(c->device));
+    const Level& L0 = c->levels[0];
+    const long N = L0.n.count();
+    // The V-cycle writes into its own buffers (the finest level's x and its
+    // ping-pong partner); r is copied in first so that it may alias z.
+    JG_CUDA(c, cudaMemcpyAsync(L0.b, r, N * sizeof(float),
+                               cudaMemcpyDeviceToDevice, c->stream));
+    float* res = nullptr;
+    jetgpu_status s = vcycle(c, L0.b, L0.x, L0.x2, &res);
+    if (s != JETGPU_OK) return s;
+    JG_CUDA(c, cudaMemcpyAsync(z, res, N * sizeof(float),
+                               cudaMemcpyDeviceToDevice, c->stream));
     JG_CUDA(c, cudaStreamSynchronize(c->stream));
     return JETGPU_OK;
 }

@@ -188,6 +188,12 @@ struct Ctx {
     int vc_precision = -1;
     float* vc_result = nullptr;
     bool vc_disabled = false;
+    // The whole FP32 PCG loop as one graph with a device-side while node
+    // (mgpcg.cu, pcg_loop_graph): V-cycle, Krylov updates and the stopping
+    // test per iteration, no host round trip. Captured for the same key as
+    // vc_exec; destroyed with the buffers.
+    cudaGraphExec_t loop_exec = nullptr;
+    bool loop_disabled = false;
 
     // Blocked pressure solver (blocked.cu): cell markers of every level,
     // finest first.

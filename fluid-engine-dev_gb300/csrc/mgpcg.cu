@@ -39,6 +39,8 @@ namespace {
 
 enum Fin : int { FIN_NONE = 0, FIN_BETA = 1, FIN_ALPHA = 2 };
 enum : int { S_ALPHA = 8, S_BETA = 9, S_FIRST = 10 };
+// Device-side PCG loop: target residual norm, iteration cap, iterations run.
+enum : int { S_LOOP_TARGET = 11, S_LOOP_MAX = 12, S_LOOP_IT = 13 };
 
 // Finishes a reduction: stores the total and derives alpha/beta.
 __device__ __forceinline__ void finish(double* scal, int target, double v,
@@ -622,6 +624,35 @@ __global__ void k_init_scalars(double* scal) {
     }
 }
 
+// k_init_scalars plus the device-side loop's target, cap and counter.
+__global__ void k_loop_start(double* scal, double target, double max_it) {
+    if (threadIdx.x == 0 && blockIdx.x == 0) {
+        scal[S_RZ] = 0.0;
+        scal[S_RZ_OLD] = 0.0;
+        scal[S_DQ] = 0.0;
+        scal[S_RR] = 0.0;
+        scal[S_ALPHA] = 0.0;
+        scal[S_BETA] = 0.0;
+        scal[S_FIRST] = 1.0;
+        scal[S_LOOP_TARGET] = target;
+        scal[S_LOOP_MAX] = max_it;
+        scal[S_LOOP_IT] = 0.0;
+    }
+}
+
+// End of a device-side PCG iteration: counts it and sets the while node's
+// condition — continue while the residual norm is above the target, finite,
+// below the iteration cap and no sweep reported a stalled copy. Every
+// launch sets the condition, and the cap bounds the loop.
+__global__ void k_loop_check(cudaGraphConditionalHandle h, double* scal) {
+    const double it = scal[S_LOOP_IT] + 1.0;
+    scal[S_LOOP_IT] = it;
+    const double rr = scal[S_RR];
+    const bool go = it < scal[S_LOOP_MAX] && isfinite(rr) &&
+                    !(sqrt(rr) <= scal[S_LOOP_TARGET]) && scal[S_WAIT] == 0.0;
+    cudaGraphSetConditional(h, go ? 1u : 0u);
+}
+
 template <typename V>
 __global__ void k_zero(V* __restrict__ p, long N) {
     for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < N;
@@ -902,6 +933,255 @@ __global__ void __launch_bounds__(1024)
         }
     }
     for (int c = threadIdx.x; c < N; c += blockDim.x) x[c] = sx[c];
+}
+
+// ---------------------------------------------------------------------------
+// The V-cycle below a level of at most kTailMaxCells cells in one CTA: every
+// level of the tail (x, b, r, the fluid SDF and the rows widened to FP32)
+// sits in shared memory, and the steps of the multi-kernel path — zero-start
+// and continued red-black half-sweeps, residual, masked restriction,
+// coarsest sweeps, correction — run as phases separated by block barriers,
+// in the order and with the arithmetic of k_rb_half (division as in the
+// fused sweep), k_residual32, k_restrict, k_coarsest and k_correct. On the
+// small levels those kernels are a few microseconds of launch and drain
+// each; here the whole tail is one launch.
+
+constexpr int kTailMaxCells = 4096;
+constexpr int kTailMaxLevels = 8;
+constexpr int kTailThreads = 1024;
+
+struct TailLevel {
+    Dims n;
+    const float* A;              // FP32 rows (structure of arrays) or null
+    const unsigned short* Ah;    // BF16 rows (mixed mode) or null
+    const float* phi;            // fluid SDF (masks the restriction)
+};
+struct TailArgs {
+    TailLevel lv[kTailMaxLevels];
+    int count;                   // levels in the tail
+    const float* b;              // right-hand side of the first tail level
+    float* x;                    // its V-cycle result
+    int pre, post, coarsest;     // sweeps
+    float omega;
+};
+
+// Shared-memory words of a tail level of N cells: x, b, r, phi, 4 rows and
+// the packed (i, j, k) of every cell (10 bits each; tail levels are at most
+// 4096 cells, so each extent is below 1024).
+__host__ __device__ inline long tail_floats(long N) { return 9 * N; }
+
+__device__ __forceinline__ void unpack_ijk(unsigned q, int& i, int& j, int& k) {
+    i = (int)(q & 1023u);
+    j = (int)((q >> 10) & 1023u);
+    k = (int)(q >> 20);
+}
+
+// One colour of a red-black SOR sweep over a level held in shared memory
+// (k_rb_half's arithmetic, with the fast division of the fused sweep): every
+// cell of `color` is updated from its neighbours; with `zero` the sweep
+// starts from x = 0, so the colour gets omega b / center and the other
+// colour is written 0. One SM does the whole tail, so instructions per cell
+// bound it.
+__device__ __forceinline__ void tail_half(const float* A, const float* b,
+                                          float* x, const unsigned* ijk,
+                                          Dims n, int color, bool zero,
+                                          float omega) {
+    const int N = (int)n.count();
+    const int sy = n.x, sz = n.x * n.y;
+    for (int c = threadIdx.x; c < N; c += blockDim.x) {
+        int i, j, k;
+        unpack_ijk(ijk[c], i, j, k);
+        const bool mine = ((i + j + k) & 1) == color;
+        if (zero) {
+            x[c] = mine ? omega * __fdividef(b[c], A[c]) : 0.0f;
+            continue;
+        }
+        if (!mine) continue;
+        float s = 0.0f;
+        if (i > 0) s += A[N + c - 1] * x[c - 1];
+        if (i + 1 < n.x) s += A[N + c] * x[c + 1];
+        if (j > 0) s += A[2 * N + c - sy] * x[c - sy];
+        if (j + 1 < n.y) s += A[2 * N + c] * x[c + sy];
+        if (k > 0) s += A[3 * N + c - sz] * x[c - sz];
+        if (k + 1 < n.z) s += A[3 * N + c] * x[c + sz];
+        x[c] = (1.0f - omega) * x[c] + omega * __fdividef(b[c] - s, A[c]);
+    }
+}
+
+// The shared-memory arrays of tail level l.
+struct TailViews {
+    float *x, *b, *r, *phi, *A;
+    unsigned* ijk;
+};
+__device__ __forceinline__ TailViews tail_views(float* base, const TailArgs& a,
+                                                int l) {
+    float* q = base;
+    for (int m = 0; m < l; ++m) q += tail_floats(a.lv[m].n.count());
+    const long N = a.lv[l].n.count();
+    return TailViews{q, q + N, q + 2 * N, q + 3 * N, q + 4 * N,
+                     reinterpret_cast<unsigned*>(q + 8 * N)};
+}
+
+__global__ void __launch_bounds__(kTailThreads) k_vcycle_tail(TailArgs a) {
+    extern __shared__ float tsm[];
+    // Load: rows (BF16 widened), fluid SDF, cell indices, the first level's
+    // b; four independent 16-byte (or 8-byte) loads per thread and step.
+    for (int l = 0; l < a.count; ++l) {
+        const TailLevel& L = a.lv[l];
+        const TailViews v = tail_views(tsm, a, l);
+        const int N = (int)L.n.count();
+        if (N % 4 == 0) {
+            const int N4 = N;  // 4 N floats of rows = N float4
+            if (L.Ah) {
+                const uint2* src = reinterpret_cast<const uint2*>(L.Ah);
+                for (int e = threadIdx.x; e < N4; e += blockDim.x) {
+                    const uint2 w = __ldg(src + e);
+                    reinterpret_cast<float4*>(v.A)[e] = make_float4(
+                        __uint_as_float(w.x << 16),
+                        __uint_as_float(w.x & 0xffff0000u),
+                        __uint_as_float(w.y << 16),
+                        __uint_as_float(w.y & 0xffff0000u));
+                }
+            } else {
+                const float4* src = reinterpret_cast<const float4*>(L.A);
+                for (int e = threadIdx.x; e < N4; e += blockDim.x)
+                    reinterpret_cast<float4*>(v.A)[e] = __ldg(src + e);
+            }
+            const float4* ph = reinterpret_cast<const float4*>(L.phi);
+            for (int e = threadIdx.x; e < N / 4; e += blockDim.x)
+                reinterpret_cast<float4*>(v.phi)[e] = __ldg(ph + e);
+        } else {
+            for (int e = threadIdx.x; e < 4 * N; e += blockDim.x)
+                v.A[e] = L.Ah ? __uint_as_float((unsigned)L.Ah[e] << 16) : L.A[e];
+            for (int e = threadIdx.x; e < N; e += blockDim.x) v.phi[e] = L.phi[e];
+        }
+        for (int c = threadIdx.x; c < N; c += blockDim.x) {
+            const int i = c % L.n.x, j = (c / L.n.x) % L.n.y,
+                      k = c / (L.n.x * L.n.y);
+            v.ijk[c] = (unsigned)i | ((unsigned)j << 10) | ((unsigned)k << 20);
+        }
+    }
+    {
+        const TailViews v0 = tail_views(tsm, a, 0);
+        for (int e = threadIdx.x; e < (int)a.lv[0].n.count(); e += blockDim.x)
+            v0.b[e] = __ldg(a.b + e);
+    }
+    __syncthreads();
+    const float w = a.omega;
+    const int last = a.count - 1;
+    // Down: pre-smoothing from zero, residual, masked restriction.
+    for (int l = 0; l < last; ++l) {
+        const TailViews v = tail_views(tsm, a, l);
+        const Dims n = a.lv[l].n;
+        const int N = (int)n.count();
+        for (int s = 0; s < a.pre; ++s) {
+            tail_half(v.A, v.b, v.x, v.ijk, n, 0, s == 0, w);
+            __syncthreads();
+            tail_half(v.A, v.b, v.x, v.ijk, n, 1, false, w);
+            __syncthreads();
+        }
+        if (a.pre == 0) {
+            for (int e = threadIdx.x; e < N; e += blockDim.x) v.x[e] = 0.0f;
+            __syncthreads();
+        }
+        const int sy = n.x, sz = n.x * n.y;
+        for (int c = threadIdx.x; c < N; c += blockDim.x) {
+            int i, j, k;
+            unpack_ijk(v.ijk[c], i, j, k);
+            const float* x = v.x;
+            const float* A = v.A;
+            float sacc = A[c] * x[c];
+            if (i > 0) sacc += A[N + c - 1] * x[c - 1];
+            if (i + 1 < n.x) sacc += A[N + c] * x[c + 1];
+            if (j > 0) sacc += A[2 * N + c - sy] * x[c - sy];
+            if (j + 1 < n.y) sacc += A[2 * N + c] * x[c + sy];
+            if (k > 0) sacc += A[3 * N + c - sz] * x[c - sz];
+            if (k + 1 < n.z) sacc += A[3 * N + c] * x[c + sz];
+            v.r[c] = v.b[c] - sacc;
+        }
+        __syncthreads();
+        const TailViews cv = tail_views(tsm, a, l + 1);
+        const Dims cn = a.lv[l + 1].n;
+        const float kern[4] = {0.125f, 0.375f, 0.375f, 0.125f};
+        for (int t = threadIdx.x; t < (int)cn.count(); t += blockDim.x) {
+            int i, j, k;
+            unpack_ijk(cv.ijk[t], i, j, k);
+            const int iI[4] = {i > 0 ? 2 * i - 1 : 2 * i, 2 * i, 2 * i + 1,
+                               i + 1 < cn.x ? 2 * i + 2 : 2 * i + 1};
+            const int jI[4] = {j > 0 ? 2 * j - 1 : 2 * j, 2 * j, 2 * j + 1,
+                               j + 1 < cn.y ? 2 * j + 2 : 2 * j + 1};
+            const int kI[4] = {k > 0 ? 2 * k - 1 : 2 * k, 2 * k, 2 * k + 1,
+                               k + 1 < cn.z ? 2 * k + 2 : 2 * k + 1};
+            float sum = 0.0f;
+#pragma unroll
+            for (int z = 0; z < 4; ++z) {
+                float syy = 0.0f;
+#pragma unroll
+                for (int y = 0; y < 4; ++y) {
+                    const float* rowp = v.r + n.x * (jI[y] + n.y * kI[z]);
+                    const float sx = kern[0] * rowp[iI[0]] + kern[1] * rowp[iI[1]] +
+                                     kern[2] * rowp[iI[2]] + kern[3] * rowp[iI[3]];
+                    syy += kern[y] * sx;
+                }
+                sum += kern[z] * syy;
+            }
+            cv.b[t] = (cv.phi[t] < 0.0f) ? sum : 0.0f;
+        }
+        __syncthreads();
+    }
+    // Coarsest level: forward sweeps from zero, then reverse.
+    {
+        const TailViews v = tail_views(tsm, a, last);
+        const Dims n = a.lv[last].n;
+        for (int e = threadIdx.x; e < (int)n.count(); e += blockDim.x)
+            v.x[e] = 0.0f;
+        __syncthreads();
+        for (int pass = 0; pass < 2 * a.coarsest; ++pass)
+            for (int h = 0; h < 2; ++h) {
+                const int color = (pass < a.coarsest) ? h : 1 - h;
+                tail_half(v.A, v.b, v.x, v.ijk, n, color, false, w);
+                __syncthreads();
+            }
+    }
+    // Up: correction, post-smoothing (colours reversed).
+    for (int l = last - 1; l >= 0; --l) {
+        const TailViews v = tail_views(tsm, a, l);
+        const Dims n = a.lv[l].n, cn = a.lv[l + 1].n;
+        const float* coarse = tail_views(tsm, a, l + 1).x;
+        for (int t = threadIdx.x; t < (int)n.count(); t += blockDim.x) {
+            int i, j, k;
+            unpack_ijk(v.ijk[t], i, j, k);
+            const int ci = i >> 1, cj = j >> 1, ck = k >> 1;
+            int i0, i1, j0, j1, k0, k1;
+            float wi0, wi1, wj0, wj1, wk0, wk1;
+            if ((i & 1) == 0) { i0 = i > 1 ? ci - 1 : ci; i1 = ci; wi0 = 0.25f; wi1 = 0.75f; }
+            else { i0 = ci; i1 = i + 1 < n.x ? ci + 1 : ci; wi0 = 0.75f; wi1 = 0.25f; }
+            if ((j & 1) == 0) { j0 = j > 1 ? cj - 1 : cj; j1 = cj; wj0 = 0.25f; wj1 = 0.75f; }
+            else { j0 = cj; j1 = j + 1 < n.y ? cj + 1 : cj; wj0 = 0.75f; wj1 = 0.25f; }
+            if ((k & 1) == 0) { k0 = k > 1 ? ck - 1 : ck; k1 = ck; wk0 = 0.25f; wk1 = 0.75f; }
+            else { k0 = ck; k1 = k + 1 < n.z ? ck + 1 : ck; wk0 = 0.75f; wk1 = 0.25f; }
+            auto C = [&](int a0, int b0, int c0) {
+                return coarse[a0 + cn.x * (b0 + cn.y * c0)];
+            };
+            const float a0 = wj0 * (wi0 * C(i0, j0, k0) + wi1 * C(i1, j0, k0)) +
+                             wj1 * (wi0 * C(i0, j1, k0) + wi1 * C(i1, j1, k0));
+            const float a1 = wj0 * (wi0 * C(i0, j0, k1) + wi1 * C(i1, j0, k1)) +
+                             wj1 * (wi0 * C(i0, j1, k1) + wi1 * C(i1, j1, k1));
+            v.x[t] += wk0 * a0 + wk1 * a1;
+        }
+        __syncthreads();
+        for (int s = 0; s < a.post; ++s) {
+            tail_half(v.A, v.b, v.x, v.ijk, n, 1, false, w);
+            __syncthreads();
+            tail_half(v.A, v.b, v.x, v.ijk, n, 0, false, w);
+            __syncthreads();
+        }
+    }
+    {
+        const TailViews v0 = tail_views(tsm, a, 0);
+        for (int e = threadIdx.x; e < (int)a.lv[0].n.count(); e += blockDim.x)
+            a.x[e] = v0.x[e];
+    }
 }
 
 // ---------------------------------------------------------------------------
@@ -1187,12 +1467,55 @@ float* smooth(Ctx* c, const Level& L, const float* b, float* x, float* alt,
     return x;
 }
 
+// First level of the one-CTA tail (k_vcycle_tail): the first level below
+// the finest whose cells, with every coarser level's, fit the tail's shared
+// memory; nl (no tail) when none does.
+unsigned tail_start(const Ctx* c) {
+    const unsigned nl = c->built_levels;
+    if (nl < 3) return nl;
+    for (unsigned l = 1; l + 1 < nl; ++l) {
+        if (c->levels[l].n.count() > kTailMaxCells) continue;
+        if (nl - l > (unsigned)kTailMaxLevels) return nl;
+        long floats = 0;
+        for (unsigned m = l; m < nl; ++m)
+            floats += tail_floats(c->levels[m].n.count());
+        return floats * 4 <= 200 * 1024 ? l : nl;
+    }
+    return nl;
+}
+
+float* vcycle_tail(Ctx* c, unsigned l, const float* b, float* x) {
+    const unsigned nl = c->built_levels;
+    const jetgpu_config& cfg = c->cfg;
+    TailArgs a{};
+    a.count = (int)(nl - l);
+    long floats = 0;
+    for (unsigned m = l; m < nl; ++m) {
+        const Level& L = c->levels[m];
+        a.lv[m - l] = TailLevel{L.n, mixed(c) ? nullptr : L.A,
+                                mixed(c) ? L.Ah : nullptr, L.phi};
+        floats += tail_floats(L.n.count());
+    }
+    a.b = b;
+    a.x = x;
+    a.pre = (int)cfg.restrict_iter;
+    a.post = (int)cfg.correct_iter;
+    a.coarsest = (int)cfg.coarsest_iter;
+    a.omega = (float)cfg.sor;
+    long cells = 0;
+    for (unsigned m = l; m < nl; ++m) cells += c->levels[m].n.count();
+    Prof pr(c, K_COARSEST, (12.0 + row_bytes(c)) * (double)cells);
+    k_vcycle_tail<<<1, kTailThreads, floats * sizeof(float), c->stream>>>(a);
+    return x;
+}
+
 // Symmetric V-cycle on level l from a zero initial guess; returns the
 // buffer (x or alt) that holds the result.
 float* vcycle_level(Ctx* c, unsigned l, const float* b, float* x, float* alt) {
     const Level& L = c->levels[l];
     const unsigned nl = c->built_levels;
     const jetgpu_config& cfg = c->cfg;
+    if (l > 0 && l == tail_start(c)) return vcycle_tail(c, l, b, x);
     if (l + 1 == nl) {
         if (L.n.count() <= kCoarsestMaxCells) {
             int nt = (int)std::min<long>(1024, ((L.n.count() + 31) / 32) * 32);
@@ -1312,6 +1635,9 @@ jetgpu_status prepare_levels(Ctx* c, unsigned lo, unsigned hi) {
 
 jetgpu_status init_kernels(Ctx* c) {
     jetgpu_status st;
+    JG_CUDA(c, cudaFuncSetAttribute(k_vcycle_tail,
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                    200 * 1024));
     if ((st = tma_prepare<RowsF>(c, &c->tma_blocks_per_sm[0])) != JETGPU_OK)
         return st;
     if ((st = tma_prepare<RowsB>(c, &c->tma_blocks_per_sm[1])) != JETGPU_OK)
@@ -1394,6 +1720,116 @@ void spmv_f32(Ctx* c, const RowsF& M, Dims n) {
             M, c->kd, c->kq, n, c->partials, c->counters, c->scal);
 }
 
+// One FP32 PCG iteration after z = M r: r.z (beta), d = z + beta d,
+// q = A d (alpha), x += alpha d, r -= alpha q (r.r).
+static void pcg_f32_updates(Ctx* c, const RowsF& M, Dims n, const float* z) {
+    const long N = n.count();
+    k_dot_rz4<<<rgrid(c, k_dot_rz4, N / 4), kThreads, 0, c->stream>>>(
+        c->kr, z, N, c->partials, c->counters, c->scal);
+    k_update_d4<<<rgrid(c, k_update_d4, N / 4), kThreads, 0, c->stream>>>(
+        c->kd, z, N, c->scal);
+    spmv_f32(c, M, n);
+    k_update_xr4<<<rgrid(c, k_update_xr4, N / 4), kThreads, 0, c->stream>>>(
+        c->kx, c->kr, c->kd, c->kq, N, c->partials, c->counters, c->scal);
+}
+
+// The multigrid FP32 PCG loop as one graph: a while node whose body is one
+// iteration (the V-cycle's launches captured directly, the Krylov updates)
+// followed by k_loop_check, which ends the loop on the device. The host
+// launches it once per refinement pass and reads the scalars once. It is
+// captured for the vectors and settings of the V-cycle graph (vc_exec),
+// is rebuilt with it, and any failure to build it turns the path off (the
+// host loop below is then used). Rows with nx % 4 != 0 use the host loop.
+static jetgpu_status pcg_loop_graph(Ctx* c, double target, unsigned max_it,
+                                    unsigned* it_out, double* rr_out,
+                                    bool* used) {
+    *used = false;
+    const Level& L0 = c->levels[0];
+    const Dims n = L0.n;
+    if (c->prof_on || c->loop_disabled || c->vc_disabled || n.x % 4 != 0 ||
+        max_it == 0)
+        return JETGPU_OK;
+    const jetgpu_config& f = c->cfg;
+    const bool same =
+        c->vc_exec && c->loop_exec && c->vc_key[0] == c->kr &&
+        c->vc_key[1] == c->kz && c->vc_key[2] == L0.x2 &&
+        c->vc_levels == c->built_levels && c->vc_iters[0] == f.restrict_iter &&
+        c->vc_iters[1] == f.correct_iter && c->vc_iters[2] == f.coarsest_iter &&
+        c->vc_iters[3] == f.final_iter && c->vc_sor == f.sor &&
+        c->vc_precision == f.precision;
+    if (!same) {
+        // (Re)capture the V-cycle graph first: it owns the key.
+        float* z = nullptr;
+        if (c->loop_exec) {
+            cudaGraphExecDestroy(c->loop_exec);
+            c->loop_exec = nullptr;
+        }
+        if (c->vc_exec) {
+            cudaGraphExecDestroy(c->vc_exec);
+            c->vc_exec = nullptr;
+        }
+        // Capture the V-cycle graph now (vcycle_graph records the key) with
+        // nothing enqueued: capture only records launches.
+        cudaGraph_t g = nullptr, body = nullptr;
+        auto give_up = [&]() {
+            if (g) cudaGraphDestroy(g);
+            c->loop_disabled = true;
+            cudaGetLastError();
+            return JETGPU_OK;
+        };
+        if (cudaGraphCreate(&g, 0) != cudaSuccess) return give_up();
+        cudaGraphConditionalHandle h;
+        if (cudaGraphConditionalHandleCreate(&h, g, 1,
+                                             cudaGraphCondAssignDefault) !=
+            cudaSuccess)
+            return give_up();
+        cudaGraphNodeParams np = {cudaGraphNodeTypeConditional};
+        std::memset(reinterpret_cast<unsigned char*>(&np), 0, sizeof(np));
+        np.type = cudaGraphNodeTypeConditional;
+        np.conditional.handle = h;
+        np.conditional.type = cudaGraphCondTypeWhile;
+        np.conditional.size = 1;
+        cudaGraphNode_t node;
+        if (cudaGraphAddNode(&node, g, nullptr, nullptr, 0, &np) != cudaSuccess)
+            return give_up();
+        body = np.conditional.phGraph_out[0];
+        if (cudaStreamBeginCaptureToGraph(c->stream, body, nullptr, nullptr, 0,
+                                          cudaStreamCaptureModeThreadLocal) !=
+            cudaSuccess)
+            return give_up();
+        z = vcycle_level(c, 0, c->kr, c->kz, L0.x2);
+        pcg_f32_updates(c, RowsF{L0.A, n.count()}, n, z);
+        k_loop_check<<<1, 1, 0, c->stream>>>(h, c->scal);
+        cudaGraph_t captured = nullptr;
+        const cudaError_t ec = cudaStreamEndCapture(c->stream, &captured);
+        if (ec != cudaSuccess) return give_up();
+        if (cudaGraphInstantiate(&c->loop_exec, g, 0) != cudaSuccess) {
+            c->loop_exec = nullptr;
+            return give_up();
+        }
+        cudaGraphDestroy(g);
+        // The V-cycle graph of the same key (used by the other solver paths).
+        float* vz = nullptr;
+        if (jetgpu_status vs = vcycle_graph(c, c->kr, c->kz, L0.x2, &vz)) {
+            (void)vz;
+            return vs;
+        }
+        // vcycle_graph launched one V-cycle: harmless (z is rewritten by the
+        // loop's first iteration), but keep the stream ordered.
+    }
+    k_loop_start<<<1, 1, 0, c->stream>>>(c->scal, target, (double)max_it);
+    JG_CUDA(c, cudaGraphLaunch(c->loop_exec, c->stream));
+    jetgpu_status s = read_scalars(c);
+    if (s != JETGPU_OK) return s;
+    const double rr = c->h_scal[S_RR];
+    if (!std::isfinite(rr))
+        return fail(c, JETGPU_NUMERICAL_ERROR, "non-finite residual in FP32 PCG");
+    *it_out = (unsigned)c->h_scal[S_LOOP_IT];
+    *rr_out = rr;
+    *used = true;
+    return JETGPU_OK;
+}
+
 // PCG on the FP32 rows for a correction e with A e = r (r = kr on entry).
 // Stops when ||r_k|| <= target or after max_it iterations.
 static jetgpu_status pcg_f32(Ctx* c, double target, unsigned max_it,
@@ -1402,6 +1838,12 @@ static jetgpu_status pcg_f32(Ctx* c, double target, unsigned max_it,
     const Dims n = L0.n;
     const long N = n.count();
     RowsF M{L0.A, N};
+    if (c->cfg.preconditioner == JETGPU_PRECOND_MULTIGRID) {
+        bool used = false;
+        jetgpu_status ls = pcg_loop_graph(c, target, max_it, it_out, rr_out,
+                                          &used);
+        if (ls != JETGPU_OK || used) return ls;
+    }
     k_init_scalars<<<1, 32, 0, c->stream>>>(c->scal);
     unsigned it = 0;
     double rr = 0;

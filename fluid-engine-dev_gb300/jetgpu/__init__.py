@@ -117,7 +117,7 @@ EXPORTS = (
     "jetgpu_build_particle_sdf", "jetgpu_flip_params_default",
     "jetgpu_fluid_cfl_device", "jetgpu_flip_substep_device",
     "jetgpu_apic_p2g_device", "jetgpu_apic_g2p_device",
-    "jetgpu_solve_pressure_collider",
+    "jetgpu_solve_pressure_collider", "jetgpu_vcycle_apply",
 )
 
 # closedDomainBoundaryFlag bits (include/jet/constants.h:312-335).
@@ -291,6 +291,8 @@ def library() -> C.CDLL:
     L.jetgpu_net_features.restype = C.c_int
     L.jetgpu_net_apply.argtypes = [vp, vp, vp]
     L.jetgpu_net_apply.restype = C.c_int
+    L.jetgpu_vcycle_apply.argtypes = [vp, vp, vp]
+    L.jetgpu_vcycle_apply.restype = C.c_int
     L.jetgpu_get_stream.argtypes = [vp, C.POINTER(C.c_void_p)]
     L.jetgpu_get_stream.restype = C.c_int
     L.jetgpu_profile.argtypes = [vp, C.c_int]

@@ -342,16 +342,84 @@ def step_energy(A, r, z):
     return (r * z).sum() ** 2 / (z * apply_rows(A, z)).sum().clamp_min(1e-30)
 
 
+def level0_rhs(solver: FdmMgpcgSolver3, n: int, device):
+    """The finest level's right-hand side of the solver's last system as an
+    FP32 (n, n, n) device tensor."""
+    torch = _torch()
+    L = library()
+    b = np.zeros(n ** 3)
+    cnt = C.c_size_t(0)
+    solver.check(L.jetgpu_get_level(solver.context(), 0, 5,
+                                    b.ctypes.data_as(C.c_void_p), b.nbytes,
+                                    C.byref(cnt)))
+    return torch.from_numpy(b.reshape(n, n, n).astype(np.float32)).to(device)
+
+
+def vcycle_apply(solver: FdmMgpcgSolver3, r):
+    """z = M r with the solver's multigrid V-cycle (jetgpu_vcycle_apply)."""
+    torch = _torch()
+    z = torch.empty_like(r).contiguous()
+    solver.check(library().jetgpu_vcycle_apply(
+        solver.context(), r.contiguous().data_ptr(), z.data_ptr()))
+    return z
+
+
+def fpcg_samples(solver: FdmMgpcgSolver3, conv, P, n: int, iters: int):
+    """Samples from the network's own flexible-PCG trajectory on the
+    solver's last system: starting from x = 0, each iteration's residual r_k
+    becomes a sample (its features, the V-cycle's correction M r_k as the
+    target, the fluid mask), and the iteration continues with the network's
+    correction, as the library's flexible PCG does (Polak-Ribiere beta).
+    The residuals a network meets inside its own solve differ from those of
+    multigrid PCG; training on them keeps it useful past the first step."""
+    torch = _torch()
+    L = library()
+    dev = P[0][0].device
+    A = level0_rows(solver, n, dev)
+    r = level0_rhs(solver, n, dev)
+    out = []
+    d = z_old = None
+    rz_old = 0.0
+    with torch.no_grad():
+        for k in range(iters):
+            rms = torch.sqrt(torch.mean(r.double() ** 2)).float()
+            if not float(rms) > 0:
+                break
+            feat = torch.empty((n, n, n, 16), dtype=torch.bfloat16, device=dev)
+            solver.check(L.jetgpu_net_features(solver.context(),
+                                               r.contiguous().data_ptr(),
+                                               feat.data_ptr()))
+            mask = feat[..., 7].float()
+            zmg = vcycle_apply(solver, r)
+            out.append((feat, (zmg * (NET_GAIN / rms)).reshape(n, n, n), mask))
+            z = forward(conv, P, feat) * (rms / NET_GAIN) * mask
+            rz = float((r * z).sum())
+            if k == 0 or d is None:
+                d = z.clone()
+            else:
+                beta = float((r * (z - z_old)).sum()) / rz_old if rz_old else 0.0
+                d = z + beta * d
+            q = apply_rows(A, d)
+            dq = float((d * q).sum())
+            if not (dq > 0 and rz > 0):
+                break
+            r = r - (rz / dq) * q
+            z_old, rz_old = z, rz
+    return out
+
+
 def train_stream(n: int = 128, seeds=range(100, 2100), pairs: int = 2,
                  lr: float = 2e-3, seed: int = 0, init=None, log=print,
-                 loss_kind: str = "energy"):
+                 loss_kind: str = "energy", own: int = 0):
     """Training at the scale of BASELINE's learned-preconditioner config:
     one sphere-union scene per seed (by default 2,000 scenes at 128^3, seeds
     100-2099), each solved on the GPU, `pairs` (residual, V-cycle
     correction) samples harvested from its MGPCG iterations and used for one
     optimiser step each, then discarded (a 128^3 sample is 64 MB of BF16
     features). Every convolution forward and backward runs on libjetgpu's
-    tensor-core kernels. Returns (params, loss history)."""
+    tensor-core kernels. With `own` > 0, the residuals of the first `own`
+    iterations of the network's own flexible PCG on each scene are added as
+    samples (fpcg_samples). Returns (params, loss history)."""
     torch = _torch()
     conv = make_conv_fn()
     solver = FdmMgpcgSolver3(200, 6, 2, 2, 10, 2, 1e-6, 1.0, True)
@@ -371,6 +439,8 @@ def train_stream(n: int = 128, seeds=range(100, 2100), pairs: int = 2,
     for si, sd in enumerate(seeds):
         sc = device_scene(n, sd, dev)
         samples = harvest_device(solver, sc, n, pairs)
+        if own > 0:
+            samples += fpcg_samples(solver, conv, P, n, own)
         A = level0_rows(solver, n, dev) if loss_kind == "energy" else None
         for feat, target, mask in samples:
             pred = forward(conv, P, feat)
@@ -503,13 +573,21 @@ if __name__ == "__main__":
                     help="energy: the error energy a step along the output "
                          "removes, relative to the V-cycle's step; mse: "
                          "relative squared error to the V-cycle's output")
+    ap.add_argument("--own", type=int, default=6,
+                    help="iterations of the network's own flexible PCG whose "
+                         "residuals are added as samples per scene")
+    ap.add_argument("--init", default=None,
+                    help="start from these weights instead of a random "
+                         "initialisation")
     ap.add_argument("--out", default=WEIGHTS)
     ap.add_argument("--eval", type=int, nargs="*", default=[128, 256],
                     help="grid sizes of the held-out evaluation solves")
     a = ap.parse_args()
     params, hist = train_stream(a.n, range(a.first_seed,
                                            a.first_seed + a.scenes),
-                                a.pairs, lr=a.lr, loss_kind=a.loss)
+                                a.pairs, lr=a.lr, loss_kind=a.loss,
+                                own=a.own,
+                                init=load(a.init) if a.init else None)
     save(params, a.out)
     print("saved", a.out, "final loss", np.mean(hist[-100:]))
     for n in a.eval:

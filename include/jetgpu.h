@@ -584,6 +584,15 @@ jetgpu_status jetgpu_harvest(struct jetgpu_ctx* ctx, unsigned int max_pairs,
                              float* r_out, float* z_out,
                              unsigned int* count);
 
+/* z = M r: one multigrid V-cycle preconditioner application (the
+ * preconditioner of FdmMgpcgSolver3, fdm_mgpcg_solver3.cpp:15-36, with this
+ * library's masked symmetric V-cycle) for residual r on the finest level of
+ * the last solved system, FP32 DEVICE arrays of cells floats (r and z may
+ * alias). For Krylov methods and training outside the library;
+ * synchronous. */
+jetgpu_status jetgpu_vcycle_apply(struct jetgpu_ctx* ctx, const float* r,
+                                  float* z);
+
 /* The network's 16 input channels (BF16, channels-last) for residual r on
  * the last solved system, and the network's output z = net(r). DEVICE
  * pointers; synchronous. */
