@@ -75,6 +75,9 @@ def parse_args():
     ap.add_argument("--variants", default=",".join(VARIANTS),
                     help="comma-separated solver variants to run "
                          "(plain_mgpcg, mixed_mgpcg, learned_fpcg)")
+    ap.add_argument("--conv-only", action="store_true",
+                    help="time only the network's 128^3 convolutions (the "
+                         "roofline_tensor block) and print it; for profiling")
     return ap.parse_args()
 
 
@@ -899,6 +902,10 @@ def run_reference(args, rank, world, pg):
 def main():
     args = parse_args()
     rank, world, local, pg = dist_setup(args)
+    if args.conv_only:
+        if rank == 0:
+            print(json.dumps(run_unet(local)), flush=True)
+        return
     if args.impl == "reference":
         line = run_reference(args, rank, world, pg)
         if line is not None:

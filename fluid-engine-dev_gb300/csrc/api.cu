@@ -256,6 +256,53 @@ jetgpu_status ensure_buffers(Ctx* c, Dims n, unsigned max_levels) {
     return JETGPU_OK;
 }
 
+// Runs the launches issued inside its scope on `st` instead of the
+// compute stream.
+struct OnStream {
+    Ctx* c;
+    cudaStream_t saved;
+    OnStream(Ctx* ctx, cudaStream_t st) : c(ctx), saved(ctx->stream) {
+        c->stream = st;
+    }
+    ~OnStream() { c->stream = saved; }
+};
+
+// Everything after the finest level's weights: the coarse levels (weight
+// pyramid, rows, BF16 copies) need only those weights, the finest level's
+// FP64 rows also the velocities. The coarse levels are built on the
+// high-priority side stream while the finest rows are built on the compute
+// stream: that kernel is FP64-bound, and the pyramid's memory-bound
+// restrictions take the SM slots its blocks free. With host inputs, the
+// coarse levels are built while the velocities still upload. The live
+// profile times launches on the compute stream, so with it on everything
+// stays on that stream.
+static jetgpu_status build_levels(Ctx* c, const GridDesc& g, const double* u,
+                                  const double* v, const double* w,
+                                  const double* su, const double* sv,
+                                  const double* sw, const SolveIo* io) {
+    const bool fork = !c->prof_on && c->built_levels > 1;
+    jetgpu_status s = JETGPU_OK;
+    if (fork) {
+        JG_CUDA(c, cudaEventRecord(c->side_ev[0], c->stream));
+        JG_CUDA(c, cudaStreamWaitEvent(c->side_stream, c->side_ev[0], 0));
+    }
+    {
+        OnStream on(c, fork ? c->side_stream : c->stream);
+        if ((s = build_pyramid(c)) != JETGPU_OK) return s;
+        if ((s = build_system(c, g, nullptr, nullptr, nullptr, nullptr,
+                              nullptr, nullptr, 1)) != JETGPU_OK)
+            return s;
+        if ((s = prepare_levels(c, 1)) != JETGPU_OK) return s;
+        if (fork) JG_CUDA(c, cudaEventRecord(c->side_ev[1], c->stream));
+    }
+    if (io) JG_CUDA(c, cudaStreamWaitEvent(c->stream, io->vel_in, 0));
+    if ((s = build_system(c, g, u, v, w, su, sv, sw, 0, 1)) != JETGPU_OK)
+        return s;
+    if ((s = prepare_levels(c, 0, 1)) != JETGPU_OK) return s;
+    if (fork) JG_CUDA(c, cudaStreamWaitEvent(c->stream, c->side_ev[1], 0));
+    return JETGPU_OK;
+}
+
 // The device-resident pipeline shared by the host and device entry points.
 jetgpu_status solve_pressure_dev(
     Ctx* c, const jetgpu_grid* grid, const double* u, const double* v,
@@ -273,23 +320,15 @@ jetgpu_status solve_pressure_dev(
     JG_CUDA(c, cudaEventRecord(c->ev[0], c->stream));
     if (io) JG_CUDA(c, cudaStreamWaitEvent(c->stream, io->sdf_in, 0));
     s = blocked ? blocked_markers(c, g, to_desc(bsdf, bdata), to_desc(fsdf, fdata))
-                : build_weights(c, g, to_desc(bsdf, bdata), to_desc(fsdf, fdata));
+                : build_weights(c, g, to_desc(bsdf, bdata), to_desc(fsdf, fdata),
+                                false);
     if (s != JETGPU_OK) return s;
-    if (io && !blocked) {
-        // The coarse levels' rows need only the weights: built while the
-        // velocities are still uploading, level 0 (which reads them) after.
-        if ((s = build_system(c, g, nullptr, nullptr, nullptr, nullptr,
-                              nullptr, nullptr, 1)) != JETGPU_OK)
-            return s;
-        if ((s = prepare_levels(c, 1)) != JETGPU_OK) return s;
-        JG_CUDA(c, cudaStreamWaitEvent(c->stream, io->vel_in, 0));
-        if ((s = build_system(c, g, u, v, w, su, sv, sw, 0, 1)) != JETGPU_OK)
-            return s;
-        if ((s = prepare_levels(c, 0, 1)) != JETGPU_OK) return s;
+    if (!blocked) {
+        s = build_levels(c, g, u, v, w, su, sv, sw, io);
+        if (s != JETGPU_OK) return s;
     } else {
         if (io) JG_CUDA(c, cudaStreamWaitEvent(c->stream, io->vel_in, 0));
-        s = blocked ? blocked_system(c, g, u, v, w)
-                    : build_system(c, g, u, v, w, su, sv, sw);
+        s = blocked_system(c, g, u, v, w);
         if (s != JETGPU_OK) return s;
         s = prepare_levels(c);
         if (s != JETGPU_OK) return s;
@@ -379,7 +418,14 @@ jetgpu_status jetgpu_create(const jetgpu_config* cfg, jetgpu_ctx** out) {
                                              cudaStreamNonBlocking));
         JG_CUDA(c, cudaStreamCreateWithFlags(&c->copy_stream,
                                              cudaStreamNonBlocking));
+        int least = 0, greatest = 0;
+        JG_CUDA(c, cudaDeviceGetStreamPriorityRange(&least, &greatest));
+        JG_CUDA(c, cudaStreamCreateWithPriority(&c->side_stream,
+                                                cudaStreamNonBlocking,
+                                                greatest));
         for (auto& e : c->io_ev)
+            JG_CUDA(c, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        for (auto& e : c->side_ev)
             JG_CUDA(c, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
         JG_CUDA(c, cudaMalloc((void**)&c->scal, S_COUNT * sizeof(double)));
         JG_CUDA(c, cudaMemset(c->scal, 0, S_COUNT * sizeof(double)));
@@ -422,6 +468,8 @@ void jetgpu_destroy(jetgpu_ctx* c) {
     release(&c->sdf_dbl);
     release(&c->sdf_valid);
     release(&c->blk_marks);
+    release(&c->build_list);
+    release(&c->build_cnt);
     release(&c->flip_marks);
     release(&c->flip_snap);
     release(&c->flip_solid);
@@ -444,6 +492,9 @@ void jetgpu_destroy(jetgpu_ctx* c) {
     }
     for (auto& e : c->io_ev)
         if (e) cudaEventDestroy(e);
+    for (auto& e : c->side_ev)
+        if (e) cudaEventDestroy(e);
+    if (c->side_stream) cudaStreamDestroy(c->side_stream);
     if (c->copy_stream) cudaStreamDestroy(c->copy_stream);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
@@ -1390,14 +1441,21 @@ jetgpu_status jetgpu_harvest(jetgpu_ctx* c, unsigned int max_pairs,
     return harvest_pairs(c, max_pairs, r_out, z_out, count);
 }
 
-jetgpu_status jetgpu_net_features(jetgpu_ctx* c, const float* r, void* feat) {
+unsigned jetgpu_net_level(const jetgpu_ctx* c) {
+    return (c && c->built_levels > 0) ? net_level(c) : 0u;
+}
+
+jetgpu_status jetgpu_net_features(jetgpu_ctx* c, unsigned level,
+                                  const float* r, void* feat) {
     if (!c || !r || !feat) return JETGPU_BAD_INPUT;
     if (c->built_levels == 0)
         return fail(c, JETGPU_BAD_INPUT, "no system: run a pressure solve first");
+    if (level >= c->built_levels)
+        return fail(c, JETGPU_BAD_INPUT, "level beyond the built hierarchy");
     JG_CUDA(c, cudaSetDevice(c->device));
-    jetgpu_status s = norm2f(c, r, c->levels[0].n.count(), S_MEAN);
+    jetgpu_status s = norm2f(c, r, c->levels[level].n.count(), S_MEAN);
     if (s != JETGPU_OK) return s;
-    s = net_features(c, r, c->scal + S_MEAN, feat);
+    s = net_features(c, level, r, c->scal + S_MEAN, feat);
     if (s != JETGPU_OK) return s;
     JG_CUDA(c, cudaStreamSynchronize(c->stream));
     return JETGPU_OK;
@@ -1423,16 +1481,36 @@ jetgpu_status jetgpu_vcycle_apply(jetgpu_ctx* c, const float* r, float* z) {
     return JETGPU_OK;
 }
 
-jetgpu_status jetgpu_net_apply(jetgpu_ctx* c, const float* r, float* z) {
-    if (!c || !r || !z) return JETGPU_BAD_INPUT;
+jetgpu_status jetgpu_net_apply(jetgpu_ctx* c, unsigned level, const float* r,
+                               float* e) {
+    if (!c || !r || !e) return JETGPU_BAD_INPUT;
+    if (c->built_levels == 0 || !c->unet)
+        return fail(c, JETGPU_BAD_INPUT,
+                    "needs a solved system and a loaded network");
+    if (level >= c->built_levels)
+        return fail(c, JETGPU_BAD_INPUT, "level beyond the built hierarchy");
+    const Dims n = c->levels[level].n;
+    if (n.x % 8 || n.y % 8 || n.z % 8)
+        return fail(c, JETGPU_BAD_INPUT,
+                    "the network needs a level whose extents are multiples "
+                    "of 8");
+    JG_CUDA(c, cudaSetDevice(c->device));
+    jetgpu_status s = norm2f(c, r, n.count(), S_MEAN);
+    if (s != JETGPU_OK) return s;
+    s = net_apply(c, level, r, c->scal + S_MEAN, e);
+    if (s != JETGPU_OK) return s;
+    JG_CUDA(c, cudaStreamSynchronize(c->stream));
+    return JETGPU_OK;
+}
+
+jetgpu_status jetgpu_learned_apply(jetgpu_ctx* c, const float* r, float* z) {
+    if (!c || !r || !z || r == z) return JETGPU_BAD_INPUT;
     if (c->built_levels == 0 || !net_supported(c))
         return fail(c, JETGPU_BAD_INPUT,
-                    "needs a solved system with resolution divisible by 8 and "
-                    "a loaded network");
+                    "needs a solved system whose network level has extents "
+                    "divisible by 8, and a loaded network");
     JG_CUDA(c, cudaSetDevice(c->device));
-    jetgpu_status s = norm2f(c, r, c->levels[0].n.count(), S_MEAN);
-    if (s != JETGPU_OK) return s;
-    s = net_apply(c, r, c->scal + S_MEAN, z);
+    jetgpu_status s = learned_precond(c, r, z);
     if (s != JETGPU_OK) return s;
     JG_CUDA(c, cudaStreamSynchronize(c->stream));
     return JETGPU_OK;

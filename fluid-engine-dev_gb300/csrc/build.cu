@@ -13,6 +13,8 @@
 
 #include "ctx.h"
 
+#include <algorithm>
+
 #include <cfloat>
 #include <cmath>
 #include <cstring>
@@ -367,6 +369,62 @@ __global__ void k_restrict_f32(const float* __restrict__ fine, Dims fs,
     }
 }
 
+// k_restrict_f32 for two coarse cells (2p, 2p+1) of a row per thread, on
+// arrays whose x axis is fully restricted (fine x = 2 coarse x, coarse x
+// even: the fluid SDF and the v/w face weights). The 6 fine x taps of the
+// pair (4p-1 .. 4p+4, clamped) are one aligned 16-byte load and two scalar
+// loads per fine row; each output keeps k_restrict_f32's weights and its
+// z, y, x order of products and sums, so the results are the same bits.
+__global__ void k_restrict_f32x2(const float* __restrict__ fine, Dims fs,
+                                 float* __restrict__ coarse, Dims cs) {
+    const Dims q{cs.x / 2, cs.y, cs.z};
+    const long G = q.count();
+    const int ksy = (fs.y != 2 * cs.y) ? 3 : 4;
+    const int ksz = (fs.z != 2 * cs.z) ? 3 : 4;
+    const float cen[4] = {0.125f, 0.375f, 0.375f, 0.125f};
+    const float stg[4] = {0.f, 1.f, 0.f, 0.f};
+    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < G;
+         t += (long)gridDim.x * blockDim.x) {
+        int p, j, k;
+        cell_ijk(t, q, p, j, k);
+        int jI[4], kI[4];
+        auto taps = [](int ks, int c, int nc, int* o) {
+            o[0] = (c > 0) ? 2 * c - 1 : 2 * c;
+            o[1] = 2 * c;
+            if (ks == 3) {
+                o[2] = (c + 1 < nc) ? 2 * c + 1 : 2 * c;
+                o[3] = 0;
+            } else {
+                o[2] = 2 * c + 1;
+                o[3] = (c + 1 < nc) ? 2 * c + 2 : 2 * c + 1;
+            }
+        };
+        taps(ksy, j, cs.y, jI);
+        taps(ksz, k, cs.z, kI);
+        const float* ky = (ksy == 3) ? stg : cen;
+        const float* kz = (ksz == 3) ? stg : cen;
+        const int xm = p > 0 ? 4 * p - 1 : 4 * p;           // tap 0 of 2p
+        const int x4 = 2 * p + 2 < cs.x ? 4 * p + 4 : 4 * p + 3;  // tap 3 of 2p+1
+        float sum0 = 0.0f, sum1 = 0.0f;
+        for (int z = 0; z < ksz; ++z)
+            for (int y = 0; y < ksy; ++y) {
+                const float* row = fine + lin(0, jI[y], kI[z], fs.x, fs.y);
+                const float4 f = *reinterpret_cast<const float4*>(row + 4 * p);
+                const float v0[4] = {row[xm], f.x, f.y, f.z};
+                const float v1[4] = {f.y, f.z, f.w, row[x4]};
+                const float wyz = ky[y] * kz[z];
+#pragma unroll
+                for (int x = 0; x < 4; ++x) {
+                    sum0 += cen[x] * wyz * v0[x];
+                    sum1 += cen[x] * wyz * v1[x];
+                }
+            }
+        const long o = lin(2 * p, j, k, cs.x, cs.y);
+        coarse[o] = sum0;
+        coarse[o + 1] = sum1;
+    }
+}
+
 // Air-side term of buildSingleSystem: term / max(theta, 0.01) with theta =
 // fractionInsideSdf(phi_c, phi_n). Out of line, so warps without a
 // free-surface face never issue its FP64 divisions.
@@ -383,151 +441,187 @@ struct SpacingInv {
     int pow2;
 };
 
-// K4: buildSingleSystem (:117-267). Writes the FP32 rows of every level;
-// on the finest level also the exact FP64 rows and rhs. u/v/w are the input
-// velocity (finest level only; coarse right-hand sides are dead, overwritten
-// by restriction in the V-cycle, include/jet/detail/mg-inl.h:28-30). Every
-// FP64 sum and product is the reference's, in its order; what changes is how
-// the exact ones are issued: classification on the FP32 SDF, exact widening
-// and power-of-two scaling on the integer pipe, divisions out of line.
-//
-// Latency-bound at the 94 registers it would take freely (two blocks per
-// SM): capped at 64 for four blocks, with a few spilled values, it runs
-// 1.6x faster (1.21 -> 0.77 ms per 256^3 solve).
-__global__ void __launch_bounds__(kThreads, 4)
-    k_build_system(Dims n, SpacingInv S,
-                               const float* __restrict__ phi,
-                               const float* __restrict__ uw,
-                               const float* __restrict__ vw,
-                               const float* __restrict__ ww,
-                               const double* __restrict__ u,
-                               const double* __restrict__ v,
-                               const double* __restrict__ w,
-                               const double* __restrict__ su,
-                               const double* __restrict__ sv,
-                               const double* __restrict__ sw,
-                               double* __restrict__ A64,
-                               double* __restrict__ b64,
-                               float* __restrict__ A32,
-                               float4* __restrict__ Alo,
-                               float2* __restrict__ bdf) {
+// Appends v to list (length *cnt) when `want`, one atomic per warp.
+__device__ __forceinline__ void append_if(bool want, int v,
+                                          int* __restrict__ list,
+                                          unsigned* __restrict__ cnt) {
+    const unsigned act = __activemask();
+    const unsigned mask = __ballot_sync(act, want);
+    if (mask == 0u) return;
+    const int lane = threadIdx.x & 31, leader = __ffs(mask) - 1;
+    unsigned base = 0u;
+    if (lane == leader) base = atomicAdd(cnt, (unsigned)__popc(mask));
+    base = __shfl_sync(act, base, leader);
+    if (want) list[base + __popc(mask & ((1u << lane) - 1u))] = v;
+}
+
+// K4: buildSingleSystem (:117-267), one cell. Writes the FP32 rows of every
+// level; on the finest level also the exact FP64 rows and rhs. u/v/w are the
+// input velocity (finest level only; coarse right-hand sides are dead,
+// overwritten by restriction in the V-cycle, include/jet/detail/mg-inl.h:
+// 28-30). Every FP64 sum and product is the reference's, in its order; what
+// changes is how the exact ones are issued: classification on the FP32 SDF,
+// exact widening and power-of-two scaling on the integer pipe, divisions out
+// of line.
+__device__ __forceinline__ void build_cell(long c, Dims n, const SpacingInv& S,
+                                           const float* __restrict__ phi,
+                                           const float* __restrict__ uw,
+                                           const float* __restrict__ vw,
+                                           const float* __restrict__ ww,
+                                           const double* __restrict__ u,
+                                           const double* __restrict__ v,
+                                           const double* __restrict__ w,
+                                           const double* __restrict__ su,
+                                           const double* __restrict__ sv,
+                                           const double* __restrict__ sw,
+                                           double* __restrict__ A64,
+                                           double* __restrict__ b64,
+                                           float* __restrict__ A32,
+                                           float4* __restrict__ Alo,
+                                           float2* __restrict__ bdf) {
     const long N = n.count();
     const int ux = n.x + 1;  // u-face row length
     const bool pw = S.pow2 != 0;
-    for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < N;
-         c += (long)gridDim.x * blockDim.x) {
-        int i, j, k;
-        cell_ijk(c, n, i, j, k);
-        double center = 0.0, right = 0.0, up = 0.0, front = 0.0, bb = 0.0;
-        const float cphf = phi[c];
-        bool fluid = false;
-        if (cphf < 0.0f) {  // the same test as on the exact widening
-            fluid = true;
-            const double cphi = widen_f32(cphf);
-            const long uR = lin(i + 1, j, k, ux, n.y), uL = lin(i, j, k, ux, n.y);
-            const long vU = lin(i, j + 1, k, n.x, n.y + 1),
-                       vD = lin(i, j, k, n.x, n.y + 1);
-            const long wF = lin(i, j, k + 1, n.x, n.y), wB = lin(i, j, k, n.x, n.y);
-            const long sy = n.x, sz = (long)n.x * n.y;
-            // One face: the centre term (or the air-side term), the
-            // off-diagonal of a fluid neighbour on the upper side, and the
-            // rhs term (weighted inside, unweighted on the domain boundary).
-            auto face = [&](bool has, const float* wts, long f, long nbc, int a,
-                            const double* vel, bool plus, double* off) {
-                if (has) {
-                    const double wd = widen_f32(wts[f]);
-                    const double term = pw ? scale_pow2(wd, S.k2[a], S.ih2[a])
-                                           : wd * S.ih2[a];
-                    const float npf = phi[nbc];
-                    if (npf < 0.0f) {
-                        center += term;
-                        if (off) *off = zero_minus(term);  // 0.0 - term
-                    } else {
-                        center += air_term(term, cphi, widen_f32(npf));
-                    }
-                    if (vel) {
-                        const double p = wd * vel[f];
-                        const double t = pw ? scale_pow2(p, S.k[a], S.ih[a])
-                                            : p * S.ih[a];
-                        bb = plus ? bb + t : bb - t;
-                    }
-                } else if (vel) {
-                    const double t = pw ? scale_pow2(vel[f], S.k[a], S.ih[a])
-                                        : vel[f] * S.ih[a];
+    int i, j, k;
+    cell_ijk(c, n, i, j, k);
+    double center = 0.0, right = 0.0, up = 0.0, front = 0.0, bb = 0.0;
+    const float cphf = phi[c];
+    bool fluid = false;
+    if (cphf < 0.0f) {  // the same test as on the exact widening
+        fluid = true;
+        const double cphi = widen_f32(cphf);
+        const long uR = lin(i + 1, j, k, ux, n.y), uL = lin(i, j, k, ux, n.y);
+        const long vU = lin(i, j + 1, k, n.x, n.y + 1),
+                   vD = lin(i, j, k, n.x, n.y + 1);
+        const long wF = lin(i, j, k + 1, n.x, n.y), wB = lin(i, j, k, n.x, n.y);
+        const long sy = n.x, sz = (long)n.x * n.y;
+        // One face: the centre term (or the air-side term), the
+        // off-diagonal of a fluid neighbour on the upper side, and the
+        // rhs term (weighted inside, unweighted on the domain boundary).
+        auto face = [&](bool has, const float* wts, long f, long nbc, int a,
+                        const double* vel, bool plus, double* off) {
+            if (has) {
+                const double wd = widen_f32(wts[f]);
+                const double term = pw ? scale_pow2(wd, S.k2[a], S.ih2[a])
+                                       : wd * S.ih2[a];
+                const float npf = phi[nbc];
+                if (npf < 0.0f) {
+                    center += term;
+                    if (off) *off = zero_minus(term);  // 0.0 - term
+                } else {
+                    center += air_term(term, cphi, widen_f32(npf));
+                }
+                if (vel) {
+                    const double p = wd * vel[f];
+                    const double t = pw ? scale_pow2(p, S.k[a], S.ih[a])
+                                        : p * S.ih[a];
                     bb = plus ? bb + t : bb - t;
                 }
-            };
-            face(i + 1 < n.x, uw, uR, c + 1, 0, u, true, &right);
-            face(i > 0, uw, uL, c - 1, 0, u, false, nullptr);
-            face(j + 1 < n.y, vw, vU, c + sy, 1, v, true, &up);
-            face(j > 0, vw, vD, c - sy, 1, v, false, nullptr);
-            face(k + 1 < n.z, ww, wF, c + sz, 2, w, true, &front);
-            face(k > 0, ww, wB, c - sz, 2, w, false, nullptr);
-            if (u && !su && !sv && !sw) {
-                // Static collider: every term of the moving-boundary sum is
-                // (1 - w) * 0 * invH = +0, so the sum is +0 and adding it
-                // only turns -0 into +0 — exactly what this does.
-                unsigned lo, hi;
-                dwords(bb, lo, hi);
-                if (hi == 0x80000000u && lo == 0u) bb = djoin(0u, 0u);
-            } else if (u) {
-                // Moving-boundary contribution (:241-255), evaluated as the
-                // reference's single left-to-right expression.
-                const double ihx = S.ih[0], ihy = S.ih[1], ihz = S.ih[2];
-                const double sR = su ? su[uR] : 0.0, sL = su ? su[uL] : 0.0;
-                const double sU = sv ? sv[vU] : 0.0, sD = sv ? sv[vD] : 0.0;
-                const double sF = sw ? sw[wF] : 0.0, sB = sw ? sw[wB] : 0.0;
-                const double contrib = (1.0 - (double)uw[uR]) * sR * ihx -
-                                       (1.0 - (double)uw[uL]) * sL * ihx +
-                                       (1.0 - (double)vw[vU]) * sU * ihy -
-                                       (1.0 - (double)vw[vD]) * sD * ihy +
-                                       (1.0 - (double)ww[wF]) * sF * ihz -
-                                       (1.0 - (double)ww[wB]) * sB * ihz;
-                bb += contrib;
+            } else if (vel) {
+                const double t = pw ? scale_pow2(vel[f], S.k[a], S.ih[a])
+                                    : vel[f] * S.ih[a];
+                bb = plus ? bb + t : bb - t;
             }
-            // center < kEpsilonD (:259-262); center is a sum of non-negative
-            // terms, so its bit pattern orders like its value.
-            unsigned clo, chi;
-            dwords(center, clo, chi);
-            const unsigned long long cbits =
-                ((unsigned long long)chi << 32) | clo;
-            if (cbits < 0x3CB0000000000000ULL) {  // DBL_EPSILON
-                center = 1.0;
-                bb = 0.0;
-            }
-        } else {
+        };
+        face(i + 1 < n.x, uw, uR, c + 1, 0, u, true, &right);
+        face(i > 0, uw, uL, c - 1, 0, u, false, nullptr);
+        face(j + 1 < n.y, vw, vU, c + sy, 1, v, true, &up);
+        face(j > 0, vw, vD, c - sy, 1, v, false, nullptr);
+        face(k + 1 < n.z, ww, wF, c + sz, 2, w, true, &front);
+        face(k > 0, ww, wB, c - sz, 2, w, false, nullptr);
+        if (u && !su && !sv && !sw) {
+            // Static collider: every term of the moving-boundary sum is
+            // (1 - w) * 0 * invH = +0, so the sum is +0 and adding it
+            // only turns -0 into +0 — exactly what this does.
+            unsigned lo, hi;
+            dwords(bb, lo, hi);
+            if (hi == 0x80000000u && lo == 0u) bb = djoin(0u, 0u);
+        } else if (u) {
+            // Moving-boundary contribution (:241-255), evaluated as the
+            // reference's single left-to-right expression.
+            const double ihx = S.ih[0], ihy = S.ih[1], ihz = S.ih[2];
+            const double sR = su ? su[uR] : 0.0, sL = su ? su[uL] : 0.0;
+            const double sU = sv ? sv[vU] : 0.0, sD = sv ? sv[vD] : 0.0;
+            const double sF = sw ? sw[wF] : 0.0, sB = sw ? sw[wB] : 0.0;
+            const double contrib = (1.0 - (double)uw[uR]) * sR * ihx -
+                                   (1.0 - (double)uw[uL]) * sL * ihx +
+                                   (1.0 - (double)vw[vU]) * sU * ihy -
+                                   (1.0 - (double)vw[vD]) * sD * ihy +
+                                   (1.0 - (double)ww[wF]) * sF * ihz -
+                                   (1.0 - (double)ww[wB]) * sB * ihz;
+            bb += contrib;
+        }
+        // center < kEpsilonD (:259-262); center is a sum of non-negative
+        // terms, so its bit pattern orders like its value.
+        unsigned clo, chi;
+        dwords(center, clo, chi);
+        const unsigned long long cbits =
+            ((unsigned long long)chi << 32) | clo;
+        if (cbits < 0x3CB0000000000000ULL) {  // DBL_EPSILON
             center = 1.0;
+            bb = 0.0;
         }
-        if (A64) {
-            A64[4 * c + 0] = center;
-            A64[4 * c + 1] = right;
-            A64[4 * c + 2] = up;
-            A64[4 * c + 3] = front;
-        }
-        if (b64) b64[c] = bb;
-        // FP32 rows (= the FP32 rounding of the exact rows) and, on the
-        // finest level, the low parts that make hi + lo carry ~48 bits of
-        // each coefficient and of b for the double-float true residual.
-        float4 hi4, lo4;
-        float bh, bl;
-        if (fluid) {
-            split_f64(center, hi4.x, lo4.x);
-            split_f64(right, hi4.y, lo4.y);
-            split_f64(up, hi4.z, lo4.z);
-            split_f64(front, hi4.w, lo4.w);
-            split_f64(bb, bh, bl);
-        } else {
-            hi4 = make_float4(1.0f, 0.0f, 0.0f, 0.0f);
-            lo4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
-            bh = bl = 0.0f;
-        }
-        A32[c] = hi4.x;  // structure of arrays: center, right, up, front
-        A32[N + c] = hi4.y;
-        A32[2 * N + c] = hi4.z;
-        A32[3 * N + c] = hi4.w;
-        if (Alo) Alo[c] = lo4;
-        if (bdf) bdf[c] = make_float2(bh, bl);
+    } else {
+        center = 1.0;
     }
+    if (A64) {  // one 32-byte row as two 16-byte stores
+        double2* row = reinterpret_cast<double2*>(A64 + 4 * c);
+        row[0] = make_double2(center, right);
+        row[1] = make_double2(up, front);
+    }
+    if (b64) b64[c] = bb;
+    // FP32 rows (= the FP32 rounding of the exact rows) and, on the
+    // finest level, the low parts that make hi + lo carry ~48 bits of
+    // each coefficient and of b for the double-float true residual.
+    float4 hi4, lo4;
+    float bh, bl;
+    if (fluid) {
+        split_f64(center, hi4.x, lo4.x);
+        split_f64(right, hi4.y, lo4.y);
+        split_f64(up, hi4.z, lo4.z);
+        split_f64(front, hi4.w, lo4.w);
+        split_f64(bb, bh, bl);
+    } else {
+        hi4 = make_float4(1.0f, 0.0f, 0.0f, 0.0f);
+        lo4 = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+        bh = bl = 0.0f;
+    }
+    A32[c] = hi4.x;  // structure of arrays: center, right, up, front
+    A32[N + c] = hi4.y;
+    A32[2 * N + c] = hi4.z;
+    A32[3 * N + c] = hi4.w;
+    if (Alo) Alo[c] = lo4;
+    if (bdf) bdf[c] = make_float2(bh, bl);
+}
+
+// K4's kernel. Latency-bound at the 94 registers it would take freely (two
+// blocks per SM): capped at 64 for four blocks, with a few spilled values,
+// it runs 1.6x faster (1.21 -> 0.77 ms per 256^3 solve). (Compacting the
+// fluid cells next to air into full warps for their FP64 divisions, as the
+// face weights do, made it slower: the sums and the rhs of every fluid cell
+// are FP64 too, so little of its FP64 work is divergent.)
+__global__ void __launch_bounds__(kThreads, 4)
+    k_build_system(Dims n, SpacingInv S,
+                   const float* __restrict__ phi,
+                   const float* __restrict__ uw,
+                   const float* __restrict__ vw,
+                   const float* __restrict__ ww,
+                   const double* __restrict__ u,
+                   const double* __restrict__ v,
+                   const double* __restrict__ w,
+                   const double* __restrict__ su,
+                   const double* __restrict__ sv,
+                   const double* __restrict__ sw,
+                   double* __restrict__ A64,
+                   double* __restrict__ b64,
+                   float* __restrict__ A32,
+                   float4* __restrict__ Alo,
+                   float2* __restrict__ bdf) {
+    const long N = n.count();
+    for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < N;
+         c += (long)gridDim.x * blockDim.x)
+        build_cell(c, n, S, phi, uw, vw, ww, u, v, w, su, sv, sw, A64, b64,
+                   A32, Alo, bdf);
 }
 
 // Double-float image of a caller-built finest-level system (the FP32 rows
@@ -808,49 +902,92 @@ __global__ void k_node_grid(FieldDesc B, const int* __restrict__ sidx,
     }
 }
 
-// Face weights from the node grid. slot[] maps a table entry to its slot.
-__global__ void k_face_weights_nodes(float* __restrict__ wgt, int axis,
+// The four corner samples of face c of axis `axis` from the node grid.
+// slot[] maps a table entry to its slot.
+template <int axis>
+__device__ __forceinline__ void face_corners(long c, Dims fn,
+                                             const int* __restrict__ slot,
+                                             const TabLayout& L, int3 S,
+                                             const double* __restrict__ node,
+                                             double p[4]) {
+    int i, j, k;
+    cell_ijk(c, fn, i, j, k);
+    // Lower/upper slot along each axis: N for the normal axis (same for
+    // both), M/P for the tangential axes.
+    const int q[3] = {i, j, k};
+    int lo[3], hi[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+        if (a == axis) {
+            lo[a] = hi[a] = slot[L.off[a][0] + q[a]];
+        } else {
+            lo[a] = slot[L.off[a][1] + q[a]];
+            hi[a] = slot[L.off[a][2] + q[a]];
+        }
+    }
+    auto at = [&](int x, int y, int z) {
+        return node[x + (long)S.x * (y + (long)S.y * z)];
+    };
+    if (axis == 0) {  // (0,-y,-z) (0,+y,-z) (0,-y,+z) (0,+y,+z)
+        p[0] = at(lo[0], lo[1], lo[2]);
+        p[1] = at(lo[0], hi[1], lo[2]);
+        p[2] = at(lo[0], lo[1], hi[2]);
+        p[3] = at(lo[0], hi[1], hi[2]);
+    } else if (axis == 1) {  // (-x,0,-z) (-x,0,+z) (+x,0,-z) (+x,0,+z)
+        p[0] = at(lo[0], lo[1], lo[2]);
+        p[1] = at(lo[0], lo[1], hi[2]);
+        p[2] = at(hi[0], lo[1], lo[2]);
+        p[3] = at(hi[0], lo[1], hi[2]);
+    } else {  // (-x,-y,0) (-x,+y,0) (+x,-y,0) (+x,+y,0)
+        p[0] = at(lo[0], lo[1], lo[2]);
+        p[1] = at(lo[0], hi[1], lo[2]);
+        p[2] = at(hi[0], lo[1], lo[2]);
+        p[3] = at(hi[0], hi[1], lo[2]);
+    }
+}
+
+
+// Face weights from the node grid, first pass: a face whose four corners
+// lie on one side gets weight 0 or 1 from integer sign tests (face_weight's
+// own shortcut); every other face (the thin shell around the collider
+// surface) is appended to a list for k_face_weights_listed. GB300 issues
+// FP64 at a small fraction of its FP32 rate and a warp runs the
+// marching-squares divisions for all its lanes, so gathering the few such
+// faces into full warps keeps the FP64 pipe from serving idle lanes.
+template <int axis>
+__global__ void k_face_weights_nodes(float* __restrict__ wgt,
                                      Dims fn, const int* __restrict__ slot,
                                      TabLayout L, int3 S,
-                                     const double* __restrict__ node) {
+                                     const double* __restrict__ node,
+                                     int* __restrict__ list,
+                                     unsigned* __restrict__ cnt) {
     const long N = fn.count();
     for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < N;
          c += (long)gridDim.x * blockDim.x) {
-        int i, j, k;
-        cell_ijk(c, fn, i, j, k);
-        // Lower/upper slot along each axis: N for the normal axis (same for
-        // both), M/P for the tangential axes.
-        const int q[3] = {i, j, k};
-        int lo[3], hi[3];
-        for (int a = 0; a < 3; ++a) {
-            if (a == axis) {
-                lo[a] = hi[a] = slot[L.off[a][0] + q[a]];
-            } else {
-                lo[a] = slot[L.off[a][1] + q[a]];
-                hi[a] = slot[L.off[a][2] + q[a]];
-            }
-        }
-        auto at = [&](int x, int y, int z) {
-            return node[x + (long)S.x * (y + (long)S.y * z)];
-        };
-        double p0, p1, p2, p3;
-        if (axis == 0) {  // (0,-y,-z) (0,+y,-z) (0,-y,+z) (0,+y,+z)
-            p0 = at(lo[0], lo[1], lo[2]);
-            p1 = at(lo[0], hi[1], lo[2]);
-            p2 = at(lo[0], lo[1], hi[2]);
-            p3 = at(lo[0], hi[1], hi[2]);
-        } else if (axis == 1) {  // (-x,0,-z) (-x,0,+z) (+x,0,-z) (+x,0,+z)
-            p0 = at(lo[0], lo[1], lo[2]);
-            p1 = at(lo[0], lo[1], hi[2]);
-            p2 = at(hi[0], lo[1], lo[2]);
-            p3 = at(hi[0], lo[1], hi[2]);
-        } else {  // (-x,-y,0) (-x,+y,0) (+x,-y,0) (+x,+y,0)
-            p0 = at(lo[0], lo[1], lo[2]);
-            p1 = at(lo[0], hi[1], lo[2]);
-            p2 = at(hi[0], lo[1], lo[2]);
-            p3 = at(hi[0], hi[1], lo[2]);
-        }
-        wgt[c] = face_weight(p0, p1, p2, p3);
+        double p[4];
+        face_corners<axis>(c, fn, slot, L, S, node, p);
+        const int nin = neg_d(p[0]) + neg_d(p[1]) + neg_d(p[2]) + neg_d(p[3]);
+        const bool hard = nin != 0 && nin != 4;
+        if (!hard) wgt[c] = nin == 4 ? 0.0f : 1.0f;
+        append_if(hard, (int)c, list, cnt);
+    }
+}
+
+// Second pass: the listed faces, with the full face_weight.
+template <int axis>
+__global__ void k_face_weights_listed(float* __restrict__ wgt,
+                                      Dims fn, const int* __restrict__ slot,
+                                      TabLayout L, int3 S,
+                                      const double* __restrict__ node,
+                                      const int* __restrict__ list,
+                                      const unsigned* __restrict__ cnt) {
+    const unsigned m = *cnt;
+    for (unsigned q = blockIdx.x * blockDim.x + threadIdx.x; q < m;
+         q += gridDim.x * blockDim.x) {
+        const long c = list[q];
+        double p[4];
+        face_corners<axis>(c, fn, slot, L, S, node, p);
+        wgt[c] = face_weight(p[0], p[1], p[2], p[3]);
     }
 }
 
@@ -1000,9 +1137,22 @@ TabLayout layout_of(const SampleTables& T) {
 
 }  // namespace
 
+// The compaction list of the two-pass face-weight kernels: room for n
+// entries and a counter.
+static jetgpu_status grow_list(Ctx* c, size_t n) {
+    if (!c->build_cnt)
+        JG_CUDA(c, cudaMalloc((void**)&c->build_cnt, sizeof(unsigned)));
+    if (c->build_cap >= n) return JETGPU_OK;
+    if (c->build_list) cudaFree(c->build_list);
+    c->build_list = nullptr;
+    c->build_cap = 0;
+    JG_CUDA(c, cudaMalloc((void**)&c->build_list, n * sizeof(int)));
+    c->build_cap = n;
+    return JETGPU_OK;
+}
+
 jetgpu_status build_weights(Ctx* c, const GridDesc& g, const FieldDesc& bsdf,
                             const FieldDesc& fsdf, bool pyramid) {
-    const unsigned nl = c->built_levels;
     Level& L0 = c->levels[0];
     const Dims n = L0.n;
     const Dims fu{n.x + 1, n.y, n.z}, fv{n.x, n.y + 1, n.z},
@@ -1031,15 +1181,30 @@ jetgpu_status build_weights(Ctx* c, const GridDesc& g, const FieldDesc& bsdf,
             const long nodes = (long)S.x * S.y * S.z;
             k_node_grid<<<blocks_for(nodes), kThreads, 0, c->stream>>>(
                 bsdf, T.sidx, T.sfrac, so, S, T.node);
-            k_face_weights_nodes<<<blocks_for(fu.count()), kThreads, 0,
-                                   c->stream>>>(L0.uw, 0, fu, T.slot, TL, S,
-                                                T.node);
-            k_face_weights_nodes<<<blocks_for(fv.count()), kThreads, 0,
-                                   c->stream>>>(L0.vw, 1, fv, T.slot, TL, S,
-                                                T.node);
-            k_face_weights_nodes<<<blocks_for(fw.count()), kThreads, 0,
-                                   c->stream>>>(L0.ww, 2, fw, T.slot, TL, S,
-                                                T.node);
+            float* wts[3] = {L0.uw, L0.vw, L0.ww};
+            const Dims fd[3] = {fu, fv, fw};
+            jetgpu_status gs = grow_list(c, (size_t)std::max(
+                                                std::max(fu.count(), fv.count()),
+                                                fw.count()));
+            if (gs != JETGPU_OK) return gs;
+            auto axis_pass = [&](auto first, auto listed, int a) {
+                JG_CUDA(c, cudaMemsetAsync(c->build_cnt, 0, sizeof(unsigned),
+                                           c->stream));
+                first<<<blocks_for(fd[a].count()), kThreads, 0, c->stream>>>(
+                    wts[a], fd[a], T.slot, TL, S, T.node, c->build_list,
+                    c->build_cnt);
+                listed<<<c->num_sms * 8, kThreads, 0, c->stream>>>(
+                    wts[a], fd[a], T.slot, TL, S, T.node, c->build_list,
+                    c->build_cnt);
+                return JETGPU_OK;
+            };
+            if ((gs = axis_pass(k_face_weights_nodes<0>,
+                                k_face_weights_listed<0>, 0)) != JETGPU_OK ||
+                (gs = axis_pass(k_face_weights_nodes<1>,
+                                k_face_weights_listed<1>, 1)) != JETGPU_OK ||
+                (gs = axis_pass(k_face_weights_nodes<2>,
+                                k_face_weights_listed<2>, 2)) != JETGPU_OK)
+                return gs;
         } else {
             k_face_weights<<<blocks_for(fu.count()), kThreads, 0, c->stream>>>(
                 L0.uw, 0, fu, g, bsdf);
@@ -1060,17 +1225,22 @@ jetgpu_status build_pyramid(Ctx* c) {
         const Level& F = c->levels[l - 1];
         Level& C = c->levels[l];
         const Dims f = F.n, s = C.n;
-        k_restrict_f32<<<blocks_for(s.count()), kThreads, 0, c->stream>>>(
-            F.phi, f, C.phi, s);
+        // Arrays whose x axis is fully restricted take the paired kernel
+        // when the coarse rows have even length.
+        auto full_x = [&](const float* fine, Dims fd, float* coarse, Dims cd) {
+            if (cd.x % 2 == 0)
+                k_restrict_f32x2<<<blocks_for(cd.count() / 2), kThreads, 0,
+                                   c->stream>>>(fine, fd, coarse, cd);
+            else
+                k_restrict_f32<<<blocks_for(cd.count()), kThreads, 0,
+                                 c->stream>>>(fine, fd, coarse, cd);
+        };
+        full_x(F.phi, f, C.phi, s);
         k_restrict_f32<<<blocks_for((long)(s.x + 1) * s.y * s.z), kThreads, 0,
                          c->stream>>>(F.uw, Dims{f.x + 1, f.y, f.z}, C.uw,
                                       Dims{s.x + 1, s.y, s.z});
-        k_restrict_f32<<<blocks_for((long)s.x * (s.y + 1) * s.z), kThreads, 0,
-                         c->stream>>>(F.vw, Dims{f.x, f.y + 1, f.z}, C.vw,
-                                      Dims{s.x, s.y + 1, s.z});
-        k_restrict_f32<<<blocks_for((long)s.x * s.y * (s.z + 1)), kThreads, 0,
-                         c->stream>>>(F.ww, Dims{f.x, f.y, f.z + 1}, C.ww,
-                                      Dims{s.x, s.y, s.z + 1});
+        full_x(F.vw, Dims{f.x, f.y + 1, f.z}, C.vw, Dims{s.x, s.y + 1, s.z});
+        full_x(F.ww, Dims{f.x, f.y, f.z + 1}, C.ww, Dims{s.x, s.y, s.z + 1});
     }
     JG_CUDA(c, cudaGetLastError());
     return JETGPU_OK;

@@ -103,6 +103,10 @@ struct Ctx {
     // compute stream by io_ev (see SolveIo).
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t io_ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    // High-priority stream for the coarse levels' set-up, which runs beside
+    // the finest level's (fork and join events).
+    cudaStream_t side_stream = nullptr;
+    cudaEvent_t side_ev[2] = {nullptr, nullptr};
     std::string err;
 
     // Allocated geometry.
@@ -194,6 +198,13 @@ struct Ctx {
     // vc_exec; destroyed with the buffers.
     cudaGraphExec_t loop_exec = nullptr;
     bool loop_disabled = false;
+
+    // Compaction list of the two-pass face-weight build (build.cu): the
+    // faces whose FP64 marching-squares work runs in a second, full-warp
+    // pass.
+    size_t build_cap = 0;
+    int* build_list = nullptr;
+    unsigned* build_cnt = nullptr;
 
     // Blocked pressure solver (blocked.cu): cell markers of every level,
     // finest first.
@@ -343,10 +354,15 @@ constexpr int kNetLayerCount = 14;
 extern const NetLayer kNetLayers[kNetLayerCount];
 size_t net_param_count();
 jetgpu_status net_load(Ctx* c, const float* params, size_t count);
+// The multigrid level the network works on: the finest level at most 64
+// cells wide on every axis (the coarsest level when none is).
+unsigned net_level(const Ctx* c);
+// A loaded network and a net_level() whose extents are multiples of 8.
 bool net_supported(const Ctx* c);
-jetgpu_status net_features(Ctx* c, const float* r, const double* rr,
-                           void* feat);
-jetgpu_status net_apply(Ctx* c, const float* r, const double* rr, float* z);
+jetgpu_status net_features(Ctx* c, unsigned level, const float* r,
+                           const double* rr, void* feat);
+jetgpu_status net_apply(Ctx* c, unsigned level, const float* r,
+                        const double* rr, float* z);
 void net_destroy(void* net);
 jetgpu_status conv3d(cudaStream_t st, const __nv_bfloat16* in, int ci,
                      const __nv_bfloat16* w, const float* bias, int co,
@@ -360,6 +376,9 @@ jetgpu_status harvest_pairs(Ctx* c, unsigned max_pairs, float* r_out,
                             float* z_out, unsigned* count);
 // sum(r^2) of an FP32 vector into scal[target] (device).
 jetgpu_status norm2f(Ctx* c, const float* r, long n, int target);
+// z = M r with the learned preconditioner (a V-cycle plus the network's
+// coarse-level correction of its error).
+jetgpu_status learned_precond(Ctx* c, const float* r, float* z);
 
 // ---- transfer.cu ----------------------------------------------------------
 jetgpu_status constrain_velocity(Ctx* c, const GridDesc& g, double* u,

@@ -129,10 +129,10 @@ struct RowsB {
 };
 struct RowsD {
     const double* A;
-    __device__ __forceinline__ double4 row(long c) const {
+    __device__ __forceinline__ double4_16a row(long c) const {
         const double2 a = reinterpret_cast<const double2*>(A)[2 * c];
         const double2 b = reinterpret_cast<const double2*>(A)[2 * c + 1];
-        return make_double4(a.x, a.y, b.x, b.y);
+        return make_double4_16a(a.x, a.y, b.x, b.y);
     }
 };
 
@@ -2015,6 +2015,118 @@ jetgpu_status norm2f(Ctx* c, const float* r, long n, int target) {
     return JETGPU_OK;
 }
 
+namespace {
+
+// fine += mask * (trilinear prolongation of coarse), k_correct's stencil and
+// order, zero outside the fluid (phi >= 0).
+__global__ void __launch_bounds__(kThreads)
+    k_correct_masked(const float* __restrict__ coarse,
+                     float* __restrict__ fine, const float* __restrict__ phi,
+                     Dims c) {
+    const Dims n{2 * c.x, 2 * c.y, 2 * c.z};
+    const long N = n.count();
+    for (long t = blockIdx.x * (long)kThreads + threadIdx.x; t < N;
+         t += (long)gridDim.x * kThreads) {
+        if (!(phi[t] < 0.0f)) continue;
+        int i, j, k;
+        cell_ijk(t, n, i, j, k);
+        const int ci = i >> 1, cj = j >> 1, ck = k >> 1;
+        int i0, i1, j0, j1, k0, k1;
+        float wi0, wi1, wj0, wj1, wk0, wk1;
+        if ((i & 1) == 0) { i0 = i > 1 ? ci - 1 : ci; i1 = ci; wi0 = 0.25f; wi1 = 0.75f; }
+        else { i0 = ci; i1 = i + 1 < n.x ? ci + 1 : ci; wi0 = 0.75f; wi1 = 0.25f; }
+        if ((j & 1) == 0) { j0 = j > 1 ? cj - 1 : cj; j1 = cj; wj0 = 0.25f; wj1 = 0.75f; }
+        else { j0 = cj; j1 = j + 1 < n.y ? cj + 1 : cj; wj0 = 0.75f; wj1 = 0.25f; }
+        if ((k & 1) == 0) { k0 = k > 1 ? ck - 1 : ck; k1 = ck; wk0 = 0.25f; wk1 = 0.75f; }
+        else { k0 = ck; k1 = k + 1 < n.z ? ck + 1 : ck; wk0 = 0.75f; wk1 = 0.25f; }
+        const float c000 = coarse[lin(i0, j0, k0, c.x, c.y)];
+        const float c100 = coarse[lin(i1, j0, k0, c.x, c.y)];
+        const float c010 = coarse[lin(i0, j1, k0, c.x, c.y)];
+        const float c110 = coarse[lin(i1, j1, k0, c.x, c.y)];
+        const float c001 = coarse[lin(i0, j0, k1, c.x, c.y)];
+        const float c101 = coarse[lin(i1, j0, k1, c.x, c.y)];
+        const float c011 = coarse[lin(i0, j1, k1, c.x, c.y)];
+        const float c111 = coarse[lin(i1, j1, k1, c.x, c.y)];
+        const float a0 = wj0 * (wi0 * c000 + wi1 * c100) + wj1 * (wi0 * c010 + wi1 * c110);
+        const float a1 = wj0 * (wi0 * c001 + wi1 * c101) + wj1 * (wi0 * c011 + wi1 * c111);
+        fine[t] += wk0 * a0 + wk1 * a1;
+    }
+}
+
+// z += e (the network's output on the finest level is already masked).
+__global__ void k_add_f32(float* __restrict__ z, const float* __restrict__ e,
+                          long N) {
+    for (long t = blockIdx.x * (long)kThreads + threadIdx.x; t < N;
+         t += (long)gridDim.x * kThreads)
+        z[t] += e[t];
+}
+
+}  // namespace
+
+// The learned preconditioner (K18): one V-cycle, then the network's
+// correction of the error the V-cycle leaves, computed on a coarse level
+// from the residual it leaves:
+//   z0 = V r,  rho = r - A z0,  z = z0 + mask P^k net(R^k rho)
+// with the V-cycle's masked restriction R and trilinear prolongation P, and
+// k = net_level(). The network is trained to minimise the A-norm of the
+// error left after the correction, so z is at least as good a step as the
+// V-cycle's wherever the training holds, and the V-cycle alone bounds how
+// bad it can be. Uses the levels' V-cycle buffers as scratch.
+jetgpu_status learned_precond(Ctx* c, const float* r, float* z) {
+    const Level& L0 = c->levels[0];
+    const long N = L0.n.count();
+    const unsigned k = net_level(c);
+    float* res = nullptr;
+    jetgpu_status s = vcycle_graph(c, r, z, L0.x2, &res);
+    if (s != JETGPU_OK) return s;
+    if (res != z)
+        JG_CUDA(c, cudaMemcpyAsync(z, res, N * sizeof(float),
+                                   cudaMemcpyDeviceToDevice, c->stream));
+    {
+        Prof pr(c, K_RESIDUAL, 28.0 * N);
+        const RowsF M{L0.A, N};
+        if (L0.n.x % 4 == 0)
+            k_residual32x4<<<grid_for(c, N / 4), kThreads, 0, c->stream>>>(
+                M, z, r, L0.r, L0.n);
+        else
+            k_residual32<<<grid_for(c, N), kThreads, 0, c->stream>>>(
+                M, z, r, L0.r, L0.n);
+    }
+    const float* rho = L0.r;
+    for (unsigned l = 1; l <= k; ++l) {
+        const Level& F = c->levels[l - 1];
+        const Level& C = c->levels[l];
+        Prof pr(c, K_RESTRICT, 4.0 * F.n.count() + 8.0 * C.n.count());
+        if (C.n.x % 2 == 0)
+            k_restrict2<<<grid_for(c, C.n.count() / 2), kThreads, 0,
+                          c->stream>>>(rho, C.b, C.phi, C.n);
+        else
+            k_restrict<<<grid_for(c, C.n.count()), kThreads, 0, c->stream>>>(
+                rho, C.b, C.phi, C.n);
+        rho = C.b;
+    }
+    const Level& K = c->levels[k];
+    if ((s = norm2f(c, rho, K.n.count(), S_MEAN)) != JETGPU_OK) return s;
+    if ((s = net_apply(c, k, rho, c->scal + S_MEAN, K.x)) != JETGPU_OK)
+        return s;
+    Prof pr(c, K_CORRECT, 12.0 * N);
+    if (k == 0) {
+        k_add_f32<<<grid_for(c, N), kThreads, 0, c->stream>>>(z, K.x, N);
+    } else {
+        for (unsigned l = k - 1; l >= 1; --l) {
+            const Level& F = c->levels[l];
+            JG_CUDA(c, cudaMemsetAsync(F.x, 0, F.n.count() * sizeof(float),
+                                       c->stream));
+            k_correct<<<grid_for(c, F.n.count()), kThreads, 0, c->stream>>>(
+                c->levels[l + 1].x, F.x, c->levels[l + 1].n);
+        }
+        k_correct_masked<<<grid_for(c, N), kThreads, 0, c->stream>>>(
+            c->levels[1].x, z, L0.phi, c->levels[1].n);
+    }
+    JG_CUDA(c, cudaGetLastError());
+    return JETGPU_OK;
+}
+
 // FPCG on the FP32 rows for a correction e with A e = r (r = kr on entry,
 // its squared norm in scal[S_R64]). Stops at ||r|| <= target, after max_it
 // iterations, or when progress stalls (*stalled = true; x so far is kept).
@@ -2034,8 +2146,7 @@ static jetgpu_status fpcg_f32(Ctx* c, double target, unsigned max_it,
     unsigned it = 0;
     double rr = 0;
     while (it < max_it) {
-        const double* rrp = c->scal + (it == 0 ? S_R64 : S_RR);
-        if (jetgpu_status s = net_apply(c, c->kr, rrp, z)) return s;
+        if (jetgpu_status s = learned_precond(c, c->kr, z)) return s;
         {
             Prof pr(c, K_DOT_RZ, 12.0 * N);
             k_dot_pr<<<rgrid(c, k_dot_pr, N), kThreads, 0,

@@ -419,11 +419,19 @@ jetgpu_status conv3d(cudaStream_t st, const __nv_bfloat16* in, int ci,
     CUtensorMap tm;
     if (n.x % 128 == 0 && bsmem <= kMaxConvSmem &&
         (reinterpret_cast<uintptr_t>(in) & 15u) == 0 && brick_map(&tm, in, ci, n)) {
+        // The largest shared-memory carveout, so that two CTAs of the
+        // smaller layers fit on an SM (with the default carveout the
+        // occupancy query, and so the grid, allowed one).
         static DeviceOnce battr;
         if (!battr.run([] {
-                return cudaFuncSetAttribute(
+                cudaError_t e = cudaFuncSetAttribute(
                     k_conv3d_brick, cudaFuncAttributeMaxDynamicSharedMemorySize,
                     (int)kMaxConvSmem);
+                if (e != cudaSuccess) return e;
+                return cudaFuncSetAttribute(
+                    k_conv3d_brick,
+                    cudaFuncAttributePreferredSharedMemoryCarveout,
+                    (int)cudaSharedmemCarveoutMaxShared);
             }))
             return JETGPU_CUDA_ERROR;
         int dev = 0, sms = 0, occ = 0;
@@ -447,9 +455,13 @@ jetgpu_status conv3d(cudaStream_t st, const __nv_bfloat16* in, int ci,
     const size_t smem = conv_smem_bytes(ci, co);
     static DeviceOnce attr;
     if (!attr.run([] {
-            return cudaFuncSetAttribute(
+            cudaError_t e = cudaFuncSetAttribute(
                 k_conv3d_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
                 (int)conv_smem_bytes(128, 128));
+            if (e != cudaSuccess) return e;
+            return cudaFuncSetAttribute(
+                k_conv3d_tc, cudaFuncAttributePreferredSharedMemoryCarveout,
+                (int)cudaSharedmemCarveoutMaxShared);
         }))
         return JETGPU_CUDA_ERROR;
     const long blocks = (n.count() + kTile - 1) / kTile;
@@ -666,9 +678,13 @@ extern "C" jetgpu_status jetgpu_conv3d_wgrad(void* stream, const void* in,
 // K17: the preconditioner network. A 3-D U-Net with 4 levels (16, 32, 48,
 // 64 channels), two 3x3x3 convolutions per level and side, 2x2x2 average
 // pooling, nearest-neighbour upsampling and skip concatenation
-// [upsampled | skip]. Input: 16 channels of per-cell features of the
-// residual and the system (net_features below). Output: channel 0 of the
-// last convolution, scaled back to the residual's units.
+// [upsampled | skip]. It runs on one coarse multigrid level (net_level:
+// the finest level at most 64 cells wide) and maps the residual a V-cycle
+// leaves, restricted to that level, to a correction of the V-cycle's error
+// there (learned_precond in mgpcg.cu). Input: 16 channels of per-cell
+// features of the residual and of that level's system (net_features below).
+// Output: channel 0 of the last convolution, scaled back to the residual's
+// units.
 
 namespace jg {
 
@@ -766,10 +782,10 @@ __global__ void k_up_concat(const __nv_bfloat16* __restrict__ coarse, int C1,
     }
 }
 
-// Output gain of the network: it predicts kNetGain * z / rms(r). For the
-// smooth error modes that dominate a preconditioned residual, z = A^-1 r is
-// about r / (3 pi^2) whatever the grid spacing, so this target is O(1) and
-// independent of the resolution (a trained network transfers across grids).
+// Output gain of the network: it predicts kNetGain * e / rms(r) for a
+// residual r and error e = A^-1 r. For the smooth error modes, e is about
+// r / (3 pi^2) whatever the grid spacing (the rows carry 1/h^2 on the unit
+// cube), so the target is O(1)-scaled and independent of the resolution.
 constexpr float kNetGain = 32.0f;
 
 // z[c] = out32[c][0] * rms(residual) / kNetGain on fluid cells, 0 elsewhere.
@@ -910,18 +926,28 @@ static jetgpu_status net_ensure_acts(Ctx* c, Net* net, Dims n) {
     return JETGPU_OK;
 }
 
-bool net_supported(const Ctx* c) {
-    const Net* net = static_cast<const Net*>(c->unet);
-    const Dims n = c->levels.empty() ? Dims{0, 0, 0} : c->levels[0].n;
-    return net && net->loaded && n.x % 8 == 0 && n.y % 8 == 0 && n.z % 8 == 0 &&
-           n.x >= 8 && n.y >= 8 && n.z >= 8;
+unsigned net_level(const Ctx* c) {
+    const unsigned nl = c->built_levels;
+    for (unsigned l = 0; l < nl; ++l) {
+        const Dims n = c->levels[l].n;
+        if (n.x <= 64 && n.y <= 64 && n.z <= 64) return l;
+    }
+    return nl > 0 ? nl - 1 : 0;
 }
 
-// Builds the 16 input channels of residual r on the current level-0 system.
-// rr: device pointer to sum(r^2).
-jetgpu_status net_features(Ctx* c, const float* r, const double* rr,
-                           void* feat) {
-    const Level& L = c->levels[0];
+bool net_supported(const Ctx* c) {
+    const Net* net = static_cast<const Net*>(c->unet);
+    if (!net || !net->loaded || c->built_levels == 0) return false;
+    const Dims n = c->levels[net_level(c)].n;
+    return n.x % 8 == 0 && n.y % 8 == 0 && n.z % 8 == 0 && n.x >= 8 &&
+           n.y >= 8 && n.z >= 8;
+}
+
+// Builds the 16 input channels of residual r on level `level` of the
+// current system. rr: device pointer to sum(r^2).
+jetgpu_status net_features(Ctx* c, unsigned level, const float* r,
+                           const double* rr, void* feat) {
+    const Level& L = c->levels[level];
     const float h2 = (float)(L.h[0] * L.h[0]);
     k_net_features<<<blocks_for(L.n.count()), kThreads, 0, c->stream>>>(
         r, rr, L.n.count(), L.uw, L.vw, L.ww, L.phi, L.A, h2, L.n,
@@ -930,17 +956,18 @@ jetgpu_status net_features(Ctx* c, const float* r, const double* rr,
     return JETGPU_OK;
 }
 
-// z = net(r) on the current level-0 system; rr = device sum(r^2).
-jetgpu_status net_apply(Ctx* c, const float* r, const double* rr, float* z) {
+// z = net(r) on level `level` of the current system; rr = device sum(r^2).
+jetgpu_status net_apply(Ctx* c, unsigned level, const float* r,
+                        const double* rr, float* z) {
     Net* net = static_cast<Net*>(c->unet);
-    const Level& L0 = c->levels[0];
+    const Level& L0 = c->levels[level];
     const Dims n0 = L0.n, n1{n0.x / 2, n0.y / 2, n0.z / 2},
                n2{n1.x / 2, n1.y / 2, n1.z / 2}, n3{n2.x / 2, n2.y / 2, n2.z / 2};
     jetgpu_status s = net_ensure_acts(c, net, n0);
     if (s != JETGPU_OK) return s;
     Prof pr(c, K_UNET, 0.0);
     cudaStream_t st = c->stream;
-    s = net_features(c, r, rr, net->feat);
+    s = net_features(c, level, r, rr, net->feat);
     if (s != JETGPU_OK) return s;
     auto conv = [&](int l, const __nv_bfloat16* in, Dims n, __nv_bfloat16* out,
                     float* out32) {

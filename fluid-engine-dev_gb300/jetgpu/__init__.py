@@ -118,6 +118,7 @@ EXPORTS = (
     "jetgpu_fluid_cfl_device", "jetgpu_flip_substep_device",
     "jetgpu_apic_p2g_device", "jetgpu_apic_g2p_device",
     "jetgpu_solve_pressure_collider", "jetgpu_vcycle_apply",
+    "jetgpu_net_level", "jetgpu_learned_apply",
 )
 
 # closedDomainBoundaryFlag bits (include/jet/constants.h:312-335).
@@ -287,10 +288,14 @@ def library() -> C.CDLL:
     L.jetgpu_load_unet.restype = C.c_int
     L.jetgpu_harvest.argtypes = [vp, C.c_uint, vp, vp, C.POINTER(C.c_uint)]
     L.jetgpu_harvest.restype = C.c_int
-    L.jetgpu_net_features.argtypes = [vp, vp, vp]
+    L.jetgpu_net_level.argtypes = [vp]
+    L.jetgpu_net_level.restype = C.c_uint
+    L.jetgpu_net_features.argtypes = [vp, C.c_uint, vp, vp]
     L.jetgpu_net_features.restype = C.c_int
-    L.jetgpu_net_apply.argtypes = [vp, vp, vp]
+    L.jetgpu_net_apply.argtypes = [vp, C.c_uint, vp, vp]
     L.jetgpu_net_apply.restype = C.c_int
+    L.jetgpu_learned_apply.argtypes = [vp, vp, vp]
+    L.jetgpu_learned_apply.restype = C.c_int
     L.jetgpu_vcycle_apply.argtypes = [vp, vp, vp]
     L.jetgpu_vcycle_apply.restype = C.c_int
     L.jetgpu_get_stream.argtypes = [vp, C.POINTER(C.c_void_p)]

@@ -1,20 +1,32 @@
 """Training of the learned preconditioner (3-D U-Net) on the tensor-core
 kernels of libjetgpu.
 
-The network maps the 16 input channels libjetgpu builds for a residual r
-(``jetgpu_net_features``: r / rms(r), the six face weights of each cell,
-fluid indicator, scaled diagonal) to NET_GAIN * z / rms(r), where z = M r is
-the multigrid V-cycle's correction. For the smooth modes that dominate a
-preconditioned residual z is about r / (3 pi^2) at any grid spacing, so the
-target is O(1) and independent of the resolution. Pairs (r_k, z_k) come from the solver's own
-MGPCG iterations (``jetgpu_harvest``). Every convolution of the forward and
-backward passes runs on libjetgpu's tcgen05 kernels (``jetgpu_conv3d`` and
-``jetgpu_conv3d_wgrad``); PyTorch supplies device memory, the optimizer and
-the element-wise glue (pooling, upsampling, concatenation, ReLU masks),
-mirroring the library's inference path (``unet.cu``) step for step.
+The learned preconditioner of libjetgpu's flexible PCG is a multigrid
+V-cycle followed by the network's correction of the error the V-cycle
+leaves (``jetgpu_learned_apply``):
 
-The trained parameters are used by the flexible PCG of libjetgpu through
-``jetgpu_load_unet`` (``preconditioner = JETGPU_PRECOND_LEARNED``).
+    z0 = V r,   rho = r - A z0,   z = z0 + mask P^k e,   e = net(R^k rho)
+
+on level k of the multigrid hierarchy (``jetgpu_net_level``: the finest
+level at most 64 cells wide), with the V-cycle's masked restriction R (1/8
+of the transposed prolongation) and trilinear prolongation P. The network
+sees 16 channels that libjetgpu builds for the restricted residual
+(``jetgpu_net_features``: rho_k / rms(rho_k), the level's six face weights,
+fluid indicator, scaled diagonal) and predicts NET_GAIN * e / rms(rho_k).
+
+It is trained to minimise the A-norm of the error left after the
+correction. With y = mask P^k e and the V-cycle's error e0 = A^-1 rho,
+||e0 - y||_A^2 = ||e0||_A^2 - 2 y.rho + y.A y, so the loss
+(y.A y - 2 y.rho) needs no solve; it is divided by the energy a steepest-
+descent step along rho removes, (rho.rho)^2 / (rho.A rho), so that samples
+of every size weigh alike. Residuals r come from the solver's own MGPCG
+iterations (``jetgpu_harvest``) on GPU-generated sphere-union scenes. Every
+convolution of the forward and backward passes runs on libjetgpu's tcgen05
+kernels (``jetgpu_conv3d`` and ``jetgpu_conv3d_wgrad``); PyTorch supplies
+device memory, the optimizer and the element-wise glue (pooling,
+upsampling, concatenation, ReLU masks, restriction and prolongation),
+mirroring the library's inference path (``unet.cu``, ``learned_precond`` in
+``mgpcg.cu``) step for step.
 """
 from __future__ import annotations
 
@@ -194,41 +206,36 @@ def forward(conv, params, feat):
 
 
 # ---------------------------------------------------------------------------
-# Data from the solver.
+# The multigrid transfers of the V-cycle, on torch tensors.
 
-def harvest(solver: FdmMgpcgSolver3, sc: dict, n: int, pairs: int):
-    """Solves the scene's pressure system, then records `pairs` (features,
-    target, fluid mask) samples from the solver's MGPCG iterations."""
+def prolong(e):
+    """Trilinear prolongation by 2 (k_correct: weights 1/4, 3/4 per axis,
+    clamped at the edges), differentiable."""
+    F = _torch().nn.functional
+    return F.interpolate(e[None, None], scale_factor=2, mode="trilinear",
+                         align_corners=False)[0, 0]
+
+
+def restrict(rho, mask_c):
+    """The V-cycle's restriction (k_restrict2): 1/8 of the transposed
+    prolongation, zero on coarse cells outside the fluid."""
     torch = _torch()
-    L = library()
-    h = 1.0 / n
-    ps = GridFractionalSinglePhasePressureSolver3(solver)
-    vel = FaceCenteredGrid3((n,) * 3, (h,) * 3, (0, 0, 0), sc["u"], sc["v"], sc["w"])
-    out = vel.clone()
-    g = lambda d: CellCenteredScalarGrid3((n,) * 3, (h,) * 3, (0, 0, 0), d)
-    ps.solve(vel, 1 / 60, out, g(sc["boundary_sdf"]), None, g(sc["fluid_sdf"]))
-    dev = torch.device("cuda", solver.config.device)
-    N = n ** 3
-    R = torch.empty((pairs, N), dtype=torch.float32, device=dev)
-    Z = torch.empty((pairs, N), dtype=torch.float32, device=dev)
-    cnt = C.c_uint(0)
-    solver.check(L.jetgpu_harvest(solver.context(), pairs, R.data_ptr(),
-                                  Z.data_ptr(), C.byref(cnt)))
-    samples = []
-    fluid = torch.from_numpy((sc["fluid_sdf"] < 0).astype(np.float32)).to(dev)
-    for k in range(cnt.value):
-        feat = torch.empty((n, n, n, 16), dtype=torch.bfloat16, device=dev)
-        solver.check(L.jetgpu_net_features(solver.context(), R[k].data_ptr(),
-                                           feat.data_ptr()))
-        rms = torch.sqrt(torch.mean(R[k].double() ** 2)).float()
-        if rms <= 0:
-            continue
-        target = (Z[k] * (NET_GAIN / rms)).reshape(n, n, n)
-        mask = feat[..., 7].float()
-        samples.append((feat, target, mask))
-    del fluid
-    return samples
+    nz, ny, nx = rho.shape
+    with torch.enable_grad():
+        x = torch.zeros((nz // 2, ny // 2, nx // 2), dtype=rho.dtype,
+                        device=rho.device, requires_grad=True)
+        (g,) = torch.autograd.grad(prolong(x), x, grad_outputs=rho)
+    return mask_c * (g * 0.125)
 
+
+def _sync():
+    """Orders torch's pending work before a library call on its own
+    stream."""
+    _torch().cuda.current_stream().synchronize()
+
+
+# ---------------------------------------------------------------------------
+# Data from the solver.
 
 def device_scene(n: int, seed: int, device):
     """The 16-sphere union scene of ``scenes.sphere_union_scene`` built on
@@ -264,9 +271,10 @@ def device_scene(n: int, seed: int, device):
 
 
 def harvest_device(solver: FdmMgpcgSolver3, sc: dict, n: int, pairs: int):
-    """harvest() for a scene already on the device (device_scene): the
-    projection through jetgpu_solve_pressure_device, then `pairs` samples of
-    the MGPCG iterations on that system."""
+    """Projects a scene already on the device (device_scene) through
+    jetgpu_solve_pressure_device, then records up to `pairs` (r_k, V r_k)
+    pairs of the MGPCG iterations on that system (jetgpu_harvest). Returns
+    (R, Z), each (count, n, n, n) FP32 on the device."""
     torch = _torch()
     from . import Grid, ScalarField, solve_pressure_device
     L = library()
@@ -286,7 +294,7 @@ def harvest_device(solver: FdmMgpcgSolver3, sc: dict, n: int, pairs: int):
         return f
 
     out = [torch.empty_like(sc[k]) for k in ("u", "v", "w")]
-    torch.cuda.synchronize()
+    _sync()
     solve_pressure_device(solver, g, sc["u"], sc["v"], sc["w"],
                           field(sc["boundary_sdf"]), field(sc["fluid_sdf"]),
                           *out)
@@ -297,17 +305,8 @@ def harvest_device(solver: FdmMgpcgSolver3, sc: dict, n: int, pairs: int):
     cnt = C.c_uint(0)
     solver.check(L.jetgpu_harvest(solver.context(), pairs, R.data_ptr(),
                                   Z.data_ptr(), C.byref(cnt)))
-    samples = []
-    for k in range(cnt.value):
-        feat = torch.empty((n, n, n, 16), dtype=torch.bfloat16, device=dev)
-        solver.check(L.jetgpu_net_features(solver.context(), R[k].data_ptr(),
-                                           feat.data_ptr()))
-        rms = torch.sqrt(torch.mean(R[k].double() ** 2)).float()
-        if rms <= 0:
-            continue
-        target = (Z[k] * (NET_GAIN / rms)).reshape(n, n, n)
-        samples.append((feat, target, feat[..., 7].float()))
-    return samples
+    k = cnt.value
+    return R[:k].reshape(k, n, n, n), Z[:k].reshape(k, n, n, n)
 
 
 def level0_rows(solver: FdmMgpcgSolver3, n: int, device):
@@ -321,6 +320,37 @@ def level0_rows(solver: FdmMgpcgSolver3, n: int, device):
                                     rows.ctypes.data_as(C.c_void_p),
                                     rows.nbytes, C.byref(cnt)))
     return torch.from_numpy(rows.reshape(n, n, n, 4).astype(np.float32)).to(device)
+
+
+def level0_rhs(solver: FdmMgpcgSolver3, n: int, device):
+    """The finest level's right-hand side of the solver's last system as an
+    FP32 (n, n, n) device tensor."""
+    torch = _torch()
+    L = library()
+    b = np.zeros(n ** 3)
+    cnt = C.c_size_t(0)
+    solver.check(L.jetgpu_get_level(solver.context(), 0, 5,
+                                    b.ctypes.data_as(C.c_void_p), b.nbytes,
+                                    C.byref(cnt)))
+    return torch.from_numpy(b.reshape(n, n, n).astype(np.float32)).to(device)
+
+
+def fluid_masks(solver: FdmMgpcgSolver3, n: int, levels: int, device):
+    """1.0 on fluid cells (fluid SDF < 0), 0.0 elsewhere, for levels
+    0..levels of the solver's last system, as (n/2^l)^3 device tensors."""
+    torch = _torch()
+    L = library()
+    out = []
+    for l in range(levels + 1):
+        m = n >> l
+        phi = np.zeros(m ** 3, np.float32)
+        cnt = C.c_size_t(0)
+        solver.check(L.jetgpu_get_level(solver.context(), l, 0,
+                                        phi.ctypes.data_as(C.c_void_p),
+                                        phi.nbytes, C.byref(cnt)))
+        out.append(torch.from_numpy((phi.reshape(m, m, m) < 0)
+                                    .astype(np.float32)).to(device))
+    return out
 
 
 def apply_rows(A, x):
@@ -342,87 +372,87 @@ def step_energy(A, r, z):
     return (r * z).sum() ** 2 / (z * apply_rows(A, z)).sum().clamp_min(1e-30)
 
 
-def level0_rhs(solver: FdmMgpcgSolver3, n: int, device):
-    """The finest level's right-hand side of the solver's last system as an
-    FP32 (n, n, n) device tensor."""
-    torch = _torch()
-    L = library()
-    b = np.zeros(n ** 3)
-    cnt = C.c_size_t(0)
-    solver.check(L.jetgpu_get_level(solver.context(), 0, 5,
-                                    b.ctypes.data_as(C.c_void_p), b.nbytes,
-                                    C.byref(cnt)))
-    return torch.from_numpy(b.reshape(n, n, n).astype(np.float32)).to(device)
-
-
 def vcycle_apply(solver: FdmMgpcgSolver3, r):
-    """z = M r with the solver's multigrid V-cycle (jetgpu_vcycle_apply)."""
+    """z = V r with the solver's multigrid V-cycle (jetgpu_vcycle_apply)."""
     torch = _torch()
-    z = torch.empty_like(r).contiguous()
+    r = r.contiguous()
+    z = torch.empty_like(r)
+    _sync()
     solver.check(library().jetgpu_vcycle_apply(
-        solver.context(), r.contiguous().data_ptr(), z.data_ptr()))
+        solver.context(), r.data_ptr(), z.data_ptr()))
     return z
 
 
-def fpcg_samples(solver: FdmMgpcgSolver3, conv, P, n: int, iters: int):
-    """Samples from the network's own flexible-PCG trajectory on the
-    solver's last system: starting from x = 0, each iteration's residual r_k
-    becomes a sample (its features, the V-cycle's correction M r_k as the
-    target, the fluid mask), and the iteration continues with the network's
-    correction, as the library's flexible PCG does (Polak-Ribiere beta).
-    The residuals a network meets inside its own solve differ from those of
-    multigrid PCG; training on them keeps it useful past the first step."""
+def learned_apply(solver: FdmMgpcgSolver3, r):
+    """z = M r with the library's learned preconditioner
+    (jetgpu_learned_apply)."""
     torch = _torch()
-    L = library()
-    dev = P[0][0].device
-    A = level0_rows(solver, n, dev)
-    r = level0_rhs(solver, n, dev)
-    out = []
-    d = z_old = None
-    rz_old = 0.0
-    with torch.no_grad():
-        for k in range(iters):
-            rms = torch.sqrt(torch.mean(r.double() ** 2)).float()
-            if not float(rms) > 0:
-                break
-            feat = torch.empty((n, n, n, 16), dtype=torch.bfloat16, device=dev)
-            solver.check(L.jetgpu_net_features(solver.context(),
-                                               r.contiguous().data_ptr(),
-                                               feat.data_ptr()))
-            mask = feat[..., 7].float()
-            zmg = vcycle_apply(solver, r)
-            out.append((feat, (zmg * (NET_GAIN / rms)).reshape(n, n, n), mask))
-            z = forward(conv, P, feat) * (rms / NET_GAIN) * mask
-            rz = float((r * z).sum())
-            if k == 0 or d is None:
-                d = z.clone()
-            else:
-                beta = float((r * (z - z_old)).sum()) / rz_old if rz_old else 0.0
-                d = z + beta * d
-            q = apply_rows(A, d)
-            dq = float((d * q).sum())
-            if not (dq > 0 and rz > 0):
-                break
-            r = r - (rz / dq) * q
-            z_old, rz_old = z, rz
-    return out
+    r = r.contiguous()
+    z = torch.empty_like(r)
+    _sync()
+    solver.check(library().jetgpu_learned_apply(
+        solver.context(), r.data_ptr(), z.data_ptr()))
+    return z
+
+
+def net_level(solver: FdmMgpcgSolver3) -> int:
+    """The hierarchy level the network works on (jetgpu_net_level)."""
+    return int(library().jetgpu_net_level(solver.context()))
+
+
+def coarse_residual(A, masks, r, z0, k):
+    """rho = r - A z0 on the finest level and its restriction to level k."""
+    rho = r - apply_rows(A, z0)
+    rk = rho
+    for l in range(1, k + 1):
+        rk = restrict(rk, masks[l])
+    return rho, rk
+
+
+def net_input(solver: FdmMgpcgSolver3, k: int, rk):
+    """The network's 16 input channels for level-k residual rk
+    (jetgpu_net_features) and rms(rk)."""
+    torch = _torch()
+    m = rk.shape[0]
+    feat = torch.empty((m, m, m, 16), dtype=torch.bfloat16, device=rk.device)
+    rk = rk.contiguous()
+    _sync()
+    solver.check(library().jetgpu_net_features(solver.context(), k,
+                                               rk.data_ptr(), feat.data_ptr()))
+    rms = torch.sqrt(torch.mean(rk.double() ** 2)).float()
+    return feat, rms
+
+
+def correction(conv, P, feat, rms, masks, k):
+    """y = mask P^k e with e = net output * rms / NET_GAIN on the level-k
+    fluid: the network's correction on the finest level (differentiable in
+    the parameters P)."""
+    e = forward(conv, P, feat) * (rms / NET_GAIN) * masks[k]
+    for _ in range(k):
+        e = prolong(e)
+    return e * masks[0]
+
+
+def correction_loss(A, rho, y):
+    """(y.A y - 2 y.rho) / ((rho.rho)^2 / (rho.A rho)): the change of the
+    error's A-norm squared that the correction y makes, in units of what a
+    steepest-descent step along rho removes (negative is better)."""
+    sd = (rho * rho).sum() ** 2 / (rho * apply_rows(A, rho)).sum().clamp_min(1e-30)
+    return ((y * apply_rows(A, y)).sum() - 2.0 * (y * rho).sum()) / sd.clamp_min(1e-30)
 
 
 def train_stream(n: int = 128, seeds=range(100, 2100), pairs: int = 2,
-                 lr: float = 2e-3, seed: int = 0, init=None, log=print,
-                 loss_kind: str = "energy", own: int = 0):
-    """Training at the scale of BASELINE's learned-preconditioner config:
-    one sphere-union scene per seed (by default 2,000 scenes at 128^3, seeds
-    100-2099), each solved on the GPU, `pairs` (residual, V-cycle
-    correction) samples harvested from its MGPCG iterations and used for one
-    optimiser step each, then discarded (a 128^3 sample is 64 MB of BF16
-    features). Every convolution forward and backward runs on libjetgpu's
-    tensor-core kernels. With `own` > 0, the residuals of the first `own`
-    iterations of the network's own flexible PCG on each scene are added as
-    samples (fpcg_samples). Returns (params, loss history)."""
+                 lr: float = 1e-3, seed: int = 0, init=None, log=print):
+    """Training at the scale of the learned-preconditioner workload: one
+    sphere-union scene per seed (by default 2,000 scenes at 128^3, seeds
+    100-2099), each projected on the GPU; `pairs` residuals of its MGPCG
+    iterations (with the V-cycle's z0 = V r) each give one optimiser step
+    on correction_loss, then are discarded. Every convolution forward and
+    backward runs on libjetgpu's tensor-core kernels. Returns (params, loss
+    history)."""
     torch = _torch()
     conv = make_conv_fn()
-    solver = FdmMgpcgSolver3(200, 6, 2, 2, 10, 2, 1e-6, 1.0, True)
+    solver = FdmMgpcgSolver3(200, 6, 2, 2, 5, 2, 1e-6, 1.2, True)
     dev = torch.device("cuda", solver.config.device)
     start = init if init is not None else init_params(seed)
     P = [(torch.tensor(w, device=dev, requires_grad=True),
@@ -438,86 +468,27 @@ def train_stream(n: int = 128, seeds=range(100, 2100), pairs: int = 2,
     hist = []
     for si, sd in enumerate(seeds):
         sc = device_scene(n, sd, dev)
-        samples = harvest_device(solver, sc, n, pairs)
-        if own > 0:
-            samples += fpcg_samples(solver, conv, P, n, own)
-        A = level0_rows(solver, n, dev) if loss_kind == "energy" else None
-        for feat, target, mask in samples:
-            pred = forward(conv, P, feat)
-            if loss_kind == "energy":
-                # One minus the energy a step along the network's output
-                # removes, relative to the V-cycle's step (scale-free).
-                r = feat[..., 0].float() * mask
-                z = pred * mask
-                loss = 1.0 - step_energy(A, r, z) / step_energy(
-                    A, r, target * mask).detach()
-            else:
-                err = (pred - target) * mask
-                loss = (err * err).sum() / ((target * mask) ** 2).sum().clamp_min(1e-30)
+        R, Z = harvest_device(solver, sc, n, pairs)
+        k = net_level(solver)
+        A = level0_rows(solver, n, dev)
+        masks = fluid_masks(solver, n, k, dev)
+        for r, z0 in zip(R, Z):
+            with torch.no_grad():
+                rho, rk = coarse_residual(A, masks, r, z0, k)
+            feat, rms = net_input(solver, k, rk)
+            if not float(rms) > 0:
+                continue
+            y = correction(conv, P, feat, rms, masks, k)
+            loss = correction_loss(A, rho, y)
             opt.zero_grad()
             loss.backward()
             torch.nn.utils.clip_grad_norm_(flat_params, 1.0)
             opt.step()
             sched.step()
             hist.append(float(loss.detach()))
-        del sc
+        del sc, R, Z
         if si % 100 == 0 or si == len(seeds) - 1:
             log(f"scene {si} (seed {sd}) loss {np.mean(hist[-2 * pairs * 50:]):.4f}")
-    params = [(w.detach().cpu().numpy(), b.detach().cpu().numpy()) for w, b in P]
-    solver.close()
-    return params, hist
-
-
-def training_scenes(n: int, count: int, first_seed: int = 100):
-    """Sphere-union scenes (16 spheres, seeds first_seed..) and FLIP first
-    sub-step boxes of varying size."""
-    out = []
-    rng = np.random.default_rng(first_seed)
-    for s in range(count):
-        if s % 2 == 0:
-            out.append(scenes.sphere_union_scene(n, seed=first_seed + s))
-        else:
-            hi = (rng.uniform(0.2, 0.9), rng.uniform(0.3, 0.9), 1.0)
-            c = (rng.uniform(0.3, 0.8), rng.uniform(0.15, 0.5), rng.uniform(0.3, 0.7))
-            out.append(scenes.flip_first_substep(n, box_hi=hi,
-                                                 sphere=(c, rng.uniform(0.08, 0.2))))
-    return out
-
-
-def train(n: int = 64, scenes_count: int = 24, pairs: int = 6,
-          steps: int = 600, lr: float = 2e-3, seed: int = 0, log=print):
-    torch = _torch()
-    conv = make_conv_fn()
-    solver = FdmMgpcgSolver3(200, 6, 2, 2, 10, 2, 1e-6, 1.0, True)
-    data = []
-    for sc in training_scenes(n, scenes_count):
-        data += harvest(solver, sc, n, pairs)
-    log(f"harvested {len(data)} samples at {n}^3")
-    dev = data[0][0].device
-    P = [(torch.tensor(w, device=dev, requires_grad=True),
-          torch.tensor(b, device=dev, requires_grad=True))
-         for w, b in init_params(seed)]
-    flat_params = [t for p in P for t in p]
-    opt = torch.optim.Adam(flat_params, lr=lr)
-    warm = max(1, min(200, steps // 10))
-    sched = torch.optim.lr_scheduler.LambdaLR(
-        opt, lambda s: min(1.0, (s + 1) / warm) *
-        0.5 * (1.0 + np.cos(np.pi * min(s, steps) / steps)))
-    rng = np.random.default_rng(seed)
-    hist = []
-    for step in range(steps):
-        feat, target, mask = data[rng.integers(len(data))]
-        pred = forward(conv, P, feat)
-        err = (pred - target) * mask
-        loss = (err * err).sum() / ((target * mask) ** 2).sum().clamp_min(1e-30)
-        opt.zero_grad()
-        loss.backward()
-        torch.nn.utils.clip_grad_norm_(flat_params, 1.0)
-        opt.step()
-        sched.step()
-        hist.append(float(loss.detach()))
-        if step % 50 == 0 or step == steps - 1:
-            log(f"step {step} loss {np.mean(hist[-50:]):.4f}")
     params = [(w.detach().cpu().numpy(), b.detach().cpu().numpy()) for w, b in P]
     solver.close()
     return params, hist
@@ -558,6 +529,104 @@ def evaluate(params, n: int, seed: int, tolerance: float = 1e-6,
     return out
 
 
+def coarse_correction_bound(n: int, scene: str = "sphere_union",
+                            seed: int = 9001, levels=(1, 2, 3),
+                            tolerance: float = 1e-6):
+    """How many flexible-PCG iterations any coarse-level correction after the
+    V-cycle can save: FPCG (FP64, torch) on the scene's finest-level system
+    with M r = V r, and with M r = V r + mask P^k G^-1 (mask P^k)^T rho for
+    rho = r - A V r and the Galerkin operator G = (mask P^k)^T A (mask P^k)
+    solved by CG to 1e-8 — the best a correction computed on level k from
+    rho can do in one step. Returns {"multigrid": (iterations, relative
+    residual), "level<k>": ...}."""
+    torch = _torch()
+    if scene == "sphere_union":
+        sc = scenes.sphere_union_scene(n, seed=seed)
+    else:
+        sc = scenes.flip_first_substep(n, box_hi=(0.3, 0.8, 1.0),
+                                       sphere=((0.6, 0.2, 0.5), 0.15))
+    h = (1.0 / n,) * 3
+    s = FdmMgpcgSolver3(200, 6, 2, 2, 5, 2, tolerance, 1.2, True)
+    ps = GridFractionalSinglePhasePressureSolver3(s)
+    vel = FaceCenteredGrid3((n,) * 3, h, (0, 0, 0), sc["u"], sc["v"], sc["w"])
+    g = lambda d: CellCenteredScalarGrid3((n,) * 3, h, (0, 0, 0), d)
+    ps.solve(vel, 1 / 60, vel.clone(), g(sc["boundary_sdf"]), None,
+             g(sc["fluid_sdf"]))
+    dev = torch.device("cuda", s.config.device)
+    A = level0_rows(s, n, dev).double()
+    b = level0_rhs(s, n, dev).double()
+    mask = fluid_masks(s, n, 0, dev)[0].double()
+
+    def V(r):
+        return vcycle_apply(s, r.float()).double()
+
+    def adjoint(y):
+        x = torch.zeros(tuple(d // 2 for d in y.shape), dtype=y.dtype,
+                        device=y.device, requires_grad=True)
+        with torch.enable_grad():
+            (gx,) = torch.autograd.grad(prolong(x), x, grad_outputs=y)
+        return gx
+
+    def cg(op, rhs, tol=1e-8, maxit=2000):
+        x = torch.zeros_like(rhs)
+        r = rhs.clone()
+        d = r.clone()
+        rr = (r * r).sum()
+        b2 = rr
+        for _ in range(maxit):
+            q = op(d)
+            a = rr / (d * q).sum()
+            x += a * d
+            r -= a * q
+            rn = (r * r).sum()
+            if rn <= tol * tol * b2:
+                break
+            d = r + (rn / rr) * d
+            rr = rn
+        return x
+
+    def fpcg(M, maxit=100):
+        x = torch.zeros_like(b)
+        r = b.clone()
+        bn = float(b.norm())
+        d = z_old = rz_old = None
+        for it in range(1, maxit + 1):
+            z = M(r)
+            rz = (r * z).sum()
+            d = z.clone() if d is None else z + (rz - (r * z_old).sum()) / rz_old * d
+            q = apply_rows(A, d)
+            a = rz / (d * q).sum()
+            x += a * d
+            r -= a * q
+            z_old, rz_old = z, rz
+            rel = float(r.norm()) / bn
+            if rel <= tolerance:
+                return it, rel
+        return maxit, rel
+
+    out = {"multigrid": fpcg(V)}
+    for k in levels:
+        def MP(e, k=k):
+            for _ in range(k):
+                e = prolong(e)
+            return mask * e
+
+        def MPt(y, k=k):
+            y = mask * y
+            for _ in range(k):
+                y = adjoint(y)
+            return y
+
+        def M(r, k=k, MP=MP, MPt=MPt):
+            z = V(r)
+            rho = r - apply_rows(A, z)
+            e = cg(lambda v: MPt(apply_rows(A, MP(v))), MPt(rho))
+            return z + MP(e)
+        out[f"level{k}"] = fpcg(M)
+    s.close()
+    return out
+
+
 if __name__ == "__main__":
     import argparse
     import json
@@ -568,25 +637,29 @@ if __name__ == "__main__":
     ap.add_argument("--first-seed", type=int, default=100)
     ap.add_argument("--scenes", type=int, default=2000)
     ap.add_argument("--pairs", type=int, default=2)
-    ap.add_argument("--lr", type=float, default=2e-3)
-    ap.add_argument("--loss", default="energy", choices=["energy", "mse"],
-                    help="energy: the error energy a step along the output "
-                         "removes, relative to the V-cycle's step; mse: "
-                         "relative squared error to the V-cycle's output")
-    ap.add_argument("--own", type=int, default=6,
-                    help="iterations of the network's own flexible PCG whose "
-                         "residuals are added as samples per scene")
+    ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--init", default=None,
                     help="start from these weights instead of a random "
                          "initialisation")
     ap.add_argument("--out", default=WEIGHTS)
     ap.add_argument("--eval", type=int, nargs="*", default=[128, 256],
                     help="grid sizes of the held-out evaluation solves")
+    ap.add_argument("--bound", type=int, nargs="*", default=None,
+                    help="instead of training: for these grid sizes, the "
+                         "FPCG iterations with an exact coarse-level "
+                         "correction after the V-cycle "
+                         "(coarse_correction_bound)")
     a = ap.parse_args()
+    if a.bound is not None:
+        for n in a.bound:
+            for scene, seed in (("sphere_union", 9001), ("flip", 0)):
+                print(json.dumps({"grid": n, "scene": scene, "seed": seed,
+                                  **coarse_correction_bound(n, scene, seed)}),
+                      flush=True)
+        raise SystemExit(0)
     params, hist = train_stream(a.n, range(a.first_seed,
                                            a.first_seed + a.scenes),
-                                a.pairs, lr=a.lr, loss_kind=a.loss,
-                                own=a.own,
+                                a.pairs, lr=a.lr,
                                 init=load(a.init) if a.init else None)
     save(params, a.out)
     print("saved", a.out, "final loss", np.mean(hist[-100:]))

@@ -60,9 +60,10 @@ typedef enum jetgpu_precision {
 
 typedef enum jetgpu_preconditioner {
     JETGPU_PRECOND_MULTIGRID = 0,
-    /* Learned U-Net preconditioner in flexible PCG, with the multigrid
-     * preconditioner as fallback when iterations stall. Requires weights
-     * loaded with jetgpu_load_unet(). */
+    /* Learned preconditioner in flexible PCG: a multigrid V-cycle plus a
+     * U-Net's coarse-level correction of its error (jetgpu_learned_apply),
+     * with plain multigrid PCG as fallback when iterations stall. Requires
+     * weights loaded with jetgpu_load_unet(). */
     JETGPU_PRECOND_LEARNED = 1,
     /* No preconditioner (plain CG); for comparisons. */
     JETGPU_PRECOND_NONE = 2
@@ -593,13 +594,28 @@ jetgpu_status jetgpu_harvest(struct jetgpu_ctx* ctx, unsigned int max_pairs,
 jetgpu_status jetgpu_vcycle_apply(struct jetgpu_ctx* ctx, const float* r,
                                   float* z);
 
+/* The level of the multigrid hierarchy of the last solved system that the
+ * network works on: the finest level at most 64 cells wide on every axis
+ * (the coarsest level when none is). */
+unsigned int jetgpu_net_level(const struct jetgpu_ctx* ctx);
+
 /* The network's 16 input channels (BF16, channels-last) for residual r on
- * the last solved system, and the network's output z = net(r). DEVICE
- * pointers; synchronous. */
-jetgpu_status jetgpu_net_features(struct jetgpu_ctx* ctx, const float* r,
-                                  void* feat);
-jetgpu_status jetgpu_net_apply(struct jetgpu_ctx* ctx, const float* r,
-                               float* z);
+ * level `level` of the last solved system, and the network's output
+ * e = net(r) there (cells of that level). DEVICE pointers; synchronous. */
+jetgpu_status jetgpu_net_features(struct jetgpu_ctx* ctx, unsigned int level,
+                                  const float* r, void* feat);
+jetgpu_status jetgpu_net_apply(struct jetgpu_ctx* ctx, unsigned int level,
+                               const float* r, float* e);
+
+/* z = M r with the learned preconditioner of JETGPU_PRECOND_LEARNED, for
+ * residual r on the finest level (FP32 DEVICE arrays of cells floats; r and
+ * z must not alias): one V-cycle z0 = V r, then the network's correction of
+ * its error from the residual it leaves, on level k = jetgpu_net_level():
+ * z = z0 + mask P^k net(R^k (r - A z0)), R the V-cycle's masked
+ * restriction, P its trilinear prolongation, mask zero outside the fluid.
+ * Synchronous. */
+jetgpu_status jetgpu_learned_apply(struct jetgpu_ctx* ctx, const float* r,
+                                   float* z);
 
 /* Library version string. */
 const char* jetgpu_version(void);
