@@ -216,6 +216,7 @@ jetgpu_status ensure_buffers(Ctx* c, Dims n, unsigned max_levels) {
         c->built_levels == nl)
         return JETGPU_OK;
     JG_CUDA(c, cudaStreamSynchronize(c->stream));
+    JG_CUDA(c, cudaStreamSynchronize(c->side_stream));
     free_buffers(c);
     c->levels.resize(nl);
     Dims s = n;
@@ -453,6 +454,7 @@ void jetgpu_destroy(jetgpu_ctx* c) {
     cudaSetDevice(c->device);
     if (c->stream) cudaStreamSynchronize(c->stream);
     if (c->copy_stream) cudaStreamSynchronize(c->copy_stream);
+    if (c->side_stream) cudaStreamSynchronize(c->side_stream);
     free_buffers(c);
     release(&c->scal);
     release(&c->partials);

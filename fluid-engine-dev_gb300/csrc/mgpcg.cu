@@ -842,57 +842,96 @@ __global__ void __launch_bounds__(kThreads)
     }
 }
 
-// k_correct for fine rows whose length is a multiple of 4: a thread owns 4
-// consecutive fine cells of a row (fine i = 4m..4m+3, coarse 2m and 2m+1),
-// so the 16 coarse values they share are loaded once, the index division is
-// done once, and the fine values move as one 16-byte load and store. Same
-// stencil, weights and x-then-y-then-z order as k_correct.
+// k_correct for fine rows whose length is a multiple of 4, marching through
+// a run of coarse planes: a thread owns 4 consecutive fine cells of a row
+// (fine i = 4m..4m+3, coarse 2m and 2m+1) and keeps the
+// x-interpolated coarse values of the three coarse planes that the fine
+// planes 2kc and 2kc+1 read (kc-1, kc, kc+1, clamped), so consecutive fine
+// planes share them instead of gathering them again. Same stencil, weights
+// and x-then-y-then-z order as k_correct.
 __global__ void __launch_bounds__(kThreads)
-    k_correct4(const float* __restrict__ coarse, float* __restrict__ fine,
-               Dims c) {
+    k_correct4z(const float* __restrict__ coarse, float* __restrict__ fine,
+                Dims c, int run) {
     const Dims n{2 * c.x, 2 * c.y, 2 * c.z};
-    const Dims q{n.x / 4, n.y, n.z};  // 4-cell groups
-    const long G = q.count();
+    const Dims q{n.x / 4, n.y, 1};  // 4-cell groups of a fine plane
+    const long P = (long)q.x * q.y;
+    const int runs = (c.z + run - 1) / run;
+    const long G = P * runs;
     for (long t = blockIdx.x * (long)kThreads + threadIdx.x; t < G;
          t += (long)gridDim.x * kThreads) {
-        int m, j, k;
-        cell_ijk(t, q, m, j, k);
-        const int cj = j >> 1, ck = k >> 1;
-        int j0, j1, k0, k1;
-        float wj0, wj1, wk0, wk1;
+        const long pr = t % P;
+        const int rz = (int)(t / P);
+        const int m = (int)(pr % q.x), j = (int)(pr / q.x);
+        const int kc0 = rz * run, kc1 = min(kc0 + run, c.z);
+        const int cj = j >> 1;
+        int j0, j1;
+        float wj0, wj1;
         if ((j & 1) == 0) { j0 = j > 1 ? cj - 1 : cj; j1 = cj; wj0 = 0.25f; wj1 = 0.75f; }
         else { j0 = cj; j1 = j + 1 < n.y ? cj + 1 : cj; wj0 = 0.75f; wj1 = 0.25f; }
-        if ((k & 1) == 0) { k0 = k > 1 ? ck - 1 : ck; k1 = ck; wk0 = 0.25f; wk1 = 0.75f; }
-        else { k0 = ck; k1 = k + 1 < n.z ? ck + 1 : ck; wk0 = 0.75f; wk1 = 0.25f; }
-        // Coarse x columns 2m-1 .. 2m+2, clamped as k_correct clamps them.
         const int x0 = 2 * m, xm = m > 0 ? x0 - 1 : x0,
                   x2 = 4 * m + 4 < n.x ? x0 + 2 : x0 + 1;
-        float r[4][4];  // [row (j0,k0),(j1,k0),(j0,k1),(j1,k1)][fine cell]
-        const int rj[4] = {j0, j1, j0, j1}, rk[4] = {k0, k0, k1, k1};
+        // x-interpolated values of coarse plane kc at rows j0 and j1.
+        auto rows = [&](int kc, float r0[4], float r1[4]) {
+            const int rj[2] = {j0, j1};
 #pragma unroll
-        for (int e = 0; e < 4; ++e) {
-            const float* row = coarse + lin(0, rj[e], rk[e], c.x, c.y);
-            const float cm = row[xm], c0 = row[x0], c1 = row[x0 + 1],
-                        c2 = row[x2];
-            r[e][0] = 0.25f * cm + 0.75f * c0;
-            r[e][1] = 0.75f * c0 + 0.25f * c1;
-            r[e][2] = 0.25f * c0 + 0.75f * c1;
-            r[e][3] = 0.75f * c1 + 0.25f * c2;
-        }
-        float4* f4 = reinterpret_cast<float4*>(fine + lin(4 * m, j, k, n.x, n.y));
-        float4 v = *f4;
-        float o[4];
+            for (int e = 0; e < 2; ++e) {
+                const float* row = coarse + lin(0, rj[e], kc, c.x, c.y);
+                const float cm = row[xm], ca = row[x0], cb = row[x0 + 1],
+                            cc = row[x2];
+                float* r = e == 0 ? r0 : r1;
+                r[0] = 0.25f * cm + 0.75f * ca;
+                r[1] = 0.75f * ca + 0.25f * cb;
+                r[2] = 0.25f * ca + 0.75f * cb;
+                r[3] = 0.75f * cb + 0.25f * cc;
+            }
+        };
+        float pm0[4], pm1[4], pc0[4], pc1[4], pp0[4], pp1[4];  // kc-1, kc, kc+1
+        rows(kc0, pc0, pc1);
+        if (kc0 > 0) {
+            rows(kc0 - 1, pm0, pm1);
+        } else {
 #pragma unroll
-        for (int l = 0; l < 4; ++l) {
-            const float a0 = wj0 * r[0][l] + wj1 * r[1][l];
-            const float a1 = wj0 * r[2][l] + wj1 * r[3][l];
-            o[l] = wk0 * a0 + wk1 * a1;
+            for (int l = 0; l < 4; ++l) { pm0[l] = pc0[l]; pm1[l] = pc1[l]; }
         }
-        v.x += o[0];
-        v.y += o[1];
-        v.z += o[2];
-        v.w += o[3];
-        *f4 = v;
+        for (int kc = kc0; kc < kc1; ++kc) {
+            if (kc + 1 < c.z) {
+                rows(kc + 1, pp0, pp1);
+            } else {
+#pragma unroll
+                for (int l = 0; l < 4; ++l) { pp0[l] = pc0[l]; pp1[l] = pc1[l]; }
+            }
+            // Fine plane 2kc: coarse kc-1 (1/4) and kc (3/4); 2kc+1: kc (3/4)
+            // and kc+1 (1/4).
+#pragma unroll
+            for (int h = 0; h < 2; ++h) {
+                const int k = 2 * kc + h;
+                const float* A0 = h == 0 ? pm0 : pc0;
+                const float* A1 = h == 0 ? pm1 : pc1;
+                const float* B0 = h == 0 ? pc0 : pp0;
+                const float* B1 = h == 0 ? pc1 : pp1;
+                const float wk0 = h == 0 ? 0.25f : 0.75f;
+                const float wk1 = h == 0 ? 0.75f : 0.25f;
+                float4* f4 = reinterpret_cast<float4*>(fine + lin(4 * m, j, k, n.x, n.y));
+                float4 v = *f4;
+                float o[4];
+#pragma unroll
+                for (int l = 0; l < 4; ++l) {
+                    const float a0 = wj0 * A0[l] + wj1 * A1[l];
+                    const float a1 = wj0 * B0[l] + wj1 * B1[l];
+                    o[l] = wk0 * a0 + wk1 * a1;
+                }
+                v.x += o[0];
+                v.y += o[1];
+                v.z += o[2];
+                v.w += o[3];
+                *f4 = v;
+            }
+#pragma unroll
+            for (int l = 0; l < 4; ++l) {
+                pm0[l] = pc0[l]; pm1[l] = pc1[l];
+                pc0[l] = pp0[l]; pc1[l] = pp1[l];
+            }
+        }
     }
 }
 
@@ -1279,7 +1318,9 @@ ColLaunch col_launch(const Ctx* c, const Level& L, int tcx, int ty,
     const long tiles = (long)r.tiles_x * ((L.n.y + ty - 1) / ty);
     r.total = tiles * L.n.z;
     long g = (long)c->num_sms * blocks_per_sm;
-    const long by_work = (r.total + 7) / 8;
+    // At least 4 planes a block (a run pays 2 extra steps to fill the
+    // pipeline), so that small levels still spread over the SMs.
+    const long by_work = (r.total + 3) / 4;
     if (g > by_work) g = by_work;
     if (g < 1) g = 1;
     // Blocks that hold neighbouring tiles should stage the same plane at the
@@ -1557,10 +1598,17 @@ float* vcycle_level(Ctx* c, unsigned l, const float* b, float* x, float* alt) {
     const float* xc = vcycle_level(c, l + 1, C.b, C.x, C.x2);
     {
         Prof pr(c, K_CORRECT, 8.0 * L.n.count() + 4.0 * C.n.count());
-        if (L.n.x % 4 == 0)
-            k_correct4<<<grid_for(c, L.n.count() / 4), kThreads, 0,
-                         c->stream>>>(xc, cur, C.n);
-        else
+        if (L.n.x % 4 == 0) {
+            // Runs of coarse planes as long as the grid still fills the
+            // GPU (2048 threads per SM), at most 4.
+            const long groups = L.n.count() / 4 / L.n.z;
+            const long full = (long)c->num_sms * 2048;
+            int run = (int)std::min<long>(
+                4, std::max<long>(1, groups * C.n.z / full));
+            const long items = groups * ((C.n.z + run - 1) / run);
+            k_correct4z<<<blocks_for(items), kThreads, 0, c->stream>>>(
+                xc, cur, C.n, run);
+        } else
             k_correct<<<grid_for(c, L.n.count()), kThreads, 0, c->stream>>>(
                 xc, cur, C.n);
     }
