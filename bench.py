@@ -192,8 +192,8 @@ def solver_params(precision: str, preconditioner: str = "multigrid"):
 # The solver variants the metric compares, all to the same 1e-6 relative
 # true residual: plain MGPCG (FP32 Krylov and V-cycle, FP64-accurate
 # reductions and refinement), the mixed-precision V-cycle (BF16 rows), and
-# the learned U-Net preconditioner in flexible PCG over the mixed V-cycle
-# fallback (when trained weights are present).
+# flexible PCG with the learned preconditioner (the mixed V-cycle plus the
+# U-Net's coarse-level correction; when trained weights are present).
 VARIANTS = {
     "plain_mgpcg": ("fp32", "multigrid"),
     "mixed_mgpcg": ("mixed", "multigrid"),
@@ -642,15 +642,14 @@ def run_smoke(args, local, variant: str, steps: int = 3, cpu: bool = False):
     """The projection of the 512^3 buoyant smoke plume (GridSmokeSolver3:
     all fluid, closed box; the source sphere r = .05 at (.5,.1,.5) pushing
     upward), one device-resident pressure solve per step to the same 1e-6
-    relative true residual, after one warm-up solve."""
+    relative true residual, after one warm-up solve: the headline variant
+    (top-level fields) and, under `variants`, the others of `--variants`
+    (the learned one when its weights are present)."""
     import torch
     import jetgpu
     n = 512
     h = 1.0 / n
     dev = torch.device("cuda", local)
-    prec, _ = VARIANTS[variant]
-    solver = jetgpu.FdmMgpcgSolver3(**solver_params(prec, "multigrid"),
-                                    device=local)
     f64 = dict(dtype=torch.float64, device=dev)
     u = torch.zeros((n, n, n + 1), **f64)
     w = torch.zeros((n + 1, n, n), **f64)
@@ -670,29 +669,55 @@ def run_smoke(args, local, variant: str, steps: int = 3, cpu: bool = False):
     fb, ff = jetgpu.ScalarField(), jetgpu.ScalarField()
     fb.kind, fb.value = 0, jetgpu.kMaxD
     ff.kind, ff.value = 0, -jetgpu.kMaxD
-    stats = jetgpu.SolveStats()
 
-    def solve():
-        jetgpu.solve_pressure_device(solver, grid, u, v, w, fb, ff, *out,
-                                     None, stats=stats)
+    def timed(name):
+        prec, pre = VARIANTS[name]
+        solver = jetgpu.FdmMgpcgSolver3(**solver_params(prec, pre),
+                                        device=local)
+        if pre == "learned":
+            from jetgpu import learned
+            if not os.path.exists(learned.WEIGHTS):
+                solver.close()
+                return None
+            solver.load_network(learned.flatten(learned.load()))
+        stats = jetgpu.SolveStats()
 
-    solve()
-    stream = torch.cuda.ExternalStream(solver.stream(), device=dev)
-    e0 = torch.cuda.Event(enable_timing=True)
-    e1 = torch.cuda.Event(enable_timing=True)
-    torch.cuda.synchronize()
-    e0.record(stream)
-    for _ in range(steps):
+        def solve():
+            jetgpu.solve_pressure_device(solver, grid, u, v, w, fb, ff, *out,
+                                         None, stats=stats)
+
         solve()
-    e1.record(stream)
-    torch.cuda.synchronize()
-    ms = e0.elapsed_time(e1) / steps
-    res = {"grid": n, "cells": n ** 3, "ms_per_solve": round(ms, 3),
-           "solves": steps, "iterations_per_solve": stats.iterations,
-           "relative_residual": stats.relative_residual,
-           "setup_ms": round(stats.setup_ms, 3), "solver": variant,
+        stream = torch.cuda.ExternalStream(solver.stream(), device=dev)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        e0.record(stream)
+        for _ in range(steps):
+            solve()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        r = {"ms_per_solve": round(e0.elapsed_time(e1) / steps, 3),
+             "iterations_per_solve": stats.iterations,
+             "relative_residual": stats.relative_residual,
+             "setup_ms": round(stats.setup_ms, 3)}
+        if pre == "learned":
+            r["multigrid_fallback_used"] = bool(stats.fallback_used)
+        solver.close()
+        return r
+
+    head = timed(variant)
+    res = {"grid": n, "cells": n ** 3, "ms_per_solve": head["ms_per_solve"],
+           "solves": steps, "iterations_per_solve": head["iterations_per_solve"],
+           "relative_residual": head["relative_residual"],
+           "setup_ms": head["setup_ms"], "solver": variant,
            "system": "all fluid, closed box (pure Neumann)"}
-    solver.close()
+    others = {}
+    for name in [x for x in args.variants.split(",") if x and x != variant]:
+        r = timed(name)
+        if r is not None:
+            others[name] = r
+    if others:
+        res["variants"] = others
     if cpu and not args.no_cpu_baseline:
         res["cpu_reference"] = smoke_cpu_sample(n)
     return res
