@@ -1304,53 +1304,38 @@ void rb_half(Ctx* c, const Level& L, const float* b, float* x, int color,
     });
 }
 
-// Launch shape of the fused sweep: a persistent grid of at most the resident
-// block count, with at least 8 planes of work per block so the warm-up of a
-// column segment stays small.
+// Launch shape of the fused sweep. Blocks that hold neighbouring tiles
+// should stage the same plane at the same time: the ring rows and the
+// partial lines at a tile's i-edges are then read from L2, where the
+// neighbour just brought them. Each tile column is cut into segments of
+// seg_len planes (at least 4: a segment pays 2 extra steps to fill the
+// pipeline), numbered segment by segment. When every tile fits in one wave,
+// each block takes one segment and all march in lock-step; otherwise a grid
+// of the resident blocks walks the items in that order, so the resident
+// blocks always work on neighbouring tiles of about the same segment.
 struct ColLaunch {
-    int grid, tiles_x;
-    long total, per_block;
+    int grid, tiles_x, tiles, seg_len;
+    long items;
 };
 ColLaunch col_launch(const Ctx* c, const Level& L, int tcx, int ty,
                      int blocks_per_sm) {
     ColLaunch r;
     r.tiles_x = (L.n.x + tcx - 1) / tcx;
-    const long tiles = (long)r.tiles_x * ((L.n.y + ty - 1) / ty);
-    r.total = tiles * L.n.z;
-    long g = (long)c->num_sms * blocks_per_sm;
-    // At least 4 planes a block (a run pays 2 extra steps to fill the
-    // pipeline), so that small levels still spread over the SMs.
-    const long by_work = (r.total + 3) / 4;
-    if (g > by_work) g = by_work;
-    if (g < 1) g = 1;
-    // Blocks that hold neighbouring tiles should stage the same plane at the
-    // same time: the ring rows and the partial lines at a tile's i-edges are
-    // then read from L2, where the neighbour just brought them. When every
-    // tile fits in one wave, each tile's column is split into m equal
-    // segments (m = resident blocks / tiles), one per block, all marching in
-    // lock-step.
-    if (tiles <= g) {
-        const long m = g / tiles;
-        r.per_block = (L.n.z + m - 1) / m;
-        r.grid = (int)((r.total + r.per_block - 1) / r.per_block);
-        return r;
+    r.tiles = r.tiles_x * ((L.n.y + ty - 1) / ty);
+    const long resident = std::max<long>(1, (long)c->num_sms * blocks_per_sm);
+    if (r.tiles <= resident) {
+        const long m = std::max<long>(
+            1, std::min<long>(resident / r.tiles, (L.n.z + 3) / 4));
+        r.seg_len = (int)((L.n.z + m - 1) / m);
+    } else {
+        // About four items per resident block.
+        const long want = 4 * resident;
+        r.seg_len = (int)std::max<long>(
+            4, std::min<long>(L.n.z, (long)r.tiles * L.n.z / want));
     }
-    // Otherwise, among range lengths up to 15% above the even split, take
-    // the one that keeps j-neighbouring tiles (tiles_x * nz items apart in
-    // the work list) nearest to the same plane.
-    const long p0 = (r.total + g - 1) / g;
-    const long stride = (long)r.tiles_x * L.n.z;
-    long best = p0, bestd = -1;
-    for (long p = p0; p <= p0 + p0 / 7 + 1; ++p) {
-        const long off = stride % p;
-        const long d = std::min(off, p - off);
-        if (bestd < 0 || d < bestd) {
-            bestd = d;
-            best = p;
-        }
-    }
-    r.per_block = best;
-    r.grid = (int)((r.total + r.per_block - 1) / r.per_block);
+    r.items = (long)r.tiles * ((L.n.z + r.seg_len - 1) / r.seg_len);
+    r.grid = (int)(r.tiles <= resident ? r.items
+                                       : std::min<long>(r.items, resident));
     return r;
 }
 
@@ -1434,12 +1419,12 @@ void launch_tma(Ctx* c, const ColLaunch& cl, const TmaMaps& m, int src,
         tsw::k_rb_sweep_tma<true, E, D, TmaCfg<R>::MINB>
             <<<cl.grid, tsw::BLOCK, smem, c->stream>>>(
                 m.b, m.r, m.b, xout, n, first, (float)c->cfg.sor, cl.tiles_x,
-                cl.total, cl.per_block, err);
+                cl.tiles, cl.seg_len, cl.items, err);
     else
         tsw::k_rb_sweep_tma<false, E, D, TmaCfg<R>::MINB>
             <<<cl.grid, tsw::BLOCK, smem, c->stream>>>(
                 m.x[src], m.r, m.b, xout, n, first, (float)c->cfg.sor,
-                cl.tiles_x, cl.total, cl.per_block, err);
+                cl.tiles_x, cl.tiles, cl.seg_len, cl.items, err);
 }
 
 // Shared-memory limit and resident blocks per SM of both TMA sweep variants

@@ -189,7 +189,8 @@ __global__ void __launch_bounds__(BLOCK, MINB)
                    const __grid_constant__ CUtensorMap tm_r,
                    const __grid_constant__ CUtensorMap tm_b,
                    float* __restrict__ xout, Dims n, int first, float omega,
-                   int tiles_x, long total, long per_block, double* err) {
+                   int tiles_x, int tiles, int seg_len, long items,
+                   double* err) {
     using Lt = Layout<E, D>;
     using El = Elem<E>;
     constexpr int XR = Lt::XR, AR = Lt::AR;
@@ -228,13 +229,14 @@ __global__ void __launch_bounds__(BLOCK, MINB)
     Ring ix, ir, wx, wr;
     unsigned nix = 0, nir = 0;
     bool bad = false;
-    long w = (long)blockIdx.x * per_block;
-    const long wend = min(total, w + per_block);
-    while (w < wend) {
-        const int tile = (int)(w / n.z);
-        const int k0 = (int)(w - (long)tile * n.z);
-        const int k1 = (int)min((long)n.z, k0 + (wend - w));
-        w += k1 - k0;
+    // Work items are column segments of seg_len planes, numbered segment
+    // by segment (item = segment * tiles + tile): a block takes items
+    // blockIdx.x, + gridDim.x, ...; the resident blocks then hold
+    // neighbouring tiles of the same segment and march through it together.
+    for (long it = blockIdx.x; it < items; it += gridDim.x) {
+        const int tile = (int)(it % tiles);
+        const int k0 = (int)(it / tiles) * seg_len;
+        const int k1 = min(n.z, k0 + seg_len);
         const int i0 = (tile % tiles_x) * TX;
         const int j0 = (tile / tiles_x) * TY;
         const int gi = i0 - 4 + 4 * gq;  // first cell of the group
