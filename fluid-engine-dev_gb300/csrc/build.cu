@@ -286,6 +286,24 @@ __global__ void k_sample_fluid(float* __restrict__ phi, Dims n, GridDesc g,
     }
 }
 
+// A constant field (ConstantScalarField3, kind 0) gives every sample its
+// value: every face has four equal corner samples and every cell the same
+// fluid SDF, so both arrays are fills (k_face_weights and k_sample_fluid
+// would compute the same values, with the position arithmetic for nothing).
+__global__ void k_fill_face_weight(float* __restrict__ w, long n,
+                                   double value) {
+    const float wv = face_weight(value, value, value, value);
+    for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < n;
+         c += (long)gridDim.x * blockDim.x)
+        w[c] = wv;
+}
+__global__ void k_fill_fluid(float* __restrict__ phi, long n, double value) {
+    const float v = (float)value;
+    for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < n;
+         c += (long)gridDim.x * blockDim.x)
+        phi[c] = v;
+}
+
 // K2: face weights from four boundary-SDF corner samples (:553-617).
 // axis 0/1/2 = u/v/w faces.
 __global__ void k_face_weights(float* __restrict__ wgt, int axis, Dims fn,
@@ -1137,6 +1155,11 @@ TabLayout layout_of(const SampleTables& T) {
 
 }  // namespace
 
+// Grid of a fill: enough blocks to cover the SMs eight times over.
+static int grid_cap(const Ctx* c, long n) {
+    return blocks_for(n, kThreads, c->num_sms * 8);
+}
+
 // The compaction list of the two-pass face-weight kernels: room for n
 // entries and a counter.
 static jetgpu_status grow_list(Ctx* c, size_t n) {
@@ -1169,6 +1192,9 @@ jetgpu_status build_weights(Ctx* c, const GridDesc& g, const FieldDesc& bsdf,
             k_sample_fluid_tab<<<blocks_for(n.count()), kThreads, 0,
                                  c->stream>>>(L0.phi, n, fsdf, T.idx, T.frac,
                                               TL);
+        else if (fsdf.kind == 0)
+            k_fill_fluid<<<grid_cap(c, n.count()), kThreads, 0, c->stream>>>(
+                L0.phi, n.count(), fsdf.value);
         else
             k_sample_fluid<<<blocks_for(n.count()), kThreads, 0, c->stream>>>(
                 L0.phi, n, g, fsdf);
@@ -1205,6 +1231,13 @@ jetgpu_status build_weights(Ctx* c, const GridDesc& g, const FieldDesc& bsdf,
                 (gs = axis_pass(k_face_weights_nodes<2>,
                                 k_face_weights_listed<2>, 2)) != JETGPU_OK)
                 return gs;
+        } else if (bsdf.kind == 0) {
+            k_fill_face_weight<<<grid_cap(c, fu.count()), kThreads, 0,
+                                 c->stream>>>(L0.uw, fu.count(), bsdf.value);
+            k_fill_face_weight<<<grid_cap(c, fv.count()), kThreads, 0,
+                                 c->stream>>>(L0.vw, fv.count(), bsdf.value);
+            k_fill_face_weight<<<grid_cap(c, fw.count()), kThreads, 0,
+                                 c->stream>>>(L0.ww, fw.count(), bsdf.value);
         } else {
             k_face_weights<<<blocks_for(fu.count()), kThreads, 0, c->stream>>>(
                 L0.uw, 0, fu, g, bsdf);

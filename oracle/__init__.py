@@ -172,7 +172,7 @@ class Oracle:
         L.orc_blocked_get_level.argtypes = [C.c_int, C.c_int, C.c_void_p]
         L.orc_level_count.restype = C.c_int
         L.orc_get_level.restype = C.c_long
-        L.orc_get_level.argtypes = [C.c_int, C.c_int, C.c_void_p]
+        L.orc_get_level.argtypes = [C.c_int, C.c_int, C.c_void_p, C.c_size_t]
         L.orc_mgpcg_system.restype = C.c_int
         L.orc_mgpcg_system.argtypes = [C.POINTER(C.c_int), C.c_int, _dp, _dp,
                                        C.POINTER(OrcMgParams), _dp,
@@ -324,7 +324,11 @@ class Oracle:
         code = {"fluid": 0, "uw": 1, "vw": 2, "ww": 3, "A": 4, "b": 5}[what]
         dt = np.float32 if code < 4 else np.float64
         out = np.zeros(shapes[what], dt)
-        n = self.lib.orc_get_level(level, code, out.ctypes.data_as(C.c_void_p))
+        n = self.lib.orc_get_level(level, code, out.ctypes.data_as(C.c_void_p),
+                                   out.nbytes)
+        if n == -2:
+            raise ValueError(f"level {level} {what} does not fit {shapes[what]}"
+                             f" (res0 must be the finest resolution)")
         if n < 0:
             raise IndexError(f"level {level} unavailable")
         return out

@@ -17,6 +17,8 @@
 #ifndef ORACLE_ORACLE_API_H_
 #define ORACLE_ORACLE_API_H_
 
+#include <stddef.h>
+
 #ifdef __cplusplus
 extern "C" {
 #endif
@@ -69,11 +71,12 @@ int orc_pressure_solve(const orc_grid* g, const double* u, const double* v,
 /* Number of multigrid levels built by the last orc_pressure_solve. */
 int orc_level_count(void);
 
-/* Copies a level of the last solve's internal state into dst.
- * what: 0 fluid SDF (float), 1/2/3 u/v/w weights (float),
+/* Copies a level of the last solve's internal state into dst (capacity
+ * bytes). what: 0 fluid SDF (float), 1/2/3 u/v/w weights (float),
  *       4 matrix rows (4 doubles per cell: center,right,up,front), 5 rhs b.
- * Returns the number of elements copied (cells or faces), or -1. */
-long orc_get_level(int level, int what, void* dst);
+ * Returns the number of elements copied (cells or faces), -1 for an
+ * unknown level or array, -2 when the array does not fit (nothing copied). */
+long orc_get_level(int level, int what, void* dst, size_t capacity);
 
 /* FdmMgpcgSolver3::solve on a caller-built multigrid system. Levels are
  * concatenated finest first; level l has resolution res0 >> l.

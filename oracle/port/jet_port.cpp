@@ -911,33 +911,29 @@ int orc_pressure_solve(const orc_grid* g, const double* u, const double* v,
 
 int orc_level_count(void) { return (int)g_state.sizes.size(); }
 
-long orc_get_level(int level, int what, void* dst) {
+long orc_get_level(int level, int what, void* dst, size_t capacity) {
     PressureState& S = g_state;
     if (level < 0 || level >= (int)S.sizes.size()) return -1;
+    // Copies n elements of `size` bytes if they fit the caller's buffer.
+    auto put = [&](const void* src, size_t n, size_t size) -> long {
+        if (n * size > capacity) return -2;
+        std::memcpy(dst, src, n * size);
+        return (long)n;
+    };
     switch (what) {
-        case 0:
-            std::memcpy(dst, S.fluid[level].data(), S.fluid[level].size() * 4);
-            return (long)S.fluid[level].size();
-        case 1:
-            std::memcpy(dst, S.uw[level].data(), S.uw[level].size() * 4);
-            return (long)S.uw[level].size();
-        case 2:
-            std::memcpy(dst, S.vw[level].data(), S.vw[level].size() * 4);
-            return (long)S.vw[level].size();
-        case 3:
-            std::memcpy(dst, S.ww[level].data(), S.ww[level].size() * 4);
-            return (long)S.ww[level].size();
+        case 0: return put(S.fluid[level].data(), S.fluid[level].size(), 4);
+        case 1: return put(S.uw[level].data(), S.uw[level].size(), 4);
+        case 2: return put(S.vw[level].data(), S.vw[level].size(), 4);
+        case 3: return put(S.ww[level].data(), S.ww[level].size(), 4);
         case 4: {
             if (level >= (int)S.levels.size()) return -1;
             const Level& L = S.levels[level];
-            std::memcpy(dst, L.A.data(), L.A.size() * sizeof(Row));
-            return (long)L.A.size();
+            return put(L.A.data(), L.A.size(), sizeof(Row));
         }
         case 5: {
             if (level >= (int)S.levels.size()) return -1;
             const Level& L = S.levels[level];
-            std::memcpy(dst, L.b.data(), L.b.size() * sizeof(double));
-            return (long)L.b.size();
+            return put(L.b.data(), L.b.size(), sizeof(double));
         }
         default:
             return -1;

@@ -204,12 +204,17 @@ int orc_level_count(void) {
     return g_solver ? (int)g_solver->_fluidSdf.size() : 0;
 }
 
-long orc_get_level(int level, int what, void* dst) {
+long orc_get_level(int level, int what, void* dst, size_t capacity) {
     if (!g_solver || level < 0 || level >= orc_level_count()) return -1;
-    auto copyF = [&](const Array3<float>& a) {
-        long n = (long)(a.size().x * a.size().y * a.size().z);
-        std::memcpy(dst, a.data(), n * sizeof(float));
+    // Copies n elements of `size` bytes if they fit the caller's buffer.
+    auto put = [&](const void* src, long n, size_t size) -> long {
+        if ((size_t)n * size > capacity) return -2;
+        std::memcpy(dst, src, (size_t)n * size);
         return n;
+    };
+    auto copyF = [&](const Array3<float>& a) {
+        return put(a.data(), (long)(a.size().x * a.size().y * a.size().z),
+                   sizeof(float));
     };
     switch (what) {
         case 0: return copyF(g_solver->_fluidSdf[level]);
@@ -218,15 +223,13 @@ long orc_get_level(int level, int what, void* dst) {
         case 3: return copyF(g_solver->_wWeights[level]);
         case 4: {
             const auto& A = g_solver->_mgSystem.A.levels[level];
-            long n = (long)(A.size().x * A.size().y * A.size().z);
-            std::memcpy(dst, A.data(), n * sizeof(FdmMatrixRow3));
-            return n;
+            return put(A.data(), (long)(A.size().x * A.size().y * A.size().z),
+                       sizeof(FdmMatrixRow3));
         }
         case 5: {
             const auto& b = g_solver->_mgSystem.b.levels[level];
-            long n = (long)(b.size().x * b.size().y * b.size().z);
-            std::memcpy(dst, b.data(), n * sizeof(double));
-            return n;
+            return put(b.data(), (long)(b.size().x * b.size().y * b.size().z),
+                       sizeof(double));
         }
         default: return -1;
     }

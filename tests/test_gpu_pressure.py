@@ -204,6 +204,35 @@ def test_all_fluid_closed_box_smoke_system(port):
         s.close()
 
 
+def test_constant_fields_build_bit_exact(port):
+    """Constant boundary and fluid SDFs (ConstantScalarField3, as
+    GridSmokeSolver3 without colliders passes them) on a power-of-two cubic
+    grid: the fluid SDF and face weights of every level (filled, not
+    sampled), and the level-0 FP64 rows (the interior unit-weight cells'
+    centre from the exact shortcut) and rhs equal the reference's bit for
+    bit."""
+    n = 32
+    h = 1.0 / n
+    rng = np.random.default_rng(5)
+    u = rng.uniform(-1, 1, (n, n, n + 1))
+    v = rng.uniform(-1, 1, (n, n + 1, n))
+    w = rng.uniform(-1, 1, (n + 1, n, n))
+    s = jetgpu.FdmMgpcgSolver3(200, 4, 2, 2, 10, 2, 1e-6, 1.0, True)
+    ps = jetgpu.GridFractionalSinglePhasePressureSolver3(s)
+    vel = jetgpu.FaceCenteredGrid3((n, n, n), (h, h, h), (0, 0, 0), u, v, w)
+    ps.solve(vel, 1 / 60, vel.clone(), jetgpu.ConstantScalarField3(KMAX),
+             None, jetgpu.ConstantScalarField3(-KMAX))
+    port.pressure_solve((n, n, n), (h, h, h), (0, 0, 0), u, v, w, KMAX, -KMAX,
+                        oracle.MgParams(1, 4, 1, 1, 1, 1, 1e-6, 1.5, True))
+    for l in range(ps.last_stats.levels):
+        for what in ("fluid", "uw", "vw", "ww"):
+            assert np.array_equal(ps.level(l, what),
+                                  port.level(l, what, (n,) * 3).reshape(-1)), (l, what)
+    assert np.array_equal(ps.level(0, "A"), port.level(0, "A", (n,) * 3).reshape(-1))
+    assert np.array_equal(ps.level(0, "b"), port.level(0, "b", (n,) * 3).reshape(-1))
+    s.close()
+
+
 def test_gradient_paths_agree():
     """The vectorised gradient (16-byte aligned faces) and the per-cell one
     (output faces at an 8-byte offset) give the same bits."""
