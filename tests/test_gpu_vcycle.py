@@ -141,7 +141,10 @@ def scene(res, seed):
                           ((72, 36, 40), 1.2, 6, "fp32"),
                           ((72, 36, 40), 1.0, 6, "mixed"),
                           ((96, 40, 48), 1.0, 6, "mixed"),
-                          ((128, 128, 128), 1.0, 6, "mixed")])
+                          ((128, 128, 128), 1.0, 6, "mixed"),
+                          # More 64x8 sweep tiles (512) than resident
+                          # blocks: the segment-by-segment work order.
+                          ((512, 512, 8), 1.2, 4, "fp32")])
 def test_vcycle_matches_numpy_model(res, sor, max_levels, precision):
     cfg = dict(pre=2, post=2, coarsest=10, final=2, sor=sor)
     h, u, v, w, solid, fluid = scene(res, seed=11)
