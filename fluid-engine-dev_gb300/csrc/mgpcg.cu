@@ -1343,8 +1343,10 @@ ColLaunch col_launch(const Ctx* c, const Level& L, int tcx, int ty,
 
 // Row element, prefetch distance (planes) and resident blocks per SM the
 // register budget is set for, of the TMA sweep: with two planes in flight a
-// block holds 68 KB of shared memory with FP32 rows (three blocks per SM)
-// and 51 KB with BF16 rows (four).
+// block holds 68 KB of shared memory with FP32 rows and 51 KB with BF16
+// rows; both run three blocks per SM (BF16 rows at four blocks spill a few
+// registers and were 1% slower; one plane in flight, or two blocks per SM
+// for FP32 rows, were slower too).
 template <typename R> struct TmaCfg;
 template <> struct TmaCfg<RowsF> {
     using E = float;
@@ -1354,7 +1356,7 @@ template <> struct TmaCfg<RowsF> {
 template <> struct TmaCfg<RowsB> {
     using E = unsigned short;
     static constexpr int D = 2;
-    static constexpr int MINB = 4;
+    static constexpr int MINB = 3;
 };
 
 bool tma_ok(const Ctx* c, const Level& L) {
