@@ -4,7 +4,7 @@ ctypes bindings for the two libraries that export ``oracle/oracle_api.h``:
 
 * ``port()``: the CPU restatement of the Jet pressure projection written in
   this repository (``oracle/port/jet_port.cpp``), built by ``oracle/Makefile``.
-  It is the checker the GPU tests compare against and the CPU baseline that
+  It is what the GPU tests compare against and the CPU baseline that
   ``bench.py`` times.
 * ``reference()``: the Jet reference compiled from its own sources
   (``oracle/Makefile.ref`` + ``oracle/ref_harness.cpp``). It exists only where

@@ -38,8 +38,8 @@ Every fixture holds inputs and the reference's outputs for one small case:
   FdmMgpcgSolver3 at tolerance 1e-10, advection) for 3 frames of 1/60 s on
   the 64^3 dam break's geometry at 24^3 (water box [0,.25]x[0,.75]x[0,1],
   8 particles per cell from seed 0, closed walls, gravity (0,-9.8,0)).
-* flip_dam_break_64.npz — FlipSolver3 for BASELINE config 1 at its own
-  size: 64^3, 60 frames of the same dam break (393,216 particles), pressure
+* flip_dam_break_64.npz — FlipSolver3 on the full-size dam break: 64^3,
+  60 frames of the same dam break (393,216 particles), pressure
   to an absolute 1e-10; the pressure after frames 1, 10, 30 and 60
   (float32), every 16th particle's final position and velocity, and the
   mean / standard deviation of all final positions.
@@ -384,7 +384,7 @@ def dam64_pressure(pr):
 
 
 def flip_dam_break_64(ref):
-    """BASELINE config 1 at its own size: FlipSolver3, 64^3 over the unit
+    """The full-size dam break: FlipSolver3, 64^3 over the unit
     cube, the water box [0,.25]x[0,.75]x[0,1] at 8 particles per cell from
     seed 0, gravity (0,-9.8,0), closed walls, maxCfl 5, 60 frames of 1/60 s,
     the pressure solved with FdmMgpcgSolver3 to an absolute 1e-10. Kept: the

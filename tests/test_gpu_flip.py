@@ -45,7 +45,7 @@ def test_dam_break_three_frames_matches_reference(flip):
     ps.close()
 
 
-# Config 1 at its own size: bounds on the GPU run's deviation from the
+# The 64^3 dam break for 60 frames: bounds on the GPU run's deviation from the
 # reference's (golden fixture flip_dam_break_64.npz). The reference itself,
 # run again with its solver at a tolerance of 1e-6 instead of 1e-10, lands
 # 3.6e-8 / 3.2e-8 / 2.2e-6 / 6.6e-2 (pressure relative L2 after frames 1,
@@ -59,7 +59,7 @@ DAM64_CLOUD = 0.01  # |mean| and |std| of all final positions, per axis
 
 
 def test_dam_break_64_sixty_frames_vs_reference():
-    """BASELINE config 1: the 64^3 FlipSolver3 dam break (393,216 particles,
+    """The 64^3 FlipSolver3 dam break (393,216 particles,
     closed box, gravity) for 60 frames of 1/60 s, resident on the GPU, against
     the reference's own run (tests/golden/flip_dam_break_64.npz, pressure
     solved to an absolute 1e-10). The GPU solves every system to a relative
