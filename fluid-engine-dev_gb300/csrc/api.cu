@@ -393,6 +393,7 @@ void jetgpu_config_default(jetgpu_config* cfg) {
     cfg->precision = JETGPU_PRECISION_FP32;
     cfg->preconditioner = JETGPU_PRECOND_MULTIGRID;
     cfg->max_refinements = 6;
+    cfg->ordered_p2g = 1;
 }
 
 jetgpu_status jetgpu_create(const jetgpu_config* cfg, jetgpu_ctx** out) {
@@ -461,6 +462,8 @@ void jetgpu_destroy(jetgpu_ctx* c) {
     release(&c->counters);
     release(&c->stage);
     release(&c->pscratch);
+    release(&c->p2g_int);
+    release(&c->p2g_dbl);
     release(&c->bc_tmp);
     release(&c->bc_valid);
     release(&c->bc_cls);

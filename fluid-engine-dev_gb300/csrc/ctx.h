@@ -155,6 +155,12 @@ struct Ctx {
     // Particle-transfer scratch.
     size_t pscratch_bytes = 0;
     unsigned char* pscratch = nullptr;
+    // Ordered P2G scratch (transfer.cu): bin keys, bin counts / offsets /
+    // cursors, scan totals and the particles listed by bin (ints); each
+    // particle's fractions on the face lattice (doubles).
+    size_t p2g_int_cap = 0, p2g_dbl_cap = 0;
+    int* p2g_int = nullptr;
+    double* p2g_dbl = nullptr;
 
     // Boundary-condition scratch (boundary.cu): bc_cap doubles and 2 x bc_cap
     // validity bytes.
@@ -379,6 +385,13 @@ jetgpu_status norm2f(Ctx* c, const float* r, long n, int target);
 // z = M r with the learned preconditioner (a V-cycle plus the network's
 // coarse-level correction of its error).
 jetgpu_status learned_precond(Ctx* c, const float* r, float* z);
+
+// ---- sdf.cu (shared scan) --------------------------------------------------
+// Exclusive scan of n int counts into off[0..n] (off[n] = the total; also in
+// *grand); tile_sum holds scan_tiles(n) ints of scratch.
+long scan_tiles(long n);
+jetgpu_status scan_counts(Ctx* c, const int* count, int* off, long n,
+                          int* tile_sum, int* grand);
 
 // ---- transfer.cu ----------------------------------------------------------
 jetgpu_status constrain_velocity(Ctx* c, const GridDesc& g, double* u,

@@ -165,6 +165,53 @@ __device__ __forceinline__ void bary<double>(double x, int iHigh, int* i,
     bary_bits(x, iHigh, i, f);
 }
 
+// F * 2^-sh for 0 < F <= 2^sh, sh <= 52 (exactly representable: at most 53
+// significant bits), assembled on the integer pipe.
+__host__ __device__ __forceinline__ double fixed_to_double(
+    unsigned long long F, int sh) {
+#ifdef __CUDA_ARCH__
+    const int p = 63 - __clzll((long long)F);
+#else
+    const int p = 63 - __builtin_clzll(F);
+#endif
+    const unsigned long long be = (unsigned long long)(p - sh + 1023);
+    return bitsd((be << 52) | ((F << (52 - p)) & 0xfffffffffffffull));
+}
+
+static __host__ __device__ __noinline__ double one_minus_slow(double f) {
+    return 1 - f;
+}
+
+// bary_bits plus g = 1 - f, the reference's (1 - fx), bit for bit. For
+// 1 <= x < iHigh the fraction is a multiple of x's last place 2^(e-52), so
+// 1 - f = (2^sh - F) * 2^-sh is exactly representable and is assembled from
+// that integer; the clamped ends give the constants 1 - 0 = 1 and
+// 1 - 1 = +0; f = x < 1 (which 1 - f may round) and NaN take the FP64
+// subtraction.
+__host__ __device__ __forceinline__ void bary_bits2(double x, int iHigh,
+                                                     int* i, double* f,
+                                                     double* g) {
+    const unsigned long long X = dbits(x);
+    const int e = (int)((X >> 52) & 0x7ffu) - 1023;
+    if (iHigh != 0 && !(X >> 63) && e >= 0 && X < dbits((double)iHigh)) {
+        const unsigned long long M = (X & 0xfffffffffffffull) | (1ull << 52);
+        const int sh = 52 - e;  // x < iHigh <= 2^31: 22 <= sh <= 52
+        *i = (int)(M >> sh);
+        const unsigned long long F = M & ((1ull << sh) - 1ull);
+        *f = F ? fixed_to_double(F, sh) : 0.0;
+        *g = fixed_to_double((1ull << sh) - F, sh);
+        return;
+    }
+    bary_bits(x, iHigh, i, f);
+    const unsigned long long fb = dbits(*f);
+    if (fb == 0ull)
+        *g = 1.0;
+    else if (fb == dbits(1.0))
+        *g = 0.0;
+    else
+        *g = one_minus_slow(*f);
+}
+
 // The reference's lerp (include/jet/detail/math_utils-inl.h),
 // (1 - f) * a + f * b, evaluated as the same IEEE operations.
 __host__ __device__ __forceinline__ double lerp_ref(double a, double b,

@@ -290,6 +290,21 @@ jetgpu_status grow(Ctx* c, T** p, size_t* cap, size_t n) {
 
 }  // namespace
 
+long scan_tiles(long n) { return (n + kScanTile - 1) / kScanTile; }
+
+jetgpu_status scan_counts(Ctx* c, const int* count, int* off, long n,
+                          int* tile_sum, int* grand) {
+    cudaStream_t st = c->stream;
+    const int cap = c->num_sms * 16;
+    const long tiles = scan_tiles(n);
+    k_scan_tiles<<<(int)tiles, kScanT, 0, st>>>(count, off, n, tile_sum);
+    k_scan_totals<<<1, kScanT, 0, st>>>(tile_sum, tiles, grand);
+    k_scan_add<<<blocks_for(n + 1, kThreads, cap), kThreads, 0, st>>>(
+        off, n, tile_sum, grand);
+    JG_CUDA(c, cudaGetLastError());
+    return JETGPU_OK;
+}
+
 jetgpu_status build_particle_sdf(Ctx* c, const GridDesc& g, long np,
                                  const double* pos, const FieldDesc& col,
                                  double max_cfl, double* out) {

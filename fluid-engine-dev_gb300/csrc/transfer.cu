@@ -11,12 +11,15 @@
 // (include/jet/detail/array_samplers3-inl.h:151-193) in double precision
 // without multiply-add contraction (this unit is built with -fmad=false), so
 // every particle's eight indices and weights are the reference's. The
-// scatter accumulates with FP64 atomics, so sums match the reference's
-// serial order to rounding, not bit for bit.
+// ordered P2G (the default) adds each face's contributions in the
+// reference's particle order, so its grids are the reference's bit for bit;
+// the atomic scatter accumulates with FP64 atomics, so its sums match the
+// reference's serial order to rounding, not bit for bit.
 
 #include "ctx.h"
 #include "sampling.cuh"
 
+#include <climits>
 #include <mutex>
 
 namespace jg {
@@ -25,42 +28,77 @@ namespace {
 using namespace smp;
 
 // K13a: scatter vel*w and w with FP64 atomics; markers set to 1.
+struct P2gLattice {
+    Dims s;                 // the component's face lattice
+    double ox, oy, oz;      // its origin
+    smp::Spacing sx, sy, sz;  // the grid spacing per axis
+};
+struct P2gLattice3 {
+    P2gLattice l[3];        // u, v, w
+};
+
+P2gLattice p2g_lattice(const FaceSet& fs, int a, const double spacing[3]) {
+    return P2gLattice{fs.s[a], fs.o[a][0], fs.o[a][1], fs.o[a][2],
+                      smp::make_spacing(spacing[0]),
+                      smp::make_spacing(spacing[1]),
+                      smp::make_spacing(spacing[2])};
+}
+P2gLattice3 p2g_lattices(const FaceSet& fs, const double spacing[3]) {
+    return P2gLattice3{{p2g_lattice(fs, 0, spacing), p2g_lattice(fs, 1, spacing),
+                        p2g_lattice(fs, 2, spacing)}};
+}
+
+// x * (1 / h), the reference's normalised coordinate: an exponent add when
+// 1 / h is a power of two.
+__device__ __forceinline__ double p2g_scale(double x, const smp::Spacing& sp) {
+    return sp.pow2 ? smp::scale_exact(x, sp.k, sp.inv) : x * sp.inv;
+}
+
+// Base corner, fractions f and complements g = 1 - f of particle p on the
+// lattice (LinearArraySampler3::getCoordinatesAndWeights, bit for bit).
+__device__ __forceinline__ void p2g_base(const double* __restrict__ pos,
+                                         long p, const P2gLattice& L, int& i,
+                                         int& j, int& k, double3& f,
+                                         double3& g) {
+    const double nx = p2g_scale(pos[3 * p] - L.ox, L.sx);
+    const double ny = p2g_scale(pos[3 * p + 1] - L.oy, L.sy);
+    const double nz = p2g_scale(pos[3 * p + 2] - L.oz, L.sz);
+    smp::bary_bits2(nx, L.s.x - 1, &i, &f.x, &g.x);
+    smp::bary_bits2(ny, L.s.y - 1, &j, &f.y, &g.y);
+    smp::bary_bits2(nz, L.s.z - 1, &k, &f.z, &g.z);
+}
+
 __global__ void k_p2g_scatter(long np, const double* __restrict__ pos,
-                              const double* __restrict__ vel, FaceSet fs,
-                              double ihx, double ihy, double ihz, double* u,
-                              double* v, double* w, double* wu, double* wv,
-                              double* ww, unsigned char* mu, unsigned char* mv,
-                              unsigned char* mw) {
+                              const double* __restrict__ vel, P2gLattice3 L,
+                              double* u, double* v, double* w, double* wu,
+                              double* wv, double* ww, unsigned char* mu,
+                              unsigned char* mv, unsigned char* mw) {
     double* grid[3] = {u, v, w};
     double* wsum[3] = {wu, wv, ww};
     unsigned char* mark[3] = {mu, mv, mw};
     for (long p = blockIdx.x * (long)blockDim.x + threadIdx.x; p < np;
          p += (long)gridDim.x * blockDim.x) {
-        const double px = pos[3 * p], py = pos[3 * p + 1], pz = pos[3 * p + 2];
+#pragma unroll
         for (int a = 0; a < 3; ++a) {
-            const Dims s = fs.s[a];
-            const double nx = (px - fs.o[a][0]) * ihx;
-            const double ny = (py - fs.o[a][1]) * ihy;
-            const double nz = (pz - fs.o[a][2]) * ihz;
+            const Dims s = L.l[a].s;
             int i, j, k;
-            double fx, fy, fz;
-            bary<double>(nx, s.x - 1, &i, &fx);
-            bary<double>(ny, s.y - 1, &j, &fy);
-            bary<double>(nz, s.z - 1, &k, &fz);
+            double3 f, g;
+            p2g_base(pos, p, L.l[a], i, j, k, f, g);
             const int ip1 = min(i + 1, s.x - 1), jp1 = min(j + 1, s.y - 1),
                       kp1 = min(k + 1, s.z - 1);
             const long idx[8] = {lin(i, j, k, s.x, s.y),     lin(ip1, j, k, s.x, s.y),
                                  lin(i, jp1, k, s.x, s.y),   lin(ip1, jp1, k, s.x, s.y),
                                  lin(i, j, kp1, s.x, s.y),   lin(ip1, j, kp1, s.x, s.y),
                                  lin(i, jp1, kp1, s.x, s.y), lin(ip1, jp1, kp1, s.x, s.y)};
-            const double wt[8] = {(1 - fx) * (1 - fy) * (1 - fz), fx * (1 - fy) * (1 - fz),
-                                  (1 - fx) * fy * (1 - fz),       fx * fy * (1 - fz),
-                                  (1 - fx) * (1 - fy) * fz,       fx * (1 - fy) * fz,
-                                  (1 - fx) * fy * fz,             fx * fy * fz};
+            // The reference's weights, (1 - fx) * (1 - fy) * (1 - fz) and so
+            // on, with the (x, y) products formed once.
+            const double xy[4] = {g.x * g.y, f.x * g.y, g.x * f.y, f.x * f.y};
             const double va = vel[3 * p + a];
+#pragma unroll
             for (int q = 0; q < 8; ++q) {
-                atomicAdd(&grid[a][idx[q]], va * wt[q]);
-                atomicAdd(&wsum[a][idx[q]], wt[q]);
+                const double wt = xy[q & 3] * ((q & 4) ? f.z : g.z);
+                atomicAdd(&grid[a][idx[q]], va * wt);
+                atomicAdd(&wsum[a][idx[q]], wt);
                 if (mark[a]) mark[a][idx[q]] = 1;
             }
         }
@@ -78,6 +116,272 @@ __global__ void k_p2g_normalize(double* __restrict__ g,
         if (ws > 0.0) v /= ws;
         g[c] = v;
         if (snap) snap[c] = (float)v;
+    }
+}
+
+// Ordered P2G (ordered_p2g): the reference adds the particles' contributions
+// to each face in particle order (a serial loop, pic_solver3.cpp:118-193);
+// summing each face's contributions in the same order gives the same bits.
+// Per component: every particle is binned by the base corner (i, j, k) of
+// its trilinear stencil on that component's face lattice; each bin lists its
+// particles in increasing index, beside a record of each one's weight
+// factors and velocity component; each face then merges the (at most eight)
+// bins whose stencils reach it, in particle order, adding each particle's
+// corners that land on it in corner order — the reference's products, in
+// the reference's order. GB300 issues FP64 at a small fraction of its
+// integer rate, so the FP64 work is cut to what the sums need: the lattice
+// coordinate is scaled exactly on the integer pipe when the spacing is a
+// power of two, the fractions and their complements (1 - f) come from the
+// coordinate's bits, the four (x, y) weight products are formed once per
+// particle, and a face's step is the z product, the velocity product and
+// the two additions.
+
+// Step 1: the bin (base corner) of every particle; bins counted.
+__global__ void k_p2g_bin(long np, const double* __restrict__ pos,
+                          P2gLattice L, int* __restrict__ key,
+                          int* __restrict__ count) {
+    for (long p = blockIdx.x * (long)blockDim.x + threadIdx.x; p < np;
+         p += (long)gridDim.x * blockDim.x) {
+        int i, j, k;
+        double3 f, g;
+        p2g_base(pos, p, L, i, j, k, f, g);
+        const int b = (int)lin(i, j, k, L.s.x, L.s.y);
+        key[p] = b;
+        atomicAdd(&count[b], 1);
+    }
+}
+
+// Step 2: particle indices into their bins (any order within a bin).
+__global__ void k_p2g_fill(long np, const int* __restrict__ key,
+                          const int* __restrict__ off, int* __restrict__ cursor,
+                          int* __restrict__ list) {
+    for (long p = blockIdx.x * (long)blockDim.x + threadIdx.x; p < np;
+         p += (long)gridDim.x * blockDim.x) {
+        const int b = key[p];
+        list[off[b] + atomicAdd(&cursor[b], 1)] = (int)p;
+    }
+}
+
+// Step 3: every particle at its place in its bin's sorted list (its rank =
+// the number of the bin's particles with a smaller index), with its record:
+// the weight products (1-fx)(1-fy), fx(1-fy), (1-fx)fy, fx fy, then
+// (1 - fz, fz, velocity component, and as a 64-bit integer the next
+// particle of the bin shifted left by 3, all ones after the last).
+__global__ void k_p2g_place(long np, const double* __restrict__ pos,
+                           const double* __restrict__ vel, P2gLattice L,
+                           int a, const int* __restrict__ key,
+                           const int* __restrict__ off,
+                           const int* __restrict__ list,
+                           int* __restrict__ slist,
+                           double4_32a* __restrict__ rec) {
+    for (long p = blockIdx.x * (long)blockDim.x + threadIdx.x; p < np;
+         p += (long)gridDim.x * blockDim.x) {
+        const int b = key[p];
+        const int lo = off[b], hi = off[b + 1];
+        int rank = 0;
+        unsigned succ = 0xffffffffu;
+        for (int q = lo; q < hi; ++q) {
+            const int v = list[q];
+            rank += v < (int)p ? 1 : 0;
+            if (v > (int)p) succ = min(succ, (unsigned)v);
+        }
+        int i, j, k;
+        double3 f, g;
+        p2g_base(pos, p, L, i, j, k, f, g);
+        const long s = lo + rank;
+        slist[s] = (int)p;
+        const unsigned long long nk = succ == 0xffffffffu
+                                          ? ~0ull
+                                          : (unsigned long long)succ << 3;
+        rec[2 * s] = make_double4_32a(g.x * g.y, f.x * g.y, g.x * f.y, f.x * f.y);
+        rec[2 * s + 1] = make_double4_32a(g.z, f.z, vel[3 * p + a],
+                                      __longlong_as_double((long long)nk));
+    }
+}
+
+// One corner's contribution (corner q of the reference's order): weight
+// xy[q & 3] * z[q >> 2], product velocity * weight, both added.
+__device__ __forceinline__ void p2g_corner(int q, const double4_32a& xy,
+                                           const double4_32a& zv, double& acc,
+                                           double& ws) {
+    const double XY = (q & 3) == 0 ? xy.x
+                    : (q & 3) == 1 ? xy.y
+                    : (q & 3) == 2 ? xy.z : xy.w;
+    const double wt = XY * ((q & 4) ? zv.y : zv.x);
+    acc += zv.z * wt;
+    ws += wt;
+}
+
+// Step 4: every face of the component, its contributions in particle order.
+// List l of a face holds the bin at the face minus corner offset l (bit 0:
+// x, bit 1: y, bit 2: z), whose particles reach the face through corner l;
+// on a lattice axis of one line (degenerate mask dm) the upper corner is
+// clamped onto the lower one, so such a bin also reaches the face through
+// the corners that differ from l only in those bits, in corner order. Each
+// list's head is the key (particle index << 3 | l) in a register, so the
+// next contribution is the minimum of eight keys; the taken list advances
+// through selects, its next key read from the record just loaded, so a
+// warp's lanes never split over the lists. A block takes chunks of kGatherChunk consecutive faces from a
+// global counter, writes the chunk's empty faces at once, sorts the others
+// by contribution count in shared memory (a counting sort) and gives each
+// warp 32 faces of (nearly) equal count at a time, so the lanes run the same
+// number of steps. K is a 32-bit key when particle indices fit in 28 bits,
+// else 64-bit.
+constexpr int kGatherChunk = 1024;
+constexpr int kGatherThreads = 256;
+constexpr int kGatherBuckets = 128;  // counts >= 127 share the last bucket
+
+template <typename K>
+__device__ __forceinline__ K p2g_min8(const K (&h)[8]) {
+    const K a = min(h[0], h[1]), b = min(h[2], h[3]);
+    const K c = min(h[4], h[5]), d = min(h[6], h[7]);
+    return min(min(a, b), min(c, d));
+}
+
+// The bin of list l of face (fi, fj, fk), or -1 outside the lattice.
+__device__ __forceinline__ long p2g_list_bin(const Dims& s, int fi, int fj,
+                                             int fk, int l) {
+    const int x = fi - (l & 1), y = fj - ((l >> 1) & 1), z = fk - (l >> 2);
+    return x >= 0 && y >= 0 && z >= 0 ? lin(x, y, z, s.x, s.y) : -1;
+}
+
+template <typename K>
+__global__ void __launch_bounds__(kGatherThreads)
+k_p2g_gather(Dims s, int dm, const int* __restrict__ count,
+             const int* __restrict__ off, const int* __restrict__ slist,
+             const double4_32a* __restrict__ rec, double* __restrict__ grid,
+             double* __restrict__ wsum, unsigned char* __restrict__ mark,
+             unsigned long long* __restrict__ counter) {
+    constexpr int kPer = kGatherChunk / kGatherThreads;
+    constexpr int kWarps = kGatherThreads / 32;
+    __shared__ unsigned short s_face[kGatherChunk];
+    __shared__ int s_hist[kGatherBuckets];
+    __shared__ long long s_c0;
+    __shared__ int s_total;
+    const K kNone = ~(K)0;
+    const long nf = s.count();
+    const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    while (true) {
+        if (tid == 0) s_c0 = (long long)atomicAdd(counter, kGatherChunk);
+        for (int t = tid; t < kGatherBuckets; t += kGatherThreads)
+            s_hist[t] = 0;
+        __syncthreads();
+        const long c0 = (long)s_c0;
+        if (c0 >= nf) break;
+        // Contribution counts; empty faces written now.
+        int bucket[kPer];
+#pragma unroll
+        for (int r = 0; r < kPer; ++r) {
+            const long f = c0 + tid + r * kGatherThreads;
+            bucket[r] = 0;
+            if (f < nf) {
+                int fi, fj, fk;
+                cell_ijk(f, s, fi, fj, fk);
+                int n = 0;
+#pragma unroll
+                for (int l = 0; l < 8; ++l) {
+                    const long b = p2g_list_bin(s, fi, fj, fk, l);
+                    n += b >= 0 ? count[b] : 0;
+                }
+                if (n == 0) {
+                    grid[f] = 0.0;
+                    wsum[f] = 0.0;
+                    if (mark) mark[f] = 0;
+                } else {
+                    bucket[r] = min(n, kGatherBuckets - 1);
+                    atomicAdd(&s_hist[bucket[r]], 1);
+                }
+            }
+        }
+        __syncthreads();
+        // Exclusive scan of the histogram (one warp), then the faces in
+        // order of count.
+        if (warp == 0) {
+            constexpr int kPerLane = kGatherBuckets / 32;
+            int v[kPerLane], sum = 0;
+#pragma unroll
+            for (int t = 0; t < kPerLane; ++t) {
+                v[t] = s_hist[lane * kPerLane + t];
+                sum += v[t];
+            }
+            int incl = sum;
+#pragma unroll
+            for (int d = 1; d < 32; d <<= 1) {
+                const int o = __shfl_up_sync(0xffffffffu, incl, d);
+                if (lane >= d) incl += o;
+            }
+            int run = incl - sum;
+#pragma unroll
+            for (int t = 0; t < kPerLane; ++t) {
+                s_hist[lane * kPerLane + t] = run;
+                run += v[t];
+            }
+            if (lane == 31) s_total = incl;
+        }
+        __syncthreads();
+#pragma unroll
+        for (int r = 0; r < kPer; ++r)
+            if (bucket[r] > 0)
+                s_face[atomicAdd(&s_hist[bucket[r]], 1)] =
+                    (unsigned short)(tid + r * kGatherThreads);
+        __syncthreads();
+        const int total = s_total;
+        for (int g0 = warp * 32; g0 < total; g0 += kWarps * 32) {
+            const int i = g0 + lane;
+            const long f = i < total ? c0 + s_face[i] : -1;
+            int cur[8];
+            K head[8];
+            int fi = 0, fj = 0, fk = 0;
+            if (f >= 0) cell_ijk(f, s, fi, fj, fk);
+#pragma unroll
+            for (int l = 0; l < 8; ++l) {
+                const long b = f >= 0 ? p2g_list_bin(s, fi, fj, fk, l) : -1;
+                cur[l] = b >= 0 ? off[b] : 0;
+                const int e = b >= 0 ? off[b + 1] : 0;
+                head[l] = cur[l] < e ? ((K)slist[cur[l]] << 3) | (K)l : kNone;
+            }
+            K key = p2g_min8(head);
+            bool busy = key != kNone;
+            double acc = 0.0, ws = 0.0;
+            while (__ballot_sync(0xffffffffu, busy)) {
+                if (busy) {
+                    const int best = (int)(key & 7);
+                    // cur[best] through a three-level select tree.
+                    const bool b0 = best & 1, b1 = best & 2, b2 = best & 4;
+                    const int s01 = b0 ? cur[1] : cur[0];
+                    const int s23 = b0 ? cur[3] : cur[2];
+                    const int s45 = b0 ? cur[5] : cur[4];
+                    const int s67 = b0 ? cur[7] : cur[6];
+                    const int s03 = b1 ? s23 : s01, s47 = b1 ? s67 : s45;
+                    const int slot = b2 ? s47 : s03;
+                    const double4_32a xy = rec[2 * (long)slot];
+                    const double4_32a zv = rec[2 * (long)slot + 1];
+                    const K nh = (K)(unsigned long long)__double_as_longlong(
+                                     zv.w) |
+                                 (K)best;
+#pragma unroll
+                    for (int l = 0; l < 8; ++l) {
+                        cur[l] = best == l ? slot + 1 : cur[l];
+                        head[l] = best == l ? nh : head[l];
+                    }
+                    if (dm == 0) {
+                        p2g_corner(best, xy, zv, acc, ws);
+                    } else {
+                        for (int q = 0; q < 8; ++q)
+                            if (((q ^ best) & ~dm & 7) == 0)
+                                p2g_corner(q, xy, zv, acc, ws);
+                    }
+                    key = p2g_min8(head);
+                    busy = key != kNone;
+                }
+            }
+            if (f >= 0) {
+                grid[f] = acc;
+                wsum[f] = ws;
+                if (mark) mark[f] = 1;
+            }
+        }
+        __syncthreads();
     }
 }
 
@@ -465,6 +769,97 @@ jetgpu_status move_particles(Ctx* c, const GridDesc& g, long np, double* pos,
     return JETGPU_OK;
 }
 
+// The ordered P2G of all three components (k_p2g_bin .. k_p2g_gather): every
+// face's value, weight sum and marker written.
+static jetgpu_status p2g_ordered(Ctx* c, const GridDesc& g, long np,
+                                 const double* pos, const double* vel,
+                                 const FaceSet& fs, const long n[3],
+                                 double* const grid[3], double* wsum,
+                                 unsigned char* const mark[3]) {
+    const long nb = std::max(std::max(n[0], n[1]), n[2]);  // bins (faces)
+    const long tiles = scan_tiles(nb);
+    // Ints: key, list, sorted list (np each), count, off (nb + 1), cursor,
+    // scan totals (tiles), the grand total, and the gather's face counter
+    // (two ints, 8-byte aligned).
+    const size_t ni = (size_t)(3 * np + 3 * nb + 1 + tiles + 1 + 3);
+    if (c->p2g_int_cap < ni) {
+        if (c->p2g_int) cudaFree(c->p2g_int);
+        c->p2g_int = nullptr;
+        c->p2g_int_cap = 0;
+        JG_CUDA(c, cudaMalloc((void**)&c->p2g_int, ni * sizeof(int)));
+        c->p2g_int_cap = ni;
+    }
+    const size_t nd = (size_t)(8 * np);  // records: two double4_32a a particle
+    if (c->p2g_dbl_cap < nd) {
+        if (c->p2g_dbl) cudaFree(c->p2g_dbl);
+        c->p2g_dbl = nullptr;
+        c->p2g_dbl_cap = 0;
+        JG_CUDA(c, cudaMalloc((void**)&c->p2g_dbl, nd * sizeof(double)));
+        c->p2g_dbl_cap = nd;
+    }
+    int* key = c->p2g_int;
+    int* list = key + np;
+    int* slist = list + np;
+    int* count = slist + np;
+    int* off = count + nb;
+    int* cursor = off + nb + 1;
+    int* tile_sum = cursor + nb;
+    int* grand = tile_sum + tiles;
+    const size_t ci = ((size_t)(grand + 1 - c->p2g_int) + 1) & ~(size_t)1;
+    unsigned long long* counter =
+        reinterpret_cast<unsigned long long*>(c->p2g_int + ci);
+    double4_32a* rec = reinterpret_cast<double4_32a*>(c->p2g_dbl);
+    const int cap = c->num_sms * 16;
+    // 32-bit keys (particle index << 3 | list) while indices fit 28 bits.
+    const bool k32 = np < (1l << 28);
+    int gather_grid = 0;
+    if (k32)
+        JG_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                       &gather_grid, k_p2g_gather<unsigned>, kGatherThreads,
+                       0));
+    else
+        JG_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                       &gather_grid, k_p2g_gather<unsigned long long>,
+                       kGatherThreads, 0));
+    gather_grid = std::max(1, gather_grid) * c->num_sms;
+    long woff = 0;
+    for (int a = 0; a < 3; ++a) {
+        // Algorithmic bytes: a third of the particles' positions and
+        // velocities, and the face's value, weight sum and marker.
+        Prof pr(c, K_P2G, 16.0 * np + 17.0 * n[a]);
+        const Dims s = fs.s[a];
+        const P2gLattice L = p2g_lattice(fs, a, g.spacing);
+        const int dm = (s.x == 1 ? 1 : 0) | (s.y == 1 ? 2 : 0) |
+                       (s.z == 1 ? 4 : 0);
+        JG_CUDA(c, cudaMemsetAsync(count, 0, n[a] * sizeof(int), c->stream));
+        JG_CUDA(c, cudaMemsetAsync(cursor, 0, n[a] * sizeof(int), c->stream));
+        JG_CUDA(c, cudaMemsetAsync(counter, 0, sizeof(unsigned long long),
+                                   c->stream));
+        k_p2g_bin<<<blocks_for(np, kThreads, cap), kThreads, 0, c->stream>>>(
+            np, pos, L, key, count);
+        jetgpu_status st = scan_counts(c, count, off, n[a], tile_sum, grand);
+        if (st != JETGPU_OK) return st;
+        k_p2g_fill<<<blocks_for(np, kThreads, cap), kThreads, 0, c->stream>>>(
+            np, key, off, cursor, list);
+        k_p2g_place<<<blocks_for(np, kThreads, cap), kThreads, 0,
+                      c->stream>>>(np, pos, vel, L, a, key, off, list, slist,
+                                   rec);
+        if (k32)
+            k_p2g_gather<unsigned>
+                <<<gather_grid, kGatherThreads, 0, c->stream>>>(
+                    s, dm, count, off, slist, rec, grid[a], wsum + woff,
+                    mark[a], counter);
+        else
+            k_p2g_gather<unsigned long long>
+                <<<gather_grid, kGatherThreads, 0, c->stream>>>(
+                    s, dm, count, off, slist, rec, grid[a], wsum + woff,
+                    mark[a], counter);
+        woff += n[a];
+    }
+    JG_CUDA(c, cudaGetLastError());
+    return JETGPU_OK;
+}
+
 jetgpu_status p2g(Ctx* c, const GridDesc& g, long np, const double* pos,
                   const double* vel, double* u, double* v, double* w,
                   unsigned char* mu, unsigned char* mv, unsigned char* mw,
@@ -483,16 +878,27 @@ jetgpu_status p2g(Ctx* c, const GridDesc& g, long np, const double* pos,
     double* grid[3] = {u, v, w};
     unsigned char* mark[3] = {mu, mv, mw};
     float* snap[3] = {su, sv, sw};
-    JG_CUDA(c, cudaMemsetAsync(wsum, 0, need, c->stream));
-    for (int a = 0; a < 3; ++a) {
-        JG_CUDA(c, cudaMemsetAsync(grid[a], 0, n[a] * sizeof(double), c->stream));
-        if (mark[a]) JG_CUDA(c, cudaMemsetAsync(mark[a], 0, n[a], c->stream));
+    // The ordered gather writes every face (value, weight sum, marker) and
+    // keeps its particle and bin numbers in ints.
+    const bool ordered = np > 0 && c->cfg.ordered_p2g && np < INT_MAX &&
+                         std::max(std::max(n[0], n[1]), n[2]) < INT_MAX;
+    if (!ordered) {
+        JG_CUDA(c, cudaMemsetAsync(wsum, 0, need, c->stream));
+        for (int a = 0; a < 3; ++a) {
+            JG_CUDA(c, cudaMemsetAsync(grid[a], 0, n[a] * sizeof(double),
+                                       c->stream));
+            if (mark[a])
+                JG_CUDA(c, cudaMemsetAsync(mark[a], 0, n[a], c->stream));
+        }
     }
-    if (np > 0) {
+    if (ordered) {
+        jetgpu_status os = p2g_ordered(c, g, np, pos, vel, fs, n, grid, wsum,
+                                       mark);
+        if (os != JETGPU_OK) return os;
+    } else if (np > 0) {
         Prof pr(c, K_P2G, 48.0 * np + 2.0 * 3 * 8.0 * (n[0] + n[1] + n[2]));
         k_p2g_scatter<<<blocks_for(np, kThreads, c->num_sms * 16), kThreads, 0,
-                        c->stream>>>(np, pos, vel, fs, 1.0 / g.spacing[0],
-                                     1.0 / g.spacing[1], 1.0 / g.spacing[2],
+                        c->stream>>>(np, pos, vel, p2g_lattices(fs, g.spacing),
                                      u, v, w, wsum, wsum + n[0],
                                      wsum + n[0] + n[1], mu, mv, mw);
     }
@@ -694,9 +1100,8 @@ extern "C" jetgpu_status jetgpu_p2g_device_noalloc(
     }
     if (np > 0)
         k_p2g_scatter<<<blocks_for(np, kThreads, sms * 16), kThreads, 0, st>>>(
-            np, pos, vel, fs, 1.0 / g.spacing[0], 1.0 / g.spacing[1],
-            1.0 / g.spacing[2], u, v, w, wsum, wsum + n[0], wsum + n[0] + n[1],
-            mu, mv, mw);
+            np, pos, vel, p2g_lattices(fs, g.spacing), u, v, w, wsum,
+            wsum + n[0], wsum + n[0] + n[1], mu, mv, mw);
     size_t off = 0;
     for (int a = 0; a < 3; ++a) {
         k_p2g_normalize<<<blocks_for((long)n[a]), kThreads, 0, st>>>(

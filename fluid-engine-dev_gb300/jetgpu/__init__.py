@@ -50,6 +50,7 @@ class Config(C.Structure):
         ("precision", C.c_int),
         ("preconditioner", C.c_int),
         ("max_refinements", C.c_uint),
+        ("ordered_p2g", C.c_int),
     ]
 
 
@@ -417,7 +418,7 @@ class FdmMgpcgSolver3:
                  numberOfCoarsestIter=5, numberOfFinalIter=2,
                  maxTolerance=1e-6, sorFactor=1.2, useRedBlackOrdering=True,
                  precision="fp32", device=0, maxRefinements=6,
-                 preconditioner="multigrid"):
+                 preconditioner="multigrid", orderedP2G=True):
         if not useRedBlackOrdering:
             raise ValueError("the GPU smoother is red-black; the lexicographic "
                              "Gauss-Seidel sweep is serial by construction")
@@ -437,6 +438,9 @@ class FdmMgpcgSolver3:
         cfg.precision = PRECISION[precision]
         cfg.preconditioner = PRECONDITIONER[preconditioner]
         cfg.max_refinements = maxRefinements
+        # P2G in particle order (bit-exact with the reference) or by FP64
+        # atomics (faster; rounding-level differences).
+        cfg.ordered_p2g = 1 if orderedP2G else 0
         self._ctx = None
         self.last_stats = SolveStats()
 

@@ -95,6 +95,12 @@ typedef struct jetgpu_config {
     int precision;              /* jetgpu_precision */
     int preconditioner;         /* jetgpu_preconditioner */
     unsigned int max_refinements; /* FP32 modes: FP64 refinement passes */
+    /* P2G (jetgpu_p2g[_device], the FLIP/PIC sub-step): nonzero sums every
+     * face's contributions in particle order, as the reference's serial loop
+     * does (pic_solver3.cpp:118-193), so the grids are bit-exact and the same
+     * from run to run; zero scatters with FP64 atomics (faster; the sums
+     * differ from the reference's in rounding only). */
+    int ordered_p2g;
 } jetgpu_config;
 
 /* Fills `cfg` with defaults: FdmMgpcgSolver3(100, 6, 2, 2, 5, 2, 1e-6, 1.2,

@@ -1,5 +1,6 @@
-// Host check of smp::bary_bits (csrc/sampling.cuh): the integer-pipe
-// barycentric split must give the same (index, fraction) bits as the FP64
+// Host check of smp::bary_bits and smp::bary_bits2 (csrc/sampling.cuh): the
+// integer-pipe barycentric split must give the same (index, fraction, and
+// for bary_bits2 one minus the fraction) bits as the FP64
 // form of getBarycentric (include/jet/detail/math_utils-inl.h:147-172) for
 // random values, random bit patterns (negatives, NaN, infinities,
 // subnormals), integers and their neighbours, and sample coordinates of the
@@ -36,19 +37,25 @@ int main() {
     std::mt19937_64 g(1);
     long bad = 0, n = 0;
     auto check = [&](double x, int ih) {
-        int i1, i2;
-        double f1, f2;
+        int i1, i2, i3;
+        double f1, f2, f3, g3;
         reference(x, ih, &i1, &f1);
         bary_bits(x, ih, &i2, &f2);
-        unsigned long long b1, b2;
-        std::memcpy(&b1, &f1, 8);
-        std::memcpy(&b2, &f2, 8);
-        const bool both_nan = std::isnan(f1) && std::isnan(f2);
+        bary_bits2(x, ih, &i3, &f3, &g3);
+        const double g1 = 1 - f1;
+        auto same = [](double a, double b) {
+            unsigned long long ba, bb;
+            std::memcpy(&ba, &a, 8);
+            std::memcpy(&bb, &b, 8);
+            return ba == bb || (std::isnan(a) && std::isnan(b));
+        };
         ++n;
-        if (i1 != i2 || (b1 != b2 && !both_nan)) {
+        if (i1 != i2 || !same(f1, f2) || i1 != i3 || !same(f1, f3) ||
+            !same(g1, g3)) {
             if (bad < 10)
-                std::printf("x=%.17g iHigh=%d reference (%d, %.17g) bits (%d, %.17g)\n",
-                            x, ih, i1, f1, i2, f2);
+                std::printf("x=%.17g iHigh=%d reference (%d, %.17g, %.17g) "
+                            "bits (%d, %.17g) bits2 (%d, %.17g, %.17g)\n",
+                            x, ih, i1, f1, g1, i2, f2, i3, f3, g3);
             ++bad;
         }
     };

@@ -18,16 +18,61 @@ def solver():
 
 
 def test_p2g_matches_reference(solver):
+    """The default P2G sums each face's contributions in particle order, as
+    the reference's serial loop does: grids, markers and FLIP snapshots
+    equal the reference's bit for bit."""
     g = golden("transfer_16.npz")
     n, h = 16, 1.0 / 16
     grid = jetgpu.FaceCenteredGrid3((n, n, n), (h, h, h))
     marks, snaps = jetgpu.transfer_from_particles_to_grids(solver, grid,
                                                            g["pos"], g["vel"])
     for a, k in enumerate("uvw"):
-        # FP64 atomics reorder the reference's serial sums: rounding only.
+        assert np.array_equal(getattr(grid, k), g[k]), k
+        assert np.array_equal(marks[a], g["m" + k].astype(np.uint8))
+        assert np.array_equal(snaps[a], g["s" + k]), k
+
+
+def test_p2g_atomic_scatter_matches_reference():
+    """orderedP2G=False: FP64 atomics reorder the reference's serial sums,
+    so the grids agree to rounding only."""
+    s = jetgpu.FdmMgpcgSolver3(200, 4, 2, 2, 10, 2, 1e-6, 1.0, True,
+                               orderedP2G=False)
+    g = golden("transfer_16.npz")
+    n, h = 16, 1.0 / 16
+    grid = jetgpu.FaceCenteredGrid3((n, n, n), (h, h, h))
+    marks, snaps = jetgpu.transfer_from_particles_to_grids(s, grid, g["pos"],
+                                                           g["vel"])
+    for a, k in enumerate("uvw"):
         assert np.allclose(getattr(grid, k), g[k], rtol=1e-12, atol=1e-13)
         assert np.array_equal(marks[a], g["m" + k].astype(np.uint8))
         assert np.allclose(snaps[a], g["s" + k], rtol=2e-7, atol=1e-30)
+    s.close()
+
+
+def test_p2g_ordered_is_deterministic_and_exact_at_size():
+    """64^3 dam break particles (393,216, jittered): the ordered P2G gives
+    the same bits on every call and equals the reference restatement's
+    serial sums bit for bit."""
+    import oracle
+    from jetgpu import scenes
+    n = 64
+    h = 1.0 / n
+    pos, vel = scenes.dam_break_particles(n, (0.25, 0.75, 1.0), seed=0)
+    rng = np.random.default_rng(3)
+    vel = rng.uniform(-1, 1, pos.shape)
+    s = jetgpu.FdmMgpcgSolver3(200, 4, 2, 2, 10, 2, 1e-6, 1.0, True)
+    out = []
+    for _ in range(2):
+        grid = jetgpu.FaceCenteredGrid3((n, n, n), (h, h, h))
+        jetgpu.transfer_from_particles_to_grids(s, grid, pos, vel)
+        out.append((grid.u.copy(), grid.v.copy(), grid.w.copy()))
+    s.close()
+    for a in range(3):
+        assert np.array_equal(out[0][a], out[1][a])
+    port = oracle.port()
+    grids, marks, snaps = port.p2g((n, n, n), (h, h, h), (0, 0, 0), pos, vel)
+    for a in range(3):
+        assert np.array_equal(out[0][a], grids[a]), a
 
 
 def test_g2p_flip_and_pic_match_reference(solver):
