@@ -331,6 +331,34 @@ __device__ T sample_face(const V* __restrict__ d, Dims s, T nx, T ny, T nz) {
                       fz);
 }
 
+// sample_face<double, double> with the complements 1 - f of the fractions
+// taken from the coordinate's bits (bary_bits2) instead of the FP64
+// subtraction: the same bits, three FP64 operations fewer per sample.
+__device__ __forceinline__ double lerp_g(double a, double b, double f,
+                                         double g) {
+    return g * a + f * b;
+}
+__device__ __forceinline__ double sample_face_d(const double* __restrict__ d,
+                                                Dims s, double nx, double ny,
+                                                double nz) {
+    int i, j, k;
+    double fx, fy, fz, gx, gy, gz;
+    bary_bits2(nx, s.x - 1, &i, &fx, &gx);
+    bary_bits2(ny, s.y - 1, &j, &fy, &gy);
+    bary_bits2(nz, s.z - 1, &k, &fz, &gz);
+    const int ip1 = min(i + 1, s.x - 1), jp1 = min(j + 1, s.y - 1),
+              kp1 = min(k + 1, s.z - 1);
+    const double f000 = d[lin(i, j, k, s.x, s.y)], f100 = d[lin(ip1, j, k, s.x, s.y)];
+    const double f010 = d[lin(i, jp1, k, s.x, s.y)], f110 = d[lin(ip1, jp1, k, s.x, s.y)];
+    const double f001 = d[lin(i, j, kp1, s.x, s.y)], f101 = d[lin(ip1, j, kp1, s.x, s.y)];
+    const double f011 = d[lin(i, jp1, kp1, s.x, s.y)], f111 = d[lin(ip1, jp1, kp1, s.x, s.y)];
+    const double b0 = lerp_g(lerp_g(f000, f100, fx, gx),
+                             lerp_g(f010, f110, fx, gx), fy, gy);
+    const double b1 = lerp_g(lerp_g(f001, f101, fx, gx),
+                             lerp_g(f011, f111, fx, gx), fy, gy);
+    return lerp_g(b0, b1, fz, gz);
+}
+
 // sample_face for points that usually sit on the sampled grid's lattice
 // (collider SDF at faces and cell centres, SDFs at nodes): same result, with
 // trilerp_grid's shortcuts. Particle positions use sample_face.

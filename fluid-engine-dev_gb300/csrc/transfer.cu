@@ -402,8 +402,8 @@ __global__ void k_g2p_flip(long np, const double* __restrict__ pos,
                            const float* __restrict__ dw,
                            const double* __restrict__ u,
                            const double* __restrict__ v,
-                           const double* __restrict__ w, double hx, double hy,
-                           double hz, double blend) {
+                           const double* __restrict__ w, Spacing hx,
+                           Spacing hy, Spacing hz, double blend) {
     const float* dl[3] = {du, dv, dw};
     const double* g[3] = {u, v, w};
     for (long p = blockIdx.x * (long)blockDim.x + threadIdx.x; p < np;
@@ -422,9 +422,9 @@ __global__ void k_g2p_flip(long np, const double* __restrict__ pos,
         if (blend > 0.0) {
             double pic[3];
             for (int a = 0; a < 3; ++a)
-                pic[a] = sample_face<double, double>(
-                    g[a], fs.s[a], (px - fs.o[a][0]) / hx,
-                    (py - fs.o[a][1]) / hy, (pz - fs.o[a][2]) / hz);
+                pic[a] = sample_face_d(
+                    g[a], fs.s[a], hx.div(px - fs.o[a][0]),
+                    hy.div(py - fs.o[a][1]), hz.div(pz - fs.o[a][2]));
             for (int a = 0; a < 3; ++a)
                 out[a] = (1 - blend) * out[a] + blend * pic[a];
         }
@@ -439,16 +439,16 @@ __global__ void k_g2p_pic(long np, const double* __restrict__ pos,
                           double* __restrict__ vel, FaceSet fs,
                           const double* __restrict__ u,
                           const double* __restrict__ v,
-                          const double* __restrict__ w, double hx, double hy,
-                          double hz) {
+                          const double* __restrict__ w, Spacing hx,
+                          Spacing hy, Spacing hz) {
     const double* g[3] = {u, v, w};
     for (long p = blockIdx.x * (long)blockDim.x + threadIdx.x; p < np;
          p += (long)gridDim.x * blockDim.x) {
         const double px = pos[3 * p], py = pos[3 * p + 1], pz = pos[3 * p + 2];
         for (int a = 0; a < 3; ++a)
-            vel[3 * p + a] = sample_face<double, double>(
-                g[a], fs.s[a], (px - fs.o[a][0]) / hx, (py - fs.o[a][1]) / hy,
-                (pz - fs.o[a][2]) / hz);
+            vel[3 * p + a] = sample_face_d(
+                g[a], fs.s[a], hx.div(px - fs.o[a][0]),
+                hy.div(py - fs.o[a][1]), hz.div(pz - fs.o[a][2]));
     }
 }
 
@@ -532,7 +532,7 @@ __global__ void k_apic_g2p(long np, const double* __restrict__ pos,
          p += (long)gridDim.x * blockDim.x) {
         const double px = pos[3 * p], py = pos[3 * p + 1], pz = pos[3 * p + 2];
         for (int a = 0; a < 3; ++a)
-            vel[3 * p + a] = sample_face<double, double>(
+            vel[3 * p + a] = sample_face_d(
                 g[a], fs.s[a], sx.div(px - fs.o[a][0]), sy.div(py - fs.o[a][1]),
                 sz.div(pz - fs.o[a][2]));
         for (int a = 0; a < 3; ++a) {
@@ -693,7 +693,7 @@ __global__ void k_move_particles(long np, double* __restrict__ pos,
             }
 #pragma unroll
             for (int a = 0; a < 3; ++a)
-                out[a] = sample_face<double, double>(
+                out[a] = sample_face_d(
                     grid[a], fs.s[a], a == 0 ? nn[0] : nt[0],
                     a == 1 ? nn[1] : nt[1], a == 2 ? nn[2] : nt[2]);
         };
@@ -926,8 +926,9 @@ jetgpu_status g2p_flip(Ctx* c, const GridDesc& g, long np, const double* pos,
         Prof pr(c, K_G2P, 48.0 * np);
         k_g2p_flip<<<blocks_for(np), kThreads, 0, c->stream>>>(
             np, pos, vel, fs, (float)g.spacing[0], (float)g.spacing[1],
-            (float)g.spacing[2], su, sv, sw, u, v, w, g.spacing[0],
-            g.spacing[1], g.spacing[2], blend);
+            (float)g.spacing[2], su, sv, sw, u, v, w,
+            make_spacing(g.spacing[0]), make_spacing(g.spacing[1]),
+            make_spacing(g.spacing[2]), blend);
     }
     JG_CUDA(c, cudaGetLastError());
     return JETGPU_OK;
@@ -1008,8 +1009,8 @@ jetgpu_status g2p_pic(Ctx* c, const GridDesc& g, long np, const double* pos,
     const FaceSet fs = face_set(g);
     if (np > 0)
         k_g2p_pic<<<blocks_for(np), kThreads, 0, c->stream>>>(
-            np, pos, vel, fs, u, v, w, g.spacing[0], g.spacing[1],
-            g.spacing[2]);
+            np, pos, vel, fs, u, v, w, make_spacing(g.spacing[0]),
+            make_spacing(g.spacing[1]), make_spacing(g.spacing[2]));
     JG_CUDA(c, cudaGetLastError());
     return JETGPU_OK;
 }

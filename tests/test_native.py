@@ -34,3 +34,4 @@ def test_lerp_fast_matches_reference_lerp(tmp_path):
     """smp::lerp_fast, the integer-pipe shortcuts of the reference's lerp
     for the fractions 0, 1/2 and 1 of grid-aligned samples."""
     run_check(tmp_path, "lerp_fast_check")
+
