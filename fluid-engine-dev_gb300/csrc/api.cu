@@ -469,6 +469,7 @@ void jetgpu_destroy(jetgpu_ctx* c) {
     release(&c->bc_cls);
     release(&c->bc_list);
     release(&c->bc_cnt);
+    release(&c->bc_nrm);
     release(&c->sdf_int);
     release(&c->sdf_dbl);
     release(&c->sdf_valid);

@@ -173,6 +173,19 @@ __global__ void k_bc_mark(FaceSet fs, int a, H3 h, ColliderDesc col,
     }
 }
 
+// sum / count for a neighbour count in 1..6, the FP64 division's bits:
+// counts 1, 2 and 4 are exact (a copy, or an exponent decrement on the
+// integer pipe); 3, 5 and 6 divide.
+static __device__ __noinline__ double div_slow(double x, double d) {
+    return x / d;
+}
+__device__ __forceinline__ double div_count(double sum, unsigned count) {
+    if (count == 1u) return sum;
+    if (count == 2u) return scale_exact(sum, -1, 0.5);
+    if (count == 4u) return scale_exact(sum, -2, 0.25);
+    return div_slow(sum, (double)count);
+}
+
 // K19b': one extrapolation pass over the listed (initially invalid) faces.
 // A face outside the list is valid by its class; a listed face is valid
 // when its state byte says so.
@@ -203,7 +216,7 @@ __global__ void k_extrapolate_list(Dims s, const int* __restrict__ lst,
         if (k + 1 < s.z && ok(c + sz)) { sum += data[c + sz]; ++count; }
         if (k > 0 && ok(c - sz)) { sum += data[c - sz]; ++count; }
         if (count > 0) {
-            data[c] = sum / (double)count;
+            data[c] = div_count(sum, count);
             st1[c] = 1;
         } else {
             st1[c] = 0;
@@ -234,7 +247,7 @@ __global__ void k_extrapolate(Dims s, double* __restrict__ data,
         if (k + 1 < s.z && v0[c + sz]) { sum += data[c + sz]; ++count; }
         if (k > 0 && v0[c - sz]) { sum += data[c - sz]; ++count; }
         if (count > 0) {
-            data[c] = sum / (double)count;
+            data[c] = div_count(sum, count);
             v1[c] = 1;
         } else {
             v1[c] = 0;
@@ -245,8 +258,9 @@ __global__ void k_extrapolate(Dims s, double* __restrict__ data,
 // ScalarGrid3::gradient at p: trilinear weights of the cell-centred sampler
 // (coordinates scaled by the inverse spacing, as getCoordinatesAndWeights
 // does) over the clamped central differences of gradient3.
-__device__ void sdf_gradient(const FieldDesc& F, const double inv[3],
-                             const double p[3], double g[3]) {
+__device__ void sdf_gradient(const FieldDesc& F, const S3& fsp,
+                             const double inv[3], const double p[3],
+                             double g[3]) {
     g[0] = g[1] = g[2] = 0.0;
     if (F.kind == 0) return;
     const Dims s{F.res[0], F.res[1], F.res[2]};
@@ -274,21 +288,53 @@ __device__ void sdf_gradient(const FieldDesc& F, const double inv[3],
         const double up = d[lin(x, y + 1 < s.y ? y + 1 : y, z, s.x, s.y)];
         const double bk = d[lin(x, y, z > 0 ? z - 1 : z, s.x, s.y)];
         const double fr = d[lin(x, y, z + 1 < s.z ? z + 1 : z, s.x, s.y)];
-        const double gx = 0.5 * (r - l) / F.spacing[0];
-        const double gy = 0.5 * (up - dn) / F.spacing[1];
-        const double gz = 0.5 * (fr - bk) / F.spacing[2];
+        const double gx = fsp.s[0].div(0.5 * (r - l));
+        const double gy = fsp.s[1].div(0.5 * (up - dn));
+        const double gz = fsp.s[2].div(0.5 * (fr - bk));
         g[0] = g[0] + w[n] * gx;
         g[1] = g[1] + w[n] * gy;
         g[2] = g[2] + w[n] * gz;
     }
 }
 
+// The collider's unit normal at face c of axis a (the SDF gradient over its
+// length, :159-163): .w = 1 with the normal, .w = 0 where the gradient
+// vanishes.
+__device__ double4_32a bc_normal(const FaceSet& fs, int a, const H3& h,
+                                 const S3& ssp, const H3& inv,
+                                 const FieldDesc& sdf, long c) {
+    int i, j, k;
+    cell_ijk(c, fs.s[a], i, j, k);
+    double p[3], g[3];
+    face_pos(fs, a, h.v, i, j, k, p);
+    sdf_gradient(sdf, ssp, inv.v, p, g);
+    if (g[0] * g[0] + g[1] * g[1] + g[2] * g[2] > 0.0) {
+        const double len = sqrt(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]);
+        return make_double4_32a(g[0] / len, g[1] / len, g[2] / len, 1.0);
+    }
+    return make_double4_32a(0.0, 0.0, 0.0, 0.0);
+}
+
+// The normals of the first `cap` listed inside faces, once per
+// classification (the collider stands still over the passes that use them).
+__global__ void k_bc_normals(FaceSet fs, int a, H3 h, S3 ssp, H3 inv,
+                             FieldDesc sdf, const int* __restrict__ lst,
+                             const unsigned* __restrict__ cnt, long cap,
+                             double4_32a* __restrict__ nrm) {
+    const long m = min((long)*cnt, cap);
+    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < m;
+         t += (long)gridDim.x * blockDim.x)
+        nrm[t] = bc_normal(fs, a, h, ssp, inv, sdf, lst[t]);
+}
+
 // K19c: the listed faces inside the collider (the others keep their
-// value); tmp[t] receives the projection of list entry t.
-__global__ void k_bc_project(FaceSet fs, int a, H3 h, S3 gsp, H3 inv,
+// value); tmp[t] receives the projection of list entry t. Entries below
+// `cap` take their normal from the classification's cache.
+__global__ void k_bc_project(FaceSet fs, int a, H3 h, S3 gsp, S3 ssp, H3 inv,
                              FieldDesc sdf, ColliderDesc col,
                              const int* __restrict__ lst,
                              const unsigned* __restrict__ cnt,
+                             const double4_32a* __restrict__ nrm, long cap,
                              const double* __restrict__ u,
                              const double* __restrict__ v,
                              const double* __restrict__ w,
@@ -303,17 +349,17 @@ __global__ void k_bc_project(FaceSet fs, int a, H3 h, S3 gsp, H3 inv,
         cell_ijk(c, s, i, j, k);
         double p[3];
         face_pos(fs, a, h.v, i, j, k, p);
-        double cv[3], fv[3], g[3];
+        double cv[3], fv[3];
         collider_vel(col, p, cv);
         for (int b = 0; b < 3; ++b)  // FaceCenteredGrid3::sample
             fv[b] = sample_face_grid(
                 vel[b], fs.s[b], gsp.s[0].div(p[0] - fs.o[b][0]),
                 gsp.s[1].div(p[1] - fs.o[b][1]),
                 gsp.s[2].div(p[2] - fs.o[b][2]));
-        sdf_gradient(sdf, inv.v, p, g);
-        if (g[0] * g[0] + g[1] * g[1] + g[2] * g[2] > 0.0) {
-            const double len = sqrt(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]);
-            const double nn[3] = {g[0] / len, g[1] / len, g[2] / len};
+        const double4_32a nq =
+            t < cap ? nrm[t] : bc_normal(fs, a, h, ssp, inv, sdf, c);
+        if (nq.w != 0.0) {
+            const double nn[3] = {nq.x, nq.y, nq.z};
             const double vr[3] = {fv[0] - cv[0], fv[1] - cv[1], fv[2] - cv[2]};
             const double dn = vr[0] * nn[0] + vr[1] * nn[1] + vr[2] * nn[2];
             double vt[3] = {vr[0] - nn[0] * dn, vr[1] - nn[1] * dn,
@@ -391,14 +437,17 @@ unsigned char* extrapolate_passes(Ctx* c, Dims s, double* data,
                                   unsigned iters) {
     for (unsigned it = 0; it < iters; ++it) {
         Prof pr(c, K_BOUNDARY, 10.0 * s.count());
-        k_extrapolate<<<blocks_for(s.count(), kThreads, c->num_sms * 8), kThreads, 0, c->stream>>>(
-            s, data, v0, v1);
+        k_extrapolate<<<blocks_for(s.count(), kThreads, c->num_sms * 8),
+                        kThreads, 0, c->stream>>>(s, data, v0, v1);
         std::swap(v0, v1);
     }
     return v0;
 }
 
 }  // namespace
+
+// Entries of the inside-face normal cache for an axis of n faces.
+static long bc_normal_cap(long n) { return (n + 7) / 8; }
 
 jetgpu_status bc_classify(Ctx* c, const GridDesc& g, const FieldDesc& sdf) {
     const FaceSet fs = face_set(g);
@@ -417,11 +466,26 @@ jetgpu_status bc_classify(Ctx* c, const GridDesc& g, const FieldDesc& sdf) {
     }
     if (!c->bc_cnt) JG_CUDA(c, cudaMalloc((void**)&c->bc_cnt, 6 * sizeof(unsigned)));
     JG_CUDA(c, cudaMemsetAsync(c->bc_cnt, 0, 6 * sizeof(unsigned), c->stream));
+    // Normal cache: up to an eighth of each axis's faces (a collider larger
+    // than that computes the rest in every pass).
+    size_t ncap = 0;
+    for (int a = 0; a < 3; ++a) ncap += (size_t)bc_normal_cap(fs.s[a].count());
+    if (c->bc_nrm_cap < ncap) {
+        JG_CUDA(c, cudaStreamSynchronize(c->stream));
+        if (c->bc_nrm) cudaFree(c->bc_nrm);
+        c->bc_nrm = nullptr;
+        c->bc_nrm_cap = 0;
+        JG_CUDA(c, cudaMalloc((void**)&c->bc_nrm, ncap * sizeof(double4_32a)));
+        c->bc_nrm_cap = ncap;
+    }
     H3 h{{g.spacing[0], g.spacing[1], g.spacing[2]}};
     S3 fsp{{make_spacing(sdf.kind == 1 ? sdf.spacing[0] : 1.0),
             make_spacing(sdf.kind == 1 ? sdf.spacing[1] : 1.0),
             make_spacing(sdf.kind == 1 ? sdf.spacing[2] : 1.0)}};
-    size_t off = 0;
+    H3 inv{{0, 0, 0}};
+    if (sdf.kind == 1)
+        for (int d = 0; d < 3; ++d) inv.v[d] = 1.0 / sdf.spacing[d];
+    size_t off = 0, noff = 0;
     for (int a = 0; a < 3; ++a) {
         const long n = fs.s[a].count();
         Prof pr(c, K_BOUNDARY, 1.0 * n);
@@ -431,7 +495,11 @@ jetgpu_status bc_classify(Ctx* c, const GridDesc& g, const FieldDesc& sdf) {
                         c->stream>>>(fs, a, h, sdf, fsp, c->bc_cls + off,
                                      c->bc_list + off, c->bc_cnt + a,
                                      c->bc_list + nf + off, c->bc_cnt + 3 + a);
+        k_bc_normals<<<c->num_sms * 8, kThreads, 0, c->stream>>>(
+            fs, a, h, fsp, inv, sdf, c->bc_list + nf + off, c->bc_cnt + 3 + a,
+            bc_normal_cap(n), c->bc_nrm + noff);
         off += n;
+        noff += (size_t)bc_normal_cap(n);
     }
     JG_CUDA(c, cudaGetLastError());
     return JETGPU_OK;
@@ -460,6 +528,9 @@ jetgpu_status bc_apply(Ctx* c, const GridDesc& g, double* u, double* v,
     H3 inv{{0, 0, 0}};
     if (sdf.kind == 1)
         for (int d = 0; d < 3; ++d) inv.v[d] = 1.0 / sdf.spacing[d];
+    S3 ssp{{make_spacing(sdf.kind == 1 ? sdf.spacing[0] : 1.0),
+            make_spacing(sdf.kind == 1 ? sdf.spacing[1] : 1.0),
+            make_spacing(sdf.kind == 1 ? sdf.spacing[2] : 1.0)}};
     double* vel[3] = {u, v, w};
     // The list passes are sized for the worst case and read their counts on
     // the device, so nothing here waits for the classification.
@@ -487,11 +558,15 @@ jetgpu_status bc_apply(Ctx* c, const GridDesc& g, double* u, double* v,
             std::swap(st0, st1);
         }
     }
+    size_t noff = 0;
     for (int a = 0; a < 3; ++a) {
         Prof pr(c, K_BOUNDARY, 0.0);
+        const long ncap = bc_normal_cap(fs.s[a].count());
         k_bc_project<<<grid, kThreads, 0, c->stream>>>(
-            fs, a, h, gsp, inv, sdf, cd, c->bc_list + nf + off[a],
-            c->bc_cnt + 3 + a, u, v, w, c->bc_tmp + off[a]);
+            fs, a, h, gsp, ssp, inv, sdf, cd, c->bc_list + nf + off[a],
+            c->bc_cnt + 3 + a, c->bc_nrm + noff, ncap, u, v, w,
+            c->bc_tmp + off[a]);
+        noff += (size_t)ncap;
     }
     for (int a = 0; a < 3; ++a) {
         Prof pr(c, K_BOUNDARY, 0.0);

@@ -171,6 +171,8 @@ struct Ctx {
     unsigned char* bc_cls = nullptr;  // face classes of the last bc_classify
     int* bc_list = nullptr;           // its invalid / inside face lists
     unsigned* bc_cnt = nullptr;       // their lengths per axis
+    size_t bc_nrm_cap = 0;            // collider normals of inside faces
+    double4_32a* bc_nrm = nullptr;
 
     // Device-resident FLIP step scratch (flip.cu): P2G markers, FLIP
     // snapshot, collider face velocities, the CFL maximum.

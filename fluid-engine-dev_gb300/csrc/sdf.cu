@@ -15,11 +15,11 @@
 // with the reference's `<= band^2`. An FP32 copy of the coordinates gives
 // the minimum squared distance to within a proven error bound (`slack`,
 // computed on the host from the grid's extent); the exact FP64 distance is
-// then formed only for the particles within that bound of the FP32 minimum
-// (one or two per cell), and the 5x5x5 window is scanned only when the 3x3x3
-// bins around the cell do not already hold a particle nearer than any
-// outside them. Bound: FP32 issue and L1 traffic over the bins, then HBM for
-// the sort.
+// then formed only for the particles whose FP32 distance is within that
+// bound of the nearest found (one or two per cell), and a bin whose lower
+// bound on the distance exceeds the nearest found is not read (inside the
+// fluid only the cell's own bin is). Bound: FP32 issue and L1 traffic over
+// the bins, then HBM for the sort.
 
 #include "ctx.h"
 #include "sampling.cuh"
@@ -39,14 +39,17 @@ struct SdfGeom {
     double band, band2, radius;
     int win[3];      // bin window half-width per axis
     float slack;     // FP32 error bound on a squared distance near the band
-    double inner2;   // (1.5 min h)^2, less a margin: the 3x3x3 bins' reach
+    Spacing sx, sy, sz;  // the spacing, for exact divisions by it
 };
 
-__device__ __forceinline__ int bin_axis(double p, double o, double h, int n) {
-    const double f = floor((p - o) / h);
-    if (!(f >= 0.0)) return 0;  // also NaN
-    if (f > (double)(n - 1)) return n - 1;
-    return (int)f;
+// floor((p - o) / h) clamped to [0, n - 1] (NaN: 0): the quotient exactly
+// (an exponent add for a power-of-two h) and the floor on the integer pipe.
+__device__ __forceinline__ int bin_axis(double p, double o, const Spacing& sp,
+                                        int n) {
+    int i;
+    double f;
+    bary_bits(sp.div(p - o), n, &i, &f);
+    return i;
 }
 
 // K21a: bin index of every particle; counts per bin.
@@ -55,9 +58,9 @@ __global__ void k_sdf_count(long np, const double* __restrict__ pos,
                             int* __restrict__ count) {
     for (long q = blockIdx.x * (long)blockDim.x + threadIdx.x; q < np;
          q += (long)gridDim.x * blockDim.x) {
-        const int bx = bin_axis(pos[3 * q], G.o[0], G.h[0], G.n.x);
-        const int by = bin_axis(pos[3 * q + 1], G.o[1], G.h[1], G.n.y);
-        const int bz = bin_axis(pos[3 * q + 2], G.o[2], G.h[2], G.n.z);
+        const int bx = bin_axis(pos[3 * q], G.o[0], G.sx, G.n.x);
+        const int by = bin_axis(pos[3 * q + 1], G.o[1], G.sy, G.n.y);
+        const int bz = bin_axis(pos[3 * q + 2], G.o[2], G.sz, G.n.z);
         const int b = bx + G.n.x * (by + G.n.y * bz);
         key[q] = b;
         atomicAdd(&count[b], 1);
@@ -163,13 +166,25 @@ __global__ void k_sdf_scatter(long np, const double* __restrict__ pos,
     }
 }
 
-// K21d: SDF at every cell centre from the particles of its window.
+// K21d: SDF at every cell centre from the particles of its window. The
+// cell's own bin is searched first; then each row of bins of the window
+// only over the bins that can still hold a nearer particle: a particle in a
+// bin m bins away along an axis is at least (m - 1/2) h from the centre
+// along it (bins are cells and the centre sits mid-cell; a particle outside
+// the grid is clamped into a boundary bin and is only farther), so a bin
+// whose squared lower bound exceeds the nearest found is skipped. Inside the
+// fluid the own bin usually holds a particle nearer than h/2 and nothing
+// else is read. An FP32 squared distance (error <= slack) screens the
+// particles; the exact FP64 distance is formed for those that can beat the
+// nearest found.
 __global__ void k_sdf_cells(SdfGeom G, const int* __restrict__ off,
                             const double* __restrict__ sp,
                             const float4* __restrict__ sf,
                             double* __restrict__ out) {
     const long N = G.n.count();
+    const float slack2 = 2.0f * G.slack;
     const float band2f = (float)G.band2;
+    const float hf[3] = {(float)G.h[0], (float)G.h[1], (float)G.h[2]};
     for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < N;
          c += (long)gridDim.x * blockDim.x) {
         int i, j, k;
@@ -179,25 +194,10 @@ __global__ void k_sdf_cells(SdfGeom G, const int* __restrict__ off,
                               G.d0[2] + G.h[2] * (double)k};
         const float cx = (float)(pt[0] - G.o[0]), cy = (float)(pt[1] - G.o[1]),
                     cz = (float)(pt[2] - G.o[2]);
-        double best = INFINITY;     // exact squared distance of the nearest
-        const int z0 = max(k - G.win[2], 0), z1 = min(k + G.win[2], G.n.z - 1);
-        const int y0 = max(j - G.win[1], 0), y1 = min(j + G.win[1], G.n.y - 1);
-        const int x0 = max(i - G.win[0], 0), x1 = min(i + G.win[0], G.n.x - 1);
-        // Two passes per region: the FP32 minimum mf of the squared
-        // distances, then the exact FP64 distance of the particles within
-        // 2 * slack of it. A particle skipped by the second pass is farther
-        // (exactly) than the one that set mf, so it cannot be the minimum,
-        // and if that one is outside the band so is it.
-        float mf = band2f;
-        auto min_f = [&](int e0, int e1) {
-            for (int e = e0; e < e1; ++e) {
-                const float4 p = sf[e];
-                const float dx = p.x - cx, dy = p.y - cy, dz = p.z - cz;
-                mf = fminf(mf, dx * dx + dy * dy + dz * dz);
-            }
-        };
-        auto exact = [&](int e0, int e1) {
-            const float thr = mf + 2.0f * G.slack;
+        double best = INFINITY;  // exact squared distance of the nearest
+        float thr = band2f + slack2;  // FP32 screen: nearer candidates pass
+        float bound = INFINITY;       // >= best: bins beyond it are skipped
+        auto scan = [&](int e0, int e1) {
             for (int e = e0; e < e1; ++e) {
                 const float4 p = sf[e];
                 const float dx = p.x - cx, dy = p.y - cy, dz = p.z - cz;
@@ -206,44 +206,49 @@ __global__ void k_sdf_cells(SdfGeom G, const int* __restrict__ off,
                 const double d0 = x[0] - pt[0], d1 = x[1] - pt[1],
                              d2 = x[2] - pt[2];
                 const double dd = d0 * d0 + d1 * d1 + d2 * d2;
-                if (dd <= G.band2 && dd < best) best = dd;
+                if (dd <= G.band2 && dd < best) {
+                    best = dd;
+                    const float bf = (float)dd * 1.0001f;
+                    bound = bf;
+                    thr = fminf(thr, bf + slack2);
+                }
             }
         };
-        // The 3x3x3 bins around the cell first. A particle in any other bin
-        // is at least 1.5 min(h) away along some axis (bins are cells, the
-        // centre sits mid-cell; clamping moves outside particles inwards
-        // only), so when the nearest found is closer than that the rest of
-        // the window cannot change the minimum.
-        const int ix0 = max(i - 1, 0), ix1 = min(i + 1, G.n.x - 1);
-        const int iy0 = max(j - 1, 0), iy1 = min(j + 1, G.n.y - 1);
-        const int iz0 = max(k - 1, 0), iz1 = min(k + 1, G.n.z - 1);
-        auto inner = [&](auto&& f) {
-            for (int bz = iz0; bz <= iz1; ++bz)
-                for (int by = iy0; by <= iy1; ++by) {
-                    const long row = (long)G.n.x * (by + (long)G.n.y * bz);
-                    f(off[row + ix0], off[row + ix1 + 1]);
-                }
+        // Squared lower bound, from below, of the distance along axis d to
+        // a bin m bins away.
+        auto lb = [&](int d, int m) {
+            const float t = ((float)m - 0.5f) * hf[d];
+            return m > 0 ? t * t * 0.9999f : 0.f;
         };
-        auto outer = [&](auto&& f) {
-            for (int bz = z0; bz <= z1; ++bz)
+        const long rowlen = G.n.x, plane = (long)G.n.x * G.n.y;
+        scan(off[c], off[c + 1]);
+        // The rows of the window: the 3 x 3 around the cell's own first.
+        const int z0 = max(k - G.win[2], 0), z1 = min(k + G.win[2], G.n.z - 1);
+        const int y0 = max(j - G.win[1], 0), y1 = min(j + G.win[1], G.n.y - 1);
+        const int x0 = max(i - G.win[0], 0), x1 = min(i + G.win[0], G.n.x - 1);
+        for (int phase = 0; phase < 2; ++phase)
+            for (int bz = z0; bz <= z1; ++bz) {
+                const int mz = abs(bz - k);
+                const float lz = lb(2, mz);
+                if (lz > bound) continue;
                 for (int by = y0; by <= y1; ++by) {
-                    const long row = (long)G.n.x * (by + (long)G.n.y * bz);
-                    if (bz >= iz0 && bz <= iz1 && by >= iy0 && by <= iy1) {
-                        if (x0 < ix0) f(off[row + x0], off[row + ix0]);
-                        if (ix1 < x1) f(off[row + ix1 + 1], off[row + x1 + 1]);
+                    const int my = abs(by - j);
+                    if ((phase == 0) != (my <= 1 && mz <= 1)) continue;
+                    const float lyz = lz + lb(1, my);
+                    if (lyz > bound) continue;
+                    // Widest x offset still within the bound.
+                    int m = 0;
+                    while (m < G.win[0] && lyz + lb(0, m + 1) <= bound) ++m;
+                    const int lo = max(x0, i - m), hi = min(x1, i + m);
+                    const long row = rowlen * by + plane * bz;
+                    if (my == 0 && mz == 0) {  // own bin already searched
+                        if (lo < i) scan(off[row + lo], off[row + i]);
+                        if (i < hi) scan(off[row + i + 1], off[row + hi + 1]);
                     } else {
-                        f(off[row + x0], off[row + x1 + 1]);
+                        scan(off[row + lo], off[row + hi + 1]);
                     }
                 }
-        };
-        inner(min_f);
-        inner(exact);
-        if (!(best < G.inner2)) {
-            // A lower mf only shrinks the threshold, so the inner particles
-            // already checked cover every inner candidate.
-            outer(min_f);
-            outer(exact);
-        }
+            }
         double minDist = G.band;
         if (best <= G.band2) {
             const double dist = sqrt(best);
@@ -255,7 +260,11 @@ __global__ void k_sdf_cells(SdfGeom G, const int* __restrict__ off,
 
 // Validity for extrapolateIntoCollider: cells whose centre is not inside the
 // collider SDF.
-__global__ void k_sdf_valid(SdfGeom G, FieldDesc col,
+struct Spacing3 {
+    Spacing s[3];
+};
+
+__global__ void k_sdf_valid(SdfGeom G, FieldDesc col, Spacing3 cs,
                             unsigned char* __restrict__ valid) {
     const long N = G.n.count();
     for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < N;
@@ -268,10 +277,9 @@ __global__ void k_sdf_valid(SdfGeom G, FieldDesc col,
             const double y = G.d0[1] + G.h[1] * (double)j;
             const double z = G.d0[2] + G.h[2] * (double)k;
             const Dims s{col.res[0], col.res[1], col.res[2]};
-            phi = sample_face_grid(col.data, s,
-                                              (x - col.origin[0]) / col.spacing[0],
-                                              (y - col.origin[1]) / col.spacing[1],
-                                              (z - col.origin[2]) / col.spacing[2]);
+            phi = sample_face_grid(col.data, s, cs.s[0].div(x - col.origin[0]),
+                                   cs.s[1].div(y - col.origin[1]),
+                                   cs.s[2].div(z - col.origin[2]));
         }
         valid[c] = phi < 0.0 ? 0 : 1;
     }
@@ -323,9 +331,9 @@ jetgpu_status build_particle_sdf(Ctx* c, const GridDesc& g, long np,
     G.band2 = G.band * G.band;
     for (int d = 0; d < 3; ++d)
         G.win[d] = (int)std::ceil(G.band / G.h[d]);
-    const double minH = std::min(std::min(G.h[0], G.h[1]), G.h[2]);
-    // The margin covers the rounding of the bin index floor((x - o) / h).
-    G.inner2 = (1.5 * minH) * (1.5 * minH) * (1.0 - 1e-9);
+    G.sx = make_spacing(G.h[0]);
+    G.sy = make_spacing(G.h[1]);
+    G.sz = make_spacing(G.h[2]);
     // FP32 error of a squared distance d^2 <= band^2 + slack between a
     // particle and a centre whose offsets from the origin are at most
     // L = extent + band: each rounded offset is off by <= u L (u = 2^-24), a
@@ -379,8 +387,10 @@ jetgpu_status build_particle_sdf(Ctx* c, const GridDesc& g, long np,
         k_sdf_cells<<<blocks_for(N, kThreads, cap), kThreads, 0, st>>>(
             G, off, sp, sf, out);
     }
+    const Spacing3 cs{{make_spacing(col.spacing[0]), make_spacing(col.spacing[1]),
+                       make_spacing(col.spacing[2])}};
     k_sdf_valid<<<blocks_for(N, kThreads, cap), kThreads, 0, st>>>(
-        G, col, c->sdf_valid);
+        G, col, cs, c->sdf_valid);
     JG_CUDA(c, cudaGetLastError());
     return extrapolate_region(c, G.n, out, c->sdf_valid,
                               (unsigned)std::ceil(max_cfl));
