@@ -183,7 +183,7 @@ __device__ __forceinline__ double div_count(double sum, unsigned count) {
     if (count == 1u) return sum;
     if (count == 2u) return scale_exact(sum, -1, 0.5);
     if (count == 4u) return scale_exact(sum, -2, 0.25);
-    return div_slow(sum, (double)count);
+    return sum == 0.0 ? sum : div_slow(sum, (double)count);
 }
 
 // K19b': one extrapolation pass over the listed (initially invalid) faces.
@@ -310,7 +310,8 @@ __device__ double4_32a bc_normal(const FaceSet& fs, int a, const H3& h,
     sdf_gradient(sdf, ssp, inv.v, p, g);
     if (g[0] * g[0] + g[1] * g[1] + g[2] * g[2] > 0.0) {
         const double len = sqrt(g[0] * g[0] + g[1] * g[1] + g[2] * g[2]);
-        return make_double4_32a(g[0] / len, g[1] / len, g[2] / len, 1.0);
+        return make_double4_32a(div_pos(g[0], len), div_pos(g[1], len),
+                                div_pos(g[2], len), 1.0);
     }
     return make_double4_32a(0.0, 0.0, 0.0, 0.0);
 }
@@ -367,8 +368,8 @@ __global__ void k_bc_project(FaceSet fs, int a, H3 h, S3 gsp, S3 ssp, H3 inv,
             const double l2 = vt[0] * vt[0] + vt[1] * vt[1] + vt[2] * vt[2];
             if (l2 > 0.0) {
                 const double veln = dmax(-dn, 0.0);
-                const double sc =
-                    dmax(1.0 - col.friction * veln / sqrt(l2), 0.0);
+                const double sc = dmax(
+                    1.0 - div_pos(col.friction * veln, sqrt(l2)), 0.0);
                 vt[0] = vt[0] * sc;
                 vt[1] = vt[1] * sc;
                 vt[2] = vt[2] * sc;

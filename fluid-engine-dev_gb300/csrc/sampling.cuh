@@ -66,6 +66,14 @@ __host__ __device__ __forceinline__ double scale_exact(double x, int k,
     return mul_slow(x, scale);
 }
 
+// x / d for a divisor known to be positive: a zero x is the quotient itself
+// (IEEE: +-0 / d = +-0 for d > 0), which keeps zero numerators off the
+// FP64 divide's special-operand path (several times the cost of a normal
+// divide on GB300).
+__host__ __device__ __forceinline__ double div_pos(double x, double d) {
+    return x == 0.0 ? x : x / d;
+}
+
 // x / h for a grid spacing h. IEEE division and multiplication both return
 // the correctly rounded exact result, and when h is a power of two x / h and
 // x * (1 / h) are the same real number (x * 2^k), so scaling the exponent

@@ -113,7 +113,7 @@ __global__ void k_p2g_normalize(double* __restrict__ g,
          c += (long)gridDim.x * blockDim.x) {
         double v = g[c];
         const double ws = wsum[c];
-        if (ws > 0.0) v /= ws;
+        if (ws > 0.0) v = div_pos(v, ws);
         g[c] = v;
         if (snap) snap[c] = (float)v;
     }
@@ -904,6 +904,7 @@ jetgpu_status p2g(Ctx* c, const GridDesc& g, long np, const double* pos,
     }
     long off = 0;
     for (int a = 0; a < 3; ++a) {
+        Prof pr(c, K_P2G, 28.0 * n[a]);
         k_p2g_normalize<<<blocks_for(n[a]), kThreads, 0, c->stream>>>(
             grid[a], wsum + off, snap[a], n[a]);
         off += n[a];
