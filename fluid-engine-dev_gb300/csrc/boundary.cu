@@ -224,33 +224,88 @@ __global__ void k_extrapolate_list(Dims s, const int* __restrict__ lst,
     }
 }
 
-// K19b: one extrapolation pass, in place on `data`.
-__global__ void k_extrapolate(Dims s, double* __restrict__ data,
-                              const unsigned char* __restrict__ v0,
-                              unsigned char* __restrict__ v1) {
+// K19b: extrapolateToRegion over its front. A pass of the reference
+// changes only the invalid entries with a valid neighbour, so each pass here
+// visits just those: an initial full pass stamps validity and lists the
+// first front, a pass updates its listed entries (the reference's
+// neighbour order and average), and the entries it made valid queue their
+// still-open neighbours for the next pass. Stamps: 0 valid at the start,
+// t + 1 made valid by pass t, kXpQueued listed for the coming pass, kXpOpen
+// neither; an entry is valid for pass t when its stamp is <= t.
+constexpr int kXpOpen = 0x7fffffff, kXpQueued = 0x7ffffffe;
+
+__global__ void k_xp_init(Dims s, const unsigned char* __restrict__ valid,
+                          int* __restrict__ stamp, int* __restrict__ lst,
+                          unsigned* __restrict__ cnt) {
     const long n = s.count();
     const long sy = s.x, sz = (long)s.x * s.y;
     for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < n;
          c += (long)gridDim.x * blockDim.x) {
-        if (v0[c]) {
-            v1[c] = 1;
-            continue;
+        bool q = false;
+        if (valid[c]) {
+            stamp[c] = 0;
+        } else {
+            int i, j, k;
+            cell_ijk(c, s, i, j, k);
+            q = (i + 1 < s.x && valid[c + 1]) || (i > 0 && valid[c - 1]) ||
+                (j + 1 < s.y && valid[c + sy]) || (j > 0 && valid[c - sy]) ||
+                (k + 1 < s.z && valid[c + sz]) || (k > 0 && valid[c - sz]);
+            stamp[c] = q ? kXpQueued : kXpOpen;
         }
+        push(lst, cnt, c, q);
+    }
+}
+
+// Pass t over its listed entries, in place on `data`: a listed entry reads
+// only neighbours valid before the pass (stamp <= t), which no thread of the
+// pass writes.
+__global__ void k_xp_pass(Dims s, double* __restrict__ data,
+                          int* __restrict__ stamp, const int* __restrict__ lst,
+                          const unsigned* __restrict__ cnt, int t) {
+    const long m = *cnt;
+    const long sy = s.x, sz = (long)s.x * s.y;
+    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < m;
+         e += (long)gridDim.x * blockDim.x) {
+        const long c = lst[e];
         int i, j, k;
         cell_ijk(c, s, i, j, k);
+        auto ok = [&](long q) { return stamp[q] <= t; };
         double sum = 0.0;
         unsigned count = 0;
-        if (i + 1 < s.x && v0[c + 1]) { sum += data[c + 1]; ++count; }
-        if (i > 0 && v0[c - 1]) { sum += data[c - 1]; ++count; }
-        if (j + 1 < s.y && v0[c + sy]) { sum += data[c + sy]; ++count; }
-        if (j > 0 && v0[c - sy]) { sum += data[c - sy]; ++count; }
-        if (k + 1 < s.z && v0[c + sz]) { sum += data[c + sz]; ++count; }
-        if (k > 0 && v0[c - sz]) { sum += data[c - sz]; ++count; }
-        if (count > 0) {
-            data[c] = div_count(sum, count);
-            v1[c] = 1;
-        } else {
-            v1[c] = 0;
+        if (i + 1 < s.x && ok(c + 1)) { sum += data[c + 1]; ++count; }
+        if (i > 0 && ok(c - 1)) { sum += data[c - 1]; ++count; }
+        if (j + 1 < s.y && ok(c + sy)) { sum += data[c + sy]; ++count; }
+        if (j > 0 && ok(c - sy)) { sum += data[c - sy]; ++count; }
+        if (k + 1 < s.z && ok(c + sz)) { sum += data[c + sz]; ++count; }
+        if (k > 0 && ok(c - sz)) { sum += data[c - sz]; ++count; }
+        if (count > 0) data[c] = div_count(sum, count);
+        stamp[c] = t + 1;
+    }
+}
+
+// The next front: the open neighbours of the entries pass t made valid,
+// each listed once (the stamp's compare-and-swap claims it).
+__global__ void k_xp_next(Dims s, int* __restrict__ stamp,
+                          const int* __restrict__ lst,
+                          const unsigned* __restrict__ cnt,
+                          int* __restrict__ nlst, unsigned* __restrict__ ncnt) {
+    const long m = *cnt;
+    const long sy = s.x, sz = (long)s.x * s.y;
+    for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < m;
+         e += (long)gridDim.x * blockDim.x) {
+        const long c = lst[e];
+        int i, j, k;
+        cell_ijk(c, s, i, j, k);
+        const bool in[6] = {i + 1 < s.x, i > 0, j + 1 < s.y,
+                            j > 0,       k + 1 < s.z, k > 0};
+        const long d[6] = {1, -1, sy, -sy, sz, -sz};
+#pragma unroll
+        for (int q = 0; q < 6; ++q) {
+            const long nb = c + d[q];
+            const bool take = in[q] && stamp[nb] == kXpOpen &&
+                              atomicCAS(&stamp[nb], kXpOpen, kXpQueued) ==
+                                  kXpOpen;
+            push(nlst, ncnt, nb, take);
         }
     }
 }
@@ -429,20 +484,6 @@ jetgpu_status bc_scratch(Ctx* c, size_t n) {
     JG_CUDA(c, cudaMalloc((void**)&c->bc_valid, 2 * n));
     c->bc_cap = n;
     return JETGPU_OK;
-}
-
-// `iters` passes on one array whose validity starts in v0; returns the
-// plane that holds the final validity.
-unsigned char* extrapolate_passes(Ctx* c, Dims s, double* data,
-                                  unsigned char* v0, unsigned char* v1,
-                                  unsigned iters) {
-    for (unsigned it = 0; it < iters; ++it) {
-        Prof pr(c, K_BOUNDARY, 10.0 * s.count());
-        k_extrapolate<<<blocks_for(s.count(), kThreads, c->num_sms * 8),
-                        kThreads, 0, c->stream>>>(s, data, v0, v1);
-        std::swap(v0, v1);
-    }
-    return v0;
 }
 
 }  // namespace
@@ -668,14 +709,38 @@ jetgpu_status constrain_velocity(Ctx* c, const GridDesc& g, double* u,
 
 jetgpu_status extrapolate_region(Ctx* c, Dims s, double* data,
                                  const unsigned char* valid, unsigned iters) {
-    const size_t n = (size_t)s.count();
-    if (jetgpu_status st = bc_scratch(c, n)) return st;
-    // The caller's validity stays untouched: passes ping-pong in scratch.
-    unsigned char* v0 = c->bc_valid;
-    unsigned char* v1 = c->bc_valid + n;
-    JG_CUDA(c, cudaMemcpyAsync(v0, valid, n, cudaMemcpyDeviceToDevice,
-                               c->stream));
-    extrapolate_passes(c, s, data, v0, v1, iters);
+    if (iters == 0) return JETGPU_OK;
+    const long n = s.count();
+    // Stamps and two front lists (n ints each), two front lengths. The
+    // caller's validity stays untouched.
+    if (c->xp_cap < (size_t)n) {
+        JG_CUDA(c, cudaStreamSynchronize(c->stream));
+        if (c->xp_int) cudaFree(c->xp_int);
+        c->xp_int = nullptr;
+        c->xp_cap = 0;
+        JG_CUDA(c, cudaMalloc((void**)&c->xp_int, 3 * (size_t)n * sizeof(int)));
+        c->xp_cap = (size_t)n;
+    }
+    if (!c->xp_cnt) JG_CUDA(c, cudaMalloc((void**)&c->xp_cnt, 2 * sizeof(unsigned)));
+    int* stamp = c->xp_int;
+    int* lst[2] = {stamp + n, stamp + 2 * n};
+    unsigned* cnt = c->xp_cnt;
+    const int grid = c->num_sms * 8;
+    Prof pr(c, K_BOUNDARY, 5.0 * n);
+    JG_CUDA(c, cudaMemsetAsync(cnt, 0, 2 * sizeof(unsigned), c->stream));
+    k_xp_init<<<blocks_for(n, kThreads, grid), kThreads, 0, c->stream>>>(
+        s, valid, stamp, lst[0], cnt);
+    for (unsigned t = 0; t < iters; ++t) {
+        const int cur = t & 1, nxt = cur ^ 1;
+        k_xp_pass<<<grid, kThreads, 0, c->stream>>>(s, data, stamp, lst[cur],
+                                                    cnt + cur, (int)t);
+        if (t + 1 < iters) {
+            JG_CUDA(c, cudaMemsetAsync(cnt + nxt, 0, sizeof(unsigned),
+                                       c->stream));
+            k_xp_next<<<grid, kThreads, 0, c->stream>>>(
+                s, stamp, lst[cur], cnt + cur, lst[nxt], cnt + nxt);
+        }
+    }
     JG_CUDA(c, cudaGetLastError());
     return JETGPU_OK;
 }

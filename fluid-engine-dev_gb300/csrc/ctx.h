@@ -173,6 +173,11 @@ struct Ctx {
     unsigned* bc_cnt = nullptr;       // their lengths per axis
     size_t bc_nrm_cap = 0;            // collider normals of inside faces
     double4_32a* bc_nrm = nullptr;
+    // extrapolate_region: stamps and two front lists (xp_cap entries each),
+    // the two front lengths.
+    size_t xp_cap = 0;
+    int* xp_int = nullptr;
+    unsigned* xp_cnt = nullptr;
 
     // Device-resident FLIP step scratch (flip.cu): P2G markers, FLIP
     // snapshot, collider face velocities, the CFL maximum.
