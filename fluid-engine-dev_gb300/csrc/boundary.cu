@@ -101,6 +101,15 @@ struct H3 {
 // the collider stands still (all calls of a sub-step).
 enum : unsigned char { kFaceValid = 1, kFaceInside = 2 };
 
+// The three face arrays of one launch (blockIdx.y = axis): each axis's
+// offset in the concatenated per-face buffers (classes, lists, validity,
+// temporaries), its velocity array, and its slice of the normal cache.
+struct Axes3 {
+    long off[3];
+    double* vel[3];
+    long noff[3], ncap[3];
+};
+
 // Appends face c to a list when `take`; one atomic per warp.
 __device__ __forceinline__ void push(int* __restrict__ lst,
                                      unsigned* __restrict__ cnt, long c,
@@ -120,13 +129,18 @@ __device__ __forceinline__ void push(int* __restrict__ lst,
 // those without a valid fraction (collider velocity, then extrapolated) and
 // those inside the collider (projected). List order is arbitrary; every
 // pass over a list is order-independent.
-__global__ void k_bc_classify(FaceSet fs, int a, H3 h, FieldDesc sdf, S3 fsp,
-                              unsigned char* __restrict__ cls,
-                              int* __restrict__ inv_list,
-                              unsigned* __restrict__ inv_cnt,
-                              int* __restrict__ in_list,
-                              unsigned* __restrict__ in_cnt) {
+__global__ void k_bc_classify(FaceSet fs, H3 h, FieldDesc sdf, S3 fsp,
+                              Axes3 ax, long nf,
+                              unsigned char* __restrict__ cls_all,
+                              int* __restrict__ list_all,
+                              unsigned* __restrict__ cnt_all) {
+    const int a = blockIdx.y;
     const Dims s = fs.s[a];
+    unsigned char* cls = cls_all + ax.off[a];
+    int* inv_list = list_all + ax.off[a];
+    unsigned* inv_cnt = cnt_all + a;
+    int* in_list = list_all + nf + ax.off[a];
+    unsigned* in_cnt = cnt_all + 3 + a;
     const long n = s.count();
     for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < n;
          c += (long)gridDim.x * blockDim.x) {
@@ -153,12 +167,16 @@ __global__ void k_bc_classify(FaceSet fs, int a, H3 h, FieldDesc sdf, S3 fsp,
 
 // K19a': the faces without a valid fraction take the collider velocity
 // (:63-67) and start the extrapolation invalid.
-__global__ void k_bc_mark(FaceSet fs, int a, H3 h, ColliderDesc col,
-                          const int* __restrict__ lst,
-                          const unsigned* __restrict__ cnt,
-                          double* __restrict__ vel,
-                          unsigned char* __restrict__ st0) {
+__global__ void k_bc_mark(FaceSet fs, H3 h, ColliderDesc col, Axes3 ax,
+                          const int* __restrict__ list_all,
+                          const unsigned* __restrict__ cnt_all,
+                          unsigned char* __restrict__ st0_all) {
+    const int a = blockIdx.y;
     const Dims s = fs.s[a];
+    const int* lst = list_all + ax.off[a];
+    const unsigned* cnt = cnt_all + a;
+    double* vel = ax.vel[a];
+    unsigned char* st0 = st0_all + ax.off[a];
     const long m = *cnt;
     for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < m;
          t += (long)gridDim.x * blockDim.x) {
@@ -189,13 +207,20 @@ __device__ __forceinline__ double div_count(double sum, unsigned count) {
 // K19b': one extrapolation pass over the listed (initially invalid) faces.
 // A face outside the list is valid by its class; a listed face is valid
 // when its state byte says so.
-__global__ void k_extrapolate_list(Dims s, const int* __restrict__ lst,
-                                   const unsigned* __restrict__ cnt,
-                                   double* __restrict__ data,
-                                   const unsigned char* __restrict__ cls,
-                                   const unsigned char* __restrict__ st0,
-                                   unsigned char* __restrict__ st1) {
-    const long m = *cnt;
+__global__ void k_extrapolate_list(FaceSet fs, Axes3 ax,
+                                   const int* __restrict__ list_all,
+                                   const unsigned* __restrict__ cnt_all,
+                                   const unsigned char* __restrict__ cls_all,
+                                   const unsigned char* __restrict__ st0_all,
+                                   unsigned char* __restrict__ st1_all) {
+    const int a = blockIdx.y;
+    const Dims s = fs.s[a];
+    const int* lst = list_all + ax.off[a];
+    const long m = cnt_all[a];
+    double* data = ax.vel[a];
+    const unsigned char* cls = cls_all + ax.off[a];
+    const unsigned char* st0 = st0_all + ax.off[a];
+    unsigned char* st1 = st1_all + ax.off[a];
     const long sy = s.x, sz = (long)s.x * s.y;
     for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < m;
          t += (long)gridDim.x * blockDim.x) {
@@ -234,9 +259,24 @@ __global__ void k_extrapolate_list(Dims s, const int* __restrict__ lst,
 // neither; an entry is valid for pass t when its stamp is <= t.
 constexpr int kXpOpen = 0x7fffffff, kXpQueued = 0x7ffffffe;
 
-__global__ void k_xp_init(Dims s, const unsigned char* __restrict__ valid,
-                          int* __restrict__ stamp, int* __restrict__ lst,
-                          unsigned* __restrict__ cnt) {
+// Up to three arrays extrapolated together (blockIdx.y = array): extents,
+// data, validity, and offsets into the shared stamp and list buffers.
+struct Xp3 {
+    Dims s[3];
+    double* data[3];
+    const unsigned char* valid[3];
+    long off[3];
+};
+
+__global__ void k_xp_init(Xp3 X, int* __restrict__ stamp_all,
+                          int* __restrict__ lst_all,
+                          unsigned* __restrict__ cnt_all) {
+    const int r = blockIdx.y;
+    const Dims s = X.s[r];
+    const unsigned char* valid = X.valid[r];
+    int* stamp = stamp_all + X.off[r];
+    int* lst = lst_all + X.off[r];
+    unsigned* cnt = cnt_all + r;
     const long n = s.count();
     const long sy = s.x, sz = (long)s.x * s.y;
     for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < n;
@@ -256,13 +296,18 @@ __global__ void k_xp_init(Dims s, const unsigned char* __restrict__ valid,
     }
 }
 
-// Pass t over its listed entries, in place on `data`: a listed entry reads
+// Pass t over its listed entries, in place on the data: a listed entry reads
 // only neighbours valid before the pass (stamp <= t), which no thread of the
 // pass writes.
-__global__ void k_xp_pass(Dims s, double* __restrict__ data,
-                          int* __restrict__ stamp, const int* __restrict__ lst,
-                          const unsigned* __restrict__ cnt, int t) {
-    const long m = *cnt;
+__global__ void k_xp_pass(Xp3 X, int* __restrict__ stamp_all,
+                          const int* __restrict__ lst_all,
+                          const unsigned* __restrict__ cnt_all, int t) {
+    const int r = blockIdx.y;
+    const Dims s = X.s[r];
+    double* data = X.data[r];
+    int* stamp = stamp_all + X.off[r];
+    const int* lst = lst_all + X.off[r];
+    const long m = cnt_all[r];
     const long sy = s.x, sz = (long)s.x * s.y;
     for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < m;
          e += (long)gridDim.x * blockDim.x) {
@@ -285,11 +330,18 @@ __global__ void k_xp_pass(Dims s, double* __restrict__ data,
 
 // The next front: the open neighbours of the entries pass t made valid,
 // each listed once (the stamp's compare-and-swap claims it).
-__global__ void k_xp_next(Dims s, int* __restrict__ stamp,
-                          const int* __restrict__ lst,
-                          const unsigned* __restrict__ cnt,
-                          int* __restrict__ nlst, unsigned* __restrict__ ncnt) {
-    const long m = *cnt;
+__global__ void k_xp_next(Xp3 X, int* __restrict__ stamp_all,
+                          const int* __restrict__ lst_all,
+                          const unsigned* __restrict__ cnt_all,
+                          int* __restrict__ nlst_all,
+                          unsigned* __restrict__ ncnt_all) {
+    const int r = blockIdx.y;
+    const Dims s = X.s[r];
+    int* stamp = stamp_all + X.off[r];
+    const int* lst = lst_all + X.off[r];
+    const long m = cnt_all[r];
+    int* nlst = nlst_all + X.off[r];
+    unsigned* ncnt = ncnt_all + r;
     const long sy = s.x, sz = (long)s.x * s.y;
     for (long e = blockIdx.x * (long)blockDim.x + threadIdx.x; e < m;
          e += (long)gridDim.x * blockDim.x) {
@@ -373,11 +425,14 @@ __device__ double4_32a bc_normal(const FaceSet& fs, int a, const H3& h,
 
 // The normals of the first `cap` listed inside faces, once per
 // classification (the collider stands still over the passes that use them).
-__global__ void k_bc_normals(FaceSet fs, int a, H3 h, S3 ssp, H3 inv,
-                             FieldDesc sdf, const int* __restrict__ lst,
-                             const unsigned* __restrict__ cnt, long cap,
-                             double4_32a* __restrict__ nrm) {
-    const long m = min((long)*cnt, cap);
+__global__ void k_bc_normals(FaceSet fs, H3 h, S3 ssp, H3 inv, FieldDesc sdf,
+                             Axes3 ax, long nf, const int* __restrict__ list_all,
+                             const unsigned* __restrict__ cnt_all,
+                             double4_32a* __restrict__ nrm_all) {
+    const int a = blockIdx.y;
+    const int* lst = list_all + nf + ax.off[a];
+    double4_32a* nrm = nrm_all + ax.noff[a];
+    const long m = min((long)cnt_all[3 + a], ax.ncap[a]);
     for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < m;
          t += (long)gridDim.x * blockDim.x)
         nrm[t] = bc_normal(fs, a, h, ssp, inv, sdf, lst[t]);
@@ -386,18 +441,20 @@ __global__ void k_bc_normals(FaceSet fs, int a, H3 h, S3 ssp, H3 inv,
 // K19c: the listed faces inside the collider (the others keep their
 // value); tmp[t] receives the projection of list entry t. Entries below
 // `cap` take their normal from the classification's cache.
-__global__ void k_bc_project(FaceSet fs, int a, H3 h, S3 gsp, S3 ssp, H3 inv,
-                             FieldDesc sdf, ColliderDesc col,
-                             const int* __restrict__ lst,
-                             const unsigned* __restrict__ cnt,
-                             const double4_32a* __restrict__ nrm, long cap,
-                             const double* __restrict__ u,
-                             const double* __restrict__ v,
-                             const double* __restrict__ w,
-                             double* __restrict__ tmp) {
+__global__ void k_bc_project(FaceSet fs, H3 h, S3 gsp, S3 ssp, H3 inv,
+                             FieldDesc sdf, ColliderDesc col, Axes3 ax, long nf,
+                             const int* __restrict__ list_all,
+                             const unsigned* __restrict__ cnt_all,
+                             const double4_32a* __restrict__ nrm_all,
+                             double* __restrict__ tmp_all) {
+    const int a = blockIdx.y;
     const Dims s = fs.s[a];
-    const long m = *cnt;
-    const double* vel[3] = {u, v, w};
+    const int* lst = list_all + nf + ax.off[a];
+    const long m = cnt_all[3 + a];
+    const double4_32a* nrm = nrm_all + ax.noff[a];
+    const long cap = ax.ncap[a];
+    double* tmp = tmp_all + ax.off[a];
+    const double* vel[3] = {ax.vel[0], ax.vel[1], ax.vel[2]};
     for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < m;
          t += (long)gridDim.x * blockDim.x) {
         const long c = lst[t];
@@ -437,20 +494,28 @@ __global__ void k_bc_project(FaceSet fs, int a, H3 h, S3 gsp, S3 ssp, H3 inv,
 }
 
 // K19d: the projected faces from the temporary (:177-187) ...
-__global__ void k_bc_store(const int* __restrict__ lst,
-                           const unsigned* __restrict__ cnt,
-                           const double* __restrict__ tmp,
-                           double* __restrict__ vel) {
-    const long m = *cnt;
+__global__ void k_bc_store(Axes3 ax, long nf, const int* __restrict__ list_all,
+                           const unsigned* __restrict__ cnt_all,
+                           const double* __restrict__ tmp_all) {
+    const int a = blockIdx.y;
+    const int* lst = list_all + nf + ax.off[a];
+    const long m = cnt_all[3 + a];
+    const double* tmp = tmp_all + ax.off[a];
+    double* vel = ax.vel[a];
     for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < m;
          t += (long)gridDim.x * blockDim.x)
         vel[lst[t]] = tmp[t];
 }
 
 // ... then zero on the closed domain walls (:189-232): the two planes of
-// axis a, plane 0 when `lo`, the last when `hi`.
-__global__ void k_bc_walls(Dims s, int a, int lo, int hi,
-                           double* __restrict__ vel) {
+// axis a = blockIdx.y, plane 0 when its low wall is closed, the last when
+// its high wall is.
+__global__ void k_bc_walls(FaceSet fs, Axes3 ax, int closed) {
+    const int a = blockIdx.y;
+    const Dims s = fs.s[a];
+    const int lo = closed & (1 << (2 * a)), hi = closed & (1 << (2 * a + 1));
+    if (!lo && !hi) return;
+    double* vel = ax.vel[a];
     const int d1 = a == 0 ? s.y : s.x;            // the plane's two extents
     const int d2 = a == 2 ? s.y : s.z;
     const int ext = a == 0 ? s.x : (a == 1 ? s.y : s.z);
@@ -491,10 +556,34 @@ jetgpu_status bc_scratch(Ctx* c, size_t n) {
 // Entries of the inside-face normal cache for an axis of n faces.
 static long bc_normal_cap(long n) { return (n + 7) / 8; }
 
+// Offsets of the three axes in the concatenated face buffers and in the
+// normal cache; the total face count.
+static size_t bc_axes(const FaceSet& fs, double* u, double* v, double* w,
+                      Axes3* ax) {
+    size_t o = 0, no = 0;
+    for (int a = 0; a < 3; ++a) {
+        const long n = fs.s[a].count();
+        ax->off[a] = (long)o;
+        ax->noff[a] = (long)no;
+        ax->ncap[a] = bc_normal_cap(n);
+        o += (size_t)n;
+        no += (size_t)bc_normal_cap(n);
+    }
+    ax->vel[0] = u;
+    ax->vel[1] = v;
+    ax->vel[2] = w;
+    return o;
+}
+
+// Grid of a launch over up to `n` entries per axis, one y row per axis.
+static dim3 bc_grid(const Ctx* c, long n) {
+    return dim3((unsigned)blocks_for(n, kThreads, c->num_sms * 4), 3);
+}
+
 jetgpu_status bc_classify(Ctx* c, const GridDesc& g, const FieldDesc& sdf) {
     const FaceSet fs = face_set(g);
-    size_t nf = 0;
-    for (int a = 0; a < 3; ++a) nf += (size_t)fs.s[a].count();
+    Axes3 ax;
+    const size_t nf = bc_axes(fs, nullptr, nullptr, nullptr, &ax);
     if (c->bc_cls_cap < nf) {
         JG_CUDA(c, cudaStreamSynchronize(c->stream));
         if (c->bc_cls) cudaFree(c->bc_cls);
@@ -510,8 +599,7 @@ jetgpu_status bc_classify(Ctx* c, const GridDesc& g, const FieldDesc& sdf) {
     JG_CUDA(c, cudaMemsetAsync(c->bc_cnt, 0, 6 * sizeof(unsigned), c->stream));
     // Normal cache: up to an eighth of each axis's faces (a collider larger
     // than that computes the rest in every pass).
-    size_t ncap = 0;
-    for (int a = 0; a < 3; ++a) ncap += (size_t)bc_normal_cap(fs.s[a].count());
+    const size_t ncap = (size_t)(ax.noff[2] + ax.ncap[2]);
     if (c->bc_nrm_cap < ncap) {
         JG_CUDA(c, cudaStreamSynchronize(c->stream));
         if (c->bc_nrm) cudaFree(c->bc_nrm);
@@ -527,22 +615,15 @@ jetgpu_status bc_classify(Ctx* c, const GridDesc& g, const FieldDesc& sdf) {
     H3 inv{{0, 0, 0}};
     if (sdf.kind == 1)
         for (int d = 0; d < 3; ++d) inv.v[d] = 1.0 / sdf.spacing[d];
-    size_t off = 0, noff = 0;
-    for (int a = 0; a < 3; ++a) {
-        const long n = fs.s[a].count();
-        Prof pr(c, K_BOUNDARY, 1.0 * n);
-        // Lists: invalid faces of axis a at bc_list + off, inside faces at
-        // bc_list + nf + off; counts bc_cnt[a], bc_cnt[3 + a].
-        k_bc_classify<<<blocks_for(n, kThreads, c->num_sms * 8), kThreads, 0,
-                        c->stream>>>(fs, a, h, sdf, fsp, c->bc_cls + off,
-                                     c->bc_list + off, c->bc_cnt + a,
-                                     c->bc_list + nf + off, c->bc_cnt + 3 + a);
-        k_bc_normals<<<c->num_sms * 8, kThreads, 0, c->stream>>>(
-            fs, a, h, fsp, inv, sdf, c->bc_list + nf + off, c->bc_cnt + 3 + a,
-            bc_normal_cap(n), c->bc_nrm + noff);
-        off += n;
-        noff += (size_t)bc_normal_cap(n);
-    }
+    long nmax = 0;
+    for (int a = 0; a < 3; ++a) nmax = std::max(nmax, fs.s[a].count());
+    Prof pr(c, K_BOUNDARY, 1.0 * (double)nf);
+    // Lists: invalid faces of axis a at bc_list + off[a], inside faces at
+    // bc_list + nf + off[a]; counts bc_cnt[a], bc_cnt[3 + a].
+    k_bc_classify<<<bc_grid(c, nmax), kThreads, 0, c->stream>>>(
+        fs, h, sdf, fsp, ax, (long)nf, c->bc_cls, c->bc_list, c->bc_cnt);
+    k_bc_normals<<<bc_grid(c, nmax / 8), kThreads, 0, c->stream>>>(
+        fs, h, fsp, inv, sdf, ax, (long)nf, c->bc_list, c->bc_cnt, c->bc_nrm);
     JG_CUDA(c, cudaGetLastError());
     return JETGPU_OK;
 }
@@ -551,8 +632,8 @@ jetgpu_status bc_apply(Ctx* c, const GridDesc& g, double* u, double* v,
                        double* w, const FieldDesc& sdf,
                        const jetgpu_collider* col, int closed, unsigned depth) {
     const FaceSet fs = face_set(g);
-    size_t nf = 0;
-    for (int a = 0; a < 3; ++a) nf += (size_t)fs.s[a].count();
+    Axes3 ax;
+    const size_t nf = bc_axes(fs, u, v, w, &ax);
     if (jetgpu_status s = bc_scratch(c, nf)) return s;
     ColliderDesc cd{};
     if (col) {
@@ -573,56 +654,36 @@ jetgpu_status bc_apply(Ctx* c, const GridDesc& g, double* u, double* v,
     S3 ssp{{make_spacing(sdf.kind == 1 ? sdf.spacing[0] : 1.0),
             make_spacing(sdf.kind == 1 ? sdf.spacing[1] : 1.0),
             make_spacing(sdf.kind == 1 ? sdf.spacing[2] : 1.0)}};
-    double* vel[3] = {u, v, w};
     // The list passes are sized for the worst case and read their counts on
-    // the device, so nothing here waits for the classification.
-    const int grid = c->num_sms * 8;
-    size_t off[3], o = 0;
-    for (int a = 0; a < 3; ++a) {
-        off[a] = o;
-        o += (size_t)fs.s[a].count();
+    // the device, so nothing here waits for the classification. One launch
+    // per step covers the three axes (blockIdx.y).
+    long nmax = 0;
+    for (int a = 0; a < 3; ++a) nmax = std::max(nmax, fs.s[a].count());
+    const dim3 grid = bc_grid(c, nmax);
+    Prof pr(c, K_BOUNDARY, 0.0);
+    unsigned char* st0 = c->bc_valid;
+    unsigned char* st1 = c->bc_valid + nf;
+    k_bc_mark<<<grid, kThreads, 0, c->stream>>>(fs, h, cd, ax, c->bc_list,
+                                                c->bc_cnt, st0);
+    for (unsigned it = 0; it < depth; ++it) {
+        k_extrapolate_list<<<grid, kThreads, 0, c->stream>>>(
+            fs, ax, c->bc_list, c->bc_cnt, c->bc_cls, st0, st1);
+        std::swap(st0, st1);
     }
-    for (int a = 0; a < 3; ++a) {
-        const int* inv_list = c->bc_list + off[a];
-        const unsigned* inv_cnt = c->bc_cnt + a;
-        const unsigned char* cls = c->bc_cls + off[a];
-        unsigned char* st0 = c->bc_valid + off[a];
-        unsigned char* st1 = c->bc_valid + nf + off[a];
-        {
-            Prof pr(c, K_BOUNDARY, 0.0);
-            k_bc_mark<<<grid, kThreads, 0, c->stream>>>(fs, a, h, cd, inv_list,
-                                                        inv_cnt, vel[a], st0);
-        }
-        for (unsigned it = 0; it < depth; ++it) {
-            Prof pr(c, K_BOUNDARY, 0.0);
-            k_extrapolate_list<<<grid, kThreads, 0, c->stream>>>(
-                fs.s[a], inv_list, inv_cnt, vel[a], cls, st0, st1);
-            std::swap(st0, st1);
-        }
-    }
-    size_t noff = 0;
-    for (int a = 0; a < 3; ++a) {
-        Prof pr(c, K_BOUNDARY, 0.0);
-        const long ncap = bc_normal_cap(fs.s[a].count());
-        k_bc_project<<<grid, kThreads, 0, c->stream>>>(
-            fs, a, h, gsp, ssp, inv, sdf, cd, c->bc_list + nf + off[a],
-            c->bc_cnt + 3 + a, c->bc_nrm + noff, ncap, u, v, w,
-            c->bc_tmp + off[a]);
-        noff += (size_t)ncap;
-    }
-    for (int a = 0; a < 3; ++a) {
-        Prof pr(c, K_BOUNDARY, 0.0);
-        k_bc_store<<<grid, kThreads, 0, c->stream>>>(
-            c->bc_list + nf + off[a], c->bc_cnt + 3 + a, c->bc_tmp + off[a],
-            vel[a]);
-        const int lo = closed & (1 << (2 * a)), hi = closed & (1 << (2 * a + 1));
-        if (lo || hi) {
+    k_bc_project<<<grid, kThreads, 0, c->stream>>>(
+        fs, h, gsp, ssp, inv, sdf, cd, ax, (long)nf, c->bc_list, c->bc_cnt,
+        c->bc_nrm, c->bc_tmp);
+    k_bc_store<<<grid, kThreads, 0, c->stream>>>(ax, (long)nf, c->bc_list,
+                                                 c->bc_cnt, c->bc_tmp);
+    if (closed) {
+        long P = 0;  // the largest wall plane
+        for (int a = 0; a < 3; ++a) {
             const Dims s = fs.s[a];
-            const long P = a == 0 ? (long)s.y * s.z
-                                  : (a == 1 ? (long)s.x * s.z : (long)s.x * s.y);
-            k_bc_walls<<<blocks_for(2 * P, kThreads, c->num_sms * 8), kThreads,
-                         0, c->stream>>>(s, a, lo, hi, vel[a]);
+            P = std::max(P, a == 0 ? (long)s.y * s.z
+                                   : (a == 1 ? (long)s.x * s.z : (long)s.x * s.y));
         }
+        k_bc_walls<<<bc_grid(c, 2 * P), kThreads, 0, c->stream>>>(fs, ax,
+                                                                  closed);
     }
     JG_CUDA(c, cudaGetLastError());
     return JETGPU_OK;
@@ -707,42 +768,59 @@ jetgpu_status constrain_velocity(Ctx* c, const GridDesc& g, double* u,
     return bc_apply(c, g, u, v, w, sdf, col, closed, depth);
 }
 
-jetgpu_status extrapolate_region(Ctx* c, Dims s, double* data,
-                                 const unsigned char* valid, unsigned iters) {
-    if (iters == 0) return JETGPU_OK;
-    const long n = s.count();
-    // Stamps and two front lists (n ints each), two front lengths. The
-    // caller's validity stays untouched.
-    if (c->xp_cap < (size_t)n) {
+jetgpu_status extrapolate_regions(Ctx* c, int na, const Dims* s,
+                                  double* const* data,
+                                  const unsigned char* const* valid,
+                                  unsigned iters) {
+    if (iters == 0 || na <= 0) return JETGPU_OK;
+    Xp3 X{};
+    long tot = 0, nmax = 0;
+    for (int r = 0; r < na; ++r) {
+        X.s[r] = s[r];
+        X.data[r] = data[r];
+        X.valid[r] = valid[r];
+        X.off[r] = tot;
+        tot += s[r].count();
+        nmax = std::max(nmax, s[r].count());
+    }
+    // Stamps and two front lists (tot ints each), two front lengths per
+    // array. The callers' validity stays untouched.
+    if (c->xp_cap < (size_t)tot) {
         JG_CUDA(c, cudaStreamSynchronize(c->stream));
         if (c->xp_int) cudaFree(c->xp_int);
         c->xp_int = nullptr;
         c->xp_cap = 0;
-        JG_CUDA(c, cudaMalloc((void**)&c->xp_int, 3 * (size_t)n * sizeof(int)));
-        c->xp_cap = (size_t)n;
+        JG_CUDA(c, cudaMalloc((void**)&c->xp_int, 3 * (size_t)tot * sizeof(int)));
+        c->xp_cap = (size_t)tot;
     }
-    if (!c->xp_cnt) JG_CUDA(c, cudaMalloc((void**)&c->xp_cnt, 2 * sizeof(unsigned)));
+    if (!c->xp_cnt) JG_CUDA(c, cudaMalloc((void**)&c->xp_cnt, 6 * sizeof(unsigned)));
     int* stamp = c->xp_int;
-    int* lst[2] = {stamp + n, stamp + 2 * n};
-    unsigned* cnt = c->xp_cnt;
-    const int grid = c->num_sms * 8;
-    Prof pr(c, K_BOUNDARY, 5.0 * n);
-    JG_CUDA(c, cudaMemsetAsync(cnt, 0, 2 * sizeof(unsigned), c->stream));
-    k_xp_init<<<blocks_for(n, kThreads, grid), kThreads, 0, c->stream>>>(
-        s, valid, stamp, lst[0], cnt);
+    int* lst[2] = {stamp + tot, stamp + 2 * tot};
+    unsigned* cnt[2] = {c->xp_cnt, c->xp_cnt + 3};
+    const dim3 full((unsigned)blocks_for(nmax, kThreads, c->num_sms * 8),
+                    (unsigned)na);
+    const dim3 grid((unsigned)(c->num_sms * 4), (unsigned)na);
+    Prof pr(c, K_BOUNDARY, 5.0 * (double)tot);
+    JG_CUDA(c, cudaMemsetAsync(c->xp_cnt, 0, 6 * sizeof(unsigned), c->stream));
+    k_xp_init<<<full, kThreads, 0, c->stream>>>(X, stamp, lst[0], cnt[0]);
     for (unsigned t = 0; t < iters; ++t) {
         const int cur = t & 1, nxt = cur ^ 1;
-        k_xp_pass<<<grid, kThreads, 0, c->stream>>>(s, data, stamp, lst[cur],
-                                                    cnt + cur, (int)t);
+        k_xp_pass<<<grid, kThreads, 0, c->stream>>>(X, stamp, lst[cur],
+                                                    cnt[cur], (int)t);
         if (t + 1 < iters) {
-            JG_CUDA(c, cudaMemsetAsync(cnt + nxt, 0, sizeof(unsigned),
+            JG_CUDA(c, cudaMemsetAsync(cnt[nxt], 0, 3 * sizeof(unsigned),
                                        c->stream));
             k_xp_next<<<grid, kThreads, 0, c->stream>>>(
-                s, stamp, lst[cur], cnt + cur, lst[nxt], cnt + nxt);
+                X, stamp, lst[cur], cnt[cur], lst[nxt], cnt[nxt]);
         }
     }
     JG_CUDA(c, cudaGetLastError());
     return JETGPU_OK;
+}
+
+jetgpu_status extrapolate_region(Ctx* c, Dims s, double* data,
+                                 const unsigned char* valid, unsigned iters) {
+    return extrapolate_regions(c, 1, &s, &data, &valid, iters);
 }
 
 }  // namespace jg

@@ -173,8 +173,8 @@ struct Ctx {
     unsigned* bc_cnt = nullptr;       // their lengths per axis
     size_t bc_nrm_cap = 0;            // collider normals of inside faces
     double4_32a* bc_nrm = nullptr;
-    // extrapolate_region: stamps and two front lists (xp_cap entries each),
-    // the two front lengths.
+    // extrapolate_region(s): stamps and two front lists (xp_cap entries
+    // each), two front lengths per array.
     size_t xp_cap = 0;
     int* xp_int = nullptr;
     unsigned* xp_cnt = nullptr;
@@ -422,6 +422,11 @@ jetgpu_status bc_apply(Ctx* c, const GridDesc& g, double* u, double* v,
                        const jetgpu_collider* col, int closed, unsigned depth);
 jetgpu_status extrapolate_region(Ctx* c, Dims s, double* data,
                                  const unsigned char* valid, unsigned iters);
+// Up to three arrays extrapolated together, one launch per step.
+jetgpu_status extrapolate_regions(Ctx* c, int na, const Dims* s,
+                                  double* const* data,
+                                  const unsigned char* const* valid,
+                                  unsigned iters);
 
 // Overlap of a host-pointer solve's copies with its kernels. The compute
 // stream waits for sdf_in before the weights build (which needs only the

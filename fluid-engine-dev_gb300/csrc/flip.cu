@@ -204,13 +204,11 @@ jetgpu_status flip_substep(Ctx* c, const GridDesc& g, long np, double* pos,
         return bc_apply(c, g, u, v, w, col_sdf, col, closed, depth);
     };
     auto to_air = [&]() -> jetgpu_status {  // extrapolateVelocityToAir
-        for (int a = 0; a < 3; ++a) {
-            jetgpu_status s = extrapolate_region(
-                c, Dims{res3[a][0], res3[a][1], res3[a][2]}, vel3[a], mk[a],
-                depth);
-            if (s != JETGPU_OK) return s;
-        }
-        return JETGPU_OK;
+        const Dims ds[3] = {Dims{res3[0][0], res3[0][1], res3[0][2]},
+                            Dims{res3[1][0], res3[1][1], res3[1][2]},
+                            Dims{res3[2][0], res3[2][1], res3[2][2]}};
+        const unsigned char* vm[3] = {mk[0], mk[1], mk[2]};
+        return extrapolate_regions(c, 3, ds, vel3, vm, depth);
     };
     jetgpu_status s;
     // beginAdvanceTimeStep

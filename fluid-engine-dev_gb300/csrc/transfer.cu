@@ -227,7 +227,6 @@ __device__ __forceinline__ void p2g_corner(int q, const double4_32a& xy,
 // warp 32 faces of (nearly) equal count at a time, so the lanes run the same
 // number of steps. K is a 32-bit key when particle indices fit in 28 bits,
 // else 64-bit.
-constexpr int kGatherChunk = 1024;
 constexpr int kGatherThreads = 256;
 constexpr int kGatherBuckets = 128;  // counts >= 127 share the last bucket
 
@@ -245,7 +244,7 @@ __device__ __forceinline__ long p2g_list_bin(const Dims& s, int fi, int fj,
     return x >= 0 && y >= 0 && z >= 0 ? lin(x, y, z, s.x, s.y) : -1;
 }
 
-template <typename K>
+template <typename K, int kGatherChunk>
 __global__ void __launch_bounds__(kGatherThreads)
 k_p2g_gather(Dims s, int dm, const int* __restrict__ count,
              const int* __restrict__ off, const int* __restrict__ slist,
@@ -810,17 +809,18 @@ static jetgpu_status p2g_ordered(Ctx* c, const GridDesc& g, long np,
         reinterpret_cast<unsigned long long*>(c->p2g_int + ci);
     double4_32a* rec = reinterpret_cast<double4_32a*>(c->p2g_dbl);
     const int cap = c->num_sms * 16;
-    // 32-bit keys (particle index << 3 | list) while indices fit 28 bits.
+    // 32-bit keys (particle index << 3 | list) while indices fit 28 bits;
+    // 1024-face chunks unless a component has fewer than two per block.
     const bool k32 = np < (1l << 28);
+    auto gk = [&](bool small) {
+        return k32 ? (small ? (const void*)k_p2g_gather<unsigned, 256>
+                            : (const void*)k_p2g_gather<unsigned, 1024>)
+                   : (small ? (const void*)k_p2g_gather<unsigned long long, 256>
+                            : (const void*)k_p2g_gather<unsigned long long, 1024>);
+    };
     int gather_grid = 0;
-    if (k32)
-        JG_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                       &gather_grid, k_p2g_gather<unsigned>, kGatherThreads,
-                       0));
-    else
-        JG_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-                       &gather_grid, k_p2g_gather<unsigned long long>,
-                       kGatherThreads, 0));
+    JG_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+                   &gather_grid, gk(false), kGatherThreads, 0));
     gather_grid = std::max(1, gather_grid) * c->num_sms;
     long woff = 0;
     for (int a = 0; a < 3; ++a) {
@@ -844,16 +844,20 @@ static jetgpu_status p2g_ordered(Ctx* c, const GridDesc& g, long np,
         k_p2g_place<<<blocks_for(np, kThreads, cap), kThreads, 0,
                       c->stream>>>(np, pos, vel, L, a, key, off, list, slist,
                                    rec);
-        if (k32)
-            k_p2g_gather<unsigned>
-                <<<gather_grid, kGatherThreads, 0, c->stream>>>(
-                    s, dm, count, off, slist, rec, grid[a], wsum + woff,
-                    mark[a], counter);
-        else
-            k_p2g_gather<unsigned long long>
-                <<<gather_grid, kGatherThreads, 0, c->stream>>>(
-                    s, dm, count, off, slist, rec, grid[a], wsum + woff,
-                    mark[a], counter);
+        const bool small = n[a] < 2048l * gather_grid;
+        Dims sa = s;
+        int dma = dm;
+        const int* count_a = count;
+        const int* off_a = off;
+        const int* slist_a = slist;
+        const double4_32a* rec_a = rec;
+        double* grid_a = grid[a];
+        double* wsum_a = wsum + woff;
+        unsigned char* mark_a = mark[a];
+        void* args[] = {&sa,      &dma,    &count_a, &off_a,  &slist_a,
+                        &rec_a,   &grid_a, &wsum_a,  &mark_a, &counter};
+        JG_CUDA(c, cudaLaunchKernel(gk(small), dim3(gather_grid),
+                                    dim3(kGatherThreads), args, 0, c->stream));
         woff += n[a];
     }
     JG_CUDA(c, cudaGetLastError());
