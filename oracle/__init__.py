@@ -217,6 +217,11 @@ class Oracle:
                 C.POINTER(OrcGrid), C.c_long, _dp, _dp, C.c_int, C.c_double,
                 C.c_double, C.c_int, _dp, C.c_int, C.POINTER(OrcMgParams),
                 C.c_int, C.POINTER(C.c_int), _dp]
+        if hasattr(L, "orc_flip_run_sphere"):
+            L.orc_flip_run_sphere.argtypes = [
+                C.POINTER(OrcGrid), C.c_long, _dp, _dp, C.c_int, C.c_double,
+                C.c_double, C.c_int, _dp, C.c_int, C.POINTER(OrcMgParams),
+                _dp, C.c_double, C.c_double]
         if hasattr(L, "orc_quaternion_matrices"):
             L.orc_quaternion_matrices.argtypes = [_dp, _dp, _dp]
         if hasattr(L, "orc_sphere_collider_sdf"):
@@ -565,6 +570,25 @@ class Oracle:
                               int(frames), float(fps), float(max_cfl),
                               int(closed), _ptr(gr), int(flip),
                               C.byref(prm))
+        return pos, vel
+
+    def flip_run_sphere(self, res, spacing, origin, pos, vel, frames, centre,
+                        radius, friction=0.0, fps=60.0, max_cfl=5.0,
+                        closed=63, gravity=(0.0, -9.8, 0.0), flip=True,
+                        params: MgParams | None = None):
+        """Reference harness only: flip_run with a static sphere collider
+        (radius `radius` at `centre`, friction coefficient `friction`)."""
+        g = self._grid(res, spacing, origin)
+        pos = np.ascontiguousarray(pos, np.float64).copy()
+        vel = np.ascontiguousarray(vel, np.float64).copy()
+        prm = (params or MgParams()).c()
+        gr = np.ascontiguousarray(gravity, np.float64)
+        cc = np.ascontiguousarray(centre, np.float64)
+        self.lib.orc_flip_run_sphere(C.byref(g), pos.shape[0], _ptr(pos),
+                                     _ptr(vel), int(frames), float(fps),
+                                     float(max_cfl), int(closed), _ptr(gr),
+                                     int(flip), C.byref(prm), _ptr(cc),
+                                     float(radius), float(friction))
         return pos, vel
 
     def flip_run_record(self, res, spacing, origin, pos, vel, frames,

@@ -200,6 +200,15 @@ void orc_flip_run_record(const orc_grid* g, long np, double* pos, double* vel,
                          const orc_mg_params* p, int nrec,
                          const int* rec_frames, double* p_out);
 
+/* orc_flip_run with a static sphere collider: a RigidBodyCollider3 over a
+ * Sphere3 of `radius` translated to `centre`, friction coefficient
+ * `friction` (GridFluidSolver3::setCollider). */
+void orc_flip_run_sphere(const orc_grid* g, long np, double* pos, double* vel,
+                         int frames, double fps, double max_cfl, int closed,
+                         const double gravity[3], int flip,
+                         const orc_mg_params* p, const double centre[3],
+                         double radius, double friction);
+
 /* Reference harness only: Transform3's orientation matrix and its inverse
  * for quaternion q = (w, x, y, z), row-major. */
 void orc_quaternion_matrices(const double q[4], double orient[9],

@@ -702,11 +702,15 @@ void orc_flip_run(const orc_grid* g, long np, double* pos, double* vel,
                         gravity, flip, p, 0, nullptr, nullptr);
 }
 
-void orc_flip_run_record(const orc_grid* g, long np, double* pos, double* vel,
-                         int frames, double fps, double max_cfl, int closed,
-                         const double gravity[3], int flip,
-                         const orc_mg_params* p, int nrec,
-                         const int* rec_frames, double* p_out) {
+namespace {
+// The harness's FLIP/PIC/APIC run, with an optional static sphere collider
+// (RigidBodyCollider3 over Sphere3 of `radius` at `centre`, friction
+// `friction`; GridFluidSolver3::setCollider).
+void flip_run_impl(const orc_grid* g, long np, double* pos, double* vel,
+                   int frames, double fps, double max_cfl, int closed,
+                   const double gravity[3], int flip, const orc_mg_params* p,
+                   int nrec, const int* rec_frames, double* p_out,
+                   const double* centre, double radius, double friction) {
     Logging::mute();
     const Size3 res(g->res[0], g->res[1], g->res[2]);
     const Vector3D h(g->spacing[0], g->spacing[1], g->spacing[2]);
@@ -735,6 +739,11 @@ void orc_flip_run_record(const orc_grid* g, long np, double* pos, double* vel,
         p->coarsest_iter, p->final_iter, p->tolerance, p->sor,
         p->red_black != 0));
     s->setPressureSolver(ps);
+    if (centre) {
+        orc_collider c{{0, 0, 0}, {0, 0, 0}, {centre[0], centre[1], centre[2]},
+                       friction};
+        s->setCollider(makeCollider(&c, radius));
+    }
     const size_t cells = res.x * res.y * res.z;
     int next = 0;
     for (Frame frame(0, 1.0 / fps); frame.index < frames; ++frame) {
@@ -753,6 +762,25 @@ void orc_flip_run_record(const orc_grid* g, long np, double* pos, double* vel,
             pos[3 * i + d] = pp[i][d];
             vel[3 * i + d] = vv[i][d];
         }
+}
+}  // namespace
+
+void orc_flip_run_record(const orc_grid* g, long np, double* pos, double* vel,
+                         int frames, double fps, double max_cfl, int closed,
+                         const double gravity[3], int flip,
+                         const orc_mg_params* p, int nrec,
+                         const int* rec_frames, double* p_out) {
+    flip_run_impl(g, np, pos, vel, frames, fps, max_cfl, closed, gravity, flip,
+                  p, nrec, rec_frames, p_out, nullptr, 0.0, 0.0);
+}
+
+void orc_flip_run_sphere(const orc_grid* g, long np, double* pos, double* vel,
+                         int frames, double fps, double max_cfl, int closed,
+                         const double gravity[3], int flip,
+                         const orc_mg_params* p, const double centre[3],
+                         double radius, double friction) {
+    flip_run_impl(g, np, pos, vel, frames, fps, max_cfl, closed, gravity, flip,
+                  p, 0, nullptr, nullptr, centre, radius, friction);
 }
 
 void orc_quaternion_matrices(const double q[4], double orient[9],

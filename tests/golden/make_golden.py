@@ -38,6 +38,10 @@ Every fixture holds inputs and the reference's outputs for one small case:
   FdmMgpcgSolver3 at tolerance 1e-10, advection) for 3 frames of 1/60 s on
   the 64^3 dam break's geometry at 24^3 (water box [0,.25]x[0,.75]x[0,1],
   8 particles per cell from seed 0, closed walls, gravity (0,-9.8,0)).
+* flip_sphere_24.npz — FlipSolver3 for 3 frames of the 24^3 dam break (as
+  flip_dam_break_24.npz) with a static sphere collider (radius 0.12 at
+  (0.3, 0.15, 0.5), friction 0.2) that cuts into the water column: the
+  reference's collider SDF on the grid and the final particles.
 * flip_dam_break_64.npz — FlipSolver3 on the full-size dam break: 64^3,
   60 frames of the same dam break (393,216 particles), pressure
   to an absolute 1e-10; the pressure after frames 1, 10, 30 and 60
@@ -364,6 +368,21 @@ def flip_dam_break(ref):
                           flip=False, params=p)
     save("flip_dam_break_24.npz", flip_pos=fp, flip_vel=fv, pic_pos=pp,
          pic_vel=pv)
+
+
+def flip_sphere(ref):
+    n = 24
+    h = 1.0 / n
+    pos, vel = scenes.dam_break_particles(n, (0.25, 0.75, 1.0), seed=0)
+    p = oracle.MgParams(100, 5, 5, 5, 20, 20, 1e-10, 1.5, True)
+    centre, radius, friction = (0.3, 0.15, 0.5), 0.12, 0.2
+    sdf = ref.sphere_collider_sdf((n, n, n), (h, h, h), (0, 0, 0), centre,
+                                  radius)
+    fp, fv = ref.flip_run_sphere((n, n, n), (h, h, h), (0, 0, 0), pos, vel, 3,
+                                 centre, radius, friction, params=p)
+    save("flip_sphere_24.npz", sdf=sdf, centre=np.array(centre),
+         radius=np.array(radius), friction=np.array(friction), flip_pos=fp,
+         flip_vel=fv)
 
 
 # Frames after which the 64^3 dam break's pressure is kept, and the particle

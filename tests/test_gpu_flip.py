@@ -45,6 +45,33 @@ def test_dam_break_three_frames_matches_reference(flip):
     ps.close()
 
 
+def test_dam_break_with_sphere_collider_matches_reference():
+    """The 24^3 dam break with a static sphere collider cutting into the
+    water column (some particles start inside it): collisions, the collider
+    classification shared by a sub-step's boundary passes, its cached
+    normals and the extrapolation fronts next to the collider, against
+    FlipSolver3 with GridFluidSolver3::setCollider (flip_sphere_24.npz)."""
+    g = golden("flip_sphere_24.npz")
+    n = 24
+    h = 1.0 / n
+    ps = jetgpu.FdmMgpcgSolver3(200, 5, 2, 2, 10, 2, 1e-6, 1.0, True)
+    sim = jetgpu.FlipSolver3((n, n, n), h, (0, 0, 0), pressureSolver=ps)
+    pos, _ = scenes.dam_break_particles(n, (0.25, 0.75, 1.0), seed=0)
+    sim.setParticles(pos)
+    centre = tuple(float(x) for x in g["centre"])
+    sim.setCollider(g["sdf"],
+                    jetgpu.Collider.make(centre=centre,
+                                         friction=float(g["friction"])),
+                    jetgpu.Sphere.make(float(g["radius"])))
+    for _ in range(3):
+        sim.update(1.0 / 60)
+    pos, vel = sim.positions(), sim.velocities()
+    assert sim.subSteps >= 3
+    assert np.abs(pos - g["flip_pos"]).max() < POS_TOL
+    assert np.abs(vel - g["flip_vel"]).max() < VEL_TOL
+    ps.close()
+
+
 # The 64^3 dam break for 60 frames: bounds on the GPU run's deviation from the
 # reference's (golden fixture flip_dam_break_64.npz). The reference itself,
 # run again with its solver at a tolerance of 1e-6 instead of 1e-10, lands
