@@ -663,6 +663,7 @@ __device__ void resolve_sphere(const SphereDesc& S, double p[3],
     for (int d = 0; d < 3; ++d) p[d] = tp[d];
 }
 
+template <bool kZeroOrigin>
 __global__ void k_move_particles(long np, double* __restrict__ pos,
                                  double* __restrict__ vel, FaceSet fs,
                                  const double* __restrict__ u,
@@ -681,13 +682,14 @@ __global__ void k_move_particles(long np, double* __restrict__ pos,
         double vv[3] = {vel[3 * q], vel[3 * q + 1], vel[3 * q + 2]};
         // The three face grids share their data origins axis by axis (the
         // grid origin on a face's normal axis, origin + h/2 on the others),
-        // so each point needs six subtractions, not nine.
+        // so each point needs six subtractions, not nine; with the grid
+        // origin at +0 the normal-axis ones are x - (+0) = x exactly.
         const Spacing sp[3] = {hx, hy, hz};
         auto sample3 = [&](const double q[3], double out[3]) {
             double nn[3], nt[3];
 #pragma unroll
             for (int d = 0; d < 3; ++d) {
-                nn[d] = sp[d].div(q[d] - fs.o[d][d]);
+                nn[d] = sp[d].div(kZeroOrigin ? q[d] : q[d] - fs.o[d][d]);
                 nt[d] = sp[d].div(q[d] - fs.o[(d + 1) % 3][d]);
             }
 #pragma unroll
@@ -757,8 +759,13 @@ jetgpu_status move_particles(Ctx* c, const GridDesc& g, long np, double* pos,
     }
     if (np > 0) {
         Prof pr(c, K_MOVE, 96.0 * np);
-        k_move_particles<<<blocks_for(np, kThreads, c->num_sms * 16), kThreads,
-                           0, c->stream>>>(
+        bool zero_origin = true;  // all three components are +0.0
+        for (int d = 0; d < 3; ++d)
+            zero_origin = zero_origin && dbits(g.origin[d]) == 0ull;
+        auto kern = zero_origin ? k_move_particles<true>
+                                : k_move_particles<false>;
+        kern<<<blocks_for(np, kThreads, c->num_sms * 16), kThreads, 0,
+               c->stream>>>(
             np, pos, vel, fs, u, v, w, make_spacing(g.spacing[0]),
             make_spacing(g.spacing[1]), make_spacing(g.spacing[2]), dt / nsub,
             nsub, closed, lo[0], lo[1], lo[2], hi[0],
