@@ -470,6 +470,7 @@ void jetgpu_destroy(jetgpu_ctx* c) {
     release(&c->bc_list);
     release(&c->bc_cnt);
     release(&c->bc_nrm);
+    release(&c->bc_flag);
     release(&c->xp_int);
     release(&c->xp_cnt);
     release(&c->sdf_int);

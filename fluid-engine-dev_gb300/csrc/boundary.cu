@@ -129,11 +129,32 @@ __device__ __forceinline__ void push(int* __restrict__ lst,
 // those without a valid fraction (collider velocity, then extrapolated) and
 // those inside the collider (projected). List order is arbitrary; every
 // pass over a list is order-independent.
+//
+// With `irregular` non-null the collider SDF lies on the velocity grid's
+// cell centres, the grid origin is +0 and the spacings are powers of two
+// (checked on the host); the flag is 0 when every SDF value is finite and
+// non-zero (checked by k_sdf_regular). Then a face's
+// two end points are exactly the centres of the cells on either side and
+// its centre exactly halfway (the coordinate arithmetic is exact), so the
+// samples are the two cell values a and b (each lerp with fraction 0 gives
+// its first operand) and half(a + b) (the fraction-1/2 rule, when a and b
+// are in its safe exponent range); an interior face then reads two values.
+// Boundary faces and out-of-range values take the samples.
+__global__ void k_sdf_regular(const double* __restrict__ d, long n,
+                              int* __restrict__ irregular) {
+    for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < n;
+         c += (long)gridDim.x * blockDim.x) {
+        const unsigned long long b = dbits(d[c]);
+        if ((b << 1) == 0ull || ((b >> 52) & 0x7ffu) == 0x7ffu) *irregular = 1;
+    }
+}
+
 __global__ void k_bc_classify(FaceSet fs, H3 h, FieldDesc sdf, S3 fsp,
                               Axes3 ax, long nf,
                               unsigned char* __restrict__ cls_all,
                               int* __restrict__ list_all,
-                              unsigned* __restrict__ cnt_all) {
+                              unsigned* __restrict__ cnt_all,
+                              const int* __restrict__ irregular) {
     const int a = blockIdx.y;
     const Dims s = fs.s[a];
     unsigned char* cls = cls_all + ax.off[a];
@@ -142,10 +163,29 @@ __global__ void k_bc_classify(FaceSet fs, H3 h, FieldDesc sdf, S3 fsp,
     int* in_list = list_all + nf + ax.off[a];
     unsigned* in_cnt = cnt_all + 3 + a;
     const long n = s.count();
+    const bool reg = irregular && !*irregular;
+    const Dims cd{sdf.res[0], sdf.res[1], sdf.res[2]};
+    const long step = a == 0 ? 1 : (a == 1 ? (long)cd.x : (long)cd.x * cd.y);
     for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < n;
          c += (long)gridDim.x * blockDim.x) {
         int i, j, k;
         cell_ijk(c, s, i, j, k);
+        const int ia = a == 0 ? i : (a == 1 ? j : k);  // index along the axis
+        if (reg && ia > 0 && ia < (a == 0 ? cd.x : (a == 1 ? cd.y : cd.z))) {
+            // The cells on either side of the face.
+            const long cb = lin(i, j, k, cd.x, cd.y);  // the upper cell
+            const double va = sdf.data[cb - step], vb = sdf.data[cb];
+            if (half_safe(dbits(va)) && half_safe(dbits(vb))) {
+                double frac = frac_inside_sdf(va, vb);
+                frac = 1.0 - (frac < 0.0 ? 0.0 : (frac > 1.0 ? 1.0 : frac));
+                unsigned char f = frac > 0.0 ? kFaceValid : 0;
+                if (va + vb < 0.0) f |= kFaceInside;
+                cls[c] = f;
+                push(inv_list, inv_cnt, c, !(f & kFaceValid));
+                push(in_list, in_cnt, c, (f & kFaceInside) != 0);
+                continue;
+            }
+        }
         double p[3], q0[3], q1[3];
         face_pos(fs, a, h.v, i, j, k, p);
         for (int d = 0; d < 3; ++d) {
@@ -618,10 +658,28 @@ jetgpu_status bc_classify(Ctx* c, const GridDesc& g, const FieldDesc& sdf) {
     long nmax = 0;
     for (int a = 0; a < 3; ++a) nmax = std::max(nmax, fs.s[a].count());
     Prof pr(c, K_BOUNDARY, 1.0 * (double)nf);
+    // The aligned case of k_bc_classify: the SDF on the grid's cell centres
+    // (same resolution and spacing, origin + h/2), grid origin +0 and
+    // power-of-two spacings; the values are checked on the device.
+    bool aligned = sdf.kind == 1;
+    for (int d = 0; d < 3 && aligned; ++d)
+        aligned = sdf.res[d] == g.res[d] && sdf.spacing[d] == g.spacing[d] &&
+                  dbits(g.origin[d]) == 0ull && fsp.s[d].pow2 &&
+                  sdf.origin[d] == 0.5 * g.spacing[d];
+    int* irregular = nullptr;
+    if (aligned) {
+        if (!c->bc_flag) JG_CUDA(c, cudaMalloc((void**)&c->bc_flag, sizeof(int)));
+        irregular = c->bc_flag;
+        JG_CUDA(c, cudaMemsetAsync(irregular, 0, sizeof(int), c->stream));
+        const long ncell = (long)g.res[0] * g.res[1] * g.res[2];
+        k_sdf_regular<<<blocks_for(ncell, kThreads, c->num_sms * 8), kThreads,
+                        0, c->stream>>>(sdf.data, ncell, irregular);
+    }
     // Lists: invalid faces of axis a at bc_list + off[a], inside faces at
     // bc_list + nf + off[a]; counts bc_cnt[a], bc_cnt[3 + a].
     k_bc_classify<<<bc_grid(c, nmax), kThreads, 0, c->stream>>>(
-        fs, h, sdf, fsp, ax, (long)nf, c->bc_cls, c->bc_list, c->bc_cnt);
+        fs, h, sdf, fsp, ax, (long)nf, c->bc_cls, c->bc_list, c->bc_cnt,
+        irregular);
     k_bc_normals<<<bc_grid(c, nmax / 8), kThreads, 0, c->stream>>>(
         fs, h, fsp, inv, sdf, ax, (long)nf, c->bc_list, c->bc_cnt, c->bc_nrm);
     JG_CUDA(c, cudaGetLastError());

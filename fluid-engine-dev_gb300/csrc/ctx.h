@@ -171,6 +171,7 @@ struct Ctx {
     unsigned char* bc_cls = nullptr;  // face classes of the last bc_classify
     int* bc_list = nullptr;           // its invalid / inside face lists
     unsigned* bc_cnt = nullptr;       // their lengths per axis
+    int* bc_flag = nullptr;           // the classification's regular SDF
     size_t bc_nrm_cap = 0;            // collider normals of inside faces
     double4_32a* bc_nrm = nullptr;
     // extrapolate_region(s): stamps and two front lists (xp_cap entries
