@@ -421,10 +421,17 @@ def run_ours(args, rank, world, local, pg):
     solve_bytes = sum(k["bytes"] for k in prof) / args.steps
     whole = solve_bytes / (ms * 1e-3) / 1e9
 
-    # End-to-end through the host-pointer C ABI with pinned host buffers.
+    # End-to-end through the host-pointer C ABI with pinned host buffers, the
+    # way GridFluidSolver3::computePressure calls its pressure solver: the
+    # output grid holds the input's values (the input is its clone), so the
+    # solver moves only the velocity faces around the fluid cells
+    # (fluid_box_io); the bytes moved are the solver's own count.
+    solver.close()
+    solver = jetgpu.FdmMgpcgSolver3(**solver_params(*VARIANTS[head]),
+                                    device=local, fluidBoxIo=True)
     pin = {k: torch.from_numpy(np.ascontiguousarray(sc[k])).pin_memory()
            for k in ("u", "v", "w", "boundary_sdf", "fluid_sdf")}
-    hout = {k: torch.empty_like(pin[k]).pin_memory() for k in ("u", "v", "w")}
+    hout = {k: pin[k].clone().pin_memory() for k in ("u", "v", "w")}
     vel = jetgpu.FaceCenteredGrid3((n, n, n), (h, h, h), (0, 0, 0),
                                    pin["u"].numpy(), pin["v"].numpy(),
                                    pin["w"].numpy())
@@ -435,7 +442,7 @@ def run_ours(args, rank, world, local, pg):
     cg = lambda t: jetgpu.CellCenteredScalarGrid3((n, n, n), (h, h, h),
                                                   (0, 0, 0), t.numpy())
     bg, fg = cg(pin["boundary_sdf"]), cg(pin["fluid_sdf"])
-    stream = r["stream"]
+    stream = torch.cuda.ExternalStream(solver.stream(), device=dev)
     for _ in range(max(1, args.warmup)):
         ps.solve(vel, 1 / 60, outg, bg, None, fg)
     # Three batches of K host-pointer solves; the median batch is reported
@@ -453,8 +460,8 @@ def run_ours(args, rank, world, local, pg):
         batches.append(max_over_ranks(pg, e0.elapsed_time(e1) / args.steps,
                                       local))
     e2e_ms = sorted(batches)[1]
-    h2d = sum(pin[k].numel() * 8 for k in pin)
-    d2h = sum(hout[k].numel() * 8 for k in hout) + n ** 3 * 8
+    h2d = int(ps.last_stats.h2d_bytes)
+    d2h = int(ps.last_stats.d2h_bytes)
     solver.close()
     return dict(ms=ms, e2e_ms=e2e_ms, e2e_batches=batches, h2d=h2d, d2h=d2h,
                 clocks=ck,

@@ -196,6 +196,46 @@ __global__ void k_rows_f32_to_f64(const float* __restrict__ A,
     }
 }
 
+// The bounding box of the fluid cells (phi < 0): box = (i0, j0, k0, i1, j1,
+// k1), empty when i1 < i0. A block reduces its cells, then one atomic per
+// bound and block.
+__global__ void k_box_init(int* box) {
+    box[0] = box[1] = box[2] = 0x7fffffff;
+    box[3] = box[4] = box[5] = -1;
+}
+__global__ void k_fluid_box(const double* __restrict__ phi, Dims n,
+                            int* __restrict__ box) {
+    __shared__ int sb[6];
+    if (threadIdx.x < 6) sb[threadIdx.x] = threadIdx.x < 3 ? 0x7fffffff : -1;
+    __syncthreads();
+    int lo[3] = {0x7fffffff, 0x7fffffff, 0x7fffffff}, hi[3] = {-1, -1, -1};
+    const long N = n.count();
+    for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < N;
+         c += (long)gridDim.x * blockDim.x) {
+        if (phi[c] < 0.0) {
+            int i, j, k;
+            cell_ijk(c, n, i, j, k);
+            lo[0] = min(lo[0], i); lo[1] = min(lo[1], j); lo[2] = min(lo[2], k);
+            hi[0] = max(hi[0], i); hi[1] = max(hi[1], j); hi[2] = max(hi[2], k);
+        }
+    }
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+        for (int o = 16; o > 0; o >>= 1) {
+            lo[d] = min(lo[d], __shfl_xor_sync(0xffffffffu, lo[d], o));
+            hi[d] = max(hi[d], __shfl_xor_sync(0xffffffffu, hi[d], o));
+        }
+    }
+    if ((threadIdx.x & 31) == 0)
+        for (int d = 0; d < 3; ++d) {
+            atomicMin(&sb[d], lo[d]);
+            atomicMax(&sb[3 + d], hi[d]);
+        }
+    __syncthreads();
+    if (threadIdx.x < 3) atomicMin(&box[threadIdx.x], sb[threadIdx.x]);
+    else if (threadIdx.x < 6) atomicMax(&box[threadIdx.x], sb[threadIdx.x]);
+}
+
 jetgpu_status grow_stage(Ctx* c, size_t bytes) {
     if (bytes <= c->stage_bytes) return JETGPU_OK;
     release(&c->stage);
@@ -296,6 +336,7 @@ static jetgpu_status build_levels(Ctx* c, const GridDesc& g, const double* u,
         if ((s = prepare_levels(c, 1)) != JETGPU_OK) return s;
         if (fork) JG_CUDA(c, cudaEventRecord(c->side_ev[1], c->stream));
     }
+    if (io && io->before_vel && (s = io->before_vel()) != JETGPU_OK) return s;
     if (io) JG_CUDA(c, cudaStreamWaitEvent(c->stream, io->vel_in, 0));
     if ((s = build_system(c, g, u, v, w, su, sv, sw, 0, 1)) != JETGPU_OK)
         return s;
@@ -328,6 +369,8 @@ jetgpu_status solve_pressure_dev(
         s = build_levels(c, g, u, v, w, su, sv, sw, io);
         if (s != JETGPU_OK) return s;
     } else {
+        if (io && io->before_vel && (s = io->before_vel()) != JETGPU_OK)
+            return s;
         if (io) JG_CUDA(c, cudaStreamWaitEvent(c->stream, io->vel_in, 0));
         s = blocked_system(c, g, u, v, w);
         if (s != JETGPU_OK) return s;
@@ -436,6 +479,9 @@ jetgpu_status jetgpu_create(const jetgpu_config* cfg, jetgpu_ctx** out) {
         JG_CUDA(c, cudaMalloc((void**)&c->counters, kRedSlots * sizeof(unsigned)));
         JG_CUDA(c, cudaMemset(c->counters, 0, kRedSlots * sizeof(unsigned)));
         JG_CUDA(c, cudaMallocHost((void**)&c->h_scal, S_COUNT * sizeof(double)));
+        JG_CUDA(c, cudaMalloc((void**)&c->box_dev, 6 * sizeof(int)));
+        JG_CUDA(c, cudaMallocHost((void**)&c->box_host, 6 * sizeof(int)));
+        JG_CUDA(c, cudaEventCreateWithFlags(&c->box_ev, cudaEventDisableTiming));
         for (auto& e : c->ev) JG_CUDA(c, cudaEventCreate(&e));
         jetgpu_status k = init_kernels(c);
         if (k != JETGPU_OK) return k;
@@ -501,6 +547,9 @@ void jetgpu_destroy(jetgpu_ctx* c) {
     }
     for (auto& e : c->io_ev)
         if (e) cudaEventDestroy(e);
+    if (c->box_ev) cudaEventDestroy(c->box_ev);
+    release(&c->box_dev);
+    if (c->box_host) cudaFreeHost(c->box_host);
     for (auto& e : c->side_ev)
         if (e) cudaEventDestroy(e);
     if (c->side_stream) cudaStreamDestroy(c->side_stream);
@@ -643,13 +692,99 @@ static jetgpu_status solve_host(
     if (db) JG_CUDA(c, cudaMemcpyAsync(db, boundary_sdf->data, nb * 8, cudaMemcpyHostToDevice, cs));
     if (df) JG_CUDA(c, cudaMemcpyAsync(df, fluid_sdf->data, nf * 8, cudaMemcpyHostToDevice, cs));
     JG_CUDA(c, cudaEventRecord(io.sdf_in, cs));
-    JG_CUDA(c, cudaMemcpyAsync(du, u, nu * 8, cudaMemcpyHostToDevice, cs));
-    JG_CUDA(c, cudaMemcpyAsync(dv, v, nv * 8, cudaMemcpyHostToDevice, cs));
-    JG_CUDA(c, cudaMemcpyAsync(dw, w, nw * 8, cudaMemcpyHostToDevice, cs));
-    if (solid_u) JG_CUDA(c, cudaMemcpyAsync(dsu, solid_u, nu * 8, cudaMemcpyHostToDevice, cs));
-    if (solid_v) JG_CUDA(c, cudaMemcpyAsync(dsv, solid_v, nv * 8, cudaMemcpyHostToDevice, cs));
-    if (solid_w) JG_CUDA(c, cudaMemcpyAsync(dsw, solid_w, nw * 8, cudaMemcpyHostToDevice, cs));
-    JG_CUDA(c, cudaEventRecord(io.vel_in, cs));
+    unsigned long long h2d = (unsigned long long)(nb + nf) * 8, d2h = 0;
+    // The face boxes of u, v, w moved in each direction (origin and extent
+    // in faces): the whole arrays, or with fluid_box_io the bounding box of
+    // the fluid cells widened by the faces that close it.
+    struct FBox {
+        long x0, y0, z0, wx, wy, wz;
+    } fb[3] = {{0, 0, 0, nx + 1, ny, nz},
+               {0, 0, 0, nx, ny + 1, nz},
+               {0, 0, 0, nx, ny, nz + 1}};
+    auto box_bytes = [&](int a) {
+        return (unsigned long long)(fb[a].wx * fb[a].wy * fb[a].wz) * 8ull;
+    };
+    auto copy_box = [&](double* dst, const double* src, int a,
+                        cudaMemcpyKind kind, cudaStream_t on) -> jetgpu_status {
+        const FBox& b = fb[a];
+        if (b.wx <= 0 || b.wy <= 0 || b.wz <= 0) return JETGPU_OK;
+        const long rx = nx + (a == 0), ry = ny + (a == 1);
+        const long rz = nz + (a == 2);
+        if (b.wx == rx && b.wy == ry && b.wz == rz) {
+            JG_CUDA(c, cudaMemcpyAsync(dst, src, (size_t)(rx * ry * rz) * 8,
+                                       kind, on));
+            return JETGPU_OK;
+        }
+        cudaMemcpy3DParms p3 = {};
+        p3.srcPtr = make_cudaPitchedPtr(const_cast<double*>(src), rx * 8, rx, ry);
+        p3.dstPtr = make_cudaPitchedPtr(dst, rx * 8, rx, ry);
+        p3.srcPos = make_cudaPos(b.x0 * 8, b.y0, b.z0);
+        p3.dstPos = p3.srcPos;
+        p3.extent = make_cudaExtent(b.wx * 8, b.wy, b.wz);
+        p3.kind = kind;
+        JG_CUDA(c, cudaMemcpy3DAsync(&p3, on));
+        return JETGPU_OK;
+    };
+    auto upload_velocities = [&]() -> jetgpu_status {
+        const double* hv[3] = {u, v, w};
+        double* dv3[3] = {du, dv, dw};
+        const double* hs[3] = {solid_u, solid_v, solid_w};
+        double* ds3[3] = {dsu, dsv, dsw};
+        for (int a = 0; a < 3; ++a) {
+            jetgpu_status e = copy_box(dv3[a], hv[a], a, cudaMemcpyHostToDevice, cs);
+            if (e != JETGPU_OK) return e;
+            h2d += box_bytes(a);
+            if (hs[a]) {
+                e = copy_box(ds3[a], hs[a], a, cudaMemcpyHostToDevice, cs);
+                if (e != JETGPU_OK) return e;
+                h2d += box_bytes(a);
+            }
+        }
+        JG_CUDA(c, cudaEventRecord(io.vel_in, cs));
+        return JETGPU_OK;
+    };
+    const bool box_io = c->cfg.fluid_box_io != 0 && !blocked;
+    if (box_io) {
+        // The box is found on the device as soon as the fluid SDF is in;
+        // the host reads it back once the set-up that needs no velocity is
+        // queued, and only then issues the velocity uploads.
+        if (df) {
+            const Dims dn{(int)nx, (int)ny, (int)nz};
+            k_box_init<<<1, 1, 0, cs>>>(c->box_dev);
+            k_fluid_box<<<blocks_for(dn.count(), kThreads, c->num_sms * 4),
+                          kThreads, 0, cs>>>(df, dn, c->box_dev);
+            JG_CUDA(c, cudaMemcpyAsync(c->box_host, c->box_dev, 6 * sizeof(int),
+                                       cudaMemcpyDeviceToHost, cs));
+            JG_CUDA(c, cudaEventRecord(c->box_ev, cs));
+        }
+        io.before_vel = [&]() -> jetgpu_status {
+            int bx[6];
+            if (df) {
+                JG_CUDA(c, cudaEventSynchronize(c->box_ev));
+                for (int d = 0; d < 6; ++d) bx[d] = c->box_host[d];
+            } else if (fluid_sdf->value < 0.0) {  // all fluid
+                bx[0] = bx[1] = bx[2] = 0;
+                bx[3] = (int)nx - 1;
+                bx[4] = (int)ny - 1;
+                bx[5] = (int)nz - 1;
+            } else {  // no fluid
+                bx[0] = bx[1] = bx[2] = 0;
+                bx[3] = bx[4] = bx[5] = -1;
+            }
+            const bool empty = bx[3] < bx[0];
+            for (int a = 0; a < 3; ++a) {
+                fb[a].x0 = bx[0];
+                fb[a].y0 = bx[1];
+                fb[a].z0 = bx[2];
+                fb[a].wx = empty ? 0 : bx[3] - bx[0] + 1 + (a == 0);
+                fb[a].wy = empty ? 0 : bx[4] - bx[1] + 1 + (a == 1);
+                fb[a].wz = empty ? 0 : bx[5] - bx[2] + 1 + (a == 2);
+            }
+            return upload_velocities();
+        };
+    } else {
+        if ((s = upload_velocities()) != JETGPU_OK) return s;
+    }
     if (col_faces) {
         GridDesc gd;
         for (int a = 0; a < 3; ++a) {
@@ -669,12 +804,22 @@ static jetgpu_status solve_host(
         if (stats) *stats = local;
         return solve_status;
     }
-    JG_CUDA(c, cudaMemcpyAsync(out_u, ou, nu * 8, cudaMemcpyDeviceToHost, st));
-    JG_CUDA(c, cudaMemcpyAsync(out_v, ov, nv * 8, cudaMemcpyDeviceToHost, st));
-    JG_CUDA(c, cudaMemcpyAsync(out_w, ow, nw * 8, cudaMemcpyDeviceToHost, st));
+    {
+        double* ho[3] = {out_u, out_v, out_w};
+        const double* dout[3] = {ou, ov, ow};
+        for (int a = 0; a < 3; ++a) {
+            if ((s = copy_box(ho[a], dout[a], a, cudaMemcpyDeviceToHost, st)) !=
+                JETGPU_OK)
+                return s;
+            d2h += box_bytes(a);
+        }
+    }
+    if (out_pressure) d2h += (unsigned long long)nx * ny * nz * 8;
     JG_CUDA(c, cudaStreamSynchronize(st));
     JG_CUDA(c, cudaStreamSynchronize(cs));
     local.total_ms = ms_since(t0);
+    local.h2d_bytes = h2d;
+    local.d2h_bytes = d2h;
     if (stats) *stats = local;
     return solve_status;
 }

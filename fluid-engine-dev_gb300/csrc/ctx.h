@@ -7,6 +7,7 @@
 #include <cuda_bf16.h>
 
 #include <mutex>
+#include <functional>
 #include <string>
 #include <unordered_map>
 #include <vector>
@@ -103,6 +104,11 @@ struct Ctx {
     // compute stream by io_ev (see SolveIo).
     cudaStream_t copy_stream = nullptr;
     cudaEvent_t io_ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    // Fluid-box transfers: the box on the device and in pinned host memory,
+    // and the event that says it has arrived.
+    int* box_dev = nullptr;
+    int* box_host = nullptr;
+    cudaEvent_t box_ev = nullptr;
     // High-priority stream for the coarse levels' set-up, which runs beside
     // the finest level's (fork and join events).
     cudaStream_t side_stream = nullptr;
@@ -439,6 +445,10 @@ struct SolveIo {
     cudaEvent_t sdf_in = nullptr, vel_in = nullptr, x_final = nullptr;
     cudaStream_t copy = nullptr;
     double* host_p = nullptr;
+    // Called once the set-up that needs no velocity is queued, before the
+    // level-0 system waits for vel_in (issues the velocity uploads when
+    // they depend on something the host must first read back).
+    std::function<jetgpu_status()> before_vel;
 };
 
 // GridFractionalSinglePhasePressureSolver3::solve on device arrays (api.cu):

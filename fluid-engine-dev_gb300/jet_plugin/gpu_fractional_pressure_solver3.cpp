@@ -23,6 +23,12 @@ GpuFractionalSinglePhasePressureSolver3::GpuFractionalSinglePhasePressureSolver3
     const jetgpu_config* cfg) {
     jetgpu_config_default(&_config);
     if (cfg) _config = *cfg;
+    // applyPressureGradient writes only the faces next to fluid cells, and
+    // GridFluidSolver3::computePressure hands in a clone of the output grid
+    // as the input: only the velocity faces around the fluid cells need to
+    // cross the host link, and the output's other faces keep their values,
+    // as the reference leaves them.
+    _config.fluid_box_io = 1;
 }
 
 GpuFractionalSinglePhasePressureSolver3::

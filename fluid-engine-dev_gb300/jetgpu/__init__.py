@@ -51,6 +51,7 @@ class Config(C.Structure):
         ("preconditioner", C.c_int),
         ("max_refinements", C.c_uint),
         ("ordered_p2g", C.c_int),
+        ("fluid_box_io", C.c_int),
     ]
 
 
@@ -85,6 +86,8 @@ class SolveStats(C.Structure):
         ("solve_ms", C.c_double),
         ("total_ms", C.c_double),
         ("fallback_used", C.c_int),
+        ("h2d_bytes", C.c_ulonglong),
+        ("d2h_bytes", C.c_ulonglong),
     ]
 
     def as_dict(self) -> dict:
@@ -418,7 +421,8 @@ class FdmMgpcgSolver3:
                  numberOfCoarsestIter=5, numberOfFinalIter=2,
                  maxTolerance=1e-6, sorFactor=1.2, useRedBlackOrdering=True,
                  precision="fp32", device=0, maxRefinements=6,
-                 preconditioner="multigrid", orderedP2G=True):
+                 preconditioner="multigrid", orderedP2G=True,
+                 fluidBoxIo=False):
         if not useRedBlackOrdering:
             raise ValueError("the GPU smoother is red-black; the lexicographic "
                              "Gauss-Seidel sweep is serial by construction")
@@ -441,6 +445,10 @@ class FdmMgpcgSolver3:
         # P2G in particle order (bit-exact with the reference) or by FP64
         # atomics (faster; rounding-level differences).
         cfg.ordered_p2g = 1 if orderedP2G else 0
+        # Host-pointer solves move only the velocity faces around the fluid
+        # (GridFluidSolver3's convention: the output holds the input's
+        # values elsewhere).
+        cfg.fluid_box_io = 1 if fluidBoxIo else 0
         self._ctx = None
         self.last_stats = SolveStats()
 

@@ -101,6 +101,17 @@ typedef struct jetgpu_config {
      * from run to run; zero scatters with FP64 atomics (faster; the sums
      * differ from the reference's in rounding only). */
     int ordered_p2g;
+    /* Host-pointer fractional solves (jetgpu_solve_pressure[_collider]):
+     * nonzero moves only the velocity faces inside the bounding box of the
+     * fluid cells (fluid_sdf < 0), widened by the faces that close it, in
+     * both directions, and leaves the output's faces outside that box as
+     * they are. The reference reads and writes velocities only at faces
+     * next to fluid cells (buildSystem, applyPressureGradient), so this
+     * gives its result whenever the output already holds the input's
+     * values outside the box — as in GridFluidSolver3::computePressure,
+     * whose input is a clone of the output grid. Inside the box, faces the
+     * projection leaves alone get the input's values (as with zero). */
+    int fluid_box_io;
 } jetgpu_config;
 
 /* Fills `cfg` with defaults: FdmMgpcgSolver3(100, 6, 2, 2, 5, 2, 1e-6, 1.2,
@@ -141,6 +152,8 @@ typedef struct jetgpu_solve_stats {
     double solve_ms;             /* Krylov solve (device time) */
     double total_ms;             /* whole call, including copies */
     int fallback_used;           /* learned preconditioner fell back */
+    unsigned long long h2d_bytes; /* host-pointer solves: bytes uploaded */
+    unsigned long long d2h_bytes; /* ... and downloaded */
 } jetgpu_solve_stats;
 
 /* Context lifetime. */

@@ -357,3 +357,49 @@ def test_device_loop_matches_host_loop(precision):
         s.close()
     assert res[0][0] == res[1][0]
     assert np.array_equal(res[0][1], res[1][1])
+
+
+@pytest.mark.parametrize("case", ["flip", "sphere_union", "noncubic_solid",
+                                  "no_fluid", "all_fluid"])
+def test_fluid_box_io_matches_full_io(case):
+    """fluid_box_io moves only the velocity faces around the fluid cells;
+    with the output holding the input's values (a clone, as
+    GridFluidSolver3::computePressure passes), pressure and output are the
+    full-transfer solve's bits, and fewer bytes cross the host link."""
+    solid = None
+    if case == "flip":
+        n = 48
+        res, h = (n,) * 3, (1.0 / n,) * 3
+        sc = scenes.flip_first_substep(n, box_hi=(0.3, 0.6, 0.8))
+        args = (sc["u"], sc["v"], sc["w"], sc["boundary_sdf"], sc["fluid_sdf"])
+    elif case == "sphere_union":
+        n = 32
+        res, h = (n,) * 3, (1.0 / n,) * 3
+        sc = scenes.sphere_union_scene(n, seed=3)
+        args = (sc["u"], sc["v"], sc["w"], sc["boundary_sdf"], sc["fluid_sdf"])
+    elif case == "noncubic_solid":
+        g = golden("noncubic_12x8x16.npz")
+        res, h = (12, 8, 16), tuple(g["spacing"])
+        args = (g["u"], g["v"], g["w"], g["boundary_sdf"], g["fluid_sdf"])
+        solid = (g["solid_u"], g["solid_v"], g["solid_w"])
+    else:
+        n = 16
+        res, h = (n,) * 3, (1.0 / n,) * 3
+        rng = np.random.default_rng(5)
+        args = (rng.uniform(-1, 1, (n, n, n + 1)),
+                rng.uniform(-1, 1, (n, n + 1, n)),
+                rng.uniform(-1, 1, (n + 1, n, n)), KMAX,
+                1.0 if case == "no_fluid" else -1.0)
+    full = solve(res, h, *args, solid=solid)
+    box = solve(res, h, *args, solid=solid, fluidBoxIo=True)
+    # (The all-fluid closed box with random velocities is a singular
+    # system that stops at the iteration cap: both report it alike.)
+    assert full[2] == box[2]
+    assert np.array_equal(full[0].pressure(), box[0].pressure())
+    for k in "uvw":
+        assert np.array_equal(getattr(full[1], k), getattr(box[1], k)), k
+    fs, bs = full[0].last_stats, box[0].last_stats
+    if case in ("flip", "sphere_union", "no_fluid"):
+        assert bs.h2d_bytes < fs.h2d_bytes and bs.d2h_bytes < fs.d2h_bytes
+    else:  # fluid cells span the grid: the box is every face
+        assert bs.h2d_bytes == fs.h2d_bytes and bs.d2h_bytes == fs.d2h_bytes
