@@ -360,10 +360,12 @@ jetgpu_status solve_pressure_dev(
     // Set-up and solve times come from events on the stream, so the host
     // never waits between the set-up kernels and the solve.
     JG_CUDA(c, cudaEventRecord(c->ev[0], c->stream));
-    if (io) JG_CUDA(c, cudaStreamWaitEvent(c->stream, io->sdf_in, 0));
+    if (io)
+        JG_CUDA(c, cudaStreamWaitEvent(c->stream,
+                                       blocked ? io->sdf_in : io->bsdf_in, 0));
     s = blocked ? blocked_markers(c, g, to_desc(bsdf, bdata), to_desc(fsdf, fdata))
                 : build_weights(c, g, to_desc(bsdf, bdata), to_desc(fsdf, fdata),
-                                false);
+                                false, io ? io->sdf_in : nullptr);
     if (s != JETGPU_OK) return s;
     if (!blocked) {
         s = build_levels(c, g, u, v, w, su, sv, sw, io);
@@ -672,10 +674,10 @@ static jetgpu_status solve_host(
     double* ou = p;
     double* ov = ou + nu;
     double* ow = ov + nv;
-    // Uploads run in order on the copy stream: the SDFs first (the weights
-    // build needs only them and starts as soon as they are in), then the
-    // velocities, which stream in under the weights build. The copy stream
-    // first waits for anything still queued on the compute stream.
+    // Uploads run in order on the copy stream: the collider SDF first (the
+    // face weights need only it and start as soon as it is in), the fluid
+    // SDF under them, then the velocities. The copy stream first waits for
+    // anything still queued on the compute stream.
     cudaStream_t st = c->stream, cs = c->copy_stream;
     struct Join {  // no exit leaves a copy in flight
         cudaStream_t s;
@@ -685,11 +687,13 @@ static jetgpu_status solve_host(
     io.sdf_in = c->io_ev[1];
     io.vel_in = c->io_ev[2];
     io.x_final = c->io_ev[3];
+    io.bsdf_in = c->io_ev[4];
     io.copy = cs;
     io.host_p = out_pressure;
     JG_CUDA(c, cudaEventRecord(c->io_ev[0], st));
     JG_CUDA(c, cudaStreamWaitEvent(cs, c->io_ev[0], 0));
     if (db) JG_CUDA(c, cudaMemcpyAsync(db, boundary_sdf->data, nb * 8, cudaMemcpyHostToDevice, cs));
+    JG_CUDA(c, cudaEventRecord(io.bsdf_in, cs));
     if (df) JG_CUDA(c, cudaMemcpyAsync(df, fluid_sdf->data, nf * 8, cudaMemcpyHostToDevice, cs));
     JG_CUDA(c, cudaEventRecord(io.sdf_in, cs));
     unsigned long long h2d = (unsigned long long)(nb + nf) * 8, d2h = 0;

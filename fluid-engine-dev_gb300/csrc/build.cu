@@ -1175,7 +1175,8 @@ static jetgpu_status grow_list(Ctx* c, size_t n) {
 }
 
 jetgpu_status build_weights(Ctx* c, const GridDesc& g, const FieldDesc& bsdf,
-                            const FieldDesc& fsdf, bool pyramid) {
+                            const FieldDesc& fsdf, bool pyramid,
+                            cudaEvent_t fluid_ready) {
     Level& L0 = c->levels[0];
     const Dims n = L0.n;
     const Dims fu{n.x + 1, n.y, n.z}, fv{n.x, n.y + 1, n.z},
@@ -1186,19 +1187,6 @@ jetgpu_status build_weights(Ctx* c, const GridDesc& g, const FieldDesc& bsdf,
     }
     const SampleTables& T = c->tabs;
     const TabLayout TL = layout_of(T);
-    {
-        Prof pr(c, K_WEIGHTS, (8.0 + 4.0) * (double)n.count());
-        if (fsdf.kind == 1)
-            k_sample_fluid_tab<<<blocks_for(n.count()), kThreads, 0,
-                                 c->stream>>>(L0.phi, n, fsdf, T.idx, T.frac,
-                                              TL);
-        else if (fsdf.kind == 0)
-            k_fill_fluid<<<grid_cap(c, n.count()), kThreads, 0, c->stream>>>(
-                L0.phi, n.count(), fsdf.value);
-        else
-            k_sample_fluid<<<blocks_for(n.count()), kThreads, 0, c->stream>>>(
-                L0.phi, n, g, fsdf);
-    }
     {
         Prof pr(c, K_WEIGHTS, (8.0 + 3.0 * 4.0) * (double)n.count());
         if (bsdf.kind == 1 && T.use_nodes) {
@@ -1246,6 +1234,22 @@ jetgpu_status build_weights(Ctx* c, const GridDesc& g, const FieldDesc& bsdf,
             k_face_weights<<<blocks_for(fw.count()), kThreads, 0, c->stream>>>(
                 L0.ww, 2, fw, g, bsdf);
         }
+    }
+    // The fluid SDF's samples after the face weights, which need only the
+    // collider SDF (a host-pointer solve uploads that one first).
+    if (fluid_ready) JG_CUDA(c, cudaStreamWaitEvent(c->stream, fluid_ready, 0));
+    {
+        Prof pr(c, K_WEIGHTS, (8.0 + 4.0) * (double)n.count());
+        if (fsdf.kind == 1)
+            k_sample_fluid_tab<<<blocks_for(n.count()), kThreads, 0,
+                                 c->stream>>>(L0.phi, n, fsdf, T.idx, T.frac,
+                                              TL);
+        else if (fsdf.kind == 0)
+            k_fill_fluid<<<grid_cap(c, n.count()), kThreads, 0, c->stream>>>(
+                L0.phi, n.count(), fsdf.value);
+        else
+            k_sample_fluid<<<blocks_for(n.count()), kThreads, 0, c->stream>>>(
+                L0.phi, n, g, fsdf);
     }
     JG_CUDA(c, cudaGetLastError());
     return pyramid ? build_pyramid(c) : JETGPU_OK;

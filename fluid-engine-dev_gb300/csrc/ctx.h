@@ -103,7 +103,7 @@ struct Ctx {
     // Host-pointer solves move data on copy_stream, ordered against the
     // compute stream by io_ev (see SolveIo).
     cudaStream_t copy_stream = nullptr;
-    cudaEvent_t io_ev[4] = {nullptr, nullptr, nullptr, nullptr};
+    cudaEvent_t io_ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
     // Fluid-box transfers: the box on the device and in pinned host memory,
     // and the event that says it has arrived.
     int* box_dev = nullptr;
@@ -318,10 +318,12 @@ inline int red_blocks(const Ctx* c, long n) {
 }
 
 // ---- build.cu -------------------------------------------------------------
-// The finest level's fluid SDF and face weights, then (with `pyramid`) the
-// coarser levels' (build_pyramid).
+// The finest level's face weights and fluid SDF, then (with `pyramid`) the
+// coarser levels' (build_pyramid). With `fluid_ready`, the fluid SDF's part
+// waits for that event (the face weights need only the collider SDF).
 jetgpu_status build_weights(Ctx* c, const GridDesc& g, const FieldDesc& bsdf,
-                            const FieldDesc& fsdf, bool pyramid = true);
+                            const FieldDesc& fsdf, bool pyramid = true,
+                            cudaEvent_t fluid_ready = nullptr);
 jetgpu_status build_pyramid(Ctx* c);
 // Levels [lo, hi) of the hierarchy; only level 0 reads the velocities.
 jetgpu_status build_system(Ctx* c, const GridDesc& g, const double* u,
@@ -442,7 +444,9 @@ jetgpu_status extrapolate_regions(Ctx* c, int na, const Dims* s,
 // pressure is downloaded on `copy` straight into host_p while the gradient
 // kernel runs.
 struct SolveIo {
-    cudaEvent_t sdf_in = nullptr, vel_in = nullptr, x_final = nullptr;
+    // bsdf_in: the collider SDF is in; sdf_in: both SDFs are.
+    cudaEvent_t bsdf_in = nullptr, sdf_in = nullptr, vel_in = nullptr,
+                x_final = nullptr;
     cudaStream_t copy = nullptr;
     double* host_p = nullptr;
     // Called once the set-up that needs no velocity is queued, before the
