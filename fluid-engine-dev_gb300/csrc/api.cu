@@ -336,11 +336,20 @@ static jetgpu_status build_levels(Ctx* c, const GridDesc& g, const double* u,
         if ((s = prepare_levels(c, 1)) != JETGPU_OK) return s;
         if (fork) JG_CUDA(c, cudaEventRecord(c->side_ev[1], c->stream));
     }
-    if (io && io->before_vel && (s = io->before_vel()) != JETGPU_OK) return s;
-    if (io) JG_CUDA(c, cudaStreamWaitEvent(c->stream, io->vel_in, 0));
-    if ((s = build_system(c, g, u, v, w, su, sv, sw, 0, 1)) != JETGPU_OK)
-        return s;
-    if ((s = prepare_levels(c, 0, 1)) != JETGPU_OK) return s;
+    if (io) {
+        // Host inputs: the finest rows while the velocities upload, the rhs
+        // once they are in.
+        if ((s = build_system0_rows(c, g)) != JETGPU_OK) return s;
+        if ((s = prepare_levels(c, 0, 1)) != JETGPU_OK) return s;
+        if (io->before_vel && (s = io->before_vel()) != JETGPU_OK) return s;
+        JG_CUDA(c, cudaStreamWaitEvent(c->stream, io->vel_in, 0));
+        if ((s = build_system0_rhs(c, g, u, v, w, su, sv, sw)) != JETGPU_OK)
+            return s;
+    } else {
+        if ((s = build_system(c, g, u, v, w, su, sv, sw, 0, 1)) != JETGPU_OK)
+            return s;
+        if ((s = prepare_levels(c, 0, 1)) != JETGPU_OK) return s;
+    }
     if (fork) JG_CUDA(c, cudaStreamWaitEvent(c->stream, c->side_ev[1], 0));
     return JETGPU_OK;
 }
@@ -519,6 +528,7 @@ void jetgpu_destroy(jetgpu_ctx* c) {
     release(&c->bc_cnt);
     release(&c->bc_nrm);
     release(&c->bc_flag);
+    release(&c->rflag);
     release(&c->xp_int);
     release(&c->xp_cnt);
     release(&c->sdf_int);

@@ -496,7 +496,8 @@ __device__ __forceinline__ void build_cell(long c, Dims n, const SpacingInv& S,
                                            double* __restrict__ b64,
                                            float* __restrict__ A32,
                                            float4* __restrict__ Alo,
-                                           float2* __restrict__ bdf) {
+                                           float2* __restrict__ bdf,
+                                           unsigned char* __restrict__ rflag) {
     const long N = n.count();
     const int ux = n.x + 1;  // u-face row length
     const bool pw = S.pow2 != 0;
@@ -578,9 +579,13 @@ __device__ __forceinline__ void build_cell(long c, Dims n, const SpacingInv& S,
         if (cbits < 0x3CB0000000000000ULL) {  // DBL_EPSILON
             center = 1.0;
             bb = 0.0;
+            if (rflag) rflag[c] = 0;
+        } else if (rflag) {
+            rflag[c] = 1;  // the rhs pass fills b
         }
     } else {
         center = 1.0;
+        if (rflag) rflag[c] = 0;
     }
     if (A64) {  // one 32-byte row as two 16-byte stores
         double2* row = reinterpret_cast<double2*>(A64 + 4 * c);
@@ -618,6 +623,7 @@ __device__ __forceinline__ void build_cell(long c, Dims n, const SpacingInv& S,
 // fluid cells next to air into full warps for their FP64 divisions, as the
 // face weights do, made it slower: the sums and the rhs of every fluid cell
 // are FP64 too, so little of its FP64 work is divergent.)
+template <bool kMarkRhs>
 __global__ void __launch_bounds__(kThreads, 4)
     k_build_system(Dims n, SpacingInv S,
                    const float* __restrict__ phi,
@@ -634,12 +640,84 @@ __global__ void __launch_bounds__(kThreads, 4)
                    double* __restrict__ b64,
                    float* __restrict__ A32,
                    float4* __restrict__ Alo,
-                   float2* __restrict__ bdf) {
+                   float2* __restrict__ bdf,
+                   unsigned char* __restrict__ rflag) {
     const long N = n.count();
     for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < N;
          c += (long)gridDim.x * blockDim.x)
         build_cell(c, n, S, phi, uw, vw, ww, u, v, w, su, sv, sw, A64, b64,
-                   A32, Alo, bdf);
+                   A32, Alo, bdf, kMarkRhs ? rflag : nullptr);
+}
+
+// The level-0 rhs alone, for a host-pointer solve whose rows were built
+// (k_build_system without velocities, marking in rflag the fluid cells
+// whose centre was kept) while the velocities were still uploading: the
+// same faces, order and expressions as build_cell's rhs, so b is the same.
+__global__ void __launch_bounds__(kThreads)
+    k_build_rhs(Dims n, SpacingInv S, const unsigned char* __restrict__ rflag,
+                const float* __restrict__ uw, const float* __restrict__ vw,
+                const float* __restrict__ ww, const double* __restrict__ u,
+                const double* __restrict__ v, const double* __restrict__ w,
+                const double* __restrict__ su, const double* __restrict__ sv,
+                const double* __restrict__ sw, double* __restrict__ b64,
+                float2* __restrict__ bdf) {
+    const long N = n.count();
+    const int ux = n.x + 1;
+    const bool pw = S.pow2 != 0;
+    for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < N;
+         c += (long)gridDim.x * blockDim.x) {
+        double bb = 0.0;
+        const bool fl = rflag[c] != 0;
+        if (fl) {
+            int i, j, k;
+            cell_ijk(c, n, i, j, k);
+            const long uR = lin(i + 1, j, k, ux, n.y), uL = lin(i, j, k, ux, n.y);
+            const long vU = lin(i, j + 1, k, n.x, n.y + 1),
+                       vD = lin(i, j, k, n.x, n.y + 1);
+            const long wF = lin(i, j, k + 1, n.x, n.y), wB = lin(i, j, k, n.x, n.y);
+            auto face = [&](bool has, const float* wts, long f, int a,
+                            const double* vel, bool plus) {
+                if (has) {
+                    const double wd = widen_f32(wts[f]);
+                    const double p = wd * vel[f];
+                    const double t = pw ? scale_pow2(p, S.k[a], S.ih[a])
+                                        : p * S.ih[a];
+                    bb = plus ? bb + t : bb - t;
+                } else {
+                    const double t = pw ? scale_pow2(vel[f], S.k[a], S.ih[a])
+                                        : vel[f] * S.ih[a];
+                    bb = plus ? bb + t : bb - t;
+                }
+            };
+            face(i + 1 < n.x, uw, uR, 0, u, true);
+            face(i > 0, uw, uL, 0, u, false);
+            face(j + 1 < n.y, vw, vU, 1, v, true);
+            face(j > 0, vw, vD, 1, v, false);
+            face(k + 1 < n.z, ww, wF, 2, w, true);
+            face(k > 0, ww, wB, 2, w, false);
+            if (!su && !sv && !sw) {
+                unsigned lo, hi;
+                dwords(bb, lo, hi);
+                if (hi == 0x80000000u && lo == 0u) bb = djoin(0u, 0u);
+            } else {
+                const double ihx = S.ih[0], ihy = S.ih[1], ihz = S.ih[2];
+                const double sR = su ? su[uR] : 0.0, sL = su ? su[uL] : 0.0;
+                const double sU = sv ? sv[vU] : 0.0, sD = sv ? sv[vD] : 0.0;
+                const double sF = sw ? sw[wF] : 0.0, sB = sw ? sw[wB] : 0.0;
+                const double contrib = (1.0 - (double)uw[uR]) * sR * ihx -
+                                       (1.0 - (double)uw[uL]) * sL * ihx +
+                                       (1.0 - (double)vw[vU]) * sU * ihy -
+                                       (1.0 - (double)vw[vD]) * sD * ihy +
+                                       (1.0 - (double)ww[wF]) * sF * ihz -
+                                       (1.0 - (double)ww[wB]) * sB * ihz;
+                bb += contrib;
+            }
+        }
+        b64[c] = bb;
+        float bh = 0.0f, bl = 0.0f;
+        if (fl) split_f64(bb, bh, bl);
+        bdf[c] = make_float2(bh, bl);
+    }
 }
 
 // Double-float image of a caller-built finest-level system (the FP32 rows
@@ -1321,14 +1399,52 @@ jetgpu_status build_system(Ctx* c, const GridDesc& g, const double* u,
         const bool top = (l == 0);
         Prof pr(c, K_SYSTEM, (top ? 16.0 + 32.0 + 8.0 + 24.0 : 16.0 + 16.0) *
                                 (double)L.n.count());
-        k_build_system<<<blocks_for(L.n.count()), kThreads, 0, c->stream>>>(
+        k_build_system<false><<<blocks_for(L.n.count()), kThreads, 0,
+                                c->stream>>>(
             L.n, spacing_inv(hx, hy, hz), L.phi, L.uw, L.vw, L.ww,
             top ? u : nullptr,
             top ? v : nullptr, top ? w : nullptr, top ? su : nullptr,
             top ? sv : nullptr, top ? sw : nullptr, top ? c->A64 : nullptr,
             top ? c->b64 : nullptr, L.A, top ? c->Alo : nullptr,
-            top ? c->bdf : nullptr);
+            top ? c->bdf : nullptr, nullptr);
     }
+    JG_CUDA(c, cudaGetLastError());
+    return JETGPU_OK;
+}
+
+jetgpu_status build_system0_rows(Ctx* c, const GridDesc& g) {
+    Level& L = c->levels[0];
+    const long N = L.n.count();
+    if (c->rflag_cap < (size_t)N) {
+        JG_CUDA(c, cudaStreamSynchronize(c->stream));
+        if (c->rflag) cudaFree(c->rflag);
+        c->rflag = nullptr;
+        c->rflag_cap = 0;
+        JG_CUDA(c, cudaMalloc((void**)&c->rflag, (size_t)N));
+        c->rflag_cap = (size_t)N;
+    }
+    L.h[0] = g.spacing[0];
+    L.h[1] = g.spacing[1];
+    L.h[2] = g.spacing[2];
+    Prof pr(c, K_SYSTEM, (16.0 + 32.0 + 1.0) * (double)N);
+    k_build_system<true><<<blocks_for(N), kThreads, 0, c->stream>>>(
+        L.n, spacing_inv(g.spacing[0], g.spacing[1], g.spacing[2]), L.phi,
+        L.uw, L.vw, L.ww, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr,
+        c->A64, nullptr, L.A, c->Alo, nullptr, c->rflag);
+    JG_CUDA(c, cudaGetLastError());
+    return JETGPU_OK;
+}
+
+jetgpu_status build_system0_rhs(Ctx* c, const GridDesc& g, const double* u,
+                                const double* v, const double* w,
+                                const double* su, const double* sv,
+                                const double* sw) {
+    const Level& L = c->levels[0];
+    const long N = L.n.count();
+    Prof pr(c, K_SYSTEM, (1.0 + 12.0 + 24.0 + 8.0 + 8.0) * (double)N);
+    k_build_rhs<<<blocks_for(N), kThreads, 0, c->stream>>>(
+        L.n, spacing_inv(g.spacing[0], g.spacing[1], g.spacing[2]), c->rflag,
+        L.uw, L.vw, L.ww, u, v, w, su, sv, sw, c->b64, c->bdf);
     JG_CUDA(c, cudaGetLastError());
     return JETGPU_OK;
 }

@@ -178,6 +178,8 @@ struct Ctx {
     int* bc_list = nullptr;           // its invalid / inside face lists
     unsigned* bc_cnt = nullptr;       // their lengths per axis
     int* bc_flag = nullptr;           // the classification's regular SDF
+    size_t rflag_cap = 0;             // build_system0_rows: rhs cells
+    unsigned char* rflag = nullptr;
     size_t bc_nrm_cap = 0;            // collider normals of inside faces
     double4_32a* bc_nrm = nullptr;
     // extrapolate_region(s): stamps and two front lists (xp_cap entries
@@ -331,6 +333,14 @@ jetgpu_status build_system(Ctx* c, const GridDesc& g, const double* u,
                            const double* su, const double* sv,
                            const double* sw, unsigned lo = 0,
                            unsigned hi = ~0u);
+// The finest level's system in two parts, for host-pointer solves: the rows
+// (no velocity needed; marks the cells whose rhs is filled), then the rhs
+// once the velocities are in. Together the same as build_system's level 0.
+jetgpu_status build_system0_rows(Ctx* c, const GridDesc& g);
+jetgpu_status build_system0_rhs(Ctx* c, const GridDesc& g, const double* u,
+                                const double* v, const double* w,
+                                const double* su, const double* sv,
+                                const double* sw);
 // Low parts of a caller-built finest-level system (jetgpu_mgpcg_solve_system).
 jetgpu_status split_system(Ctx* c);
 jetgpu_status apply_gradient(Ctx* c, const GridDesc& g, const double* u,
