@@ -114,7 +114,10 @@ void GpuFractionalSinglePhasePressureSolver3::solve(
         sw = _solidW.data();
     }
 
+    // The pressure stays on the device until pressure() asks for it
+    // (FlipSolver3 never does): no 8-byte-per-cell download per solve.
     _pressure.resize(res);
+    _pressureStale = true;
     auto u = input.uConstAccessor();
     auto v = input.vConstAccessor();
     auto w = input.wConstAccessor();
@@ -124,12 +127,12 @@ void GpuFractionalSinglePhasePressureSolver3::solve(
     if (moving_rigid)
         _status = jetgpu_solve_pressure_collider(
             _ctx, &g, u.data(), v.data(), w.data(), &bsdf, &fsdf, &motion,
-            ou.data(), ov.data(), ow.data(), _pressure.data(), &_stats);
+            ou.data(), ov.data(), ow.data(), nullptr, &_stats);
     else
         _status = jetgpu_solve_pressure(_ctx, &g, u.data(), v.data(),
                                         w.data(), &bsdf, &fsdf, su, sv, sw,
                                         ou.data(), ov.data(), ow.data(),
-                                        _pressure.data(), &_stats);
+                                        nullptr, &_stats);
     if (_status != JETGPU_OK) {
         // The reference ignores its linear solver's result
         // (grid_fractional_single_phase_pressure_solver3.cpp:466-483); the
@@ -137,6 +140,23 @@ void GpuFractionalSinglePhasePressureSolver3::solve(
         JET_WARN << "jetgpu_solve_pressure: status " << _status << ": "
                  << jetgpu_last_error(_ctx);
     }
+}
+
+const jet::FdmVector3& GpuFractionalSinglePhasePressureSolver3::pressure()
+    const {
+    if (_pressureStale && _ctx) {
+        size_t count = 0;
+        const jetgpu_status s = jetgpu_get_level(
+            _ctx, 0, 6, _pressure.data(),
+            _pressure.width() * _pressure.height() * _pressure.depth() *
+                sizeof(double),
+            &count);
+        if (s != JETGPU_OK)
+            JET_WARN << "jetgpu_get_level: status " << s << ": "
+                     << jetgpu_last_error(_ctx);
+        _pressureStale = false;
+    }
+    return _pressure;
 }
 
 }  // namespace jetgpu_jet

@@ -64,8 +64,9 @@ class GpuFractionalSinglePhasePressureSolver3 : public jet::GridPressureSolver3 
     jet::GridBoundaryConditionSolver3Ptr suggestedBoundaryConditionSolver()
         const override;
 
-    //! Level-0 pressure of the last solve (cf. :512-518).
-    const jet::FdmVector3& pressure() const { return _pressure; }
+    //! Level-0 pressure of the last solve (cf. :512-518), read from the
+    //! device on first use after a solve.
+    const jet::FdmVector3& pressure() const;
 
     unsigned int lastNumberOfIterations() const { return _stats.iterations; }
     double lastResidual() const { return _stats.relative_residual; }
@@ -75,7 +76,8 @@ class GpuFractionalSinglePhasePressureSolver3 : public jet::GridPressureSolver3 
  private:
     jetgpu_config _config;
     struct jetgpu_ctx* _ctx = nullptr;
-    jet::FdmVector3 _pressure;
+    mutable jet::FdmVector3 _pressure;
+    mutable bool _pressureStale = false;
     jetgpu_solve_stats _stats{};
     jetgpu_status _status = JETGPU_OK;
     std::vector<double> _fluidRaster, _boundaryRaster;

@@ -567,6 +567,14 @@ class GridFractionalSinglePhasePressureSolver3:
         return "GridFractionalBoundaryConditionSolver3"
 
     def pressure(self) -> np.ndarray:
+        """The last solve's pressure ((nz, ny, nx)), read from the device on
+        first use after the solve (the solve itself downloads none)."""
+        if self._pressure is None and getattr(self, "_pshape", None):
+            p = self._pressure_buffer(self._pshape)
+            cnt = C.c_size_t(0)
+            self._solver.check(library().jetgpu_get_level(
+                self._solver.context(), 0, 6, _p(p), p.nbytes, C.byref(cnt)))
+            self._pressure = p
         return self._pressure
 
     def solve(self, input: FaceCenteredGrid3, timeIntervalInSeconds: float,
@@ -601,7 +609,7 @@ class GridFractionalSinglePhasePressureSolver3:
             if a.shape != ref.shape or a.dtype != np.float64 or not a.flags.c_contiguous:
                 raise ValueError("output arrays must match the input layout")
         nx, ny, nz = input.resolution
-        p = self._pressure_buffer((nz, ny, nx))
+        p = None  # the pressure stays on the device until pressure()
         solver = self._solver
         if collider is not None:
             st = library().jetgpu_solve_pressure_collider(
@@ -616,7 +624,8 @@ class GridFractionalSinglePhasePressureSolver3:
                 C.byref(self.last_stats))
         solver.last_stats = self.last_stats
         solver.check(st, allow=SOLVED)
-        self._pressure = p
+        self._pressure = None
+        self._pshape = (nz, ny, nx)
         return st
 
     def _pressure_buffer(self, shape) -> np.ndarray:
@@ -694,7 +703,7 @@ class GridSinglePhasePressureSolver3(GridFractionalSinglePhasePressureSolver3):
             if a.shape != ref.shape or a.dtype != np.float64 or not a.flags.c_contiguous:
                 raise ValueError("output arrays must match the input layout")
         nx, ny, nz = input.resolution
-        p = self._pressure_buffer((nz, ny, nx))
+        p = None  # the pressure stays on the device until pressure()
         solver = self._solver
         st = library().jetgpu_solve_pressure_blocked(
             solver.context(), C.byref(g), _p(u), _p(v), _p(w), C.byref(bs),
@@ -702,7 +711,8 @@ class GridSinglePhasePressureSolver3(GridFractionalSinglePhasePressureSolver3):
             C.byref(self.last_stats))
         solver.last_stats = self.last_stats
         solver.check(st, allow=SOLVED)
-        self._pressure = p
+        self._pressure = None
+        self._pshape = (nz, ny, nx)
         return st
 
 

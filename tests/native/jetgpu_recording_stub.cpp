@@ -103,6 +103,13 @@ jetgpu_status jetgpu_solve_pressure_collider(
     return JETGPU_OK;
 }
 
+jetgpu_status jetgpu_get_level(struct jetgpu_ctx*, int, int, void* dst,
+                               size_t capacity, size_t* count) {
+    if (dst && capacity) std::memset(dst, 0, capacity);
+    if (count) *count = 0;
+    return JETGPU_OK;
+}
+
 jetgpu_status jetgpu_solve_pressure_blocked(
     struct jetgpu_ctx*, const jetgpu_grid* grid, const double* u,
     const double* v, const double* w, const jetgpu_scalar_field* boundary_sdf,
