@@ -10,9 +10,11 @@ MGPCG and the pressure-gradient update — the whole projection per step.
 Arms:
 * ours (default): `value` = ms per pressure solve with inputs resident in
   HBM (device-pointer C ABI); `e2e` = the same through the host-pointer C ABI
-  with pinned host buffers (H2D of the inputs and D2H of the projected
-  velocity and pressure inside the timed region), the median of three
-  batches of K solves.
+  with pinned host buffers, called the way GridFluidSolver3 calls its
+  pressure solver (the output holds the input's values; fluid_box_io, as
+  the C++ adapter sets it): H2D of the SDFs and of the velocity faces
+  around the fluid, D2H of the projected velocity faces, inside the timed
+  region; the median of three batches of K solves.
 * --impl reference: the reference's CPU algorithm (the oracle port, bit-exact
   with the reference; or the reference itself where it was compiled on this
   machine) on all host cores, each step one full reference pressure solve
