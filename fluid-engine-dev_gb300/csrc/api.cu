@@ -555,6 +555,7 @@ void jetgpu_destroy(jetgpu_ctx* c) {
         release(&T.slot);
         release(&T.sidx);
         release(&T.sfrac);
+        release(&T.irregular);
         release(&T.node);
     }
     for (auto& e : c->io_ev)

@@ -1088,14 +1088,39 @@ __global__ void k_face_weights_listed(float* __restrict__ wgt,
 }
 
 // Fluid SDF at cell centres from the C tables.
+// 1 in *irregular when some value is zero or not finite.
+__global__ void k_values_regular(const double* __restrict__ d, long n,
+                                 int* __restrict__ irregular) {
+    for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < n;
+         c += (long)gridDim.x * blockDim.x) {
+        unsigned lo, hi;
+        dwords(d[c], lo, hi);
+        if (((hi << 1) | lo) == 0u || ((hi >> 20) & 0x7ffu) == 0x7ffu)
+            *irregular = 1;
+    }
+}
+
+// The fluid SDF's samples at the cell centres. With `irregular` non-null the
+// SDF lies on the cells (each centre's entry is its own index with fraction
+// 0, or for the last centre the one before with fraction 1); when the flag
+// is 0 (no zero, no non-finite value) every lerp of a sample returns the
+// operand of that cell, so the sample is the cell's own value.
 __global__ void k_sample_fluid_tab(float* __restrict__ phi, Dims n,
                                    FieldDesc F, const int* __restrict__ idx,
                                    const double* __restrict__ frac,
-                                   TabLayout L) {
+                                   TabLayout L,
+                                   const int* __restrict__ irregular) {
     const long N = n.count();
     const int ox = L.off[0][3], oy = L.off[1][3], oz = L.off[2][3];
+    const bool own = irregular && !*irregular;
     for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < N;
          c += (long)gridDim.x * blockDim.x) {
+        if (own) {
+            float hi, lo;
+            split_f64(F.data[c], hi, lo);
+            phi[c] = hi;
+            continue;
+        }
         int i, j, k;
         cell_ijk(c, n, i, j, k);
         float hi, lo;
@@ -1202,6 +1227,21 @@ jetgpu_status ensure_tables(Ctx* c, const GridDesc& g, const FieldDesc& B,
     const size_t nodes = (size_t)nslot[0] * nslot[1] * nslot[2];
     const size_t cells = (size_t)(g.res[0] + 1) * (g.res[1] + 1) * (g.res[2] + 1);
     T.use_nodes = nodes <= 4 * cells;
+    // getBarycentric puts the last centre at (n - 2, 1): the same value.
+    T.fluid_on_cells = F.kind == 1;
+    for (int a = 0; a < 3 && T.fluid_on_cells; ++a) {
+        const int n = g.res[a];
+        T.fluid_on_cells = F.res[a] == n;
+        for (int i = 0; i < n && T.fluid_on_cells; ++i) {
+            const int e = L.off[a][3] + i;
+            T.fluid_on_cells = (hidx[e] == i && hfrac[e] == 0.0 &&
+                                !std::signbit(hfrac[e])) ||
+                               (i == n - 1 && n >= 2 && hidx[e] == n - 2 &&
+                                hfrac[e] == 1.0);
+        }
+    }
+    if (!T.irregular)
+        JG_CUDA(c, cudaMalloc((void**)&T.irregular, sizeof(int)));
     if (T.use_nodes && nodes > T.node_cap) {
         if (T.node) cudaFree(T.node);
         T.node = nullptr;
@@ -1318,10 +1358,20 @@ jetgpu_status build_weights(Ctx* c, const GridDesc& g, const FieldDesc& bsdf,
     if (fluid_ready) JG_CUDA(c, cudaStreamWaitEvent(c->stream, fluid_ready, 0));
     {
         Prof pr(c, K_WEIGHTS, (8.0 + 4.0) * (double)n.count());
-        if (fsdf.kind == 1)
+        if (fsdf.kind == 1) {
+            int* irregular = nullptr;
+            if (T.fluid_on_cells) {
+                irregular = T.irregular;
+                JG_CUDA(c, cudaMemsetAsync(irregular, 0, sizeof(int),
+                                           c->stream));
+                k_values_regular<<<grid_cap(c, n.count()), kThreads, 0,
+                                   c->stream>>>(fsdf.data, n.count(),
+                                                irregular);
+            }
             k_sample_fluid_tab<<<blocks_for(n.count()), kThreads, 0,
                                  c->stream>>>(L0.phi, n, fsdf, T.idx, T.frac,
-                                              TL);
+                                              TL, irregular);
+        }
         else if (fsdf.kind == 0)
             k_fill_fluid<<<grid_cap(c, n.count()), kThreads, 0, c->stream>>>(
                 L0.phi, n.count(), fsdf.value);

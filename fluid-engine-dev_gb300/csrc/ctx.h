@@ -71,6 +71,10 @@ const char* kernel_class_name(int cls);
 struct SampleTables {
     bool valid = false;
     bool use_nodes = false;
+    // The fluid SDF lies on the grid's cells: every cell centre's table
+    // entry is (its own index, fraction +0), the last (n - 2, 1).
+    bool fluid_on_cells = false;
+    int* irregular = nullptr;  // device flag: a zero or non-finite SDF value
     GridDesc g{};
     FieldDesc B{}, F{};
     int off[3][4] = {};   // entry offsets [axis][N,M,P,C]
