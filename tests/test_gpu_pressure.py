@@ -360,7 +360,7 @@ def test_device_loop_matches_host_loop(precision):
 
 
 @pytest.mark.parametrize("case", ["flip", "sphere_union", "noncubic_solid",
-                                  "no_fluid", "all_fluid"])
+                                  "moving_collider", "no_fluid", "all_fluid"])
 def test_fluid_box_io_matches_full_io(case):
     """fluid_box_io moves only the velocity faces around the fluid cells;
     with the output holding the input's values (a clone, as
@@ -372,11 +372,14 @@ def test_fluid_box_io_matches_full_io(case):
         res, h = (n,) * 3, (1.0 / n,) * 3
         sc = scenes.flip_first_substep(n, box_hi=(0.3, 0.6, 0.8))
         args = (sc["u"], sc["v"], sc["w"], sc["boundary_sdf"], sc["fluid_sdf"])
-    elif case == "sphere_union":
+    elif case in ("sphere_union", "moving_collider"):
         n = 32
         res, h = (n,) * 3, (1.0 / n,) * 3
         sc = scenes.sphere_union_scene(n, seed=3)
         args = (sc["u"], sc["v"], sc["w"], sc["boundary_sdf"], sc["fluid_sdf"])
+        if case == "moving_collider":  # face velocities made on the device
+            solid = jetgpu.Collider.make((0.2, -0.1, 0.05), (0.3, 0.0, -0.4),
+                                         (0.5, 0.5, 0.5), 0.0)
     elif case == "noncubic_solid":
         g = golden("noncubic_12x8x16.npz")
         res, h = (12, 8, 16), tuple(g["spacing"])
@@ -399,7 +402,7 @@ def test_fluid_box_io_matches_full_io(case):
     for k in "uvw":
         assert np.array_equal(getattr(full[1], k), getattr(box[1], k)), k
     fs, bs = full[0].last_stats, box[0].last_stats
-    if case in ("flip", "sphere_union", "no_fluid"):
+    if case in ("flip", "sphere_union", "moving_collider", "no_fluid"):
         assert bs.h2d_bytes < fs.h2d_bytes and bs.d2h_bytes < fs.d2h_bytes
     else:  # fluid cells span the grid: the box is every face
         assert bs.h2d_bytes == fs.h2d_bytes and bs.d2h_bytes == fs.d2h_bytes
