@@ -3,7 +3,9 @@
 
 #include "ctx.h"
 
+#include <algorithm>
 #include <chrono>
+#include <climits>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -398,8 +400,19 @@ jetgpu_status solve_pressure_dev(
     // The reference applies the gradient whatever the solver returned
     // (grid_fractional_single_phase_pressure_solver3.cpp:466-483,
     // grid_single_phase_pressure_solver3.cpp:194-210).
-    s = blocked ? blocked_gradient(c, g, u, v, w, ou, ov, ow)
-                : apply_gradient(c, g, u, v, w, ou, ov, ow);
+    const int slabs = (io && io->grad_slabs && !blocked) ? *io->grad_slabs : 0;
+    if (blocked) {
+        s = blocked_gradient(c, g, u, v, w, ou, ov, ow);
+    } else if (slabs > 0) {
+        for (int k = 0; k < slabs; ++k) {
+            s = apply_gradient(c, g, u, v, w, ou, ov, ow, io->grad_cuts[k],
+                               io->grad_cuts[k + 1]);
+            if (s != JETGPU_OK) return s;
+            JG_CUDA(c, cudaEventRecord(c->grad_ev[k], c->stream));
+        }
+    } else {
+        s = apply_gradient(c, g, u, v, w, ou, ov, ow);
+    }
     if (s != JETGPU_OK) return s;
     // Issued after the gradient launch, so that a pageable destination
     // (whose copy blocks the host) still overlaps the gradient kernel.
@@ -412,6 +425,7 @@ jetgpu_status solve_pressure_dev(
     if (op)
         JG_CUDA(c, cudaMemcpyAsync(op, c->x64, n.count() * sizeof(double),
                                    cudaMemcpyDeviceToDevice, c->stream));
+    if (io && io->after_grad && (s = io->after_grad()) != JETGPU_OK) return s;
     JG_CUDA(c, cudaStreamSynchronize(c->stream));
     float setup = 0.0f, solve = 0.0f;
     JG_CUDA(c, cudaEventElapsedTime(&setup, c->ev[0], c->ev[1]));
@@ -480,6 +494,8 @@ jetgpu_status jetgpu_create(const jetgpu_config* cfg, jetgpu_ctx** out) {
                                                 cudaStreamNonBlocking,
                                                 greatest));
         for (auto& e : c->io_ev)
+            JG_CUDA(c, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+        for (auto& e : c->grad_ev)
             JG_CUDA(c, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
         for (auto& e : c->side_ev)
             JG_CUDA(c, cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
@@ -559,6 +575,8 @@ void jetgpu_destroy(jetgpu_ctx* c) {
         release(&T.node);
     }
     for (auto& e : c->io_ev)
+        if (e) cudaEventDestroy(e);
+    for (auto& e : c->grad_ev)
         if (e) cudaEventDestroy(e);
     if (c->box_ev) cudaEventDestroy(c->box_ev);
     release(&c->box_dev);
@@ -716,28 +734,52 @@ static jetgpu_status solve_host(
     } fb[3] = {{0, 0, 0, nx + 1, ny, nz},
                {0, 0, 0, nx, ny + 1, nz},
                {0, 0, 0, nx, ny, nz + 1}};
-    auto box_bytes = [&](int a) {
-        return (unsigned long long)(fb[a].wx * fb[a].wy * fb[a].wz) * 8ull;
-    };
+    // The part of face box a in face planes [zlo, zhi); the bytes moved
+    // are added to `moved`. Host-to-device copies whose rows leave less
+    // than 256 bytes between them (a box nearly as wide as the array) run
+    // at a fraction of the link's rate on GB300 (25-80 GB/s against 200
+    // GB/s, for row pitches that are not multiples of 2 KB), so such boxes
+    // go up as whole rows: the extra faces hold the caller's own values.
+    // Whole rows go as one run per plane range, or as one row of y-ranges
+    // per plane.
     auto copy_box = [&](double* dst, const double* src, int a,
-                        cudaMemcpyKind kind, cudaStream_t on) -> jetgpu_status {
+                        cudaMemcpyKind kind, cudaStream_t on,
+                        unsigned long long& moved, long zlo = 0,
+                        long zhi = LONG_MAX) -> jetgpu_status {
         const FBox& b = fb[a];
         if (b.wx <= 0 || b.wy <= 0 || b.wz <= 0) return JETGPU_OK;
+        const long z0 = std::max(b.z0, zlo), z1 = std::min(b.z0 + b.wz, zhi);
+        if (z1 <= z0) return JETGPU_OK;
         const long rx = nx + (a == 0), ry = ny + (a == 1);
-        const long rz = nz + (a == 2);
-        if (b.wx == rx && b.wy == ry && b.wz == rz) {
-            JG_CUDA(c, cudaMemcpyAsync(dst, src, (size_t)(rx * ry * rz) * 8,
-                                       kind, on));
+        long x0 = b.x0, wx = b.wx;
+        if (kind == cudaMemcpyHostToDevice && wx < rx && (rx - wx) * 8 < 256) {
+            x0 = 0;
+            wx = rx;
+        }
+        if (wx == rx && b.wy == ry) {  // whole planes: one contiguous run
+            const size_t off = (size_t)(z0 * rx * ry);
+            const size_t bytes = (size_t)(rx * ry * (z1 - z0)) * 8;
+            JG_CUDA(c, cudaMemcpyAsync(dst + off, src + off, bytes, kind, on));
+            moved += bytes;
+            return JETGPU_OK;
+        }
+        if (wx == rx) {  // whole rows: the y-range of each plane is one run
+            const size_t off = (size_t)((z0 * ry + b.y0) * rx);
+            const size_t pitch = (size_t)(rx * ry) * 8, width = (size_t)(b.wy * rx) * 8;
+            JG_CUDA(c, cudaMemcpy2DAsync(dst + off, pitch, src + off, pitch,
+                                         width, (size_t)(z1 - z0), kind, on));
+            moved += width * (size_t)(z1 - z0);
             return JETGPU_OK;
         }
         cudaMemcpy3DParms p3 = {};
         p3.srcPtr = make_cudaPitchedPtr(const_cast<double*>(src), rx * 8, rx, ry);
         p3.dstPtr = make_cudaPitchedPtr(dst, rx * 8, rx, ry);
-        p3.srcPos = make_cudaPos(b.x0 * 8, b.y0, b.z0);
+        p3.srcPos = make_cudaPos(x0 * 8, b.y0, z0);
         p3.dstPos = p3.srcPos;
-        p3.extent = make_cudaExtent(b.wx * 8, b.wy, b.wz);
+        p3.extent = make_cudaExtent(wx * 8, b.wy, z1 - z0);
         p3.kind = kind;
         JG_CUDA(c, cudaMemcpy3DAsync(&p3, on));
+        moved += (unsigned long long)(wx * b.wy * (z1 - z0)) * 8;
         return JETGPU_OK;
     };
     auto upload_velocities = [&]() -> jetgpu_status {
@@ -746,17 +788,32 @@ static jetgpu_status solve_host(
         const double* hs[3] = {solid_u, solid_v, solid_w};
         double* ds3[3] = {dsu, dsv, dsw};
         for (int a = 0; a < 3; ++a) {
-            jetgpu_status e = copy_box(dv3[a], hv[a], a, cudaMemcpyHostToDevice, cs);
+            jetgpu_status e =
+                copy_box(dv3[a], hv[a], a, cudaMemcpyHostToDevice, cs, h2d);
             if (e != JETGPU_OK) return e;
-            h2d += box_bytes(a);
             if (hs[a]) {
-                e = copy_box(ds3[a], hs[a], a, cudaMemcpyHostToDevice, cs);
+                e = copy_box(ds3[a], hs[a], a, cudaMemcpyHostToDevice, cs, h2d);
                 if (e != JETGPU_OK) return e;
-                h2d += box_bytes(a);
             }
         }
         JG_CUDA(c, cudaEventRecord(io.vel_in, cs));
         return JETGPU_OK;
+    };
+    // The gradient runs in slabs of cell planes spread over the box's, and
+    // each slab's faces go down under the next slab. Cell plane k writes
+    // the u and v faces of plane k and the w faces of plane k + 1 (plane
+    // 0 also w plane 0).
+    int cuts[Ctx::kGradSlabs + 1];
+    int nslab = 0;
+    io.grad_cuts = cuts;
+    io.grad_slabs = &nslab;
+    auto set_cuts = [&](long z0, long z1) {  // the box's cell planes
+        if (blocked || z1 <= z0) return;
+        nslab = Ctx::kGradSlabs;
+        cuts[0] = 0;
+        cuts[nslab] = (int)nz;
+        for (int k = 1; k < nslab; ++k)
+            cuts[k] = (int)(z0 + (z1 - z0) * k / nslab);
     };
     const bool box_io = c->cfg.fluid_box_io != 0 && !blocked;
     if (box_io) {
@@ -795,9 +852,11 @@ static jetgpu_status solve_host(
                 fb[a].wy = empty ? 0 : bx[4] - bx[1] + 1 + (a == 1);
                 fb[a].wz = empty ? 0 : bx[5] - bx[2] + 1 + (a == 2);
             }
+            if (!empty) set_cuts(bx[2], bx[5] + 1);
             return upload_velocities();
         };
     } else {
+        set_cuts(0, nz);
         if ((s = upload_velocities()) != JETGPU_OK) return s;
     }
     if (col_faces) {
@@ -810,6 +869,30 @@ static jetgpu_status solve_host(
         if ((s = solid_face_velocities(c, gd, *collider, dsu)) != JETGPU_OK)
             return s;
     }
+    // The projected velocity goes down as soon as the gradient is queued:
+    // slab by slab on the copy stream, or after the whole gradient.
+    io.after_grad = [&]() -> jetgpu_status {
+        double* ho[3] = {out_u, out_v, out_w};
+        const double* dout[3] = {ou, ov, ow};
+        if (nslab > 0) {
+            for (int k = 0; k < nslab; ++k) {
+                JG_CUDA(c, cudaStreamWaitEvent(cs, c->grad_ev[k], 0));
+                for (int a = 0; a < 3; ++a) {
+                    const long lo = a < 2 ? cuts[k] : (k ? cuts[k] + 1 : 0);
+                    const long hi = cuts[k + 1] + (a == 2);
+                    if ((s = copy_box(ho[a], dout[a], a, cudaMemcpyDeviceToHost,
+                                      cs, d2h, lo, hi)) != JETGPU_OK)
+                        return s;
+                }
+            }
+        } else {
+            for (int a = 0; a < 3; ++a)
+                if ((s = copy_box(ho[a], dout[a], a, cudaMemcpyDeviceToHost,
+                                  st, d2h)) != JETGPU_OK)
+                    return s;
+        }
+        return JETGPU_OK;
+    };
     jetgpu_solve_stats local;
     std::memset(&local, 0, sizeof(local));
     jetgpu_status solve_status = solve_pressure_dev(
@@ -818,16 +901,6 @@ static jetgpu_status solve_host(
     if (!usable(solve_status)) {
         if (stats) *stats = local;
         return solve_status;
-    }
-    {
-        double* ho[3] = {out_u, out_v, out_w};
-        const double* dout[3] = {ou, ov, ow};
-        for (int a = 0; a < 3; ++a) {
-            if ((s = copy_box(ho[a], dout[a], a, cudaMemcpyDeviceToHost, st)) !=
-                JETGPU_OK)
-                return s;
-            d2h += box_bytes(a);
-        }
     }
     if (out_pressure) d2h += (unsigned long long)nx * ny * nz * 8;
     JG_CUDA(c, cudaStreamSynchronize(st));

@@ -761,13 +761,13 @@ __global__ void k_apply_gradient(Dims n, SpacingInv S,
                                  const double* __restrict__ x,
                                  const double* u, const double* v,
                                  const double* w, double* ou, double* ov,
-                                 double* ow, int copy) {
-    const long N = n.count();
+                                 double* ow, int copy, int kz0, int kz1) {
     const int ux = n.x + 1;
     const long sz = (long)n.x * n.y;
+    const long N = kz1 * sz;
     const bool pw = S.pow2 != 0;
-    for (long c = blockIdx.x * (long)blockDim.x + threadIdx.x; c < N;
-         c += (long)gridDim.x * blockDim.x) {
+    for (long c = kz0 * sz + blockIdx.x * (long)blockDim.x + threadIdx.x;
+         c < N; c += (long)gridDim.x * blockDim.x) {
         int i, j, k;
         cell_ijk(c, n, i, j, k);
         const float cphf = phi[c];
@@ -813,14 +813,15 @@ __global__ void k_apply_gradient4(Dims n, SpacingInv S,
                                   const double* __restrict__ x,
                                   const double* u, const double* v,
                                   const double* w, double* ou, double* ov,
-                                  double* ow) {
+                                  double* ow, int kz0, int kz1) {
     const Dims g{n.x / 4, n.y, n.z};
-    const long G = g.count();
+    const long gz = (long)g.x * g.y;
+    const long G = kz1 * gz;
     const int ux = n.x + 1;
     const long sy = n.x, sz = (long)n.x * n.y;
     const bool pw = S.pow2 != 0;
-    for (long t = blockIdx.x * (long)blockDim.x + threadIdx.x; t < G;
-         t += (long)gridDim.x * blockDim.x) {
+    for (long t = kz0 * gz + blockIdx.x * (long)blockDim.x + threadIdx.x;
+         t < G; t += (long)gridDim.x * blockDim.x) {
         int m, j, k;
         cell_ijk(t, g, m, j, k);
         const int i = 4 * m;
@@ -1513,24 +1514,29 @@ static bool aligned16(const void* p) {
 
 jetgpu_status apply_gradient(Ctx* c, const GridDesc& g, const double* u,
                              const double* v, const double* w, double* ou,
-                             double* ov, double* ow) {
+                             double* ov, double* ow, int kz0, int kz1) {
     const Level& L = c->levels[0];
     const Dims n = L.n;
     const bool alias = (ou == u) && (ov == v) && (ow == w);
     if (!alias && ((ou == u) || (ov == v) || (ow == w)))
         return fail(c, JETGPU_BAD_INPUT,
                     "output faces must all alias the input or none");
-    Prof pr(c, K_GRADIENT, (4.0 + 12.0 + 8.0 + 48.0) * (double)n.count());
+    if (kz1 < 0) kz1 = n.z;
+    if (kz0 < 0 || kz0 > kz1 || kz1 > n.z)
+        return fail(c, JETGPU_BAD_INPUT, "gradient planes out of range");
+    if (kz0 == kz1) return JETGPU_OK;
+    const long cells = (long)(kz1 - kz0) * n.x * n.y;
+    Prof pr(c, K_GRADIENT, (4.0 + 12.0 + 8.0 + 48.0) * (double)cells);
     if (n.x % 4 == 0 && aligned16(u) && aligned16(v) && aligned16(w) &&
         aligned16(ou) && aligned16(ov) && aligned16(ow))
-        k_apply_gradient4<<<blocks_for(n.count() / 4), kThreads, 0,
-                            c->stream>>>(
+        k_apply_gradient4<<<blocks_for(cells / 4), kThreads, 0, c->stream>>>(
             n, spacing_inv(g.spacing[0], g.spacing[1], g.spacing[2]), L.phi,
-            L.uw, L.vw, L.ww, c->x64, u, v, w, ou, ov, ow);
+            L.uw, L.vw, L.ww, c->x64, u, v, w, ou, ov, ow, kz0, kz1);
     else
-        k_apply_gradient<<<blocks_for(n.count()), kThreads, 0, c->stream>>>(
+        k_apply_gradient<<<blocks_for(cells), kThreads, 0, c->stream>>>(
             n, spacing_inv(g.spacing[0], g.spacing[1], g.spacing[2]), L.phi,
-            L.uw, L.vw, L.ww, c->x64, u, v, w, ou, ov, ow, alias ? 0 : 1);
+            L.uw, L.vw, L.ww, c->x64, u, v, w, ou, ov, ow, alias ? 0 : 1,
+            kz0, kz1);
     JG_CUDA(c, cudaGetLastError());
     return JETGPU_OK;
 }

@@ -113,6 +113,10 @@ struct Ctx {
     int* box_dev = nullptr;
     int* box_host = nullptr;
     cudaEvent_t box_ev = nullptr;
+    // One event per slab of cell planes of the pressure gradient, so that
+    // the download of the faces a slab completes runs under the next slab.
+    static constexpr int kGradSlabs = 4;
+    cudaEvent_t grad_ev[kGradSlabs] = {nullptr, nullptr, nullptr, nullptr};
     // High-priority stream for the coarse levels' set-up, which runs beside
     // the finest level's (fork and join events).
     cudaStream_t side_stream = nullptr;
@@ -347,9 +351,12 @@ jetgpu_status build_system0_rhs(Ctx* c, const GridDesc& g, const double* u,
                                 const double* sw);
 // Low parts of a caller-built finest-level system (jetgpu_mgpcg_solve_system).
 jetgpu_status split_system(Ctx* c);
+// The pressure gradient of the cells in planes [kz0, kz1) (kz1 < 0: to
+// the last plane); each cell writes the faces it owns.
 jetgpu_status apply_gradient(Ctx* c, const GridDesc& g, const double* u,
                              const double* v, const double* w, double* ou,
-                             double* ov, double* ow);
+                             double* ov, double* ow, int kz0 = 0,
+                             int kz1 = -1);
 
 // ---- blocked.cu ------------------------------------------------------------
 // GridSinglePhasePressureSolver3: markers of every level (and phi = -1 for
@@ -467,6 +474,15 @@ struct SolveIo {
     // level-0 system waits for vel_in (issues the velocity uploads when
     // they depend on something the host must first read back).
     std::function<jetgpu_status()> before_vel;
+    // When *grad_slabs > 0, the gradient runs as that many launches over
+    // the cell planes [grad_cuts[s], grad_cuts[s + 1]), each followed by
+    // Ctx::grad_ev[s] on the compute stream (the caller sets both, up to
+    // the point where before_vel returns).
+    const int* grad_cuts = nullptr;
+    const int* grad_slabs = nullptr;
+    // Called once the gradient is queued, before the host waits for it
+    // (issues the downloads of the projected velocity).
+    std::function<jetgpu_status()> after_grad;
 };
 
 // GridFractionalSinglePhasePressureSolver3::solve on device arrays (api.cu):

@@ -359,8 +359,9 @@ def test_device_loop_matches_host_loop(precision):
     assert np.array_equal(res[0][1], res[1][1])
 
 
-@pytest.mark.parametrize("case", ["flip", "sphere_union", "noncubic_solid",
-                                  "moving_collider", "no_fluid", "all_fluid"])
+@pytest.mark.parametrize("case", ["flip", "wide_fluid", "sphere_union",
+                                  "noncubic_solid", "moving_collider",
+                                  "no_fluid", "all_fluid"])
 def test_fluid_box_io_matches_full_io(case):
     """fluid_box_io moves only the velocity faces around the fluid cells;
     with the output holding the input's values (a clone, as
@@ -371,6 +372,11 @@ def test_fluid_box_io_matches_full_io(case):
         n = 48
         res, h = (n,) * 3, (1.0 / n,) * 3
         sc = scenes.flip_first_substep(n, box_hi=(0.3, 0.6, 0.8))
+        args = (sc["u"], sc["v"], sc["w"], sc["boundary_sdf"], sc["fluid_sdf"])
+    elif case == "wide_fluid":  # the box spans x: whole rows each way
+        n = 64
+        res, h = (n,) * 3, (1.0 / n,) * 3
+        sc = scenes.flip_first_substep(n, box_hi=(1.0, 0.5, 0.7))
         args = (sc["u"], sc["v"], sc["w"], sc["boundary_sdf"], sc["fluid_sdf"])
     elif case in ("sphere_union", "moving_collider"):
         n = 32
@@ -402,7 +408,8 @@ def test_fluid_box_io_matches_full_io(case):
     for k in "uvw":
         assert np.array_equal(getattr(full[1], k), getattr(box[1], k)), k
     fs, bs = full[0].last_stats, box[0].last_stats
-    if case in ("flip", "sphere_union", "moving_collider", "no_fluid"):
+    if case in ("flip", "wide_fluid", "sphere_union", "moving_collider",
+                "no_fluid"):
         assert bs.h2d_bytes < fs.h2d_bytes and bs.d2h_bytes < fs.d2h_bytes
     else:  # fluid cells span the grid: the box is every face
         assert bs.h2d_bytes == fs.h2d_bytes and bs.d2h_bytes == fs.d2h_bytes
