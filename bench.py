@@ -33,8 +33,10 @@ one solve of the reference's CPU algorithm beside it.
 Timing: W warm-up solves, then K solves bracketed by a barrier and
 synchronize, timed with CUDA events on the library's own stream, max over
 ranks. The working set (0.5 GB of FP64 inputs, 3+ GB of solver state) is
-far larger than L2, so no flush is needed. Clocks are sampled with
-nvidia-smi during the timed region.
+far larger than L2, so no flush is needed. Clocks are sampled during the
+timed region: SM clock and clock-event reasons read through NVML every
+5 ms (read-only queries), or nvidia-smi every 200 ms where NVML does not
+load.
 """
 from __future__ import annotations
 
@@ -120,8 +122,85 @@ def max_over_ranks(pg, value: float, device=None) -> float:
     return float(t.item())
 
 
+class NvmlClocks:
+    """SM clock and clock-event reasons read through NVML (the driver's
+    libnvidia-ml, read-only queries) every few milliseconds from a thread,
+    so that a timed region of well under a second still gets a dozen
+    samples. Same result dictionary as Clocks; `ok` is False where NVML
+    cannot be loaded."""
+
+    # nvmlClocksEventReasons bits
+    REASONS = {0x8: "hw_slowdown", 0x40: "hw_thermal_slowdown",
+               0x20: "sw_thermal_slowdown", 0x4: "sw_power_cap"}
+
+    def __init__(self, gpu: int, period_s: float = 0.005):
+        import ctypes
+        import threading
+        self.C, self.threading = ctypes, threading
+        self.period = period_s
+        self.ok = False
+        self.rows = []
+        try:
+            nv = ctypes.CDLL("libnvidia-ml.so.1")
+            if nv.nvmlInit_v2() != 0:
+                return
+            h = ctypes.c_void_p()
+            if nv.nvmlDeviceGetHandleByIndex_v2(ctypes.c_uint(gpu),
+                                                ctypes.byref(h)) != 0:
+                return
+            self.nv, self.h = nv, h
+            self.reasons_fn = getattr(nv, "nvmlDeviceGetCurrentClocksEventReasons",
+                                      None) or nv.nvmlDeviceGetCurrentClocksThrottleReasons
+            mx = ctypes.c_uint()
+            if nv.nvmlDeviceGetMaxClockInfo(h, 1, ctypes.byref(mx)) != 0:
+                return
+            self.max_mhz = float(mx.value)
+            self.ok = True
+        except (OSError, AttributeError):
+            self.ok = False
+
+    def _sample(self):
+        C = self.C
+        mhz, rs = C.c_uint(), C.c_ulonglong()
+        if (self.nv.nvmlDeviceGetClockInfo(self.h, 1, C.byref(mhz)) == 0 and
+                self.reasons_fn(self.h, C.byref(rs)) == 0):
+            self.rows.append((float(mhz.value), int(rs.value)))
+
+    def start(self):
+        self.rows, self.stop_ev = [], self.threading.Event()
+
+        def run():
+            while not self.stop_ev.is_set():
+                self._sample()
+                self.stop_ev.wait(self.period)
+
+        self._sample()
+        self.thread = self.threading.Thread(target=run, daemon=True)
+        self.thread.start()
+
+    def stop(self) -> dict:
+        self.stop_ev.set()
+        self.thread.join(timeout=5)
+        self._sample()
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"]}
+        sm = sorted(r[0] for r in self.rows)
+        reasons = sorted({name for _, bits in self.rows
+                          for bit, name in self.REASONS.items() if bits & bit})
+        return {"sm_mhz": sm[len(sm) // 2], "sm_max_mhz": self.max_mhz,
+                "reasons": reasons, "samples": len(self.rows),
+                "source": "nvml"}
+
+
 class Clocks:
-    """nvidia-smi sampling during the timed region."""
+    """nvidia-smi sampling during the timed region (NVML polling where the
+    driver's library loads; nvidia-smi's 200 ms period otherwise)."""
+
+    def __new__(cls, gpu: int):
+        nv = NvmlClocks(gpu)
+        if nv.ok:
+            return nv
+        return super().__new__(cls)
 
     QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,"
              "clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
