@@ -618,13 +618,14 @@ __device__ __forceinline__ void build_cell(long c, Dims n, const SpacingInv& S,
 }
 
 // K4's kernel. Latency-bound at the 94 registers it would take freely (two
-// blocks per SM): capped at 64 for four blocks, with a few spilled values,
-// it runs 1.6x faster (1.21 -> 0.77 ms per 256^3 solve). (Compacting the
+// blocks per SM): capped at 40 for six blocks, with a few spilled values,
+// it runs 1.9x faster (1.21 -> 0.77 ms per 256^3 solve at four blocks,
+// 0.64 ms at six; eight blocks spill too much, 0.79 ms). (Compacting the
 // fluid cells next to air into full warps for their FP64 divisions, as the
 // face weights do, made it slower: the sums and the rhs of every fluid cell
 // are FP64 too, so little of its FP64 work is divergent.)
 template <bool kMarkRhs>
-__global__ void __launch_bounds__(kThreads, 4)
+__global__ void __launch_bounds__(kThreads, 6)
     k_build_system(Dims n, SpacingInv S,
                    const float* __restrict__ phi,
                    const float* __restrict__ uw,
@@ -804,16 +805,17 @@ __global__ void k_apply_gradient(Dims n, SpacingInv S,
 // per-face rule and arithmetic for each cell, with the cell values, the
 // v and w faces and their weights moved as 16-byte accesses. Every owned
 // face is written (its input value when untouched), which with an aliased
-// output rewrites the value already there.
-__global__ void k_apply_gradient4(Dims n, SpacingInv S,
-                                  const float* __restrict__ phi,
-                                  const float* __restrict__ uw,
-                                  const float* __restrict__ vw,
-                                  const float* __restrict__ ww,
-                                  const double* __restrict__ x,
-                                  const double* u, const double* v,
-                                  const double* w, double* ou, double* ov,
-                                  double* ow, int kz0, int kz1) {
+// output rewrites the value already there. Four blocks per SM (64
+// registers, a few spilled) run it 6% faster than the three that 78
+// registers allow.
+__global__ void __launch_bounds__(kThreads, 4)
+    k_apply_gradient4(Dims n, SpacingInv S, const float* __restrict__ phi,
+                      const float* __restrict__ uw,
+                      const float* __restrict__ vw,
+                      const float* __restrict__ ww,
+                      const double* __restrict__ x, const double* u,
+                      const double* v, const double* w, double* ou,
+                      double* ov, double* ow, int kz0, int kz1) {
     const Dims g{n.x / 4, n.y, n.z};
     const long gz = (long)g.x * g.y;
     const long G = kz1 * gz;
