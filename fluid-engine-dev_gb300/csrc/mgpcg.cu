@@ -471,8 +471,9 @@ __global__ void __launch_bounds__(kThreads)
 // k_residual_df over 4-cell groups (n.x a multiple of 4): each cell's terms
 // in k_residual_df's order, from 16-byte loads of the row components and of
 // the double-float iterate and rhs; the low parts of the neighbours' rows are
-// read as single components.
-__global__ void __launch_bounds__(kThreads)
+// read as single components. Capped at 64 registers (four blocks per SM
+// instead of three), a few values spilled: slightly faster.
+__global__ void __launch_bounds__(kThreads, 4)
     k_residual_df4(RowsF Ahi, const float4* __restrict__ Alo,
                    const float2* __restrict__ x, const float2* __restrict__ b,
                    float* __restrict__ r32, float* __restrict__ zero32, Dims n,
@@ -848,8 +849,9 @@ __global__ void __launch_bounds__(kThreads)
 // x-interpolated coarse values of the three coarse planes that the fine
 // planes 2kc and 2kc+1 read (kc-1, kc, kc+1, clamped), so consecutive fine
 // planes share them instead of gathering them again. Same stencil, weights
-// and x-then-y-then-z order as k_correct.
-__global__ void __launch_bounds__(kThreads)
+// and x-then-y-then-z order as k_correct. Five blocks per SM (48
+// registers) run it 5% faster than four.
+__global__ void __launch_bounds__(kThreads, 5)
     k_correct4z(const float* __restrict__ coarse, float* __restrict__ fine,
                 Dims c, int run) {
     const Dims n{2 * c.x, 2 * c.y, 2 * c.z};
